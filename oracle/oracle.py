@@ -1,0 +1,246 @@
+"""ctypes front end of the CPU oracle (oracle/manta_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU legs as the parity checker / CPU baseline, never by the
+product package.
+
+Arrays use the reference's memory layout (source/grid.h:70): Real grids are
+float32 arrays of shape (nz, ny, nx), Vec3/MAC grids (nz, ny, nx, 3), flag
+grids int32 (nz, ny, nx).  All calls modify their outputs in place.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libmantaoracle.so")
+
+FLUID, OBSTACLE, EMPTY, INFLOW, OUTFLOW, OPEN, STICK = 1, 2, 4, 8, 16, 32, 64
+KIND_REAL, KIND_VEC3, KIND_MAC = 0, 1, 2
+PC_NONE, PC_MIC, PC_MG_DYNAMIC, PC_MG_STATIC = 0, 1, 2, 3
+
+
+class Dims(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("is3d", C.c_int)]
+
+
+class PressureParams(C.Structure):
+    _fields_ = [("cgAccuracy", C.c_float), ("gfClamp", C.c_float), ("cgMaxIterFac", C.c_float),
+                ("preconditioner", C.c_int), ("enforceCompatibility", C.c_int), ("useL2Norm", C.c_int),
+                ("zeroPressureFixing", C.c_int), ("surfTens", C.c_float)]
+
+
+class PressureResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("resNorm", C.c_float), ("fixPidx", C.c_int)]
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (gcc/g++ only)."""
+    if force or not os.path.exists(_LIB_PATH) or \
+            os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "manta_oracle.cpp")):
+        subprocess.run(["make", "-C", _HERE, "-s"], check=True)
+    return _LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+        F = C.c_float
+        I = C.c_int
+        L.og_advect_semi_lagrange.argtypes = [Dims, ip, fp, I, fp, I, F, I, I, I, F]
+        L.og_advect_semi_lagrange.restype = I
+        L.og_set_wall_bcs.argtypes = [Dims, ip, fp, C.c_void_p]
+        L.og_add_buoyancy.argtypes = [Dims, ip, fp, fp, F, F, F, F, I, F]
+        L.og_add_gravity.argtypes = [Dims, ip, fp, F, F, F, C.c_void_p, I, F]
+        L.og_extrapolate_mac_simple.argtypes = [Dims, ip, fp, I, I]
+        L.og_mg_create.argtypes = [Dims]
+        L.og_mg_create.restype = C.c_void_p
+        L.og_mg_destroy.argtypes = [C.c_void_p]
+        L.og_compute_pressure_rhs.argtypes = [Dims, fp, fp, ip, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.POINTER(PressureParams)]
+        L.og_solve_pressure.argtypes = [Dims, fp, fp, ip, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.POINTER(PressureParams), C.POINTER(C.c_void_p),
+                                        C.POINTER(PressureResult), C.c_void_p]
+        L.og_solve_pressure.restype = I
+        L.og_make_laplace_matrix.argtypes = [Dims, ip, fp, fp, fp, fp]
+        L.og_apply_ghost_fluid_diagonal.argtypes = [Dims, fp, ip, fp, F]
+        L.og_mic_init.argtypes = [Dims, ip, fp, fp, fp, fp, fp]
+        L.og_mic_apply.argtypes = [Dims, fp, fp, ip, fp, fp, fp, fp]
+        L.og_apply_matrix.argtypes = [Dims, ip, fp, fp, fp, fp, fp, fp]
+        L.og_mg_vcycle.argtypes = [C.c_void_p, fp, fp, fp, fp, fp, fp, F]
+        L.og_mg_num_levels.argtypes = [C.c_void_p]
+        L.og_mg_num_levels.restype = I
+        L.og_mg_level_size.argtypes = [C.c_void_p, I, C.POINTER(C.c_int * 3)]
+        L.og_mg_level_types.argtypes = [C.c_void_p, I]
+        L.og_mg_level_types.restype = C.POINTER(C.c_int8)
+        L.og_mg_level_matrix.argtypes = [C.c_void_p, I]
+        L.og_mg_level_matrix.restype = C.POINTER(C.c_float)
+        L.og_init_domain.argtypes = [Dims, ip, I, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p]
+        L.og_fill_grid.argtypes = [Dims, ip, I]
+        L.og_set_open_bound.argtypes = [Dims, ip, I, C.c_char_p, I]
+        L.og_update_from_levelset.argtypes = [Dims, ip, fp]
+        L.og_box_sdf.argtypes = [Dims, fp, F, F, F, F, F, F]
+        L.og_cylinder_apply.argtypes = [Dims, fp, F, F, F, F, F, F, F, F, C.c_void_p]
+        L.og_box_apply.argtypes = [Dims, fp, F, F, F, F, F, F, F, C.c_void_p]
+        L.og_join_real.argtypes = [C.c_longlong, fp, fp, I]
+        L.og_get_max_abs.argtypes = [C.c_longlong, fp]
+        L.og_get_max_abs.restype = F
+        L.og_set_num_threads.argtypes = [I]
+        L.og_get_num_threads.restype = I
+        _lib = L
+    return _lib
+
+
+def dims(shape):
+    """Dims from a (nz, ny, nx[, 3]) array shape."""
+    nz, ny, nx = shape[:3]
+    return Dims(nx, ny, nz, 1 if nz > 1 else 0)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def set_num_threads(n):
+    lib().og_set_num_threads(int(n))
+
+
+def advect_semi_lagrange(flags, vel, grid, kind, order=1, strength=1.0, orderSpace=1, clampMode=2,
+                         orderTrace=1, dt=1.0):
+    st = lib().og_advect_semi_lagrange(dims(flags.shape), flags, vel, kind, grid, order, strength, orderSpace,
+                                       clampMode, orderTrace, dt)
+    if st != 0:
+        raise RuntimeError("AdvectSemiLagrange: Only order 1 (regular SL) and 2 (MacCormack) supported")
+
+
+def set_wall_bcs(flags, vel, obvel=None):
+    lib().og_set_wall_bcs(dims(flags.shape), flags, vel, _ptr(obvel))
+
+
+def add_buoyancy(flags, density, vel, gravity, coefficient=1.0, scale=True, dt=1.0):
+    lib().og_add_buoyancy(dims(flags.shape), flags, density, vel, *map(float, gravity), coefficient, int(scale), dt)
+
+
+def add_gravity(flags, vel, gravity, exclude=None, scale=True, dt=1.0):
+    lib().og_add_gravity(dims(flags.shape), flags, vel, *map(float, gravity), _ptr(exclude), int(scale), dt)
+
+
+def extrapolate_mac_simple(flags, vel, distance=4, intoObs=False):
+    lib().og_extrapolate_mac_simple(dims(flags.shape), flags, vel, distance, int(intoObs))
+
+
+def params(cgAccuracy=1e-3, gfClamp=1e-4, cgMaxIterFac=1.5, preconditioner=PC_MIC, enforceCompatibility=False,
+           useL2Norm=False, zeroPressureFixing=False, surfTens=0.0):
+    return PressureParams(cgAccuracy, gfClamp, cgMaxIterFac, preconditioner, int(enforceCompatibility),
+                          int(useL2Norm), int(zeroPressureFixing), surfTens)
+
+
+class MGCache:
+    """The per-solver static multigrid slot (plugin/pressure.cpp:250)."""
+
+    def __init__(self):
+        self.ptr = C.c_void_p(None)
+
+    def release(self):
+        if self.ptr.value:
+            lib().og_mg_destroy(self.ptr)
+            self.ptr = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def compute_pressure_rhs(rhs, vel, flags, phi=None, perCellCorr=None, curv=None, **kw):
+    p = params(**kw)
+    lib().og_compute_pressure_rhs(dims(flags.shape), rhs, vel, flags, _ptr(phi), _ptr(perCellCorr), _ptr(curv),
+                                  C.byref(p))
+
+
+def solve_pressure(flags, vel, pressure, phi=None, perCellCorr=None, curv=None, mg_cache=None, retRhs=None, **kw):
+    """solvePressure; returns (iterations, resNorm, fixPidx)."""
+    p = params(**kw)
+    res = PressureResult()
+    cache = mg_cache if mg_cache is not None else MGCache()
+    st = lib().og_solve_pressure(dims(flags.shape), vel, pressure, flags, _ptr(phi), _ptr(perCellCorr), _ptr(curv),
+                                 C.byref(p), C.byref(cache.ptr), C.byref(res), _ptr(retRhs))
+    if st == -4:
+        raise RuntimeError("GridCg::iterate: The CG solver diverged, residual norm > 1e30, stopping.")
+    if st == -5:
+        raise RuntimeError("GridCg<APPLYMAT>::setICPreconditioner: Invalid method specified.")
+    if st != 0:
+        raise RuntimeError("solvePressure failed (%d)" % st)
+    return res.iterations, res.resNorm, res.fixPidx
+
+
+def make_laplace_matrix(flags):
+    A = [np.zeros(flags.shape, np.float32) for _ in range(4)]
+    lib().og_make_laplace_matrix(dims(flags.shape), flags, *A)
+    return A
+
+
+def apply_ghost_fluid_diagonal(A0, flags, phi, gfClamp=1e-4):
+    lib().og_apply_ghost_fluid_diagonal(dims(flags.shape), A0, flags, phi, gfClamp)
+
+
+def mic_init(flags, A0, Ai, Aj, Ak):
+    P = np.zeros(flags.shape, np.float32)
+    lib().og_mic_init(dims(flags.shape), flags, P, A0, Ai, Aj, Ak)
+    return P
+
+
+def mic_apply(dst, src, flags, P, Ai, Aj, Ak):
+    lib().og_mic_apply(dims(flags.shape), dst, src, flags, P, Ai, Aj, Ak)
+
+
+def apply_matrix(flags, dst, src, A0, Ai, Aj, Ak):
+    lib().og_apply_matrix(dims(flags.shape), flags, dst, src, A0, Ai, Aj, Ak)
+
+
+def init_domain(flags, boundaryWidth=0, wall="xXyYzZ", open="      ", inflow="      ", outflow="      "):
+    lib().og_init_domain(dims(flags.shape), flags, boundaryWidth, wall.encode(), open.encode(), inflow.encode(),
+                         outflow.encode())
+
+
+def fill_grid(flags, type=FLUID):
+    lib().og_fill_grid(dims(flags.shape), flags, type)
+
+
+def set_open_bound(flags, bWidth, openBound="", type=OUTFLOW | EMPTY):
+    lib().og_set_open_bound(dims(flags.shape), flags, bWidth, openBound.encode(), type)
+
+
+def update_from_levelset(flags, phi):
+    lib().og_update_from_levelset(dims(flags.shape), flags, phi)
+
+
+def box_sdf(phi, p0, p1):
+    lib().og_box_sdf(dims(phi.shape), phi, *map(float, p0), *map(float, p1))
+
+
+def cylinder_apply(grid, center, radius, z, value, respectFlags=None):
+    lib().og_cylinder_apply(dims(grid.shape), grid, *map(float, center), float(radius), *map(float, z), float(value),
+                            _ptr(respectFlags))
+
+
+def box_apply(grid, p0, p1, value, respectFlags=None):
+    lib().og_box_apply(dims(grid.shape), grid, *map(float, p0), *map(float, p1), float(value), _ptr(respectFlags))
+
+
+def join_real(a, b, keepMax=True):
+    lib().og_join_real(a.size, a, b, int(keepMax))
+
+
+def get_max_abs(a):
+    return lib().og_get_max_abs(a.size, a)
