@@ -1,0 +1,401 @@
+"""Throughput of the grid-step hot path on GB300.
+
+Workload: the 3D smoke plume at 256^3 (float32 MAC grid, walls with an open
+top, cylinder source with seeded uniform inflow noise, buoyancy (0,-4e-3,0),
+dt = 1, MacCormack advection of density and velocity with clampMode 2,
+setWallBcs, addBuoyancy, solvePressure with PcMIC at cgAccuracy 1e-3).  One
+step is that full sequence; the metric is cells / step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Multi-GPU runs (torchrun) are independent replicas, one scene per GPU:
+value = all ranks' cells / the slowest rank's time ("scaling": "weak").
+Prints one JSON line (rank 0).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s per full step at 256³; batched sims/h + p99 latency vs plain"
+
+# Algorithmic bytes per cell of each kernel family, in the formulation the
+# kernel implements (inputs read once, outputs written once; gathered
+# neighbours count once; matrix-free Poisson stencil codes of 2 B per cell).
+BYTES_PER_CELL = {
+    "mic_forward": 4 + 4 + 2 + 4,           # r, P, code -> z
+    "mic_backward": 4 + 4 + 2 + 4 + 4,      # z, P, code, r (fused dot) -> z
+    "mic_init": 4 + 2 + 4,                  # A0/code (+GF diag) -> P
+    "pcg_spmv": 4 + 2 + 4,                  # search, code -> tmp (+dot)
+    "pcg_axpy": 4 + 4 + 4 + 4 + 4 + 4,      # p, s, r, tmp -> p, r (+max-abs)
+    "pcg_update": 4 + 4 + 4,                # tmp, s -> s
+    "pcg_init": 4 + 4 + 4 + 4,              # rhs -> p, r, tmp
+    "pcg_set_search": 4 + 4 + 4,            # tmp, r -> search (+dot)
+    "advect_real_fwd": 12 + 4 + 4,          # vel, src -> fwd
+    "advect_real_maccormack": 12 + 4 + 4 + 4 + 4,  # vel, fwd, orig, flags -> new
+    "advect_mac_fwd": 12 + 12,              # vel (= src) -> fwd
+    "advect_mac_maccormack": 12 + 12 + 4 + 12,     # vel (= orig), fwd, flags -> new
+    "advect_outflow": 4,                    # flags (outflow cells only do work)
+    "set_wall_bcs": 4 + 12 + 12,
+    "add_buoyancy": 4 + 4 + 12 + 12,
+    "make_rhs": 4 + 12 + 4,
+    "make_codes": 4 + 2 + 2 + 2,
+    "correct_velocity": 4 + 4 + 12 + 12,
+    "join": 4 + 4 + 4,
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+class Plume:
+    """The plume scene on the GPU through the scene-script API."""
+
+    def __init__(self, m, n, pc, seed, nsteps_noise):
+        self.m, self.n, self.pc = m, n, pc
+        s = m.Solver(name="plume%d" % n, gridSize=m.vec3(n, n, n), dim=3)
+        s.timestep = 1.0
+        self.s = s
+        gs = m.vec3(n, n, n)
+        self.flags = s.create(m.FlagGrid)
+        self.flags.initDomain(boundaryWidth=0)
+        self.flags.fillGrid()
+        m.setOpenBound(self.flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
+        self.vel = s.create(m.MACGrid)
+        self.density = s.create(m.RealGrid)
+        self.pressure = s.create(m.RealGrid)
+        mask = s.create(m.RealGrid)
+        src = s.create(m.Cylinder, center=gs * m.vec3(0.5, 0.1, 0.5), radius=n * 0.14, z=gs * m.vec3(0, 0.02, 0))
+        src.applyToGrid(grid=mask, value=1.0)
+        self.mask = mask.numpy()
+        self.rng = np.random.default_rng(seed)
+        self.iters = []
+
+    def noise(self):
+        n = self.n
+        return (self.rng.random((n, n, n), dtype=np.float32) * self.mask).astype(np.float32)
+
+    def step(self, noise_grid):
+        m = self.m
+        self.density.join(noise_grid)
+        m.advectSemiLagrange(flags=self.flags, vel=self.vel, grid=self.density, order=2, clampMode=2)
+        m.advectSemiLagrange(flags=self.flags, vel=self.vel, grid=self.vel, order=2, clampMode=2)
+        m.setWallBcs(flags=self.flags, vel=self.vel)
+        m.addBuoyancy(density=self.density, vel=self.vel, gravity=m.vec3(0, -4e-3, 0), flags=self.flags)
+        m.solvePressure(flags=self.flags, vel=self.vel, pressure=self.pressure, cgAccuracy=1e-3,
+                        preconditioner=self.pc)
+        self.iters.append(m.lastSolveStats()[0])
+
+
+def cpu_plume_steps(n, steps, warm, threads, seed, state=None, pc=1):
+    """The same plume step with the CPU oracle (OpenMP sweeps, serial MIC as
+    in the reference).  Returns (seconds per timed step list, iterations)."""
+    from oracle import oracle as og
+    og.set_num_threads(threads)
+    f = np.zeros((n, n, n), np.int32)
+    og.init_domain(f, 0)
+    og.fill_grid(f)
+    og.set_open_bound(f, 0, "Y")
+    mask = np.zeros((n, n, n), np.float32)
+    gs = np.float32([n, n, n])
+    og.cylinder_apply(mask, gs * np.float32([0.5, 0.1, 0.5]), np.float32(n * 0.14), gs * np.float32([0, 0.02, 0]), 1.0)
+    if state is None:
+        dens = np.zeros((n, n, n), np.float32)
+        vel = np.zeros((n, n, n, 3), np.float32)
+    else:
+        dens, vel = state
+    pres = np.zeros((n, n, n), np.float32)
+    rng = np.random.default_rng(seed)
+    times, iters = [], []
+    for t in range(warm + steps):
+        a = (rng.random((n, n, n), dtype=np.float32) * mask).astype(np.float32)
+        t0 = time.perf_counter()
+        og.join_real(dens, a)
+        og.advect_semi_lagrange(f, vel, dens, og.KIND_REAL, order=2, clampMode=2)
+        og.advect_semi_lagrange(f, vel, vel, og.KIND_MAC, order=2, clampMode=2)
+        og.set_wall_bcs(f, vel)
+        og.add_buoyancy(f, dens, vel, (0, -4e-3, 0))
+        it, _, _ = og.solve_pressure(f, vel, pres, cgAccuracy=1e-3, preconditioner=pc)
+        dt = time.perf_counter() - t0
+        if t >= warm:
+            times.append(dt)
+            iters.append(it)
+    og.set_num_threads(1)
+    return times, iters
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def allmax(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank, dist):
+    """--impl reference: the CPU path of the reference restated by the
+    oracle (the reference itself needs its own code generator and CMake
+    build, which this project does not run), all host threads."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    warm = min(args.warmup, 1)
+    steps = min(args.steps, 2)
+    times, iters = cpu_plume_steps(args.size, steps, warm, threads, args.seed)
+    t = statistics.median(times)
+    value = args.size ** 3 / t
+    sample = ("256^3 plume steps %d..%d from rest (first %d untimed), full CG to cgAccuracy 1e-3 with MIC(0); "
+              "CG iterations %s" % (warm + 1, warm + steps, warm, iters)) if args.size == 256 else \
+        "%d^3 plume, %d timed steps" % (args.size, steps)
+    out = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": steps, "warmup": warm,
+           "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "3D smoke plume %d^3, MacCormack + MIC-PCG (cgAccuracy 1e-3)" % args.size,
+                      "global_batch": 1, "seq_len": args.size ** 3, "parallelism": "cpu-openmp"},
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--pc", default="mic", choices=["mic", "mgstatic", "mgdynamic"])
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--cpu-steps", type=int, default=1, help="timed oracle steps for cpu_baseline (0: skip)")
+    ap.add_argument("--no-profile", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, dist)
+        return
+    os.environ["MANTA_GB300_DEVICE"] = str(local)
+    import mantaflow_gb300 as m
+    from mantaflow_gb300 import _lib
+    pc = {"mic": m.PcMIC, "mgstatic": m.PcMGStatic, "mgdynamic": m.PcMGDynamic}[args.pc]
+    n = args.size
+    K, W = args.steps, max(3, args.warmup)
+    sim = Plume(m, n, pc, args.seed + rank, W + 2 * K + 4)
+    L = _lib.load()
+
+    # inflow noise for every step, generated up front (host) and uploaded
+    # before the device-resident timed region
+    noise_dev = []
+    for _ in range(W + K):
+        g = sim.s.create(m.RealGrid)
+        m.copyArrayToGridReal(sim.noise(), g)
+        noise_dev.append(g)
+    for t in range(W):
+        sim.step(noise_dev[t])
+    sim.s.sync()
+    if dist is not None:
+        dist.barrier()
+
+    # ---- device-resident throughput (value)
+    cnt0 = C.c_longlong()
+    _lib.check(L.mg_launch_count(C.byref(cnt0)))
+    clocks = ClockSampler(local)
+    clocks.start()
+    _lib.check(L.mg_mark(sim.s._h, 0))
+    it0 = len(sim.iters)
+    for t in range(K):
+        sim.step(noise_dev[W + t])
+    _lib.check(L.mg_mark(sim.s._h, 1))
+    ms = C.c_float()
+    _lib.check(L.mg_elapsed(sim.s._h, 0, 1, C.byref(ms)))
+    clk = clocks.stop()
+    cnt1 = C.c_longlong()
+    _lib.check(L.mg_launch_count(C.byref(cnt1)))
+    elapsed = allmax(dist, ms.value / 1e3)
+    timed_iters = sim.iters[it0:]
+    value = world * n ** 3 * K / elapsed
+    for g in noise_dev:
+        del g
+    noise_dev = None
+
+    # ---- end to end through the API with host buffers: every step uploads
+    # its inflow noise from pinned host memory and downloads the new state
+    nb = n ** 3 * 4
+    pin = C.c_void_p()
+    _lib.check(L.mg_host_alloc(nb * 6, C.byref(pin)))
+    hbuf = np.ctypeslib.as_array((C.c_float * (n ** 3 * 6)).from_address(pin.value))
+    h_noise = hbuf[: n ** 3].reshape(n, n, n)
+    h_dens = hbuf[n ** 3: 2 * n ** 3].reshape(n, n, n)
+    h_pres = hbuf[2 * n ** 3: 3 * n ** 3].reshape(n, n, n)
+    h_vel = hbuf[3 * n ** 3:].reshape(n, n, n, 3)
+    noise_host = [sim.noise() for _ in range(K)]
+    noise_g = sim.s.create(m.RealGrid)
+    sim.s.sync()
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for t in range(K):
+        h_noise[...] = noise_host[t]
+        _lib.check(L.mg_grid_upload(noise_g._h, pin, nb))
+        sim.step(noise_g)
+        _lib.check(L.mg_grid_download(sim.density._h, C.c_void_p(pin.value + nb), nb))
+        _lib.check(L.mg_grid_download(sim.pressure._h, C.c_void_p(pin.value + 2 * nb), nb))
+        _lib.check(L.mg_grid_download(sim.vel._h, C.c_void_p(pin.value + 3 * nb), 3 * nb))
+    sim.s.sync()
+    e2e_t = allmax(dist, time.perf_counter() - t0)
+    e2e = {"value": world * n ** 3 * K / e2e_t, "unit": "cells/s", "h2d_bytes_per_step": nb,
+           "d2h_bytes_per_step": 5 * nb}
+
+    # ---- per-kernel device time (separate pass, events around each family)
+    roofline = None
+    kernels = {}
+    if not args.no_profile:
+        _lib.check(L.mg_profile_reset(sim.s._h))
+        _lib.check(L.mg_profile_enable(sim.s._h, 1))
+        for t in range(2):
+            h_noise[...] = sim.noise()
+            _lib.check(L.mg_grid_upload(noise_g._h, pin, nb))
+            sim.step(noise_g)
+        _lib.check(L.mg_profile_enable(sim.s._h, 0))
+        cap = C.c_int(64)
+        names = (C.c_char_p * 64)()
+        tms = (C.c_double * 64)()
+        lns = (C.c_longlong * 64)()
+        _lib.check(L.mg_profile_read(sim.s._h, C.byref(cap), names, tms, lns))
+        for i in range(cap.value):
+            kernels[names[i].decode()] = (tms[i], lns[i])
+        hbm, src = load_peaks()
+        cand = {k: v for k, v in kernels.items() if k in BYTES_PER_CELL}
+        if cand:
+            top = max(cand, key=lambda k: cand[k][0])
+            tot_ms, launches = cand[top]
+            per = tot_ms / 1e3 / launches
+            bpl = BYTES_PER_CELL[top] * n ** 3
+            achieved = bpl / per / 1e9
+            traffic = None
+            tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+            if os.path.exists(tp):
+                with open(tp) as f:
+                    tr = json.load(f).get(top)
+                if tr:
+                    traffic = tr["bytes_per_cell"] * n ** 3
+            roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
+                        "bytes_per_cell": BYTES_PER_CELL[top], "avg_launch_ms": 1e3 * per,
+                        "share_of_step": tot_ms / sum(v[0] for v in kernels.values())}
+    L.mg_host_free(pin)
+
+    # ---- CPU baseline on a bounded sample (rank 0, one GPU)
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_steps > 0:
+        state = (sim.density.numpy(), sim.vel.numpy())
+        threads = os.cpu_count() or 1
+        times, iters = cpu_plume_steps(n, args.cpu_steps, 0, threads, args.seed + 99, state=state, pc=pc)
+        tc = statistics.median(times)
+        cpu = {"value": n ** 3 / tc, "unit": "cells/s", "cores": threads, "kind": "port",
+               "sample": "%d step(s) of the %d^3 plume continued from the GPU run's state on %d host threads "
+                         "(OpenMP sweeps, serial MIC(0) as in the reference); CG iterations %s" %
+                         (args.cpu_steps, n, threads, iters)}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": K, "warmup": W,
+               "ms_per_step": 1e3 * elapsed / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f32", "data": "synthetic",
+               "config": {"workload": "3D smoke plume %d^3, MacCormack advection + MIC(0)-PCG (cgAccuracy 1e-3)"
+                                      % n if pc == m.PcMIC else "3D smoke plume %d^3, %s" % (n, args.pc),
+                          "global_batch": world, "seq_len": n ** 3, "parallelism": "replicas x%d" % world,
+                          "l2": "inputs larger than L2 (working set > 1 GB per step)",
+                          "cg_iterations": timed_iters},
+               "gpu_launches": int(cnt1.value - cnt0.value),
+               "clocks": clk, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+               "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])}}
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

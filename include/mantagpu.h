@@ -1,0 +1,199 @@
+/*
+ * mantagpu.h -- C ABI of libmantagpu, the GB300 implementation of mantaflow's
+ * grid-step hot path.
+ *
+ * Every entry point replaces one mantaflow Python plugin or one member of the
+ * classes those plugins take (paths relative to the mantaflow source tree).
+ * A plugin translation unit of the reference (source/plugin/*.cpp) calls
+ * these with the grids it receives; INTEGRATION.md shows that binding.
+ *
+ * Conventions
+ *  - Every function returns MG_OK (0) or an MG_ERR_* code; mg_last_error()
+ *    returns the message of the calling thread's last failure.  Messages the
+ *    reference raises as Manta::Error (source/general.h:42-58) are reproduced
+ *    verbatim.
+ *  - Grids live in device memory and are owned by the library.  Host buffers
+ *    passed to mg_grid_upload / mg_grid_download use the reference layout
+ *    (source/grid.h:70): x fastest, Real = float, Vec3/MAC = 3 floats per
+ *    cell, flags = int32.
+ *  - Calls on one solver are ordered on that solver's CUDA stream.  Plugin
+ *    calls return once the work is queued unless they must report a value
+ *    (mg_solve_pressure's iteration count, downloads, reductions).
+ */
+#ifndef MANTAGPU_H
+#define MANTAGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MG_OK 0
+#define MG_ERR_ARG 1
+#define MG_ERR_CUDA 2
+#define MG_ERR_UNSUPPORTED 3
+#define MG_ERR_SOLVER 4      /* the reference's errMsg paths (divergence, asserts) */
+#define MG_ERR_TIMEOUT 5     /* a bounded device-side wait gave up */
+#define MG_ERR_NOMEM 6
+#define MG_ERR_STATE 7       /* library not initialised / wrong device */
+
+/* FlagGrid::CellType (source/grid.h:292-304) */
+#define MG_FLAG_FLUID 1
+#define MG_FLAG_OBSTACLE 2
+#define MG_FLAG_EMPTY 4
+#define MG_FLAG_INFLOW 8
+#define MG_FLAG_OUTFLOW 16
+#define MG_FLAG_OPEN 32
+#define MG_FLAG_STICK 64
+
+/* preconditioners (plugin/pressure.cpp:27) */
+#define MG_PC_NONE 0
+#define MG_PC_MIC 1
+#define MG_PC_MG_DYNAMIC 2
+#define MG_PC_MG_STATIC 3
+
+/* grid kinds: Grid<Real>, Grid<int>, Grid<Vec3>, MACGrid, FlagGrid,
+ * LevelsetGrid (source/grid.h:92-365, source/levelset.h:23) */
+enum mg_grid_kind { MG_REAL = 0, MG_INT = 1, MG_VEC3 = 2, MG_MAC = 3, MG_FLAGS = 4, MG_LEVELSET = 5 };
+
+typedef struct mg_solver_s* mg_solver; /* FluidSolver (source/fluidsolver.h) */
+typedef struct mg_grid_s* mg_grid;     /* a grid bound to one solver */
+
+/* ---- library ------------------------------------------------------------ */
+int mg_init(int device);               /* select the CUDA device; idempotent */
+int mg_shutdown(void);                 /* free every solver and grid */
+const char* mg_last_error(void);
+int mg_version(void);
+int mg_device_count(int* out);
+
+/* ---- FluidSolver (source/fluidsolver.cpp:107-158) ------------------------ */
+/* FluidSolver(name, gridSize, dim): nz must be 1 for dim == 2 */
+int mg_solver_create(int nx, int ny, int nz, int dim, mg_solver* out);
+int mg_solver_destroy(mg_solver s);
+/* FluidSolver::mDt, the `timestep` property; default 1.0 */
+int mg_solver_set_dt(mg_solver s, float dt);
+int mg_solver_get_dt(mg_solver s, float* dt);
+/* wait for all queued work of the solver */
+int mg_solver_sync(mg_solver s);
+/* bytes of device memory held by the solver (grids, pool, solver state) */
+int mg_solver_memory(mg_solver s, size_t* bytes);
+
+/* ---- grids (source/grid.cpp) --------------------------------------------- */
+/* Grid<T>(parent): a zero-initialised grid (grid.cpp:48-58) */
+int mg_grid_create(mg_solver s, int kind, mg_grid* out);
+int mg_grid_destroy(mg_grid g);
+/* host <-> device in the reference layout; bytes must equal the grid size */
+int mg_grid_upload(mg_grid g, const void* host, size_t bytes);
+int mg_grid_download(mg_grid g, void* host, size_t bytes);
+/* Grid<T>::swap (grid.cpp:99-110): exchanges the storage of two grids */
+int mg_grid_swap(mg_grid a, mg_grid b);
+/* Grid<T>::copyFrom */
+int mg_grid_copy(mg_grid dst, mg_grid src);
+/* Grid<T>::setConst (Real/Int/Levelset use x; Vec3/MAC use x,y,z) */
+int mg_grid_set_const(mg_grid g, float x, float y, float z);
+/* Grid<Real>::join (grid.cpp:303-311), knJoinReal */
+int mg_grid_join(mg_grid a, mg_grid b, int keepMax);
+/* Grid<Real>::getMaxAbs (grid.cpp:319-323) */
+int mg_grid_get_max_abs(mg_grid g, float* out);
+/* page-locked host memory for fast uploads/downloads */
+int mg_host_alloc(size_t bytes, void** out);
+int mg_host_free(void* p);
+
+/* ---- plugins: advection (plugin/advection.cpp) --------------------------- */
+/* advectSemiLagrange (:442-460); dt from the solver */
+int mg_advect_semi_lagrange(mg_grid flags, mg_grid vel, mg_grid grid, int order, float strength, int orderSpace,
+                            int openBounds, int boundaryWidth, int clampMode, int orderTrace);
+/* resetPhiInObs (:401) */
+int mg_reset_phi_in_obs(mg_grid flags, mg_grid sdf);
+
+/* ---- plugins: forces and boundaries (plugin/extforces.cpp) --------------- */
+/* setWallBcs (:307-315); obvel, fractions, phiObs may be NULL */
+int mg_set_wall_bcs(mg_grid flags, mg_grid vel, mg_grid obvel, mg_grid fractions, mg_grid phiObs, int boundaryWidth);
+/* addBuoyancy (:83-87) */
+int mg_add_buoyancy(mg_grid flags, mg_grid density, mg_grid vel, float gx, float gy, float gz, float coefficient,
+                    int scale);
+/* addGravity (:61-65); exclude may be NULL */
+int mg_add_gravity(mg_grid flags, mg_grid vel, float gx, float gy, float gz, mg_grid exclude, int scale);
+/* addGravityNoScale (:67-69) */
+int mg_add_gravity_no_scale(mg_grid flags, mg_grid vel, float gx, float gy, float gz, mg_grid exclude);
+/* setOpenBound (:105-130); type defaults to Outflow|Empty in the reference */
+int mg_set_open_bound(mg_grid flags, int bWidth, const char* openBound, int type);
+/* resetOutflow (:133-160) without particles; phi, real may be NULL */
+int mg_reset_outflow(mg_grid flags, mg_grid phi, mg_grid real);
+
+/* ---- plugins: simple extrapolation (fastmarch.cpp) ----------------------- */
+/* extrapolateMACSimple (:337-375); phiObs must be NULL */
+int mg_extrapolate_mac_simple(mg_grid flags, mg_grid vel, int distance, mg_grid phiObs, int intoObs);
+
+/* ---- plugins: pressure (plugin/pressure.cpp) ----------------------------- */
+typedef struct {
+  float cgAccuracy;          /* 1e-3 */
+  float gfClamp;             /* 1e-4 */
+  float cgMaxIterFac;        /* 1.5 */
+  int precondition;          /* 1 (deprecated switch: 0 forces PcNone) */
+  int preconditioner;        /* MG_PC_MIC */
+  int enforceCompatibility;  /* 0 */
+  int useL2Norm;             /* 0 */
+  int zeroPressureFixing;    /* 0 */
+  float surfTens;            /* 0 */
+} mg_pressure_params;
+
+typedef struct {
+  int iterations;            /* GridCg::getIterations */
+  float resNorm;             /* GridCg::getResNorm */
+} mg_pressure_result;
+
+void mg_pressure_params_default(mg_pressure_params* p);
+/* solvePressure (:480-521).  phi, perCellCorr, curv, retRhs may be NULL;
+ * fractions and obvel must be NULL.  out may be NULL. */
+int mg_solve_pressure(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p, mg_grid phi,
+                      mg_grid perCellCorr, mg_grid fractions, mg_grid obvel, mg_grid curv, mg_grid retRhs,
+                      mg_pressure_result* out);
+/* computePressureRhs (:277-299) */
+int mg_compute_pressure_rhs(mg_grid rhs, mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p,
+                            mg_grid phi, mg_grid perCellCorr, mg_grid fractions, mg_grid obvel, mg_grid curv);
+/* solvePressureSystem (:312-452); rhs is modified when pressure is pinned */
+int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p,
+                             mg_grid phi, mg_grid perCellCorr, mg_grid fractions, mg_grid curv,
+                             mg_pressure_result* out);
+/* correctVelocity (:455-476) */
+int mg_correct_velocity(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p, mg_grid phi,
+                        mg_grid perCellCorr, mg_grid fractions, mg_grid curv);
+/* releaseMG (:252-266); s == NULL releases every solver's hierarchy */
+int mg_release_mg(mg_solver s);
+
+/* ---- scene setup (source/grid.cpp, source/shapes.cpp) -------------------- */
+/* FlagGrid::initDomain (grid.cpp:732-822); phiWalls must be NULL */
+int mg_flags_init_domain(mg_grid flags, int boundaryWidth, const char* wall, const char* open, const char* inflow,
+                         const char* outflow, mg_grid phiWalls);
+/* FlagGrid::fillGrid (grid.cpp:856-861) */
+int mg_flags_fill_grid(mg_grid flags, int type);
+/* FlagGrid::updateFromLevelset (grid.cpp:844-854) */
+int mg_flags_update_from_levelset(mg_grid flags, mg_grid levelset);
+/* Shape::applyToGrid for Box (shapes.cpp:38-86, 151-154); value[3] for
+ * Vec3/MAC, value[0] for Real, ivalue for Int/Flags; respectFlags may be NULL */
+int mg_shape_box_apply(mg_grid grid, const float* p0, const float* p1, const float* value, int ivalue,
+                       mg_grid respectFlags);
+/* Shape::applyToGrid for Cylinder(center, radius, z) (shapes.cpp:316-329) */
+int mg_shape_cylinder_apply(mg_grid grid, const float* center, float radius, const float* z, const float* value,
+                            int ivalue, mg_grid respectFlags);
+/* Box::computeLevelset (BoxSDF, shapes.cpp:178-232) into a Real/Levelset grid */
+int mg_shape_box_levelset(mg_grid phi, const float* p0, const float* p1);
+
+/* ---- timing (CUDA events on the solver's stream) ------------------------- */
+/* per-kernel-family device time accumulated while profiling is on */
+int mg_profile_enable(mg_solver s, int on);
+/* name[i] / milliseconds[i] / launches[i] for i < *count (in, capacity; out, used) */
+int mg_profile_read(mg_solver s, int* count, const char** names, double* ms, long long* launches);
+int mg_profile_reset(mg_solver s);
+/* device time between two marks on the solver's stream, in ms */
+int mg_mark(mg_solver s, int slot);
+int mg_elapsed(mg_solver s, int slot0, int slot1, float* ms);
+/* kernels launched by this library since load (all solvers) */
+int mg_launch_count(long long* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,117 @@
+// Host-side launcher declarations for the grid-step kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mg_common.cuh"
+
+namespace mgpu {
+
+// number of kernels this library has launched (the bench's gpu_launches)
+extern unsigned long long g_launches;
+inline void count_launch() { g_launches++; }
+
+// ---- advection (advect.cu)
+void launch_advect_sl(const Dims& d, int ch, CMac vel, const float* src, float* dst, float dt, int orderSpace,
+                      int orderTrace, cudaStream_t s);
+void launch_advect_maccormack(const Dims& d, int ch, const int* flags, CMac vel, const float* orig, const float* fwd,
+                              float* dst, float dt, float strength, int clampMode, int orderSpace, int orderTrace,
+                              cudaStream_t s);
+void launch_advect_sl_mac(const Dims& d, CMac vel, CMac src, Mac dst, float dt, int orderTrace, cudaStream_t s);
+void launch_advect_maccormack_mac(const Dims& d, const int* flags, CMac vel, CMac orig, CMac fwd, Mac dst, float dt,
+                                  float strength, int clampMode, int orderTrace, cudaStream_t s);
+void launch_outflow_bc(const Dims& d, const int* flags, CMac vel, CMac velPrev, Mac velDst, Mac velOut, float timeStep,
+                       cudaStream_t s);
+void launch_reset_phi_in_obs(const Dims& d, const int* flags, float* sdf, cudaStream_t s);
+
+// ---- forces, setup, utilities (forces.cu)
+void launch_set_wall_bcs(const Dims& d, const int* flags, Mac vel, const Mac* obvel, cudaStream_t s);
+void launch_add_buoyancy(const Dims& d, const int* flags, const float* rho, Mac vel, float hx, float hy, float hz,
+                         cudaStream_t s);
+void launch_add_force(const Dims& d, const int* flags, Mac vel, float fx, float fy, float fz, const float* exclude,
+                      cudaStream_t s);
+void launch_extrapolate_mac_simple(const Dims& d, const int* flags, Mac vel, int* tmp, Mac snap, int distance, int intoObs,
+                                   cudaStream_t s);
+void launch_init_domain(const Dims& d, int* flags, int bw, const int* types, cudaStream_t s);
+void launch_fill_grid(const Dims& d, int* flags, int type, cudaStream_t s);
+void launch_set_open_bound(const Dims& d, int* flags, int bw, const int* lo, const int* up, int type, cudaStream_t s);
+void launch_reset_outflow(const Dims& d, int* flags, float* phi, float* real, cudaStream_t s);
+void launch_update_from_levelset(const Dims& d, int* flags, const float* phi, cudaStream_t s);
+void launch_box_sdf(const Dims& d, float* phi, const float* p0, const float* p1, cudaStream_t s);
+void launch_shape_apply(const Dims& d, int shape, float* freal, int* fint, Mac* mac, const float* value, int ivalue,
+                        const int* respect, const float* a, const float* b, float radius, float mZ, cudaStream_t s);
+void launch_aos_to_soa(long long n, const float* aos, Mac soa, cudaStream_t s);
+void launch_soa_to_aos(long long n, CMac soa, float* aos, cudaStream_t s);
+void launch_join(long long n, float* a, const float* b, int keepMax, cudaStream_t s);
+void launch_set_const(long long n, float* a, float v, cudaStream_t s);
+int launch_minmax_partial(long long n, const float* a, float* part, cudaStream_t s);
+
+// ---- pressure projection (pressure.cu)
+// Per-cell 7-point stencil code replacing the reference's four stored
+// coefficient grids A0/Ai/Aj/Ak (conjugategrad.h:154-187):
+//   bits 0-2  A0: number of non-obstacle neighbours (interior fluid cells)
+//   bit  3    cell is fluid
+//   bits 4-6  Ai(c-x), Aj(c-y), Ak(c-z) == -1   (link to the lower neighbour)
+//   bits 7-9  Ai(c),   Aj(c),   Ak(c)   == -1   (link to the upper neighbour)
+typedef uint16_t code_t;
+enum : int { kCodeFluid = 8, kLowX = 16, kLowY = 32, kLowZ = 64, kHighX = 128, kHighY = 256, kHighZ = 512 };
+
+// device-resident scalars of one CG solve (GridCg members, conjugategrad.h:65-114)
+struct CgScalars {
+  float sigma, alpha, beta, resNorm, dp, accuracy;
+  int iterations, done, status, maxIter;
+  int useL2, pad;
+  double sum;   // MakeRhs sum (enforceCompatibility)
+  int cnt, pad2;
+  unsigned int counters[8];  // last-block tickets
+};
+
+enum { kPcNone = 0, kPcMic = 1, kPcMg = 2 };
+
+struct PcgBuffers {
+  Dims d;
+  const int* flags;
+  code_t* code;
+  float* A0f;       // non-null with ghost fluid: float diagonal
+  float* rhs;
+  float* pressure;
+  float* residual;
+  float* search;
+  float* tmp;
+  float* P;         // MIC diagonal (Aprecond)
+  double* part;     // per-block / per-tile partial sums
+  float* partf;     // per-block partial max/min
+  CgScalars* sc;
+  int nblocks;      // blocks of the streaming kernels
+};
+
+struct MicPlan {
+  int tx, ty, tz;         // tiles per axis
+  int ntiles;
+  int* order;             // tile dispatch order (wavefront levels)
+  unsigned int* tileDone; // epoch stamp per tile
+  int* counter;           // dispenser, zeroed before each sweep
+  int* error;             // spin-limit diagnostics
+  int ctas;               // persistent CTAs
+};
+
+void launch_make_rhs(const PcgBuffers& b, const float* vu, const float* vv, const float* vw, const float* perCellCorr,
+                     const float* phi, const float* curv, float surfTens, float gfClamp, cudaStream_t s);
+void launch_compat_shift(const PcgBuffers& b, cudaStream_t s);
+void launch_make_codes(const PcgBuffers& b, cudaStream_t s);
+void launch_ghost_fluid_diag(const PcgBuffers& b, const float* phi, float gfClamp, cudaStream_t s);
+void launch_count_empty(const PcgBuffers& b, int* out, cudaStream_t s);
+void launch_fix_pressure(const PcgBuffers& b, long long fix, cudaStream_t s);
+void launch_pcg_init(const PcgBuffers& b, cudaStream_t s);
+void launch_pcg_set_search(const PcgBuffers& b, cudaStream_t s);
+void launch_pcg_spmv(const PcgBuffers& b, cudaStream_t s);
+void launch_pcg_axpy(const PcgBuffers& b, cudaStream_t s);
+void launch_pcg_copy_dot(const PcgBuffers& b, cudaStream_t s);   // PcNone: tmp = residual, sigmaNew
+void launch_pcg_update(const PcgBuffers& b, cudaStream_t s);
+void launch_mic(const PcgBuffers& b, const MicPlan& m, int mode, unsigned int epoch, long long spinLimit, cudaStream_t s);
+void launch_correct_velocity(const Dims& d, const int* flags, Mac vel, const float* p, const float* phi, const float* curv,
+                             float gfClamp, float surfTens, cudaStream_t s);
+void mic_plan_order(int tx, int ty, int tz, int* order);
+int mic_ctas_per_sm();
+
+}  // namespace mgpu

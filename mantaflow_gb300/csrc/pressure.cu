@@ -1,0 +1,835 @@
+// Pressure projection on the GPU: plugin/pressure.cpp + conjugategrad.*.
+//
+//  * The Poisson matrix is not stored as four float grids.  A 16-bit stencil
+//    code per cell (see mg_kernels.h) carries the same coefficients: A0 is a
+//    small integer and every off-diagonal entry is 0 or -1 without
+//    fractions, so the SpMV below performs exactly the reference's float
+//    operations (x*A0 + x(c-X)*Ai(c-X) + ...) while reading 2 bytes of
+//    matrix per cell instead of 16.  With ghost fluid the diagonal is kept
+//    as a float grid.
+//  * PCG scalars live on the device.  Reductions are two-level: per-block
+//    (or per-tile) partials, then the last block to finish reduces them in
+//    index order (deterministic) and updates the scalars.  Dot products
+//    accumulate float products in double, as GridDotProduct does.
+//  * MIC(0) (conjugategrad.cpp:66-97, 135-160) is a lexicographic recurrence.
+//    The sweeps run as tiled wavefronts: 16^3 tiles dispatched in
+//    i+j+k tile order to persistent CTAs, each tile waiting (bounded spin)
+//    for its three upwind tiles, and inside a tile one thread per (y,z) line
+//    stepping through the 46 cell levels.  Each cell sees exactly the values
+//    the serial loop would, so the result is the reference's bit for bit.
+#include "mg_common.cuh"
+#include "mg_kernels.h"
+
+#include <cfloat>
+
+namespace mgpu {
+
+static const dim3 kBlk(32, 8, 1);
+static const int kThreads = 256;
+
+#define CELL_IJK                                        \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x; \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y; \
+  const int k = blockIdx.z;                             \
+  if (i >= d.nx || j >= d.ny) return;                   \
+  const long long idx = ix(d, i, j, k);
+
+#define INNER (i >= 1 && i < d.nx - 1 && j >= 1 && j < d.ny - 1 && (!d.is3d || (k >= 1 && k < d.nz - 1)))
+
+// ------------------------------------------------------------ reductions
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int lin_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
+__device__ __forceinline__ int nwarps() { return (blockDim.x * blockDim.y * blockDim.z) >> 5; }
+
+// block sum in a fixed order; result valid in thread 0
+template <typename T>
+__device__ __forceinline__ T block_sum(T v) {
+  __shared__ T sh[32];
+  const int t = lin_tid();
+  const int lane = t & 31, wid = t >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  T r = 0;
+  if (t == 0)
+    for (int q = 0; q < nwarps(); q++) r += sh[q];
+  return r;
+}
+
+__device__ __forceinline__ void block_minmax(float& mn, float& mx) {
+  __shared__ float s0[32], s1[32];
+  const int t = lin_tid();
+  const int lane = t & 31, wid = t >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  __syncthreads();
+  if (lane == 0) { s0[wid] = mn; s1[wid] = mx; }
+  __syncthreads();
+  if (t == 0)
+    for (int q = 1; q < nwarps(); q++) { mn = fminf(mn, s0[q]); mx = fmaxf(mx, s1[q]); }
+}
+
+// "last block" ticket: returns true in thread 0 of the block that finishes last
+__device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int total) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int t = atomicAdd(counter, 1u);
+    last = (t == total - 1);
+    if (last) *counter = 0;  // reset for the next launch
+  }
+  __syncthreads();
+  return last;
+}
+
+// ------------------------------------------------------------------ MakeRhs
+// MakeRhs (pressure.cpp:32-84) without fractions/obvel.
+__global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict__ flags, float* rhs, const float* __restrict__ vu,
+                                                  const float* __restrict__ vv, const float* __restrict__ vw,
+                                                  const float* __restrict__ corr, const float* __restrict__ phi,
+                                                  const float* __restrict__ curv, float surfTens, float gfClamp,
+                                                  double* part, CgScalars* sc, unsigned int nblk);
+
+__device__ __forceinline__ float theta_helper(float inside, float outside) {
+  const float denom = inside - outside;
+  if ((double)denom > -1e-04) return 0.5f;
+  float r = inside / denom;
+  r = r < 1.f ? r : 1.f;       // std::min(Real(1), .)
+  return 0.f < r ? r : 0.f;    // std::max(Real(0), .)
+}
+// ghostFluidHelper (pressure.cpp:121-126): returns gfClamp when clamped,
+// else (float)(1. - 1./alpha) computed in double (surface cells only)
+__device__ __forceinline__ float gf_helper(const float* __restrict__ phi, long long idx, long long off, float gfClamp) {
+  const float alpha = theta_helper(phi[idx], phi[idx + off]);
+  if (alpha < gfClamp) return gfClamp;
+  return (float)(1. - (1. / (double)alpha));
+}
+__device__ __forceinline__ float surf_tens_helper(const float* phi, const float* curv, long long idx, long long off,
+                                                  float st, float gfc) {
+  return st * (curv[idx + off] - gf_helper(phi, idx, off, gfc) * curv[idx]);
+}
+
+__global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict__ flags, float* rhs, const float* __restrict__ vu,
+                                                  const float* __restrict__ vv, const float* __restrict__ vw,
+                                                  const float* __restrict__ corr, const float* __restrict__ phi,
+                                                  const float* __restrict__ curv, float surfTens, float gfClamp,
+                                                  double* part, CgScalars* sc, unsigned int nblk) {
+  double sum = 0.;
+  double cnt = 0.;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i < d.nx && j < d.ny) {
+    const long long idx = ix(d, i, j, k);
+    if (INNER) {
+      if (!isF(flags, idx)) {
+        rhs[idx] = 0.f;
+      } else {
+        float set = vu[idx] - vu[idx + 1] + vv[idx] - vv[idx + d.sy];
+        if (d.is3d) set += vw[idx] - vw[idx + d.sz];
+        if (phi && curv) {
+          const long long X = 1, Y = d.sy, Z = d.sz;
+          if (isE(flags, idx - X)) set += surf_tens_helper(phi, curv, idx, -X, surfTens, gfClamp);
+          if (isE(flags, idx + X)) set += surf_tens_helper(phi, curv, idx, +X, surfTens, gfClamp);
+          if (isE(flags, idx - Y)) set += surf_tens_helper(phi, curv, idx, -Y, surfTens, gfClamp);
+          if (isE(flags, idx + Y)) set += surf_tens_helper(phi, curv, idx, +Y, surfTens, gfClamp);
+          if (d.is3d) {
+            if (isE(flags, idx - Z)) set += surf_tens_helper(phi, curv, idx, -Z, surfTens, gfClamp);
+            if (isE(flags, idx + Z)) set += surf_tens_helper(phi, curv, idx, +Z, surfTens, gfClamp);
+          }
+        }
+        if (corr) set += corr[idx];
+        sum = set;
+        cnt = 1.;
+        rhs[idx] = set;
+      }
+    } else {
+      rhs[idx] = 0.f;  // fresh grid: the border stays zero
+    }
+  }
+  const unsigned int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  const double bs = block_sum(sum);
+  const double bc = block_sum(cnt);
+  if (threadIdx.x + blockDim.x * threadIdx.y == 0) {
+    part[2 * b] = bs;
+    part[2 * b + 1] = bc;
+  }
+  (void)nblk;
+}
+
+// rhs += (Real)(-sum / (Real)cnt) on every cell (pressure.cpp:296-297)
+__global__ void k_compat_reduce(const double* part, int nb, CgScalars* sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0., c = 0.;
+  for (int q = 0; q < nb; q++) { s += part[2 * q]; c += part[2 * q + 1]; }
+  sc->sum = s;
+  sc->cnt = (int)c;
+}
+__global__ void k_compat_shift(long long n, float* rhs, const CgScalars* sc) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const float add = (float)(-sc->sum / (double)(float)sc->cnt);
+  rhs[idx] += add;
+}
+
+// ------------------------------------------------------- stencil codes
+// MakeLaplaceMatrix (conjugategrad.h:154-187) as codes.  Pass 1: A0 count,
+// fluid bit and the upward links of interior fluid cells.
+__global__ void k_make_codes(Dims d, const int* __restrict__ flags, code_t* code) {
+  CELL_IJK
+  const bool fl = isF(flags, idx);
+  int c = fl ? kCodeFluid : 0;
+  if (fl && INNER) {
+    int a0 = 0;
+    a0 += !isO(flags, idx - 1);
+    a0 += !isO(flags, idx + 1);
+    a0 += !isO(flags, idx - d.sy);
+    a0 += !isO(flags, idx + d.sy);
+    if (d.is3d) {
+      a0 += !isO(flags, idx - d.sz);
+      a0 += !isO(flags, idx + d.sz);
+    }
+    c |= a0;
+    if (isF(flags, idx + 1)) c |= kHighX;
+    if (isF(flags, idx + d.sy)) c |= kHighY;
+    if (d.is3d && isF(flags, idx + d.sz)) c |= kHighZ;
+  }
+  code[idx] = (code_t)c;
+}
+// pass 2: lower links mirror the upper link of the lower neighbour
+__global__ void k_make_codes_low(Dims d, code_t* code) {
+  CELL_IJK
+  int c = code[idx];
+  if (i > 0 && (code[idx - 1] & kHighX)) c |= kLowX;
+  if (j > 0 && (code[idx - d.sy] & kHighY)) c |= kLowY;
+  if (k > 0 && (code[idx - d.sz] & kHighZ)) c |= kLowZ;
+  code[idx] = (code_t)c;
+}
+
+// ApplyGhostFluidDiagonal (pressure.cpp:136-151): float diagonal
+__global__ void k_ghost_fluid_diag(Dims d, const int* __restrict__ flags, const code_t* __restrict__ code,
+                                   const float* __restrict__ phi, float gfClamp, float* A0f) {
+  CELL_IJK
+  float a = (float)(code[idx] & 7);
+  if (INNER && isF(flags, idx)) {
+    const long long X = 1, Y = d.sy, Z = d.sz;
+    if (isE(flags, idx - X)) a -= gf_helper(phi, idx, -X, gfClamp);
+    if (isE(flags, idx + X)) a -= gf_helper(phi, idx, +X, gfClamp);
+    if (isE(flags, idx - Y)) a -= gf_helper(phi, idx, -Y, gfClamp);
+    if (isE(flags, idx + Y)) a -= gf_helper(phi, idx, +Y, gfClamp);
+    if (d.is3d) {
+      if (isE(flags, idx - Z)) a -= gf_helper(phi, idx, -Z, gfClamp);
+      if (isE(flags, idx + Z)) a -= gf_helper(phi, idx, +Z, gfClamp);
+    }
+  }
+  A0f[idx] = a;
+}
+
+// CountEmptyCells (pressure.cpp:217-220)
+__global__ void k_count_empty(long long n, const int* __restrict__ flags, int* out) {
+  int c = 0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x)
+    c += (__ldg(flags + idx) & kEmpty) ? 1 : 0;
+  c = warp_sum(c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// fixPressure(fixPidx, 0, ...) (pressure.cpp:226-245): the rhs updates of
+// the neighbours subtract A*0 and leave them unchanged.
+__global__ void k_fix_pressure(Dims d, long long f, code_t* code, float* A0f, float* rhs) {
+  if (threadIdx.x != 0) return;
+  rhs[f] = 0.f;
+  code[f] = (code_t)((code[f] & kCodeFluid) | 1);
+  if (A0f) A0f[f] = 1.f;
+  code[f - 1] &= (code_t)~kHighX;
+  code[f + 1] &= (code_t)~kLowX;
+  code[f - d.sy] &= (code_t)~kHighY;
+  code[f + d.sy] &= (code_t)~kLowY;
+  if (d.is3d) {
+    code[f - d.sz] &= (code_t)~kHighZ;
+    code[f + d.sz] &= (code_t)~kLowZ;
+  }
+}
+
+__device__ __forceinline__ float diag(const code_t c, const float* A0f, long long idx) {
+  return A0f ? A0f[idx] : (float)(c & 7);
+}
+
+// ------------------------------------------------------------------- PCG
+// doInit part 1 (conjugategrad.cpp:209-216): dst=0, residual=rhs, tmp=0
+__global__ void k_pcg_init(long long n, float* p, const float* __restrict__ rhs, float* r, float* tmp) {
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+    p[idx] = 0.f;
+    r[idx] = rhs[idx];
+    tmp[idx] = 0.f;
+  }
+}
+
+// search = tmp; sigma = dot(tmp, residual) (conjugategrad.cpp:232-234)
+__global__ void __launch_bounds__(256) k_pcg_set_search(long long n, const float* __restrict__ tmp,
+                                                        const float* __restrict__ r, float* search, double* part,
+                                                        CgScalars* sc) {
+  double acc = 0.;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+    const float t = tmp[idx];
+    search[idx] = t;
+    acc += (double)(t * r[idx]);
+  }
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
+  if (last_block(&sc->counters[0], gridDim.x)) {
+    double s = 0.;
+    for (unsigned q = 0; q < gridDim.x; q++) s += part[q];
+    sc->sigma = (float)s;
+  }
+}
+
+// tmp = A*search (ApplyMatrix, conjugategrad.h:118-151) and dp = dot(tmp,
+// search); the last block forms alpha = sigma/dp (conjugategrad.cpp:249-253)
+__global__ void __launch_bounds__(256) k_pcg_spmv(Dims d, const code_t* __restrict__ code, const float* __restrict__ A0f,
+                                                  const float* __restrict__ x, float* y, double* part, CgScalars* sc) {
+  if (sc->done) return;
+  double acc = 0.;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < d.n; idx += (long long)gridDim.x * blockDim.x) {
+    const int c = code[idx];
+    const float xc = x[idx];
+    float v;
+    if (!(c & kCodeFluid)) {
+      v = xc;
+    } else {
+      v = xc * diag((code_t)c, A0f, idx);
+      if (c & kLowX) v = v - x[idx - 1];
+      if (c & kHighX) v = v - x[idx + 1];
+      if (c & kLowY) v = v - x[idx - d.sy];
+      if (c & kHighY) v = v - x[idx + d.sy];
+      if (c & kLowZ) v = v - x[idx - d.sz];
+      if (c & kHighZ) v = v - x[idx + d.sz];
+    }
+    y[idx] = v;
+    acc += (double)(v * xc);
+  }
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
+  if (last_block(&sc->counters[1], gridDim.x)) {
+    double s = 0.;
+    for (unsigned q = 0; q < gridDim.x; q++) s += part[q];
+    const float dp = (float)s;
+    sc->dp = dp;
+    float alpha = 0.f;
+    if (fabsf(dp) > 0.f) alpha = sc->sigma / dp;
+    sc->alpha = alpha;
+  }
+}
+
+// dst += alpha*search, residual += -alpha*tmp, then the residual norm
+// (max-abs, or sum of squares with useL2Norm) and the convergence test
+// (conjugategrad.cpp:255-276).
+__global__ void __launch_bounds__(256) k_pcg_axpy(long long n, float* p, const float* __restrict__ s, float* r,
+                                                  const float* __restrict__ t, double* part, float* partf, CgScalars* sc) {
+  if (sc->done) return;
+  const float alpha = sc->alpha, na = -alpha;
+  const int l2 = sc->useL2;
+  float mn = FLT_MAX, mx = -FLT_MAX;
+  double ss = 0.;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+    p[idx] = p[idx] + alpha * s[idx];
+    const float rv = r[idx] + na * t[idx];
+    r[idx] = rv;
+    mn = fminf(mn, rv);
+    mx = fmaxf(mx, rv);
+    if (l2) ss += (double)rv * (double)rv;
+  }
+  block_minmax(mn, mx);
+  const double bs = l2 ? block_sum(ss) : 0.;
+  if (threadIdx.x == 0) {
+    partf[2 * blockIdx.x] = mn;
+    partf[2 * blockIdx.x + 1] = mx;
+    part[blockIdx.x] = bs;
+  }
+  if (last_block(&sc->counters[2], gridDim.x)) {
+    float res;
+    if (l2) {
+      double a = 0.;
+      for (unsigned q = 0; q < gridDim.x; q++) a += part[q];
+      res = (float)a;
+    } else {
+      float amin = FLT_MAX, amax = -FLT_MAX;
+      for (unsigned q = 0; q < gridDim.x; q++) {
+        amin = fminf(amin, partf[2 * q]);
+        amax = fmaxf(amax, partf[2 * q + 1]);
+      }
+      const float x = fabsf(amin), y = fabsf(amax);
+      res = x < y ? y : x;
+    }
+    sc->iterations += 1;
+    sc->resNorm = res;
+    if (res < sc->accuracy) {
+      sc->sigma = res;
+      sc->done = 1;
+    }
+  }
+}
+
+// PcNone: tmp = residual and sigmaNew = dot(tmp, residual)
+__global__ void __launch_bounds__(256) k_pcg_copy_dot(long long n, const float* __restrict__ r, float* tmp, double* part,
+                                                      CgScalars* sc) {
+  if (sc->done) return;
+  double acc = 0.;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+    const float v = r[idx];
+    tmp[idx] = v;
+    acc += (double)(v * v);
+  }
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
+  if (last_block(&sc->counters[3], gridDim.x)) {
+    double s = 0.;
+    for (unsigned q = 0; q < gridDim.x; q++) s += part[q];
+    const float sigmaNew = (float)s;
+    sc->beta = sigmaNew / sc->sigma;
+    sc->sigma = sigmaNew;
+    if (!(sc->resNorm < 1e35f)) { sc->status = 2; sc->done = 1; }
+  }
+}
+
+// search = tmp + beta*search (UpdateSearchVec, conjugategrad.cpp:193-196)
+__global__ void k_pcg_update(long long n, const float* __restrict__ t, float* s, const CgScalars* sc) {
+  if (sc->done) return;
+  const float beta = sc->beta;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x)
+    s[idx] = t[idx] + beta * s[idx];
+}
+
+// ---------------------------------------------------------------- MIC(0)
+constexpr int T = 16;           // tile edge
+constexpr int TC = T * T * T;   // cells per tile
+constexpr int NL = 3 * T - 2;   // cell levels per tile
+
+struct MicArgs {
+  Dims d;
+  const code_t* code;
+  const float* A0f;
+  float* P;
+  const float* r;     // residual (forward input) / residual for the dot (backward)
+  float* z;           // tmp
+  double* part;       // per-tile dot partials (backward)
+  CgScalars* sc;
+  int tx, ty, tz, ntiles;
+  const int* order;
+  unsigned int* tileDone;
+  int* counter;
+  int* error;
+  unsigned int epoch;
+  long long spinLimit;
+};
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Wait (thread 0) until tile `t` carries this sweep's epoch; gives up after
+// spinLimit polls, records the failure and lets the sweep finish.
+__device__ __forceinline__ void wait_tile(const MicArgs& a, int t) {
+  if (t < 0) return;
+  long long n = 0;
+  while (ld_acquire(a.tileDone + t) != a.epoch) {
+    // once any wait has given up the sweep is already wrong: stop waiting
+    if (++n > a.spinLimit || *((volatile int*)a.error) != 0) {
+      atomicExch(a.error, 1);
+      return;
+    }
+    __nanosleep(32);
+  }
+}
+
+// MODE 0: InitPreconditionModifiedIncompCholesky2 -> P
+// MODE 1: forward substitution r -> z
+// MODE 2: backward substitution z -> z, plus dot(z, r) per tile
+template <int MODE>
+__global__ void __launch_bounds__(256) k_mic(MicArgs a) {
+  __shared__ float s_val[TC];     // z (fwd/bwd) or P (init)
+  __shared__ float s_P[TC];       // P (fwd/bwd) / A0 (init)
+  __shared__ code_t s_code[TC];
+  __shared__ float h_val[3][T * T];   // halo faces: value (z or P)
+  __shared__ float h_P[3][T * T];     // halo faces: P (fwd/bwd)
+  __shared__ code_t h_code[3][T * T]; // halo faces: code (init)
+  __shared__ int s_tile;
+  const Dims& d = a.d;
+  const int tid = threadIdx.x;
+  const int ly = tid & (T - 1), lz = tid >> 4;
+  if (MODE != 0 && a.sc->done) return;  // converged before this application
+  for (;;) {
+    if (tid == 0) {
+      const int q = atomicAdd(a.counter, 1);
+      s_tile = q < a.ntiles ? (MODE == 2 ? a.order[a.ntiles - 1 - q] : a.order[q]) : -1;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile < 0) return;
+    const int ta = tile % a.tx, tb = (tile / a.tx) % a.ty, tcz = tile / (a.tx * a.ty);
+    const int x0 = ta * T, y0 = tb * T, z0 = tcz * T;
+    // stage this tile's inputs (independent of the neighbours)
+    for (int e = tid; e < TC; e += kThreads) {
+      const int x = x0 + (e & (T - 1)), y = y0 + ((e >> 4) & (T - 1)), zc = z0 + (e >> 8);
+      code_t c = 0;
+      float v = 0.f, p = 0.f;
+      if (x < d.nx && y < d.ny && zc < d.nz) {
+        const long long g = ix(d, x, y, zc);
+        c = a.code[g];
+        if (MODE == 0) {
+          p = a.A0f ? a.A0f[g] : (float)(c & 7);
+        } else {
+          p = a.P[g];
+          v = MODE == 1 ? a.r[g] : a.z[g];
+        }
+      }
+      s_code[e] = c;
+      s_P[e] = p;
+      s_val[e] = v;
+    }
+    // wait for the upwind tiles (downwind for the backward sweep)
+    if (tid == 0) {
+      if (MODE == 2) {
+        wait_tile(a, ta + 1 < a.tx ? tile + 1 : -1);
+        wait_tile(a, tb + 1 < a.ty ? tile + a.tx : -1);
+        wait_tile(a, tcz + 1 < a.tz ? tile + a.tx * a.ty : -1);
+      } else {
+        wait_tile(a, ta > 0 ? tile - 1 : -1);
+        wait_tile(a, tb > 0 ? tile - a.tx : -1);
+        wait_tile(a, tcz > 0 ? tile - a.tx * a.ty : -1);
+      }
+    }
+    __syncthreads();
+    // halo faces from the neighbours (written by other CTAs: bypass L1)
+    for (int f = 0; f < 3; f++) {
+      const int u = tid & (T - 1), w = tid >> 4;  // face coordinates
+      int x, y, zc;
+      if (f == 0) { x = MODE == 2 ? x0 + T : x0 - 1; y = y0 + u; zc = z0 + w; }
+      else if (f == 1) { x = x0 + u; y = MODE == 2 ? y0 + T : y0 - 1; zc = z0 + w; }
+      else { x = x0 + u; y = y0 + w; zc = MODE == 2 ? z0 + T : z0 - 1; }
+      float hv = 0.f, hp = 0.f;
+      code_t hc = 0;
+      if (x >= 0 && y >= 0 && zc >= 0 && x < d.nx && y < d.ny && zc < d.nz) {
+        const long long g = ix(d, x, y, zc);
+        hc = a.code[g];
+        if (MODE == 0) {
+          hv = __ldcg(a.P + g);
+        } else {
+          hv = __ldcg(a.z + g);
+          hp = a.P[g];
+        }
+      }
+      h_val[f][tid] = hv;
+      h_P[f][tid] = hp;
+      h_code[f][tid] = hc;
+    }
+    __syncthreads();
+    double acc = 0.;
+    // the wavefront: thread (ly, lz) owns the x-line of the tile
+    for (int s = 0; s < NL; s++) {
+      const int L = MODE == 2 ? NL - 1 - s : s;
+      const int x = L - ly - lz;
+      if (x >= 0 && x < T) {
+        const int e = x + T * ly + T * T * lz;
+        const int c = s_code[e];
+        if (MODE == 0) {
+          float pv = 0.f;
+          if (c & kCodeFluid) {
+            // neighbour P values and the codes of the lower neighbours
+            const float px = x > 0 ? s_val[e - 1] : h_val[0][ly + T * lz];
+            const float py = ly > 0 ? s_val[e - T] : h_val[1][x + T * lz];
+            const float pz = lz > 0 ? s_val[e - T * T] : h_val[2][x + T * ly];
+            const int cx = x > 0 ? s_code[e - 1] : h_code[0][ly + T * lz];
+            const int cy = ly > 0 ? s_code[e - T] : h_code[1][x + T * lz];
+            const int cz = lz > 0 ? s_code[e - T * T] : h_code[2][x + T * ly];
+            const float A0 = s_P[e];
+            float ev = A0;
+            if (c & kLowX) ev = ev - px * px;
+            if (c & kLowY) ev = ev - py * py;
+            if (c & kLowZ) ev = ev - pz * pz;
+            // Ai(c-x)*(Aj(c-x)+Ak(c-x)) etc. are 0, 1 or 2
+            const float k1 = (c & kLowX) ? (float)(((cx & kHighY) ? 1 : 0) + ((cx & kHighZ) ? 1 : 0)) : 0.f;
+            const float k2 = (c & kLowY) ? (float)(((cy & kHighX) ? 1 : 0) + ((cy & kHighZ) ? 1 : 0)) : 0.f;
+            const float k3 = (c & kLowZ) ? (float)(((cz & kHighX) ? 1 : 0) + ((cz & kHighY) ? 1 : 0)) : 0.f;
+            const float t1 = k1 * (px * px), t2 = k2 * (py * py), t3 = k3 * (pz * pz);
+            const float S = (t1 + t2) + t3;
+            ev = fmaf(-0.97f, S, ev);       // e -= tau*(...) in double, one rounding
+            if (ev < 0.25f * A0) ev = A0;   // stability cutoff sigma = 0.25
+            pv = 1.f / sqrtf(ev);
+          }
+          s_val[e] = pv;
+        } else if (MODE == 1) {
+          float zv = 0.f;
+          if (c & kCodeFluid) {
+            float t = s_val[e];
+            if (c & kLowX) t = t + (x > 0 ? s_val[e - 1] * s_P[e - 1] : h_val[0][ly + T * lz] * h_P[0][ly + T * lz]);
+            if (c & kLowY) t = t + (ly > 0 ? s_val[e - T] * s_P[e - T] : h_val[1][x + T * lz] * h_P[1][x + T * lz]);
+            if (c & kLowZ) t = t + (lz > 0 ? s_val[e - T * T] * s_P[e - T * T] : h_val[2][x + T * ly] * h_P[2][x + T * ly]);
+            zv = s_P[e] * t;
+          }
+          s_val[e] = zv;
+        } else {
+          float zv = 0.f;
+          if (c & kCodeFluid) {
+            const float p = s_P[e];
+            float t = s_val[e];
+            if (c & kHighX) t = t + (x < T - 1 ? s_val[e + 1] : h_val[0][ly + T * lz]) * p;
+            if (c & kHighY) t = t + (ly < T - 1 ? s_val[e + T] : h_val[1][x + T * lz]) * p;
+            if (c & kHighZ) t = t + (lz < T - 1 ? s_val[e + T * T] : h_val[2][x + T * ly]) * p;
+            zv = p * t;
+          }
+          s_val[e] = zv;
+        }
+      }
+      __syncthreads();
+    }
+    // write back, and the fused dot(z, residual) for the backward sweep
+    for (int e = tid; e < TC; e += kThreads) {
+      const int x = x0 + (e & (T - 1)), y = y0 + ((e >> 4) & (T - 1)), zc = z0 + (e >> 8);
+      if (x < d.nx && y < d.ny && zc < d.nz) {
+        const long long g = ix(d, x, y, zc);
+        if (MODE == 0) {
+          a.P[g] = s_val[e];
+        } else {
+          a.z[g] = s_val[e];
+          if (MODE == 2) acc += (double)(s_val[e] * a.r[g]);
+        }
+      }
+    }
+    if (MODE == 2) {
+      const double b = block_sum(acc);
+      if (tid == 0) a.part[tile] = b;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      st_release(a.tileDone + tile, a.epoch);
+    }
+  }
+}
+
+// sigmaNew = sum of per-tile partials in tile order; beta; divergence check
+__global__ void k_mic_finish_dot(const double* part, int ntiles, CgScalars* sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (sc->done) return;
+  double s = 0.;
+  for (int q = 0; q < ntiles; q++) s += part[q];
+  const float sigmaNew = (float)s;
+  sc->beta = sigmaNew / sc->sigma;
+  sc->sigma = sigmaNew;
+  if (!(sc->resNorm < 1e35f)) { sc->status = 2; sc->done = 1; }
+}
+
+// sigma for doInit after the first MIC application
+__global__ void k_mic_init_sigma(const double* part, int ntiles, CgScalars* sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.;
+  for (int q = 0; q < ntiles; q++) s += part[q];
+  sc->sigma = (float)s;
+}
+
+// ------------------------------------------------------- correctVelocity
+// knCorrectVelocity (pressure.cpp:87-109)
+__global__ void k_correct_velocity(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ p) {
+  CELL_IJK
+  if (!INNER) return;
+  const long long X = 1, Y = d.sy, Z = d.sz;
+  if (isF(flags, idx)) {
+    float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
+    const float pc = p[idx];
+    if (isF(flags, idx - X)) u -= (pc - p[idx - X]);
+    if (isF(flags, idx - Y)) v -= (pc - p[idx - Y]);
+    if (d.is3d && isF(flags, idx - Z)) w -= (pc - p[idx - Z]);
+    if (isE(flags, idx - X)) u -= pc;
+    if (isE(flags, idx - Y)) v -= pc;
+    if (d.is3d && isE(flags, idx - Z)) w -= pc;
+    vel.u[idx] = u; vel.v[idx] = v; vel.w[idx] = w;
+  } else if (isE(flags, idx) && !isOut(flags, idx)) {
+    float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
+    if (isF(flags, idx - X)) u += p[idx - X]; else u = 0.f;
+    if (isF(flags, idx - Y)) v += p[idx - Y]; else v = 0.f;
+    if (d.is3d) { if (isF(flags, idx - Z)) w += p[idx - Z]; else w = 0.f; }
+    vel.u[idx] = u; vel.v[idx] = v; vel.w[idx] = w;
+  }
+}
+
+// knCorrectVelocityGhostFluid (pressure.cpp:154-187)
+__global__ void k_correct_velocity_gf(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ p,
+                                      const float* __restrict__ phi, float gfc, const float* __restrict__ curv, float st) {
+  CELL_IJK
+  if (!INNER) return;
+  const long long X = 1, Y = d.sy, Z = d.sz;
+  float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
+  if (isF(flags, idx)) {
+    if (isE(flags, idx - X)) u += p[idx] * gf_helper(phi, idx, -X, gfc);
+    if (isE(flags, idx - Y)) v += p[idx] * gf_helper(phi, idx, -Y, gfc);
+    if (d.is3d && isE(flags, idx - Z)) w += p[idx] * gf_helper(phi, idx, -Z, gfc);
+  } else if (isE(flags, idx) && !isOut(flags, idx)) {
+    if (isF(flags, idx - X)) u -= p[idx - X] * gf_helper(phi, idx - X, +X, gfc); else u = 0.f;
+    if (isF(flags, idx - Y)) v -= p[idx - Y] * gf_helper(phi, idx - Y, +Y, gfc); else v = 0.f;
+    if (d.is3d) { if (isF(flags, idx - Z)) w -= p[idx - Z] * gf_helper(phi, idx - Z, +Z, gfc); else w = 0.f; }
+  }
+  if (curv) {
+    if (isF(flags, idx)) {
+      if (isE(flags, idx - X)) u += surf_tens_helper(phi, curv, idx, -X, st, gfc);
+      if (isE(flags, idx - Y)) v += surf_tens_helper(phi, curv, idx, -Y, st, gfc);
+      if (d.is3d && isE(flags, idx - Z)) w += surf_tens_helper(phi, curv, idx, -Z, st, gfc);
+    } else if (isE(flags, idx) && !isOut(flags, idx)) {
+      u -= isF(flags, idx - X) ? surf_tens_helper(phi, curv, idx - X, +X, st, gfc) : 0.f;
+      v -= isF(flags, idx - Y) ? surf_tens_helper(phi, curv, idx - Y, +Y, st, gfc) : 0.f;
+      if (d.is3d) w -= isF(flags, idx - Z) ? surf_tens_helper(phi, curv, idx - Z, +Z, st, gfc) : 0.f;
+    }
+  }
+  vel.u[idx] = u; vel.v[idx] = v; vel.w[idx] = w;
+}
+
+// knReplaceClampedGhostFluidVels (pressure.cpp:198-214): writes only empty
+// cells and reads only fluid ones, so it is race free in place.
+__global__ void k_replace_clamped_gf(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ phi, float gfc) {
+  CELL_IJK
+  if (!INNER) return;
+  if (!isE(flags, idx)) return;
+  const long long X = 1, Y = d.sy, Z = d.sz;
+#define CLAMPED(e, off) (theta_helper(phi[(e)], phi[(e) + (off)]) < gfc)
+  if (isF(flags, idx - X) && CLAMPED(idx - X, +X)) vel.u[idx] = vel.u[idx - X];
+  if (isF(flags, idx - Y) && CLAMPED(idx - Y, +Y)) vel.v[idx] = vel.v[idx - Y];
+  if (d.is3d && isF(flags, idx - Z) && CLAMPED(idx - Z, +Z)) vel.w[idx] = vel.w[idx - Z];
+  if (isF(flags, idx + X) && CLAMPED(idx + X, -X)) vel.u[idx] = vel.u[idx + X];
+  if (isF(flags, idx + Y) && CLAMPED(idx + Y, -Y)) vel.v[idx] = vel.v[idx + Y];
+  if (d.is3d && isF(flags, idx + Z) && CLAMPED(idx + Z, -Z)) vel.w[idx] = vel.w[idx + Z];
+#undef CLAMPED
+}
+
+// ------------------------------------------------------------- launchers
+void launch_make_rhs(const PcgBuffers& b, const float* vu, const float* vv, const float* vw, const float* perCellCorr,
+                     const float* phi, const float* curv, float surfTens, float gfClamp, cudaStream_t s) {
+  const dim3 g = grid3(b.d, kBlk);
+  count_launch();
+  k_make_rhs<<<g, kBlk, 0, s>>>(b.d, b.flags, b.rhs, vu, vv, vw, perCellCorr, phi, curv, surfTens, gfClamp, b.part, b.sc,
+                                g.x * g.y * g.z);
+}
+void launch_compat_shift(const PcgBuffers& b, cudaStream_t s) {
+  const dim3 g = grid3(b.d, kBlk);
+  count_launch();
+  k_compat_reduce<<<1, 32, 0, s>>>(b.part, (int)(g.x * g.y * g.z), b.sc);
+  count_launch();
+  k_compat_shift<<<(unsigned)((b.d.n + 255) / 256), 256, 0, s>>>(b.d.n, b.rhs, b.sc);
+}
+void launch_make_codes(const PcgBuffers& b, cudaStream_t s) {
+  count_launch();
+  k_make_codes<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.flags, b.code);
+  count_launch();
+  k_make_codes_low<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.code);
+}
+void launch_ghost_fluid_diag(const PcgBuffers& b, const float* phi, float gfClamp, cudaStream_t s) {
+  count_launch();
+  k_ghost_fluid_diag<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.flags, b.code, phi, gfClamp, b.A0f);
+}
+void launch_count_empty(const PcgBuffers& b, int* out, cudaStream_t s) {
+  cudaMemsetAsync(out, 0, sizeof(int), s);
+  count_launch();
+  k_count_empty<<<304, 256, 0, s>>>(b.d.n, b.flags, out);
+}
+void launch_fix_pressure(const PcgBuffers& b, long long fix, cudaStream_t s) {
+  count_launch();
+  k_fix_pressure<<<1, 32, 0, s>>>(b.d, fix, b.code, b.A0f, b.rhs);
+}
+void launch_pcg_init(const PcgBuffers& b, cudaStream_t s) {
+  count_launch();
+  k_pcg_init<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.pressure, b.rhs, b.residual, b.tmp);
+}
+void launch_pcg_set_search(const PcgBuffers& b, cudaStream_t s) {
+  count_launch();
+  k_pcg_set_search<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.tmp, b.residual, b.search, b.part, b.sc);
+}
+void launch_pcg_spmv(const PcgBuffers& b, cudaStream_t s) {
+  count_launch();
+  k_pcg_spmv<<<b.nblocks, kThreads, 0, s>>>(b.d, b.code, b.A0f, b.search, b.tmp, b.part, b.sc);
+}
+void launch_pcg_axpy(const PcgBuffers& b, cudaStream_t s) {
+  count_launch();
+  k_pcg_axpy<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.pressure, b.search, b.residual, b.tmp, b.part, b.partf, b.sc);
+}
+void launch_pcg_copy_dot(const PcgBuffers& b, cudaStream_t s) {
+  count_launch();
+  k_pcg_copy_dot<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.residual, b.tmp, b.part, b.sc);
+}
+void launch_pcg_update(const PcgBuffers& b, cudaStream_t s) {
+  count_launch();
+  k_pcg_update<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.tmp, b.search, b.sc);
+}
+
+// mode: 0 init P, 1 forward, 2 backward (+dot, beta), 3 backward for doInit (+sigma)
+void launch_mic(const PcgBuffers& b, const MicPlan& m, int mode, unsigned int epoch, long long spinLimit, cudaStream_t s) {
+  MicArgs a;
+  a.d = b.d;
+  a.code = b.code;
+  a.A0f = b.A0f;
+  a.P = b.P;
+  a.r = b.residual;
+  a.z = b.tmp;
+  a.part = b.part;
+  a.sc = b.sc;
+  a.tx = m.tx; a.ty = m.ty; a.tz = m.tz; a.ntiles = m.ntiles;
+  a.order = m.order;
+  a.tileDone = m.tileDone;
+  a.counter = m.counter;
+  a.error = m.error;
+  a.epoch = epoch;
+  a.spinLimit = spinLimit;
+  cudaMemsetAsync(m.counter, 0, sizeof(int), s);
+  const int ctas = m.ctas < m.ntiles ? m.ctas : m.ntiles;
+  if (mode == 0) { count_launch(); k_mic<0><<<ctas, kThreads, 0, s>>>(a); }
+  else if (mode == 1) { count_launch(); k_mic<1><<<ctas, kThreads, 0, s>>>(a); }
+  else {
+    count_launch();
+    k_mic<2><<<ctas, kThreads, 0, s>>>(a);
+    if (mode == 2) { count_launch(); k_mic_finish_dot<<<1, 32, 0, s>>>(b.part, m.ntiles, b.sc); }
+    else { count_launch(); k_mic_init_sigma<<<1, 32, 0, s>>>(b.part, m.ntiles, b.sc); }
+  }
+}
+
+// forward dispatch order: tiles sorted by wavefront level a+b+c
+void mic_plan_order(int tx, int ty, int tz, int* order) {
+  int n = 0;
+  for (int L = 0; L <= tx + ty + tz - 3; L++)
+    for (int c = 0; c < tz; c++)
+      for (int b = 0; b < ty; b++) {
+        const int a = L - b - c;
+        if (a >= 0 && a < tx) order[n++] = a + tx * (b + ty * c);
+      }
+}
+
+int mic_ctas_per_sm() {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_mic<1>, kThreads, 0);
+  return nb > 0 ? nb : 1;
+}
+
+void launch_correct_velocity(const Dims& d, const int* flags, Mac vel, const float* p, const float* phi, const float* curv,
+                             float gfClamp, float surfTens, cudaStream_t s) {
+  count_launch();
+  k_correct_velocity<<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, p);
+  if (phi) {
+    count_launch();
+    k_correct_velocity_gf<<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, p, phi, gfClamp, curv, surfTens);
+    count_launch();
+    k_replace_clamped_gf<<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, phi, gfClamp);
+  }
+}
+
+}  // namespace mgpu

@@ -1,0 +1,264 @@
+"""GPU parity: libmantagpu (through its C ABI, via the scene-script API) against
+the reference's golden outputs and the CPU oracle on the same seeded inputs.
+
+Tolerances
+ * advection, forces, boundary conditions, extrapolation, setup: the kernels
+   repeat the reference's float operations, so results are expected bit for
+   bit.  The test allows 1e-6 relative (the benchmark spec's bound is 1e-5) and
+   requires at least 99.9% of cells to be bit-identical: where the reference
+   forms a float expression in double and rounds twice, the GPU rounds once
+   (fmaf), which can differ by one ulp in rare ties.
+ * pressure: the CG's double-precision dot products are summed in a
+   different order than the serial reference, so iterates drift at round-off
+   level.  Pressure must match within the reference's own float threshold
+   (1e-4, tools/tests/test_0100_psolve.py), the iteration count within +-1,
+   and the divergence left after projection must be no worse than the
+   reference's at the same cgAccuracy.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as og
+from tests.conftest import golden_path
+
+pytestmark = pytest.mark.gpu
+
+m = pytest.importorskip("mantaflow_gb300")
+
+
+def load(name):
+    return np.load(golden_path(name), allow_pickle=False)
+
+
+def close_bitwise(got, want, what, rel=1e-6, min_exact=0.999):
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    assert got.shape == want.shape, what
+    exact = np.mean(got == want)
+    diff = np.abs(got - want)
+    bound = rel * np.maximum(1.0, np.abs(want))
+    worst = float(np.max(diff - bound))
+    assert worst <= 0.0, "%s: max diff %g beyond %g relative" % (what, float(diff.max()), rel)
+    assert exact >= min_exact, "%s: only %.5f of cells bit-identical" % (what, exact)
+
+
+def make_solver(shape, dt=1.0):
+    nz, ny, nx = shape[:3]
+    dim = 3 if nz > 1 else 2
+    s = m.Solver(name="t", gridSize=m.vec3(nx, ny, nz), dim=dim)
+    s.timestep = dt
+    return s
+
+
+def grid_from(s, cls, arr):
+    g = s.create(cls)
+    m.copyArrayToGridReal(arr, g)
+    return g
+
+
+@pytest.mark.parametrize("tag", ["3d", "2d"])
+def test_advection(tag):
+    g = load("advect_" + tag)
+    flags_a, vel_a, dens_a, vec_a, dt = g["flags"], g["vel"], g["dens"], g["vec3"], float(g["dt"])
+    s = make_solver(flags_a.shape, dt)
+    flags = grid_from(s, m.FlagGrid, flags_a)
+    for name_kind, meta in zip(g["names"], g["meta"]):
+        name, kind = str(name_kind).split(":")
+        order, clamp, ospace, otrace, strength = meta
+        vel = grid_from(s, m.MACGrid, vel_a)
+        if kind == "mac" and int(ospace) != 1:
+            continue
+        if kind == "real":
+            tgt = grid_from(s, m.RealGrid, dens_a)
+        elif kind == "vec3":
+            tgt = grid_from(s, m.VecGrid, vec_a)
+        else:
+            tgt = vel
+        m.advectSemiLagrange(flags=flags, vel=vel, grid=tgt, order=int(order), strength=float(strength),
+                             orderSpace=int(ospace), clampMode=int(clamp), orderTrace=int(otrace))
+        close_bitwise(tgt.numpy(), g[name], "advect %s %s" % (tag, name))
+
+
+@pytest.mark.parametrize("tag", ["3d", "2d"])
+def test_forces_and_walls(tag):
+    g = load("forces_" + tag)
+    s = make_solver(g["flags"].shape, float(g["dt"]))
+    flags = grid_from(s, m.FlagGrid, g["flags"])
+    dens = grid_from(s, m.RealGrid, g["dens"])
+    obv = grid_from(s, m.MACGrid, g["obvel"])
+
+    def fresh():
+        return grid_from(s, m.MACGrid, g["vel"])
+
+    v = fresh(); m.setWallBcs(flags=flags, vel=v); close_bitwise(v.numpy(), g["wall"], "setWallBcs")
+    v = fresh(); m.setWallBcs(flags=flags, vel=v, obvel=obv); close_bitwise(v.numpy(), g["wall_obvel"], "obvel")
+    v = fresh(); m.addBuoyancy(flags=flags, density=dens, vel=v, gravity=m.vec3(0, -4e-3, 0))
+    close_bitwise(v.numpy(), g["buoy"], "addBuoyancy")
+    v = fresh(); m.addBuoyancy(flags=flags, density=dens, vel=v, gravity=m.vec3(1e-3, -6e-3, 2e-3), coefficient=0.7,
+                               scale=False)
+    close_bitwise(v.numpy(), g["buoy_noscale"], "addBuoyancy noscale")
+    v = fresh(); m.addGravity(flags=flags, vel=v, gravity=m.vec3(0, -1e-3, 0))
+    close_bitwise(v.numpy(), g["grav"], "addGravity")
+    v = fresh(); m.addGravity(flags=flags, vel=v, gravity=m.vec3(2e-3, -1e-3, 5e-4), scale=False)
+    close_bitwise(v.numpy(), g["grav_noscale"], "addGravity noscale")
+
+
+@pytest.mark.parametrize("tag", ["3d", "2d"])
+def test_extrapolate_mac_simple(tag):
+    g = load("extrap_" + tag)
+    s = make_solver(g["flags"].shape)
+    flags = grid_from(s, m.FlagGrid, g["flags"])
+    v = grid_from(s, m.MACGrid, g["vel"])
+    m.extrapolateMACSimple(flags=flags, vel=v, distance=4)
+    close_bitwise(v.numpy(), g["ext4"], "extrap 4")
+    v = grid_from(s, m.MACGrid, g["vel"])
+    m.extrapolateMACSimple(flags=flags, vel=v, distance=2, intoObs=True)
+    close_bitwise(v.numpy(), g["ext2_obs"], "extrap 2 intoObs")
+
+
+def test_setup():
+    g = load("setup_3d")
+    nx, ny, nz = [int(x) for x in g["size"]]
+    s = m.Solver(name="setup", gridSize=m.vec3(nx, ny, nz), dim=3)
+    gs = m.vec3(nx, ny, nz)
+    flags = s.create(m.FlagGrid)
+    flags.initDomain(boundaryWidth=0)
+    assert np.array_equal(flags.numpy(), g["flags_init"])
+    flags.fillGrid()
+    assert np.array_equal(flags.numpy(), g["flags_fill"])
+    m.setOpenBound(flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
+    assert np.array_equal(flags.numpy(), g["flags_open"])
+    flags.initDomain(boundaryWidth=1, wall="xXyY", outflow="zZ")
+    assert np.array_equal(flags.numpy(), g["flags_init_bw1"])
+    mask = s.create(m.RealGrid)
+    src = s.create(m.Cylinder, center=gs * m.vec3(0.5, 0.1, 0.5), radius=nx * 0.14, z=gs * m.vec3(0, 0.02, 0))
+    src.applyToGrid(grid=mask, value=1.0)
+    assert np.array_equal(mask.numpy(), g["cyl_mask"])
+    box = s.create(m.Box, p0=m.vec3(0, 0, 0), p1=m.vec3(nx * 0.4, ny * 0.6, nz))
+    phi = box.computeLevelset()
+    close_bitwise(phi.numpy(), g["box_phi"], "box sdf")
+    flags.initDomain(boundaryWidth=0)
+    flags.updateFromLevelset(phi)
+    assert np.array_equal(flags.numpy(), g["flags_lvl"])
+
+
+def divergence(flags, vel):
+    """max |MakeRhs| over fluid cells, computed by the oracle on the CPU"""
+    rhs = np.zeros(flags.shape, np.float32)
+    og.compute_pressure_rhs(rhs, vel.astype(np.float32).copy(), flags)
+    fl = (flags & og.FLUID) != 0
+    return float(np.max(np.abs(rhs[fl]))) if fl.any() else 0.0
+
+
+PRESSURE_CASES = {
+    "mic": dict(preconditioner=1),
+    "mic_acc1e5": dict(preconditioner=1, cgAccuracy=1e-5),
+    "mic_l2": dict(preconditioner=1, useL2Norm=True, cgAccuracy=1e-6),
+    "mic_compat": dict(preconditioner=1, enforceCompatibility=True),
+    "mic_closed_fix": dict(preconditioner=1, zeroPressureFixing=True, cgAccuracy=1e-4),
+    "gf_mic": dict(preconditioner=1),
+}
+
+
+@pytest.mark.parametrize("tag", ["3d", "2d"])
+@pytest.mark.parametrize("case", sorted(PRESSURE_CASES))
+def test_solve_pressure(tag, case):
+    g = load("pressure_" + tag)
+    names = [str(n) for n in g["names"]]
+    if case not in names:
+        pytest.skip("no golden for %s %s" % (tag, case))
+    idx = names.index(case)
+    if case.startswith("gf_"):
+        flags_a, phi_a = g["flags_liquid"], g["phi"]
+    else:
+        flags_a, phi_a = (g["flags_closed"] if "closed" in case else g["flags_smoke"]), None
+    s = make_solver(flags_a.shape)
+    flags = grid_from(s, m.FlagGrid, flags_a)
+    vel = grid_from(s, m.MACGrid, g["vel"])
+    p = s.create(m.RealGrid)
+    rhs = s.create(m.RealGrid)
+    phi = grid_from(s, m.LevelsetGrid, phi_a) if phi_a is not None else None
+    m.solvePressure(flags=flags, vel=vel, pressure=p, phi=phi, retRhs=rhs, **PRESSURE_CASES[case])
+    it, res = m.lastSolveStats()
+    ref_it = int(g["iters"][idx])
+    assert abs(it - ref_it) <= 1, "%s %s: %d iterations vs reference %d" % (tag, case, it, ref_it)
+    close_bitwise(rhs.numpy(), g["rhs_" + case], "rhs %s" % case)
+    pg = p.numpy()
+    assert np.max(np.abs(pg - g["p_" + case])) <= 1e-4, "%s pressure off by %g" % (
+        case, np.max(np.abs(pg - g["p_" + case])))
+    vg = vel.numpy()
+    assert np.max(np.abs(vg - g["v_" + case])) <= 1e-4
+    acc = PRESSURE_CASES[case].get("cgAccuracy", 1e-3)
+    d_gpu = divergence(flags_a, vg)
+    d_ref = divergence(flags_a, g["v_" + case])
+    assert d_gpu <= max(1.05 * d_ref, acc), "divergence %g vs reference %g" % (d_gpu, d_ref)
+
+
+def test_pcnone_rejected_like_reference():
+    g = load("pressure_3d")
+    s = make_solver(g["flags_smoke"].shape)
+    flags = grid_from(s, m.FlagGrid, g["flags_smoke"])
+    vel = grid_from(s, m.MACGrid, g["vel"])
+    p = s.create(m.RealGrid)
+    with pytest.raises(m.MantaError) as e:
+        m.solvePressure(flags=flags, vel=vel, pressure=p, preconditioner=m.PcNone)
+    assert str(g["none_error"]).startswith(str(e.value).split("\n")[0][:40])
+
+
+def test_plume_steps_against_reference():
+    """8 full plume steps (24^3, MacCormack + MIC) against the reference
+    executable's per-step outputs; thresholds of tools/tests/test_2010."""
+    g = load("plume_mic24")
+    n = g["flags"].shape[0]
+    s = m.Solver(name="plume", gridSize=m.vec3(n, n, n), dim=3)
+    s.timestep = 1.0
+    flags = s.create(m.FlagGrid)
+    flags.initDomain(boundaryWidth=0)
+    flags.fillGrid()
+    m.setOpenBound(flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
+    assert np.array_equal(flags.numpy(), g["flags"])
+    vel = s.create(m.MACGrid)
+    dens = s.create(m.RealGrid)
+    pres = s.create(m.RealGrid)
+    noise = s.create(m.RealGrid)
+    mask = g["mask"]
+    rng = np.random.default_rng(int(g["seed"]))
+    for t in range(len(g["iters"])):
+        a = (rng.random((n, n, n), dtype=np.float32) * mask).astype(np.float32)
+        m.copyArrayToGridReal(a, noise)
+        dens.join(noise)
+        m.advectSemiLagrange(flags=flags, vel=vel, grid=dens, order=2, clampMode=2)
+        m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=2, clampMode=2)
+        m.setWallBcs(flags=flags, vel=vel)
+        m.addBuoyancy(density=dens, vel=vel, gravity=m.vec3(0, -4e-3, 0), flags=flags)
+        m.solvePressure(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, preconditioner=m.PcMIC)
+        it, _ = m.lastSolveStats()
+        assert abs(it - int(g["iters"][t])) <= 1
+        assert np.max(np.abs(dens.numpy() - g["density"][t])) <= 1e-3
+        assert np.max(np.abs(vel.numpy() - g["vel"][t])) <= 5e-3
+        s.step()
+
+
+def test_mic_large_against_oracle():
+    """MIC-PCG on a 70x66x62 grid (several 16^3 tiles per axis, ragged edge
+    tiles): pressure and iterations against the oracle."""
+    rng = np.random.default_rng(7)
+    nx, ny, nz = 70, 66, 62
+    f = np.full((nz, ny, nx), og.FLUID, np.int32)
+    og.init_domain(f, 0)
+    og.fill_grid(f)
+    og.set_open_bound(f, 0, "Y")
+    f[20:40, 10:30, 25:45] = og.OBSTACLE
+    v = (rng.random((nz, ny, nx, 3), dtype=np.float32) - 0.5).astype(np.float32)
+    pv = np.zeros((nz, ny, nx), np.float32)
+    vo = v.copy()
+    it_ref, _, _ = og.solve_pressure(f, vo, pv, preconditioner=og.PC_MIC, cgAccuracy=1e-4)
+    s = m.Solver(name="big", gridSize=m.vec3(nx, ny, nz), dim=3)
+    flags = grid_from(s, m.FlagGrid, f)
+    vel = grid_from(s, m.MACGrid, v)
+    p = s.create(m.RealGrid)
+    m.solvePressure(flags=flags, vel=vel, pressure=p, preconditioner=m.PcMIC, cgAccuracy=1e-4)
+    it, _ = m.lastSolveStats()
+    assert abs(it - it_ref) <= 1, (it, it_ref)
+    assert np.max(np.abs(p.numpy() - pv)) <= 1e-4
+    assert divergence(f, vel.numpy()) <= max(1.05 * divergence(f, vo), 1e-4)
