@@ -109,6 +109,23 @@ void launch_pcg_axpy(const PcgBuffers& b, cudaStream_t s);
 void launch_pcg_copy_dot(const PcgBuffers& b, cudaStream_t s);   // PcNone: tmp = residual, sigmaNew
 void launch_pcg_update(const PcgBuffers& b, cudaStream_t s);
 void launch_mic(const PcgBuffers& b, const MicPlan& m, int mode, unsigned int epoch, long long spinLimit, cudaStream_t s);
+// column-block MIC sweeps (mic.cu), for grids with nx % 8 == 0
+struct MicColPlan {
+  int nby, nbz, nblocks;
+  int* order;                 // block dispatch order ((b + c) levels)
+  unsigned long long* prog;   // per-block progress, epoch in the high word
+  int* counter;
+  int* error;
+};
+bool mic_col_supported(const Dims& d);
+void mic_col_geometry(const Dims& d, int* nby, int* nbz);
+void mic_col_order(int nby, int nbz, int* order);
+int mic_col_prepare();
+void launch_mic_col(const PcgBuffers& b, const MicColPlan& m, int mode, unsigned int epoch, long long spinLimit,
+                    int ctas, cudaStream_t s);
+// sum of nparts per-block dot partials -> beta/sigma (init: sigma only)
+void launch_mic_finish(const PcgBuffers& b, int nparts, bool init, cudaStream_t s);
+
 void launch_correct_velocity(const Dims& d, const int* flags, Mac vel, const float* p, const float* phi, const float* curv,
                              float gfClamp, float surfTens, cudaStream_t s);
 void mic_plan_order(int tx, int ty, int tz, int* order);

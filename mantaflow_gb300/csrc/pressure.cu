@@ -77,7 +77,27 @@ __device__ __forceinline__ void block_minmax(float& mn, float& mx) {
     for (int q = 1; q < nwarps(); q++) { mn = fminf(mn, s0[q]); mx = fmaxf(mx, s1[q]); }
 }
 
-// "last block" ticket: returns true in thread 0 of the block that finishes last
+// all threads of a block: sum of part[0..n) in a fixed order (strided
+// per-thread sums, then a fixed tree); the result is valid in thread 0.
+// The partials come from other blocks, so they are read from L2.
+__device__ __forceinline__ double sum_partials(const double* part, int n) {
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  double v = 0.;
+  for (int q = lin_tid(); q < n; q += nt) v += __ldcg(part + q);
+  return block_sum(v);
+}
+__device__ __forceinline__ void minmax_partials(const float* part, int n, float& mn, float& mx) {
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  mn = FLT_MAX;
+  mx = -FLT_MAX;
+  for (int q = lin_tid(); q < n; q += nt) {
+    mn = fminf(mn, __ldcg(part + 2 * q));
+    mx = fmaxf(mx, __ldcg(part + 2 * q + 1));
+  }
+  block_minmax(mn, mx);
+}
+
+// "last block" ticket: true in every thread of the block that finishes last
 __device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int total) {
   __shared__ bool last;
   __syncthreads();
@@ -168,11 +188,15 @@ __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict_
 
 // rhs += (Real)(-sum / (Real)cnt) on every cell (pressure.cpp:296-297)
 __global__ void k_compat_reduce(const double* part, int nb, CgScalars* sc) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int nt = blockDim.x;
   double s = 0., c = 0.;
-  for (int q = 0; q < nb; q++) { s += part[2 * q]; c += part[2 * q + 1]; }
-  sc->sum = s;
-  sc->cnt = (int)c;
+  for (int q = threadIdx.x; q < nb; q += nt) { s += __ldcg(part + 2 * q); c += __ldcg(part + 2 * q + 1); }
+  s = block_sum(s);
+  c = block_sum(c);
+  if (threadIdx.x == 0) {
+    sc->sum = s;
+    sc->cnt = (int)c;
+  }
 }
 __global__ void k_compat_shift(long long n, float* rhs, const CgScalars* sc) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -287,9 +311,8 @@ __global__ void __launch_bounds__(256) k_pcg_set_search(long long n, const float
   const double b = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = b;
   if (last_block(&sc->counters[0], gridDim.x)) {
-    double s = 0.;
-    for (unsigned q = 0; q < gridDim.x; q++) s += part[q];
-    sc->sigma = (float)s;
+    const double s = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) sc->sigma = (float)s;
   }
 }
 
@@ -320,13 +343,14 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(Dims d, const code_t* __restri
   const double b = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = b;
   if (last_block(&sc->counters[1], gridDim.x)) {
-    double s = 0.;
-    for (unsigned q = 0; q < gridDim.x; q++) s += part[q];
-    const float dp = (float)s;
-    sc->dp = dp;
-    float alpha = 0.f;
-    if (fabsf(dp) > 0.f) alpha = sc->sigma / dp;
-    sc->alpha = alpha;
+    const double s = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      const float dp = (float)s;
+      sc->dp = dp;
+      float alpha = 0.f;
+      if (fabsf(dp) > 0.f) alpha = sc->sigma / dp;
+      sc->alpha = alpha;
+    }
   }
 }
 
@@ -356,20 +380,17 @@ __global__ void __launch_bounds__(256) k_pcg_axpy(long long n, float* p, const f
     part[blockIdx.x] = bs;
   }
   if (last_block(&sc->counters[2], gridDim.x)) {
-    float res;
+    float res = 0.f;
     if (l2) {
-      double a = 0.;
-      for (unsigned q = 0; q < gridDim.x; q++) a += part[q];
+      const double a = sum_partials(part, gridDim.x);
       res = (float)a;
     } else {
-      float amin = FLT_MAX, amax = -FLT_MAX;
-      for (unsigned q = 0; q < gridDim.x; q++) {
-        amin = fminf(amin, partf[2 * q]);
-        amax = fmaxf(amax, partf[2 * q + 1]);
-      }
+      float amin, amax;
+      minmax_partials(partf, gridDim.x, amin, amax);
       const float x = fabsf(amin), y = fabsf(amax);
       res = x < y ? y : x;
     }
+    if (threadIdx.x != 0) return;
     sc->iterations += 1;
     sc->resNorm = res;
     if (res < sc->accuracy) {
@@ -392,8 +413,8 @@ __global__ void __launch_bounds__(256) k_pcg_copy_dot(long long n, const float* 
   const double b = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = b;
   if (last_block(&sc->counters[3], gridDim.x)) {
-    double s = 0.;
-    for (unsigned q = 0; q < gridDim.x; q++) s += part[q];
+    const double s = sum_partials(part, gridDim.x);
+    if (threadIdx.x != 0) return;
     const float sigmaNew = (float)s;
     sc->beta = sigmaNew / sc->sigma;
     sc->sigma = sigmaNew;
@@ -624,10 +645,9 @@ __global__ void __launch_bounds__(256) k_mic(MicArgs a) {
 
 // sigmaNew = sum of per-tile partials in tile order; beta; divergence check
 __global__ void k_mic_finish_dot(const double* part, int ntiles, CgScalars* sc) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (sc->done) return;
-  double s = 0.;
-  for (int q = 0; q < ntiles; q++) s += part[q];
+  const double s = sum_partials(part, ntiles);
+  if (threadIdx.x != 0) return;
   const float sigmaNew = (float)s;
   sc->beta = sigmaNew / sc->sigma;
   sc->sigma = sigmaNew;
@@ -636,10 +656,8 @@ __global__ void k_mic_finish_dot(const double* part, int ntiles, CgScalars* sc) 
 
 // sigma for doInit after the first MIC application
 __global__ void k_mic_init_sigma(const double* part, int ntiles, CgScalars* sc) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double s = 0.;
-  for (int q = 0; q < ntiles; q++) s += part[q];
-  sc->sigma = (float)s;
+  const double s = sum_partials(part, ntiles);
+  if (threadIdx.x == 0) sc->sigma = (float)s;
 }
 
 // ------------------------------------------------------- correctVelocity
@@ -725,7 +743,7 @@ void launch_make_rhs(const PcgBuffers& b, const float* vu, const float* vv, cons
 void launch_compat_shift(const PcgBuffers& b, cudaStream_t s) {
   const dim3 g = grid3(b.d, kBlk);
   count_launch();
-  k_compat_reduce<<<1, 32, 0, s>>>(b.part, (int)(g.x * g.y * g.z), b.sc);
+  k_compat_reduce<<<1, 256, 0, s>>>(b.part, (int)(g.x * g.y * g.z), b.sc);
   count_launch();
   k_compat_shift<<<(unsigned)((b.d.n + 255) / 256), 256, 0, s>>>(b.d.n, b.rhs, b.sc);
 }
@@ -798,9 +816,14 @@ void launch_mic(const PcgBuffers& b, const MicPlan& m, int mode, unsigned int ep
   else {
     count_launch();
     k_mic<2><<<ctas, kThreads, 0, s>>>(a);
-    if (mode == 2) { count_launch(); k_mic_finish_dot<<<1, 32, 0, s>>>(b.part, m.ntiles, b.sc); }
-    else { count_launch(); k_mic_init_sigma<<<1, 32, 0, s>>>(b.part, m.ntiles, b.sc); }
+    launch_mic_finish(b, m.ntiles, mode == 3, s);
   }
+}
+
+void launch_mic_finish(const PcgBuffers& b, int nparts, bool init, cudaStream_t s) {
+  count_launch();
+  if (init) k_mic_init_sigma<<<1, 256, 0, s>>>(b.part, nparts, b.sc);
+  else k_mic_finish_dot<<<1, 256, 0, s>>>(b.part, nparts, b.sc);
 }
 
 // forward dispatch order: tiles sorted by wavefront level a+b+c

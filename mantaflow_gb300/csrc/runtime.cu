@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -82,6 +83,8 @@ struct mg_solver_s {
   int nblocks = 0;
   size_t partCount = 0;
   MicPlan mic{};
+  MicColPlan micCol{};
+  bool useMicCol = false;
   unsigned int epoch = 0;
   mgpu::MgHierarchy* mg = nullptr;  // static multigrid cache (gMapMG)
   // profiling
@@ -224,6 +227,7 @@ extern "C" int mg_init(int device) {
   CK(cudaGetDeviceProperties(&prop, device));
   g_ctx.sms = prop.multiProcessorCount;
   g_ctx.micCtasPerSm = mic_ctas_per_sm();
+  if (mic_col_prepare()) return fail(MG_ERR_CUDA, "mg_init: cannot configure the MIC kernels");
   g_ctx.device = device;
   g_ctx.init = true;
   return MG_OK;
@@ -286,6 +290,8 @@ static void free_cg_state(mg_solver s) {
   s->code = nullptr; s->A0f = nullptr; s->residual = s->search = s->tmp = s->P = nullptr;
   s->part = nullptr; s->partf = nullptr; s->sc = nullptr; s->scHost = nullptr; s->intScratch = nullptr;
   s->mic = MicPlan{};
+  cudaFree(s->micCol.order); cudaFree(s->micCol.prog); cudaFree(s->micCol.counter); cudaFree(s->micCol.error);
+  s->micCol = MicColPlan{};
 }
 
 extern "C" int mg_solver_destroy(mg_solver s) {
@@ -726,6 +732,24 @@ static int ensure_cg_state(mg_solver s) {
     CK(cudaMalloc(&m.error, sizeof(int)));
     CK(cudaMemset(m.error, 0, sizeof(int)));
     m.ctas = g_ctx.sms * g_ctx.micCtasPerSm;
+    // column-block sweeps unless the grid's x size rules them out (or the
+    // tiled sweeps are requested for testing)
+    const char* ev = getenv("MANTA_GB300_MIC");
+    s->useMicCol = mic_col_supported(s->d) && !(ev && std::string(ev) == "tile");
+    if (s->useMicCol) {
+      MicColPlan& c = s->micCol;
+      mic_col_geometry(s->d, &c.nby, &c.nbz);
+      c.nblocks = c.nby * c.nbz;
+      std::vector<int> ord((size_t)c.nblocks);
+      mic_col_order(c.nby, c.nbz, ord.data());
+      CK(cudaMalloc(&c.order, ord.size() * sizeof(int)));
+      CK(cudaMemcpy(c.order, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice));
+      CK(cudaMalloc(&c.prog, ord.size() * sizeof(unsigned long long)));
+      CK(cudaMemset(c.prog, 0, ord.size() * sizeof(unsigned long long)));
+      CK(cudaMalloc(&c.counter, sizeof(int)));
+      c.error = m.error;
+      if ((size_t)c.nblocks > s->partCount) return fail(MG_ERR_STATE, "MIC: partial buffer too small");
+    }
   }
   return MG_OK;
 }
@@ -783,11 +807,13 @@ static int apply_precond(mg_solver s, const PcgBuffers& b, int pc, bool init) {
   if (pc == kPcMic) {
     {
       ProfScope ps(s, "mic_forward");
-      launch_mic(b, s->mic, 1, ++s->epoch, 1LL << 22, s->stream);
+      if (s->useMicCol) launch_mic_col(b, s->micCol, 1, ++s->epoch, 1LL << 22, g_ctx.sms, s->stream);
+      else launch_mic(b, s->mic, 1, ++s->epoch, 1LL << 22, s->stream);
     }
     {
       ProfScope ps(s, "mic_backward");
-      launch_mic(b, s->mic, init ? 3 : 2, ++s->epoch, 1LL << 22, s->stream);
+      if (s->useMicCol) launch_mic_col(b, s->micCol, init ? 3 : 2, ++s->epoch, 1LL << 22, g_ctx.sms, s->stream);
+      else launch_mic(b, s->mic, init ? 3 : 2, ++s->epoch, 1LL << 22, s->stream);
     }
   } else if (pc == kPcMg) {
     ProfScope ps(s, "mg_vcycle");
@@ -892,7 +918,8 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   if (pc == kPcMic) {
     ProfScope ps(s, "mic_init");
     CK(cudaMemsetAsync(s->mic.error, 0, sizeof(int), s->stream));
-    launch_mic(b, s->mic, 0, ++s->epoch, 1LL << 22, s->stream);
+    if (s->useMicCol) launch_mic_col(b, s->micCol, 0, ++s->epoch, 1LL << 22, g_ctx.sms, s->stream);
+    else launch_mic(b, s->mic, 0, ++s->epoch, 1LL << 22, s->stream);
     CKL();
   }
   if (pc != kPcNone) {

@@ -239,11 +239,16 @@ def test_plume_steps_against_reference():
         s.step()
 
 
-def test_mic_large_against_oracle():
-    """MIC-PCG on a 70x66x62 grid (several 16^3 tiles per axis, ragged edge
-    tiles): pressure and iterations against the oracle."""
+@pytest.mark.parametrize("shape,kernel", [((70, 66, 62), "tile"), ((64, 72, 45), "column"),
+                                          ((64, 72, 45), "tile")])
+def test_mic_large_against_oracle(shape, kernel, monkeypatch):
+    """MIC-PCG on grids with several wavefront blocks per axis and ragged
+    edge blocks, through both sweep kernels (the column-block sweep needs
+    nx % 8 == 0; the tiled sweep handles any size): pressure and iteration
+    count against the oracle."""
+    monkeypatch.setenv("MANTA_GB300_MIC", kernel)
     rng = np.random.default_rng(7)
-    nx, ny, nz = 70, 66, 62
+    nx, ny, nz = shape
     f = np.full((nz, ny, nx), og.FLUID, np.int32)
     og.init_domain(f, 0)
     og.fill_grid(f)
