@@ -116,6 +116,7 @@ struct MicColPlan {
   unsigned long long* prog;   // per-block progress, epoch in the high word
   int* counter;
   int* error;
+  int pubMask;                // progress published every pubMask+1 steps
 };
 bool mic_col_supported(const Dims& d);
 void mic_col_geometry(const Dims& d, int* nby, int* nbz);

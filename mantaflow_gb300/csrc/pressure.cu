@@ -463,13 +463,18 @@ __device__ __forceinline__ void st_release(unsigned int* p, unsigned int v) {
 }
 
 // Wait (thread 0) until tile `t` carries this sweep's epoch; gives up after
-// spinLimit polls, records the failure and lets the sweep finish.
+// spinLimit nanoseconds, records the failure and lets the sweep finish.
+__device__ __forceinline__ unsigned long long gtimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
 __device__ __forceinline__ void wait_tile(const MicArgs& a, int t) {
   if (t < 0) return;
-  long long n = 0;
+  const unsigned long long t0 = gtimer_ns();
   while (ld_acquire(a.tileDone + t) != a.epoch) {
     // once any wait has given up the sweep is already wrong: stop waiting
-    if (++n > a.spinLimit || *((volatile int*)a.error) != 0) {
+    if (gtimer_ns() - t0 > (unsigned long long)a.spinLimit || *((volatile int*)a.error) != 0) {
       atomicExch(a.error, 1);
       return;
     }

@@ -24,6 +24,10 @@ using namespace mgpu;
 
 unsigned long long mgpu::g_launches = 0;
 
+// upper bound on any single device-side wait in the MIC wavefronts (ns);
+// a wait that runs out flags an error instead of spinning on
+static const long long kWaitNs = 200000000LL;
+
 // ------------------------------------------------------------------ errors
 static thread_local std::string g_err;
 
@@ -38,10 +42,24 @@ static int fail(int code, const std::string& msg) {
     if (e_ != cudaSuccess) return fail(MG_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
   } while (0)
 
-#define CKL()                                                                                      \
-  do {                                                                                             \
-    cudaError_t e_ = cudaGetLastError();                                                           \
-    if (e_ != cudaSuccess) return fail(MG_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+// MANTA_GB300_SYNC_CHECK=1 synchronises after every launch site so that a
+// failing kernel is reported where it was launched (debugging aid).
+static bool sync_check() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("MANTA_GB300_SYNC_CHECK");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+
+#define CKL()                                                                                         \
+  do {                                                                                                \
+    cudaError_t e_ = cudaGetLastError();                                                              \
+    if (e_ == cudaSuccess && sync_check()) e_ = cudaDeviceSynchronize();                              \
+    if (e_ != cudaSuccess)                                                                            \
+      return fail(MG_ERR_CUDA, std::string("kernel launch (") + __func__ + ":" + std::to_string(__LINE__) + \
+                                   "): " + cudaGetErrorString(e_));                                   \
   } while (0)
 
 // ----------------------------------------------------------------- context
@@ -290,7 +308,9 @@ static void free_cg_state(mg_solver s) {
   s->code = nullptr; s->A0f = nullptr; s->residual = s->search = s->tmp = s->P = nullptr;
   s->part = nullptr; s->partf = nullptr; s->sc = nullptr; s->scHost = nullptr; s->intScratch = nullptr;
   s->mic = MicPlan{};
-  cudaFree(s->micCol.order); cudaFree(s->micCol.prog); cudaFree(s->micCol.counter); cudaFree(s->micCol.error);
+  // micCol.error aliases mic.error (freed above)
+  cudaFree(s->micCol.order); cudaFree(s->micCol.prog); cudaFree(s->micCol.counter);
+  cudaGetLastError();  // a failed free must not surface as a later launch error
   s->micCol = MicColPlan{};
 }
 
@@ -732,10 +752,10 @@ static int ensure_cg_state(mg_solver s) {
     CK(cudaMalloc(&m.error, sizeof(int)));
     CK(cudaMemset(m.error, 0, sizeof(int)));
     m.ctas = g_ctx.sms * g_ctx.micCtasPerSm;
-    // column-block sweeps unless the grid's x size rules them out (or the
-    // tiled sweeps are requested for testing)
+    // tiled sweeps by default; MANTA_GB300_MIC=column selects the
+    // column-block sweeps (mic.cu) where the grid's x size allows them
     const char* ev = getenv("MANTA_GB300_MIC");
-    s->useMicCol = mic_col_supported(s->d) && !(ev && std::string(ev) == "tile");
+    s->useMicCol = mic_col_supported(s->d) && ev && std::string(ev) == "column";
     if (s->useMicCol) {
       MicColPlan& c = s->micCol;
       mic_col_geometry(s->d, &c.nby, &c.nbz);
@@ -748,6 +768,7 @@ static int ensure_cg_state(mg_solver s) {
       CK(cudaMemset(c.prog, 0, ord.size() * sizeof(unsigned long long)));
       CK(cudaMalloc(&c.counter, sizeof(int)));
       c.error = m.error;
+      c.pubMask = 7;  // progress published every 8 steps
       if ((size_t)c.nblocks > s->partCount) return fail(MG_ERR_STATE, "MIC: partial buffer too small");
     }
   }
@@ -807,13 +828,13 @@ static int apply_precond(mg_solver s, const PcgBuffers& b, int pc, bool init) {
   if (pc == kPcMic) {
     {
       ProfScope ps(s, "mic_forward");
-      if (s->useMicCol) launch_mic_col(b, s->micCol, 1, ++s->epoch, 1LL << 22, g_ctx.sms, s->stream);
-      else launch_mic(b, s->mic, 1, ++s->epoch, 1LL << 22, s->stream);
+      if (s->useMicCol) launch_mic_col(b, s->micCol, 1, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
+      else launch_mic(b, s->mic, 1, ++s->epoch, kWaitNs, s->stream);
     }
     {
       ProfScope ps(s, "mic_backward");
-      if (s->useMicCol) launch_mic_col(b, s->micCol, init ? 3 : 2, ++s->epoch, 1LL << 22, g_ctx.sms, s->stream);
-      else launch_mic(b, s->mic, init ? 3 : 2, ++s->epoch, 1LL << 22, s->stream);
+      if (s->useMicCol) launch_mic_col(b, s->micCol, init ? 3 : 2, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
+      else launch_mic(b, s->mic, init ? 3 : 2, ++s->epoch, kWaitNs, s->stream);
     }
   } else if (pc == kPcMg) {
     ProfScope ps(s, "mg_vcycle");
@@ -918,8 +939,8 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   if (pc == kPcMic) {
     ProfScope ps(s, "mic_init");
     CK(cudaMemsetAsync(s->mic.error, 0, sizeof(int), s->stream));
-    if (s->useMicCol) launch_mic_col(b, s->micCol, 0, ++s->epoch, 1LL << 22, g_ctx.sms, s->stream);
-    else launch_mic(b, s->mic, 0, ++s->epoch, 1LL << 22, s->stream);
+    if (s->useMicCol) launch_mic_col(b, s->micCol, 0, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
+    else launch_mic(b, s->mic, 0, ++s->epoch, kWaitNs, s->stream);
     CKL();
   }
   if (pc != kPcNone) {
