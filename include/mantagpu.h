@@ -104,6 +104,19 @@ int mg_host_free(void* p);
 /* advectSemiLagrange (:442-460); dt from the solver */
 int mg_advect_semi_lagrange(mg_grid flags, mg_grid vel, mg_grid grid, int order, float strength, int orderSpace,
                             int openBounds, int boundaryWidth, int clampMode, int orderTrace);
+/* No counterpart in the reference.  Same arguments and results as
+ * mg_advect_semi_lagrange, but allocates no device memory: its two
+ * temporaries live in a fixed 24 MiB device array inside the library, for
+ * callers that cannot allocate once running (a host whose own allocator holds
+ * the rest of the GPU, a latency-bound loop that cannot afford a
+ * cudaMalloc/cudaFree).  Limit: grids of up to 3,145,728 floats (a Real grid
+ * of 3,145,728 cells, a Vec3/MAC grid of 1,048,576 cells); larger grids return
+ * MG_ERR_ARG.  The result is written back into the grid's own storage.  The
+ * first call on a device looks up the array's address, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * (solvers on different streams) race. */
+int mg_advect_semi_lagrange_noalloc(mg_grid flags, mg_grid vel, mg_grid grid, int order, float strength,
+                                    int orderSpace, int openBounds, int boundaryWidth, int clampMode, int orderTrace);
 /* resetPhiInObs (:401) */
 int mg_reset_phi_in_obs(mg_grid flags, mg_grid sdf);
 

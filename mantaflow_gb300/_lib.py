@@ -53,6 +53,7 @@ SIGNATURES = [
     ("mg_host_alloc", _I, [C.c_size_t, C.POINTER(_P)]),
     ("mg_host_free", _I, [_P]),
     ("mg_advect_semi_lagrange", _I, [_P, _P, _P, _I, _F, _I, _I, _I, _I, _I]),
+    ("mg_advect_semi_lagrange_noalloc", _I, [_P, _P, _P, _I, _F, _I, _I, _I, _I, _I]),
     ("mg_reset_phi_in_obs", _I, [_P, _P]),
     ("mg_set_wall_bcs", _I, [_P, _P, _P, _P, _P, _I]),
     ("mg_add_buoyancy", _I, [_P, _P, _P, _F, _F, _F, _F, _I]),

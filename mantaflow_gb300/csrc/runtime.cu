@@ -586,6 +586,106 @@ extern "C" int mg_advect_semi_lagrange(mg_grid flags, mg_grid vel, mg_grid grid,
   return MG_OK;
 }
 
+// ---------------------------------------------- advection without allocation
+// mg_advect_semi_lagrange_noalloc keeps its two temporaries (the forward
+// trace and the MacCormack / outflow result) in this fixed device array
+// instead of the solver's pool, for callers that must not allocate device
+// memory once they run: hosts that have handed the rest of the GPU to their
+// own allocator, and latency-bound loops where a cudaMalloc/cudaFree (which
+// may synchronise the device) cannot be afforded.  Each temporary holds up to
+// kNoAllocSlotFloats floats: a Real or levelset grid of up to 3,145,728 cells,
+// a Vec3 or MAC grid of up to 1,048,576 cells.  Every launch of a call writes
+// each cell that a later launch of the same call reads, so nothing has to
+// start at zero.  All calls share the one array: calls that overlap on the GPU
+// (solvers on different streams running at the same time) race on it.
+constexpr size_t kNoAllocSlotFloats = (size_t)3 << 20;
+static __device__ __align__(256) float g_noallocScratch[2 * kNoAllocSlotFloats];
+static float* g_noallocPtr[64] = {};  // per device ordinal, set on first use
+
+// Resolves the array's device address for the current device.  Runs once per
+// device, on the first call, which should therefore come before any stream
+// capture on that device.
+static int noalloc_scratch(float** out) {
+  std::lock_guard<std::mutex> lk(g_ctx.mu);
+  const int dev = g_ctx.device;
+  if (dev < 0 || dev >= 64) return fail(MG_ERR_STATE, "advectSemiLagrange (no-alloc): device ordinal out of range");
+  if (!g_noallocPtr[dev]) {
+    CK(cudaSetDevice(dev));
+    void* p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_noallocScratch));
+    g_noallocPtr[dev] = (float*)p;
+  }
+  *out = g_noallocPtr[dev];
+  return MG_OK;
+}
+
+extern "C" int mg_advect_semi_lagrange_noalloc(mg_grid flags, mg_grid vel, mg_grid grid, int order, float strength,
+                                               int orderSpace, int openBounds, int boundaryWidth, int clampMode,
+                                               int orderTrace) {
+  NEED_GRID(flags, "advectSemiLagrange");
+  NEED_GRID(vel, "advectSemiLagrange");
+  NEED_GRID(grid, "advectSemiLagrange");
+  (void)openBounds;
+  (void)boundaryWidth;
+  if (!(order == 1 || order == 2))
+    return fail(MG_ERR_SOLVER, "AdvectSemiLagrange: Only order 1 (regular SL) and 2 (MacCormack) supported");
+  if (flags->kind != MG_FLAGS || vel->kind != MG_MAC) return fail(MG_ERR_ARG, "advectSemiLagrange: flags must be a FlagGrid and vel a MACGrid");
+  if (flags->s != vel->s || grid->s != vel->s) return fail(MG_ERR_ARG, "advectSemiLagrange: grids of different solvers");
+  if (orderTrace != 1 && orderTrace != 2) return fail(MG_ERR_SOLVER, "Unknown backtracing order " + std::to_string(orderTrace));
+  if (orderSpace != 1 && orderSpace != 2) return fail(MG_ERR_SOLVER, "Unknown interpolation order " + std::to_string(orderSpace));
+  if (grid->kind == MG_INT || grid->kind == MG_FLAGS)
+    return fail(MG_ERR_SOLVER, "AdvectSemiLagrange: Grid Type is not supported (only Real, Vec3, MAC, Levelset)");
+  if (grid->kind == MG_MAC && orderSpace != 1)
+    return fail(MG_ERR_UNSUPPORTED, "advectSemiLagrange: cubic (orderSpace=2) MAC advection is not supported");
+  mg_solver s = flags->s;
+  const Dims& d = s->d;
+  const float dt = s->dt;
+  const size_t floats = (size_t)grid->comps() * (size_t)d.n;
+  if (floats > kNoAllocSlotFloats)
+    return fail(MG_ERR_ARG, "mg_advect_semi_lagrange_noalloc: the grid holds " + std::to_string(floats) +
+                                " floats; the fixed scratch takes at most " + std::to_string(kNoAllocSlotFloats) +
+                                " (a Real grid of 3145728 cells, a Vec3/MAC grid of 1048576 cells)");
+  float* scratch = nullptr;
+  const int st = noalloc_scratch(&scratch);
+  if (st) return st;
+  float* A = scratch;
+  float* B = scratch + kNoAllocSlotFloats;
+  const Mac mA{A, A + d.n, A + 2 * d.n}, mB{B, B + d.n, B + 2 * d.n};
+  const CMac cA{A, A + d.n, A + 2 * d.n}, cB{B, B + d.n, B + 2 * d.n};
+  const float* result;
+  if (grid->kind == MG_MAC) {
+    launch_advect_sl_mac(d, vel->cmac(), grid->cmac(), mA, dt, orderTrace, s->stream);
+    CKL();
+    const float ts = (float)std::max(1.0, (double)dt * 4);
+    if (order == 1) {
+      launch_outflow_bc(d, flags->i(), cA, grid->cmac(), mB, mA, ts, s->stream);
+      result = A;
+    } else {
+      launch_advect_maccormack_mac(d, flags->i(), vel->cmac(), grid->cmac(), cA, mB, dt, strength, clampMode, orderTrace,
+                                   s->stream);
+      CKL();
+      launch_outflow_bc(d, flags->i(), cB, grid->cmac(), mA, mB, ts, s->stream);
+      result = B;
+    }
+    CKL();
+  } else {
+    const int ch = grid->comps();
+    launch_advect_sl(d, ch, vel->cmac(), grid->f(), A, dt, orderSpace, orderTrace, s->stream);
+    CKL();
+    result = A;
+    if (order == 2) {
+      launch_advect_maccormack(d, ch, flags->i(), vel->cmac(), grid->f(), A, B, dt, strength, clampMode, orderSpace,
+                               orderTrace, s->stream);
+      CKL();
+      result = B;
+    }
+  }
+  // the result goes back into the grid's own storage (the pooled entry point
+  // swaps storage instead)
+  CK(cudaMemcpyAsync(grid->data, result, floats * sizeof(float), cudaMemcpyDeviceToDevice, s->stream));
+  return MG_OK;
+}
+
 extern "C" int mg_reset_phi_in_obs(mg_grid flags, mg_grid sdf) {
   NEED_GRID(flags, "resetPhiInObs");
   NEED_GRID(sdf, "resetPhiInObs");
