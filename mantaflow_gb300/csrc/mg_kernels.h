@@ -124,6 +124,28 @@ void mic_col_order(int nby, int nbz, int* order);
 int mic_col_prepare();
 void launch_mic_col(const PcgBuffers& b, const MicColPlan& m, int mode, unsigned int epoch, long long spinLimit,
                     int ctas, cudaStream_t s);
+// warp-wavefront MIC sweeps (micwave.cu), for grids with nx % 8 == 0
+struct MicWavePlan {
+  int zw;                          // z-lines per lane: 4 or 8
+  int nyb, nzb, nunits, rows;
+  int* order;                      // unit dispatch order ((yb + zb) levels)
+  int* counter;
+  int* error;
+  unsigned long long* exchange;    // face words, epoch-tagged (zeroed once)
+};
+bool mic_wave_supported(const Dims& d);
+void mic_wave_geometry(const Dims& d, int zw, int* nyb, int* nzb, int* rows);
+size_t mic_wave_exchange_words(const Dims& d, int zw);
+void mic_wave_order(int nyb, int nzb, int* order);
+int mic_wave_prepare(int* ctasPerSm4, int* ctasPerSm8);
+void launch_mic_wave(const PcgBuffers& b, const MicWavePlan& m, int mode, unsigned int epoch, long long spinLimit,
+                     int ctas, cudaStream_t s);
+// tile-dataflow MIC sweeps (micflow.cu): the tiles of a MicPlan, faces
+// published as epoch-tagged words (face: mic_flow_face_words() words)
+int mic_flow_prepare(int* ctasPerSm);
+size_t mic_flow_face_words(int ntiles);
+void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* face, int mode, unsigned int epoch,
+                     long long spinLimit, cudaStream_t s);
 // sum of nparts per-block dot partials -> beta/sigma (init: sigma only)
 void launch_mic_finish(const PcgBuffers& b, int nparts, bool init, cudaStream_t s);
 

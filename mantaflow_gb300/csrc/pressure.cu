@@ -20,6 +20,7 @@
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 
+#include <algorithm>
 #include <cfloat>
 
 namespace mgpu {
@@ -430,6 +431,138 @@ __global__ void k_pcg_update(long long n, const float* __restrict__ t, float* s,
     s[idx] = t[idx] + beta * s[idx];
 }
 
+// ---- four cells per thread (x size a multiple of 4, so a float4 never
+// leaves its x-row and every row starts 16-byte aligned).  A thread keeps
+// 48-64 bytes of loads in flight per iteration instead of 12-16, which is
+// what it takes to cover HBM latency at full bandwidth.  Each cell performs
+// the same float operations as the scalar kernels above.
+__device__ __forceinline__ float fget(const float4& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+
+__global__ void __launch_bounds__(256) k_pcg_spmv4(Dims d, const code_t* __restrict__ code,
+                                                   const float* __restrict__ A0f, const float* __restrict__ x,
+                                                   float* y, double* part, CgScalars* sc) {
+  if (sc->done) return;
+  double acc = 0.;
+  const long long nq = d.n >> 2;
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
+    const long long idx = q << 2;
+    const uint2 cw = __ldg(reinterpret_cast<const uint2*>(code) + q);
+    const int c[4] = {(int)(cw.x & 0xffffu), (int)(cw.x >> 16), (int)(cw.y & 0xffffu), (int)(cw.y >> 16)};
+    const int any = c[0] | c[1] | c[2] | c[3];
+    const float4 xc = __ldg(x4 + q);
+    const float4 ylo = (any & kLowY) ? __ldg(x4 + q - (d.sy >> 2)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 yhi = (any & kHighY) ? __ldg(x4 + q + (d.sy >> 2)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 zlo = (any & kLowZ) ? __ldg(x4 + q - (d.sz >> 2)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 zhi = (any & kHighZ) ? __ldg(x4 + q + (d.sz >> 2)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float xl = (c[0] & kLowX) ? __ldg(x + idx - 1) : 0.f;
+    const float xr = (c[3] & kHighX) ? __ldg(x + idx + 4) : 0.f;
+    float4 A0 = make_float4((float)(c[0] & 7), (float)(c[1] & 7), (float)(c[2] & 7), (float)(c[3] & 7));
+    if (A0f) A0 = __ldg(reinterpret_cast<const float4*>(A0f) + q);
+    float out[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int ce = c[e];
+      const float xv = fget(xc, e);
+      float v;
+      if (!(ce & kCodeFluid)) {
+        v = xv;
+      } else {
+        v = xv * fget(A0, e);
+        if (ce & kLowX) v = v - (e == 0 ? xl : fget(xc, e - 1));
+        if (ce & kHighX) v = v - (e == 3 ? xr : fget(xc, e + 1));
+        if (ce & kLowY) v = v - fget(ylo, e);
+        if (ce & kHighY) v = v - fget(yhi, e);
+        if (ce & kLowZ) v = v - fget(zlo, e);
+        if (ce & kHighZ) v = v - fget(zhi, e);
+      }
+      out[e] = v;
+      acc += (double)(v * xv);
+    }
+    reinterpret_cast<float4*>(y)[q] = make_float4(out[0], out[1], out[2], out[3]);
+  }
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
+  if (last_block(&sc->counters[1], gridDim.x)) {
+    const double s = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      const float dp = (float)s;
+      sc->dp = dp;
+      float alpha = 0.f;
+      if (fabsf(dp) > 0.f) alpha = sc->sigma / dp;
+      sc->alpha = alpha;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_pcg_axpy4(long long n, float* p, const float* __restrict__ s, float* r,
+                                                   const float* __restrict__ t, double* part, float* partf,
+                                                   CgScalars* sc) {
+  if (sc->done) return;
+  const float alpha = sc->alpha, na = -alpha;
+  const int l2 = sc->useL2;
+  float mn = FLT_MAX, mx = -FLT_MAX;
+  double ss = 0.;
+  const long long nq = n >> 2;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
+    float4 pv = reinterpret_cast<const float4*>(p)[q];
+    const float4 sv = __ldg(reinterpret_cast<const float4*>(s) + q);
+    float4 rv = reinterpret_cast<const float4*>(r)[q];
+    const float4 tv = __ldg(reinterpret_cast<const float4*>(t) + q);
+    pv.x = pv.x + alpha * sv.x; pv.y = pv.y + alpha * sv.y; pv.z = pv.z + alpha * sv.z; pv.w = pv.w + alpha * sv.w;
+    rv.x = rv.x + na * tv.x; rv.y = rv.y + na * tv.y; rv.z = rv.z + na * tv.z; rv.w = rv.w + na * tv.w;
+    reinterpret_cast<float4*>(p)[q] = pv;
+    reinterpret_cast<float4*>(r)[q] = rv;
+    mn = fminf(fminf(mn, fminf(rv.x, rv.y)), fminf(rv.z, rv.w));
+    mx = fmaxf(fmaxf(mx, fmaxf(rv.x, rv.y)), fmaxf(rv.z, rv.w));
+    if (l2) {
+      ss += (double)rv.x * (double)rv.x;
+      ss += (double)rv.y * (double)rv.y;
+      ss += (double)rv.z * (double)rv.z;
+      ss += (double)rv.w * (double)rv.w;
+    }
+  }
+  block_minmax(mn, mx);
+  const double bs = l2 ? block_sum(ss) : 0.;
+  if (threadIdx.x == 0) {
+    partf[2 * blockIdx.x] = mn;
+    partf[2 * blockIdx.x + 1] = mx;
+    part[blockIdx.x] = bs;
+  }
+  if (last_block(&sc->counters[2], gridDim.x)) {
+    float res = 0.f;
+    if (l2) {
+      const double a = sum_partials(part, gridDim.x);
+      res = (float)a;
+    } else {
+      float amin, amax;
+      minmax_partials(partf, gridDim.x, amin, amax);
+      const float x = fabsf(amin), y = fabsf(amax);
+      res = x < y ? y : x;
+    }
+    if (threadIdx.x != 0) return;
+    sc->iterations += 1;
+    sc->resNorm = res;
+    if (res < sc->accuracy) {
+      sc->sigma = res;
+      sc->done = 1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_pcg_update4(long long n, const float* __restrict__ t, float* s,
+                                                     const CgScalars* sc) {
+  if (sc->done) return;
+  const float beta = sc->beta;
+  const long long nq = n >> 2;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
+    const float4 tv = __ldg(reinterpret_cast<const float4*>(t) + q);
+    float4 sv = reinterpret_cast<const float4*>(s)[q];
+    sv.x = tv.x + beta * sv.x; sv.y = tv.y + beta * sv.y; sv.z = tv.z + beta * sv.z; sv.w = tv.w + beta * sv.w;
+    reinterpret_cast<float4*>(s)[q] = sv;
+  }
+}
+
 // ---------------------------------------------------------------- MIC(0)
 constexpr int T = 16;           // tile edge
 constexpr int TC = T * T * T;   // cells per tile
@@ -779,13 +912,26 @@ void launch_pcg_set_search(const PcgBuffers& b, cudaStream_t s) {
   count_launch();
   k_pcg_set_search<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.tmp, b.residual, b.search, b.part, b.sc);
 }
+// four-cell kernels need rows of a multiple of 4 cells
+static bool vec4_ok(const Dims& d) { return (d.nx & 3) == 0; }
+static int vec4_blocks(const PcgBuffers& b) {
+  const long long need = (b.d.n / 4 + kThreads - 1) / kThreads;
+  return (int)std::max(1LL, std::min((long long)b.nblocks, need));
+}
 void launch_pcg_spmv(const PcgBuffers& b, cudaStream_t s) {
   count_launch();
-  k_pcg_spmv<<<b.nblocks, kThreads, 0, s>>>(b.d, b.code, b.A0f, b.search, b.tmp, b.part, b.sc);
+  if (vec4_ok(b.d))
+    k_pcg_spmv4<<<vec4_blocks(b), kThreads, 0, s>>>(b.d, b.code, b.A0f, b.search, b.tmp, b.part, b.sc);
+  else
+    k_pcg_spmv<<<b.nblocks, kThreads, 0, s>>>(b.d, b.code, b.A0f, b.search, b.tmp, b.part, b.sc);
 }
 void launch_pcg_axpy(const PcgBuffers& b, cudaStream_t s) {
   count_launch();
-  k_pcg_axpy<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.pressure, b.search, b.residual, b.tmp, b.part, b.partf, b.sc);
+  if (vec4_ok(b.d))
+    k_pcg_axpy4<<<vec4_blocks(b), kThreads, 0, s>>>(b.d.n, b.pressure, b.search, b.residual, b.tmp, b.part, b.partf,
+                                                    b.sc);
+  else
+    k_pcg_axpy<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.pressure, b.search, b.residual, b.tmp, b.part, b.partf, b.sc);
 }
 void launch_pcg_copy_dot(const PcgBuffers& b, cudaStream_t s) {
   count_launch();
@@ -793,7 +939,10 @@ void launch_pcg_copy_dot(const PcgBuffers& b, cudaStream_t s) {
 }
 void launch_pcg_update(const PcgBuffers& b, cudaStream_t s) {
   count_launch();
-  k_pcg_update<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.tmp, b.search, b.sc);
+  if (vec4_ok(b.d))
+    k_pcg_update4<<<vec4_blocks(b), kThreads, 0, s>>>(b.d.n, b.tmp, b.search, b.sc);
+  else
+    k_pcg_update<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.tmp, b.search, b.sc);
 }
 
 // mode: 0 init P, 1 forward, 2 backward (+dot, beta), 3 backward for doInit (+sigma)

@@ -68,6 +68,8 @@ struct Ctx {
   int device = -1;
   int sms = 0;
   int micCtasPerSm = 1;
+  int waveCtasPerSm4 = 1, waveCtasPerSm8 = 1;
+  int flowCtasPerSm = 1;
   std::set<mg_solver> solvers;
   std::mutex mu;
 };
@@ -103,6 +105,10 @@ struct mg_solver_s {
   MicPlan mic{};
   MicColPlan micCol{};
   bool useMicCol = false;
+  MicWavePlan micWave{};
+  bool useMicWave = false;
+  unsigned long long* micFace = nullptr;  // tile-dataflow sweeps: face words
+  bool useMicFlow = false;
   unsigned int epoch = 0;
   mgpu::MgHierarchy* mg = nullptr;  // static multigrid cache (gMapMG)
   // profiling
@@ -245,7 +251,9 @@ extern "C" int mg_init(int device) {
   CK(cudaGetDeviceProperties(&prop, device));
   g_ctx.sms = prop.multiProcessorCount;
   g_ctx.micCtasPerSm = mic_ctas_per_sm();
-  if (mic_col_prepare()) return fail(MG_ERR_CUDA, "mg_init: cannot configure the MIC kernels");
+  if (mic_col_prepare() || mic_wave_prepare(&g_ctx.waveCtasPerSm4, &g_ctx.waveCtasPerSm8) ||
+      mic_flow_prepare(&g_ctx.flowCtasPerSm))
+    return fail(MG_ERR_CUDA, "mg_init: cannot configure the MIC kernels");
   g_ctx.device = device;
   g_ctx.init = true;
   return MG_OK;
@@ -310,8 +318,13 @@ static void free_cg_state(mg_solver s) {
   s->mic = MicPlan{};
   // micCol.error aliases mic.error (freed above)
   cudaFree(s->micCol.order); cudaFree(s->micCol.prog); cudaFree(s->micCol.counter);
+  // micWave.error aliases mic.error as well
+  cudaFree(s->micWave.order); cudaFree(s->micWave.counter); cudaFree(s->micWave.exchange);
+  cudaFree(s->micFace);
+  s->micFace = nullptr;
   cudaGetLastError();  // a failed free must not surface as a later launch error
   s->micCol = MicColPlan{};
+  s->micWave = MicWavePlan{};
 }
 
 extern "C" int mg_solver_destroy(mg_solver s) {
@@ -852,10 +865,36 @@ static int ensure_cg_state(mg_solver s) {
     CK(cudaMalloc(&m.error, sizeof(int)));
     CK(cudaMemset(m.error, 0, sizeof(int)));
     m.ctas = g_ctx.sms * g_ctx.micCtasPerSm;
-    // tiled sweeps by default; MANTA_GB300_MIC=column selects the
-    // column-block sweeps (mic.cu) where the grid's x size allows them
+    // tile-dataflow sweeps (micflow.cu) by default; MANTA_GB300_MIC selects
+    // the whole-tile sweeps ("tile", pressure.cu), the column-block sweeps
+    // ("column", mic.cu) or the warp wavefronts ("wave", micwave.cu)
     const char* ev = getenv("MANTA_GB300_MIC");
-    s->useMicCol = mic_col_supported(s->d) && ev && std::string(ev) == "column";
+    const std::string mk = ev ? std::string(ev) : std::string("flow");
+    s->useMicCol = mic_col_supported(s->d) && mk == "column";
+    s->useMicWave = mic_wave_supported(s->d) && mk == "wave";
+    s->useMicFlow = !s->useMicCol && !s->useMicWave && mk != "tile";
+    if (s->useMicFlow) {
+      const size_t words = mic_flow_face_words(m.ntiles);
+      CK(cudaMalloc(&s->micFace, words * sizeof(unsigned long long)));
+      CK(cudaMemset(s->micFace, 0, words * sizeof(unsigned long long)));
+    }
+    if (s->useMicWave) {
+      MicWavePlan& w = s->micWave;
+      const char* zv = getenv("MANTA_GB300_MIC_ZW");  // tuning: z-lines per lane
+      w.zw = (zv && atoi(zv) == 4) ? 4 : 8;
+      mic_wave_geometry(s->d, w.zw, &w.nyb, &w.nzb, &w.rows);
+      w.nunits = w.nyb * w.nzb;
+      std::vector<int> ord((size_t)w.nunits);
+      mic_wave_order(w.nyb, w.nzb, ord.data());
+      CK(cudaMalloc(&w.order, ord.size() * sizeof(int)));
+      CK(cudaMemcpy(w.order, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice));
+      CK(cudaMalloc(&w.counter, sizeof(int)));
+      const size_t words = mic_wave_exchange_words(s->d, w.zw);
+      CK(cudaMalloc(&w.exchange, words * sizeof(unsigned long long)));
+      CK(cudaMemset(w.exchange, 0, words * sizeof(unsigned long long)));
+      w.error = m.error;
+      if ((size_t)w.nunits > s->partCount) return fail(MG_ERR_STATE, "MIC: partial buffer too small");
+    }
     if (s->useMicCol) {
       MicColPlan& c = s->micCol;
       mic_col_geometry(s->d, &c.nby, &c.nbz);
@@ -873,6 +912,16 @@ static int ensure_cg_state(mg_solver s) {
     }
   }
   return MG_OK;
+}
+
+static MicPlan flow_plan(mg_solver s) {
+  MicPlan m = s->mic;
+  m.ctas = g_ctx.sms * g_ctx.flowCtasPerSm;
+  return m;
+}
+
+static int wave_ctas(mg_solver s) {
+  return g_ctx.sms * (s->micWave.zw == 4 ? g_ctx.waveCtasPerSm4 : g_ctx.waveCtasPerSm8);
 }
 
 static PcgBuffers cg_buffers(mg_solver s, mg_grid flags, float* rhs, mg_grid pressure) {
@@ -928,12 +977,17 @@ static int apply_precond(mg_solver s, const PcgBuffers& b, int pc, bool init) {
   if (pc == kPcMic) {
     {
       ProfScope ps(s, "mic_forward");
-      if (s->useMicCol) launch_mic_col(b, s->micCol, 1, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
+      if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 1, ++s->epoch, kWaitNs, s->stream);
+      else if (s->useMicWave) launch_mic_wave(b, s->micWave, 1, ++s->epoch, kWaitNs, wave_ctas(s), s->stream);
+      else if (s->useMicCol) launch_mic_col(b, s->micCol, 1, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
       else launch_mic(b, s->mic, 1, ++s->epoch, kWaitNs, s->stream);
     }
     {
       ProfScope ps(s, "mic_backward");
-      if (s->useMicCol) launch_mic_col(b, s->micCol, init ? 3 : 2, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
+      if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, init ? 3 : 2, ++s->epoch, kWaitNs, s->stream);
+      else if (s->useMicWave)
+        launch_mic_wave(b, s->micWave, init ? 3 : 2, ++s->epoch, kWaitNs, wave_ctas(s), s->stream);
+      else if (s->useMicCol) launch_mic_col(b, s->micCol, init ? 3 : 2, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
       else launch_mic(b, s->mic, init ? 3 : 2, ++s->epoch, kWaitNs, s->stream);
     }
   } else if (pc == kPcMg) {
@@ -1039,7 +1093,9 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   if (pc == kPcMic) {
     ProfScope ps(s, "mic_init");
     CK(cudaMemsetAsync(s->mic.error, 0, sizeof(int), s->stream));
-    if (s->useMicCol) launch_mic_col(b, s->micCol, 0, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
+    if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 0, ++s->epoch, kWaitNs, s->stream);
+    else if (s->useMicWave) launch_mic_wave(b, s->micWave, 0, ++s->epoch, kWaitNs, wave_ctas(s), s->stream);
+    else if (s->useMicCol) launch_mic_col(b, s->micCol, 0, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
     else launch_mic(b, s->mic, 0, ++s->epoch, kWaitNs, s->stream);
     CKL();
   }

@@ -162,7 +162,11 @@ PRESSURE_CASES = {
 
 @pytest.mark.parametrize("tag", ["3d", "2d"])
 @pytest.mark.parametrize("case", sorted(PRESSURE_CASES))
-def test_solve_pressure(tag, case):
+@pytest.mark.parametrize("kernel", ["tile", "wave", "flow"])
+def test_solve_pressure(tag, case, kernel, monkeypatch):
+    if tag == "2d" and kernel != "tile":
+        pytest.skip("MIC(0) runs in 3D only; 2D uses PcNone")
+    monkeypatch.setenv("MANTA_GB300_MIC", kernel)
     g = load("pressure_" + tag)
     names = [str(n) for n in g["names"]]
     if case not in names:
@@ -205,9 +209,11 @@ def test_pcnone_rejected_like_reference():
     assert str(g["none_error"]).startswith(str(e.value).split("\n")[0][:40])
 
 
-def test_plume_steps_against_reference():
+@pytest.mark.parametrize("kernel", ["tile", "wave", "flow"])
+def test_plume_steps_against_reference(kernel, monkeypatch):
     """8 full plume steps (24^3, MacCormack + MIC) against the reference
     executable's per-step outputs; thresholds of tools/tests/test_2010."""
+    monkeypatch.setenv("MANTA_GB300_MIC", kernel)
     g = load("plume_mic24")
     n = g["flags"].shape[0]
     s = m.Solver(name="plume", gridSize=m.vec3(n, n, n), dim=3)
@@ -240,12 +246,14 @@ def test_plume_steps_against_reference():
 
 
 @pytest.mark.parametrize("shape,kernel", [((70, 66, 62), "tile"), ((64, 72, 45), "column"),
-                                          ((64, 72, 45), "tile")])
+                                          ((64, 72, 45), "tile"), ((64, 72, 45), "wave"),
+                                          ((96, 40, 70), "wave"), ((16, 100, 17), "wave"),
+                                          ((70, 66, 62), "flow"), ((64, 72, 45), "flow"), ((16, 100, 17), "flow")])
 def test_mic_large_against_oracle(shape, kernel, monkeypatch):
     """MIC-PCG on grids with several wavefront blocks per axis and ragged
-    edge blocks, through both sweep kernels (the column-block sweep needs
-    nx % 8 == 0; the tiled sweep handles any size): pressure and iteration
-    count against the oracle."""
+    edge blocks, through every sweep kernel (the column-block and warp
+    wavefront sweeps need nx % 8 == 0; the tiled sweep handles any size):
+    pressure and iteration count against the oracle."""
     monkeypatch.setenv("MANTA_GB300_MIC", kernel)
     rng = np.random.default_rng(7)
     nx, ny, nz = shape
