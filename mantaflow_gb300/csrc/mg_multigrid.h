@@ -1,4 +1,5 @@
-// Multigrid preconditioner on the GPU (multigrid.cpp, Dick et al. 2015).
+// Multigrid preconditioner on the GPU (GridMg, multigrid.cpp; Dick,
+// Rogowsky and Westermann 2015, without topology awareness).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -10,11 +11,19 @@ struct MgHierarchy;
 
 MgHierarchy* mg_hierarchy_create(const Dims& d);
 void mg_hierarchy_destroy(MgHierarchy* h);
+// forget the matrix: the next mg_setup builds the hierarchy again (the
+// reference deletes the GridMg of a PcMGDynamic solve, pressure.cpp:418-451).
+// Device buffers and the coarse-vertex selection cache are kept.
+void mg_hierarchy_reset(MgHierarchy* h);
 size_t mg_hierarchy_bytes(const MgHierarchy* h);
-// GridMg::setA when the hierarchy has no matrix yet, then
-// setCoarsestLevelAccuracy; returns 0 on success
+int mg_hierarchy_levels(const MgHierarchy* h);
+// GridMg::setA when the hierarchy has no matrix yet (InitPreconditionMultigrid,
+// conjugategrad.cpp:100-106), then setCoarsestLevelAccuracy; 0 on success.
+// The matrix is read from b.code / b.A0f on the GPU.
 int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStream_t s);
-// setRhs(residual) + doVCycle(tmp); init selects the doInit bookkeeping
+// ApplyPreconditionMultigrid (conjugategrad.cpp:162-167): setRhs(residual)
+// and doVCycle(tmp) from a zero guess.  Unless init, the last kernel also
+// forms sigmaNew = dot(tmp, residual) and beta like GridCg::iterate.
 int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s);
 
 }  // namespace mgpu

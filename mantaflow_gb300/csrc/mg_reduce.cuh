@@ -1,0 +1,85 @@
+// Deterministic block and grid reductions shared by the PCG and multigrid
+// kernels: warp shuffles, per-warp partials summed in warp order, and a
+// "last block" ticket so the block that finishes last reduces the per-block
+// partials in index order.  Results do not depend on block scheduling.
+#pragma once
+#include <cfloat>
+#include <cuda_runtime.h>
+
+namespace mgpu {
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int lin_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
+__device__ __forceinline__ int nwarps() { return (blockDim.x * blockDim.y * blockDim.z) >> 5; }
+
+// block sum in a fixed order; result valid in thread 0
+template <typename T>
+__device__ __forceinline__ T block_sum(T v) {
+  __shared__ T sh[32];
+  const int t = lin_tid();
+  const int lane = t & 31, wid = t >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  T r = 0;
+  if (t == 0)
+    for (int q = 0; q < nwarps(); q++) r += sh[q];
+  return r;
+}
+
+__device__ __forceinline__ void block_minmax(float& mn, float& mx) {
+  __shared__ float s0[32], s1[32];
+  const int t = lin_tid();
+  const int lane = t & 31, wid = t >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  __syncthreads();
+  if (lane == 0) { s0[wid] = mn; s1[wid] = mx; }
+  __syncthreads();
+  if (t == 0)
+    for (int q = 1; q < nwarps(); q++) { mn = fminf(mn, s0[q]); mx = fmaxf(mx, s1[q]); }
+}
+
+// all threads of a block: sum of part[0..n) in a fixed order (strided
+// per-thread sums, then a fixed tree); the result is valid in thread 0.
+// The partials come from other blocks, so they are read from L2.
+__device__ __forceinline__ double sum_partials(const double* part, int n) {
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  double v = 0.;
+  for (int q = lin_tid(); q < n; q += nt) v += __ldcg(part + q);
+  return block_sum(v);
+}
+__device__ __forceinline__ void minmax_partials(const float* part, int n, float& mn, float& mx) {
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  mn = FLT_MAX;
+  mx = -FLT_MAX;
+  for (int q = lin_tid(); q < n; q += nt) {
+    mn = fminf(mn, __ldcg(part + 2 * q));
+    mx = fmaxf(mx, __ldcg(part + 2 * q + 1));
+  }
+  block_minmax(mn, mx);
+}
+
+// "last block" ticket: true in every thread of the block that finishes last
+__device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int total) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int t = atomicAdd(counter, 1u);
+    last = (t == total - 1);
+    if (last) *counter = 0;  // reset for the next launch
+  }
+  __syncthreads();
+  return last;
+}
+
+}  // namespace mgpu

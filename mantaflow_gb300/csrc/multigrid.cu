@@ -1,16 +1,928 @@
-// Multigrid preconditioner (placeholder until the GPU hierarchy lands).
+// Multigrid preconditioner on the GPU: GridMg (multigrid.cpp:220-954), the
+// Galerkin multigrid of Dick, Rogowsky and Westermann (2015) without topology
+// awareness, as the reference ships it.
+//
+// Hierarchy.  Level sizes (n+2)/2 per axis until every side is <= 5 or a
+// level has <= 1000 vertices (multigrid.cpp:240-265).  Level 0 is the
+// pressure matrix itself, held as the 16-bit Poisson code of pressure.cu
+// (A0 count, fluid bit, -1 links) plus two bits: vertex active (A0 != 0) and
+// "trivial" (A0 == 1 without links, whose row and right-hand side are scaled
+// by 1e-6, multigrid.cpp:345-347, 377-382).  With ghost fluid the float
+// diagonal is kept beside it.  Coarse levels store their symmetric 27-point
+// (3D) / 9-point (2D) Galerkin stencils as 14 / 5 planes of n floats
+// (structure of arrays, so neighbouring threads read neighbouring words),
+// plus a byte of vertex type and x, b, r vectors.
+//
+// Setup (GridMg::setA, multigrid.cpp:386-415).  The coarse-vertex selection
+// (genCoarseGrid, :520-578) is a sequential bucket-queue algorithm whose
+// order decides which coarse vertices survive, so it runs on the host on the
+// vertex-type bytes of the finer level, keeping the reference's queue order.
+// It depends only on the level-0 types: a selection is reused while they are
+// unchanged (a PcMGDynamic solve on unchanged flags rebuilds only the
+// operators).  The Galerkin operators R*A*I (knGenCoarseGridOperator,
+// :580-657) are computed on the GPU, one thread per coarse vertex, adding
+// the same terms in the same order as the reference (level 1 walks the
+// reference's sorted table of fine-grid paths).
+//
+// V-cycle (doVCycle, :448-504; V(1,1), zero initial guess).  Gauss-Seidel
+// colour passes are one launch per colour: red/black on level 0 (7-point
+// stencil), eight (four in 2D) 2x2x2 block colours on coarse levels.  Within
+// a colour every vertex reads only other colours, so each pass reproduces the
+// reference's float arithmetic exactly; restriction and interpolation sum
+// their terms in the reference's loop order.  The coarsest level is solved by
+// Jacobi-preconditioned CG in double (solveCG, :793-902) by one CTA with the
+// vectors in shared memory; its dot products are tree sums, so it differs
+// from the serial reference only in the last bits of double rounding.
 #include "mg_multigrid.h"
+#include "mg_reduce.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
 
 namespace mgpu {
 
-struct MgHierarchy {
-  Dims d;
+namespace {
+
+enum : int8_t { kVtInactive = 0, kVtActive = 1, kVtTrivial = 2 };
+// level-0 bits above the Poisson code (bits 0-9)
+enum : int { kMgActive = 1 << 10, kMgTrivial = 1 << 11 };
+constexpr float kTrivialScale = 1e-6f;  // GridMg::mTrivialEquationScale
+constexpr int kMaxLevels = 32;
+constexpr int kCgThreads = 1024;        // coarsest level: <= 1000 vertices
+constexpr int kThreads1 = 256;
+const dim3 kBlk0(32, 8, 1);
+
+// a coarse level (l >= 1)
+struct Lev {
+  int sx, sy, sz;
+  long long n, py, pz;
+  int8_t* type;
+  float* A;  // stencil entry s of vertex v at A[s * n + v]
+  float* x;
+  float* b;
+  float* r;
 };
 
-MgHierarchy* mg_hierarchy_create(const Dims& d) { return new MgHierarchy{d}; }
-void mg_hierarchy_destroy(MgHierarchy* h) { delete h; }
-size_t mg_hierarchy_bytes(const MgHierarchy*) { return 0; }
-int mg_setup(MgHierarchy*, const PcgBuffers&, float, cudaStream_t) { return 1; }
-int mg_apply(MgHierarchy*, const PcgBuffers&, bool, cudaStream_t) { return 1; }
+// level 0: snapshot of the Poisson matrix taken by setA
+struct Lev0 {
+  Dims d;
+  uint16_t* code;  // Poisson code | kMgActive | kMgTrivial
+  float* a0f;      // trivial-scaled float diagonal (ghost fluid) or null
+  float* r;        // residual
+};
+
+// One term of the level-1 Galerkin product (knGenCoarseGridOperator, level
+// 1 branch): coarse neighbour N = V + n, fine vertices U = 2V + u and W = 2V
+// + w, fine stencil entry sf taken at U (inU) or W, weights rw / iw, added
+// into coarse entry sc.  Built once per dimension like the reference's
+// precomputed path list, sorted by (sc, U).
+struct Path {
+  signed char n[3], u[3], w[3];
+  signed char sc, sf, inU;
+  float rw, iw;
+};
+constexpr int kMaxPaths = 512;
+__constant__ Path c_paths[2][kMaxPaths];  // [0] 2D, [1] 3D
+int g_npaths[2] = {0, 0};
+bool g_pathsReady = false;
+
+__host__ __device__ __forceinline__ int parity3(int a, int b, int c) { return (a & 1) + (b & 1) + (c & 1); }
+__host__ __device__ __forceinline__ float inv_pow2(int e) { return 1.f / (float)(1 << e); }
+
+__device__ __forceinline__ float l0_diag(int c, const float* __restrict__ a0f, long long v) {
+  if (a0f) return a0f[v];
+  return (c & kMgTrivial) ? kTrivialScale : (float)(c & 7);
+}
+__device__ __forceinline__ float l0_rhs(int c, const float* __restrict__ res, long long v) {
+  const float b = res[v];
+  return (c & kMgTrivial) ? b * kTrivialScale : b;
+}
+// fine-level stencil entry sf of level-0 vertex u: A0, Ai, Aj, Ak
+__device__ __forceinline__ float l0_entry(const Lev0& F, long long u, int sf) {
+  const int c = F.code[u];
+  if (sf == 0) return l0_diag(c, F.a0f, u);
+  const int bit = sf == 1 ? kHighX : (sf == 2 ? kHighY : kHighZ);
+  return (c & bit) ? -1.f : 0.f;
+}
+
+__device__ __forceinline__ long long lin(const Lev& L, int x, int y, int z) { return x + L.py * y + L.pz * z; }
+__device__ __forceinline__ bool inside(const Lev& L, int x, int y, int z) {
+  return x >= 0 && y >= 0 && z >= 0 && x < L.sx && y < L.sy && z < L.sz;
+}
+__device__ __forceinline__ void coords(const Lev& L, long long v, int& x, int& y, int& z) {
+  x = (int)(v % L.sx);
+  y = (int)((v / L.sx) % L.sy);
+  z = (int)(v / L.pz);
+}
+
+#define GRID_STRIDE(v, n) \
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < (n); v += (long long)gridDim.x * blockDim.x)
+
+// ---------------------------------------------------------------- setup
+// knCopyA + knActivateVertices (multigrid.cpp:333-384)
+__global__ void k_mg_snapshot0(Dims d, const code_t* __restrict__ code, const float* __restrict__ A0f, uint16_t* code0,
+                               float* a0f0, int8_t* type0) {
+  GRID_STRIDE(v, d.n) {
+    int c = code[v] & 0x3ff;
+    float a0 = A0f ? A0f[v] : (float)(c & 7);
+    int8_t t = kVtInactive;
+    if (a0 != 0.f) {
+      t = kVtActive;
+      c |= kMgActive;
+      const int links = c & (kLowX | kLowY | kLowZ | kHighX | kHighY | kHighZ);
+      if (a0 == 1.f && !links) {
+        t = kVtTrivial;
+        c |= kMgTrivial;
+        a0 = a0 * kTrivialScale;
+      }
+    }
+    code0[v] = (uint16_t)c;
+    if (a0f0) a0f0[v] = a0;
+    type0[v] = t;
+  }
+}
+
+// knGenCoarseGridOperator, level 1 from the 7-point level 0 (paths)
+template <bool IS3D>
+__global__ void k_mg_coarse_op1(Lev C, Lev0 F, int S, int npaths) {
+  const Path* P = c_paths[IS3D ? 1 : 0];
+  const int fx = F.d.nx, fy = F.d.ny, fz = F.d.nz;
+  GRID_STRIDE(v, C.n) {
+    if (C.type[v] == kVtInactive) continue;
+    int vx, vy, vz;
+    coords(C, v, vx, vy, vz);
+    int cur = 0;
+    float acc = 0.f;
+    for (int q = 0; q < npaths; q++) {
+      const Path& p = P[q];
+      if (p.sc != cur) {
+        C.A[(long long)cur * C.n + v] = acc;
+        for (int e = cur + 1; e < p.sc; e++) C.A[(long long)e * C.n + v] = 0.f;
+        cur = p.sc;
+        acc = 0.f;
+      }
+      const int nx = vx + p.n[0], ny = vy + p.n[1], nz = vz + p.n[2];
+      if (!inside(C, nx, ny, nz) || C.type[lin(C, nx, ny, nz)] == kVtInactive) continue;
+      const int ux = 2 * vx + p.u[0], uy = 2 * vy + p.u[1], uz = 2 * vz + p.u[2];
+      if (ux < 0 || uy < 0 || uz < 0 || ux >= fx || uy >= fy || uz >= fz) continue;
+      const long long u = ix(F.d, ux, uy, uz);
+      if (!(F.code[u] & kMgActive)) continue;
+      const int wx = 2 * vx + p.w[0], wy = 2 * vy + p.w[1], wz = 2 * vz + p.w[2];
+      if (wx < 0 || wy < 0 || wz < 0 || wx >= fx || wy >= fy || wz >= fz) continue;
+      const long long w = ix(F.d, wx, wy, wz);
+      if (!(F.code[w] & kMgActive)) continue;
+      const float a = l0_entry(F, p.inU ? u : w, p.sf);
+      acc = acc + (p.rw * a) * p.iw;
+    }
+    C.A[(long long)cur * C.n + v] = acc;
+    for (int e = cur + 1; e < S; e++) C.A[(long long)e * C.n + v] = 0.f;
+  }
+}
+
+// knGenCoarseGridOperator, levels >= 2 from a 27-point (9-point) level
+template <bool IS3D>
+__global__ void k_mg_coarse_op(Lev C, Lev F, int S) {
+  constexpr int SZ = IS3D ? 1 : 0;  // stencil half-extent in z
+  GRID_STRIDE(v, C.n) {
+    if (C.type[v] == kVtInactive) continue;
+    float A[14];
+#pragma unroll
+    for (int e = 0; e < 14; e++) A[e] = 0.f;
+    int vx, vy, vz;
+    coords(C, v, vx, vy, vz);
+    const int ulo[3] = {max(0, 2 * vx - 1), max(0, 2 * vy - 1), max(0, 2 * vz - 1)};
+    const int uhi[3] = {min(F.sx - 1, 2 * vx + 1), min(F.sy - 1, 2 * vy + 1), min(F.sz - 1, 2 * vz + 1)};
+    for (int uz = ulo[2]; uz <= uhi[2]; uz++)
+      for (int uy = ulo[1]; uy <= uhi[1]; uy++)
+        for (int ux = ulo[0]; ux <= uhi[0]; ux++) {
+          const long long u = lin(F, ux, uy, uz);
+          if (F.type[u] == kVtInactive) continue;
+          const float rw = inv_pow2(parity3(ux, uy, uz));
+          const int nlo[3] = {(ux - 1) / 2, (uy - 1) / 2, (uz - 1) / 2};
+          const int nhi[3] = {min(C.sx - 1, (ux + 2) / 2), min(C.sy - 1, (uy + 2) / 2), min(C.sz - 1, (uz + 2) / 2)};
+          for (int nz = nlo[2]; nz <= nhi[2]; nz++)
+            for (int ny = nlo[1]; ny <= nhi[1]; ny++)
+              for (int nx = nlo[0]; nx <= nhi[0]; nx++) {
+                const long long nn = lin(C, nx, ny, nz);
+                if (C.type[nn] == kVtInactive) continue;
+                const int sc = (nx - vx + 1) + 3 * (ny - vy + 1) + 9 * (nz - vz + SZ);
+                if (sc < S - 1) continue;
+                const int wlo[3] = {max(0, max(ux - 1, 2 * nx - 1)), max(0, max(uy - 1, 2 * ny - 1)),
+                                    max(0, max(uz - 1, 2 * nz - 1))};
+                const int whi[3] = {min(F.sx - 1, min(ux + 1, 2 * nx + 1)), min(F.sy - 1, min(uy + 1, 2 * ny + 1)),
+                                    min(F.sz - 1, min(uz + 1, 2 * nz + 1))};
+                for (int wz = wlo[2]; wz <= whi[2]; wz++)
+                  for (int wy = wlo[1]; wy <= whi[1]; wy++)
+                    for (int wx = wlo[0]; wx <= whi[0]; wx++) {
+                      const long long w = lin(F, wx, wy, wz);
+                      if (F.type[w] == kVtInactive) continue;
+                      const int sf = (wx - ux + 1) + 3 * (wy - uy + 1) + 9 * (wz - uz + SZ);
+                      const float iw = inv_pow2(parity3(wx, wy, wz));
+                      const float a = sf < S ? F.A[(long long)(S - 1 - sf) * F.n + w] : F.A[(long long)(sf - S + 1) * F.n + u];
+                      A[sc - S + 1] = A[sc - S + 1] + (rw * a) * iw;
+                    }
+              }
+        }
+    for (int e = 0; e < S; e++) C.A[(long long)e * C.n + v] = A[e];
+  }
+}
+
+// ------------------------------------------------------------ V-cycle
+// Sum over the 27 (9) stencil neighbours of a coarse vertex, in the
+// reference's FOR_VECLIN_MINMAX order (x fastest): sum -= A * x[N].
+template <bool IS3D, bool SKIP_CENTER>
+__device__ __forceinline__ float stencil_sub(const Lev& L, int S, int vx, int vy, int vz, long long v, float sum) {
+  constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
+  int s = 0;
+#pragma unroll
+  for (int dz = ZL; dz <= ZH; dz++)
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+      for (int dx = -1; dx <= 1; dx++, s++) {
+        if (SKIP_CENTER && s == S - 1) continue;
+        const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
+        if (!inside(L, nx, ny, nz)) continue;
+        const long long nn = lin(L, nx, ny, nz);
+        if (L.type[nn] == kVtInactive) continue;
+        const float a = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
+        sum = sum - a * L.x[nn];
+      }
+  return sum;
+}
+
+// knSmoothColor on level 0 (7-point stencil; colour = parity of i+j+k).
+// MODE 0: first pass of a V-cycle, x = 0 before it: every cell is written,
+// cells of the colour get b/A0 (their neighbours are all zero) and the rest 0.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_mg0_smooth(Lev0 F, const float* __restrict__ res, float* x, int color,
+                                                    const CgScalars* sc) {
+  if (sc->done) return;
+  const Dims& d = F.d;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  const long long v = ix(d, i, j, k);
+  const int c = F.code[v];
+  const bool mine = ((i + j + k) & 1) == color && (c & kMgActive);
+  if (MODE == 0) {
+    x[v] = mine ? l0_rhs(c, res, v) / l0_diag(c, F.a0f, v) : 0.f;
+    return;
+  }
+  if (!mine) return;
+  // sum -= A*x with A = -1 on a link and 0 otherwise (interior cells only
+  // carry links, so every neighbour is inside the grid)
+  float sum = l0_rhs(c, res, v);
+  if (c & kLowX) sum = sum + x[v - 1];
+  if (c & kHighX) sum = sum + x[v + 1];
+  if (c & kLowY) sum = sum + x[v - d.sy];
+  if (c & kHighY) sum = sum + x[v + d.sy];
+  if (c & kLowZ) sum = sum + x[v - d.sz];
+  if (c & kHighZ) sum = sum + x[v + d.sz];
+  x[v] = sum / l0_diag(c, F.a0f, v);
+}
+
+// knCalcResidual on level 0
+__global__ void __launch_bounds__(256) k_mg0_residual(Lev0 F, const float* __restrict__ res, const float* __restrict__ x,
+                                                      const CgScalars* sc) {
+  if (sc->done) return;
+  const Dims& d = F.d;
+  GRID_STRIDE(v, d.n) {
+    const int c = F.code[v];
+    if (!(c & kMgActive)) continue;
+    float sum = l0_rhs(c, res, v);
+    if (c & kLowX) sum = sum + x[v - 1];
+    if (c & kHighX) sum = sum + x[v + 1];
+    if (c & kLowY) sum = sum + x[v - d.sy];
+    if (c & kHighY) sum = sum + x[v + d.sy];
+    if (c & kLowZ) sum = sum + x[v - d.sz];
+    if (c & kHighZ) sum = sum + x[v + d.sz];
+    sum = sum - l0_diag(c, F.a0f, v) * x[v];
+    F.r[v] = sum;
+  }
+}
+
+// knSmoothColor on a coarse level: colour offset (ox, oy, oz) in 2x2x2 blocks
+template <bool IS3D>
+__global__ void __launch_bounds__(256) k_mg_smooth(Lev L, int S, int ox, int oy, int oz, const CgScalars* sc) {
+  if (sc->done) return;
+  const int bx = (L.sx + 1) / 2, by = (L.sy + 1) / 2, bz = (L.sz + 1) / 2;
+  const long long nb = (long long)bx * by * bz;
+  GRID_STRIDE(bi, nb) {
+    const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
+    if (!inside(L, vx, vy, vz)) continue;
+    const long long v = lin(L, vx, vy, vz);
+    if (L.type[v] == kVtInactive) continue;
+    const float sum = stencil_sub<IS3D, true>(L, S, vx, vy, vz, v, L.b[v]);
+    L.x[v] = sum / L.A[v];
+  }
+}
+
+// knCalcResidual on a coarse level
+template <bool IS3D>
+__global__ void __launch_bounds__(256) k_mg_residual(Lev L, int S, const CgScalars* sc) {
+  if (sc->done) return;
+  GRID_STRIDE(v, L.n) {
+    if (L.type[v] == kVtInactive) continue;
+    int vx, vy, vz;
+    coords(L, v, vx, vy, vz);
+    L.r[v] = stencil_sub<IS3D, false>(L, S, vx, vy, vz, v, L.b[v]);
+  }
+}
+
+// knRestrict into level D from the level below (level 0 when FROM0), plus
+// knSet(x[D], 0) of the next smoothing's initial guess
+template <bool FROM0>
+__global__ void __launch_bounds__(256) k_mg_restrict(Lev D, Lev S, Lev0 F, const CgScalars* sc) {
+  if (sc->done) return;
+  const int sx = FROM0 ? F.d.nx : S.sx, sy = FROM0 ? F.d.ny : S.sy, sz = FROM0 ? F.d.nz : S.sz;
+  const long long py = FROM0 ? F.d.sy : S.py, pz = FROM0 ? F.d.sz : S.pz;
+  GRID_STRIDE(v, D.n) {
+    D.x[v] = 0.f;
+    if (D.type[v] == kVtInactive) continue;
+    int vx, vy, vz;
+    coords(D, v, vx, vy, vz);
+    const int lx = max(0, 2 * vx - 1), ly = max(0, 2 * vy - 1), lz = max(0, 2 * vz - 1);
+    const int hx = min(sx - 1, 2 * vx + 1), hy = min(sy - 1, 2 * vy + 1), hz = min(sz - 1, 2 * vz + 1);
+    float sum = 0.f;
+    for (int rz = lz; rz <= hz; rz++)
+      for (int ry = ly; ry <= hy; ry++)
+        for (int rx = lx; rx <= hx; rx++) {
+          const long long r = rx + py * ry + pz * rz;
+          float rv;
+          if (FROM0) {
+            if (!(F.code[r] & kMgActive)) continue;
+            rv = F.r[r];
+          } else {
+            if (S.type[r] == kVtInactive) continue;
+            rv = S.r[r];
+          }
+          sum = sum + inv_pow2(parity3(rx, ry, rz)) * rv;
+        }
+    D.b[v] = sum;
+  }
+}
+
+// knInterpolate from level S = D+1 and knAddAssign: x[D] += I * x[S]
+// (into the level-0 result x0 when TO0)
+template <bool TO0>
+__global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev0 F, float* x0, Lev S, const CgScalars* sc) {
+  if (sc->done) return;
+  const long long n = TO0 ? F.d.n : D.n;
+  GRID_STRIDE(v, n) {
+    int vx, vy, vz;
+    if (TO0) {
+      if (!(F.code[v] & kMgActive)) continue;
+      vx = (int)(v % F.d.nx);
+      vy = (int)((v / F.d.nx) % F.d.ny);
+      vz = F.d.is3d ? (int)(v / F.d.sz) : 0;
+    } else {
+      if (D.type[v] == kVtInactive) continue;
+      coords(D, v, vx, vy, vz);
+    }
+    float sum = 0.f;
+    for (int iz = vz / 2; iz <= (vz + 1) / 2; iz++)
+      for (int iy = vy / 2; iy <= (vy + 1) / 2; iy++)
+        for (int ixx = vx / 2; ixx <= (vx + 1) / 2; ixx++) {
+          const long long q = lin(S, ixx, iy, iz);
+          if (S.type[q] != kVtInactive) sum = sum + S.x[q];
+        }
+    const float r = inv_pow2(parity3(vx, vy, vz)) * sum;
+    float* xd = TO0 ? x0 : D.x;
+    xd[v] = xd[v] + r;
+  }
+}
+
+// all threads: sum of one double per thread, in a fixed order
+__device__ __forceinline__ double cta_allsum(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = 0.;
+  for (int q = 0; q < nw; q++) t += red[q];
+  __syncthreads();
+  return t;
+}
+__device__ __forceinline__ void cta_allsum2(double& a, double& b, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if (lane == 0) {
+    red[wid] = a;
+    red[32 + wid] = b;
+  }
+  __syncthreads();
+  double ta = 0., tb = 0.;
+  for (int q = 0; q < nw; q++) {
+    ta += red[q];
+    tb += red[32 + q];
+  }
+  __syncthreads();
+  a = ta;
+  b = tb;
+}
+
+// applyAStencil of solveCG: the level-0 or coarse stencil in double
+template <bool IS3D, bool L0>
+__device__ __forceinline__ double cg_apply(const Lev& L, const Lev0& F, int S, int v, int c, float diag, const double* p) {
+  double sum = 0.;
+  if (L0) {
+    const Dims& d = F.d;
+    if (c & kLowX) sum += -p[v - 1];
+    if (c & kHighX) sum += -p[v + 1];
+    if (c & kLowY) sum += -p[v - d.sy];
+    if (c & kHighY) sum += -p[v + d.sy];
+    if (c & kLowZ) sum += -p[v - d.sz];
+    if (c & kHighZ) sum += -p[v + d.sz];
+    sum += (double)diag * p[v];
+  } else {
+    constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
+    int vx, vy, vz;
+    coords(L, v, vx, vy, vz);
+    int s = 0;
+#pragma unroll
+    for (int dz = ZL; dz <= ZH; dz++)
+#pragma unroll
+      for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+        for (int dx = -1; dx <= 1; dx++, s++) {
+          const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
+          if (!inside(L, nx, ny, nz)) continue;
+          const int nn = (int)lin(L, nx, ny, nz);
+          if (L.type[nn] == kVtInactive) continue;
+          const float a = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
+          sum += (double)a * p[nn];
+        }
+  }
+  return sum;
+}
+
+// GridMg::solveCG on the coarsest level: Jacobi-PCG in double, one CTA,
+// one vertex per thread
+template <bool IS3D, bool L0>
+__global__ void __launch_bounds__(kCgThreads) k_mg_coarse_cg(Lev L, Lev0 F, const float* __restrict__ res, float* x0, int S,
+                                                             float accuracy, const CgScalars* sc) {
+  if (sc->done) return;
+  __shared__ double sp[kCgThreads];
+  __shared__ double red[64];
+  const int n = L0 ? (int)F.d.n : (int)L.n;
+  const int v = threadIdx.x;
+  bool act = false;
+  int c = 0;
+  float diag = 1.f, bv = 0.f;
+  if (v < n) {
+    if (L0) {
+      c = F.code[v];
+      act = (c & kMgActive) != 0;
+      if (act) {
+        diag = l0_diag(c, F.a0f, v);
+        bv = l0_rhs(c, res, v);
+      }
+    } else {
+      act = L.type[v] != kVtInactive;
+      if (act) {
+        diag = L.A[v];
+        bv = L.b[v];
+      }
+    }
+  }
+  // x = mx[l] = 0, so r = b - A*0 = b
+  double x = 0., r = 0., z = 0., p = 0.;
+  if (act) {
+    r = (double)bv;
+    z = r / (double)diag;
+    p = z;
+  }
+  sp[v] = p;
+  double ir = r * r, alphaTop = r * z;
+  cta_allsum2(ir, alphaTop, red);  // its barriers also publish sp
+  const double initialResidual = sqrt(ir);
+  for (int iter = 0; iter < 10000 && initialResidual > 1E-12; iter++) {
+    const double q = act ? cg_apply<IS3D, L0>(L, F, S, v, c, diag, sp) : 0.;
+    const double alphaBot = cta_allsum(act ? p * q : 0., red);
+    const double alpha = alphaTop / alphaBot;
+    double rr = 0., rz = 0.;
+    if (act) {
+      x += alpha * p;
+      r -= alpha * q;
+      z = r / (double)diag;
+      rr = r * r;
+      rz = r * z;
+    }
+    cta_allsum2(rr, rz, red);
+    const double residual = sqrt(rr);
+    if (residual / initialResidual < (double)accuracy) break;
+    const double beta = rz / alphaTop;
+    alphaTop = rz;
+    p = z + beta * p;
+    sp[v] = p;
+    __syncthreads();
+  }
+  if (v < n) {
+    if (L0) x0[v] = (float)x;
+    else L.x[v] = (float)x;
+  }
+}
+
+// sigmaNew = dot(tmp, residual) and beta (GridCg::iterate after the
+// preconditioner, conjugategrad.cpp:277-299)
+__global__ void __launch_bounds__(256) k_mg_dot_beta(long long n, const float* __restrict__ t, const float* __restrict__ r,
+                                                     double* part, CgScalars* sc) {
+  if (sc->done) return;
+  double acc = 0.;
+  GRID_STRIDE(idx, n) acc += (double)(t[idx] * r[idx]);
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
+  if (last_block(&sc->counters[4], gridDim.x)) {
+    const double s = sum_partials(part, gridDim.x);
+    if (threadIdx.x != 0) return;
+    const float sigmaNew = (float)s;
+    sc->beta = sigmaNew / sc->sigma;
+    sc->sigma = sigmaNew;
+    if (!(sc->resNorm < 1e35f)) {
+      sc->status = 2;
+      sc->done = 1;
+    }
+  }
+}
+
+// ------------------------------------------------------------- host side
+// The reference's precomputed coarsening paths (GridMg ctor,
+// multigrid.cpp:285-318) around the coarse vertex V = (1,1,1), sorted by
+// coarse entry and fine vertex.
+void build_paths(int dim, std::vector<Path>& out) {
+  static const int p7[7][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+  const int smin[3] = {-1, -1, dim == 3 ? -1 : 0}, smax[3] = {1, 1, dim == 3 ? 1 : 0};
+  const int V[3] = {1, 1, 1};
+  struct Tmp {
+    Path p;
+    int key;
+  };
+  std::vector<Tmp> t;
+  int U[3];
+  for (U[2] = 2 * V[2] + smin[2]; U[2] <= 2 * V[2] + smax[2]; U[2]++)
+    for (U[1] = 2 * V[1] + smin[1]; U[1] <= 2 * V[1] + smax[1]; U[1]++)
+      for (U[0] = 2 * V[0] + smin[0]; U[0] <= 2 * V[0] + smax[0]; U[0]++)
+        for (int i = 0; i < 1 + 2 * dim; i++) {
+          const int W[3] = {U[0] + p7[i][0], U[1] + p7[i][1], U[2] + p7[i][2]};
+          int N[3];
+          for (N[2] = W[2] / 2; N[2] <= (W[2] + 1) / 2; N[2]++)
+            for (N[1] = W[1] / 2; N[1] <= (W[1] + 1) / 2; N[1]++)
+              for (N[0] = W[0] / 2; N[0] <= (W[0] + 1) / 2; N[0]++) {
+                const int s = N[0] + 3 * N[1] + 9 * N[2];
+                if (s < 13) continue;
+                Tmp e;
+                for (int c = 0; c < 3; c++) {
+                  e.p.n[c] = (signed char)(N[c] - V[c]);
+                  e.p.u[c] = (signed char)(U[c] - 2 * V[c]);
+                  e.p.w[c] = (signed char)(W[c] - 2 * V[c]);
+                }
+                e.p.sc = (signed char)(s - 13);
+                e.p.sf = (signed char)((i + 1) / 2);
+                e.p.inU = (signed char)(i % 2 == 0);
+                e.p.rw = inv_pow2(parity3(U[0], U[1], U[2]));
+                e.p.iw = inv_pow2(parity3(W[0], W[1], W[2]));
+                e.key = (U[0] - 2 * V[0] + 1) + 3 * (U[1] - 2 * V[1] + 1) + 9 * (U[2] - 2 * V[2] + 1);
+                t.push_back(e);
+              }
+        }
+  // std::sort with the reference's comparator (coarse entry, then fine
+  // vertex): elements with equal keys keep the order std::sort gives them
+  std::sort(t.begin(), t.end(), [](const Tmp& a, const Tmp& b) {
+    if (a.p.sc == b.p.sc) return a.key < b.key;
+    return a.p.sc < b.p.sc;
+  });
+  out.clear();
+  for (auto& e : t) out.push_back(e.p);
+}
+
+int ensure_paths() {
+  if (g_pathsReady) return 0;
+  for (int dim = 2; dim <= 3; dim++) {
+    std::vector<Path> p;
+    build_paths(dim, p);
+    if ((int)p.size() > kMaxPaths) return 1;
+    g_npaths[dim - 2] = (int)p.size();
+    if (cudaMemcpyToSymbol(c_paths, p.data(), p.size() * sizeof(Path), (size_t)(dim - 2) * kMaxPaths * sizeof(Path)) !=
+        cudaSuccess)
+      return 1;
+  }
+  g_pathsReady = true;
+  return 0;
+}
+
+// genCoarseGrid (multigrid.cpp:520-578): every active fine vertex starts
+// with the number of coarse vertices it can interpolate from (2^#odd
+// coordinates) as key; repeatedly the vertex with the fewest free coarse
+// parents is taken, its first free parent becomes a coarse vertex and the
+// others are removed, and every fine vertex near a decided parent loses one
+// from its key.  Keys are 1..8, held as buckets of doubly linked lists with
+// insertion at the head; the next vertex is the head of the lowest non-empty
+// bucket -- the order the reference's NKMinHeap yields.
+void gen_coarse_grid(const int fs[3], const std::vector<int8_t>& tf, const int cs[3], std::vector<int8_t>& tc) {
+  enum : int8_t { kFree = 5, kZero = 4, kRemoved = 3 };
+  const long long nf = (long long)fs[0] * fs[1] * fs[2];
+  const long long nc = (long long)cs[0] * cs[1] * cs[2];
+  const long long fpy = fs[0], fpz = (long long)fs[0] * fs[1];
+  const long long cpy = cs[0], cpz = (long long)cs[0] * cs[1];
+  tc.assign((size_t)nc, kFree);
+  constexpr int kBuckets = 9;
+  std::vector<int> key((size_t)nf, -1), prv((size_t)nf), nxt((size_t)nf);
+  int head[kBuckets];
+  for (int b = 0; b < kBuckets; b++) head[b] = -1;
+  int count = 0;
+  // node ids: >= 0 vertices; prv == -(b+1) marks the head of bucket b
+  auto unlink = [&](int id) {
+    const int p = prv[id], q = nxt[id];
+    if (p < 0) head[-p - 1] = q;
+    else nxt[p] = q;
+    if (q >= 0) prv[q] = p;
+    count--;
+  };
+  auto set_key = [&](int id, int k) {
+    if (key[id] == k) return;
+    if (key[id] != -1) unlink(id);
+    key[id] = k;
+    if (k == -1) return;
+    const int h = head[k];
+    prv[id] = -(k + 1);
+    nxt[id] = h;
+    if (h >= 0) prv[h] = id;
+    head[k] = id;
+    count++;
+  };
+  for (long long v = 0; v < nf; v++) {
+    if (tf[(size_t)v] == kVtInactive) continue;
+    const int x = (int)(v % fs[0]), y = (int)((v / fpy) % fs[1]), z = (int)(v / fpz);
+    set_key((int)v, 1 << parity3(x, y, z));
+  }
+  while (count > 0) {
+    int b = 1;
+    while (head[b] < 0) b++;
+    const int v = head[b];
+    unlink(v);
+    key[v] = -1;
+    const int X = (int)(v % fs[0]), Y = (int)((v / fpy) % fs[1]), Z = (int)(v / fpz);
+    bool vdone = false;
+    for (int iz = Z / 2; iz <= (Z + 1) / 2; iz++)
+      for (int iy = Y / 2; iy <= (Y + 1) / 2; iy++)
+        for (int ixx = X / 2; ixx <= (X + 1) / 2; ixx++) {
+          const long long i = ixx + cpy * iy + cpz * iz;
+          if (tc[(size_t)i] != kFree) continue;
+          if (vdone) tc[(size_t)i] = kRemoved;
+          else {
+            tc[(size_t)i] = kZero;
+            vdone = true;
+          }
+          const int lx = std::max(0, ixx * 2 - 1), hx = std::min(fs[0] - 1, ixx * 2 + 1);
+          const int ly = std::max(0, iy * 2 - 1), hy = std::min(fs[1] - 1, iy * 2 + 1);
+          const int lz = std::max(0, iz * 2 - 1), hz = std::min(fs[2] - 1, iz * 2 + 1);
+          for (int rz = lz; rz <= hz; rz++)
+            for (int ry = ly; ry <= hy; ry++)
+              for (int rx = lx; rx <= hx; rx++) {
+                const int r = (int)(rx + fpy * ry + fpz * rz);
+                const int k = key[r];
+                if (k > 1) set_key(r, k - 1);
+                else if (k > -1) set_key(r, -1);
+              }
+        }
+  }
+  for (long long i = 0; i < nc; i++) {
+    int8_t& t = tc[(size_t)i];
+    t = (t == kZero) ? kVtActive : kVtInactive;
+  }
+}
+
+int blocks_for(long long n) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+  }
+  const long long b = (n + kThreads1 - 1) / kThreads1;
+  return (int)std::max(1LL, std::min(b, (long long)sms * 8));
+}
+
+}  // namespace
+
+struct MgHierarchy {
+  Dims d;
+  int nlev = 0, is3d = 0, S = 0;
+  int size[kMaxLevels][3];
+  Lev lev[kMaxLevels];
+  Lev0 l0;
+  int8_t* type0 = nullptr;
+  std::vector<int8_t> htype[kMaxLevels];
+  std::vector<int8_t> selType0;  // level-0 types the current selection was made for
+  bool selValid = false;
+  bool isASet = false;
+  bool useA0f = false;  // the snapshot has a float diagonal (ghost fluid)
+  float coarseAcc = 1e-8f;
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+  bool ok = true;
+
+  template <typename T>
+  T* alloc(long long count) {
+    void* p = nullptr;
+    const size_t nb = sizeof(T) * (size_t)std::max(1LL, count);
+    if (cudaMalloc(&p, nb) != cudaSuccess) {
+      ok = false;
+      return nullptr;
+    }
+    cudaMemset(p, 0, nb);
+    allocs.push_back(p);
+    bytes += nb;
+    return (T*)p;
+  }
+};
+
+MgHierarchy* mg_hierarchy_create(const Dims& d) {
+  if (ensure_paths()) return nullptr;
+  MgHierarchy* h = new MgHierarchy();
+  h->d = d;
+  h->is3d = d.is3d;
+  h->S = d.is3d ? 14 : 5;
+  // level sizes (GridMg ctor, multigrid.cpp:240-265)
+  h->size[0][0] = d.nx;
+  h->size[0][1] = d.ny;
+  h->size[0][2] = d.nz;
+  int L = 1;
+  long long n = d.n;
+  for (int l = 1; l <= 100 && l < kMaxLevels; l++) {
+    if (h->size[l - 1][0] <= 5 && h->size[l - 1][1] <= 5 && h->size[l - 1][2] <= 5) break;
+    if (n <= 1000) break;
+    for (int c = 0; c < 3; c++) h->size[l][c] = (h->size[l - 1][c] + 2) / 2;
+    n = (long long)h->size[l][0] * h->size[l][1] * h->size[l][2];
+    L = l + 1;
+  }
+  h->nlev = L;
+  const long long n0 = d.n;
+  h->l0.d = d;
+  h->l0.code = h->alloc<uint16_t>(n0);
+  h->l0.a0f = nullptr;
+  h->l0.r = L > 1 ? h->alloc<float>(n0) : nullptr;
+  h->type0 = h->alloc<int8_t>(n0);
+  for (int l = 1; l < L; l++) {
+    Lev& v = h->lev[l];
+    v.sx = h->size[l][0];
+    v.sy = h->size[l][1];
+    v.sz = h->size[l][2];
+    v.n = (long long)v.sx * v.sy * v.sz;
+    v.py = v.sx;
+    v.pz = (long long)v.sx * v.sy;
+    v.type = h->alloc<int8_t>(v.n);
+    v.A = h->alloc<float>(v.n * h->S);
+    v.x = h->alloc<float>(v.n);
+    v.b = h->alloc<float>(v.n);
+    v.r = h->alloc<float>(v.n);
+  }
+  const long long nc = L > 1 ? h->lev[L - 1].n : n0;
+  if (nc > kCgThreads) h->ok = false;  // the level loop guarantees <= 1000
+  if (!h->ok) {
+    mg_hierarchy_destroy(h);
+    return nullptr;
+  }
+  return h;
+}
+
+void mg_hierarchy_destroy(MgHierarchy* h) {
+  if (!h) return;
+  for (void* p : h->allocs) cudaFree(p);
+  delete h;
+}
+
+void mg_hierarchy_reset(MgHierarchy* h) {
+  if (h) h->isASet = false;
+}
+
+size_t mg_hierarchy_bytes(const MgHierarchy* h) { return h ? h->bytes : 0; }
+int mg_hierarchy_levels(const MgHierarchy* h) { return h ? h->nlev : 0; }
+
+int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStream_t s) {
+  h->coarseAcc = coarseAccuracy;
+  if (h->isASet) return 0;
+  const Dims& d = h->d;
+  if (b.A0f && !h->l0.a0f) {
+    h->l0.a0f = h->alloc<float>(d.n);
+    if (!h->ok) return 1;
+  }
+  float* a0f = b.A0f ? h->l0.a0f : nullptr;
+  Lev0 l0 = h->l0;
+  l0.a0f = a0f;
+  count_launch();
+  k_mg_snapshot0<<<blocks_for(d.n), kThreads1, 0, s>>>(d, b.code, b.A0f, h->l0.code, a0f, h->type0);
+  if (cudaGetLastError() != cudaSuccess) return 1;
+  h->useA0f = a0f != nullptr;
+  if (h->nlev > 1) {
+    // vertex selection on the host, reused while the level-0 types repeat
+    h->htype[0].resize((size_t)d.n);
+    if (cudaMemcpyAsync(h->htype[0].data(), h->type0, (size_t)d.n, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 1;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return 1;
+    for (auto& t : h->htype[0])
+      if (t == kVtTrivial) t = kVtActive;  // genCoarseGrid tests only for inactive
+    const bool reuse = h->selValid && h->selType0 == h->htype[0];
+    if (!reuse) {
+      for (int l = 1; l < h->nlev; l++) {
+        gen_coarse_grid(h->size[l - 1], h->htype[l - 1], h->size[l], h->htype[l]);
+        if (cudaMemcpyAsync(h->lev[l].type, h->htype[l].data(), h->htype[l].size(), cudaMemcpyHostToDevice, s) !=
+            cudaSuccess)
+          return 1;
+      }
+      h->selType0 = h->htype[0];
+      h->selValid = true;
+      if (cudaStreamSynchronize(s) != cudaSuccess) return 1;
+    }
+    // Galerkin operators
+    for (int l = 1; l < h->nlev; l++) {
+      const long long n = h->lev[l].n;
+      count_launch();
+      if (l == 1) {
+        if (h->is3d) k_mg_coarse_op1<true><<<blocks_for(n), kThreads1, 0, s>>>(h->lev[1], l0, h->S, g_npaths[1]);
+        else k_mg_coarse_op1<false><<<blocks_for(n), kThreads1, 0, s>>>(h->lev[1], l0, h->S, g_npaths[0]);
+      } else {
+        if (h->is3d) k_mg_coarse_op<true><<<blocks_for(n), kThreads1, 0, s>>>(h->lev[l], h->lev[l - 1], h->S);
+        else k_mg_coarse_op<false><<<blocks_for(n), kThreads1, 0, s>>>(h->lev[l], h->lev[l - 1], h->S);
+      }
+      if (cudaGetLastError() != cudaSuccess) return 1;
+    }
+  }
+  h->isASet = true;
+  return 0;
+}
+
+int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
+  const Dims& d = h->d;
+  const int L = h->nlev - 1;
+  const int S = h->S;
+  Lev0 l0 = h->l0;
+  if (!h->useA0f) l0.a0f = nullptr;
+  const CgScalars* sc = b.sc;
+  float* x0 = b.tmp;
+  const float* res = b.residual;
+  const Lev none{};
+  const dim3 g0 = grid3(d, kBlk0);
+  static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+  const int ncol = h->is3d ? 8 : 4;
+  auto smooth = [&](int l, bool reversed) {
+    const Lev& v = h->lev[l];
+    const int nb = blocks_for((long long)((v.sx + 1) / 2) * ((v.sy + 1) / 2) * ((v.sz + 1) / 2));
+    for (int q = 0; q < ncol; q++) {
+      const int c = reversed ? ncol - 1 - q : q;
+      count_launch();
+      if (h->is3d) k_mg_smooth<true><<<nb, kThreads1, 0, s>>>(v, S, off[c][0], off[c][1], off[c][2], sc);
+      else k_mg_smooth<false><<<nb, kThreads1, 0, s>>>(v, S, off[c][0], off[c][1], off[c][2], sc);
+    }
+  };
+  if (L == 0) {
+    // a single level: the whole V-cycle is the coarsest-level CG
+    count_launch();
+    if (h->is3d) k_mg_coarse_cg<true, true><<<1, kCgThreads, 0, s>>>(none, l0, res, x0, S, h->coarseAcc, sc);
+    else k_mg_coarse_cg<false, true><<<1, kCgThreads, 0, s>>>(none, l0, res, x0, S, h->coarseAcc, sc);
+  } else {
+    // level 0 pre-smoothing (colour 0 from x = 0, then colour 1)
+    count_launch();
+    k_mg0_smooth<0><<<g0, kBlk0, 0, s>>>(l0, res, x0, 0, sc);
+    count_launch();
+    k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, 1, sc);
+    count_launch();
+    k_mg0_residual<<<blocks_for(d.n), kThreads1, 0, s>>>(l0, res, x0, sc);
+    count_launch();
+    k_mg_restrict<true><<<blocks_for(h->lev[1].n), kThreads1, 0, s>>>(h->lev[1], none, l0, sc);
+    for (int l = 1; l < L; l++) {
+      smooth(l, false);
+      count_launch();
+      if (h->is3d) k_mg_residual<true><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], S, sc);
+      else k_mg_residual<false><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], S, sc);
+      count_launch();
+      k_mg_restrict<false><<<blocks_for(h->lev[l + 1].n), kThreads1, 0, s>>>(h->lev[l + 1], h->lev[l], l0, sc);
+    }
+    count_launch();
+    if (h->is3d) k_mg_coarse_cg<true, false><<<1, kCgThreads, 0, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
+    else k_mg_coarse_cg<false, false><<<1, kCgThreads, 0, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
+    for (int l = L - 1; l >= 1; l--) {
+      count_launch();
+      k_mg_interp_add<false><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], l0, nullptr, h->lev[l + 1], sc);
+      smooth(l, true);
+    }
+    count_launch();
+    k_mg_interp_add<true><<<blocks_for(d.n), kThreads1, 0, s>>>(none, l0, x0, h->lev[1], sc);
+    count_launch();
+    k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, 1, sc);
+    count_launch();
+    k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, 0, sc);
+  }
+  if (!init) {
+    count_launch();
+    k_mg_dot_beta<<<b.nblocks, kThreads1, 0, s>>>(d.n, b.tmp, b.residual, b.part, b.sc);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
 
 }  // namespace mgpu

@@ -1067,10 +1067,9 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   } else {
     maxIter = 100;
     pc = kPcMg;
-    if (s->mg && preconditioner == MG_PC_MG_DYNAMIC) {
-      mg_hierarchy_destroy(s->mg);
-      s->mg = nullptr;
-    }
+    // PcMGDynamic builds the hierarchy for this matrix and forgets it
+    // afterwards; PcMGStatic keeps the first one (pressure.cpp:418-451)
+    if (s->mg && preconditioner == MG_PC_MG_DYNAMIC) mg_hierarchy_reset(s->mg);
     if (!s->mg) {
       s->mg = mg_hierarchy_create(d);
       if (!s->mg) return fail(MG_ERR_NOMEM, "solvePressureSystem: multigrid allocation failed");
@@ -1155,10 +1154,7 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   }
   if (s->scHost->status == 2)
     return fail(MG_ERR_SOLVER, "GridCg::iterate: The CG solver diverged, residual norm > 1e30, stopping.");
-  if (s->mg && preconditioner == MG_PC_MG_DYNAMIC) {
-    mg_hierarchy_destroy(s->mg);
-    s->mg = nullptr;
-  }
+  if (s->mg && preconditioner == MG_PC_MG_DYNAMIC) mg_hierarchy_reset(s->mg);
   return MG_OK;
 }
 

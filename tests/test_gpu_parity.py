@@ -198,6 +198,126 @@ def test_solve_pressure(tag, case, kernel, monkeypatch):
     assert d_gpu <= max(1.05 * d_ref, acc), "divergence %g vs reference %g" % (d_gpu, d_ref)
 
 
+@pytest.mark.parametrize("tag", ["3d", "2d"])
+def test_solve_pressure_sequence(tag):
+    """Every golden pressure case in the generator's order on ONE solver, so
+    the static multigrid hierarchy built by mgstat_a is reused by mgstat_b
+    and the dynamic ones are rebuilt (pressure.cpp:418-451)."""
+    g = load("pressure_" + tag)
+    names = [str(n) for n in g["names"]]
+    s = make_solver(g["flags_smoke"].shape)
+    flags = s.create(m.FlagGrid)
+    vel = s.create(m.MACGrid)
+    p = s.create(m.RealGrid)
+    rhs = s.create(m.RealGrid)
+    phi = grid_from(s, m.LevelsetGrid, g["phi"])
+    pc = {"mic": m.PcMIC, "mgdyn": m.PcMGDynamic, "mgstat": m.PcMGStatic}
+    for idx, name in enumerate(names):
+        base = name.replace("gf_", "")
+        kw = dict(preconditioner=[v for k, v in pc.items() if base.startswith(k)][0])
+        kw.update({k: v for k, v in PRESSURE_CASES.get(name, {}).items() if k != "preconditioner"})
+        if name == "mgdyn_closed_fix":
+            kw.update(zeroPressureFixing=True, cgAccuracy=1e-4)
+        if name == "mgstat_b":
+            kw["cgAccuracy"] = 1e-4
+        if name.startswith("gf_"):
+            flags_a, use_phi = g["flags_liquid"], phi
+            if name == "gf_mic":
+                m.releaseMG(s)
+        else:
+            flags_a, use_phi = (g["flags_closed"] if "closed" in name else g["flags_smoke"]), None
+        v0 = g["vel"]
+        if name == "mgstat_b":
+            v0 = (g["vel"] * 0.5 + 0.1).astype(np.float32)
+        m.copyArrayToGridReal(flags_a, flags)
+        m.copyArrayToGridReal(v0, vel)
+        p.setConst(0.0)
+        m.solvePressure(flags=flags, vel=vel, pressure=p, phi=use_phi, retRhs=rhs, **kw)
+        it, _ = m.lastSolveStats()
+        ref_it = int(g["iters"][idx])
+        assert abs(it - ref_it) <= 1, "%s %s: %d iterations vs reference %d" % (tag, name, it, ref_it)
+        close_bitwise(rhs.numpy(), g["rhs_" + name], "rhs %s" % name)
+        dp = float(np.max(np.abs(p.numpy() - g["p_" + name])))
+        assert dp <= 1e-4, "%s %s pressure off by %g" % (tag, name, dp)
+        vg = vel.numpy()
+        assert np.max(np.abs(vg - g["v_" + name])) <= 1e-4, name
+        acc = kw.get("cgAccuracy", 1e-3)
+        assert divergence(flags_a, vg) <= max(1.05 * divergence(flags_a, g["v_" + name]), acc), name
+
+
+def _obstacle_scene(shape, seed, liquid=False):
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = shape
+    f = np.full((nz, ny, nx), og.FLUID, np.int32)
+    og.init_domain(f, 0)
+    og.fill_grid(f)
+    if liquid:
+        f[:, int(ny * 0.55):, :][f[:, int(ny * 0.55):, :] == og.FLUID] = og.EMPTY
+    else:
+        og.set_open_bound(f, 0, "Y")
+    if nz > 1:
+        f[nz // 4:nz // 2, ny // 5:ny // 2, nx // 3:nx // 2] = og.OBSTACLE
+    else:
+        f[0, ny // 5:ny // 2, nx // 3:nx // 2] = og.OBSTACLE
+    v = (rng.random((nz, ny, nx, 3), dtype=np.float32) - 0.5).astype(np.float32)
+    if nz == 1:
+        v[..., 2] = 0
+    return f, v
+
+
+@pytest.mark.parametrize("shape,pcname", [((70, 66, 62), "static"), ((64, 72, 45), "dynamic"),
+                                          ((33, 17, 90), "static"), ((130, 96, 1), "static"),
+                                          ((61, 203, 1), "dynamic")])
+def test_multigrid_large_against_oracle(shape, pcname):
+    """MG-preconditioned CG on multi-level hierarchies with obstacles and
+    ragged level sizes, 3D and 2D: two solves on one solver (the second one
+    reuses a static hierarchy), pressure, iterations and divergence against
+    the oracle."""
+    f, v = _obstacle_scene(shape, 17)
+    pc_m = m.PcMGStatic if pcname == "static" else m.PcMGDynamic
+    pc_o = og.PC_MG_STATIC if pcname == "static" else og.PC_MG_DYNAMIC
+    nx, ny, nz = shape
+    s = m.Solver(name="mg", gridSize=m.vec3(nx, ny, nz), dim=3 if nz > 1 else 2)
+    flags = grid_from(s, m.FlagGrid, f)
+    vel = s.create(m.MACGrid)
+    p = s.create(m.RealGrid)
+    cache = og.MGCache()
+    for rep, scale in enumerate([1.0, 0.3]):
+        v0 = (v * scale).astype(np.float32)
+        vo, pv = v0.copy(), np.zeros(f.shape, np.float32)
+        it_ref, _, _ = og.solve_pressure(f, vo, pv, preconditioner=pc_o, cgAccuracy=1e-4, mg_cache=cache)
+        m.copyArrayToGridReal(v0, vel)
+        p.setConst(0.0)
+        m.solvePressure(flags=flags, vel=vel, pressure=p, preconditioner=pc_m, cgAccuracy=1e-4)
+        it, _ = m.lastSolveStats()
+        assert abs(it - it_ref) <= 1, (rep, it, it_ref)
+        assert np.max(np.abs(p.numpy() - pv)) <= 1e-4 * max(1.0, float(np.max(np.abs(pv))))
+        assert divergence(f, vel.numpy()) <= max(1.05 * divergence(f, vo), 1e-4)
+    cache.release()
+
+
+def test_multigrid_ghost_fluid_against_oracle():
+    """Ghost-fluid free surface (float diagonal) under the multigrid
+    preconditioner on a multi-level hierarchy."""
+    shape = (40, 44, 36)
+    f, v = _obstacle_scene(shape, 23, liquid=True)
+    nx, ny, nz = shape
+    phi_a = np.zeros(f.shape, np.float32)
+    og.box_sdf(phi_a, (0, 0, 0), (nx, ny * 0.55 - 0.3, nz))
+    vo, pv = v.copy(), np.zeros(f.shape, np.float32)
+    it_ref, _, _ = og.solve_pressure(f, vo, pv, phi=phi_a, preconditioner=og.PC_MG_DYNAMIC)
+    s = m.Solver(name="gfmg", gridSize=m.vec3(nx, ny, nz), dim=3)
+    flags = grid_from(s, m.FlagGrid, f)
+    vel = grid_from(s, m.MACGrid, v)
+    phi = grid_from(s, m.LevelsetGrid, phi_a)
+    p = s.create(m.RealGrid)
+    m.solvePressure(flags=flags, vel=vel, pressure=p, phi=phi, preconditioner=m.PcMGDynamic)
+    it, _ = m.lastSolveStats()
+    assert abs(it - it_ref) <= 1, (it, it_ref)
+    assert np.max(np.abs(p.numpy() - pv)) <= 1e-4 * max(1.0, float(np.max(np.abs(pv))))
+    assert np.max(np.abs(vel.numpy() - vo)) <= 1e-4
+
+
 def test_pcnone_rejected_like_reference():
     g = load("pressure_3d")
     s = make_solver(g["flags_smoke"].shape)
@@ -214,7 +334,17 @@ def test_plume_steps_against_reference(kernel, monkeypatch):
     """8 full plume steps (24^3, MacCormack + MIC) against the reference
     executable's per-step outputs; thresholds of tools/tests/test_2010."""
     monkeypatch.setenv("MANTA_GB300_MIC", kernel)
-    g = load("plume_mic24")
+    _plume_steps("plume_mic24", m.PcMIC)
+
+
+def test_plume_steps_mgstatic_against_reference():
+    """4 plume steps (24^3, MacCormack + PcMGStatic, one hierarchy for all
+    steps) against the reference executable's per-step outputs."""
+    _plume_steps("plume_mgstat24", m.PcMGStatic)
+
+
+def _plume_steps(golden, pc):
+    g = load(golden)
     n = g["flags"].shape[0]
     s = m.Solver(name="plume", gridSize=m.vec3(n, n, n), dim=3)
     s.timestep = 1.0
@@ -237,7 +367,7 @@ def test_plume_steps_against_reference(kernel, monkeypatch):
         m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=2, clampMode=2)
         m.setWallBcs(flags=flags, vel=vel)
         m.addBuoyancy(density=dens, vel=vel, gravity=m.vec3(0, -4e-3, 0), flags=flags)
-        m.solvePressure(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, preconditioner=m.PcMIC)
+        m.solvePressure(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, preconditioner=pc)
         it, _ = m.lastSolveStats()
         assert abs(it - int(g["iters"][t])) <= 1
         assert np.max(np.abs(dens.numpy() - g["density"][t])) <= 1e-3
