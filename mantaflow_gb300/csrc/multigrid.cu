@@ -30,9 +30,10 @@
 // a colour every vertex reads only other colours, so each pass reproduces the
 // reference's float arithmetic exactly; restriction and interpolation sum
 // their terms in the reference's loop order.  The coarsest level is solved by
-// Jacobi-preconditioned CG in double (solveCG, :793-902) by one CTA with the
-// vectors in shared memory; its dot products are tree sums, so it differs
-// from the serial reference only in the last bits of double rounding.
+// Jacobi-preconditioned CG (solveCG, :793-902) by one CTA with the vectors in
+// shared memory, in double-float arithmetic with tree-summed dot products:
+// it differs from the serial double reference only far below float
+// resolution.
 #include "mg_multigrid.h"
 #include "mg_reduce.cuh"
 
@@ -396,137 +397,216 @@ __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev0 F, float* x0,
   }
 }
 
-// all threads: sum of one double per thread, in a fixed order
-__device__ __forceinline__ double cta_allsum(double v, double* red) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  v = warp_sum(v);
-  if (lane == 0) red[wid] = v;
-  __syncthreads();
-  double t = 0.;
-  for (int q = 0; q < nw; q++) t += red[q];
-  __syncthreads();
-  return t;
+// ---- coarsest level: GridMg::solveCG in double-float arithmetic
+// GB300 executes FP64 at a small fraction of its FP32 rate, and a CG on
+// <= 1000 unknowns is latency bound, so the vectors and dot products use
+// unevaluated float pairs (h + l, 48-bit significand: Dekker's exact
+// product via FMA and Knuth's exact two-sum) and only the per-iteration
+// scalars (alpha, beta, the residual ratio) are formed in double, once per
+// CTA.  The iterates agree with an IEEE-double CG to ~1e-14 relative, far
+// below the float resolution of the result; the stopping rule, iteration
+// limit and order of operations are the reference's.
+struct ff {
+  float h, l;
+};
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return ff{s, (a - (s - bb)) + (b - bb)};
 }
-__device__ __forceinline__ void cta_allsum2(double& a, double& b, double* red) {
+__device__ __forceinline__ ff quick_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return ff{s, b - (s - a)};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  const float p = a * b;
+  return ff{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = two_sum(a.h, b.h);
+  const ff t = two_sum(a.l, b.l);
+  s.l = s.l + t.h;
+  s = quick_two_sum(s.h, s.l);
+  s.l = s.l + t.l;
+  return quick_two_sum(s.h, s.l);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  ff p = two_prod(a.h, b.h);
+  p.l = p.l + (a.h * b.l + a.l * b.h);
+  return quick_two_sum(p.h, p.l);
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+  ff p = two_prod(a.h, b);
+  p.l = p.l + a.l * b;
+  return quick_two_sum(p.h, p.l);
+}
+__device__ __forceinline__ ff ff_div_f(ff a, float b) {
+  const float q1 = a.h / b;
+  const ff p = two_prod(q1, b);
+  ff r = two_sum(a.h, -p.h);
+  r.l = (r.l - p.l) + a.l;
+  const float q2 = (r.h + r.l) / b;
+  return quick_two_sum(q1, q2);
+}
+__device__ __forceinline__ double ff_d(ff a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ ff d_ff(double d) {
+  const float h = (float)d;
+  return ff{h, (float)(d - (double)h)};
+}
+__device__ __forceinline__ ff warp_sum_ff(ff v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const ff w{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+    v = ff_add(v, w);
+  }
+  return v;
+}
+// CTA sum of NV pairs per thread in a fixed order; the sums are valid in
+// thread 0 after the call (the caller publishes derived scalars)
+template <int NV>
+__device__ __forceinline__ void cta_sum_ff(ff* v, ff (*red)[32]) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  a = warp_sum(a);
-  b = warp_sum(b);
-  if (lane == 0) {
-    red[wid] = a;
-    red[32 + wid] = b;
-  }
+#pragma unroll
+  for (int q = 0; q < NV; q++) v[q] = warp_sum_ff(v[q]);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++) red[q][wid] = v[q];
   __syncthreads();
-  double ta = 0., tb = 0.;
-  for (int q = 0; q < nw; q++) {
-    ta += red[q];
-    tb += red[32 + q];
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      ff t = lane < nw ? red[q][lane] : ff{0.f, 0.f};
+      v[q] = warp_sum_ff(t);
+    }
   }
-  __syncthreads();
-  a = ta;
-  b = tb;
 }
 
-// applyAStencil of solveCG: the level-0 or coarse stencil in double
-template <bool IS3D, bool L0>
-__device__ __forceinline__ double cg_apply(const Lev& L, const Lev0& F, int S, int v, int c, float diag, const double* p) {
-  double sum = 0.;
-  if (L0) {
-    const Dims& d = F.d;
-    if (c & kLowX) sum += -p[v - 1];
-    if (c & kHighX) sum += -p[v + 1];
-    if (c & kLowY) sum += -p[v - d.sy];
-    if (c & kHighY) sum += -p[v + d.sy];
-    if (c & kLowZ) sum += -p[v - d.sz];
-    if (c & kHighZ) sum += -p[v + d.sz];
-    sum += (double)diag * p[v];
-  } else {
-    constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
-    int vx, vy, vz;
-    coords(L, v, vx, vy, vz);
-    int s = 0;
-#pragma unroll
-    for (int dz = ZL; dz <= ZH; dz++)
-#pragma unroll
-      for (int dy = -1; dy <= 1; dy++)
-#pragma unroll
-        for (int dx = -1; dx <= 1; dx++, s++) {
-          const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
-          if (!inside(L, nx, ny, nz)) continue;
-          const int nn = (int)lin(L, nx, ny, nz);
-          if (L.type[nn] == kVtInactive) continue;
-          const float a = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
-          sum += (double)a * p[nn];
-        }
-  }
-  return sum;
-}
+constexpr int kCgNb = 27;  // stencil entries per vertex (level 0: 7)
 
-// GridMg::solveCG on the coarsest level: Jacobi-PCG in double, one CTA,
-// one vertex per thread
+// GridMg::solveCG on the coarsest level, one CTA, one vertex per thread.
+// The stencil of each vertex (coefficients in applyAStencil's order and the
+// neighbours' indices) is gathered once into shared memory.
 template <bool IS3D, bool L0>
 __global__ void __launch_bounds__(kCgThreads) k_mg_coarse_cg(Lev L, Lev0 F, const float* __restrict__ res, float* x0, int S,
                                                              float accuracy, const CgScalars* sc) {
   if (sc->done) return;
-  __shared__ double sp[kCgThreads];
-  __shared__ double red[64];
+  extern __shared__ __align__(16) unsigned char cg_smem[];
+  float* coef = (float*)cg_smem;                                  // [kCgNb][kCgThreads]
+  short* nbr = (short*)(cg_smem + kCgNb * kCgThreads * sizeof(float));  // [kCgNb][kCgThreads]
+  __shared__ float sph[kCgThreads], spl[kCgThreads];
+  __shared__ ff red[2][32];
+  __shared__ double bc[4];
+  __shared__ int stop;
   const int n = L0 ? (int)F.d.n : (int)L.n;
   const int v = threadIdx.x;
   bool act = false;
-  int c = 0;
   float diag = 1.f, bv = 0.f;
+  int nn = 0;
   if (v < n) {
     if (L0) {
-      c = F.code[v];
+      const int c = F.code[v];
       act = (c & kMgActive) != 0;
       if (act) {
         diag = l0_diag(c, F.a0f, v);
         bv = l0_rhs(c, res, v);
+        const Dims& d = F.d;
+        const int lo[3] = {kLowX, kLowY, kLowZ}, hi[3] = {kHighX, kHighY, kHighZ};
+        const long long st[3] = {1, d.sy, d.sz};
+        for (int q = 0; q < (IS3D ? 3 : 2); q++) {
+          if (c & lo[q]) { coef[nn * kCgThreads + v] = -1.f; nbr[nn * kCgThreads + v] = (short)(v - st[q]); nn++; }
+          if (c & hi[q]) { coef[nn * kCgThreads + v] = -1.f; nbr[nn * kCgThreads + v] = (short)(v + st[q]); nn++; }
+        }
+        coef[nn * kCgThreads + v] = diag;
+        nbr[nn * kCgThreads + v] = (short)v;
+        nn++;
       }
     } else {
       act = L.type[v] != kVtInactive;
       if (act) {
         diag = L.A[v];
         bv = L.b[v];
+        constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
+        int vx, vy, vz;
+        coords(L, v, vx, vy, vz);
+        int s = 0;
+        for (int dz = ZL; dz <= ZH; dz++)
+          for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++, s++) {
+              const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
+              if (!inside(L, nx, ny, nz)) continue;
+              const int q = (int)lin(L, nx, ny, nz);
+              if (L.type[q] == kVtInactive) continue;
+              coef[nn * kCgThreads + v] =
+                  s < S ? L.A[(long long)(S - 1 - s) * L.n + q] : L.A[(long long)(s - S + 1) * L.n + v];
+              nbr[nn * kCgThreads + v] = (short)q;
+              nn++;
+            }
       }
     }
   }
   // x = mx[l] = 0, so r = b - A*0 = b
-  double x = 0., r = 0., z = 0., p = 0.;
+  ff x{0.f, 0.f}, r{0.f, 0.f}, z{0.f, 0.f}, p{0.f, 0.f};
   if (act) {
-    r = (double)bv;
-    z = r / (double)diag;
+    r = ff{bv, 0.f};
+    z = ff_div_f(r, diag);
     p = z;
   }
-  sp[v] = p;
-  double ir = r * r, alphaTop = r * z;
-  cta_allsum2(ir, alphaTop, red);  // its barriers also publish sp
-  const double initialResidual = sqrt(ir);
-  for (int iter = 0; iter < 10000 && initialResidual > 1E-12; iter++) {
-    const double q = act ? cg_apply<IS3D, L0>(L, F, S, v, c, diag, sp) : 0.;
-    const double alphaBot = cta_allsum(act ? p * q : 0., red);
-    const double alpha = alphaTop / alphaBot;
-    double rr = 0., rz = 0.;
-    if (act) {
-      x += alpha * p;
-      r -= alpha * q;
-      z = r / (double)diag;
-      rr = r * r;
-      rz = r * z;
+  sph[v] = p.h;
+  spl[v] = p.l;
+  {
+    ff t[2] = {ff_mul(r, r), ff_mul(r, z)};
+    cta_sum_ff<2>(t, red);
+    if (v == 0) {
+      bc[0] = sqrt(ff_d(t[0]));  // initialResidual
+      bc[1] = ff_d(t[1]);        // alphaTop
     }
-    cta_allsum2(rr, rz, red);
-    const double residual = sqrt(rr);
-    if (residual / initialResidual < (double)accuracy) break;
-    const double beta = rz / alphaTop;
-    alphaTop = rz;
-    p = z + beta * p;
-    sp[v] = p;
+    __syncthreads();
+  }
+  const double initialResidual = bc[0];
+  double alphaTop = bc[1];  // meaningful in thread 0
+  for (int iter = 0; iter < 10000 && initialResidual > 1E-12; iter++) {
+    ff q{0.f, 0.f};
+    for (int e = 0; e < nn; e++) {
+      const int k = nbr[e * kCgThreads + v];
+      q = ff_add(q, ff_mul_f(ff{sph[k], spl[k]}, coef[e * kCgThreads + v]));
+    }
+    {
+      ff t[1] = {act ? ff_mul(p, q) : ff{0.f, 0.f}};
+      cta_sum_ff<1>(t, red);
+      if (v == 0) bc[2] = alphaTop / ff_d(t[0]);  // alpha
+      __syncthreads();
+    }
+    const ff alpha = d_ff(bc[2]);
+    ff t[2] = {ff{0.f, 0.f}, ff{0.f, 0.f}};
+    if (act) {
+      x = ff_add(x, ff_mul(alpha, p));
+      r = ff_add(r, ff_neg(ff_mul(alpha, q)));
+      z = ff_div_f(r, diag);
+      t[0] = ff_mul(r, r);
+      t[1] = ff_mul(r, z);
+    }
+    cta_sum_ff<2>(t, red);
+    if (v == 0) {
+      const double residual = sqrt(ff_d(t[0]));
+      const double atn = ff_d(t[1]);
+      stop = residual / initialResidual < (double)accuracy;
+      bc[3] = atn / alphaTop;  // beta
+      alphaTop = atn;
+    }
+    __syncthreads();
+    if (stop) break;
+    p = ff_add(z, ff_mul(d_ff(bc[3]), p));
+    sph[v] = p.h;
+    spl[v] = p.l;
     __syncthreads();
   }
   if (v < n) {
-    if (L0) x0[v] = (float)x;
-    else L.x[v] = (float)x;
+    const float xf = (float)ff_d(x);
+    if (L0) x0[v] = xf;
+    else L.x[v] = xf;
   }
 }
+constexpr size_t kCgDynSmem = (size_t)kCgNb * kCgThreads * (sizeof(float) + sizeof(short));
 
 // sigmaNew = dot(tmp, residual) and beta (GridCg::iterate after the
 // preconditioner, conjugategrad.cpp:277-299)
@@ -611,6 +691,12 @@ int ensure_paths() {
         cudaSuccess)
       return 1;
   }
+  const int dyn = (int)kCgDynSmem;
+  if (cudaFuncSetAttribute(k_mg_coarse_cg<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg_coarse_cg<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg_coarse_cg<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg_coarse_cg<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+    return 1;
   g_pathsReady = true;
   return 0;
 }
@@ -883,8 +969,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   if (L == 0) {
     // a single level: the whole V-cycle is the coarsest-level CG
     count_launch();
-    if (h->is3d) k_mg_coarse_cg<true, true><<<1, kCgThreads, 0, s>>>(none, l0, res, x0, S, h->coarseAcc, sc);
-    else k_mg_coarse_cg<false, true><<<1, kCgThreads, 0, s>>>(none, l0, res, x0, S, h->coarseAcc, sc);
+    if (h->is3d) k_mg_coarse_cg<true, true><<<1, kCgThreads, kCgDynSmem, s>>>(none, l0, res, x0, S, h->coarseAcc, sc);
+    else k_mg_coarse_cg<false, true><<<1, kCgThreads, kCgDynSmem, s>>>(none, l0, res, x0, S, h->coarseAcc, sc);
   } else {
     // level 0 pre-smoothing (colour 0 from x = 0, then colour 1)
     count_launch();
@@ -904,8 +990,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       k_mg_restrict<false><<<blocks_for(h->lev[l + 1].n), kThreads1, 0, s>>>(h->lev[l + 1], h->lev[l], l0, sc);
     }
     count_launch();
-    if (h->is3d) k_mg_coarse_cg<true, false><<<1, kCgThreads, 0, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
-    else k_mg_coarse_cg<false, false><<<1, kCgThreads, 0, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
+    if (h->is3d) k_mg_coarse_cg<true, false><<<1, kCgThreads, kCgDynSmem, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
+    else k_mg_coarse_cg<false, false><<<1, kCgThreads, kCgDynSmem, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
     for (int l = L - 1; l >= 1; l--) {
       count_launch();
       k_mg_interp_add<false><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], l0, nullptr, h->lev[l + 1], sc);
