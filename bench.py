@@ -3,8 +3,10 @@
 Workload: the 3D smoke plume at 256^3 (float32 MAC grid, walls with an open
 top, cylinder source with seeded uniform inflow noise, buoyancy (0,-4e-3,0),
 dt = 1, MacCormack advection of density and velocity with clampMode 2,
-setWallBcs, addBuoyancy, solvePressure with PcMIC at cgAccuracy 1e-3).  One
-step is that full sequence; the metric is cells / step time.
+setWallBcs, addBuoyancy, solvePressure at cgAccuracy 1e-3 with the static
+multigrid preconditioner -- the reference's fastest solver for this scene;
+--pc mic selects MIC(0), which is also measured and reported beside the
+headline).  One step is that full sequence; the metric is cells / step time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -52,6 +54,13 @@ BYTES_PER_CELL = {
     "make_codes": 4 + 2 + 2 + 2,
     "correct_velocity": 4 + 4 + 12 + 12,
     "join": 4 + 4 + 4,
+    # multigrid V-cycle, level 0 (bytes per fine cell)
+    "mg_smooth_l0": 2 + 4 + 4 + 2,          # code, residual, x (every cell a neighbour or updated) -> x (half)
+    "mg_smooth_l0_first": 2 + 4 + 4,        # code, residual -> x (all cells, from a zero guess)
+    "mg_residual_l0": 2 + 4 + 4 + 4,        # code, residual, x -> r
+    "mg_restrict_l0": 4 + 0.5,              # r -> coarse b (1/8 of the cells)
+    "mg_interp_l0": 2 + 4 + 4 + 0.5,        # code, x, coarse x -> x
+    "mg_dot": 4 + 4,                        # z, residual (+dot)
 }
 
 
@@ -157,6 +166,14 @@ class Plume:
         self.iters.append(m.lastSolveStats()[0])
 
 
+PC_NAMES = {"mic": "MIC(0)-PCG (PcMIC)", "mgstatic": "multigrid-PCG (PcMGStatic)",
+            "mgdynamic": "multigrid-PCG (PcMGDynamic)"}
+
+
+def workload(n, pcname):
+    return "3D smoke plume %d^3, MacCormack advection + %s, cgAccuracy 1e-3" % (n, PC_NAMES[pcname])
+
+
 def cpu_plume_steps(n, steps, warm, threads, seed, state=None, pc=1):
     """The same plume step with the CPU oracle (OpenMP sweeps, serial MIC as
     in the reference).  Returns (seconds per timed step list, iterations)."""
@@ -223,16 +240,18 @@ def run_reference(args, world, rank, dist):
     threads = os.cpu_count() or 1
     warm = min(args.warmup, 1)
     steps = min(args.steps, 2)
-    times, iters = cpu_plume_steps(args.size, steps, warm, threads, args.seed)
+    pc = {"mic": 1, "mgdynamic": 2, "mgstatic": 3}[args.pc]
+    times, iters = cpu_plume_steps(args.size, steps, warm, threads, args.seed, pc=pc)
     t = statistics.median(times)
     value = args.size ** 3 / t
-    sample = ("256^3 plume steps %d..%d from rest (first %d untimed), full CG to cgAccuracy 1e-3 with MIC(0); "
-              "CG iterations %s" % (warm + 1, warm + steps, warm, iters)) if args.size == 256 else \
-        "%d^3 plume, %d timed steps" % (args.size, steps)
+    sample = ("%d^3 plume steps %d..%d from rest (first %d untimed%s), full CG to cgAccuracy 1e-3 with %s; "
+              "CG iterations %s" % (args.size, warm + 1, warm + steps, warm,
+                                    ", it builds the static multigrid hierarchy" if args.pc == "mgstatic" else "",
+                                    PC_NAMES[args.pc], iters))
     out = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": steps, "warmup": warm,
            "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "3D smoke plume %d^3, MacCormack + MIC-PCG (cgAccuracy 1e-3)" % args.size,
+           "config": {"workload": workload(args.size, args.pc),
                       "global_batch": 1, "seq_len": args.size ** 3, "parallelism": "cpu-openmp"},
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port", "sample": sample},
@@ -247,7 +266,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--pc", default="mic", choices=["mic", "mgstatic", "mgdynamic"])
+    ap.add_argument("--pc", default="mgstatic", choices=["mic", "mgstatic", "mgdynamic"])
+    ap.add_argument("--mic-steps", type=int, default=10, help="timed PcMIC steps reported beside the headline (0: skip)")
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--cpu-steps", type=int, default=1, help="timed oracle steps for cpu_baseline (0: skip)")
     ap.add_argument("--no-profile", action="store_true")
@@ -367,30 +387,57 @@ def main():
                         "share_of_step": tot_ms / sum(v[0] for v in kernels.values())}
     L.mg_host_free(pin)
 
+    # ---- the same scene with PcMIC, reported beside the headline
+    alt = None
+    if args.mic_steps > 0 and pc != m.PcMIC:
+        KM = args.mic_steps
+        mic = Plume(m, n, m.PcMIC, args.seed + 7 + rank, 0)
+        ng = mic.s.create(m.RealGrid)
+        for t in range(3):
+            m.copyArrayToGridReal(mic.noise(), ng)
+            mic.step(ng)
+        noise_m = [mic.s.create(m.RealGrid) for _ in range(KM)]
+        for g in noise_m:
+            m.copyArrayToGridReal(mic.noise(), g)
+        mic.s.sync()
+        _lib.check(L.mg_mark(mic.s._h, 0))
+        i0 = len(mic.iters)
+        for t in range(KM):
+            mic.step(noise_m[t])
+        _lib.check(L.mg_mark(mic.s._h, 1))
+        msm = C.c_float()
+        _lib.check(L.mg_elapsed(mic.s._h, 0, 1, C.byref(msm)))
+        alt = {"workload": workload(n, "mic"), "value": n ** 3 * KM / (msm.value / 1e3), "unit": "cells/s",
+               "ms_per_step": msm.value / KM, "steps": KM, "warmup": 3, "cg_iterations": mic.iters[i0:]}
+        del noise_m, ng, mic
+
     # ---- CPU baseline on a bounded sample (rank 0, one GPU)
     cpu = None
     if rank == 0 and world == 1 and args.cpu_steps > 0:
         state = (sim.density.numpy(), sim.vel.numpy())
         threads = os.cpu_count() or 1
-        times, iters = cpu_plume_steps(n, args.cpu_steps, 0, threads, args.seed + 99, state=state, pc=pc)
+        warm = 1 if pc == m.PcMGStatic else 0  # the static hierarchy is built in an untimed step
+        times, iters = cpu_plume_steps(n, args.cpu_steps, warm, threads, args.seed + 99, state=state, pc=pc)
         tc = statistics.median(times)
         cpu = {"value": n ** 3 / tc, "unit": "cells/s", "cores": threads, "kind": "port",
-               "sample": "%d step(s) of the %d^3 plume continued from the GPU run's state on %d host threads "
-                         "(OpenMP sweeps, serial MIC(0) as in the reference); CG iterations %s" %
-                         (args.cpu_steps, n, threads, iters)}
+               "sample": "%d step(s) of the %d^3 plume continued from the GPU run's state%s on %d host threads "
+                         "(the oracle: OpenMP sweeps; serial MIC(0) and serial coarse-grid selection as in the "
+                         "reference), %s; CG iterations %s" %
+                         (args.cpu_steps, n, " after one untimed step that builds the hierarchy" if warm else "",
+                          threads, PC_NAMES[args.pc], iters)}
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": 1e3 * elapsed / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f32", "data": "synthetic",
-               "config": {"workload": "3D smoke plume %d^3, MacCormack advection + MIC(0)-PCG (cgAccuracy 1e-3)"
-                                      % n if pc == m.PcMIC else "3D smoke plume %d^3, %s" % (n, args.pc),
+               "config": {"workload": workload(n, args.pc),
                           "global_batch": world, "seq_len": n ** 3, "parallelism": "replicas x%d" % world,
                           "l2": "inputs larger than L2 (working set > 1 GB per step)",
                           "cg_iterations": timed_iters},
                "gpu_launches": int(cnt1.value - cnt0.value),
                "clocks": clk, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
-               "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])}}
+               "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])},
+               "same_scene_pc_mic": alt}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()

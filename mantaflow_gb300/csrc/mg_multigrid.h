@@ -17,6 +17,10 @@ void mg_hierarchy_destroy(MgHierarchy* h);
 void mg_hierarchy_reset(MgHierarchy* h);
 size_t mg_hierarchy_bytes(const MgHierarchy* h);
 int mg_hierarchy_levels(const MgHierarchy* h);
+// changes whenever the kernel parameters of mg_apply change (rebuild,
+// coarsest-level accuracy, ghost-fluid diagonal): a captured graph of
+// mg_apply stays valid while the signature and the PcgBuffers are the same
+unsigned long long mg_hierarchy_signature(const MgHierarchy* h);
 // GridMg::setA when the hierarchy has no matrix yet (InitPreconditionMultigrid,
 // conjugategrad.cpp:100-106), then setCoarsestLevelAccuracy; 0 on success.
 // The matrix is read from b.code / b.A0f on the GPU.
@@ -25,5 +29,9 @@ int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStre
 // and doVCycle(tmp) from a zero guess.  Unless init, the last kernel also
 // forms sigmaNew = dot(tmp, residual) and beta like GridCg::iterate.
 int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s);
+// per-kernel-family timing: mg_apply calls hook(ctx, family, 1) before and
+// hook(ctx, family, 0) after each family of launches while a hook is set
+typedef void (*MgProfHook)(void* ctx, const char* family, int begin);
+void mg_set_profiler(MgHierarchy* h, MgProfHook hook, void* ctx);
 
 }  // namespace mgpu

@@ -55,10 +55,16 @@ constexpr int kCgThreads = 1024;        // coarsest level: <= 1000 vertices
 constexpr int kThreads1 = 256;
 const dim3 kBlk0(32, 8, 1);
 
-// a coarse level (l >= 1)
+// a coarse level (l >= 1).  Smoothed levels are stored colour-blocked: the
+// vertices of each of the 8 (2D: 4) Gauss-Seidel colours (x&1, y&1, z&1)
+// form their own sub-grid of 2x2x2 blocks, so a colour pass and the
+// neighbours it reads are contiguous in memory.  The coarsest level keeps the
+// plain x-fastest order.
 struct Lev {
   int sx, sy, sz;
-  long long n, py, pz;
+  long long n, py, pz;  // n: storage slots (colour-blocked: ncol * nb)
+  int colored, bx, by;  // colour-blocked: blocks per row / column
+  long long nb;         // blocks per colour
   int8_t* type;
   float* A;  // stencil entry s of vertex v at A[s * n + v]
   float* x;
@@ -108,11 +114,25 @@ __device__ __forceinline__ float l0_entry(const Lev0& F, long long u, int sf) {
   return (c & bit) ? -1.f : 0.f;
 }
 
-__device__ __forceinline__ long long lin(const Lev& L, int x, int y, int z) { return x + L.py * y + L.pz * z; }
+__host__ __device__ __forceinline__ long long lin(const Lev& L, int x, int y, int z) {
+  if (L.colored)
+    return (long long)((x & 1) | ((y & 1) << 1) | ((z & 1) << 2)) * L.nb + (x >> 1) +
+           (long long)L.bx * ((y >> 1) + (long long)L.by * (z >> 1));
+  return x + L.py * y + L.pz * z;
+}
 __device__ __forceinline__ bool inside(const Lev& L, int x, int y, int z) {
   return x >= 0 && y >= 0 && z >= 0 && x < L.sx && y < L.sy && z < L.sz;
 }
+// slot -> vertex; padding slots of a colour-blocked level map outside the
+// grid and have type inactive
 __device__ __forceinline__ void coords(const Lev& L, long long v, int& x, int& y, int& z) {
+  if (L.colored) {
+    const long long c = v / L.nb, bi = v - c * L.nb;
+    x = 2 * (int)(bi % L.bx) + (int)(c & 1);
+    y = 2 * (int)((bi / L.bx) % L.by) + (int)((c >> 1) & 1);
+    z = 2 * (int)(bi / ((long long)L.bx * L.by)) + (int)(c >> 2);
+    return;
+  }
   x = (int)(v % L.sx);
   y = (int)((v / L.sx) % L.sy);
   z = (int)(v / L.pz);
@@ -233,24 +253,34 @@ __global__ void k_mg_coarse_op(Lev C, Lev F, int S) {
 // ------------------------------------------------------------ V-cycle
 // Sum over the 27 (9) stencil neighbours of a coarse vertex, in the
 // reference's FOR_VECLIN_MINMAX order (x fastest): sum -= A * x[N].
+// Inactive and padding vertices hold x = 0 (and zero matrix entries), so
+// their terms subtract zero and need no type test.  The loads of one z-plane
+// of the stencil (9 matrix entries, 9 values) are issued together before
+// its subtractions; the chain of float operations is the reference's.
 template <bool IS3D, bool SKIP_CENTER>
-__device__ __forceinline__ float stencil_sub(const Lev& L, int S, int vx, int vy, int vz, long long v, float sum) {
+__device__ __forceinline__ float stencil_sub(const Lev& L, int vx, int vy, int vz, long long v, float sum) {
   constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
-  int s = 0;
+  constexpr int S = IS3D ? 14 : 5;
 #pragma unroll
-  for (int dz = ZL; dz <= ZH; dz++)
+  for (int dz = ZL; dz <= ZH; dz++) {
+    float a[9], xv[9];
+    bool in[9];
 #pragma unroll
     for (int dy = -1; dy <= 1; dy++)
 #pragma unroll
-      for (int dx = -1; dx <= 1; dx++, s++) {
-        if (SKIP_CENTER && s == S - 1) continue;
+      for (int dx = -1; dx <= 1; dx++) {
+        const int q = (dy + 1) * 3 + (dx + 1);
+        const int s = (dz - ZL) * 9 + q;
         const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
-        if (!inside(L, nx, ny, nz)) continue;
-        const long long nn = lin(L, nx, ny, nz);
-        if (L.type[nn] == kVtInactive) continue;
-        const float a = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
-        sum = sum - a * L.x[nn];
+        in[q] = inside(L, nx, ny, nz) && !(SKIP_CENTER && s == S - 1);
+        const long long nn = in[q] ? lin(L, nx, ny, nz) : v;
+        a[q] = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
+        xv[q] = L.x[nn];
       }
+#pragma unroll
+    for (int q = 0; q < 9; q++)
+      if (in[q]) sum = sum - a[q] * xv[q];
+  }
   return sum;
 }
 
@@ -274,15 +304,18 @@ __global__ void __launch_bounds__(256) k_mg0_smooth(Lev0 F, const float* __restr
     return;
   }
   if (!mine) return;
-  // sum -= A*x with A = -1 on a link and 0 otherwise (interior cells only
-  // carry links, so every neighbour is inside the grid)
-  float sum = l0_rhs(c, res, v);
-  if (c & kLowX) sum = sum + x[v - 1];
-  if (c & kHighX) sum = sum + x[v + 1];
-  if (c & kLowY) sum = sum + x[v - d.sy];
-  if (c & kHighY) sum = sum + x[v + d.sy];
-  if (c & kLowZ) sum = sum + x[v - d.sz];
-  if (c & kHighZ) sum = sum + x[v + d.sz];
+  // sum -= A*x with A = -1 on a link and 0 otherwise.  Active cells are
+  // interior (only they carry A0 != 0), so all six neighbours exist.
+  const float b = l0_rhs(c, res, v);
+  const float xm = x[v - 1], xp = x[v + 1], ym = x[v - d.sy], yp = x[v + d.sy];
+  const float zm = d.is3d ? x[v - d.sz] : 0.f, zp = d.is3d ? x[v + d.sz] : 0.f;
+  float sum = b;
+  if (c & kLowX) sum = sum + xm;
+  if (c & kHighX) sum = sum + xp;
+  if (c & kLowY) sum = sum + ym;
+  if (c & kHighY) sum = sum + yp;
+  if (c & kLowZ) sum = sum + zm;
+  if (c & kHighZ) sum = sum + zp;
   x[v] = sum / l0_diag(c, F.a0f, v);
 }
 
@@ -294,43 +327,46 @@ __global__ void __launch_bounds__(256) k_mg0_residual(Lev0 F, const float* __res
   GRID_STRIDE(v, d.n) {
     const int c = F.code[v];
     if (!(c & kMgActive)) continue;
-    float sum = l0_rhs(c, res, v);
-    if (c & kLowX) sum = sum + x[v - 1];
-    if (c & kHighX) sum = sum + x[v + 1];
-    if (c & kLowY) sum = sum + x[v - d.sy];
-    if (c & kHighY) sum = sum + x[v + d.sy];
-    if (c & kLowZ) sum = sum + x[v - d.sz];
-    if (c & kHighZ) sum = sum + x[v + d.sz];
-    sum = sum - l0_diag(c, F.a0f, v) * x[v];
+    const float b = l0_rhs(c, res, v), xc = x[v];
+    const float xm = x[v - 1], xp = x[v + 1], ym = x[v - d.sy], yp = x[v + d.sy];
+    const float zm = d.is3d ? x[v - d.sz] : 0.f, zp = d.is3d ? x[v + d.sz] : 0.f;
+    float sum = b;
+    if (c & kLowX) sum = sum + xm;
+    if (c & kHighX) sum = sum + xp;
+    if (c & kLowY) sum = sum + ym;
+    if (c & kHighY) sum = sum + yp;
+    if (c & kLowZ) sum = sum + zm;
+    if (c & kHighZ) sum = sum + zp;
+    sum = sum - l0_diag(c, F.a0f, v) * xc;
     F.r[v] = sum;
   }
 }
 
 // knSmoothColor on a coarse level: colour offset (ox, oy, oz) in 2x2x2 blocks
 template <bool IS3D>
-__global__ void __launch_bounds__(256) k_mg_smooth(Lev L, int S, int ox, int oy, int oz, const CgScalars* sc) {
+__global__ void __launch_bounds__(256, 3) k_mg_smooth(Lev L, int S, int ox, int oy, int oz, const CgScalars* sc) {
   if (sc->done) return;
   const int bx = (L.sx + 1) / 2, by = (L.sy + 1) / 2, bz = (L.sz + 1) / 2;
   const long long nb = (long long)bx * by * bz;
   GRID_STRIDE(bi, nb) {
     const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
     if (!inside(L, vx, vy, vz)) continue;
-    const long long v = lin(L, vx, vy, vz);
+    const long long v = L.colored ? (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi : lin(L, vx, vy, vz);
     if (L.type[v] == kVtInactive) continue;
-    const float sum = stencil_sub<IS3D, true>(L, S, vx, vy, vz, v, L.b[v]);
+    const float sum = stencil_sub<IS3D, true>(L, vx, vy, vz, v, L.b[v]);
     L.x[v] = sum / L.A[v];
   }
 }
 
 // knCalcResidual on a coarse level
 template <bool IS3D>
-__global__ void __launch_bounds__(256) k_mg_residual(Lev L, int S, const CgScalars* sc) {
+__global__ void __launch_bounds__(256, 3) k_mg_residual(Lev L, int S, const CgScalars* sc) {
   if (sc->done) return;
   GRID_STRIDE(v, L.n) {
     if (L.type[v] == kVtInactive) continue;
     int vx, vy, vz;
     coords(L, v, vx, vy, vz);
-    L.r[v] = stencil_sub<IS3D, false>(L, S, vx, vy, vz, v, L.b[v]);
+    L.r[v] = stencil_sub<IS3D, false>(L, vx, vy, vz, v, L.b[v]);
   }
 }
 
@@ -340,29 +376,29 @@ template <bool FROM0>
 __global__ void __launch_bounds__(256) k_mg_restrict(Lev D, Lev S, Lev0 F, const CgScalars* sc) {
   if (sc->done) return;
   const int sx = FROM0 ? F.d.nx : S.sx, sy = FROM0 ? F.d.ny : S.sy, sz = FROM0 ? F.d.nz : S.sz;
-  const long long py = FROM0 ? F.d.sy : S.py, pz = FROM0 ? F.d.sz : S.pz;
+  const long long py = F.d.sy, pz = F.d.sz;
   GRID_STRIDE(v, D.n) {
     D.x[v] = 0.f;
     if (D.type[v] == kVtInactive) continue;
     int vx, vy, vz;
     coords(D, v, vx, vy, vz);
-    const int lx = max(0, 2 * vx - 1), ly = max(0, 2 * vy - 1), lz = max(0, 2 * vz - 1);
-    const int hx = min(sx - 1, 2 * vx + 1), hy = min(sy - 1, 2 * vy + 1), hz = min(sz - 1, 2 * vz + 1);
+    // the fine vertices 2V-1 .. 2V+1 inside the level, in the reference's
+    // loop order; all loads first
+    float rv[27];
+    bool in[27];
+#pragma unroll
+    for (int q = 0; q < 27; q++) {
+      const int rx = 2 * vx - 1 + q % 3, ry = 2 * vy - 1 + (q / 3) % 3, rz = 2 * vz - 1 + q / 9;
+      in[q] = rx >= 0 && ry >= 0 && rz >= 0 && rx < sx && ry < sy && rz < sz;
+      // inactive fine vertices hold r = 0: adding their term adds zero
+      rv[q] = in[q] ? (FROM0 ? F.r[rx + py * ry + pz * rz] : S.r[lin(S, rx, ry, rz)]) : 0.f;
+    }
     float sum = 0.f;
-    for (int rz = lz; rz <= hz; rz++)
-      for (int ry = ly; ry <= hy; ry++)
-        for (int rx = lx; rx <= hx; rx++) {
-          const long long r = rx + py * ry + pz * rz;
-          float rv;
-          if (FROM0) {
-            if (!(F.code[r] & kMgActive)) continue;
-            rv = F.r[r];
-          } else {
-            if (S.type[r] == kVtInactive) continue;
-            rv = S.r[r];
-          }
-          sum = sum + inv_pow2(parity3(rx, ry, rz)) * rv;
-        }
+#pragma unroll
+    for (int q = 0; q < 27; q++) {
+      const int rx = 2 * vx - 1 + q % 3, ry = 2 * vy - 1 + (q / 3) % 3, rz = 2 * vz - 1 + q / 9;
+      if (in[q]) sum = sum + inv_pow2(parity3(rx, ry, rz)) * rv[q];
+    }
     D.b[v] = sum;
   }
 }
@@ -384,13 +420,22 @@ __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev0 F, float* x0,
       if (D.type[v] == kVtInactive) continue;
       coords(D, v, vx, vy, vz);
     }
+    // coarse parents V/2 .. (V+1)/2 per axis (one or two), in the
+    // reference's loop order; inactive coarse vertices hold x = 0
+    const int hx = (vx + 1) / 2 - vx / 2, hy = (vy + 1) / 2 - vy / 2, hz = (vz + 1) / 2 - vz / 2;
+    float cv[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
+      const bool use = (ox <= hx) && (oy <= hy) && (oz <= hz);
+      cv[q] = use ? S.x[lin(S, vx / 2 + ox, vy / 2 + oy, vz / 2 + oz)] : 0.f;
+    }
     float sum = 0.f;
-    for (int iz = vz / 2; iz <= (vz + 1) / 2; iz++)
-      for (int iy = vy / 2; iy <= (vy + 1) / 2; iy++)
-        for (int ixx = vx / 2; ixx <= (vx + 1) / 2; ixx++) {
-          const long long q = lin(S, ixx, iy, iz);
-          if (S.type[q] != kVtInactive) sum = sum + S.x[q];
-        }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
+      if ((ox <= hx) && (oy <= hy) && (oz <= hz)) sum = sum + cv[q];
+    }
     const float r = inv_pow2(parity3(vx, vy, vz)) * sum;
     float* xd = TO0 ? x0 : D.x;
     xd[v] = xd[v] + r;
@@ -784,15 +829,10 @@ void gen_coarse_grid(const int fs[3], const std::vector<int8_t>& tf, const int c
 }
 
 int blocks_for(long long n) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 148;
-  }
+  // one vertex per thread: each thread's loads are then independent of the
+  // others' (a grid-stride loop would serialise their memory latency)
   const long long b = (n + kThreads1 - 1) / kThreads1;
-  return (int)std::max(1LL, std::min(b, (long long)sms * 8));
+  return (int)std::max(1LL, std::min(b, 1LL << 30));
 }
 
 }  // namespace
@@ -804,11 +844,15 @@ struct MgHierarchy {
   Lev lev[kMaxLevels];
   Lev0 l0;
   int8_t* type0 = nullptr;
-  std::vector<int8_t> htype[kMaxLevels];
+  std::vector<int8_t> htype[kMaxLevels];   // vertex types, x-fastest
+  std::vector<int8_t> upload[kMaxLevels];  // the same in storage order
   std::vector<int8_t> selType0;  // level-0 types the current selection was made for
   bool selValid = false;
   bool isASet = false;
+  unsigned long long gen = 0;  // bumped by every rebuild
   bool useA0f = false;  // the snapshot has a float diagonal (ghost fluid)
+  MgProfHook hook = nullptr;
+  void* hookCtx = nullptr;
   float coarseAcc = 1e-8f;
   size_t bytes = 0;
   std::vector<void*> allocs;
@@ -860,9 +904,13 @@ MgHierarchy* mg_hierarchy_create(const Dims& d) {
     v.sx = h->size[l][0];
     v.sy = h->size[l][1];
     v.sz = h->size[l][2];
-    v.n = (long long)v.sx * v.sy * v.sz;
     v.py = v.sx;
     v.pz = (long long)v.sx * v.sy;
+    v.colored = l < L - 1;
+    v.bx = (v.sx + 1) / 2;
+    v.by = (v.sy + 1) / 2;
+    v.nb = (long long)v.bx * v.by * ((v.sz + 1) / 2);
+    v.n = v.colored ? v.nb * (d.is3d ? 8 : 4) : (long long)v.sx * v.sy * v.sz;
     v.type = h->alloc<int8_t>(v.n);
     v.A = h->alloc<float>(v.n * h->S);
     v.x = h->alloc<float>(v.n);
@@ -889,15 +937,33 @@ void mg_hierarchy_reset(MgHierarchy* h) {
 }
 
 size_t mg_hierarchy_bytes(const MgHierarchy* h) { return h ? h->bytes : 0; }
+unsigned long long mg_hierarchy_signature(const MgHierarchy* h) {
+  if (!h) return 0;
+  unsigned int acc;
+  std::memcpy(&acc, &h->coarseAcc, sizeof acc);
+  return (h->gen << 34) ^ ((unsigned long long)h->useA0f << 33) ^ (unsigned long long)acc;
+}
 int mg_hierarchy_levels(const MgHierarchy* h) { return h ? h->nlev : 0; }
 
 int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStream_t s) {
   h->coarseAcc = coarseAccuracy;
   if (h->isASet) return 0;
+  h->gen++;
   const Dims& d = h->d;
   if (b.A0f && !h->l0.a0f) {
     h->l0.a0f = h->alloc<float>(d.n);
     if (!h->ok) return 1;
+  }
+  // inactive vertices keep zero x, b, r and matrix rows: the V-cycle
+  // kernels rely on it instead of testing vertex types
+  if (h->l0.r && cudaMemsetAsync(h->l0.r, 0, sizeof(float) * (size_t)d.n, s) != cudaSuccess) return 1;
+  for (int l = 1; l < h->nlev; l++) {
+    const Lev& v = h->lev[l];
+    if (cudaMemsetAsync(v.A, 0, sizeof(float) * (size_t)(v.n * h->S), s) != cudaSuccess ||
+        cudaMemsetAsync(v.x, 0, sizeof(float) * (size_t)v.n, s) != cudaSuccess ||
+        cudaMemsetAsync(v.b, 0, sizeof(float) * (size_t)v.n, s) != cudaSuccess ||
+        cudaMemsetAsync(v.r, 0, sizeof(float) * (size_t)v.n, s) != cudaSuccess)
+      return 1;
   }
   float* a0f = b.A0f ? h->l0.a0f : nullptr;
   Lev0 l0 = h->l0;
@@ -917,9 +983,14 @@ int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStre
     if (!reuse) {
       for (int l = 1; l < h->nlev; l++) {
         gen_coarse_grid(h->size[l - 1], h->htype[l - 1], h->size[l], h->htype[l]);
-        if (cudaMemcpyAsync(h->lev[l].type, h->htype[l].data(), h->htype[l].size(), cudaMemcpyHostToDevice, s) !=
-            cudaSuccess)
-          return 1;
+        const Lev& v = h->lev[l];
+        std::vector<int8_t>& st = h->upload[l];
+        st.assign((size_t)v.n, kVtInactive);
+        long long q = 0;
+        for (int z = 0; z < v.sz; z++)
+          for (int y = 0; y < v.sy; y++)
+            for (int x = 0; x < v.sx; x++) st[(size_t)lin(v, x, y, z)] = h->htype[l][(size_t)q++];
+        if (cudaMemcpyAsync(v.type, st.data(), st.size(), cudaMemcpyHostToDevice, s) != cudaSuccess) return 1;
       }
       h->selType0 = h->htype[0];
       h->selValid = true;
@@ -943,6 +1014,24 @@ int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStre
   return 0;
 }
 
+void mg_set_profiler(MgHierarchy* h, MgProfHook hook, void* ctx) {
+  h->hook = hook;
+  h->hookCtx = ctx;
+}
+
+namespace {
+struct Fam {
+  const MgHierarchy* h;
+  const char* name;
+  Fam(const MgHierarchy* h_, const char* n) : h(h_), name(n) {
+    if (h->hook) h->hook(h->hookCtx, name, 1);
+  }
+  ~Fam() {
+    if (h->hook) h->hook(h->hookCtx, name, 0);
+  }
+};
+}  // namespace
+
 int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   const Dims& d = h->d;
   const int L = h->nlev - 1;
@@ -957,6 +1046,7 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
   const int ncol = h->is3d ? 8 : 4;
   auto smooth = [&](int l, bool reversed) {
+    Fam f(h, "mg_smooth_coarse");
     const Lev& v = h->lev[l];
     const int nb = blocks_for((long long)((v.sx + 1) / 2) * ((v.sy + 1) / 2) * ((v.sz + 1) / 2));
     for (int q = 0; q < ncol; q++) {
@@ -968,43 +1058,68 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   };
   if (L == 0) {
     // a single level: the whole V-cycle is the coarsest-level CG
+    Fam f(h, "mg_coarse_cg");
     count_launch();
     if (h->is3d) k_mg_coarse_cg<true, true><<<1, kCgThreads, kCgDynSmem, s>>>(none, l0, res, x0, S, h->coarseAcc, sc);
     else k_mg_coarse_cg<false, true><<<1, kCgThreads, kCgDynSmem, s>>>(none, l0, res, x0, S, h->coarseAcc, sc);
   } else {
     // level 0 pre-smoothing (colour 0 from x = 0, then colour 1)
-    count_launch();
-    k_mg0_smooth<0><<<g0, kBlk0, 0, s>>>(l0, res, x0, 0, sc);
-    count_launch();
-    k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, 1, sc);
-    count_launch();
-    k_mg0_residual<<<blocks_for(d.n), kThreads1, 0, s>>>(l0, res, x0, sc);
-    count_launch();
-    k_mg_restrict<true><<<blocks_for(h->lev[1].n), kThreads1, 0, s>>>(h->lev[1], none, l0, sc);
+    {
+      Fam f(h, "mg_smooth_l0_first");
+      count_launch();
+      k_mg0_smooth<0><<<g0, kBlk0, 0, s>>>(l0, res, x0, 0, sc);
+    }
+    {
+      Fam f(h, "mg_smooth_l0");
+      count_launch();
+      k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, 1, sc);
+    }
+    {
+      Fam f(h, "mg_residual_l0");
+      count_launch();
+      k_mg0_residual<<<blocks_for(d.n), kThreads1, 0, s>>>(l0, res, x0, sc);
+    }
+    {
+      Fam f(h, "mg_restrict_l0");
+      count_launch();
+      k_mg_restrict<true><<<blocks_for(h->lev[1].n), kThreads1, 0, s>>>(h->lev[1], none, l0, sc);
+    }
     for (int l = 1; l < L; l++) {
       smooth(l, false);
+      Fam f(h, "mg_transfer_coarse");
       count_launch();
       if (h->is3d) k_mg_residual<true><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], S, sc);
       else k_mg_residual<false><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], S, sc);
       count_launch();
       k_mg_restrict<false><<<blocks_for(h->lev[l + 1].n), kThreads1, 0, s>>>(h->lev[l + 1], h->lev[l], l0, sc);
     }
-    count_launch();
-    if (h->is3d) k_mg_coarse_cg<true, false><<<1, kCgThreads, kCgDynSmem, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
-    else k_mg_coarse_cg<false, false><<<1, kCgThreads, kCgDynSmem, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
+    {
+      Fam f(h, "mg_coarse_cg");
+      count_launch();
+      if (h->is3d) k_mg_coarse_cg<true, false><<<1, kCgThreads, kCgDynSmem, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
+      else k_mg_coarse_cg<false, false><<<1, kCgThreads, kCgDynSmem, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
+    }
     for (int l = L - 1; l >= 1; l--) {
+      {
+      Fam f(h, "mg_transfer_coarse");
       count_launch();
       k_mg_interp_add<false><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], l0, nullptr, h->lev[l + 1], sc);
+      }
       smooth(l, true);
     }
-    count_launch();
-    k_mg_interp_add<true><<<blocks_for(d.n), kThreads1, 0, s>>>(none, l0, x0, h->lev[1], sc);
-    count_launch();
-    k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, 1, sc);
-    count_launch();
-    k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, 0, sc);
+    {
+      Fam f(h, "mg_interp_l0");
+      count_launch();
+      k_mg_interp_add<true><<<blocks_for(d.n), kThreads1, 0, s>>>(none, l0, x0, h->lev[1], sc);
+    }
+    for (int c = 1; c >= 0; c--) {
+      Fam f(h, "mg_smooth_l0");
+      count_launch();
+      k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, c, sc);
+    }
   }
   if (!init) {
+    Fam f(h, "mg_dot");
     count_launch();
     k_mg_dot_beta<<<b.nblocks, kThreads1, 0, s>>>(d.n, b.tmp, b.residual, b.part, b.sc);
   }

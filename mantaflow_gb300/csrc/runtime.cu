@@ -111,9 +111,17 @@ struct mg_solver_s {
   bool useMicFlow = false;
   unsigned int epoch = 0;
   mgpu::MgHierarchy* mg = nullptr;  // static multigrid cache (gMapMG)
+  // one MG-PCG iteration captured as a CUDA graph, replayed while the
+  // buffers and hierarchy it was captured with are unchanged
+  cudaGraphExec_t iterGraph = nullptr;
+  PcgBuffers iterKey{};
+  unsigned long long iterSig = 0;
+  const void* iterMg = nullptr;
+  unsigned long long iterNodes = 0;
   // profiling
   bool prof = false;
   std::vector<Prof> profEvents;
+  Prof profOpen;
   std::vector<cudaEvent_t> evFree;
   std::map<std::string, std::pair<double, long long>> profAcc;
   cudaEvent_t marks[8] = {};
@@ -142,7 +150,7 @@ struct ProfScope {
   mg_solver s;
   Prof p;
   bool on;
-  ProfScope(mg_solver s_, const char* name) : s(s_), on(s_->prof) {
+  ProfScope(mg_solver s_, const char* name) : s(s_), on(s_->prof && name) {
     if (!on) return;
     p.name = name;
     p.a = take();
@@ -339,6 +347,7 @@ extern "C" int mg_solver_destroy(mg_solver s) {
   s->pool.clear();
   free_cg_state(s);
   if (s->mg) mg_hierarchy_destroy(s->mg);
+  if (s->iterGraph) cudaGraphExecDestroy(s->iterGraph);
   prof_collect(s);
   for (auto e : s->evFree) cudaEventDestroy(e);
   for (auto e : s->marks) cudaEventDestroy(e);
@@ -972,6 +981,21 @@ extern "C" int mg_compute_pressure_rhs(mg_grid rhs, mg_grid vel, mg_grid pressur
   return MG_OK;
 }
 
+// event pairs around the multigrid kernel families while profiling
+static void mg_prof_hook(void* ctx, const char* family, int begin) {
+  mg_solver s = (mg_solver)ctx;
+  if (begin) {
+    ProfScope tk(s, nullptr);
+    s->profOpen.name = family;
+    s->profOpen.a = tk.take();
+    s->profOpen.b = tk.take();
+    cudaEventRecord(s->profOpen.a, s->stream);
+  } else {
+    cudaEventRecord(s->profOpen.b, s->stream);
+    s->profEvents.push_back(s->profOpen);
+  }
+}
+
 // doInit's preconditioner application: r -> tmp
 static int apply_precond(mg_solver s, const PcgBuffers& b, int pc, bool init) {
   if (pc == kPcMic) {
@@ -991,7 +1015,7 @@ static int apply_precond(mg_solver s, const PcgBuffers& b, int pc, bool init) {
       else launch_mic(b, s->mic, init ? 3 : 2, ++s->epoch, kWaitNs, s->stream);
     }
   } else if (pc == kPcMg) {
-    ProfScope ps(s, "mg_vcycle");
+    mg_set_profiler(s->mg, s->prof ? mg_prof_hook : nullptr, s);
     const int st = mg_apply(s->mg, b, init, s->stream);
     if (st) return fail(MG_ERR_CUDA, "multigrid V-cycle failed");
   } else {
@@ -999,6 +1023,50 @@ static int apply_precond(mg_solver s, const PcgBuffers& b, int pc, bool init) {
     launch_pcg_copy_dot(b, s->stream);
   }
   CKL();
+  return MG_OK;
+}
+
+static bool same_buffers(const PcgBuffers& a, const PcgBuffers& b) {
+  return a.d.nx == b.d.nx && a.d.ny == b.d.ny && a.d.nz == b.d.nz && a.code == b.code &&
+         a.A0f == b.A0f && a.pressure == b.pressure && a.residual == b.residual &&
+         a.search == b.search && a.tmp == b.tmp && a.P == b.P && a.part == b.part && a.partf == b.partf &&
+         a.sc == b.sc && a.nblocks == b.nblocks;
+}
+
+// GridCg::iterate with the multigrid preconditioner as one graph launch:
+// about a hundred short kernels per iteration, most of them on small coarse
+// levels, whose launch gaps would otherwise dominate.  Captured on first use
+// and whenever the buffers or the hierarchy's kernel parameters change.
+static int mg_iteration_graph(mg_solver s, const PcgBuffers& b) {
+  const unsigned long long sig = mg_hierarchy_signature(s->mg);
+  if (s->iterGraph && same_buffers(s->iterKey, b) && s->iterSig == sig && s->iterMg == s->mg) return MG_OK;
+  if (s->iterGraph) {
+    cudaGraphExecDestroy(s->iterGraph);
+    s->iterGraph = nullptr;
+  }
+  const unsigned long long before = g_launches;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  launch_pcg_spmv(b, s->stream);
+  launch_pcg_axpy(b, s->stream);
+  const int e = mg_apply(s->mg, b, false, s->stream);
+  launch_pcg_update(b, s->stream);
+  const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+  s->iterNodes = g_launches - before;
+  g_launches = before;
+  if (e || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(MG_ERR_CUDA, std::string("capturing the multigrid iteration failed: ") + cudaGetErrorString(ce));
+  }
+  const cudaError_t ie = cudaGraphInstantiate(&s->iterGraph, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) {
+    s->iterGraph = nullptr;
+    return fail(MG_ERR_CUDA, std::string("instantiating the multigrid iteration failed: ") + cudaGetErrorString(ie));
+  }
+  s->iterKey = b;
+  s->iterSig = sig;
+  s->iterMg = s->mg;
   return MG_OK;
 }
 
@@ -1118,7 +1186,24 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   bool done = false;
   int* doneHost = &s->scHost->done;
   *doneHost = 0;
+  // the MG iteration runs as a CUDA graph unless per-kernel profiling is on
+  const bool graph = pc == kPcMg && !s->prof;
+  if (graph) {
+    st = mg_iteration_graph(s, b);
+    if (st) return st;
+  }
   while (it < maxIter && !done) {
+    if (graph) {
+      CK(cudaGraphLaunch(s->iterGraph, s->stream));
+      g_launches += s->iterNodes;
+      it++;
+      if (it % lag == 0 || it == maxIter) {
+        CK(cudaMemcpyAsync(s->scHost, s->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        done = s->scHost->done != 0;
+      }
+      continue;
+    }
     {
       ProfScope ps(s, "pcg_spmv");
       launch_pcg_spmv(b, s->stream);
