@@ -175,6 +175,13 @@ int mg_correct_velocity(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_p
                         mg_grid perCellCorr, mg_grid fractions, mg_grid curv);
 /* releaseMG (:252-266); s == NULL releases every solver's hierarchy */
 int mg_release_mg(mg_solver s);
+/* One multigrid V-cycle dst = M^-1 src for the Poisson matrix of flags (with
+ * the ghost-fluid diagonal when phi is given): GridMg::setA, setRhs and
+ * doVCycle (source/multigrid.cpp:386-504) on a fresh hierarchy, as
+ * InitPreconditionMultigrid / ApplyPreconditionMultigrid do
+ * (conjugategrad.cpp:100-106, 162-167).  A diagnostic entry for checking
+ * the preconditioner on its own; solvePressure does not need it. */
+int mg_multigrid_vcycle(mg_grid flags, mg_grid phi, mg_grid src, mg_grid dst, float gfClamp, float coarseAccuracy);
 
 /* ---- scene setup (source/grid.cpp, source/shapes.cpp) -------------------- */
 /* FlagGrid::initDomain (grid.cpp:732-822); phiWalls must be NULL */

@@ -70,6 +70,7 @@ SIGNATURES = [
                                       C.POINTER(PressureResult)]),
     ("mg_correct_velocity", _I, [_P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P]),
     ("mg_release_mg", _I, [_P]),
+    ("mg_multigrid_vcycle", _I, [_P, _P, _P, _P, _F, _F]),
     ("mg_flags_init_domain", _I, [_P, _I, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, _P]),
     ("mg_flags_fill_grid", _I, [_P, _I]),
     ("mg_flags_update_from_levelset", _I, [_P, _P]),

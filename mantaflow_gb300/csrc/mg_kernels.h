@@ -95,8 +95,9 @@ struct MicPlan {
   int ctas;               // persistent CTAs
 };
 
+// sums: also the per-block sums of rhs and fluid cells (enforceCompatibility)
 void launch_make_rhs(const PcgBuffers& b, const float* vu, const float* vv, const float* vw, const float* perCellCorr,
-                     const float* phi, const float* curv, float surfTens, float gfClamp, cudaStream_t s);
+                     const float* phi, const float* curv, float surfTens, float gfClamp, bool sums, cudaStream_t s);
 void launch_compat_shift(const PcgBuffers& b, cudaStream_t s);
 void launch_make_codes(const PcgBuffers& b, cudaStream_t s);
 void launch_ghost_fluid_diag(const PcgBuffers& b, const float* phi, float gfClamp, cudaStream_t s);

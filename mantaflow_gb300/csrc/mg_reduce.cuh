@@ -82,4 +82,21 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int t
   return last;
 }
 
+// Per-thread sum of float products as an unevaluated pair h + l: each
+// addition is Knuth's exact two-sum, its rounding error kept in l.  This
+// carries ~48 bits, far beyond the float terms, and costs a few FP32
+// instructions instead of a convert and an add on the FP64 pipe, which
+// GB300 runs at a small fraction of its FP32 rate.  Threads convert to
+// double once, before the block and grid sums.
+struct FSum {
+  float h = 0.f, l = 0.f;
+  __device__ __forceinline__ void add(float p) {
+    const float s = h + p;
+    const float bb = s - h;
+    l += (h - (s - bb)) + (p - bb);
+    h = s;
+  }
+  __device__ __forceinline__ double value() const { return (double)h + (double)l; }
+};
+
 }  // namespace mgpu

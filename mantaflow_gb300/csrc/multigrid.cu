@@ -53,7 +53,6 @@ constexpr float kTrivialScale = 1e-6f;  // GridMg::mTrivialEquationScale
 constexpr int kMaxLevels = 32;
 constexpr int kCgThreads = 1024;        // coarsest level: <= 1000 vertices
 constexpr int kThreads1 = 256;
-const dim3 kBlk0(32, 8, 1);
 
 // a coarse level (l >= 1).  Smoothed levels are stored colour-blocked: the
 // vertices of each of the 8 (2D: 4) Gauss-Seidel colours (x&1, y&1, z&1)
@@ -78,6 +77,7 @@ struct Lev0 {
   uint16_t* code;  // Poisson code | kMgActive | kMgTrivial
   float* a0f;      // trivial-scaled float diagonal (ghost fluid) or null
   float* r;        // residual
+  float* xd;       // x after pre-smoothing: read (with halo) by the up pass
 };
 
 // One term of the level-1 Galerkin product (knGenCoarseGridOperator, level
@@ -284,64 +284,6 @@ __device__ __forceinline__ float stencil_sub(const Lev& L, int vx, int vy, int v
   return sum;
 }
 
-// knSmoothColor on level 0 (7-point stencil; colour = parity of i+j+k).
-// MODE 0: first pass of a V-cycle, x = 0 before it: every cell is written,
-// cells of the colour get b/A0 (their neighbours are all zero) and the rest 0.
-template <int MODE>
-__global__ void __launch_bounds__(256) k_mg0_smooth(Lev0 F, const float* __restrict__ res, float* x, int color,
-                                                    const CgScalars* sc) {
-  if (sc->done) return;
-  const Dims& d = F.d;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= d.nx || j >= d.ny) return;
-  const long long v = ix(d, i, j, k);
-  const int c = F.code[v];
-  const bool mine = ((i + j + k) & 1) == color && (c & kMgActive);
-  if (MODE == 0) {
-    x[v] = mine ? l0_rhs(c, res, v) / l0_diag(c, F.a0f, v) : 0.f;
-    return;
-  }
-  if (!mine) return;
-  // sum -= A*x with A = -1 on a link and 0 otherwise.  Active cells are
-  // interior (only they carry A0 != 0), so all six neighbours exist.
-  const float b = l0_rhs(c, res, v);
-  const float xm = x[v - 1], xp = x[v + 1], ym = x[v - d.sy], yp = x[v + d.sy];
-  const float zm = d.is3d ? x[v - d.sz] : 0.f, zp = d.is3d ? x[v + d.sz] : 0.f;
-  float sum = b;
-  if (c & kLowX) sum = sum + xm;
-  if (c & kHighX) sum = sum + xp;
-  if (c & kLowY) sum = sum + ym;
-  if (c & kHighY) sum = sum + yp;
-  if (c & kLowZ) sum = sum + zm;
-  if (c & kHighZ) sum = sum + zp;
-  x[v] = sum / l0_diag(c, F.a0f, v);
-}
-
-// knCalcResidual on level 0
-__global__ void __launch_bounds__(256) k_mg0_residual(Lev0 F, const float* __restrict__ res, const float* __restrict__ x,
-                                                      const CgScalars* sc) {
-  if (sc->done) return;
-  const Dims& d = F.d;
-  GRID_STRIDE(v, d.n) {
-    const int c = F.code[v];
-    if (!(c & kMgActive)) continue;
-    const float b = l0_rhs(c, res, v), xc = x[v];
-    const float xm = x[v - 1], xp = x[v + 1], ym = x[v - d.sy], yp = x[v + d.sy];
-    const float zm = d.is3d ? x[v - d.sz] : 0.f, zp = d.is3d ? x[v + d.sz] : 0.f;
-    float sum = b;
-    if (c & kLowX) sum = sum + xm;
-    if (c & kHighX) sum = sum + xp;
-    if (c & kLowY) sum = sum + ym;
-    if (c & kHighY) sum = sum + yp;
-    if (c & kLowZ) sum = sum + zm;
-    if (c & kHighZ) sum = sum + zp;
-    sum = sum - l0_diag(c, F.a0f, v) * xc;
-    F.r[v] = sum;
-  }
-}
-
 // knSmoothColor on a coarse level: colour offset (ox, oy, oz) in 2x2x2 blocks
 template <bool IS3D>
 __global__ void __launch_bounds__(256, 3) k_mg_smooth(Lev L, int S, int ox, int oy, int oz, const CgScalars* sc) {
@@ -404,22 +346,13 @@ __global__ void __launch_bounds__(256) k_mg_restrict(Lev D, Lev S, Lev0 F, const
 }
 
 // knInterpolate from level S = D+1 and knAddAssign: x[D] += I * x[S]
-// (into the level-0 result x0 when TO0)
-template <bool TO0>
-__global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev0 F, float* x0, Lev S, const CgScalars* sc) {
+template <bool IS3D>
+__global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev S, const CgScalars* sc) {
   if (sc->done) return;
-  const long long n = TO0 ? F.d.n : D.n;
-  GRID_STRIDE(v, n) {
+  GRID_STRIDE(v, D.n) {
+    if (D.type[v] == kVtInactive) continue;
     int vx, vy, vz;
-    if (TO0) {
-      if (!(F.code[v] & kMgActive)) continue;
-      vx = (int)(v % F.d.nx);
-      vy = (int)((v / F.d.nx) % F.d.ny);
-      vz = F.d.is3d ? (int)(v / F.d.sz) : 0;
-    } else {
-      if (D.type[v] == kVtInactive) continue;
-      coords(D, v, vx, vy, vz);
-    }
+    coords(D, v, vx, vy, vz);
     // coarse parents V/2 .. (V+1)/2 per axis (one or two), in the
     // reference's loop order; inactive coarse vertices hold x = 0
     const int hx = (vx + 1) / 2 - vx / 2, hy = (vy + 1) / 2 - vy / 2, hz = (vz + 1) / 2 - vz / 2;
@@ -436,11 +369,243 @@ __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev0 F, float* x0,
       const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
       if ((ox <= hx) && (oy <= hy) && (oz <= hz)) sum = sum + cv[q];
     }
-    const float r = inv_pow2(parity3(vx, vy, vz)) * sum;
-    float* xd = TO0 ? x0 : D.x;
-    xd[v] = xd[v] + r;
+    D.x[v] = D.x[v] + inv_pow2(parity3(vx, vy, vz)) * sum;
   }
 }
+
+// ---- fused level-0 passes.  A CTA of 32 x 8 threads owns a 28 x 12 x 8
+// box of fine cells (28 x 12 in 2D) and stages code and residual of the box
+// plus a 2-cell halo -- a 32 x 16 x 12 region, one warp per region row -- in
+// shared memory.  Every cell goes through exactly the float operations of
+// the per-colour Gauss-Seidel passes, in the same order; halo cells are
+// recomputed by each CTA that needs them.
+constexpr int kTX = 28, kTY = 12, kTZ = 8;
+template <bool IS3D>
+struct Tile0 {
+  static constexpr int tz = IS3D ? kTZ : 1, hz = IS3D ? 2 : 0;
+  static constexpr int RX = 32, RY = 16, RZ = tz + 2 * hz;
+  static constexpr int NR = RX * RY * RZ;
+  static constexpr int PER = RZ * 2;  // region cells per thread: (ty, ty+8) x RZ planes
+  static constexpr size_t smem = (size_t)NR * (sizeof(uint16_t) + 2 * sizeof(float));
+  // level-1 parents of the region (the region starts at an even coordinate)
+  static constexpr int CX = RX / 2 + 1, CY = RY / 2 + 1, CZ = IS3D ? RZ / 2 + 1 : 1;
+  static constexpr int CN = CX * CY * CZ;
+};
+// region cell k of this thread: x = lane, y = ty + 8 (k & 1), z = k >> 1
+#define T0_CELL(k, lx, ly, lz, q)                          \
+  const int lx = threadIdx.x & 31;                         \
+  const int ly = (threadIdx.x >> 5) + 8 * ((k) & 1);       \
+  const int lz = (k) >> 1;                                 \
+  const int q = lx + T::RX * (ly + T::RY * lz);
+
+// the linked neighbours (kLow/kHigh order of the reference's sums) added
+template <bool IS3D>
+__device__ __forceinline__ float add_links(int c, const float* __restrict__ sx, int q, float sum) {
+  constexpr int RX = 32, RXY = 32 * 16;
+  if (c & kLowX) sum = sum + sx[q - 1];
+  if (c & kHighX) sum = sum + sx[q + 1];
+  if (c & kLowY) sum = sum + sx[q - RX];
+  if (c & kHighY) sum = sum + sx[q + RX];
+  if (IS3D) {
+    if (c & kLowZ) sum = sum + sx[q - RXY];
+    if (c & kHighZ) sum = sum + sx[q + RXY];
+  }
+  return sum;
+}
+
+// stage code and residual (masked to active cells) of the region; the
+// loads of one chunk are all issued before its stores
+template <bool IS3D>
+__device__ __forceinline__ void tile0_load(const Lev0& F, const float* __restrict__ res, uint16_t* scode, float* sres,
+                                           const float* __restrict__ xsrc, float* sx, int ox, int oy, int oz) {
+  using T = Tile0<IS3D>;
+  constexpr int CH = 8;
+  const Dims& d = F.d;
+#pragma unroll 1
+  for (int k0 = 0; k0 < T::PER; k0 += CH) {
+    int cv[CH];
+    float rv[CH], xv[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+      const int k = k0 + j;
+      T0_CELL(k, lx, ly, lz, q)
+      (void)q;
+      const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+      const bool in = k < T::PER && gx >= 0 && gy >= 0 && gz >= 0 && gx < d.nx && gy < d.ny && gz < d.nz;
+      const long long g = in ? ix(d, gx, gy, gz) : 0;
+      cv[j] = in ? F.code[g] : 0;
+      rv[j] = in ? res[g] : 0.f;
+      xv[j] = (in && xsrc) ? xsrc[g] : 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+      const int k = k0 + j;
+      if (k >= T::PER) continue;
+      T0_CELL(k, lx, ly, lz, q)
+      (void)lx; (void)ly; (void)lz;
+      scode[q] = (uint16_t)cv[j];
+      sres[q] = (cv[j] & kMgActive) ? rv[j] : 0.f;
+      if (xsrc) sx[q] = xv[j];
+    }
+  }
+}
+
+__device__ __forceinline__ float scaled_b(int c, float r) { return (c & kMgTrivial) ? r * kTrivialScale : r; }
+
+// V-cycle entry on level 0: colour 0 from x = 0, colour 1, then the
+// residual (knSmoothColor x2 + knCalcResidual); writes x (to F.xd) and r of
+// the box
+template <bool IS3D>
+__global__ void __launch_bounds__(256, 3) k_mg0_down(Lev0 F, const float* __restrict__ res, const CgScalars* sc) {
+  if (sc->done) return;
+  using T = Tile0<IS3D>;
+  extern __shared__ __align__(16) unsigned char t0_smem[];
+  float* sres = (float*)t0_smem;
+  float* sx = sres + T::NR;
+  uint16_t* scode = (uint16_t*)(sx + T::NR);
+  const Dims& d = F.d;
+  const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2, oz = blockIdx.z * T::tz - T::hz;
+  tile0_load<IS3D>(F, res, scode, sres, nullptr, sx, ox, oy, oz);
+  __syncthreads();
+  // colour 0 from the zero guess: x = b / A0, over the whole region
+#pragma unroll 4
+  for (int k = 0; k < T::PER; k++) {
+    T0_CELL(k, lx, ly, lz, q)
+    const int c = scode[q];
+    float v = 0.f;
+    if ((((ox + lx) + (oy + ly) + (oz + lz)) & 1) == 0 && (c & kMgActive))
+      v = scaled_b(c, sres[q]) / l0_diag(c, F.a0f, ix(d, ox + lx, oy + ly, oz + lz));
+    sx[q] = v;
+  }
+  __syncthreads();
+  // colour 1 on the region minus its outer ring (reads colour-0 values only)
+#pragma unroll 4
+  for (int k = 0; k < T::PER; k++) {
+    T0_CELL(k, lx, ly, lz, q)
+    if (lx < 1 || lx > T::RX - 2 || ly < 1 || ly > T::RY - 2) continue;
+    if (IS3D && (lz < 1 || lz > T::RZ - 2)) continue;
+    const int c = scode[q];
+    if ((((ox + lx) + (oy + ly) + (oz + lz)) & 1) == 0 || !(c & kMgActive)) continue;
+    sx[q] = add_links<IS3D>(c, sx, q, scaled_b(c, sres[q])) / l0_diag(c, F.a0f, ix(d, ox + lx, oy + ly, oz + lz));
+  }
+  __syncthreads();
+  // residual and x of the owned box
+#pragma unroll 4
+  for (int k = 0; k < T::PER; k++) {
+    T0_CELL(k, lx, ly, lz, q)
+    if (lx < 2 || lx >= 2 + kTX || ly < 2 || ly >= 2 + kTY || lz < T::hz || lz >= T::hz + T::tz) continue;
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+    if (gx >= d.nx || gy >= d.ny || gz >= d.nz) continue;
+    const long long g = ix(d, gx, gy, gz);
+    const int c = scode[q];
+    F.xd[g] = sx[q];
+    if (!(c & kMgActive)) continue;
+    float sum = add_links<IS3D>(c, sx, q, scaled_b(c, sres[q]));
+    sum = sum - l0_diag(c, F.a0f, g) * sx[q];
+    F.r[g] = sum;
+  }
+}
+
+// V-cycle exit on level 0: interpolation from level 1 added to x
+// (knInterpolate + knAddAssign), colour 1, colour 0, then (unless init)
+// sigmaNew = dot(x, residual) and beta like GridCg::iterate.  It reads x
+// from F.xd, halo included, and writes the result to x0: reading and writing
+// one array would race with the neighbouring CTAs' writes.
+template <bool IS3D, bool DOT>
+__global__ void __launch_bounds__(256, 3) k_mg0_up(Lev0 F, const float* __restrict__ res, float* x0, Lev C, double* part,
+                                                   CgScalars* sc) {
+  if (sc->done) return;
+  using T = Tile0<IS3D>;
+  extern __shared__ __align__(16) unsigned char t0_smem[];
+  float* sres = (float*)t0_smem;
+  float* sx = sres + T::NR;
+  uint16_t* scode = (uint16_t*)(sx + T::NR);
+  __shared__ float scx[T::CN];
+  const Dims& d = F.d;
+  const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2, oz = blockIdx.z * T::tz - T::hz;
+  tile0_load<IS3D>(F, res, scode, sres, F.xd, sx, ox, oy, oz);
+  // coarse parents of the region: level-1 vertices c*0 .. c*0 + C* - 1
+  const int cx0 = ox >> 1, cy0 = oy >> 1, cz0 = oz >> 1;
+  {
+    constexpr int NIT = (T::CN + 255) / 256;
+    float cv[NIT];
+#pragma unroll
+    for (int k = 0; k < NIT; k++) {
+      const int q = threadIdx.x + 256 * k;
+      const int ax = cx0 + q % T::CX, ay = cy0 + (q / T::CX) % T::CY, az = cz0 + q / (T::CX * T::CY);
+      const bool in = q < T::CN && ax >= 0 && ay >= 0 && az >= 0 && ax < C.sx && ay < C.sy && az < C.sz;
+      cv[k] = in ? C.x[lin(C, ax, ay, az)] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < NIT; k++) {
+      const int q = threadIdx.x + 256 * k;
+      if (q < T::CN) scx[q] = cv[k];
+    }
+  }
+  __syncthreads();
+  // x + I * x[1] over the whole region (inactive cells keep x = 0;
+  // inactive coarse vertices hold x = 0)
+#pragma unroll 4
+  for (int k = 0; k < T::PER; k++) {
+    T0_CELL(k, lx, ly, lz, q)
+    if (!(scode[q] & kMgActive)) continue;
+    const int vx = ox + lx, vy = oy + ly, vz = oz + lz;
+    const int hx = vx & 1, hy = vy & 1, hz = vz & 1;  // two parents along odd axes
+    const int b0 = (vx / 2 - cx0) + T::CX * ((vy / 2 - cy0) + T::CY * (vz / 2 - cz0));
+    float sum = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int ax = j & 1, ay = (j >> 1) & 1, az = j >> 2;
+      if (ax <= hx && ay <= hy && az <= hz) sum = sum + scx[b0 + ax + T::CX * (ay + T::CY * az)];
+    }
+    sx[q] = sx[q] + inv_pow2(hx + hy + hz) * sum;
+  }
+  __syncthreads();
+  // colour 1 on the region minus its outer ring
+#pragma unroll 4
+  for (int k = 0; k < T::PER; k++) {
+    T0_CELL(k, lx, ly, lz, q)
+    if (lx < 1 || lx > T::RX - 2 || ly < 1 || ly > T::RY - 2) continue;
+    if (IS3D && (lz < 1 || lz > T::RZ - 2)) continue;
+    const int c = scode[q];
+    if ((((ox + lx) + (oy + ly) + (oz + lz)) & 1) == 0 || !(c & kMgActive)) continue;
+    sx[q] = add_links<IS3D>(c, sx, q, scaled_b(c, sres[q])) / l0_diag(c, F.a0f, ix(d, ox + lx, oy + ly, oz + lz));
+  }
+  __syncthreads();
+  // colour 0 of the owned box (reads colour-1 values only), store, dot
+  FSum acc;
+#pragma unroll 4
+  for (int k = 0; k < T::PER; k++) {
+    T0_CELL(k, lx, ly, lz, q)
+    if (lx < 2 || lx >= 2 + kTX || ly < 2 || ly >= 2 + kTY || lz < T::hz || lz >= T::hz + T::tz) continue;
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+    if (gx >= d.nx || gy >= d.ny || gz >= d.nz) continue;
+    const long long g = ix(d, gx, gy, gz);
+    const int c = scode[q];
+    float v = sx[q];
+    if (((gx + gy + gz) & 1) == 0 && (c & kMgActive))
+      v = add_links<IS3D>(c, sx, q, scaled_b(c, sres[q])) / l0_diag(c, F.a0f, g);
+    x0[g] = v;
+    if (DOT) acc.add(v * sres[q]);  // inactive cells: x = 0
+  }
+  if (!DOT) return;
+  const double bsum = block_sum(acc.value());
+  const unsigned int nblk = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (threadIdx.x == 0) part[bid] = bsum;
+  if (last_block(&sc->counters[4], nblk)) {
+    const double s = sum_partials(part, nblk);
+    if (threadIdx.x != 0) return;
+    const float sigmaNew = (float)s;
+    sc->beta = sigmaNew / sc->sigma;
+    sc->sigma = sigmaNew;
+    if (!(sc->resNorm < 1e35f)) {
+      sc->status = 2;
+      sc->done = 1;
+    }
+  }
+}
+#undef T0_CELL
 
 // ---- coarsest level: GridMg::solveCG in double-float arithmetic
 // GB300 executes FP64 at a small fraction of its FP32 rate, and a CG on
@@ -658,9 +823,9 @@ constexpr size_t kCgDynSmem = (size_t)kCgNb * kCgThreads * (sizeof(float) + size
 __global__ void __launch_bounds__(256) k_mg_dot_beta(long long n, const float* __restrict__ t, const float* __restrict__ r,
                                                      double* part, CgScalars* sc) {
   if (sc->done) return;
-  double acc = 0.;
-  GRID_STRIDE(idx, n) acc += (double)(t[idx] * r[idx]);
-  const double b = block_sum(acc);
+  FSum acc;
+  GRID_STRIDE(idx, n) acc.add(t[idx] * r[idx]);
+  const double b = block_sum(acc.value());
   if (threadIdx.x == 0) part[blockIdx.x] = b;
   if (last_block(&sc->counters[4], gridDim.x)) {
     const double s = sum_partials(part, gridDim.x);
@@ -741,6 +906,14 @@ int ensure_paths() {
       cudaFuncSetAttribute(k_mg_coarse_cg<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(k_mg_coarse_cg<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(k_mg_coarse_cg<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+    return 1;
+  const int t3 = (int)Tile0<true>::smem, t2 = (int)Tile0<false>::smem;
+  if (cudaFuncSetAttribute(k_mg0_down<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t3) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_down<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t2) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t3) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t3) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t2) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t2) != cudaSuccess)
     return 1;
   g_pathsReady = true;
   return 0;
@@ -898,6 +1071,7 @@ MgHierarchy* mg_hierarchy_create(const Dims& d) {
   h->l0.code = h->alloc<uint16_t>(n0);
   h->l0.a0f = nullptr;
   h->l0.r = L > 1 ? h->alloc<float>(n0) : nullptr;
+  h->l0.xd = L > 1 ? h->alloc<float>(n0) : nullptr;
   h->type0 = h->alloc<int8_t>(n0);
   for (int l = 1; l < L; l++) {
     Lev& v = h->lev[l];
@@ -1042,7 +1216,7 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   float* x0 = b.tmp;
   const float* res = b.residual;
   const Lev none{};
-  const dim3 g0 = grid3(d, kBlk0);
+  const dim3 gt((d.nx + kTX - 1) / kTX, (d.ny + kTY - 1) / kTY, d.is3d ? (d.nz + kTZ - 1) / kTZ : 1);
   static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
   const int ncol = h->is3d ? 8 : 4;
   auto smooth = [&](int l, bool reversed) {
@@ -1065,19 +1239,10 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   } else {
     // level 0 pre-smoothing (colour 0 from x = 0, then colour 1)
     {
-      Fam f(h, "mg_smooth_l0_first");
+      Fam f(h, "mg_down_l0");
       count_launch();
-      k_mg0_smooth<0><<<g0, kBlk0, 0, s>>>(l0, res, x0, 0, sc);
-    }
-    {
-      Fam f(h, "mg_smooth_l0");
-      count_launch();
-      k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, 1, sc);
-    }
-    {
-      Fam f(h, "mg_residual_l0");
-      count_launch();
-      k_mg0_residual<<<blocks_for(d.n), kThreads1, 0, s>>>(l0, res, x0, sc);
+      if (h->is3d) k_mg0_down<true><<<gt, kThreads1, Tile0<true>::smem, s>>>(l0, res, sc);
+      else k_mg0_down<false><<<gt, kThreads1, Tile0<false>::smem, s>>>(l0, res, sc);
     }
     {
       Fam f(h, "mg_restrict_l0");
@@ -1103,22 +1268,24 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       {
       Fam f(h, "mg_transfer_coarse");
       count_launch();
-      k_mg_interp_add<false><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], l0, nullptr, h->lev[l + 1], sc);
+      if (h->is3d) k_mg_interp_add<true><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], h->lev[l + 1], sc);
+      else k_mg_interp_add<false><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], h->lev[l + 1], sc);
       }
       smooth(l, true);
     }
     {
-      Fam f(h, "mg_interp_l0");
+      Fam f(h, "mg_up_l0");
       count_launch();
-      k_mg_interp_add<true><<<blocks_for(d.n), kThreads1, 0, s>>>(none, l0, x0, h->lev[1], sc);
-    }
-    for (int c = 1; c >= 0; c--) {
-      Fam f(h, "mg_smooth_l0");
-      count_launch();
-      k_mg0_smooth<1><<<g0, kBlk0, 0, s>>>(l0, res, x0, c, sc);
+      if (h->is3d) {
+        if (init) k_mg0_up<true, false><<<gt, kThreads1, Tile0<true>::smem, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+        else k_mg0_up<true, true><<<gt, kThreads1, Tile0<true>::smem, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+      } else {
+        if (init) k_mg0_up<false, false><<<gt, kThreads1, Tile0<false>::smem, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+        else k_mg0_up<false, true><<<gt, kThreads1, Tile0<false>::smem, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+      }
     }
   }
-  if (!init) {
+  if (!init && L == 0) {
     Fam f(h, "mg_dot");
     count_launch();
     k_mg_dot_beta<<<b.nblocks, kThreads1, 0, s>>>(d.n, b.tmp, b.residual, b.part, b.sc);

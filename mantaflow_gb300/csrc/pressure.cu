@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict_
       rhs[idx] = 0.f;  // fresh grid: the border stays zero
     }
   }
+  if (!nblk) return;  // the sums serve enforceCompatibility only
   const unsigned int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
   const double bs = block_sum(sum);
   const double bc = block_sum(cnt);
@@ -110,7 +111,6 @@ __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict_
     part[2 * b] = bs;
     part[2 * b + 1] = bc;
   }
-  (void)nblk;
 }
 
 // rhs += (Real)(-sum / (Real)cnt) on every cell (pressure.cpp:296-297)
@@ -229,13 +229,13 @@ __global__ void k_pcg_init(long long n, float* p, const float* __restrict__ rhs,
 __global__ void __launch_bounds__(256) k_pcg_set_search(long long n, const float* __restrict__ tmp,
                                                         const float* __restrict__ r, float* search, double* part,
                                                         CgScalars* sc) {
-  double acc = 0.;
+  FSum acc;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
     const float t = tmp[idx];
     search[idx] = t;
-    acc += (double)(t * r[idx]);
+    acc.add(t * r[idx]);
   }
-  const double b = block_sum(acc);
+  const double b = block_sum(acc.value());
   if (threadIdx.x == 0) part[blockIdx.x] = b;
   if (last_block(&sc->counters[0], gridDim.x)) {
     const double s = sum_partials(part, gridDim.x);
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(256) k_pcg_set_search(long long n, const float
 __global__ void __launch_bounds__(256) k_pcg_spmv(Dims d, const code_t* __restrict__ code, const float* __restrict__ A0f,
                                                   const float* __restrict__ x, float* y, double* part, CgScalars* sc) {
   if (sc->done) return;
-  double acc = 0.;
+  FSum acc;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < d.n; idx += (long long)gridDim.x * blockDim.x) {
     const int c = code[idx];
     const float xc = x[idx];
@@ -265,9 +265,9 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(Dims d, const code_t* __restri
       if (c & kHighZ) v = v - x[idx + d.sz];
     }
     y[idx] = v;
-    acc += (double)(v * xc);
+    acc.add(v * xc);
   }
-  const double b = block_sum(acc);
+  const double b = block_sum(acc.value());
   if (threadIdx.x == 0) part[blockIdx.x] = b;
   if (last_block(&sc->counters[1], gridDim.x)) {
     const double s = sum_partials(part, gridDim.x);
@@ -331,13 +331,13 @@ __global__ void __launch_bounds__(256) k_pcg_axpy(long long n, float* p, const f
 __global__ void __launch_bounds__(256) k_pcg_copy_dot(long long n, const float* __restrict__ r, float* tmp, double* part,
                                                       CgScalars* sc) {
   if (sc->done) return;
-  double acc = 0.;
+  FSum acc;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
     const float v = r[idx];
     tmp[idx] = v;
-    acc += (double)(v * v);
+    acc.add(v * v);
   }
-  const double b = block_sum(acc);
+  const double b = block_sum(acc.value());
   if (threadIdx.x == 0) part[blockIdx.x] = b;
   if (last_block(&sc->counters[3], gridDim.x)) {
     const double s = sum_partials(part, gridDim.x);
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(256) k_pcg_spmv4(Dims d, const code_t* __restr
                                                    const float* __restrict__ A0f, const float* __restrict__ x,
                                                    float* y, double* part, CgScalars* sc) {
   if (sc->done) return;
-  double acc = 0.;
+  FSum acc;
   const long long nq = d.n >> 2;
   const float4* x4 = reinterpret_cast<const float4*>(x);
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
@@ -403,11 +403,11 @@ __global__ void __launch_bounds__(256) k_pcg_spmv4(Dims d, const code_t* __restr
         if (ce & kHighZ) v = v - fget(zhi, e);
       }
       out[e] = v;
-      acc += (double)(v * xv);
+      acc.add(v * xv);
     }
     reinterpret_cast<float4*>(y)[q] = make_float4(out[0], out[1], out[2], out[3]);
   }
-  const double b = block_sum(acc);
+  const double b = block_sum(acc.value());
   if (threadIdx.x == 0) part[blockIdx.x] = b;
   if (last_block(&sc->counters[1], gridDim.x)) {
     const double s = sum_partials(part, gridDim.x);
@@ -798,11 +798,11 @@ __global__ void k_replace_clamped_gf(Dims d, const int* __restrict__ flags, Mac 
 
 // ------------------------------------------------------------- launchers
 void launch_make_rhs(const PcgBuffers& b, const float* vu, const float* vv, const float* vw, const float* perCellCorr,
-                     const float* phi, const float* curv, float surfTens, float gfClamp, cudaStream_t s) {
+                     const float* phi, const float* curv, float surfTens, float gfClamp, bool sums, cudaStream_t s) {
   const dim3 g = grid3(b.d, kBlk);
   count_launch();
   k_make_rhs<<<g, kBlk, 0, s>>>(b.d, b.flags, b.rhs, vu, vv, vw, perCellCorr, phi, curv, surfTens, gfClamp, b.part, b.sc,
-                                g.x * g.y * g.z);
+                                sums ? g.x * g.y * g.z : 0u);
 }
 void launch_compat_shift(const PcgBuffers& b, cudaStream_t s) {
   const dim3 g = grid3(b.d, kBlk);

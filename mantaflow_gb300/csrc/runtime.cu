@@ -971,7 +971,7 @@ extern "C" int mg_compute_pressure_rhs(mg_grid rhs, mg_grid vel, mg_grid pressur
   {
     ProfScope ps(s, "make_rhs");
     launch_make_rhs(b, v.u, v.v, v.w, perCellCorr ? perCellCorr->f() : nullptr, phi ? phi->f() : nullptr,
-                    curv ? curv->f() : nullptr, p->surfTens, p->gfClamp, s->stream);
+                    curv ? curv->f() : nullptr, p->surfTens, p->gfClamp, p->enforceCompatibility != 0, s->stream);
   }
   CKL();
   if (p->enforceCompatibility) {
@@ -1294,6 +1294,39 @@ extern "C" int mg_solve_pressure(mg_grid vel, mg_grid pressure, mg_grid flags, c
     NEED_GRID(retRhs, "solvePressure");
     CK(cudaMemcpyAsync(retRhs->data, rhs.p, sizeof(float) * (size_t)s->d.n, cudaMemcpyDeviceToDevice, s->stream));
   }
+  return MG_OK;
+}
+
+extern "C" int mg_multigrid_vcycle(mg_grid flags, mg_grid phi, mg_grid src, mg_grid dst, float gfClamp,
+                                   float coarseAccuracy) {
+  NEED_GRID(flags, "mg_multigrid_vcycle");
+  NEED_GRID(src, "mg_multigrid_vcycle");
+  NEED_GRID(dst, "mg_multigrid_vcycle");
+  mg_solver s = flags->s;
+  int st = ensure_cg_state(s);
+  if (st) return st;
+  PcgBuffers b = cg_buffers(s, flags, nullptr, nullptr);
+  launch_make_codes(b, s->stream);
+  CKL();
+  if (phi) {
+    if (!s->A0f) CK(cudaMalloc(&s->A0f, sizeof(float) * (size_t)s->d.n));
+    b.A0f = s->A0f;
+    launch_ghost_fluid_diag(b, phi->f(), gfClamp, s->stream);
+    CKL();
+  }
+  mgpu::MgHierarchy* h = mg_hierarchy_create(s->d);
+  if (!h) return fail(MG_ERR_NOMEM, "mg_multigrid_vcycle: multigrid allocation failed");
+  CgScalars init{};
+  CK(cudaMemcpyAsync(s->sc, &init, sizeof(CgScalars), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(b.residual, src->f(), sizeof(float) * (size_t)s->d.n, cudaMemcpyDeviceToDevice, s->stream));
+  int e = mg_setup(h, b, coarseAccuracy, s->stream);
+  if (!e) e = mg_apply(h, b, true, s->stream);
+  if (!e)
+    e = cudaMemcpyAsync(dst->f(), b.tmp, sizeof(float) * (size_t)s->d.n, cudaMemcpyDeviceToDevice, s->stream) !=
+        cudaSuccess;
+  cudaStreamSynchronize(s->stream);
+  mg_hierarchy_destroy(h);
+  if (e) return fail(MG_ERR_CUDA, "mg_multigrid_vcycle: multigrid failed");
   return MG_OK;
 }
 

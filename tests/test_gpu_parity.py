@@ -318,6 +318,47 @@ def test_multigrid_ghost_fluid_against_oracle():
     assert np.max(np.abs(vel.numpy() - vo)) <= 1e-4
 
 
+@pytest.mark.parametrize("shape,liquid", [((40, 36, 30), False), ((37, 29, 41), True), ((90, 70, 1), False),
+                                          ((24, 20, 18), False)])
+def test_multigrid_vcycle_against_oracle(shape, liquid):
+    """One V-cycle of the multigrid preconditioner (GridMg::setA + setRhs +
+    doVCycle) on a random residual against the oracle's restatement of the
+    reference.  Smoothing, restriction, interpolation and the Galerkin
+    operators repeat the reference's float operations, so the cells must
+    agree bit for bit; only the coarsest-level CG (double-float, tree sums)
+    may move a last bit, which the smoothers then spread a little."""
+    import ctypes as C
+    f, _ = _obstacle_scene(shape, 31, liquid=liquid)
+    nx, ny, nz = shape
+    rng = np.random.default_rng(5)
+    src = (rng.random(f.shape, dtype=np.float32) - 0.5).astype(np.float32)
+    src[(f & og.FLUID) == 0] = 0
+    phi_a = None
+    A = og.make_laplace_matrix(f)
+    if liquid:
+        phi_a = np.zeros(f.shape, np.float32)
+        og.box_sdf(phi_a, (0, 0, 0), (nx, ny * 0.55 - 0.3, nz))
+        og.apply_ghost_fluid_diagonal(A[0], f, phi_a)
+    L = og.lib()
+    mg = L.og_mg_create(og.dims(f.shape))
+    want = np.zeros(f.shape, np.float32)
+    L.og_mg_vcycle(mg, A[0], A[1], A[2], A[3], want, src, C.c_float(1e-7))
+    L.og_mg_destroy(mg)
+    s = m.Solver(name="vc", gridSize=m.vec3(nx, ny, nz), dim=3 if nz > 1 else 2)
+    flags = grid_from(s, m.FlagGrid, f)
+    sg = grid_from(s, m.RealGrid, src)
+    dg = s.create(m.RealGrid)
+    phi = grid_from(s, m.LevelsetGrid, phi_a) if liquid else None
+    from mantaflow_gb300 import _lib as mlib
+    lib = mlib.load()
+    mlib.check(lib.mg_multigrid_vcycle(flags._h, phi._h if phi is not None else None, sg._h, dg._h,
+                                         C.c_float(1e-4), C.c_float(1e-7)))
+    got = dg.numpy()
+    scale = float(np.max(np.abs(want)))
+    assert np.max(np.abs(got - want)) <= 1e-5 * scale, (np.max(np.abs(got - want)), scale)
+    assert np.mean(got == want) >= 0.999, np.mean(got == want)
+
+
 def test_pcnone_rejected_like_reference():
     g = load("pressure_3d")
     s = make_solver(g["flags_smoke"].shape)
