@@ -23,6 +23,21 @@
 #include <omp.h>
 #endif
 
+/* Real-typed helpers: the float build keeps the reference's float calls and
+ * literals (OG_R(0.5) is 0.5f), the double build the double ones */
+#define OG_R(x) ((og_real)(x))
+#if defined(OG_REAL_IS_DOUBLE)
+#define og_fabs fabs
+#define og_sqrt sqrt
+#define OG_REAL_MAX DBL_MAX
+#define OG_VEC_EPS 1e-10
+#else
+#define og_fabs fabsf
+#define og_sqrt sqrtf
+#define OG_REAL_MAX FLT_MAX
+#define OG_VEC_EPS 1e-6f
+#endif
+
 static int g_threads = 1;
 void og_set_num_threads(int n) { g_threads = n < 1 ? 1 : n; }
 int og_get_num_threads(void) { return g_threads; }
@@ -51,41 +66,41 @@ static inline int iclamp(int v, int lo, int hi) { if (v < lo) return lo; if (v >
 
 /* ------------------------------------------------------------------------ */
 /* MAC accessors, source/grid.h:424-470.  0.5*(a+b) and 0.25*(...) are exact
- * scalings of a float sum, so float arithmetic reproduces them.            */
+ * scalings of a Real sum, so Real arithmetic reproduces them.            */
 
-typedef struct { float x, y, z; } v3;
+typedef struct { og_real x, y, z; } v3;
 
-static inline v3 mac_centered(og_dims d, const float* u, ll idx) {
+static inline v3 mac_centered(og_dims d, const og_real* u, ll idx) {
   v3 v;
-  v.x = 0.5f * (u[3 * idx + 0] + u[3 * (idx + 1) + 0]);
-  v.y = 0.5f * (u[3 * idx + 1] + u[3 * (idx + SY(d)) + 1]);
-  v.z = 0.f;
-  if (d.is3d) v.z = 0.5f * (u[3 * idx + 2] + u[3 * (idx + SZ(d)) + 2]);
+  v.x = OG_R(0.5) * (u[3 * idx + 0] + u[3 * (idx + 1) + 0]);
+  v.y = OG_R(0.5) * (u[3 * idx + 1] + u[3 * (idx + SY(d)) + 1]);
+  v.z = OG_R(0.);
+  if (d.is3d) v.z = OG_R(0.5) * (u[3 * idx + 2] + u[3 * (idx + SZ(d)) + 2]);
   return v;
 }
-static inline v3 mac_at_x(og_dims d, const float* u, ll idx) {
+static inline v3 mac_at_x(og_dims d, const og_real* u, ll idx) {
   const ll Y = SY(d), Z = SZ(d);
   v3 v;
   v.x = u[3 * idx];
-  v.y = 0.25f * (u[3 * idx + 1] + u[3 * (idx - 1) + 1] + u[3 * (idx + Y) + 1] + u[3 * (idx + Y - 1) + 1]);
-  v.z = 0.f;
-  if (d.is3d) v.z = 0.25f * (u[3 * idx + 2] + u[3 * (idx - 1) + 2] + u[3 * (idx + Z) + 2] + u[3 * (idx + Z - 1) + 2]);
+  v.y = OG_R(0.25) * (u[3 * idx + 1] + u[3 * (idx - 1) + 1] + u[3 * (idx + Y) + 1] + u[3 * (idx + Y - 1) + 1]);
+  v.z = OG_R(0.);
+  if (d.is3d) v.z = OG_R(0.25) * (u[3 * idx + 2] + u[3 * (idx - 1) + 2] + u[3 * (idx + Z) + 2] + u[3 * (idx + Z - 1) + 2]);
   return v;
 }
-static inline v3 mac_at_y(og_dims d, const float* u, ll idx) {
+static inline v3 mac_at_y(og_dims d, const og_real* u, ll idx) {
   const ll Y = SY(d), Z = SZ(d);
   v3 v;
-  v.x = 0.25f * (u[3 * idx] + u[3 * (idx - Y)] + u[3 * (idx + 1)] + u[3 * (idx + 1 - Y)]);
+  v.x = OG_R(0.25) * (u[3 * idx] + u[3 * (idx - Y)] + u[3 * (idx + 1)] + u[3 * (idx + 1 - Y)]);
   v.y = u[3 * idx + 1];
-  v.z = 0.f;
-  if (d.is3d) v.z = 0.25f * (u[3 * idx + 2] + u[3 * (idx - Y) + 2] + u[3 * (idx + Z) + 2] + u[3 * (idx + Z - Y) + 2]);
+  v.z = OG_R(0.);
+  if (d.is3d) v.z = OG_R(0.25) * (u[3 * idx + 2] + u[3 * (idx - Y) + 2] + u[3 * (idx + Z) + 2] + u[3 * (idx + Z - Y) + 2]);
   return v;
 }
-static inline v3 mac_at_z(og_dims d, const float* u, ll idx) {
+static inline v3 mac_at_z(og_dims d, const og_real* u, ll idx) {
   const ll Y = SY(d), Z = SZ(d);
   v3 v;
-  v.x = 0.25f * (u[3 * idx] + u[3 * (idx - Z)] + u[3 * (idx + 1)] + u[3 * (idx + 1 - Z)]);
-  v.y = 0.25f * (u[3 * idx + 1] + u[3 * (idx - Z) + 1] + u[3 * (idx + Y) + 1] + u[3 * (idx + Y - Z) + 1]);
+  v.x = OG_R(0.25) * (u[3 * idx] + u[3 * (idx - Z)] + u[3 * (idx + 1)] + u[3 * (idx + 1 - Z)]);
+  v.y = OG_R(0.25) * (u[3 * idx + 1] + u[3 * (idx - Z) + 1] + u[3 * (idx + Y) + 1] + u[3 * (idx + Y - Z) + 1]);
   v.z = u[3 * idx + 2];
   return v;
 }
@@ -96,42 +111,42 @@ static inline v3 mac_at_z(og_dims d, const float* u, ll idx) {
 
 typedef struct {
   int xi, yi, zi;
-  float s0, s1, t0, t1, f0, f1;
+  og_real s0, s1, t0, t1, f0, f1;
 } wts;
 
-static inline wts build_index(og_dims d, float x, float y, float z) {
+static inline wts build_index(og_dims d, og_real x, og_real y, og_real z) {
   wts w;
-  float px = x - 0.5f, py = y - 0.5f, pz = z - 0.5f;
+  og_real px = x - OG_R(0.5), py = y - OG_R(0.5), pz = z - OG_R(0.5);
   w.xi = (int)px; w.yi = (int)py; w.zi = (int)pz;
-  w.s1 = px - (float)w.xi; w.s0 = 1.f - w.s1;
-  w.t1 = py - (float)w.yi; w.t0 = 1.f - w.t1;
-  w.f1 = pz - (float)w.zi; w.f0 = 1.f - w.f1;
-  if (px < 0.f) { w.xi = 0; w.s0 = 1.f; w.s1 = 0.f; }
-  if (py < 0.f) { w.yi = 0; w.t0 = 1.f; w.t1 = 0.f; }
-  if (pz < 0.f) { w.zi = 0; w.f0 = 1.f; w.f1 = 0.f; }
-  if (w.xi >= d.nx - 1) { w.xi = d.nx - 2; w.s0 = 0.f; w.s1 = 1.f; }
-  if (w.yi >= d.ny - 1) { w.yi = d.ny - 2; w.t0 = 0.f; w.t1 = 1.f; }
-  if (d.nz > 1) { if (w.zi >= d.nz - 1) { w.zi = d.nz - 2; w.f0 = 0.f; w.f1 = 1.f; } }
+  w.s1 = px - (og_real)w.xi; w.s0 = OG_R(1.) - w.s1;
+  w.t1 = py - (og_real)w.yi; w.t0 = OG_R(1.) - w.t1;
+  w.f1 = pz - (og_real)w.zi; w.f0 = OG_R(1.) - w.f1;
+  if (px < OG_R(0.)) { w.xi = 0; w.s0 = OG_R(1.); w.s1 = OG_R(0.); }
+  if (py < OG_R(0.)) { w.yi = 0; w.t0 = OG_R(1.); w.t1 = OG_R(0.); }
+  if (pz < OG_R(0.)) { w.zi = 0; w.f0 = OG_R(1.); w.f1 = OG_R(0.); }
+  if (w.xi >= d.nx - 1) { w.xi = d.nx - 2; w.s0 = OG_R(0.); w.s1 = OG_R(1.); }
+  if (w.yi >= d.ny - 1) { w.yi = d.ny - 2; w.t0 = OG_R(0.); w.t1 = OG_R(1.); }
+  if (d.nz > 1) { if (w.zi >= d.nz - 1) { w.zi = d.nz - 2; w.f0 = OG_R(0.); w.f1 = OG_R(1.); } }
   return w;
 }
 
-static inline wts build_index_shift(og_dims d, float x, float y, float z) {
+static inline wts build_index_shift(og_dims d, og_real x, og_real y, og_real z) {
   wts w;
   w.xi = (int)x; w.yi = (int)y; w.zi = (int)z;
-  w.s1 = x - (float)w.xi; w.s0 = 1.f - w.s1;
-  w.t1 = y - (float)w.yi; w.t0 = 1.f - w.t1;
-  w.f1 = z - (float)w.zi; w.f0 = 1.f - w.f1;
-  if (x < 0) { w.xi = 0; w.s0 = 1.f; w.s1 = 0.f; }
-  if (y < 0) { w.yi = 0; w.t0 = 1.f; w.t1 = 0.f; }
-  if (z < 0) { w.zi = 0; w.f0 = 1.f; w.f1 = 0.f; }
-  if (w.xi >= d.nx - 1) { w.xi = d.nx - 2; w.s0 = 0.f; w.s1 = 1.f; }
-  if (w.yi >= d.ny - 1) { w.yi = d.ny - 2; w.t0 = 0.f; w.t1 = 1.f; }
-  if (d.nz > 1) { if (w.zi >= d.nz - 1) { w.zi = d.nz - 2; w.f0 = 0.f; w.f1 = 1.f; } }
+  w.s1 = x - (og_real)w.xi; w.s0 = OG_R(1.) - w.s1;
+  w.t1 = y - (og_real)w.yi; w.t0 = OG_R(1.) - w.t1;
+  w.f1 = z - (og_real)w.zi; w.f0 = OG_R(1.) - w.f1;
+  if (x < 0) { w.xi = 0; w.s0 = OG_R(1.); w.s1 = OG_R(0.); }
+  if (y < 0) { w.yi = 0; w.t0 = OG_R(1.); w.t1 = OG_R(0.); }
+  if (z < 0) { w.zi = 0; w.f0 = OG_R(1.); w.f1 = OG_R(0.); }
+  if (w.xi >= d.nx - 1) { w.xi = d.nx - 2; w.s0 = OG_R(0.); w.s1 = OG_R(1.); }
+  if (w.yi >= d.ny - 1) { w.yi = d.ny - 2; w.t0 = OG_R(0.); w.t1 = OG_R(1.); }
+  if (d.nz > 1) { if (w.zi >= d.nz - 1) { w.zi = d.nz - 2; w.f0 = OG_R(0.); w.f1 = OG_R(1.); } }
   return w;
 }
 
-/* interpol<T> on one float channel: data[stride*idx + c] */
-static inline float interp_ch(og_dims d, const float* data, int stride, int c, float x, float y, float z) {
+/* interpol<T> on one Real channel: data[stride*idx + c] */
+static inline og_real interp_ch(og_dims d, const og_real* data, int stride, int c, og_real x, og_real y, og_real z) {
   wts w = build_index(d, x, y, z);
   const ll X = 1, Y = SY(d), Z = SZ(d);
   const ll idx = (ll)w.xi + Y * w.yi + Z * w.zi;
@@ -142,7 +157,7 @@ static inline float interp_ch(og_dims d, const float* data, int stride, int c, f
 }
 
 /* interpolMAC (util/interpol.h:127-157) */
-static inline v3 interp_mac(og_dims d, const float* u, float x, float y, float z) {
+static inline v3 interp_mac(og_dims d, const og_real* u, og_real x, og_real y, og_real z) {
   wts w = build_index(d, x, y, z);
   wts s = build_index_shift(d, x, y, z);
   const ll X = 1, Y = SY(d), Z = SZ(d);
@@ -175,66 +190,66 @@ static inline v3 interp_mac(og_dims d, const float* u, float x, float y, float z
 /* Catmull-Rom cubic, util/interpolHigh.h:22-40, 42-160.  For Real grids the
  * reference forms a2/a3 in double (double literals) and rounds once.        */
 
-static inline float cubic_real(float t, const float* p) {
-  float d0 = (float)((double)(p[2] - p[0]) * 0.5);
-  float d1 = (float)((double)(p[3] - p[1]) * 0.5);
-  float dk = p[2] - p[1];
-  float a0 = p[1], a1 = d0;
-  float a2 = (float)(3.0 * dk - 2.0 * d0 - d1);
-  float a3 = (float)(-2.0 * dk + d0 + d1);
-  float sq = t * t, cu = sq * t;
+static inline og_real cubic_real(og_real t, const og_real* p) {
+  og_real d0 = (og_real)((double)(p[2] - p[0]) * 0.5);
+  og_real d1 = (og_real)((double)(p[3] - p[1]) * 0.5);
+  og_real dk = p[2] - p[1];
+  og_real a0 = p[1], a1 = d0;
+  og_real a2 = (og_real)(3.0 * dk - 2.0 * d0 - d1);
+  og_real a3 = (og_real)(-2.0 * dk + d0 + d1);
+  og_real sq = t * t, cu = sq * t;
   return a3 * cu + a2 * sq + a1 * t + a0;
 }
-/* Vec3 variant: every Vec3 operator rounds to float per component */
-static inline float cubic_vec(float t, const float* p) {
-  float d0 = (float)((double)(p[2] - p[0]) * 0.5);
-  float d1 = (float)((double)(p[3] - p[1]) * 0.5);
-  float dk = p[2] - p[1];
-  float a0 = p[1], a1 = d0;
-  float a2 = (float)(3.0 * dk);
-  a2 = a2 - (float)(2.0 * d0);
+/* Vec3 variant: every Vec3 operator rounds to Real per component */
+static inline og_real cubic_vec(og_real t, const og_real* p) {
+  og_real d0 = (og_real)((double)(p[2] - p[0]) * 0.5);
+  og_real d1 = (og_real)((double)(p[3] - p[1]) * 0.5);
+  og_real dk = p[2] - p[1];
+  og_real a0 = p[1], a1 = d0;
+  og_real a2 = (og_real)(3.0 * dk);
+  a2 = a2 - (og_real)(2.0 * d0);
   a2 = a2 - d1;
-  float a3 = (float)(-2.0 * dk);
+  og_real a3 = (og_real)(-2.0 * dk);
   a3 = a3 + d0;
   a3 = a3 + d1;
-  float sq = t * t, cu = sq * t;
+  og_real sq = t * t, cu = sq * t;
   return a3 * cu + a2 * sq + a1 * t + a0;
 }
 
-static float interp_cubic_ch(og_dims d, const float* data, int stride, int c, float x, float y, float z, int vecmode) {
-  float (*cub)(float, const float*) = vecmode ? cubic_vec : cubic_real;
+static og_real interp_cubic_ch(og_dims d, const og_real* data, int stride, int c, og_real x, og_real y, og_real z, int vecmode) {
+  og_real (*cub)(og_real, const og_real*) = vecmode ? cubic_vec : cubic_real;
   const ll Z = SZ(d);
   if (Z == 0) {
-    const float px = x - 0.5f, py = y - 0.5f;
+    const og_real px = x - OG_R(0.5), py = y - OG_R(0.5);
     const int x1 = (int)px, x2 = x1 + 1, x3 = x1 + 2, x0 = x1 - 1;
     const int y1 = (int)py, y2 = y1 + 1, y3 = y1 + 2, y0 = y1 - 1;
     if (x0 < 0 || y0 < 0 || x3 >= d.nx || y3 >= d.ny) return interp_ch(d, data, stride, c, x, y, z);
-    const float xI = px - x1, yI = py - y1;
+    const og_real xI = px - x1, yI = py - y1;
     const int yy[4] = {y0 * d.nx, y1 * d.nx, y2 * d.nx, y3 * d.nx};
     const int xx[4] = {x0, x1, x2, x3};
-    float fin[4];
+    og_real fin[4];
     for (int r = 0; r < 4; r++) {
-      float pts[4];
+      og_real pts[4];
       for (int q = 0; q < 4; q++) pts[q] = data[stride * (ll)(xx[q] + yy[r]) + c];
       fin[r] = cub(xI, pts);
     }
     return cub(yI, fin);
   }
-  const float px = x - 0.5f, py = y - 0.5f, pz = z - 0.5f;
+  const og_real px = x - OG_R(0.5), py = y - OG_R(0.5), pz = z - OG_R(0.5);
   const int x1 = (int)px, x2 = x1 + 1, x3 = x1 + 2, x0 = x1 - 1;
   const int y1 = (int)py, y2 = y1 + 1, y3 = y1 + 2, y0 = y1 - 1;
   const int z1 = (int)pz, z2 = z1 + 1, z3 = z1 + 2, z0 = z1 - 1;
   if (x0 < 0 || y0 < 0 || z0 < 0 || x3 >= d.nx || y3 >= d.ny || z3 >= d.nz) return interp_ch(d, data, stride, c, x, y, z);
-  const float xI = px - x1, yI = py - y1, zI = pz - z1;
+  const og_real xI = px - x1, yI = py - y1, zI = pz - z1;
   const int slab = d.nx * d.ny;
   const int zz[4] = {z0 * slab, z1 * slab, z2 * slab, z3 * slab};
   const int yy[4] = {y0 * d.nx, y1 * d.nx, y2 * d.nx, y3 * d.nx};
   const int xx[4] = {x0, x1, x2, x3};
-  float zp[4];
+  og_real zp[4];
   for (int s = 0; s < 4; s++) {
-    float yp[4];
+    og_real yp[4];
     for (int r = 0; r < 4; r++) {
-      float pts[4];
+      og_real pts[4];
       for (int q = 0; q < 4; q++) pts[q] = data[stride * (ll)(xx[q] + yy[r] + zz[s]) + c];
       yp[r] = cub(xI, pts);
     }
@@ -246,7 +261,7 @@ static float interp_cubic_ch(og_dims d, const float* data, int stride, int c, fl
 /* ------------------------------------------------------------------------ */
 /* SemiLagrange (advection.cpp:25-41) for Real (ch=1) and Vec3 (ch=3) grids */
 
-static void semi_lagrange(og_dims d, const float* vel, float* dst, const float* src, int ch, float dt,
+static void semi_lagrange(og_dims d, const og_real* vel, og_real* dst, const og_real* src, int ch, og_real dt,
                           int orderSpace, int orderTrace) {
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
@@ -254,17 +269,17 @@ static void semi_lagrange(og_dims d, const float* vel, float* dst, const float* 
     for (int j = 1; j < d.ny - 1; j++)
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
-        float px, py, pz;
+        og_real px, py, pz;
         v3 vc = mac_centered(d, vel, idx);
         if (orderTrace == 1) {
-          px = (i + 0.5f) - vc.x * dt;
-          py = (j + 0.5f) - vc.y * dt;
-          pz = (k + 0.5f) - vc.z * dt;
+          px = (i + OG_R(0.5)) - vc.x * dt;
+          py = (j + OG_R(0.5)) - vc.y * dt;
+          pz = (k + OG_R(0.5)) - vc.z * dt;
         } else {
-          const float p0x = i + 0.5f, p0y = j + 0.5f, p0z = k + 0.5f;
-          const float p1x = p0x - (float)((double)(vc.x * dt) * 0.5);
-          const float p1y = p0y - (float)((double)(vc.y * dt) * 0.5);
-          const float p1z = p0z - (float)((double)(vc.z * dt) * 0.5);
+          const og_real p0x = i + OG_R(0.5), p0y = j + OG_R(0.5), p0z = k + OG_R(0.5);
+          const og_real p1x = p0x - (og_real)((double)(vc.x * dt) * 0.5);
+          const og_real p1y = p0y - (og_real)((double)(vc.y * dt) * 0.5);
+          const og_real p1z = p0z - (og_real)((double)(vc.z * dt) * 0.5);
           v3 vi = interp_mac(d, vel, p1x, p1y, p1z);
           px = p0x - vi.x * dt;
           py = p0y - vi.y * dt;
@@ -280,15 +295,15 @@ static void semi_lagrange(og_dims d, const float* vel, float* dst, const float* 
 }
 
 /* cubic MAC sampling, util/interpolHigh.h:171-178 */
-static float interp_cubic_mac_c(og_dims d, const float* u, int c, float x, float y, float z) {
-  if (c == 0) return interp_cubic_ch(d, u, 3, 0, x + 0.5f, y, z, 1);
-  if (c == 1) return interp_cubic_ch(d, u, 3, 1, x, y + 0.5f, z, 1);
-  if (SZ(d) == 0) return 0.f;
-  return interp_cubic_ch(d, u, 3, 2, x, y, z + 0.5f, 1);
+static og_real interp_cubic_mac_c(og_dims d, const og_real* u, int c, og_real x, og_real y, og_real z) {
+  if (c == 0) return interp_cubic_ch(d, u, 3, 0, x + OG_R(0.5), y, z, 1);
+  if (c == 1) return interp_cubic_ch(d, u, 3, 1, x, y + OG_R(0.5), z, 1);
+  if (SZ(d) == 0) return OG_R(0.);
+  return interp_cubic_ch(d, u, 3, 2, x, y, z + OG_R(0.5), 1);
 }
 
 /* SemiLagrangeMAC (advection.cpp:44-77) */
-static void semi_lagrange_mac(og_dims d, const float* vel, float* dst, const float* src, float dt,
+static void semi_lagrange_mac(og_dims d, const og_real* vel, og_real* dst, const og_real* src, og_real dt,
                               int orderSpace, int orderTrace) {
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
@@ -296,33 +311,33 @@ static void semi_lagrange_mac(og_dims d, const float* vel, float* dst, const flo
     for (int j = 1; j < d.ny - 1; j++)
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
-        float out[3];
+        og_real out[3];
         if (orderTrace == 1) {
           v3 a[3];
           a[0] = mac_at_x(d, vel, idx);
           a[1] = mac_at_y(d, vel, idx);
           a[2] = mac_at_z(d, vel, idx);
           for (int c = 0; c < 3; c++) {
-            const float px = (i + 0.5f) - a[c].x * dt;
-            const float py = (j + 0.5f) - a[c].y * dt;
-            const float pz = (k + 0.5f) - a[c].z * dt;
+            const og_real px = (i + OG_R(0.5)) - a[c].x * dt;
+            const og_real py = (j + OG_R(0.5)) - a[c].y * dt;
+            const og_real pz = (k + OG_R(0.5)) - a[c].z * dt;
             out[c] = orderSpace == 1 ? interp_ch(d, src, 3, c, px, py, pz) : interp_cubic_mac_c(d, src, c, px, py, pz);
           }
         } else {
-          const float p0x = (float)(i + 0.5), p0y = (float)(j + 0.5), p0z = (float)(k + 0.5);
+          const og_real p0x = (og_real)(i + 0.5), p0y = (og_real)(j + 0.5), p0z = (og_real)(k + 0.5);
           for (int c = 0; c < 3; c++) {
-            float q0x = (float)i + (c == 0 ? 0.f : 0.5f);
-            float q0y = (float)j + (c == 1 ? 0.f : 0.5f);
-            float q0z = (float)k + (c == 2 ? 0.f : 0.5f);
-            if (c == 0) { q0x = (float)i; q0y = j + 0.5f; q0z = k + 0.5f; }
-            if (c == 1) { q0x = i + 0.5f; q0y = (float)j; q0z = k + 0.5f; }
-            if (c == 2) { q0x = i + 0.5f; q0y = j + 0.5f; q0z = (float)k; }
+            og_real q0x = (og_real)i + (c == 0 ? OG_R(0.) : OG_R(0.5));
+            og_real q0y = (og_real)j + (c == 1 ? OG_R(0.) : OG_R(0.5));
+            og_real q0z = (og_real)k + (c == 2 ? OG_R(0.) : OG_R(0.5));
+            if (c == 0) { q0x = (og_real)i; q0y = j + OG_R(0.5); q0z = k + OG_R(0.5); }
+            if (c == 1) { q0x = i + OG_R(0.5); q0y = (og_real)j; q0z = k + OG_R(0.5); }
+            if (c == 2) { q0x = i + OG_R(0.5); q0y = j + OG_R(0.5); q0z = (og_real)k; }
             v3 a = c == 0 ? mac_at_x(d, src, idx) : (c == 1 ? mac_at_y(d, src, idx) : mac_at_z(d, src, idx));
-            const float q1x = q0x - (float)((double)(a.x * dt) * 0.5);
-            const float q1y = q0y - (float)((double)(a.y * dt) * 0.5);
-            const float q1z = q0z - (float)((double)(a.z * dt) * 0.5);
+            const og_real q1x = q0x - (og_real)((double)(a.x * dt) * 0.5);
+            const og_real q1y = q0y - (og_real)((double)(a.y * dt) * 0.5);
+            const og_real q1z = q0z - (og_real)((double)(a.z * dt) * 0.5);
             v3 vi = interp_mac(d, src, q1x, q1y, q1z);
-            const float px = p0x - vi.x * dt, py = p0y - vi.y * dt, pz = p0z - vi.z * dt;
+            const og_real px = p0x - vi.x * dt, py = p0y - vi.y * dt, pz = p0z - vi.z * dt;
             out[c] = orderSpace == 1 ? interp_ch(d, src, 3, c, px, py, pz) : interp_cubic_mac_c(d, src, c, px, py, pz);
           }
         }
@@ -334,19 +349,19 @@ static void semi_lagrange_mac(og_dims d, const float* vel, float* dst, const flo
 
 /* MacCormackCorrect (advection.cpp:81-91): dst = fwd (+ correction on fluid
  * cells), the correction formed in double as in the reference.  ch=1/3.   */
-static void maccormack_correct(og_dims d, const int* flags, float* dst, const float* old, const float* fwd,
-                               const float* bwd, float strength, int ch) {
+static void maccormack_correct(og_dims d, const int* flags, og_real* dst, const og_real* old, const og_real* fwd,
+                               const og_real* bwd, og_real strength, int ch) {
   const ll n = NCELL(d);
   ll idx;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (idx = 0; idx < n; idx++) {
     for (int c = 0; c < ch; c++) {
-      float v = fwd[ch * idx + c];
+      og_real v = fwd[ch * idx + c];
       if (isF(flags, idx)) {
         if (ch == 1)
-          v = (float)((double)v + (double)strength * 0.5 * (double)(old[idx] - bwd[idx]));
+          v = (og_real)((double)v + (double)strength * 0.5 * (double)(old[idx] - bwd[idx]));
         else /* Vec3 += : strength*0.5*(Vec3) rounds per component first */
-          v = v + (float)((double)strength * 0.5 * (double)(old[3 * idx + c] - bwd[3 * idx + c]));
+          v = v + (og_real)((double)strength * 0.5 * (double)(old[3 * idx + c] - bwd[3 * idx + c]));
       }
       dst[ch * idx + c] = v;
     }
@@ -354,8 +369,8 @@ static void maccormack_correct(og_dims d, const int* flags, float* dst, const fl
 }
 
 /* MacCormackCorrectMAC (advection.cpp:94-115) */
-static void maccormack_correct_mac(og_dims d, const int* flags, float* dst, const float* old, const float* fwd,
-                                   const float* bwd, float strength) {
+static void maccormack_correct_mac(og_dims d, const int* flags, og_real* dst, const og_real* old, const og_real* fwd,
+                                   const og_real* bwd, og_real strength) {
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (k = 0; k < d.nz; k++)
@@ -370,7 +385,7 @@ static void maccormack_correct_mac(og_dims d, const int* flags, float* dst, cons
         for (int c = 0; c < 3; c++) {
           const ll e = 3 * idx + c;
           if (skip[c]) dst[e] = fwd[e];
-          else dst[e] = (float)((double)fwd[e] + (double)strength * 0.5 * (double)(old[e] - bwd[e]));
+          else dst[e] = (og_real)((double)fwd[e] + (double)strength * 0.5 * (double)(old[e] - bwd[e]));
         }
       }
 }
@@ -379,11 +394,11 @@ static void maccormack_correct_mac(og_dims d, const int* flags, float* dst, cons
 
 /* doClampComponent (advection.cpp:144-186) for ch channels; cmpMinMax of a
  * Vec3 reverts the whole vector when any component is out of range.       */
-static void clamp_component(og_dims d, const int* flags, float* dv, const float* orig, const float* fwd,
-                            int ch, float posx, float posy, float posz, v3 vel, int clampMode) {
-  float mn[3], mx[3];
+static void clamp_component(og_dims d, const int* flags, og_real* dv, const og_real* orig, const og_real* fwd,
+                            int ch, og_real posx, og_real posy, og_real posz, v3 vel, int clampMode) {
+  og_real mn[3], mx[3];
   int haveFl = 0;
-  for (int c = 0; c < ch; c++) { mn[c] = FLT_MAX; mx[c] = -FLT_MAX; }
+  for (int c = 0; c < ch; c++) { mn[c] = OG_REAL_MAX; mx[c] = -OG_REAL_MAX; }
   int px[2], py[2], pz[2], np = 1;
   px[0] = (int)(posx - vel.x); py[0] = (int)(posy - vel.y); pz[0] = (int)(posz - vel.z);
   if (clampMode == 1) { np = 2; px[1] = (int)(posx + vel.x); py[1] = (int)(posy + vel.y); pz[1] = (int)(posz + vel.z); }
@@ -401,7 +416,7 @@ static void clamp_component(og_dims d, const int* flags, float* dv, const float*
       const ll e = IX(d, ci[q], cj[q], ck[q]);
       if (CHECKF(flags[e])) {
         for (int c = 0; c < ch; c++) {
-          const float v = orig[ch * e + c];
+          const og_real v = orig[ch * e + c];
           if (v < mn[c]) mn[c] = v;
           if (v > mx[c]) mx[c] = v;
         }
@@ -423,22 +438,22 @@ static void clamp_component(og_dims d, const int* flags, float* dv, const float*
 }
 
 /* MacCormackClamp (advection.cpp:241-267) */
-static void maccormack_clamp(og_dims d, const int* flags, const float* vel, float* dst, const float* orig,
-                             const float* fwd, float dt, int clampMode, int ch) {
+static void maccormack_clamp(og_dims d, const int* flags, const og_real* vel, og_real* dst, const og_real* orig,
+                             const og_real* fwd, og_real dt, int clampMode, int ch) {
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (k = KLO(d, 1); k < KHI(d, 1); k++)
     for (int j = 1; j < d.ny - 1; j++)
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
-        float dv[3];
+        og_real dv[3];
         for (int c = 0; c < ch; c++) dv[c] = dst[ch * idx + c];
         v3 vc = mac_centered(d, vel, idx);
         v3 vd = {vc.x * dt, vc.y * dt, vc.z * dt};
-        clamp_component(d, flags, dv, orig, fwd + ch * idx, ch, (float)i, (float)j, (float)k, vd, clampMode);
+        clamp_component(d, flags, dv, orig, fwd + ch * idx, ch, (og_real)i, (og_real)j, (og_real)k, vd, clampMode);
         if (clampMode == 1) {
-          const int fx = (int)(((float)i + 0.5f) - vd.x), fy = (int)(((float)j + 0.5f) - vd.y), fz = (int)(((float)k + 0.5f) - vd.z);
-          const int bx = (int)(((float)i + 0.5f) + vd.x), by = (int)(((float)j + 0.5f) + vd.y), bz = (int)(((float)k + 0.5f) + vd.z);
+          const int fx = (int)(((og_real)i + OG_R(0.5)) - vd.x), fy = (int)(((og_real)j + OG_R(0.5)) - vd.y), fz = (int)(((og_real)k + OG_R(0.5)) - vd.z);
+          const int bx = (int)(((og_real)i + OG_R(0.5)) + vd.x), by = (int)(((og_real)j + OG_R(0.5)) + vd.y), bz = (int)(((og_real)k + OG_R(0.5)) + vd.z);
           const int gx = d.nx - 1, gy = d.ny - 1, gz = d.nz - 1;
           int rev = fx < 0 || fy < 0 || fz < 0 || bx < 0 || by < 0 || bz < 0 ||
                     fx > gx || fy > gy || ((fz > gz) && d.is3d) ||
@@ -451,10 +466,10 @@ static void maccormack_clamp(og_dims d, const int* flags, const float* vel, floa
 }
 
 /* doClampComponentMAC (advection.cpp:191-235) */
-static float clamp_component_mac(og_dims d, const int* flags, float dst, const float* orig, float fwd, int c,
+static og_real clamp_component_mac(og_dims d, const int* flags, og_real dst, const og_real* orig, og_real fwd, int c,
                                  int i, int j, int k, v3 vel, int clampMode) {
-  float mn = FLT_MAX, mx = -FLT_MAX;
-  const float posx = (float)i, posy = (float)j, posz = (float)k;
+  og_real mn = OG_REAL_MAX, mx = -OG_REAL_MAX;
+  const og_real posx = (og_real)i, posy = (og_real)j, posz = (og_real)k;
   int px[2], py[2], pz[2], np = 1;
   px[0] = (int)(posx - vel.x); py[0] = (int)(posy - vel.y); pz[0] = (int)(posz - vel.z);
   if (clampMode == 1) { np = 2; px[1] = (int)(posx + vel.x); py[1] = (int)(posy + vel.y); pz[1] = (int)(posz + vel.z); }
@@ -472,7 +487,7 @@ static float clamp_component_mac(og_dims d, const int* flags, float dst, const f
     const int ck[8] = {k0, k0, k0, k0, k1, k1, k1, k1};
     const int ncorner = d.is3d ? 8 : 4;
     for (int q = 0; q < ncorner; q++) {
-      const float v = orig[3 * IX(d, ci[q], cj[q], ck[q]) + c];
+      const og_real v = orig[3 * IX(d, ci[q], cj[q], ck[q]) + c];
       if (v < mn) mn = v;
       if (v > mx) mx = v;
     }
@@ -487,8 +502,8 @@ static float clamp_component_mac(og_dims d, const int* flags, float dst, const f
 }
 
 /* MacCormackClampMAC (advection.cpp:270-287) */
-static void maccormack_clamp_mac(og_dims d, const int* flags, const float* vel, float* dst, const float* orig,
-                                 const float* fwd, float dt, int clampMode) {
+static void maccormack_clamp_mac(og_dims d, const int* flags, const og_real* vel, og_real* dst, const og_real* orig,
+                                 const og_real* fwd, og_real dt, int clampMode) {
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (k = KLO(d, 1); k < KHI(d, 1); k++)
@@ -511,10 +526,10 @@ static void maccormack_clamp_mac(og_dims d, const int* flags, const float* vel, 
 
 /* getBulkVel + extrapolateVelConvectiveBC + copyChangedVels
  * (advection.cpp:324-391) */
-static void apply_outflow_bc(og_dims d, const int* flags, float* vel, const float* velPrev, double timeStep) {
+static void apply_outflow_bc(og_dims d, const int* flags, og_real* vel, const og_real* velPrev, double timeStep) {
   const ll n = NCELL(d);
-  float* velDst = (float*)calloc((size_t)(3 * n), sizeof(float));
-  const float ts = (float)(timeStep * 4 > 1.0 ? timeStep * 4 : 1.0);
+  og_real* velDst = (og_real*)calloc((size_t)(3 * n), sizeof(og_real));
+  const og_real ts = (og_real)(timeStep * 4 > 1.0 ? timeStep * 4 : 1.0);
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (k = 0; k < d.nz; k++)
@@ -523,7 +538,7 @@ static void apply_outflow_bc(og_dims d, const int* flags, float* vel, const floa
         const ll idx = IX(d, i, j, k);
         if (!isOut(flags, idx)) continue;
         /* bulk velocity: mean over the 3^dim neighbourhood of fluid/outflow cells */
-        float ax = 0.f, ay = 0.f, az = 0.f;
+        og_real ax = OG_R(0.), ay = OG_R(0.), az = OG_R(0.);
         int count = 0;
         const int nmax = d.is3d ? 1 : 0;
         for (int nn = -nmax; nn <= nmax; nn++)
@@ -538,15 +553,15 @@ static void apply_outflow_bc(og_dims d, const int* flags, float* vel, const floa
                 }
               }
             }
-        float bulk[3] = {ax, ay, az};
-        if (count > 0) { bulk[0] = ax / (float)count; bulk[1] = ay / (float)count; bulk[2] = az / (float)count; }
+        og_real bulk[3] = {ax, ay, az};
+        if (count > 0) { bulk[0] = ax / (og_real)count; bulk[1] = ay / (og_real)count; bulk[2] = az / (og_real)count; }
         const int dim = d.is3d ? 3 : 2;
         int cnt = 0;
-        float dx = 0.f, dy = 0.f, dz = 0.f;
+        og_real dx = OG_R(0.), dy = OG_R(0.), dz = OG_R(0.);
         const int cur[3] = {i, j, k};
         for (int c = 0; c < dim; c++) {
           int lo[3] = {i, j, k}, up[3] = {i, j, k}, fl[3] = {i, j, k}, fu[3] = {i, j, k};
-          const float factor = ts * (bulk[c] > 1.0f ? bulk[c] : 1.0f);
+          const og_real factor = ts * (bulk[c] > OG_R(1.0) ? bulk[c] : OG_R(1.0));
           lo[c] = fl[c] = cur[c] - 1;
           up[c] = fu[c] = cur[c] + 1;
           for (int dd = 0; dd < 2; dd++) {
@@ -575,7 +590,7 @@ static void apply_outflow_bc(og_dims d, const int* flags, float* vel, const floa
             fu[c]++;
           }
         }
-        if (cnt > 0) { dx /= (float)cnt; dy /= (float)cnt; dz /= (float)cnt; }
+        if (cnt > 0) { dx /= (og_real)cnt; dy /= (og_real)cnt; dz /= (og_real)cnt; }
         velDst[3 * idx] = dx; velDst[3 * idx + 1] = dy; velDst[3 * idx + 2] = dz;
       }
   ll idx;
@@ -590,24 +605,24 @@ static void apply_outflow_bc(og_dims d, const int* flags, float* vel, const floa
 
 /* fnAdvectSemiLagrange and its MAC specialisation (advection.cpp:292-321,
  * 406-436); advectSemiLagrange dispatch (:442-460).                        */
-int og_advect_semi_lagrange(og_dims d, const int* flags, const float* vel, int kind, float* grid, int order,
-                            float strength, int orderSpace, int clampMode, int orderTrace, float dt) {
+int og_advect_semi_lagrange(og_dims d, const int* flags, const og_real* vel, int kind, og_real* grid, int order,
+                            og_real strength, int orderSpace, int clampMode, int orderTrace, og_real dt) {
   if (order != 1 && order != 2) return -1;
   if (orderTrace != 1 && orderTrace != 2) return -2;
   const ll n = NCELL(d);
   const int ch = kind == OG_KIND_REAL ? 1 : 3;
-  float* fwd = (float*)calloc((size_t)(ch * n), sizeof(float));
+  og_real* fwd = (og_real*)calloc((size_t)(ch * n), sizeof(og_real));
   if (kind != OG_KIND_MAC) {
     semi_lagrange(d, vel, fwd, grid, ch, dt, orderSpace, orderTrace);
     if (order == 1) {
-      memcpy(grid, fwd, sizeof(float) * ch * n);
+      memcpy(grid, fwd, sizeof(og_real) * ch * n);
     } else {
-      float* bwd = (float*)calloc((size_t)(ch * n), sizeof(float));
-      float* nw = (float*)calloc((size_t)(ch * n), sizeof(float));
+      og_real* bwd = (og_real*)calloc((size_t)(ch * n), sizeof(og_real));
+      og_real* nw = (og_real*)calloc((size_t)(ch * n), sizeof(og_real));
       semi_lagrange(d, vel, bwd, fwd, ch, -dt, orderSpace, orderTrace);
       maccormack_correct(d, flags, nw, grid, fwd, bwd, strength, ch);
       maccormack_clamp(d, flags, vel, nw, grid, fwd, dt, clampMode, ch);
-      memcpy(grid, nw, sizeof(float) * ch * n);
+      memcpy(grid, nw, sizeof(og_real) * ch * n);
       free(bwd);
       free(nw);
     }
@@ -615,15 +630,15 @@ int og_advect_semi_lagrange(og_dims d, const int* flags, const float* vel, int k
     semi_lagrange_mac(d, vel, fwd, grid, dt, orderSpace, orderTrace);
     if (order == 1) {
       apply_outflow_bc(d, flags, fwd, grid, (double)dt);
-      memcpy(grid, fwd, sizeof(float) * 3 * n);
+      memcpy(grid, fwd, sizeof(og_real) * 3 * n);
     } else {
-      float* bwd = (float*)calloc((size_t)(3 * n), sizeof(float));
-      float* nw = (float*)calloc((size_t)(3 * n), sizeof(float));
+      og_real* bwd = (og_real*)calloc((size_t)(3 * n), sizeof(og_real));
+      og_real* nw = (og_real*)calloc((size_t)(3 * n), sizeof(og_real));
       semi_lagrange_mac(d, vel, bwd, fwd, -dt, orderSpace, orderTrace);
       maccormack_correct_mac(d, flags, nw, grid, fwd, bwd, strength);
       maccormack_clamp_mac(d, flags, vel, nw, grid, fwd, dt, clampMode);
       apply_outflow_bc(d, flags, nw, grid, (double)dt);
-      memcpy(grid, nw, sizeof(float) * 3 * n);
+      memcpy(grid, nw, sizeof(og_real) * 3 * n);
       free(bwd);
       free(nw);
     }
@@ -636,7 +651,7 @@ int og_advect_semi_lagrange(og_dims d, const int* flags, const float* vel, int k
 /* Forces and wall boundary conditions, plugin/extforces.cpp                */
 
 /* KnSetWallBcs (:186-217), all cells, i>0 checks */
-void og_set_wall_bcs(og_dims d, const int* flags, float* vel, const float* obvel) {
+void og_set_wall_bcs(og_dims d, const int* flags, og_real* vel, const og_real* obvel) {
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (k = 0; k < d.nz; k++)
@@ -645,39 +660,39 @@ void og_set_wall_bcs(og_dims d, const int* flags, float* vel, const float* obvel
         const ll idx = IX(d, i, j, k);
         const int curFluid = isF(flags, idx), curObs = isO(flags, idx);
         if (!curFluid && !curObs) continue;
-        float bx = 0.f, by = 0.f, bz = 0.f;
+        og_real bx = OG_R(0.), by = OG_R(0.), bz = OG_R(0.);
         if (obvel) {
           bx = obvel[3 * idx]; by = obvel[3 * idx + 1];
           if (d.is3d) bz = obvel[3 * idx + 2];
         }
-        float* v = vel + 3 * idx;
+        og_real* v = vel + 3 * idx;
         if (i > 0 && isO(flags, idx - 1)) v[0] = bx;
         if (i > 0 && curObs && isF(flags, idx - 1)) v[0] = bx;
         if (j > 0 && isO(flags, idx - SY(d))) v[1] = by;
         if (j > 0 && curObs && isF(flags, idx - SY(d))) v[1] = by;
         if (!d.is3d) {
-          v[2] = 0.f;
+          v[2] = OG_R(0.);
         } else {
           if (k > 0 && isO(flags, idx - SZ(d))) v[2] = bz;
           if (k > 0 && curObs && isF(flags, idx - SZ(d))) v[2] = bz;
         }
         if (curFluid) {
-          if ((i > 0 && isStk(flags, idx - 1)) || (i < d.nx - 1 && isStk(flags, idx + 1))) v[1] = v[2] = 0.f;
-          if ((j > 0 && isStk(flags, idx - SY(d))) || (j < d.ny - 1 && isStk(flags, idx + SY(d)))) v[0] = v[2] = 0.f;
-          if (d.is3d && ((k > 0 && isStk(flags, idx - SZ(d))) || (k < d.nz - 1 && isStk(flags, idx + SZ(d))))) v[0] = v[1] = 0.f;
+          if ((i > 0 && isStk(flags, idx - 1)) || (i < d.nx - 1 && isStk(flags, idx + 1))) v[1] = v[2] = OG_R(0.);
+          if ((j > 0 && isStk(flags, idx - SY(d))) || (j < d.ny - 1 && isStk(flags, idx + SY(d)))) v[0] = v[2] = OG_R(0.);
+          if (d.is3d && ((k > 0 && isStk(flags, idx - SZ(d))) || (k < d.nz - 1 && isStk(flags, idx + SZ(d))))) v[0] = v[1] = OG_R(0.);
         }
       }
 }
 
 /* addBuoyancy (:83-87) -> KnAddBuoyancy (:72-80).  The increment
  * (0.5*s)*(rho+rho') is formed in double and added in double. */
-void og_add_buoyancy(og_dims d, const int* flags, const float* density, float* vel, float gx, float gy, float gz,
-                     float coefficient, int scale, float dt) {
-  const float dx = (float)(1.0 / (double)imax(d.nx, imax(d.ny, d.nz)));
-  const float gridScale = scale ? dx : 1.f;
-  const float fx = ((-gx) * dt) / gridScale * coefficient;
-  const float fy = ((-gy) * dt) / gridScale * coefficient;
-  const float fz = ((-gz) * dt) / gridScale * coefficient;
+void og_add_buoyancy(og_dims d, const int* flags, const og_real* density, og_real* vel, og_real gx, og_real gy, og_real gz,
+                     og_real coefficient, int scale, og_real dt) {
+  const og_real dx = (og_real)(1.0 / (double)imax(d.nx, imax(d.ny, d.nz)));
+  const og_real gridScale = scale ? dx : OG_R(1.);
+  const og_real fx = ((-gx) * dt) / gridScale * coefficient;
+  const og_real fy = ((-gy) * dt) / gridScale * coefficient;
+  const og_real fz = ((-gz) * dt) / gridScale * coefficient;
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (k = KLO(d, 1); k < KHI(d, 1); k++)
@@ -685,22 +700,22 @@ void og_add_buoyancy(og_dims d, const int* flags, const float* density, float* v
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
         if (!isF(flags, idx)) continue;
-        float* v = vel + 3 * idx;
+        og_real* v = vel + 3 * idx;
         if (isF(flags, idx - 1))
-          v[0] = (float)((double)v[0] + (0.5 * fx) * (double)(density[idx] + density[idx - 1]));
+          v[0] = (og_real)((double)v[0] + (0.5 * fx) * (double)(density[idx] + density[idx - 1]));
         if (isF(flags, idx - SY(d)))
-          v[1] = (float)((double)v[1] + (0.5 * fy) * (double)(density[idx] + density[idx - SY(d)]));
+          v[1] = (og_real)((double)v[1] + (0.5 * fy) * (double)(density[idx] + density[idx - SY(d)]));
         if (d.is3d && isF(flags, idx - SZ(d)))
-          v[2] = (float)((double)v[2] + (0.5 * fz) * (double)(density[idx] + density[idx - SZ(d)]));
+          v[2] = (og_real)((double)v[2] + (0.5 * fz) * (double)(density[idx] + density[idx - SZ(d)]));
       }
 }
 
 /* addGravity (:61-65) -> KnApplyForce (:46-58), additive */
-void og_add_gravity(og_dims d, const int* flags, float* vel, float gx, float gy, float gz, const float* exclude,
-                    int scale, float dt) {
-  const float dx = (float)(1.0 / (double)imax(d.nx, imax(d.ny, d.nz)));
-  const float gridScale = scale ? dx : 1.f;
-  const float fx = (gx * dt) / gridScale, fy = (gy * dt) / gridScale, fz = (gz * dt) / gridScale;
+void og_add_gravity(og_dims d, const int* flags, og_real* vel, og_real gx, og_real gy, og_real gz, const og_real* exclude,
+                    int scale, og_real dt) {
+  const og_real dx = (og_real)(1.0 / (double)imax(d.nx, imax(d.ny, d.nz)));
+  const og_real gridScale = scale ? dx : OG_R(1.);
+  const og_real fx = (gx * dt) / gridScale, fy = (gy * dt) / gridScale, fz = (gz * dt) / gridScale;
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (k = KLO(d, 1); k < KHI(d, 1); k++)
@@ -710,7 +725,7 @@ void og_add_gravity(og_dims d, const int* flags, float* vel, float gx, float gy,
         const int curFluid = isF(flags, idx), curEmpty = isE(flags, idx);
         if (!curFluid && !curEmpty) continue;
         if (exclude && (exclude[idx] < 0.)) continue;
-        float* v = vel + 3 * idx;
+        og_real* v = vel + 3 * idx;
         if (isF(flags, idx - 1) || (curFluid && isE(flags, idx - 1))) v[0] = v[0] + fx;
         if (isF(flags, idx - SY(d)) || (curFluid && isE(flags, idx - SY(d)))) v[1] = v[1] + fy;
         if (d.is3d && (isF(flags, idx - SZ(d)) || (curFluid && isE(flags, idx - SZ(d))))) v[2] = v[2] + fz;
@@ -720,7 +735,7 @@ void og_add_gravity(og_dims d, const int* flags, float* vel, float gx, float gy,
 /* extrapolateMACSimple (fastmarch.cpp:337-375) with knExtrapolateMACSimple
  * (:230-258, in place: a cell reads neighbours of layer d only, so the
  * in-place update is order independent) and knExtrapolateIntoBnd (:260-300) */
-void og_extrapolate_mac_simple(og_dims d, const int* flags, float* vel, int distance, int intoObs) {
+void og_extrapolate_mac_simple(og_dims d, const int* flags, og_real* vel, int distance, int intoObs) {
   const ll n = NCELL(d);
   int* tmp = (int*)malloc(sizeof(int) * (size_t)n);
   const int dim = d.is3d ? 3 : 2;
@@ -747,38 +762,38 @@ void og_extrapolate_mac_simple(og_dims d, const int* flags, float* vel, int dist
             if (tmp[idx] != 0) continue;
             const ll nbo[6] = {1, -1, SY(d), -SY(d), SZ(d), -SZ(d)};
             int nbs = 0;
-            float avg = 0.f;
+            og_real avg = OG_R(0.);
             for (int q = 0; q < 2 * dim; q++)
               if (tmp[idx + nbo[q]] == dd) { avg += vel[3 * (idx + nbo[q]) + c]; nbs++; }
             if (nbs > 0) {
               tmp[idx] = dd + 1;
-              vel[3 * idx + c] = avg / (float)nbs;
+              vel[3 * idx + c] = avg / (og_real)nbs;
             }
           }
     }
   }
   /* copy tangential values into the domain sides from a snapshot */
-  float* vt = (float*)malloc(sizeof(float) * 3 * (size_t)n);
-  memcpy(vt, vel, sizeof(float) * 3 * (size_t)n);
+  og_real* vt = (og_real*)malloc(sizeof(og_real) * 3 * (size_t)n);
+  memcpy(vt, vel, sizeof(og_real) * 3 * (size_t)n);
   for (int k = 0; k < d.nz; k++)
     for (int j = 0; j < d.ny; j++)
       for (int i = 0; i < d.nx; i++) {
         const ll idx = IX(d, i, j, k);
         int cc = 0;
-        float v[3] = {0.f, 0.f, 0.f};
+        og_real v[3] = {OG_R(0.), OG_R(0.), OG_R(0.)};
         const int obs = isO(flags, idx);
 #define TAKE(e) do { v[0] = vt[3 * (e)]; v[1] = vt[3 * (e) + 1]; v[2] = vt[3 * (e) + 2]; } while (0)
-        if (i == 0) { TAKE(idx + 1); if (obs && v[0] < 0.f) v[0] = 0.f; cc++; }
-        else if (i == d.nx - 1) { TAKE(idx - 1); if (obs && v[0] > 0.f) v[0] = 0.f; cc++; }
-        if (j == 0) { TAKE(idx + SY(d)); if (obs && v[1] < 0.f) v[1] = 0.f; cc++; }
-        else if (j == d.ny - 1) { TAKE(idx - SY(d)); if (obs && v[1] > 0.f) v[1] = 0.f; cc++; }
+        if (i == 0) { TAKE(idx + 1); if (obs && v[0] < OG_R(0.)) v[0] = OG_R(0.); cc++; }
+        else if (i == d.nx - 1) { TAKE(idx - 1); if (obs && v[0] > OG_R(0.)) v[0] = OG_R(0.); cc++; }
+        if (j == 0) { TAKE(idx + SY(d)); if (obs && v[1] < OG_R(0.)) v[1] = OG_R(0.); cc++; }
+        else if (j == d.ny - 1) { TAKE(idx - SY(d)); if (obs && v[1] > OG_R(0.)) v[1] = OG_R(0.); cc++; }
         if (d.is3d) {
-          if (k == 0) { TAKE(idx + SZ(d)); if (obs && v[2] < 0.f) v[2] = 0.f; cc++; }
-          else if (k == d.nz - 1) { TAKE(idx - SZ(d)); if (obs && v[2] > 0.f) v[2] = 0.f; cc++; }
+          if (k == 0) { TAKE(idx + SZ(d)); if (obs && v[2] < OG_R(0.)) v[2] = OG_R(0.); cc++; }
+          else if (k == d.nz - 1) { TAKE(idx - SZ(d)); if (obs && v[2] > OG_R(0.)) v[2] = OG_R(0.); cc++; }
         }
 #undef TAKE
         if (cc > 0) {
-          vel[3 * idx] = v[0] / (float)cc; vel[3 * idx + 1] = v[1] / (float)cc; vel[3 * idx + 2] = v[2] / (float)cc;
+          vel[3 * idx] = v[0] / (og_real)cc; vel[3 * idx + 1] = v[1] / (og_real)cc; vel[3 * idx + 2] = v[2] / (og_real)cc;
         }
       }
   free(vt);
@@ -789,26 +804,26 @@ void og_extrapolate_mac_simple(og_dims d, const int* flags, float* vel, int dist
 /* Pressure projection, plugin/pressure.cpp + conjugategrad.*               */
 
 /* thetaHelper / ghostFluidHelper (pressure.cpp:115-128) */
-static inline float theta_helper(float inside, float outside) {
-  const float denom = inside - outside;
-  if (denom > -1e-04) return 0.5f;
-  float r = inside / denom;
-  if (r > 1.f) r = 1.f;
-  if (r < 0.f) r = 0.f;
+static inline og_real theta_helper(og_real inside, og_real outside) {
+  const og_real denom = inside - outside;
+  if (denom > -1e-04) return OG_R(0.5);
+  og_real r = inside / denom;
+  if (r > OG_R(1.)) r = OG_R(1.);
+  if (r < OG_R(0.)) r = OG_R(0.);
   return r;
 }
-static inline float gf_helper(const float* phi, ll idx, ll off, float gfClamp) {
-  float alpha = theta_helper(phi[idx], phi[idx + off]);
+static inline og_real gf_helper(const og_real* phi, ll idx, ll off, og_real gfClamp) {
+  og_real alpha = theta_helper(phi[idx], phi[idx + off]);
   if (alpha < gfClamp) return gfClamp;
-  return (float)(1. - (1. / (double)alpha));
+  return (og_real)(1. - (1. / (double)alpha));
 }
-static inline float surf_tens_helper(const float* phi, const float* curv, ll idx, ll off, float surfTens, float gfClamp) {
+static inline og_real surf_tens_helper(const og_real* phi, const og_real* curv, ll idx, ll off, og_real surfTens, og_real gfClamp) {
   return surfTens * (curv[idx + off] - gf_helper(phi, idx, off, gfClamp) * curv[idx]);
 }
 
 /* MakeRhs (pressure.cpp:32-84) without fractions/obvel; returns sum, cnt */
-static void make_rhs(og_dims d, const int* flags, float* rhs, const float* vel, const float* perCellCorr,
-                     const float* phi, const float* curv, float surfTens, float gfClamp, double* sumOut, int* cntOut) {
+static void make_rhs(og_dims d, const int* flags, og_real* rhs, const og_real* vel, const og_real* perCellCorr,
+                     const og_real* phi, const og_real* curv, og_real surfTens, og_real gfClamp, double* sumOut, int* cntOut) {
   double sum = 0;
   int cnt = 0;
   const ll X = 1, Y = SY(d), Z = SZ(d);
@@ -816,8 +831,8 @@ static void make_rhs(og_dims d, const int* flags, float* rhs, const float* vel, 
     for (int j = 1; j < d.ny - 1; j++)
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
-        if (!isF(flags, idx)) { rhs[idx] = 0.f; continue; }
-        float set = vel[3 * idx] - vel[3 * (idx + X)] + vel[3 * idx + 1] - vel[3 * (idx + Y) + 1];
+        if (!isF(flags, idx)) { rhs[idx] = OG_R(0.); continue; }
+        og_real set = vel[3 * idx] - vel[3 * (idx + X)] + vel[3 * idx + 1] - vel[3 * (idx + Y) + 1];
         if (d.is3d) set += vel[3 * idx + 2] - vel[3 * (idx + Z) + 2];
         if (phi && curv) {
           if (isE(flags, idx - X)) set += surf_tens_helper(phi, curv, idx, -X, surfTens, gfClamp);
@@ -838,23 +853,23 @@ static void make_rhs(og_dims d, const int* flags, float* rhs, const float* vel, 
   *cntOut = cnt;
 }
 
-void og_compute_pressure_rhs(og_dims d, float* rhs, const float* vel, const int* flags, const float* phi,
-                             const float* perCellCorr, const float* curv, const og_pressure_params* p) {
+void og_compute_pressure_rhs(og_dims d, og_real* rhs, const og_real* vel, const int* flags, const og_real* phi,
+                             const og_real* perCellCorr, const og_real* curv, const og_pressure_params* p) {
   double sum;
   int cnt;
   make_rhs(d, flags, rhs, vel, perCellCorr, phi, curv, p->surfTens, p->gfClamp, &sum, &cnt);
   if (p->enforceCompatibility) {
-    const float add = (float)(-sum / (double)(float)cnt);
+    const og_real add = (og_real)(-sum / (double)(og_real)cnt);
     const ll n = NCELL(d);
     for (ll idx = 0; idx < n; idx++) rhs[idx] += add;
   }
 }
 
 /* MakeLaplaceMatrix (conjugategrad.h:154-187), no fractions; A* zeroed */
-void og_make_laplace_matrix(og_dims d, const int* flags, float* A0, float* Ai, float* Aj, float* Ak) {
+void og_make_laplace_matrix(og_dims d, const int* flags, og_real* A0, og_real* Ai, og_real* Aj, og_real* Ak) {
   const ll n = NCELL(d);
-  memset(A0, 0, sizeof(float) * n); memset(Ai, 0, sizeof(float) * n);
-  memset(Aj, 0, sizeof(float) * n); memset(Ak, 0, sizeof(float) * n);
+  memset(A0, 0, sizeof(og_real) * n); memset(Ai, 0, sizeof(og_real) * n);
+  memset(Aj, 0, sizeof(og_real) * n); memset(Ak, 0, sizeof(og_real) * n);
   const ll X = 1, Y = SY(d), Z = SZ(d);
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
@@ -863,20 +878,20 @@ void og_make_laplace_matrix(og_dims d, const int* flags, float* A0, float* Ai, f
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
         if (!isF(flags, idx)) continue;
-        if (!isO(flags, idx - X)) A0[idx] += 1.f;
-        if (!isO(flags, idx + X)) A0[idx] += 1.f;
-        if (!isO(flags, idx - Y)) A0[idx] += 1.f;
-        if (!isO(flags, idx + Y)) A0[idx] += 1.f;
-        if (d.is3d && !isO(flags, idx - Z)) A0[idx] += 1.f;
-        if (d.is3d && !isO(flags, idx + Z)) A0[idx] += 1.f;
-        if (isF(flags, idx + X)) Ai[idx] = -1.f;
-        if (isF(flags, idx + Y)) Aj[idx] = -1.f;
-        if (d.is3d && isF(flags, idx + Z)) Ak[idx] = -1.f;
+        if (!isO(flags, idx - X)) A0[idx] += OG_R(1.);
+        if (!isO(flags, idx + X)) A0[idx] += OG_R(1.);
+        if (!isO(flags, idx - Y)) A0[idx] += OG_R(1.);
+        if (!isO(flags, idx + Y)) A0[idx] += OG_R(1.);
+        if (d.is3d && !isO(flags, idx - Z)) A0[idx] += OG_R(1.);
+        if (d.is3d && !isO(flags, idx + Z)) A0[idx] += OG_R(1.);
+        if (isF(flags, idx + X)) Ai[idx] = -OG_R(1.);
+        if (isF(flags, idx + Y)) Aj[idx] = -OG_R(1.);
+        if (d.is3d && isF(flags, idx + Z)) Ak[idx] = -OG_R(1.);
       }
 }
 
 /* ApplyGhostFluidDiagonal (pressure.cpp:136-151) */
-void og_apply_ghost_fluid_diagonal(og_dims d, float* A0, const int* flags, const float* phi, float gfClamp) {
+void og_apply_ghost_fluid_diagonal(og_dims d, og_real* A0, const int* flags, const og_real* phi, og_real gfClamp) {
   const ll X = 1, Y = SY(d), Z = SZ(d);
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
@@ -898,49 +913,49 @@ void og_apply_ghost_fluid_diagonal(og_dims d, float* A0, const int* flags, const
 
 /* InitPreconditionModifiedIncompCholesky2 (conjugategrad.cpp:66-97).  The
  * recurrence is lexicographic and serial in the reference. */
-void og_mic_init(og_dims d, const int* flags, float* P, const float* A0, const float* Ai, const float* Aj,
-                 const float* Ak) {
+void og_mic_init(og_dims d, const int* flags, og_real* P, const og_real* A0, const og_real* Ai, const og_real* Aj,
+                 const og_real* Ak) {
   const ll n = NCELL(d);
-  memset(P, 0, sizeof(float) * n);
+  memset(P, 0, sizeof(og_real) * n);
   const ll X = 1, Y = SY(d), Z = SZ(d);
   for (int k = 0; k < d.nz; k++)
     for (int j = 0; j < d.ny; j++)
       for (int i = 0; i < d.nx; i++) {
         const ll idx = IX(d, i, j, k);
         if (!isF(flags, idx)) continue;
-        const float tau = 0.97f, sigma = 0.25f;
+        const og_real tau = OG_R(0.97), sigma = OG_R(0.25);
         /* neighbours outside the grid contribute nothing (the reference
          * reads out of range there; fluid never touches the border) */
-        const float ai = i > 0 ? Ai[idx - X] : 0.f, pi = i > 0 ? P[idx - X] : 0.f;
-        const float aj = j > 0 ? Aj[idx - Y] : 0.f, pj = j > 0 ? P[idx - Y] : 0.f;
-        const float ak = k > 0 ? Ak[idx - Z] : 0.f, pk = k > 0 ? P[idx - Z] : 0.f;
-        const float aji = i > 0 ? Aj[idx - X] : 0.f, aki = i > 0 ? Ak[idx - X] : 0.f;
-        const float aij = j > 0 ? Ai[idx - Y] : 0.f, akj = j > 0 ? Ak[idx - Y] : 0.f;
-        const float aik = k > 0 ? Ai[idx - Z] : 0.f, ajk = k > 0 ? Aj[idx - Z] : 0.f;
-        float e = 0.f;
-        const float q1 = ai * pi, q2 = aj * pj, q3 = ak * pk;
+        const og_real ai = i > 0 ? Ai[idx - X] : OG_R(0.), pi = i > 0 ? P[idx - X] : OG_R(0.);
+        const og_real aj = j > 0 ? Aj[idx - Y] : OG_R(0.), pj = j > 0 ? P[idx - Y] : OG_R(0.);
+        const og_real ak = k > 0 ? Ak[idx - Z] : OG_R(0.), pk = k > 0 ? P[idx - Z] : OG_R(0.);
+        const og_real aji = i > 0 ? Aj[idx - X] : OG_R(0.), aki = i > 0 ? Ak[idx - X] : OG_R(0.);
+        const og_real aij = j > 0 ? Ai[idx - Y] : OG_R(0.), akj = j > 0 ? Ak[idx - Y] : OG_R(0.);
+        const og_real aik = k > 0 ? Ai[idx - Z] : OG_R(0.), ajk = k > 0 ? Aj[idx - Z] : OG_R(0.);
+        og_real e = OG_R(0.);
+        const og_real q1 = ai * pi, q2 = aj * pj, q3 = ak * pk;
         e = A0[idx] - q1 * q1 - q2 * q2 - q3 * q3;
-        const float t1 = ai * (aji + aki) * (pi * pi);
-        const float t2 = aj * (aij + akj) * (pj * pj);
-        const float t3 = ak * (aik + ajk) * (pk * pk);
+        const og_real t1 = ai * (aji + aki) * (pi * pi);
+        const og_real t2 = aj * (aij + akj) * (pj * pj);
+        const og_real t3 = ak * (aik + ajk) * (pk * pk);
         const double s = (double)(t1 + t2 + t3) + 0.;
-        e = (float)((double)e - (double)tau * s);
+        e = (og_real)((double)e - (double)tau * s);
         if (e < sigma * A0[idx]) e = A0[idx];
-        P[idx] = (float)(1. / (double)sqrtf(e));
+        P[idx] = (og_real)(1. / (double)og_sqrt(e));
       }
 }
 
 /* ApplyPreconditionModifiedIncompCholesky2 (conjugategrad.cpp:135-160) */
-void og_mic_apply(og_dims d, float* dst, const float* src, const int* flags, const float* P, const float* Ai,
-                  const float* Aj, const float* Ak) {
+void og_mic_apply(og_dims d, og_real* dst, const og_real* src, const int* flags, const og_real* P, const og_real* Ai,
+                  const og_real* Aj, const og_real* Ak) {
   const ll X = 1, Y = SY(d), Z = SZ(d);
   for (int k = 0; k < d.nz; k++)
     for (int j = 0; j < d.ny; j++)
       for (int i = 0; i < d.nx; i++) {
         const ll idx = IX(d, i, j, k);
         if (!isF(flags, idx)) continue;
-        const float p = P[idx];
-        float t = src[idx];
+        const og_real p = P[idx];
+        og_real t = src[idx];
         if (i > 0) t = t - dst[idx - X] * Ai[idx - X] * P[idx - X];
         if (j > 0) t = t - dst[idx - Y] * Aj[idx - Y] * P[idx - Y];
         if (k > 0) t = t - dst[idx - Z] * Ak[idx - Z] * P[idx - Z];
@@ -951,8 +966,8 @@ void og_mic_apply(og_dims d, float* dst, const float* src, const int* flags, con
       for (int i = d.nx - 1; i >= 0; i--) {
         const ll idx = IX(d, i, j, k);
         if (!isF(flags, idx)) continue;
-        const float p = P[idx];
-        float t = dst[idx];
+        const og_real p = P[idx];
+        og_real t = dst[idx];
         if (i < d.nx - 1) t = t - dst[idx + X] * Ai[idx] * p;
         if (j < d.ny - 1) t = t - dst[idx + Y] * Aj[idx] * p;
         if (k < d.nz - 1) t = t - dst[idx + Z] * Ak[idx] * p;
@@ -961,24 +976,24 @@ void og_mic_apply(og_dims d, float* dst, const float* src, const int* flags, con
 }
 
 /* ApplyMatrix / ApplyMatrix2D (conjugategrad.h:118-151) */
-void og_apply_matrix(og_dims d, const int* flags, float* dst, const float* src, const float* A0, const float* Ai,
-                     const float* Aj, const float* Ak) {
+void og_apply_matrix(og_dims d, const int* flags, og_real* dst, const og_real* src, const og_real* A0, const og_real* Ai,
+                     const og_real* Aj, const og_real* Ak) {
   const ll n = NCELL(d);
   const ll X = 1, Y = SY(d), Z = SZ(d);
   ll idx;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (idx = 0; idx < n; idx++) {
     if (!isF(flags, idx)) { dst[idx] = src[idx]; continue; }
-    float v = src[idx] * A0[idx] + src[idx - X] * Ai[idx - X] + src[idx + X] * Ai[idx] + src[idx - Y] * Aj[idx - Y] +
+    og_real v = src[idx] * A0[idx] + src[idx - X] * Ai[idx - X] + src[idx + X] * Ai[idx] + src[idx - Y] * Aj[idx - Y] +
               src[idx + Y] * Aj[idx];
     if (d.is3d) v = v + src[idx - Z] * Ak[idx - Z] + src[idx + Z] * Ak[idx];
     dst[idx] = v;
   }
 }
 
-/* GridDotProduct (conjugategrad.cpp:175-178): float products, double sum.
+/* GridDotProduct (conjugategrad.cpp:175-178): Real products, double sum.
  * Partials per thread are combined in thread order. */
-static double dot_product(ll n, const float* a, const float* b) {
+static double dot_product(ll n, const og_real* a, const og_real* b) {
   double total = 0.;
   if (g_threads <= 1) {
     for (ll i = 0; i < n; i++) total += (a[i] * b[i]);
@@ -1006,20 +1021,20 @@ static double dot_product(ll n, const float* a, const float* b) {
   return total;
 }
 
-static double sum_sqr(ll n, const float* a) {
+static double sum_sqr(ll n, const og_real* a) {
   double s = 0.;
   for (ll i = 0; i < n; i++) s += (double)a[i] * (double)a[i];
   return s;
 }
 
 /* Grid<Real>::getMaxAbs (grid.cpp:319-323) */
-float og_get_max_abs(ll n, const float* a) {
-  float amin = FLT_MAX, amax = -FLT_MAX;
+og_real og_get_max_abs(ll n, const og_real* a) {
+  og_real amin = OG_REAL_MAX, amax = -OG_REAL_MAX;
   for (ll i = 0; i < n; i++) {
     if (a[i] < amin) amin = a[i];
     if (a[i] > amax) amax = a[i];
   }
-  const float x = fabsf(amin), y = fabsf(amax);
+  const og_real x = og_fabs(amin), y = og_fabs(amax);
   return x > y ? x : y;
 }
 
@@ -1029,7 +1044,7 @@ float og_get_max_abs(ll n, const float* a) {
 
 enum { VT_INACTIVE = 0, VT_ACTIVE = 1, VT_ACTIVE_TRIVIAL = 2, VT_REMOVED = 3, VT_ZERO = 4, VT_FREE = 5 };
 
-typedef struct { int U[3], W[3], N[3]; int sc, sf; float rw, iw; int inU; } og_path;
+typedef struct { int U[3], W[3], N[3]; int sc, sf; og_real rw, iw; int inU; } og_path;
 
 #define MG_MAXL 32
 struct og_mg {
@@ -1039,16 +1054,16 @@ struct og_mg {
   int size[MG_MAXL][3];
   int pitch[MG_MAXL][3];
   ll n[MG_MAXL];
-  float* A[MG_MAXL];
-  float* x[MG_MAXL];
-  float* b[MG_MAXL];
-  float* r[MG_MAXL];
+  og_real* A[MG_MAXL];
+  og_real* x[MG_MAXL];
+  og_real* b[MG_MAXL];
+  og_real* r[MG_MAXL];
   signed char* type[MG_MAXL];
   double *cg1, *cg2, *cg3, *cg4;
   og_path* paths;
   int npaths;
   int isASet;
-  float coarseAcc, trivialScale;
+  og_real coarseAcc, trivialScale;
 };
 
 static inline ll mg_lin(const og_mg* m, int l, const int* V) {
@@ -1074,8 +1089,8 @@ og_mg* og_mg_create(og_dims d) {
   m->S0 = m->is3d ? 4 : 3;
   m->smin[0] = -1; m->smin[1] = -1; m->smin[2] = m->is3d ? -1 : 0;
   m->smax[0] = 1; m->smax[1] = 1; m->smax[2] = m->is3d ? 1 : 0;
-  m->coarseAcc = 1e-8f;
-  m->trivialScale = 1e-6f;
+  m->coarseAcc = OG_R(1e-8);
+  m->trivialScale = OG_R(1e-6);
   m->size[0][0] = d.nx; m->size[0][1] = d.ny; m->size[0][2] = d.nz;
   int L = 1;
   ll n = (ll)d.nx * d.ny * d.nz;
@@ -1092,10 +1107,10 @@ og_mg* og_mg_create(og_dims d) {
     m->pitch[l][1] = m->size[l][0];
     m->pitch[l][2] = m->size[l][0] * m->size[l][1];
     m->n[l] = (ll)m->size[l][0] * m->size[l][1] * m->size[l][2];
-    m->A[l] = (float*)calloc((size_t)(m->n[l] * (l == 0 ? m->S0 : m->S)), sizeof(float));
-    m->x[l] = (float*)calloc((size_t)m->n[l], sizeof(float));
-    m->b[l] = (float*)calloc((size_t)m->n[l], sizeof(float));
-    m->r[l] = (float*)calloc((size_t)m->n[l], sizeof(float));
+    m->A[l] = (og_real*)calloc((size_t)(m->n[l] * (l == 0 ? m->S0 : m->S)), sizeof(og_real));
+    m->x[l] = (og_real*)calloc((size_t)m->n[l], sizeof(og_real));
+    m->b[l] = (og_real*)calloc((size_t)m->n[l], sizeof(og_real));
+    m->r[l] = (og_real*)calloc((size_t)m->n[l], sizeof(og_real));
     m->type[l] = (signed char*)calloc((size_t)m->n[l], 1);
   }
   const ll nc = m->n[L - 1];
@@ -1129,8 +1144,8 @@ og_mg* og_mg_create(og_dims d) {
                   p->sc = s - 13;
                   p->sf = (i + 1) / 2;
                   p->inU = (i % 2 == 0);
-                  p->rw = 1.f / (float)(1 << ((U[0] % 2) + (U[1] % 2) + (U[2] % 2)));
-                  p->iw = 1.f / (float)(1 << ((W[0] % 2) + (W[1] % 2) + (W[2] % 2)));
+                  p->rw = OG_R(1.) / (og_real)(1 << ((U[0] % 2) + (U[1] % 2) + (U[2] % 2)));
+                  p->iw = OG_R(1.) / (og_real)(1 << ((W[0] % 2) + (W[1] % 2) + (W[2] % 2)));
                 }
               }
         }
@@ -1157,7 +1172,7 @@ void og_mg_destroy(og_mg* m) {
 int og_mg_num_levels(const og_mg* m) { return m->nlev; }
 void og_mg_level_size(const og_mg* m, int l, int* sz) { sz[0] = m->size[l][0]; sz[1] = m->size[l][1]; sz[2] = m->size[l][2]; }
 const signed char* og_mg_level_types(const og_mg* m, int l) { return m->type[l]; }
-const float* og_mg_level_matrix(const og_mg* m, int l) { return m->A[l]; }
+const og_real* og_mg_level_matrix(const og_mg* m, int l) { return m->A[l]; }
 
 /* NKMinHeap (multigrid.cpp:59-203): bucket lists, head insertion */
 typedef struct { int key, prev, next; } hentry;
@@ -1260,8 +1275,8 @@ static void mg_gen_coarse_op(og_mg* m, int l) {
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (idx = 0; idx < m->n[l]; idx++) {
     if (m->type[l][idx] == VT_INACTIVE) continue;
-    float* A = m->A[l] + idx * S;
-    for (int i = 0; i < S; i++) A[i] = 0.f;
+    og_real* A = m->A[l] + idx * S;
+    for (int i = 0; i < S; i++) A[i] = OG_R(0.);
     int V[3];
     mg_vec(m, l, idx, V);
     if (l == 1) {
@@ -1289,7 +1304,7 @@ static void mg_gen_coarse_op(og_mg* m, int l) {
           for (U[0] = ulo[0]; U[0] <= uhi[0]; U[0]++) {
             const ll u = mg_lin(m, l - 1, U);
             if (m->type[l - 1][u] == VT_INACTIVE) continue;
-            const float rw = 1.f / (float)(1 << ((U[0] % 2) + (U[1] % 2) + (U[2] % 2)));
+            const og_real rw = OG_R(1.) / (og_real)(1 << ((U[0] % 2) + (U[1] % 2) + (U[2] % 2)));
             int nlo[3], nhi[3], N[3];
             for (int c = 0; c < 3; c++) { nlo[c] = (U[c] - 1) / 2; nhi[c] = imin(m->size[l][c] - 1, (U[c] + 2) / 2); }
             for (N[2] = nlo[2]; N[2] <= nhi[2]; N[2]++)
@@ -1310,7 +1325,7 @@ static void mg_gen_coarse_op(og_mg* m, int l) {
                         const ll w = mg_lin(m, l - 1, W);
                         if (m->type[l - 1][w] == VT_INACTIVE) continue;
                         const int sf = (W[0] - U[0] + m->smax[0]) + 3 * (W[1] - U[1] + m->smax[1]) + 9 * (W[2] - U[2] + m->smax[2]);
-                        const float iw = 1.f / (float)(1 << ((W[0] % 2) + (W[1] % 2) + (W[2] % 2)));
+                        const og_real iw = OG_R(1.) / (og_real)(1 << ((W[0] % 2) + (W[1] % 2) + (W[2] % 2)));
                         if (sf < S) A[sc - S + 1] += rw * m->A[l - 1][w * S + S - 1 - sf] * iw;
                         else A[sc - S + 1] += rw * m->A[l - 1][u * S + sf - S + 1] * iw;
                       }
@@ -1321,7 +1336,7 @@ static void mg_gen_coarse_op(og_mg* m, int l) {
 }
 
 /* GridMg::setA (multigrid.cpp:386-415) with knCopyA/knActivateVertices */
-static void mg_set_a(og_mg* m, const float* A0, const float* Ai, const float* Aj, const float* Ak) {
+static void mg_set_a(og_mg* m, const og_real* A0, const og_real* Ai, const og_real* Aj, const og_real* Ak) {
   const int S0 = m->S0;
   const ll n = m->n[0];
   for (ll v = 0; v < n; v++) {
@@ -1332,19 +1347,19 @@ static void mg_set_a(og_mg* m, const float* A0, const float* Ai, const float* Aj
   }
   for (ll v = 0; v < n; v++) {
     m->type[0][v] = VT_INACTIVE;
-    if (m->A[0][v * S0 + 0] != 0.f) {
+    if (m->A[0][v * S0 + 0] != OG_R(0.)) {
       m->type[0][v] = VT_ACTIVE;
       int V[3];
       mg_vec(m, 0, v, V);
-      float a[7];
+      og_real a[7];
       a[0] = m->A[0][v * S0 + 0];
       a[1] = m->A[0][v * S0 + 1];
       a[2] = m->A[0][v * S0 + 2];
-      a[3] = m->is3d ? m->A[0][v * S0 + 3] : 0.f;
-      a[4] = V[0] != 0 ? m->A[0][(v - m->pitch[0][0]) * S0 + 1] : 0.f;
-      a[5] = V[1] != 0 ? m->A[0][(v - m->pitch[0][1]) * S0 + 2] : 0.f;
-      a[6] = (V[2] != 0 && m->is3d) ? m->A[0][(v - m->pitch[0][2]) * S0 + 3] : 0.f;
-      const int trivial = a[0] == 1.f && a[1] == 0.f && a[2] == 0.f && a[3] == 0.f && a[4] == 0.f && a[5] == 0.f && a[6] == 0.f;
+      a[3] = m->is3d ? m->A[0][v * S0 + 3] : OG_R(0.);
+      a[4] = V[0] != 0 ? m->A[0][(v - m->pitch[0][0]) * S0 + 1] : OG_R(0.);
+      a[5] = V[1] != 0 ? m->A[0][(v - m->pitch[0][1]) * S0 + 2] : OG_R(0.);
+      a[6] = (V[2] != 0 && m->is3d) ? m->A[0][(v - m->pitch[0][2]) * S0 + 3] : OG_R(0.);
+      const int trivial = a[0] == OG_R(1.) && a[1] == OG_R(0.) && a[2] == OG_R(0.) && a[3] == OG_R(0.) && a[4] == OG_R(0.) && a[5] == OG_R(0.) && a[6] == OG_R(0.);
       if (trivial) {
         m->type[0][v] = VT_ACTIVE_TRIVIAL;
         m->A[0][v * S0 + 0] *= m->trivialScale;
@@ -1385,7 +1400,7 @@ static void mg_smooth(og_mg* m, int l, int reversed) {
   const int bs[3] = {(m->size[l][0] + 1) / 2, (m->size[l][1] + 1) / 2, (m->size[l][2] + 1) / 2};
   const ll nb = (ll)bs[0] * bs[1] * bs[2];
   const int S = m->S, S0 = m->S0;
-  float* x = m->x[l];
+  og_real* x = m->x[l];
   for (int cc = 0; cc < nc; cc++) {
     const int color = reversed ? nc - 1 - cc : cc;
     ll bi;
@@ -1398,7 +1413,7 @@ static void mg_smooth(og_mg* m, int l, int reversed) {
         if (!mg_in(m, l, V)) continue;
         const ll v = mg_lin(m, l, V);
         if (m->type[l][v] == VT_INACTIVE) continue;
-        float sum = m->b[l][v];
+        og_real sum = m->b[l][v];
         if (l == 0) {
           for (int dd = 0; dd < m->dim; dd++) {
             if (V[dd] > 0) { const ll nn = v - m->pitch[0][dd]; sum -= m->A[0][nn * S0 + dd + 1] * x[nn]; }
@@ -1428,14 +1443,14 @@ static void mg_smooth(og_mg* m, int l, int reversed) {
 /* knCalcResidual (multigrid.cpp:739-771) */
 static void mg_residual(og_mg* m, int l) {
   const int S = m->S, S0 = m->S0;
-  const float* x = m->x[l];
+  const og_real* x = m->x[l];
   ll idx;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (idx = 0; idx < m->n[l]; idx++) {
     if (m->type[l][idx] == VT_INACTIVE) continue;
     int V[3];
     mg_vec(m, l, idx, V);
-    float sum = m->b[l][idx];
+    og_real sum = m->b[l][idx];
     if (l == 0) {
       for (int dd = 0; dd < m->dim; dd++) {
         if (V[dd] > 0) { const ll nn = idx - m->pitch[0][dd]; sum -= m->A[0][nn * S0 + dd + 1] * x[nn]; }
@@ -1469,13 +1484,13 @@ static void mg_restrict(og_mg* m, int ld) {
     int V[3], lo[3], hi[3], R[3];
     mg_vec(m, ld, idx, V);
     for (int c = 0; c < 3; c++) { lo[c] = imax(0, V[c] * 2 - 1); hi[c] = imin(m->size[ls][c] - 1, V[c] * 2 + 1); }
-    float sum = 0.f;
+    og_real sum = OG_R(0.);
     for (R[2] = lo[2]; R[2] <= hi[2]; R[2]++)
       for (R[1] = lo[1]; R[1] <= hi[1]; R[1]++)
         for (R[0] = lo[0]; R[0] <= hi[0]; R[0]++) {
           const ll r = mg_lin(m, ls, R);
           if (m->type[ls][r] == VT_INACTIVE) continue;
-          const float rw = 1.f / (float)(1 << ((R[0] % 2) + (R[1] % 2) + (R[2] % 2)));
+          const og_real rw = OG_R(1.) / (og_real)(1 << ((R[0] % 2) + (R[1] % 2) + (R[2] % 2)));
           sum += rw * m->r[ls][r];
         }
     m->b[ld][idx] = sum;
@@ -1491,14 +1506,14 @@ static void mg_interpolate(og_mg* m, int ld) {
     if (m->type[ld][idx] == VT_INACTIVE) continue;
     int V[3], I[3];
     mg_vec(m, ld, idx, V);
-    float sum = 0.f;
+    og_real sum = OG_R(0.);
     for (I[2] = V[2] / 2; I[2] <= (V[2] + 1) / 2; I[2]++)
       for (I[1] = V[1] / 2; I[1] <= (V[1] + 1) / 2; I[1]++)
         for (I[0] = V[0] / 2; I[0] <= (V[0] + 1) / 2; I[0]++) {
           const ll i = mg_lin(m, ls, I);
           if (m->type[ls][i] != VT_INACTIVE) sum += m->x[ls][i];
         }
-    const float iw = 1.f / (float)(1 << ((V[0] % 2) + (V[1] % 2) + (V[2] % 2)));
+    const og_real iw = OG_R(1.) / (og_real)(1 << ((V[0] % 2) + (V[1] % 2) + (V[2] % 2)));
     m->r[ld][idx] = iw * sum;
   }
 }
@@ -1575,20 +1590,20 @@ static void mg_solve_cg(og_mg* m, int l) {
     alphaTop = alphaTopNew;
     for (ll v = 0; v < n; v++) p[v] = z[v] + beta * p[v];
   }
-  for (ll v = 0; v < n; v++) m->x[l][v] = (float)x[v];
+  for (ll v = 0; v < n; v++) m->x[l][v] = (og_real)x[v];
 }
 
 /* GridMg::doVCycle (multigrid.cpp:448-504) from a zero initial guess.  The
  * trailing residual norm of the reference is not used by the CG and is not
  * computed here. */
-static void mg_do_vcycle(og_mg* m, float* dst) {
+static void mg_do_vcycle(og_mg* m, og_real* dst) {
   const int maxL = m->nlev - 1;
-  memset(m->x[0], 0, sizeof(float) * m->n[0]);
+  memset(m->x[0], 0, sizeof(og_real) * m->n[0]);
   for (int l = 0; l < maxL; l++) {
     mg_smooth(m, l, 0);
     mg_residual(m, l);
     mg_restrict(m, l + 1);
-    memset(m->x[l + 1], 0, sizeof(float) * m->n[l + 1]);
+    memset(m->x[l + 1], 0, sizeof(og_real) * m->n[l + 1]);
   }
   mg_solve_cg(m, maxL);
   for (int l = maxL - 1; l >= 0; l--) {
@@ -1596,19 +1611,19 @@ static void mg_do_vcycle(og_mg* m, float* dst) {
     for (ll i = 0; i < m->n[l]; i++) m->x[l][i] += m->r[l][i];
     mg_smooth(m, l, 1);
   }
-  memcpy(dst, m->x[0], sizeof(float) * m->n[0]);
+  memcpy(dst, m->x[0], sizeof(og_real) * m->n[0]);
 }
 
 /* knSetRhs (multigrid.cpp:417-432) */
-static void mg_set_rhs(og_mg* m, const float* rhs) {
+static void mg_set_rhs(og_mg* m, const og_real* rhs) {
   for (ll i = 0; i < m->n[0]; i++) {
     m->b[0][i] = rhs[i];
     if (m->type[0][i] == VT_ACTIVE_TRIVIAL) m->b[0][i] *= m->trivialScale;
   }
 }
 
-void og_mg_vcycle(og_mg* m, const float* A0, const float* Ai, const float* Aj, const float* Ak, float* dst,
-                  const float* rhs, float coarseAccuracy) {
+void og_mg_vcycle(og_mg* m, const og_real* A0, const og_real* Ai, const og_real* Aj, const og_real* Ak, og_real* dst,
+                  const og_real* rhs, og_real coarseAccuracy) {
   if (!m->isASet) mg_set_a(m, A0, Ai, Aj, Ak);
   m->coarseAcc = coarseAccuracy;
   mg_set_rhs(m, rhs);
@@ -1619,23 +1634,23 @@ void og_mg_vcycle(og_mg* m, const float* A0, const float* Ai, const float* Aj, c
 /* solvePressureSystem (pressure.cpp:312-452) with GridCg (conjugategrad.cpp
  * :209-299)                                                                 */
 
-static void scaled_add(ll n, float* me, const float* other, float factor) {
+static void scaled_add(ll n, og_real* me, const og_real* other, og_real factor) {
   ll i;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (i = 0; i < n; i++) me[i] += factor * other[i];
 }
 
-int og_solve_pressure_system(og_dims d, float* rhs, float* pressure, const int* flags, const float* phi,
+int og_solve_pressure_system(og_dims d, og_real* rhs, og_real* pressure, const int* flags, const og_real* phi,
                              const og_pressure_params* p, og_mg** mg_cache, og_pressure_result* out) {
   const ll n = NCELL(d);
-  float* residual = (float*)calloc((size_t)n, sizeof(float));
-  float* search = (float*)calloc((size_t)n, sizeof(float));
-  float* A0 = (float*)calloc((size_t)n, sizeof(float));
-  float* Ai = (float*)calloc((size_t)n, sizeof(float));
-  float* Aj = (float*)calloc((size_t)n, sizeof(float));
-  float* Ak = (float*)calloc((size_t)n, sizeof(float));
-  float* tmp = (float*)calloc((size_t)n, sizeof(float));
-  float* pca0 = NULL;
+  og_real* residual = (og_real*)calloc((size_t)n, sizeof(og_real));
+  og_real* search = (og_real*)calloc((size_t)n, sizeof(og_real));
+  og_real* A0 = (og_real*)calloc((size_t)n, sizeof(og_real));
+  og_real* Ai = (og_real*)calloc((size_t)n, sizeof(og_real));
+  og_real* Aj = (og_real*)calloc((size_t)n, sizeof(og_real));
+  og_real* Ak = (og_real*)calloc((size_t)n, sizeof(og_real));
+  og_real* tmp = (og_real*)calloc((size_t)n, sizeof(og_real));
+  og_real* pca0 = NULL;
   int pc = p->preconditioner;
   int status = 0;
   og_make_laplace_matrix(d, flags, A0, Ai, Aj, Ak);
@@ -1661,7 +1676,7 @@ int og_solve_pressure_system(og_dims d, float* rhs, float* pressure, const int* 
     if (fixPidx >= 0) {
       /* fixPressure(fixPidx, 0, ...) (pressure.cpp:226-245) */
       const ll X = 1, Y = SY(d), Z = SZ(d);
-      const float value = 0.f;
+      const og_real value = OG_R(0.);
       rhs[fixPidx + X] -= Ai[fixPidx] * value;
       rhs[fixPidx + Y] -= Aj[fixPidx] * value;
       rhs[fixPidx - X] -= Ai[fixPidx - X] * value;
@@ -1671,11 +1686,11 @@ int og_solve_pressure_system(og_dims d, float* rhs, float* pressure, const int* 
         rhs[fixPidx - Z] -= Ak[fixPidx - Z] * value;
       }
       rhs[fixPidx] = value;
-      A0[fixPidx] = 1.f;
-      Ai[fixPidx] = Aj[fixPidx] = Ak[fixPidx] = 0.f;
-      Ai[fixPidx - X] = 0.f;
-      Aj[fixPidx - Y] = 0.f;
-      if (d.is3d) Ak[fixPidx - Z] = 0.f;
+      A0[fixPidx] = OG_R(1.);
+      Ai[fixPidx] = Aj[fixPidx] = Ak[fixPidx] = OG_R(0.);
+      Ai[fixPidx - X] = OG_R(0.);
+      Aj[fixPidx - Y] = OG_R(0.);
+      if (d.is3d) Ak[fixPidx - Z] = OG_R(0.);
     }
   }
 
@@ -1687,9 +1702,9 @@ int og_solve_pressure_system(og_dims d, float* rhs, float* pressure, const int* 
     goto done;
   }
   if (pc == OG_PC_MIC) {
-    maxIter = (int)(p->cgMaxIterFac * (float)imax(d.nx, imax(d.ny, d.nz))) * (d.is3d ? 1 : 4);
+    maxIter = (int)(p->cgMaxIterFac * (og_real)imax(d.nx, imax(d.ny, d.nz))) * (d.is3d ? 1 : 4);
     if (!d.is3d) pc = OG_PC_NONE; /* mICP only in 3D (conjugategrad.cpp:315-321) */
-    if (pc == OG_PC_MIC) pca0 = (float*)calloc((size_t)n, sizeof(float));
+    if (pc == OG_PC_MIC) pca0 = (og_real*)calloc((size_t)n, sizeof(og_real));
   } else if (pc == OG_PC_MG_DYNAMIC || pc == OG_PC_MG_STATIC) {
     maxIter = 100;
     mg = *mg_cache;
@@ -1702,42 +1717,42 @@ int og_solve_pressure_system(og_dims d, float* rhs, float* pressure, const int* 
 
   {
     /* GridCg::doInit (conjugategrad.cpp:209-235) */
-    const float acc = p->cgAccuracy;
+    const og_real acc = p->cgAccuracy;
     int iterations = 0;
-    float sigma, resNorm = 1e20f;
-    memset(pressure, 0, sizeof(float) * n);
-    memcpy(residual, rhs, sizeof(float) * n);
+    og_real sigma, resNorm = OG_R(1e20);
+    memset(pressure, 0, sizeof(og_real) * n);
+    memcpy(residual, rhs, sizeof(og_real) * n);
     if (pc == OG_PC_MIC) {
       og_mic_init(d, flags, pca0, A0, Ai, Aj, Ak);
       og_mic_apply(d, tmp, residual, flags, pca0, Ai, Aj, Ak);
     } else if (mg) {
       if (!mg->isASet) mg_set_a(mg, A0, Ai, Aj, Ak);
-      mg->coarseAcc = (float)((double)acc * 1E-4);
+      mg->coarseAcc = (og_real)((double)acc * 1E-4);
       mg_set_rhs(mg, residual);
       mg_do_vcycle(mg, tmp);
     } else {
-      memcpy(tmp, residual, sizeof(float) * n);
+      memcpy(tmp, residual, sizeof(og_real) * n);
     }
-    memcpy(search, tmp, sizeof(float) * n);
-    sigma = (float)dot_product(n, tmp, residual);
+    memcpy(search, tmp, sizeof(og_real) * n);
+    sigma = (og_real)dot_product(n, tmp, residual);
 
     for (int iter = 0; iter < maxIter; iter++) {
       /* GridCg::iterate (conjugategrad.cpp:237-299) */
       iterations++;
       og_apply_matrix(d, flags, tmp, search, A0, Ai, Aj, Ak);
-      const float dp = (float)dot_product(n, tmp, search);
-      float alpha = 0.f;
-      if (fabsf(dp) > 0.f) alpha = sigma / dp;
+      const og_real dp = (og_real)dot_product(n, tmp, search);
+      og_real alpha = OG_R(0.);
+      if (og_fabs(dp) > OG_R(0.)) alpha = sigma / dp;
       scaled_add(n, pressure, search, alpha);
       scaled_add(n, residual, tmp, -alpha);
       if (pc == OG_PC_MIC) og_mic_apply(d, tmp, residual, flags, pca0, Ai, Aj, Ak);
       else if (mg) { mg_set_rhs(mg, residual); mg_do_vcycle(mg, tmp); }
-      else memcpy(tmp, residual, sizeof(float) * n);
-      if (p->useL2Norm) resNorm = (float)sum_sqr(n, residual);
+      else memcpy(tmp, residual, sizeof(og_real) * n);
+      if (p->useL2Norm) resNorm = (og_real)sum_sqr(n, residual);
       else resNorm = og_get_max_abs(n, residual);
       if (resNorm < acc) { sigma = resNorm; break; }
-      const float sigmaNew = (float)dot_product(n, tmp, residual);
-      const float beta = sigmaNew / sigma;
+      const og_real sigmaNew = (og_real)dot_product(n, tmp, residual);
+      const og_real beta = sigmaNew / sigma;
       ll i;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
       for (i = 0; i < n; i++) search[i] = tmp[i] + beta * search[i];
@@ -1755,8 +1770,8 @@ done:
 
 /* knCorrectVelocity (pressure.cpp:87-109), knCorrectVelocityGhostFluid
  * (:154-187), knReplaceClampedGhostFluidVels (:198-214) */
-void og_correct_velocity(og_dims d, float* vel, const float* pr, const int* flags, const float* phi,
-                         const float* curv, const og_pressure_params* p) {
+void og_correct_velocity(og_dims d, og_real* vel, const og_real* pr, const int* flags, const og_real* phi,
+                         const og_real* curv, const og_pressure_params* p) {
   const ll X = 1, Y = SY(d), Z = SZ(d);
   int k;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
@@ -1764,7 +1779,7 @@ void og_correct_velocity(og_dims d, float* vel, const float* pr, const int* flag
     for (int j = 1; j < d.ny - 1; j++)
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
-        float* v = vel + 3 * idx;
+        og_real* v = vel + 3 * idx;
         if (isF(flags, idx)) {
           if (isF(flags, idx - X)) v[0] -= (pr[idx] - pr[idx - X]);
           if (isF(flags, idx - Y)) v[1] -= (pr[idx] - pr[idx - Y]);
@@ -1773,38 +1788,38 @@ void og_correct_velocity(og_dims d, float* vel, const float* pr, const int* flag
           if (isE(flags, idx - Y)) v[1] -= pr[idx];
           if (d.is3d && isE(flags, idx - Z)) v[2] -= pr[idx];
         } else if (isE(flags, idx) && !isOut(flags, idx)) {
-          if (isF(flags, idx - X)) v[0] += pr[idx - X]; else v[0] = 0.f;
-          if (isF(flags, idx - Y)) v[1] += pr[idx - Y]; else v[1] = 0.f;
-          if (d.is3d) { if (isF(flags, idx - Z)) v[2] += pr[idx - Z]; else v[2] = 0.f; }
+          if (isF(flags, idx - X)) v[0] += pr[idx - X]; else v[0] = OG_R(0.);
+          if (isF(flags, idx - Y)) v[1] += pr[idx - Y]; else v[1] = OG_R(0.);
+          if (d.is3d) { if (isF(flags, idx - Z)) v[2] += pr[idx - Z]; else v[2] = OG_R(0.); }
         }
       }
   if (!phi) return;
-  const float gfc = p->gfClamp;
+  const og_real gfc = p->gfClamp;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (k = KLO(d, 1); k < KHI(d, 1); k++)
     for (int j = 1; j < d.ny - 1; j++)
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
-        float* v = vel + 3 * idx;
+        og_real* v = vel + 3 * idx;
         if (isF(flags, idx)) {
           if (isE(flags, idx - X)) v[0] += pr[idx] * gf_helper(phi, idx, -X, gfc);
           if (isE(flags, idx - Y)) v[1] += pr[idx] * gf_helper(phi, idx, -Y, gfc);
           if (d.is3d && isE(flags, idx - Z)) v[2] += pr[idx] * gf_helper(phi, idx, -Z, gfc);
         } else if (isE(flags, idx) && !isOut(flags, idx)) {
-          if (isF(flags, idx - X)) v[0] -= pr[idx - X] * gf_helper(phi, idx - X, +X, gfc); else v[0] = 0.f;
-          if (isF(flags, idx - Y)) v[1] -= pr[idx - Y] * gf_helper(phi, idx - Y, +Y, gfc); else v[1] = 0.f;
-          if (d.is3d) { if (isF(flags, idx - Z)) v[2] -= pr[idx - Z] * gf_helper(phi, idx - Z, +Z, gfc); else v[2] = 0.f; }
+          if (isF(flags, idx - X)) v[0] -= pr[idx - X] * gf_helper(phi, idx - X, +X, gfc); else v[0] = OG_R(0.);
+          if (isF(flags, idx - Y)) v[1] -= pr[idx - Y] * gf_helper(phi, idx - Y, +Y, gfc); else v[1] = OG_R(0.);
+          if (d.is3d) { if (isF(flags, idx - Z)) v[2] -= pr[idx - Z] * gf_helper(phi, idx - Z, +Z, gfc); else v[2] = OG_R(0.); }
         }
         if (curv) {
-          const float st = p->surfTens;
+          const og_real st = p->surfTens;
           if (isF(flags, idx)) {
             if (isE(flags, idx - X)) v[0] += surf_tens_helper(phi, curv, idx, -X, st, gfc);
             if (isE(flags, idx - Y)) v[1] += surf_tens_helper(phi, curv, idx, -Y, st, gfc);
             if (d.is3d && isE(flags, idx - Z)) v[2] += surf_tens_helper(phi, curv, idx, -Z, st, gfc);
           } else if (isE(flags, idx) && !isOut(flags, idx)) {
-            v[0] -= isF(flags, idx - X) ? surf_tens_helper(phi, curv, idx - X, +X, st, gfc) : 0.f;
-            v[1] -= isF(flags, idx - Y) ? surf_tens_helper(phi, curv, idx - Y, +Y, st, gfc) : 0.f;
-            if (d.is3d) v[2] -= isF(flags, idx - Z) ? surf_tens_helper(phi, curv, idx - Z, +Z, st, gfc) : 0.f;
+            v[0] -= isF(flags, idx - X) ? surf_tens_helper(phi, curv, idx - X, +X, st, gfc) : OG_R(0.);
+            v[1] -= isF(flags, idx - Y) ? surf_tens_helper(phi, curv, idx - Y, +Y, st, gfc) : OG_R(0.);
+            if (d.is3d) v[2] -= isF(flags, idx - Z) ? surf_tens_helper(phi, curv, idx - Z, +Z, st, gfc) : OG_R(0.);
           }
         }
       }
@@ -1815,7 +1830,7 @@ void og_correct_velocity(og_dims d, float* vel, const float* pr, const int* flag
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
         if (!isE(flags, idx)) continue;
-        float* v = vel + 3 * idx;
+        og_real* v = vel + 3 * idx;
         if (isF(flags, idx - X) && CLAMPED(idx - X, +X)) v[0] = vel[3 * (idx - X) + 0];
         if (isF(flags, idx - Y) && CLAMPED(idx - Y, +Y)) v[1] = vel[3 * (idx - Y) + 1];
         if (d.is3d && isF(flags, idx - Z) && CLAMPED(idx - Z, +Z)) v[2] = vel[3 * (idx - Z) + 2];
@@ -1826,15 +1841,15 @@ void og_correct_velocity(og_dims d, float* vel, const float* pr, const int* flag
 #undef CLAMPED
 }
 
-int og_solve_pressure(og_dims d, float* vel, float* pressure, const int* flags, const float* phi,
-                      const float* perCellCorr, const float* curv, const og_pressure_params* p, og_mg** mg_cache,
-                      og_pressure_result* out, float* retRhs) {
+int og_solve_pressure(og_dims d, og_real* vel, og_real* pressure, const int* flags, const og_real* phi,
+                      const og_real* perCellCorr, const og_real* curv, const og_pressure_params* p, og_mg** mg_cache,
+                      og_pressure_result* out, og_real* retRhs) {
   const ll n = NCELL(d);
-  float* rhs = (float*)calloc((size_t)n, sizeof(float));
+  og_real* rhs = (og_real*)calloc((size_t)n, sizeof(og_real));
   og_compute_pressure_rhs(d, rhs, vel, flags, phi, perCellCorr, curv, p);
   int st = og_solve_pressure_system(d, rhs, pressure, flags, phi, p, mg_cache, out);
   if (st == 0) og_correct_velocity(d, vel, pressure, flags, phi, curv, p);
-  if (retRhs) memcpy(retRhs, rhs, sizeof(float) * n);
+  if (retRhs) memcpy(retRhs, rhs, sizeof(og_real) * n);
   free(rhs);
   return st;
 }
@@ -1921,39 +1936,39 @@ void og_set_open_bound(og_dims d, int* flags, int bWidth, const char* openBound,
 
 /* FlagGrid::updateFromLevelset (grid.cpp:844-854); invalidTimeValue is
  * -1000 (levelset.h) */
-void og_update_from_levelset(og_dims d, int* flags, const float* phi) {
+void og_update_from_levelset(og_dims d, int* flags, const og_real* phi) {
   const ll n = NCELL(d);
   for (ll idx = 0; idx < n; idx++) {
     if (!isO(flags, idx) && !isOut(flags, idx)) {
-      const float ph = phi[idx];
-      if (ph <= -1000.f) continue;
+      const og_real ph = phi[idx];
+      if (ph <= -OG_R(1000.)) continue;
       flags[idx] &= ~(OG_EMPTY | OG_FLUID);
       flags[idx] |= (ph <= 0) ? OG_FLUID : OG_EMPTY;
     }
   }
 }
 
-static inline float fmaxf_(float a, float b) { return a < b ? b : a; }
-static inline float fminf_(float a, float b) { return b < a ? b : a; }
+static inline og_real fmaxf_(og_real a, og_real b) { return a < b ? b : a; }
+static inline og_real fminf_(og_real a, og_real b) { return b < a ? b : a; }
 
-/* norm() of vectorbase.h:379-384 in float */
-static inline float vnorm(float x, float y, float z) {
-  const float l = x * x + y * y + z * z;
-  if (l <= 1e-6f * 1e-6f) return 0.f;
-  return (fabs(l - 1.) < 1e-6f * 1e-6f) ? 1.f : sqrtf(l);
+/* norm() of vectorbase.h:379-384 in Real */
+static inline og_real vnorm(og_real x, og_real y, og_real z) {
+  const og_real l = x * x + y * y + z * z;
+  if (l <= OG_VEC_EPS * OG_VEC_EPS) return OG_R(0.);
+  return (fabs(l - 1.) < OG_VEC_EPS * OG_VEC_EPS) ? OG_R(1.) : og_sqrt(l);
 }
 
 /* BoxSDF (shapes.cpp:178-228) */
-void og_box_sdf(og_dims d, float* phi, float p1x, float p1y, float p1z, float p2x, float p2y, float p2z) {
+void og_box_sdf(og_dims d, og_real* phi, og_real p1x, og_real p1y, og_real p1z, og_real p2x, og_real p2y, og_real p2z) {
   for (int k = 0; k < d.nz; k++)
     for (int j = 0; j < d.ny; j++)
       for (int i = 0; i < d.nx; i++) {
         const ll idx = IX(d, i, j, k);
-        const float px = (float)(i + 0.5), py = (float)(j + 0.5), pz = (float)(k + 0.5);
-        float v;
+        const og_real px = (og_real)(i + 0.5), py = (og_real)(j + 0.5), pz = (og_real)(k + 0.5);
+        og_real v;
 #define SQ(a) ((a) * (a))
         if (px <= p2x && px >= p1x && py <= p2y && py >= p1y && pz <= p2z && pz >= p1z) {
-          float mx = fmaxf_(px - p2x, p1x - px), my = fmaxf_(py - p2y, p1y - py), mz = fmaxf_(pz - p2z, p1z - pz);
+          og_real mx = fmaxf_(px - p2x, p1x - px), my = fmaxf_(py - p2y, p1y - py), mz = fmaxf_(pz - p2z, p1z - pz);
           if (!d.is3d) mz = mx;
           v = fmaxf_(mx, fmaxf_(my, mz));
         } else if (py <= p2y && py >= p1y && pz <= p2z && pz >= p1z) {
@@ -1963,19 +1978,19 @@ void og_box_sdf(og_dims d, float* phi, float p1x, float p1y, float p1z, float p2
         } else if (px <= p2x && px >= p1x && py <= p2y && py >= p1y) {
           v = fmaxf_(pz - p2z, p1z - pz);
         } else if (px > p1x && px < p2x) {
-          float m1 = sqrtf(SQ(p1y - py) + SQ(p1z - pz)), m2 = sqrtf(SQ(p2y - py) + SQ(p1z - pz));
-          float m3 = sqrtf(SQ(p1y - py) + SQ(p2z - pz)), m4 = sqrtf(SQ(p2y - py) + SQ(p2z - pz));
+          og_real m1 = og_sqrt(SQ(p1y - py) + SQ(p1z - pz)), m2 = og_sqrt(SQ(p2y - py) + SQ(p1z - pz));
+          og_real m3 = og_sqrt(SQ(p1y - py) + SQ(p2z - pz)), m4 = og_sqrt(SQ(p2y - py) + SQ(p2z - pz));
           v = fminf_(m1, fminf_(m2, fminf_(m3, m4)));
         } else if (py > p1y && py < p2y) {
-          float m1 = sqrtf(SQ(p1x - px) + SQ(p1z - pz)), m2 = sqrtf(SQ(p2x - px) + SQ(p1z - pz));
-          float m3 = sqrtf(SQ(p1x - px) + SQ(p2z - pz)), m4 = sqrtf(SQ(p2x - px) + SQ(p2z - pz));
+          og_real m1 = og_sqrt(SQ(p1x - px) + SQ(p1z - pz)), m2 = og_sqrt(SQ(p2x - px) + SQ(p1z - pz));
+          og_real m3 = og_sqrt(SQ(p1x - px) + SQ(p2z - pz)), m4 = og_sqrt(SQ(p2x - px) + SQ(p2z - pz));
           v = fminf_(m1, fminf_(m2, fminf_(m3, m4)));
         } else if (pz > p1x && pz < p2z) {
-          float m1 = sqrtf(SQ(p1y - py) + SQ(p1x - px)), m2 = sqrtf(SQ(p2y - py) + SQ(p1x - px));
-          float m3 = sqrtf(SQ(p1y - py) + SQ(p2x - px)), m4 = sqrtf(SQ(p2y - py) + SQ(p2x - px));
+          og_real m1 = og_sqrt(SQ(p1y - py) + SQ(p1x - px)), m2 = og_sqrt(SQ(p2y - py) + SQ(p1x - px));
+          og_real m3 = og_sqrt(SQ(p1y - py) + SQ(p2x - px)), m4 = og_sqrt(SQ(p2y - py) + SQ(p2x - px));
           v = fminf_(m1, fminf_(m2, fminf_(m3, m4)));
         } else {
-          float m = vnorm(px - p1x, py - p1y, pz - p1z);
+          og_real m = vnorm(px - p1x, py - p1y, pz - p1z);
           m = fminf_(m, vnorm(px - p1x, py - p1y, pz - p2z));
           m = fminf_(m, vnorm(px - p1x, py - p2y, pz - p1z));
           m = fminf_(m, vnorm(px - p1x, py - p2y, pz - p2z));
@@ -1992,48 +2007,48 @@ void og_box_sdf(og_dims d, float* phi, float p1x, float p1y, float p1z, float p2
 
 /* Cylinder ctor normalisation (shapes.cpp:316-322) + isInside (:324-329)
  * at cell centres, ApplyShapeToGrid (:38-45) */
-void og_cylinder_apply(og_dims d, float* grid, float cx, float cy, float cz, float radius, float zx, float zy, float zz,
-                       float value, const int* respectFlags) {
+void og_cylinder_apply(og_dims d, og_real* grid, og_real cx, og_real cy, og_real cz, og_real radius, og_real zx, og_real zy, og_real zz,
+                       og_real value, const int* respectFlags) {
   /* normalize(mZDir): returns the length, scales by 1/len in double */
-  float nz_ = 0.f;
+  og_real nz_ = OG_R(0.);
   {
-    const float l = zx * zx + zy * zy + zz * zz;
-    if (fabs(l - 1.) < 1e-6f * 1e-6f) nz_ = 1.f;
-    else if (l > 1e-6f * 1e-6f) {
-      nz_ = sqrtf(l);
-      /* v *= 1./norm: operator*=(S) takes the factor as float */
-      const float inv = (float)(1. / (double)nz_);
+    const og_real l = zx * zx + zy * zy + zz * zz;
+    if (fabs(l - 1.) < OG_VEC_EPS * OG_VEC_EPS) nz_ = OG_R(1.);
+    else if (l > OG_VEC_EPS * OG_VEC_EPS) {
+      nz_ = og_sqrt(l);
+      /* v *= 1./norm: operator*=(S) takes the factor as Real */
+      const og_real inv = (og_real)(1. / (double)nz_);
       zx = zx * inv; zy = zy * inv; zz = zz * inv;
-    } else { zx = zy = zz = 0.f; nz_ = 0.f; }
+    } else { zx = zy = zz = OG_R(0.); nz_ = OG_R(0.); }
   }
-  const float mZ = nz_;
+  const og_real mZ = nz_;
   for (int k = 0; k < d.nz; k++)
     for (int j = 0; j < d.ny; j++)
       for (int i = 0; i < d.nx; i++) {
         const ll idx = IX(d, i, j, k);
         if (respectFlags && isO(respectFlags, idx)) continue;
-        const float px = (float)(i + 0.5) - cx, py = (float)(j + 0.5) - cy, pz = (float)(k + 0.5) - cz;
-        const float z = px * zx + py * zy + pz * zz;
-        if (fabsf(z) > mZ) continue;
-        const float r2 = (px * px + py * py + pz * pz) - z * z;
+        const og_real px = (og_real)(i + 0.5) - cx, py = (og_real)(j + 0.5) - cy, pz = (og_real)(k + 0.5) - cz;
+        const og_real z = px * zx + py * zy + pz * zz;
+        if (og_fabs(z) > mZ) continue;
+        const og_real r2 = (px * px + py * py + pz * pz) - z * z;
         if (r2 < radius * radius) grid[idx] = value;
       }
 }
 
 /* Box::isInside (shapes.cpp:151-154) at cell centres */
-void og_box_apply(og_dims d, float* grid, float p0x, float p0y, float p0z, float p1x, float p1y, float p1z, float value,
+void og_box_apply(og_dims d, og_real* grid, og_real p0x, og_real p0y, og_real p0z, og_real p1x, og_real p1y, og_real p1z, og_real value,
                   const int* respectFlags) {
   for (int k = 0; k < d.nz; k++)
     for (int j = 0; j < d.ny; j++)
       for (int i = 0; i < d.nx; i++) {
         const ll idx = IX(d, i, j, k);
         if (respectFlags && isO(respectFlags, idx)) continue;
-        const float px = (float)(i + 0.5), py = (float)(j + 0.5), pz = (float)(k + 0.5);
+        const og_real px = (og_real)(i + 0.5), py = (og_real)(j + 0.5), pz = (og_real)(k + 0.5);
         if (px >= p0x && py >= p0y && pz >= p0z && px <= p1x && py <= p1y && pz <= p1z) grid[idx] = value;
       }
 }
 
 /* knJoinReal (grid.cpp): keep max (or min) per cell */
-void og_join_real(ll n, float* a, const float* b, int keepMax) {
+void og_join_real(ll n, og_real* a, const og_real* b, int keepMax) {
   for (ll i = 0; i < n; i++) a[i] = keepMax ? fmaxf_(a[i], b[i]) : fminf_(a[i], b[i]);
 }

@@ -26,36 +26,54 @@ class Dims(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("is3d", C.c_int)]
 
 
-class PressureParams(C.Structure):
-    _fields_ = [("cgAccuracy", C.c_float), ("gfClamp", C.c_float), ("cgMaxIterFac", C.c_float),
-                ("preconditioner", C.c_int), ("enforceCompatibility", C.c_int), ("useL2Norm", C.c_int),
-                ("zeroPressureFixing", C.c_int), ("surfTens", C.c_float)]
+def _structs(R):
+    class PressureParams(C.Structure):
+        _fields_ = [("cgAccuracy", R), ("gfClamp", R), ("cgMaxIterFac", R),
+                    ("preconditioner", C.c_int), ("enforceCompatibility", C.c_int), ("useL2Norm", C.c_int),
+                    ("zeroPressureFixing", C.c_int), ("surfTens", R)]
+
+    class PressureResult(C.Structure):
+        _fields_ = [("iterations", C.c_int), ("resNorm", R), ("fixPidx", C.c_int)]
+
+    return PressureParams, PressureResult
 
 
-class PressureResult(C.Structure):
-    _fields_ = [("iterations", C.c_int), ("resNorm", C.c_float), ("fixPidx", C.c_int)]
+# float build (the reference's float executable, pinned by the goldens) and
+# double build (the reference's -DDOUBLEPRECISION=ON executable)
+_PREC = {np.float32: ("libmantaoracle.so", C.c_float), np.float64: ("libmantaoracle64.so", C.c_double)}
+_STRUCTS = {t: _structs(r) for t, (_, r) in _PREC.items()}
+PressureParams, PressureResult = _STRUCTS[np.float32]
 
 
 def build(force=False):
     """Compile the oracle with its Makefile (gcc/g++ only)."""
-    if force or not os.path.exists(_LIB_PATH) or \
-            os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "manta_oracle.cpp")):
+    src = os.path.getmtime(os.path.join(_HERE, "manta_oracle.cpp"))
+    paths = [os.path.join(_HERE, "_build", f) for f, _ in _PREC.values()]
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < src for p in paths):
         subprocess.run(["make", "-C", _HERE, "-s"], check=True)
     return _LIB_PATH
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def _prec(dtype):
+    t = np.dtype(dtype).type
+    if t not in _PREC:
+        raise TypeError("oracle grids are float32 or float64, not %s" % np.dtype(dtype))
+    return t
+
+
+def lib(dtype=np.float32):
+    t = _prec(dtype)
+    if t not in _libs:
         build()
-        L = C.CDLL(_LIB_PATH)
-        fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L = C.CDLL(os.path.join(_HERE, "_build", _PREC[t][0]))
+        fp = np.ctypeslib.ndpointer(dtype=t, flags="C_CONTIGUOUS")
         ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
-        F = C.c_float
+        F = _PREC[t][1]
         I = C.c_int
+        PP, PR = _STRUCTS[t]
         L.og_advect_semi_lagrange.argtypes = [Dims, ip, fp, I, fp, I, F, I, I, I, F]
         L.og_advect_semi_lagrange.restype = I
         L.og_set_wall_bcs.argtypes = [Dims, ip, fp, C.c_void_p]
@@ -65,11 +83,9 @@ def lib():
         L.og_mg_create.argtypes = [Dims]
         L.og_mg_create.restype = C.c_void_p
         L.og_mg_destroy.argtypes = [C.c_void_p]
-        L.og_compute_pressure_rhs.argtypes = [Dims, fp, fp, ip, C.c_void_p, C.c_void_p, C.c_void_p,
-                                              C.POINTER(PressureParams)]
+        L.og_compute_pressure_rhs.argtypes = [Dims, fp, fp, ip, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(PP)]
         L.og_solve_pressure.argtypes = [Dims, fp, fp, ip, C.c_void_p, C.c_void_p, C.c_void_p,
-                                        C.POINTER(PressureParams), C.POINTER(C.c_void_p),
-                                        C.POINTER(PressureResult), C.c_void_p]
+                                        C.POINTER(PP), C.POINTER(C.c_void_p), C.POINTER(PR), C.c_void_p]
         L.og_solve_pressure.restype = I
         L.og_make_laplace_matrix.argtypes = [Dims, ip, fp, fp, fp, fp]
         L.og_apply_ghost_fluid_diagonal.argtypes = [Dims, fp, ip, fp, F]
@@ -83,7 +99,7 @@ def lib():
         L.og_mg_level_types.argtypes = [C.c_void_p, I]
         L.og_mg_level_types.restype = C.POINTER(C.c_int8)
         L.og_mg_level_matrix.argtypes = [C.c_void_p, I]
-        L.og_mg_level_matrix.restype = C.POINTER(C.c_float)
+        L.og_mg_level_matrix.restype = C.POINTER(F)
         L.og_init_domain.argtypes = [Dims, ip, I, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p]
         L.og_fill_grid.argtypes = [Dims, ip, I]
         L.og_set_open_bound.argtypes = [Dims, ip, I, C.c_char_p, I]
@@ -96,8 +112,8 @@ def lib():
         L.og_get_max_abs.restype = F
         L.og_set_num_threads.argtypes = [I]
         L.og_get_num_threads.restype = I
-        _lib = L
-    return _lib
+        _libs[t] = L
+    return _libs[t]
 
 
 def dims(shape):
@@ -111,37 +127,39 @@ def _ptr(a):
 
 
 def set_num_threads(n):
-    lib().og_set_num_threads(int(n))
+    for t in _PREC:
+        lib(t).og_set_num_threads(int(n))
 
 
 def advect_semi_lagrange(flags, vel, grid, kind, order=1, strength=1.0, orderSpace=1, clampMode=2,
                          orderTrace=1, dt=1.0):
-    st = lib().og_advect_semi_lagrange(dims(flags.shape), flags, vel, kind, grid, order, strength, orderSpace,
+    st = lib(vel.dtype).og_advect_semi_lagrange(dims(flags.shape), flags, vel, kind, grid, order, strength, orderSpace,
                                        clampMode, orderTrace, dt)
     if st != 0:
         raise RuntimeError("AdvectSemiLagrange: Only order 1 (regular SL) and 2 (MacCormack) supported")
 
 
 def set_wall_bcs(flags, vel, obvel=None):
-    lib().og_set_wall_bcs(dims(flags.shape), flags, vel, _ptr(obvel))
+    lib(vel.dtype).og_set_wall_bcs(dims(flags.shape), flags, vel, _ptr(obvel))
 
 
 def add_buoyancy(flags, density, vel, gravity, coefficient=1.0, scale=True, dt=1.0):
-    lib().og_add_buoyancy(dims(flags.shape), flags, density, vel, *map(float, gravity), coefficient, int(scale), dt)
+    lib(vel.dtype).og_add_buoyancy(dims(flags.shape), flags, density, vel, *map(float, gravity), coefficient, int(scale), dt)
 
 
 def add_gravity(flags, vel, gravity, exclude=None, scale=True, dt=1.0):
-    lib().og_add_gravity(dims(flags.shape), flags, vel, *map(float, gravity), _ptr(exclude), int(scale), dt)
+    lib(vel.dtype).og_add_gravity(dims(flags.shape), flags, vel, *map(float, gravity), _ptr(exclude), int(scale), dt)
 
 
 def extrapolate_mac_simple(flags, vel, distance=4, intoObs=False):
-    lib().og_extrapolate_mac_simple(dims(flags.shape), flags, vel, distance, int(intoObs))
+    lib(vel.dtype).og_extrapolate_mac_simple(dims(flags.shape), flags, vel, distance, int(intoObs))
 
 
 def params(cgAccuracy=1e-3, gfClamp=1e-4, cgMaxIterFac=1.5, preconditioner=PC_MIC, enforceCompatibility=False,
-           useL2Norm=False, zeroPressureFixing=False, surfTens=0.0):
-    return PressureParams(cgAccuracy, gfClamp, cgMaxIterFac, preconditioner, int(enforceCompatibility),
-                          int(useL2Norm), int(zeroPressureFixing), surfTens)
+           useL2Norm=False, zeroPressureFixing=False, surfTens=0.0, dtype=np.float32):
+    PP = _STRUCTS[_prec(dtype)][0]
+    return PP(cgAccuracy, gfClamp, cgMaxIterFac, preconditioner, int(enforceCompatibility),
+              int(useL2Norm), int(zeroPressureFixing), surfTens)
 
 
 class MGCache:
@@ -149,10 +167,11 @@ class MGCache:
 
     def __init__(self):
         self.ptr = C.c_void_p(None)
+        self.dtype = np.float32
 
     def release(self):
         if self.ptr.value:
-            lib().og_mg_destroy(self.ptr)
+            lib(self.dtype).og_mg_destroy(self.ptr)
             self.ptr = C.c_void_p(None)
 
     def __del__(self):
@@ -163,17 +182,21 @@ class MGCache:
 
 
 def compute_pressure_rhs(rhs, vel, flags, phi=None, perCellCorr=None, curv=None, **kw):
-    p = params(**kw)
-    lib().og_compute_pressure_rhs(dims(flags.shape), rhs, vel, flags, _ptr(phi), _ptr(perCellCorr), _ptr(curv),
+    p = params(dtype=vel.dtype, **kw)
+    lib(vel.dtype).og_compute_pressure_rhs(dims(flags.shape), rhs, vel, flags, _ptr(phi), _ptr(perCellCorr), _ptr(curv),
                                   C.byref(p))
 
 
 def solve_pressure(flags, vel, pressure, phi=None, perCellCorr=None, curv=None, mg_cache=None, retRhs=None, **kw):
     """solvePressure; returns (iterations, resNorm, fixPidx)."""
-    p = params(**kw)
-    res = PressureResult()
+    t = _prec(vel.dtype)
+    p = params(dtype=t, **kw)
+    res = _STRUCTS[t][1]()
     cache = mg_cache if mg_cache is not None else MGCache()
-    st = lib().og_solve_pressure(dims(flags.shape), vel, pressure, flags, _ptr(phi), _ptr(perCellCorr), _ptr(curv),
+    if cache.ptr.value and cache.dtype is not t:
+        raise ValueError("a multigrid cache serves one precision")
+    cache.dtype = t
+    st = lib(t).og_solve_pressure(dims(flags.shape), vel, pressure, flags, _ptr(phi), _ptr(perCellCorr), _ptr(curv),
                                  C.byref(p), C.byref(cache.ptr), C.byref(res), _ptr(retRhs))
     if st == -4:
         raise RuntimeError("GridCg::iterate: The CG solver diverged, residual norm > 1e30, stopping.")
@@ -184,28 +207,28 @@ def solve_pressure(flags, vel, pressure, phi=None, perCellCorr=None, curv=None, 
     return res.iterations, res.resNorm, res.fixPidx
 
 
-def make_laplace_matrix(flags):
-    A = [np.zeros(flags.shape, np.float32) for _ in range(4)]
-    lib().og_make_laplace_matrix(dims(flags.shape), flags, *A)
+def make_laplace_matrix(flags, dtype=np.float32):
+    A = [np.zeros(flags.shape, dtype) for _ in range(4)]
+    lib(dtype).og_make_laplace_matrix(dims(flags.shape), flags, *A)
     return A
 
 
 def apply_ghost_fluid_diagonal(A0, flags, phi, gfClamp=1e-4):
-    lib().og_apply_ghost_fluid_diagonal(dims(flags.shape), A0, flags, phi, gfClamp)
+    lib(A0.dtype).og_apply_ghost_fluid_diagonal(dims(flags.shape), A0, flags, phi, gfClamp)
 
 
 def mic_init(flags, A0, Ai, Aj, Ak):
-    P = np.zeros(flags.shape, np.float32)
-    lib().og_mic_init(dims(flags.shape), flags, P, A0, Ai, Aj, Ak)
+    P = np.zeros(flags.shape, A0.dtype)
+    lib(A0.dtype).og_mic_init(dims(flags.shape), flags, P, A0, Ai, Aj, Ak)
     return P
 
 
 def mic_apply(dst, src, flags, P, Ai, Aj, Ak):
-    lib().og_mic_apply(dims(flags.shape), dst, src, flags, P, Ai, Aj, Ak)
+    lib(dst.dtype).og_mic_apply(dims(flags.shape), dst, src, flags, P, Ai, Aj, Ak)
 
 
 def apply_matrix(flags, dst, src, A0, Ai, Aj, Ak):
-    lib().og_apply_matrix(dims(flags.shape), flags, dst, src, A0, Ai, Aj, Ak)
+    lib(dst.dtype).og_apply_matrix(dims(flags.shape), flags, dst, src, A0, Ai, Aj, Ak)
 
 
 def init_domain(flags, boundaryWidth=0, wall="xXyYzZ", open="      ", inflow="      ", outflow="      "):
@@ -222,25 +245,25 @@ def set_open_bound(flags, bWidth, openBound="", type=OUTFLOW | EMPTY):
 
 
 def update_from_levelset(flags, phi):
-    lib().og_update_from_levelset(dims(flags.shape), flags, phi)
+    lib(phi.dtype).og_update_from_levelset(dims(flags.shape), flags, phi)
 
 
 def box_sdf(phi, p0, p1):
-    lib().og_box_sdf(dims(phi.shape), phi, *map(float, p0), *map(float, p1))
+    lib(phi.dtype).og_box_sdf(dims(phi.shape), phi, *map(float, p0), *map(float, p1))
 
 
 def cylinder_apply(grid, center, radius, z, value, respectFlags=None):
-    lib().og_cylinder_apply(dims(grid.shape), grid, *map(float, center), float(radius), *map(float, z), float(value),
+    lib(grid.dtype).og_cylinder_apply(dims(grid.shape), grid, *map(float, center), float(radius), *map(float, z), float(value),
                             _ptr(respectFlags))
 
 
 def box_apply(grid, p0, p1, value, respectFlags=None):
-    lib().og_box_apply(dims(grid.shape), grid, *map(float, p0), *map(float, p1), float(value), _ptr(respectFlags))
+    lib(grid.dtype).og_box_apply(dims(grid.shape), grid, *map(float, p0), *map(float, p1), float(value), _ptr(respectFlags))
 
 
 def join_real(a, b, keepMax=True):
-    lib().og_join_real(a.size, a, b, int(keepMax))
+    lib(a.dtype).og_join_real(a.size, a, b, int(keepMax))
 
 
 def get_max_abs(a):
-    return lib().og_get_max_abs(a.size, a)
+    return lib(a.dtype).og_get_max_abs(a.size, a)
