@@ -173,6 +173,26 @@ int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressure, mg_grid
 /* correctVelocity (:455-476) */
 int mg_correct_velocity(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p, mg_grid phi,
                         mg_grid perCellCorr, mg_grid fractions, mg_grid curv);
+/* Precision form of solvePressure (no counterpart in the reference; its
+ * FP64 build, -DDOUBLEPRECISION=ON, is what it reproduces).  The stencils
+ * and the inner PCG run in FP32; the pressure is accumulated in double and
+ * after every inner solve the residual max|b - A p| is recomputed in double:
+ * FP32 PCG solves of A delta = r repeat until it is below refineAccuracy,
+ * each inner solve to cgAccuracy = innerAccuracy * max|r| (the first one at
+ * the caller's cgAccuracy).  maxRefine bounds the inner solves. */
+typedef struct {
+  double refineAccuracy;     /* 1e-5 */
+  double innerAccuracy;      /* 1e-2 */
+  int maxRefine;             /* 10 */
+} mg_refine_params;
+typedef struct {
+  int refinements;           /* inner solves */
+  int iterations;            /* CG iterations over all inner solves */
+  double resNorm;            /* final max|b - A p| in double */
+} mg_refine_result;
+void mg_refine_params_default(mg_refine_params* r);
+int mg_solve_pressure_refined(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p, mg_grid phi,
+                              const mg_refine_params* rp, mg_refine_result* out);
 /* releaseMG (:252-266); s == NULL releases every solver's hierarchy */
 int mg_release_mg(mg_solver s);
 /* One multigrid V-cycle dst = M^-1 src for the Poisson matrix of flags (with

@@ -24,6 +24,14 @@ class PressureResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("resNorm", C.c_float)]
 
 
+class RefineParams(C.Structure):
+    _fields_ = [("refineAccuracy", C.c_double), ("innerAccuracy", C.c_double), ("maxRefine", C.c_int)]
+
+
+class RefineResult(C.Structure):
+    _fields_ = [("refinements", C.c_int), ("iterations", C.c_int), ("resNorm", C.c_double)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _P = C.c_void_p
 _I = C.c_int
@@ -65,6 +73,9 @@ SIGNATURES = [
     ("mg_pressure_params_default", None, [C.POINTER(PressureParams)]),
     ("mg_solve_pressure", _I, [_P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P, _P, _P,
                                C.POINTER(PressureResult)]),
+    ("mg_refine_params_default", None, [C.POINTER(RefineParams)]),
+    ("mg_solve_pressure_refined", _I, [_P, _P, _P, C.POINTER(PressureParams), _P, C.POINTER(RefineParams),
+                                       C.POINTER(RefineResult)]),
     ("mg_compute_pressure_rhs", _I, [_P, _P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P, _P]),
     ("mg_solve_pressure_system", _I, [_P, _P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P,
                                       C.POINTER(PressureResult)]),

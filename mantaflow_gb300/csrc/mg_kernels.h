@@ -150,6 +150,14 @@ void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* 
 // sum of nparts per-block dot partials -> beta/sigma (init: sigma only)
 void launch_mic_finish(const PcgBuffers& b, int nparts, bool init, cudaStream_t s);
 
+// precision form (refine.cu): FP64 residual refinement around the FP32 PCG
+void launch_to_double(long long n, const float* a, double* b, cudaStream_t s);
+void launch_to_float(long long n, const double* a, float* b, cudaStream_t s);
+void launch_add_delta(long long n, double* p, const float* d, cudaStream_t s);
+// r = b - A p (double), rf = (float) r, *norm = max|r|; counter starts at 0
+void launch_residual64(const Dims& d, const code_t* code, const float* A0f, const double* b, const double* p, float* rf,
+                       double* part, unsigned int* counter, double* norm, cudaStream_t s);
+
 void launch_correct_velocity(const Dims& d, const int* flags, Mac vel, const float* p, const float* phi, const float* curv,
                              float gfClamp, float surfTens, cudaStream_t s);
 void mic_plan_order(int tx, int ty, int tz, int* order);

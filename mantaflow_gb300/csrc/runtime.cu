@@ -1243,6 +1243,97 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   return MG_OK;
 }
 
+extern "C" void mg_refine_params_default(mg_refine_params* r) {
+  if (!r) return;
+  r->refineAccuracy = 1e-5;
+  r->innerAccuracy = 1e-2;
+  r->maxRefine = 10;
+}
+
+// solvePressure with FP64 residual refinement: MakeRhs, then FP32 PCG solves
+// of A delta = (float) r accumulated into a double pressure until the
+// double-precision residual max|b - A p| drops below refineAccuracy, then
+// correctVelocity with the rounded pressure
+extern "C" int mg_solve_pressure_refined(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p,
+                                         mg_grid phi, const mg_refine_params* rp, mg_refine_result* out) {
+  NEED_GRID(vel, "solvePressureRefined");
+  NEED_GRID(pressure, "solvePressureRefined");
+  NEED_GRID(flags, "solvePressureRefined");
+  mg_pressure_params def;
+  if (!p) {
+    mg_pressure_params_default(&def);
+    p = &def;
+  }
+  mg_refine_params rdef;
+  if (!rp) {
+    mg_refine_params_default(&rdef);
+    rp = &rdef;
+  }
+  if (!(rp->refineAccuracy > 0.) || !(rp->innerAccuracy > 0.) || rp->maxRefine < 1)
+    return fail(MG_ERR_ARG, "solvePressureRefined: refineAccuracy and innerAccuracy must be > 0, maxRefine >= 1");
+  if (p->enforceCompatibility) return fail(MG_ERR_UNSUPPORTED, "solvePressureRefined: enforceCompatibility is not supported");
+  mg_solver s = flags->s;
+  const size_t n = (size_t)s->d.n;
+  Tmp rhs(s, sizeof(float) * n), delta(s, sizeof(float) * n), b64(s, sizeof(double) * n), p64(s, sizeof(double) * n),
+      norm(s, sizeof(double));
+  if (!rhs.p || !delta.p || !b64.p || !p64.p || !norm.p) return fail(MG_ERR_NOMEM, "solvePressureRefined: out of device memory");
+  mg_grid_s rg, dg;
+  rg.s = dg.s = s;
+  rg.kind = dg.kind = MG_REAL;
+  rg.data = rhs.p;
+  dg.data = delta.p;
+  s->grids.insert(&rg);
+  s->grids.insert(&dg);
+  struct Unreg {
+    mg_solver s;
+    mg_grid a, b;
+    ~Unreg() {
+      s->grids.erase(a);
+      s->grids.erase(b);
+    }
+  } unreg{s, &rg, &dg};
+  int st = mg_compute_pressure_rhs(&rg, vel, pressure, flags, p, phi, nullptr, nullptr, nullptr, nullptr);
+  if (st) return st;
+  CK(cudaMemsetAsync(p64.p, 0, sizeof(double) * n, s->stream));
+  double* const P64 = (double*)p64.p;
+  double* const B64 = (double*)b64.p;
+  mg_pressure_params pin = *p;
+  double rnorm = 0.;
+  int total = 0, k = 0;
+  for (; k < rp->maxRefine; k++) {
+    // inner FP32 solve of A delta = r (the first one is the plain solve; it
+    // also applies the pressure pinning to rhs, which the double right-hand
+    // side then takes over)
+    if (k > 0) pin.cgAccuracy = (float)(rp->innerAccuracy * rnorm);
+    if (k > 0 && pin.cgAccuracy < 1e-30f) break;
+    mg_pressure_result r{};
+    st = mg_solve_pressure_system(&rg, vel, &dg, flags, &pin, phi, nullptr, nullptr, nullptr, &r);
+    if (st) return st;
+    total += r.iterations;
+    if (k == 0) launch_to_double((long long)n, rhs.f(), B64, s->stream);
+    launch_add_delta((long long)n, P64, delta.f(), s->stream);
+    launch_residual64(s->d, s->code, phi ? s->A0f : nullptr, B64, P64, rhs.f(), s->part, &s->sc->counters[5],
+                      (double*)norm.p, s->stream);
+    CKL();
+    CK(cudaMemcpyAsync(&rnorm, norm.p, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (rnorm < rp->refineAccuracy) {
+      k++;
+      break;
+    }
+  }
+  launch_to_float((long long)n, P64, pressure->f(), s->stream);
+  CKL();
+  st = mg_correct_velocity(vel, pressure, flags, p, phi, nullptr, nullptr, nullptr);
+  if (st) return st;
+  if (out) {
+    out->refinements = k;
+    out->iterations = total;
+    out->resNorm = rnorm;
+  }
+  return MG_OK;
+}
+
 extern "C" int mg_correct_velocity(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p,
                                    mg_grid phi, mg_grid perCellCorr, mg_grid fractions, mg_grid curv) {
   NEED_GRID(vel, "correctVelocity");

@@ -460,6 +460,25 @@ def solvePressure(vel, pressure, flags, cgAccuracy=1e-3, phi=None, perCellCorr=N
     _last_cg["resNorm"] = res.resNorm
 
 
+def solvePressureRefined(vel, pressure, flags, cgAccuracy=1e-3, refineAccuracy=1e-5, innerAccuracy=1e-2,
+                         maxRefine=10, phi=None, gfClamp=1e-04, cgMaxIterFac=1.5, preconditioner=PcMIC,
+                         useL2Norm=False, zeroPressureFixing=False):
+    """Precision form of solvePressure: FP32 PCG inner solves with the
+    pressure accumulated in double and the residual recomputed in double
+    after each, until max|b - A p| < refineAccuracy.  The first inner solve
+    runs at cgAccuracy, later ones at innerAccuracy * max|r|.  Returns
+    (inner solves, total CG iterations, final double residual)."""
+    from ._lib import RefineParams, RefineResult
+    p = _params(cgAccuracy, gfClamp, cgMaxIterFac, True, preconditioner, False, useL2Norm, zeroPressureFixing, 0.)
+    rp = RefineParams(float(refineAccuracy), float(innerAccuracy), int(maxRefine))
+    res = RefineResult()
+    check(_lib.load().mg_solve_pressure_refined(vel._h, pressure._h, flags._h, C.byref(p), _h(phi), C.byref(rp),
+                                                C.byref(res)))
+    _last_cg["iterations"] = res.iterations
+    _last_cg["resNorm"] = res.resNorm
+    return res.refinements, res.iterations, res.resNorm
+
+
 def lastSolveStats():
     """(iterations, residual norm) of the last pressure solve of this process."""
     return _last_cg["iterations"], _last_cg["resNorm"]
