@@ -149,6 +149,8 @@ class Plume:
         self.mask = mask.numpy()
         self.rng = np.random.default_rng(seed)
         self.iters = []
+        self.refined = False
+        self.refine_stats = []
 
     def noise(self):
         n = self.n
@@ -161,8 +163,13 @@ class Plume:
         m.advectSemiLagrange(flags=self.flags, vel=self.vel, grid=self.vel, order=2, clampMode=2)
         m.setWallBcs(flags=self.flags, vel=self.vel)
         m.addBuoyancy(density=self.density, vel=self.vel, gravity=m.vec3(0, -4e-3, 0), flags=self.flags)
-        m.solvePressure(flags=self.flags, vel=self.vel, pressure=self.pressure, cgAccuracy=1e-3,
-                        preconditioner=self.pc)
+        if self.refined:
+            self.refine_stats.append(m.solvePressureRefined(flags=self.flags, vel=self.vel, pressure=self.pressure,
+                                                            cgAccuracy=1e-3, refineAccuracy=1e-5,
+                                                            preconditioner=self.pc)[:2])
+        else:
+            m.solvePressure(flags=self.flags, vel=self.vel, pressure=self.pressure, cgAccuracy=1e-3,
+                            preconditioner=self.pc)
         self.iters.append(m.lastSolveStats()[0])
 
 
@@ -209,6 +216,73 @@ def cpu_plume_steps(n, steps, warm, threads, seed, state=None, pc=1):
             iters.append(it)
     og.set_num_threads(1)
     return times, iters
+
+
+def precision_form(m, n, steps, seed):
+    """Config-2 precision form on a bounded sample: the plume for `steps`
+    steps at n^3 through the plain FP32 path (cgAccuracy 1e-3, PcMIC and
+    PcMGStatic) and through the FP64-refined solve (target 1e-5), each
+    against the FP64 oracle (the reference's double build restated, PcMIC
+    at cgAccuracy 1e-5).  Per field: max-abs error and relative L2 error."""
+    from oracle import oracle as og
+    og.set_num_threads(os.cpu_count() or 1)
+    f = np.zeros((n, n, n), np.int32)
+    og.init_domain(f, 0)
+    og.fill_grid(f)
+    og.set_open_bound(f, 0, "Y")
+    mask = np.zeros((n, n, n), np.float32)
+    gs = np.float32([n, n, n])
+    og.cylinder_apply(mask, gs * np.float32([0.5, 0.1, 0.5]), np.float32(n * 0.14), gs * np.float32([0, 0.02, 0]), 1.0)
+    rng = np.random.default_rng(seed)
+    noise = [(rng.random(f.shape, dtype=np.float32) * mask).astype(np.float32) for _ in range(steps)]
+
+    def divergence(vel):
+        rhs = np.zeros(f.shape, np.float64)
+        og.compute_pressure_rhs(rhs, vel.astype(np.float64), f)
+        return rhs
+
+    d64 = np.zeros(f.shape, np.float64)
+    v64 = np.zeros(f.shape + (3,), np.float64)
+    p64 = np.zeros(f.shape, np.float64)
+    for t in range(steps):
+        og.join_real(d64, noise[t].astype(np.float64))
+        og.advect_semi_lagrange(f, v64, d64, og.KIND_REAL, order=2, clampMode=2)
+        og.advect_semi_lagrange(f, v64, v64, og.KIND_MAC, order=2, clampMode=2)
+        og.set_wall_bcs(f, v64)
+        og.add_buoyancy(f, d64, v64, (0, -4e-3, 0))
+        og.solve_pressure(f, v64, p64, cgAccuracy=1e-5, preconditioner=og.PC_MIC)
+    div64 = divergence(v64)
+    og.set_num_threads(1)
+
+    def err(a, b):
+        a = np.asarray(a, np.float64)
+        return {"max_abs": float(np.max(np.abs(a - b))),
+                "rel_l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))}
+
+    out = {"workload": "3D smoke plume %d^3, %d steps, MacCormack + walls + buoyancy + pressure" % (n, steps),
+           "fp64_oracle": "oracle restatement compiled as the reference's double build, PcMIC, cgAccuracy 1e-5"}
+    for name, pc, refined in (("fp32_pcmic_acc1e-3", m.PcMIC, False), ("fp32_pcmgstatic_acc1e-3", m.PcMGStatic, False),
+                              ("fp32_refined_fp64_to_1e-5", m.PcMGStatic, True)):
+        s = m.Solver(name="prec", gridSize=m.vec3(n, n, n), dim=3)
+        flags = s.create(m.FlagGrid)
+        m.copyArrayToGridReal(f, flags)
+        vel, dens, pres, src = s.create(m.MACGrid), s.create(m.RealGrid), s.create(m.RealGrid), s.create(m.RealGrid)
+        for t in range(steps):
+            m.copyArrayToGridReal(noise[t], src)
+            dens.join(src)
+            m.advectSemiLagrange(flags=flags, vel=vel, grid=dens, order=2, clampMode=2)
+            m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=2, clampMode=2)
+            m.setWallBcs(flags=flags, vel=vel)
+            m.addBuoyancy(density=dens, vel=vel, gravity=m.vec3(0, -4e-3, 0), flags=flags)
+            if refined:
+                m.solvePressureRefined(flags=flags, vel=vel, pressure=pres, refineAccuracy=1e-5, preconditioner=pc)
+            else:
+                m.solvePressure(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, preconditioner=pc)
+        v = vel.numpy()
+        out[name] = {"density": err(dens.numpy(), d64), "velocity": err(v, v64), "pressure": err(pres.numpy(), p64),
+                     "divergence": err(divergence(v), div64)}
+        del s
+    return out
 
 
 def dist_setup():
@@ -271,6 +345,10 @@ def main():
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--cpu-steps", type=int, default=1, help="timed oracle steps for cpu_baseline (0: skip)")
     ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--precision-size", type=int, default=64, help="grid side of the precision-form sample (0: skip)")
+    ap.add_argument("--precision-steps", type=int, default=10)
+    ap.add_argument("--refined-steps", type=int, default=5,
+                    help="timed 256^3 steps of the FP64-refined form reported beside the headline (0: skip)")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
@@ -411,6 +489,36 @@ def main():
                "ms_per_step": msm.value / KM, "steps": KM, "warmup": 3, "cg_iterations": mic.iters[i0:]}
         del noise_m, ng, mic
 
+    # ---- precision form: the refined solve's throughput on the headline
+    # scene, and per-field errors against the FP64 oracle on a bounded sample
+    refined = None
+    if args.refined_steps > 0 and rank == 0:
+        KR = args.refined_steps
+        rp = Plume(m, n, m.PcMGStatic, args.seed + 11, 0)
+        rp.refined = True
+        ng = rp.s.create(m.RealGrid)
+        for t in range(3):
+            m.copyArrayToGridReal(rp.noise(), ng)
+            rp.step(ng)
+        noise_r = [rp.s.create(m.RealGrid) for _ in range(KR)]
+        for g in noise_r:
+            m.copyArrayToGridReal(rp.noise(), g)
+        rp.s.sync()
+        _lib.check(L.mg_mark(rp.s._h, 0))
+        for t in range(KR):
+            rp.step(noise_r[t])
+        _lib.check(L.mg_mark(rp.s._h, 1))
+        msr = C.c_float()
+        _lib.check(L.mg_elapsed(rp.s._h, 0, 1, C.byref(msr)))
+        refined = {"workload": "3D smoke plume %d^3, MacCormack advection + FP32 multigrid-PCG inner solves with "
+                               "FP64 residual refinement to max|b - Ap| < 1e-5" % n,
+                   "value": n ** 3 * KR / (msr.value / 1e3), "unit": "cells/s", "ms_per_step": msr.value / KR,
+                   "steps": KR, "warmup": 3, "refine_stats": rp.refine_stats[-KR:]}
+        del noise_r, ng, rp
+    precision = None
+    if args.precision_size > 0 and rank == 0 and world == 1:
+        precision = precision_form(m, args.precision_size, args.precision_steps, args.seed + 5)
+
     # ---- CPU baseline on a bounded sample (rank 0, one GPU)
     cpu = None
     if rank == 0 and world == 1 and args.cpu_steps > 0:
@@ -437,7 +545,7 @@ def main():
                "gpu_launches": int(cnt1.value - cnt0.value),
                "clocks": clk, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])},
-               "same_scene_pc_mic": alt}
+               "same_scene_pc_mic": alt, "precision_form": {"refined_256": refined, "errors_vs_fp64": precision}}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()

@@ -221,6 +221,45 @@ int mg_shape_cylinder_apply(mg_grid grid, const float* center, float radius, con
 /* Box::computeLevelset (BoxSDF, shapes.cpp:178-232) into a Real/Levelset grid */
 int mg_shape_box_levelset(mg_grid phi, const float* p0, const float* p1);
 
+/* ---- batched form (no counterpart in the reference) ---------------------- */
+/* Many independent plume scenes (the reference's smoke plume: walls, open
+ * top, cylinder source with seeded uniform inflow noise, buoyancy, MacCormack
+ * advection, setWallBcs, addBuoyancy, solvePressure) stepped together: every
+ * stage is one launch over all scenes' tiles, and the pressure solve iterates
+ * until every scene has converged, each with its own CG scalars.  The
+ * pressure solve is GridCg with PcNone -- the reference's 2D path
+ * (conjugategrad.cpp:315-321) -- for 2D and 3D scenes alike, with the 2D
+ * iteration limit (int)(cgMaxIterFac * max size) * 4. */
+typedef struct mg_batch_s* mg_batch;
+typedef struct {
+  int sweeps;                  /* CG iterations launched (the slowest scene's count) */
+  int maxIterations;           /* largest per-scene iteration count */
+  long long totalIterations;   /* sum over scenes */
+  int diverged;                /* scenes whose residual exceeded 1e35 */
+} mg_batch_stats;
+#define MG_BATCH_DENSITY 0
+#define MG_BATCH_VELOCITY 1    /* AoS Vec3, 3 floats per cell */
+#define MG_BATCH_PRESSURE 2
+#define MG_BATCH_FLAGS 3
+#define MG_BATCH_SOURCE 4      /* the inflow cylinder mask */
+/* sizes: count*3 ints (nx, ny, nz; nz = 1 for 2D); gravity: count*3 floats
+ * (addBuoyancy's gravity, scaled by dt/dx); seeds: per-scene inflow noise */
+int mg_batch_create(int count, const int* sizes, const float* gravity, const unsigned long long* seeds, float dt,
+                    mg_batch* out);
+int mg_batch_destroy(mg_batch b);
+/* solvePressure's cgAccuracy (1e-3) and cgMaxIterFac (1.5) */
+int mg_batch_set_solver(mg_batch b, float cgAccuracy, float cgMaxIterFac);
+/* one plume step of every scene; stats may be NULL */
+int mg_batch_step(mg_batch b, mg_batch_stats* stats);
+int mg_batch_scene_iterations(mg_batch b, int scene, int* iterations, float* resNorm);
+/* a field of one scene in the reference layout; bytes must match */
+int mg_batch_download(mg_batch b, int scene, int what, void* host, size_t bytes);
+/* the uniform [0,1) inflow noise a scene with this seed uses at a step, per
+ * cell (host computation, for feeding the same inflow to a single scene) */
+int mg_batch_noise(unsigned long long seed, int step, long long cells, float* out);
+int mg_batch_info(mg_batch b, int* count, long long* cells, long long* tiles, size_t* bytes);
+int mg_batch_sync(mg_batch b);
+
 /* ---- timing (CUDA events on the solver's stream) ------------------------- */
 /* per-kernel-family device time accumulated while profiling is on */
 int mg_profile_enable(mg_solver s, int on);

@@ -24,6 +24,11 @@ class PressureResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("resNorm", C.c_float)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("sweeps", C.c_int), ("maxIterations", C.c_int), ("totalIterations", C.c_longlong),
+                ("diverged", C.c_int)]
+
+
 class RefineParams(C.Structure):
     _fields_ = [("refineAccuracy", C.c_double), ("innerAccuracy", C.c_double), ("maxRefine", C.c_int)]
 
@@ -76,6 +81,16 @@ SIGNATURES = [
     ("mg_refine_params_default", None, [C.POINTER(RefineParams)]),
     ("mg_solve_pressure_refined", _I, [_P, _P, _P, C.POINTER(PressureParams), _P, C.POINTER(RefineParams),
                                        C.POINTER(RefineResult)]),
+    ("mg_batch_create", _I, [_I, C.POINTER(_I), _FP, C.POINTER(C.c_ulonglong), _F, C.POINTER(_P)]),
+    ("mg_batch_destroy", _I, [_P]),
+    ("mg_batch_set_solver", _I, [_P, _F, _F]),
+    ("mg_batch_step", _I, [_P, C.POINTER(BatchStats)]),
+    ("mg_batch_scene_iterations", _I, [_P, _I, C.POINTER(_I), _FP]),
+    ("mg_batch_download", _I, [_P, _I, _I, _P, C.c_size_t]),
+    ("mg_batch_noise", _I, [C.c_ulonglong, _I, C.c_longlong, _FP]),
+    ("mg_batch_info", _I, [_P, C.POINTER(_I), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                           C.POINTER(C.c_size_t)]),
+    ("mg_batch_sync", _I, [_P]),
     ("mg_compute_pressure_rhs", _I, [_P, _P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P, _P]),
     ("mg_solve_pressure_system", _I, [_P, _P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P,
                                       C.POINTER(PressureResult)]),

@@ -1,0 +1,96 @@
+"""Batched form: many independent smoke-plume scenes stepped together on
+one GPU (mg_batch_* of include/mantagpu.h).
+
+Every scene is the reference's plume (walls, open top, cylinder source with
+seeded uniform inflow noise, buoyancy, MacCormack advection, setWallBcs,
+addBuoyancy, solvePressure), with its own size, gravity and noise seed.
+Each stage of a step is one launch over the tiles of all scenes; the
+pressure solve iterates until every scene has converged.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, ensure_init
+
+DENSITY, VELOCITY, PRESSURE, FLAGS, SOURCE = 0, 1, 2, 3, 4
+
+
+class BatchedPlumes:
+    def __init__(self, sizes, gravity, seeds, dt=1.0, cgAccuracy=1e-3, cgMaxIterFac=1.5):
+        ensure_init()
+        self._L = _lib.load()
+        sizes = [tuple(int(v) for v in s) + ((1,) if len(s) == 2 else ()) for s in sizes]
+        self.sizes = [s[:3] for s in sizes]
+        n = len(self.sizes)
+        sz = (C.c_int * (3 * n))(*[v for s in self.sizes for v in s])
+        gr = (C.c_float * (3 * n))(*[float(v) for g in gravity for v in g])
+        sd = (C.c_ulonglong * n)(*[int(x) for x in seeds])
+        self.seeds = [int(x) for x in seeds]
+        h = C.c_void_p()
+        check(self._L.mg_batch_create(n, sz, gr, sd, float(dt), C.byref(h)))
+        self._h = h
+        check(self._L.mg_batch_set_solver(h, float(cgAccuracy), float(cgMaxIterFac)))
+        self.steps = 0
+
+    def __len__(self):
+        return len(self.sizes)
+
+    def step(self):
+        st = _lib.BatchStats()
+        check(self._L.mg_batch_step(self._h, C.byref(st)))
+        self.steps += 1
+        return {"sweeps": st.sweeps, "max_iterations": st.maxIterations, "total_iterations": st.totalIterations}
+
+    def iterations(self, scene):
+        it = C.c_int()
+        res = C.c_float()
+        check(self._L.mg_batch_scene_iterations(self._h, int(scene), C.byref(it), C.byref(res)))
+        return it.value, res.value
+
+    def _shape(self, scene):
+        nx, ny, nz = self.sizes[scene]
+        return (nz, ny, nx)
+
+    def download(self, scene, what):
+        shape = self._shape(scene)
+        if what == VELOCITY:
+            a = np.empty(shape + (3,), np.float32)
+        elif what == FLAGS:
+            a = np.empty(shape, np.int32)
+        else:
+            a = np.empty(shape, np.float32)
+        check(self._L.mg_batch_download(self._h, int(scene), int(what), a.ctypes.data_as(C.c_void_p), a.nbytes))
+        return a
+
+    def inflow(self, scene, step):
+        """density source the batch joins into scene `scene` at `step`:
+        U[0,1) noise times the cylinder mask"""
+        shape = self._shape(scene)
+        u = np.empty(shape, np.float32)
+        check(self._L.mg_batch_noise(C.c_ulonglong(self.seeds[scene]), int(step), u.size,
+                                     u.ctypes.data_as(C.POINTER(C.c_float))))
+        return (u * self.download(scene, SOURCE)).astype(np.float32)
+
+    def info(self):
+        c = C.c_int()
+        cells = C.c_longlong()
+        tiles = C.c_longlong()
+        nbytes = C.c_size_t()
+        check(self._L.mg_batch_info(self._h, C.byref(c), C.byref(cells), C.byref(tiles), C.byref(nbytes)))
+        return {"scenes": c.value, "cells": cells.value, "tiles": tiles.value, "bytes": nbytes.value}
+
+    def sync(self):
+        check(self._L.mg_batch_sync(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.mg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

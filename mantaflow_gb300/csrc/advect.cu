@@ -9,6 +9,7 @@
 // Per cell the arithmetic is the reference's, so the result is the same.
 #include "mg_common.cuh"
 #include "mg_kernels.h"
+#include "mg_batch.h"
 
 #include <cfloat>
 
@@ -17,12 +18,8 @@ namespace mgpu {
 // ---------------------------------------------------------------- scalar SL
 // SemiLagrange (advection.cpp:25-41) for CH float planes (1: Real, 3: Vec3)
 template <int CH, int kOrderSpace, int kTrace>
-__global__ void __launch_bounds__(256) k_sl_cell(Dims d, CMac vel, const float* __restrict__ src, float* __restrict__ dst,
-                                                 float dt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= d.nx || j >= d.ny) return;
+__device__ __forceinline__ void sl_real_cell(const Dims& d, CMac vel, const float* __restrict__ src, float* __restrict__ dst,
+                                                 float dt, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   const bool inner = i >= 1 && i < d.nx - 1 && j >= 1 && j < d.ny - 1 && (!d.is3d || (k >= 1 && k < d.nz - 1));
   if (!inner) {
@@ -48,6 +45,16 @@ __global__ void __launch_bounds__(256) k_sl_cell(Dims d, CMac vel, const float* 
     const float* s = src + c * d.n;
     dst[c * d.n + idx] = kOrderSpace == 1 ? interp(d, s, px, py, pz) : interp_cubic<CH == 3>(d, s, px, py, pz);
   }
+}
+
+template <int CH, int kOrderSpace, int kTrace>
+__global__ void __launch_bounds__(256) k_sl_cell(Dims d, CMac vel, const float* __restrict__ src, float* __restrict__ dst,
+                                                 float dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  sl_real_cell<CH, kOrderSpace, kTrace>(d, vel, src, dst, dt, i, j, k);
 }
 
 // doClampComponent (advection.cpp:144-186) over CH planes.  Returns true
@@ -114,13 +121,9 @@ __device__ __forceinline__ void clamp_component(const Dims& d, const int* __rest
 // bwd = SL(fwd, -dt), MacCormackCorrect (advection.cpp:81-91) and
 // MacCormackClamp (:241-267) in one sweep.  newGrid -> dst.
 template <int CH, int kOrderSpace, int kTrace>
-__global__ void __launch_bounds__(256) k_maccormack_cell(Dims d, const int* __restrict__ flags, CMac vel,
+__device__ __forceinline__ void maccormack_real_cell(const Dims& d, const int* __restrict__ flags, CMac vel,
                                                          const float* __restrict__ orig, const float* __restrict__ fwd,
-                                                         float* __restrict__ dst, float dt, float strength, int clampMode) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= d.nx || j >= d.ny) return;
+                                                         float* __restrict__ dst, float dt, float strength, int clampMode, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   const bool fluid = isF(flags, idx);
   const float hs = strength * 0.5f;  // exact
@@ -183,6 +186,17 @@ __global__ void __launch_bounds__(256) k_maccormack_cell(Dims d, const int* __re
   for (int c = 0; c < CH; c++) dst[c * d.n + idx] = dv[c];
 }
 
+template <int CH, int kOrderSpace, int kTrace>
+__global__ void __launch_bounds__(256) k_maccormack_cell(Dims d, const int* __restrict__ flags, CMac vel,
+                                                         const float* __restrict__ orig, const float* __restrict__ fwd,
+                                                         float* __restrict__ dst, float dt, float strength, int clampMode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  maccormack_real_cell<CH, kOrderSpace, kTrace>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode, i, j, k);
+}
+
 // ------------------------------------------------------------------- MAC SL
 // SemiLagrangeMAC (advection.cpp:44-77), src sampled per component.
 template <int kTrace>
@@ -211,11 +225,7 @@ __device__ __forceinline__ void sl_mac_cell(const Dims& d, CMac vel, CMac src, i
 }
 
 template <int kTrace>
-__global__ void __launch_bounds__(256) k_sl_mac(Dims d, CMac vel, CMac src, Mac dst, float dt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= d.nx || j >= d.ny) return;
+__device__ __forceinline__ void sl_mac_grid_cell(const Dims& d, CMac vel, CMac src, Mac dst, float dt, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   const bool inner = i >= 1 && i < d.nx - 1 && j >= 1 && j < d.ny - 1 && (!d.is3d || (k >= 1 && k < d.nz - 1));
   float out[3] = {0.f, 0.f, 0.f};
@@ -223,6 +233,15 @@ __global__ void __launch_bounds__(256) k_sl_mac(Dims d, CMac vel, CMac src, Mac 
   dst.u[idx] = out[0];
   dst.v[idx] = out[1];
   dst.w[idx] = out[2];
+}
+
+template <int kTrace>
+__global__ void __launch_bounds__(256) k_sl_mac(Dims d, CMac vel, CMac src, Mac dst, float dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  sl_mac_grid_cell<kTrace>(d, vel, src, dst, dt, i, j, k);
 }
 
 // doClampComponentMAC (advection.cpp:191-235)
@@ -266,12 +285,8 @@ __device__ __forceinline__ float clamp_component_mac(const Dims& d, const int* _
 // bwd = SLMAC(fwd, -dt) on the fly, MacCormackCorrectMAC (advection.cpp:94-115),
 // MacCormackClampMAC (:270-287).  orig is the grid being advected.
 template <int kTrace>
-__global__ void __launch_bounds__(256) k_maccormack_mac(Dims d, const int* __restrict__ flags, CMac vel, CMac orig,
-                                                        CMac fwd, Mac dst, float dt, float strength, int clampMode) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= d.nx || j >= d.ny) return;
+__device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __restrict__ flags, CMac vel, CMac orig,
+                                                        CMac fwd, Mac dst, float dt, float strength, int clampMode, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   bool skip[3];
   const bool fl = isF(flags, idx);
@@ -304,13 +319,19 @@ __global__ void __launch_bounds__(256) k_maccormack_mac(Dims d, const int* __res
   dst.w[idx] = val[2];
 }
 
-// extrapolateVelConvectiveBC (advection.cpp:346-381): velDst for outflow
-// cells, from vel (the advected field) and velPrev (the field before).
-__global__ void k_outflow_bc(Dims d, const int* __restrict__ flags, CMac vel, CMac velPrev, Mac velDst, float timeStep) {
+template <int kTrace>
+__global__ void __launch_bounds__(256) k_maccormack_mac(Dims d, const int* __restrict__ flags, CMac vel, CMac orig,
+                                                        CMac fwd, Mac dst, float dt, float strength, int clampMode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= d.nx || j >= d.ny) return;
+  maccormack_mac_cell<kTrace>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode, i, j, k);
+}
+
+// extrapolateVelConvectiveBC (advection.cpp:346-381): velDst for outflow
+// cells, from vel (the advected field) and velPrev (the field before).
+__device__ __forceinline__ void outflow_bc_cell(const Dims& d, const int* __restrict__ flags, CMac vel, CMac velPrev, Mac velDst, float timeStep, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   if (!isOut(flags, idx)) return;
   float ax = 0.f, ay = 0.f, az = 0.f;
@@ -380,12 +401,16 @@ __global__ void k_outflow_bc(Dims d, const int* __restrict__ flags, CMac vel, CM
   velDst.w[idx] = dz;
 }
 
-// copyChangedVels (advection.cpp:384)
-__global__ void k_copy_outflow(Dims d, const int* __restrict__ flags, CMac src, Mac dst) {
+__global__ void k_outflow_bc(Dims d, const int* __restrict__ flags, CMac vel, CMac velPrev, Mac velDst, float timeStep) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= d.nx || j >= d.ny) return;
+  outflow_bc_cell(d, flags, vel, velPrev, velDst, timeStep, i, j, k);
+}
+
+// copyChangedVels (advection.cpp:384)
+__device__ __forceinline__ void copy_outflow_cell(const Dims& d, const int* __restrict__ flags, CMac src, Mac dst, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   if (!isOut(flags, idx)) return;
   dst.u[idx] = src.u[idx];
@@ -393,11 +418,71 @@ __global__ void k_copy_outflow(Dims d, const int* __restrict__ flags, CMac src, 
   dst.w[idx] = src.w[idx];
 }
 
+__global__ void k_copy_outflow(Dims d, const int* __restrict__ flags, CMac src, Mac dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  copy_outflow_cell(d, flags, src, dst, i, j, k);
+}
+
 // knResetPhiInObs (advection.cpp:394-399)
 __global__ void k_reset_phi_in_obs(Dims d, const int* __restrict__ flags, float* sdf) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= d.n) return;
   if (isO(flags, idx) && sdf[idx] < 0.f) sdf[idx] = 0.1f;
+}
+
+// ----------------------------------------------------------------- batched
+// The plume's advection for every scene of a batch (advectSemiLagrange
+// order 2, clampMode 2, of density and then of velocity, both with the
+// velocity at the start of the step): the same cell bodies as above.
+#define BATCH_CELL                                                       \
+  const BTile tl = tiles[blockIdx.x];                                    \
+  const BScene& sc = S[tl.scene];                                        \
+  const Dims d = sc.d;                                                   \
+  const int i = tl.x0 + threadIdx.x, j = tl.y0 + threadIdx.y, k = tl.z; \
+  if (i >= d.nx || j >= d.ny) return;
+
+// forward SL of density (into sc.fwd plane 3) and velocity (sc.fwd planes 0-2)
+__global__ void __launch_bounds__(256) k_b_advect_fwd(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
+  BATCH_CELL
+  const CMac v = bcmac(sc.vel[cur], d.n);
+  sl_real_cell<1, 1, 1>(d, v, sc.dens[cur], sc.fwd + 3 * d.n, sc.dt, i, j, k);
+  sl_mac_grid_cell<1>(d, v, v, bmac(sc.fwd, d.n), sc.dt, i, j, k);
+}
+// MacCormack correction and clamp of both into the next buffers
+__global__ void __launch_bounds__(256) k_b_advect_mc(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
+  BATCH_CELL
+  const CMac v = bcmac(sc.vel[cur], d.n);
+  maccormack_real_cell<1, 1, 1>(d, sc.flags, v, sc.dens[cur], sc.fwd + 3 * d.n, sc.dens[1 - cur], sc.dt, 1.f, 2, i, j, k);
+  maccormack_mac_cell<1>(d, sc.flags, v, v, bcmac(sc.fwd, d.n), bmac(sc.vel[1 - cur], d.n), sc.dt, 1.f, 2, i, j, k);
+}
+// applyOutflowBC (advection.cpp:387-391): convective values into the scratch
+__global__ void __launch_bounds__(256) k_b_outflow(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
+  BATCH_CELL
+  const float ts = fmaxf(1.f, sc.dt * 4.f);
+  outflow_bc_cell(d, sc.flags, bcmac(sc.vel[1 - cur], d.n), bcmac(sc.vel[cur], d.n), bmac(sc.fwd, d.n), ts, i, j, k);
+}
+__global__ void __launch_bounds__(256) k_b_outflow_copy(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
+  BATCH_CELL
+  copy_outflow_cell(d, sc.flags, bcmac(sc.fwd, d.n), bmac(sc.vel[1 - cur], d.n), i, j, k);
+}
+#undef BATCH_CELL
+
+void launch_b_advect_density(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st) {
+  (void)t; (void)nt; (void)s; (void)cur; (void)st;  // density and velocity advect together (launch_b_advect_velocity)
+}
+void launch_b_advect_velocity(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st) {
+  const dim3 b(kBTX, kBTY, 1);
+  count_launch();
+  k_b_advect_fwd<<<nt, b, 0, st>>>(t, s, cur);
+  count_launch();
+  k_b_advect_mc<<<nt, b, 0, st>>>(t, s, cur);
+  count_launch();
+  k_b_outflow<<<nt, b, 0, st>>>(t, s, cur);
+  count_launch();
+  k_b_outflow_copy<<<nt, b, 0, st>>>(t, s, cur);
 }
 
 // ------------------------------------------------------------- launchers

@@ -2,6 +2,7 @@
 // grid utilities (plugin/extforces.cpp, fastmarch.cpp, grid.cpp, shapes.cpp).
 #include "mg_common.cuh"
 #include "mg_kernels.h"
+#include "mg_batch.h"
 
 #include <cfloat>
 
@@ -19,8 +20,8 @@ static const dim3 kBlk(32, 8, 1);
 #define INNER (i >= 1 && i < d.nx - 1 && j >= 1 && j < d.ny - 1 && (!d.is3d || (k >= 1 && k < d.nz - 1)))
 
 // KnSetWallBcs (extforces.cpp:186-217): every cell, i>0 style checks
-__global__ void k_set_wall_bcs(Dims d, const int* __restrict__ flags, Mac vel, CMac obvel, int hasObvel) {
-  CELL_IJK
+__device__ __forceinline__ void set_wall_bcs_cell(const Dims& d, const int* __restrict__ flags, Mac vel, CMac obvel, int hasObvel, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   const int f = __ldg(flags + idx);
   const bool curFluid = f & kFluid, curObs = f & kObstacle;
   if (!curFluid && !curObs) return;
@@ -52,17 +53,34 @@ __global__ void k_set_wall_bcs(Dims d, const int* __restrict__ flags, Mac vel, C
   vel.w[idx] = w;
 }
 
+__global__ void k_set_wall_bcs(Dims d, const int* __restrict__ flags, Mac vel, CMac obvel, int hasObvel) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  set_wall_bcs_cell(d, flags, vel, obvel, hasObvel, i, j, k);
+}
+
 // KnAddBuoyancy (extforces.cpp:72-80).  (0.5*s)*(rho+rho') is formed in
 // double and added in double in the reference: one fmaf rounding here.
-__global__ void k_add_buoyancy(Dims d, const int* __restrict__ flags, const float* __restrict__ rho, Mac vel, float hx,
-                               float hy, float hz) {
-  CELL_IJK
+__device__ __forceinline__ void add_buoyancy_cell(const Dims& d, const int* __restrict__ flags, const float* __restrict__ rho, Mac vel, float hx,
+                               float hy, float hz, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   if (!INNER) return;
   if (!isF(flags, idx)) return;
   const float r = __ldg(rho + idx);
   if (isF(flags, idx - 1)) vel.u[idx] = fmaf(hx, r + __ldg(rho + idx - 1), vel.u[idx]);
   if (isF(flags, idx - d.sy)) vel.v[idx] = fmaf(hy, r + __ldg(rho + idx - d.sy), vel.v[idx]);
   if (d.is3d && isF(flags, idx - d.sz)) vel.w[idx] = fmaf(hz, r + __ldg(rho + idx - d.sz), vel.w[idx]);
+}
+
+__global__ void k_add_buoyancy(Dims d, const int* __restrict__ flags, const float* __restrict__ rho, Mac vel, float hx,
+                               float hy, float hz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  add_buoyancy_cell(d, flags, rho, vel, hx, hy, hz, i, j, k);
 }
 
 // KnApplyForce additive (extforces.cpp:46-58)
@@ -438,6 +456,43 @@ int launch_minmax_partial(long long n, const float* a, float* part, cudaStream_t
   count_launch();
   k_minmax_partial<<<blocks, 256, 0, s>>>(n, a, part);
   return blocks;
+}
+
+// ----------------------------------------------------------------- batched
+#define BATCH_CELL                                                       \
+  const BTile tl = tiles[blockIdx.x];                                    \
+  const BScene& sc = S[tl.scene];                                        \
+  const Dims d = sc.d;                                                   \
+  const int i = tl.x0 + threadIdx.x, j = tl.y0 + threadIdx.y, k = tl.z; \
+  if (i >= d.nx || j >= d.ny) return;
+
+// inflow: density = max(density, U[0,1) * source) (Grid::join, grid.cpp:303-311)
+__global__ void __launch_bounds__(256) k_b_inflow(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur,
+                                                  int step) {
+  BATCH_CELL
+  const long long idx = ix(d, i, j, k);
+  const float b = batch_noise(sc.seed, step, idx) * sc.mask[idx];
+  float* a = sc.dens[cur];
+  const float x = a[idx];
+  a[idx] = x < b ? b : x;
+}
+// setWallBcs then addBuoyancy: both read and write only their own cell's
+// velocity, so one pass applies them in the reference's order
+__global__ void __launch_bounds__(256) k_b_forces(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int nxt) {
+  BATCH_CELL
+  const Mac v = bmac(sc.vel[nxt], d.n);
+  set_wall_bcs_cell(d, sc.flags, v, CMac{nullptr, nullptr, nullptr}, 0, i, j, k);
+  add_buoyancy_cell(d, sc.flags, sc.dens[nxt], v, sc.bx, sc.by, sc.bz, i, j, k);
+}
+#undef BATCH_CELL
+
+void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, int step, cudaStream_t st) {
+  count_launch();
+  k_b_inflow<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, cur, step);
+}
+void launch_b_forces(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
+  count_launch();
+  k_b_forces<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, nxt);
 }
 
 }  // namespace mgpu

@@ -1,0 +1,77 @@
+// Batched form: many independent scenes of uneven sizes stepped together.
+//
+// Every stage is one kernel launch over a flat list of tiles spanning all
+// scenes.  A tile is a 32 x 8 block of cells in one z-plane of one scene
+// (one CTA); the CTA reads its scene's sizes and buffers from the scene
+// table and runs exactly the per-cell code of the single-scene kernel.  The
+// pressure solve keeps one CgScalars per scene: each tile leaves its partial
+// dot products / norms in a slot of its own, and the last tile of a scene
+// to finish (a per-scene ticket) reduces that scene's slots in tile order,
+// so per-scene results do not depend on how tiles are scheduled.
+#pragma once
+#include <string>
+
+#include "mg_kernels.h"
+
+namespace mgpu {
+
+constexpr int kBTX = 32, kBTY = 8;  // tile = CTA shape
+
+// runtime.cu: the calling thread's error text, and whether mg_init ran
+int set_error(int code, const std::string& msg);
+bool library_ready();
+// Cylinder's axis: the unit direction and the length of the z vector
+void cylinder_axis(const float* z, float* zn, float* mZ);
+
+struct BTile {
+  int scene;
+  int x0, y0, z;
+  int local;  // index of the tile within its scene
+};
+
+// one scene of a batch (device pointers; MAC grids are 3 planes of n floats)
+struct BScene {
+  Dims d;
+  int* flags;
+  float* vel[2];   // ping-pong velocity (MAC)
+  float* dens[2];  // ping-pong density
+  float* fwd;      // 3 planes: forward SL values, then outflow scratch
+  float* mask;     // inflow source (Shape::applyToGrid value 1)
+  float* pres;
+  float* rhs;
+  float* res;
+  float* search;
+  float* tmp;
+  code_t* code;
+  CgScalars* sc;
+  double* part;    // per-tile partials (ntiles doubles, 2 per tile for max-abs)
+  float dt;
+  float bx, by, bz;  // buoyancy factors -gravity*dt/dx*coefficient (KnAddBuoyancy), 0.5 applied in-kernel
+  unsigned long long seed;
+  int ntiles;
+};
+
+__host__ __device__ inline Mac bmac(float* p, long long n) { return Mac{p, p + n, p + 2 * n}; }
+__host__ __device__ inline CMac bcmac(const float* p, long long n) { return CMac{p, p + n, p + 2 * n}; }
+
+// stages (cur: index of the current vel/dens buffers; results go to 1-cur)
+void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, int step, cudaStream_t st);
+void launch_b_advect_density(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
+void launch_b_advect_velocity(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
+void launch_b_forces(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
+void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
+void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, cudaStream_t st);
+void launch_b_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
+// uniform [0,1) inflow noise of a scene's cell at a step (the batch's
+// per-scene seeded source); also used to fill single-scene grids for
+// comparisons
+__host__ __device__ inline float batch_noise(unsigned long long seed, int step, long long cell) {
+  // splitmix64 of (seed, step, cell): a counter-based generator
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * ((unsigned long long)step * 0x100000001B3ull + (unsigned long long)cell + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  return (float)(z >> 40) * (1.0f / 16777216.0f);  // 24 random bits
+}
+
+}  // namespace mgpu

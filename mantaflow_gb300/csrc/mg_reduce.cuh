@@ -72,7 +72,7 @@ __device__ __forceinline__ void minmax_partials(const float* part, int n, float&
 __device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int total) {
   __shared__ bool last;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (lin_tid() == 0) {
     __threadfence();
     const unsigned int t = atomicAdd(counter, 1u);
     last = (t == total - 1);

@@ -20,6 +20,7 @@
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 #include "mg_reduce.cuh"
+#include "mg_batch.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -65,6 +66,14 @@ __device__ __forceinline__ float surf_tens_helper(const float* phi, const float*
   return st * (curv[idx + off] - gf_helper(phi, idx, off, gfc) * curv[idx]);
 }
 
+// -div(u) of a fluid cell as MakeRhs forms it
+__device__ __forceinline__ float mac_neg_div(const Dims& d, const float* __restrict__ vu, const float* __restrict__ vv,
+                                             const float* __restrict__ vw, long long idx) {
+  float set = vu[idx] - vu[idx + 1] + vv[idx] - vv[idx + d.sy];
+  if (d.is3d) set += vw[idx] - vw[idx + d.sz];
+  return set;
+}
+
 __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict__ flags, float* rhs, const float* __restrict__ vu,
                                                   const float* __restrict__ vv, const float* __restrict__ vw,
                                                   const float* __restrict__ corr, const float* __restrict__ phi,
@@ -81,8 +90,7 @@ __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict_
       if (!isF(flags, idx)) {
         rhs[idx] = 0.f;
       } else {
-        float set = vu[idx] - vu[idx + 1] + vv[idx] - vv[idx + d.sy];
-        if (d.is3d) set += vw[idx] - vw[idx + d.sz];
+        float set = mac_neg_div(d, vu, vv, vw, idx);
         if (phi && curv) {
           const long long X = 1, Y = d.sy, Z = d.sz;
           if (isE(flags, idx - X)) set += surf_tens_helper(phi, curv, idx, -X, surfTens, gfClamp);
@@ -135,8 +143,8 @@ __global__ void k_compat_shift(long long n, float* rhs, const CgScalars* sc) {
 // ------------------------------------------------------- stencil codes
 // MakeLaplaceMatrix (conjugategrad.h:154-187) as codes.  Pass 1: A0 count,
 // fluid bit and the upward links of interior fluid cells.
-__global__ void k_make_codes(Dims d, const int* __restrict__ flags, code_t* code) {
-  CELL_IJK
+__device__ __forceinline__ void make_codes_cell(const Dims& d, const int* __restrict__ flags, code_t* code, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   const bool fl = isF(flags, idx);
   int c = fl ? kCodeFluid : 0;
   if (fl && INNER) {
@@ -156,14 +164,30 @@ __global__ void k_make_codes(Dims d, const int* __restrict__ flags, code_t* code
   }
   code[idx] = (code_t)c;
 }
+
+__global__ void k_make_codes(Dims d, const int* __restrict__ flags, code_t* code) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  make_codes_cell(d, flags, code, i, j, k);
+}
 // pass 2: lower links mirror the upper link of the lower neighbour
-__global__ void k_make_codes_low(Dims d, code_t* code) {
-  CELL_IJK
+__device__ __forceinline__ void make_codes_low_cell(const Dims& d, code_t* code, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   int c = code[idx];
   if (i > 0 && (code[idx - 1] & kHighX)) c |= kLowX;
   if (j > 0 && (code[idx - d.sy] & kHighY)) c |= kLowY;
   if (k > 0 && (code[idx - d.sz] & kHighZ)) c |= kLowZ;
   code[idx] = (code_t)c;
+}
+
+__global__ void k_make_codes_low(Dims d, code_t* code) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  make_codes_low_cell(d, code, i, j, k);
 }
 
 // ApplyGhostFluidDiagonal (pressure.cpp:136-151): float diagonal
@@ -726,8 +750,8 @@ __global__ void k_mic_init_sigma(const double* part, int ntiles, CgScalars* sc) 
 
 // ------------------------------------------------------- correctVelocity
 // knCorrectVelocity (pressure.cpp:87-109)
-__global__ void k_correct_velocity(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ p) {
-  CELL_IJK
+__device__ __forceinline__ void correct_velocity_cell(const Dims& d, const int* __restrict__ flags, Mac vel, const float* __restrict__ p, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   if (!INNER) return;
   const long long X = 1, Y = d.sy, Z = d.sz;
   if (isF(flags, idx)) {
@@ -747,6 +771,14 @@ __global__ void k_correct_velocity(Dims d, const int* __restrict__ flags, Mac ve
     if (d.is3d) { if (isF(flags, idx - Z)) w += p[idx - Z]; else w = 0.f; }
     vel.u[idx] = u; vel.v[idx] = v; vel.w[idx] = w;
   }
+}
+
+__global__ void k_correct_velocity(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= d.nx || j >= d.ny) return;
+  correct_velocity_cell(d, flags, vel, p, i, j, k);
 }
 
 // knCorrectVelocityGhostFluid (pressure.cpp:154-187)
@@ -933,6 +965,183 @@ void launch_correct_velocity(const Dims& d, const int* flags, Mac vel, const flo
     count_launch();
     k_replace_clamped_gf<<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, phi, gfClamp);
   }
+}
+
+// ----------------------------------------------------------------- batched
+// The plume's solvePressure for every scene of a batch: MakeRhs,
+// MakeLaplaceMatrix (as codes), GridCg with PcNone -- the reference's 2D
+// path, run for every scene here -- and knCorrectVelocity.  Per-scene CG
+// scalars; per-tile partials reduced by the scene's last tile in tile order.
+#define BATCH_TILE                                                       \
+  const BTile tl = tiles[blockIdx.x];                                    \
+  const BScene& sc = S[tl.scene];                                        \
+  const Dims d = sc.d;                                                   \
+  const int i = tl.x0 + threadIdx.x, j = tl.y0 + threadIdx.y, k = tl.z; \
+  const bool in = i < d.nx && j < d.ny;                                  \
+  const long long idx = in ? ix(d, i, j, k) : 0;
+
+// MakeRhs and MakeLaplaceMatrix pass 1
+__global__ void __launch_bounds__(256) k_b_rhs_codes(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int nxt) {
+  BATCH_TILE
+  if (!in) return;
+  float r = 0.f;
+  if (INNER && isF(sc.flags, idx)) {
+    const float* v = sc.vel[nxt];
+    r = mac_neg_div(d, v, v + d.n, v + 2 * d.n, idx);
+  }
+  sc.rhs[idx] = r;
+  make_codes_cell(d, sc.flags, sc.code, i, j, k);
+}
+
+// MakeLaplaceMatrix pass 2 and GridCg::doInit with PcNone: x = 0, r = rhs,
+// z = r, s = z, sigma = dot(z, r)
+__global__ void __launch_bounds__(256) k_b_pcg_init(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
+  BATCH_TILE
+  FSum acc;
+  if (in) {
+    make_codes_low_cell(d, sc.code, i, j, k);
+    const float r = sc.rhs[idx];
+    sc.pres[idx] = 0.f;
+    sc.res[idx] = r;
+    sc.tmp[idx] = r;
+    sc.search[idx] = r;
+    acc.add(r * r);
+  }
+  const double b = block_sum(acc.value());
+  if (lin_tid() == 0) sc.part[tl.local] = b;
+  if (last_block(&sc.sc->counters[0], sc.ntiles)) {
+    const double s2 = sum_partials(sc.part, sc.ntiles);
+    if (lin_tid() == 0) sc.sc->sigma = (float)s2;
+  }
+}
+
+// tmp = A s (ApplyMatrix) and dot(tmp, s) -> alpha
+__global__ void __launch_bounds__(256) k_b_pcg_spmv(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
+  BATCH_TILE
+  CgScalars* g = sc.sc;
+  if (g->done) return;
+  FSum acc;
+  if (in) {
+    const int c = sc.code[idx];
+    const float* x = sc.search;
+    const float xc = x[idx];
+    float v;
+    if (!(c & kCodeFluid)) {
+      v = xc;
+    } else {
+      v = xc * (float)(c & 7);
+      if (c & kLowX) v = v - x[idx - 1];
+      if (c & kHighX) v = v - x[idx + 1];
+      if (c & kLowY) v = v - x[idx - d.sy];
+      if (c & kHighY) v = v - x[idx + d.sy];
+      if (c & kLowZ) v = v - x[idx - d.sz];
+      if (c & kHighZ) v = v - x[idx + d.sz];
+    }
+    sc.tmp[idx] = v;
+    acc.add(v * xc);
+  }
+  const double b = block_sum(acc.value());
+  if (lin_tid() == 0) sc.part[tl.local] = b;
+  if (last_block(&g->counters[1], sc.ntiles)) {
+    const double s2 = sum_partials(sc.part, sc.ntiles);
+    if (lin_tid() == 0) {
+      const float dp = (float)s2;
+      g->dp = dp;
+      g->alpha = fabsf(dp) > 0.f ? g->sigma / dp : 0.f;
+    }
+  }
+}
+
+// x += alpha s, r -= alpha tmp, z = r (PcNone), resNorm = max|r| and the
+// convergence test; then sigmaNew = dot(z, r) and beta (GridCg::iterate)
+__global__ void __launch_bounds__(256) k_b_pcg_axpy(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                    int* ndone) {
+  BATCH_TILE
+  CgScalars* g = sc.sc;
+  if (g->done) return;
+  const float alpha = g->alpha, na = -alpha;
+  float mx = 0.f;
+  FSum acc;
+  if (in) {
+    sc.pres[idx] = sc.pres[idx] + alpha * sc.search[idx];
+    const float rv = sc.res[idx] + na * sc.tmp[idx];
+    sc.res[idx] = rv;
+    sc.tmp[idx] = rv;
+    mx = fabsf(rv);
+    acc.add(rv * rv);
+  }
+  const double b = block_sum(acc.value());
+  __shared__ float smx[32];
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((lin_tid() & 31) == 0) smx[lin_tid() >> 5] = mx;
+  __syncthreads();
+  if (lin_tid() == 0) {
+    float m = 0.f;
+    for (int q = 0; q < nwarps(); q++) m = fmaxf(m, smx[q]);
+    sc.part[tl.local] = b;
+    sc.part[sc.ntiles + tl.local] = (double)m;
+  }
+  if (last_block(&g->counters[2], sc.ntiles)) {
+    const double s2 = sum_partials(sc.part, sc.ntiles);
+    if (lin_tid() != 0) return;
+    float res = 0.f;
+    for (int q = 0; q < sc.ntiles; q++) res = fmaxf(res, (float)__ldcg(sc.part + sc.ntiles + q));
+    g->iterations += 1;
+    g->resNorm = res;
+    if (res < g->accuracy) {
+      g->sigma = res;
+      g->done = 1;
+      atomicAdd(ndone, 1);
+      return;
+    }
+    const float sigmaNew = (float)s2;
+    g->beta = sigmaNew / g->sigma;
+    g->sigma = sigmaNew;
+    if (!(res < 1e35f)) {
+      g->status = 2;
+      g->done = 1;
+      atomicAdd(ndone, 1);
+    } else if (g->iterations >= g->maxIter) {
+      g->done = 1;
+      atomicAdd(ndone, 1);
+    }
+  }
+}
+
+// s = z + beta s (UpdateSearchVec)
+__global__ void __launch_bounds__(256) k_b_pcg_update(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
+  BATCH_TILE
+  if (!in || sc.sc->done) return;
+  const float beta = sc.sc->beta;
+  sc.search[idx] = sc.tmp[idx] + beta * sc.search[idx];
+}
+
+__global__ void __launch_bounds__(256) k_b_correct(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int nxt) {
+  BATCH_TILE
+  if (!in) return;
+  correct_velocity_cell(d, sc.flags, bmac(sc.vel[nxt], d.n), sc.pres, i, j, k);
+}
+#undef BATCH_TILE
+
+void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
+  const dim3 b(kBTX, kBTY, 1);
+  count_launch();
+  k_b_rhs_codes<<<nt, b, 0, st>>>(t, s, nxt);
+  count_launch();
+  k_b_pcg_init<<<nt, b, 0, st>>>(t, s);
+}
+void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, cudaStream_t st) {
+  const dim3 b(kBTX, kBTY, 1);
+  count_launch();
+  k_b_pcg_spmv<<<nt, b, 0, st>>>(t, s);
+  count_launch();
+  k_b_pcg_axpy<<<nt, b, 0, st>>>(t, s, ndone);
+  count_launch();
+  k_b_pcg_update<<<nt, b, 0, st>>>(t, s);
+}
+void launch_b_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
+  count_launch();
+  k_b_correct<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, nxt);
 }
 
 }  // namespace mgpu

@@ -19,6 +19,7 @@
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 #include "mg_multigrid.h"
+#include "mg_batch.h"
 
 using namespace mgpu;
 
@@ -35,6 +36,9 @@ static int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+
+// for the other translation units of the library (batch.cu, serve.cu)
+int mgpu::set_error(int code, const std::string& msg) { return fail(code, msg); }
 
 #define CK(call)                                                                              \
   do {                                                                                        \
@@ -235,6 +239,8 @@ struct Tmp {
 
 static bool valid_solver(mg_solver s) { return s && g_ctx.solvers.count(s); }
 static bool valid_grid(mg_grid g) { return g && valid_solver(g->s) && g->s->grids.count(g); }
+
+bool mgpu::library_ready() { return g_ctx.init; }
 
 #define NEED_INIT() \
   if (!g_ctx.init) return fail(MG_ERR_STATE, "mg_init has not been called")
@@ -1484,6 +1490,28 @@ extern "C" int mg_flags_update_from_levelset(mg_grid flags, mg_grid levelset) {
   return MG_OK;
 }
 
+// Cylinder ctor: mZ = normalize(mZDir) (shapes.cpp:316-322, vectorbase.h:416-432)
+void mgpu::cylinder_axis(const float* z, float* zn, float* mZout) {
+  float zx = z[0], zy = z[1], zz = z[2], mZ;
+  const float l = zx * zx + zy * zy + zz * zz;
+  if (std::fabs((double)l - 1.) < (double)(1e-6f * 1e-6f)) {
+    mZ = 1.f;
+  } else if (l > 1e-6f * 1e-6f) {
+    mZ = std::sqrt(l);
+    const float inv = (float)(1. / (double)mZ);
+    zx = zx * inv;
+    zy = zy * inv;
+    zz = zz * inv;
+  } else {
+    zx = zy = zz = 0.f;
+    mZ = 0.f;
+  }
+  zn[0] = zx;
+  zn[1] = zy;
+  zn[2] = zz;
+  *mZout = mZ;
+}
+
 static int shape_apply(mg_grid grid, int shape, const float* a, const float* b, float radius, float mZ, const float* value,
                        int ivalue, mg_grid respect) {
   mg_solver s = grid->s;
@@ -1521,22 +1549,8 @@ extern "C" int mg_shape_cylinder_apply(mg_grid grid, const float* center, float 
                                        const float* value, int ivalue, mg_grid respectFlags) {
   NEED_GRID(grid, "Cylinder.applyToGrid");
   if (!center || !z || !value) return fail(MG_ERR_ARG, "Cylinder.applyToGrid: null argument");
-  // Cylinder ctor: mZ = normalize(mZDir) (shapes.cpp:316-322, vectorbase.h:416-432)
-  float zx = z[0], zy = z[1], zz = z[2], mZ;
-  const float l = zx * zx + zy * zy + zz * zz;
-  if (std::fabs((double)l - 1.) < (double)(1e-6f * 1e-6f)) {
-    mZ = 1.f;
-  } else if (l > 1e-6f * 1e-6f) {
-    mZ = std::sqrt(l);
-    const float inv = (float)(1. / (double)mZ);
-    zx = zx * inv;
-    zy = zy * inv;
-    zz = zz * inv;
-  } else {
-    zx = zy = zz = 0.f;
-    mZ = 0.f;
-  }
-  const float zn[3] = {zx, zy, zz};
+  float zn[3], mZ;
+  cylinder_axis(z, zn, &mZ);
   return shape_apply(grid, 1, center, zn, radius, mZ, value, ivalue, respectFlags);
 }
 
