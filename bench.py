@@ -285,6 +285,90 @@ def precision_form(m, n, steps, seed):
     return out
 
 
+def batch_config(seed, n2=512, n3=64):
+    """Config 4: 512 2D scenes with sides round(exp(U[ln 64, ln 512])) and 64
+    3D scenes with sides U{32..96}; buoyancy magnitudes U[1e-3, 8e-3]."""
+    rng = np.random.default_rng(seed)
+    sizes = [(int(round(np.exp(rng.uniform(np.log(64), np.log(512))))),) * 2 + (1,) for _ in range(n2)]
+    sizes += [(int(rng.integers(32, 97)),) * 3 for _ in range(n3)]
+    grav = [(0.0, -float(g), 0.0) for g in rng.uniform(1e-3, 8e-3, len(sizes))]
+    seeds = [int(x) for x in rng.integers(1, 2 ** 62, len(sizes))]
+    return sizes, grav, seeds
+
+
+def batched_form(m, steps, seed, plain_steps, plain_scenes, sim_steps=100):
+    """Config 4, batched against plain: the whole batch for `steps` steps,
+    and the plain per-scene path (one solver per scene, scenes one after
+    another) on a stratified sample of the same scenes; sims/hour for
+    `sim_steps`-step simulations and per-step latency percentiles."""
+    from mantaflow_gb300 import batch as mb
+    sizes, grav, seeds = batch_config(seed)
+    b = mb.BatchedPlumes(sizes, grav, seeds)
+    info = b.info()
+    b.step()  # untimed first step
+    b.sync()
+    lat, sweeps = [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        st = b.step()
+        lat.append(time.perf_counter() - t0)
+        sweeps.append(st["sweeps"])
+    b.close()
+    per_step = statistics.mean(lat)
+    batched = {"sims_per_hour": len(sizes) * 3600.0 / (per_step * sim_steps), "step_ms_mean": 1e3 * per_step,
+               "step_ms_p50": 1e3 * float(np.percentile(lat, 50)), "step_ms_p99": 1e3 * float(np.percentile(lat, 99)),
+               "cells_per_s": info["cells"] / per_step, "cg_sweeps_per_step": sweeps, "steps_timed": steps}
+    # plain: every k-th scene in size order (2D and 3D separately)
+    order2 = sorted(range(512), key=lambda i: sizes[i][0])
+    order3 = sorted(range(512, len(sizes)), key=lambda i: sizes[i][0])
+    k2 = max(1, len(order2) // max(1, plain_scenes - 4))
+    pick = order2[k2 // 2::k2][: plain_scenes - 4] + order3[len(order3) // 8::len(order3) // 4][:4]
+    per_scene, plain_lat = [], []
+    for i in pick:
+        nx, ny, nz = sizes[i]
+        s = m.Solver(name="plain", gridSize=m.vec3(nx, ny, nz), dim=3 if nz > 1 else 2)
+        flags = s.create(m.FlagGrid)
+        flags.initDomain(boundaryWidth=0)
+        flags.fillGrid()
+        m.setOpenBound(flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
+        vel, dens, pres, src = s.create(m.MACGrid), s.create(m.RealGrid), s.create(m.RealGrid), s.create(m.RealGrid)
+        gs = m.vec3(nx, ny, nz)
+        mask = s.create(m.RealGrid)
+        s.create(m.Cylinder, center=gs * m.vec3(0.5, 0.1, 0.5), radius=nx * 0.14,
+                 z=gs * m.vec3(0, 0.02, 0)).applyToGrid(grid=mask, value=1.0)
+        mk = mask.numpy()
+        rng = np.random.default_rng(seeds[i] % (2 ** 32))
+        ts = []
+        for t in range(plain_steps + 1):
+            m.copyArrayToGridReal((rng.random(mk.shape, dtype=np.float32) * mk).astype(np.float32), src)
+            s.sync()
+            t0 = time.perf_counter()
+            dens.join(src)
+            m.advectSemiLagrange(flags=flags, vel=vel, grid=dens, order=2, clampMode=2)
+            m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=2, clampMode=2)
+            m.setWallBcs(flags=flags, vel=vel)
+            m.addBuoyancy(density=dens, vel=vel, gravity=m.vec3(*grav[i]), flags=flags)
+            m.solvePressure(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, preconditioner=m.PcMIC)
+            s.sync()
+            if t > 0:
+                ts.append(time.perf_counter() - t0)
+        per_scene.append(statistics.mean(ts))
+        plain_lat += ts
+        del s
+    w2 = 512 / (len(pick) - 4)
+    w3 = (len(sizes) - 512) / 4
+    est = sum(t * (w2 if i < 512 else w3) for t, i in zip(per_scene, pick))  # seconds per step of all scenes
+    plain = {"sims_per_hour": len(sizes) * 3600.0 / (est * sim_steps), "step_ms_p50": 1e3 * float(np.percentile(plain_lat, 50)),
+             "step_ms_p99": 1e3 * float(np.percentile(plain_lat, 99)), "all_scenes_step_s_estimate": est,
+             "sample": "%d scenes (every %d-th 2D scene by size, 4 of the 3D scenes), %d timed steps each after one "
+                       "untimed; per-step time extrapolated by scene class" % (len(pick), k2, plain_steps)}
+    return {"workload": "config 4: %d 2D plume scenes (sides log-uniform in [64,512]) + %d 3D (sides U{32..96}), "
+                        "buoyancy U[1e-3,8e-3], cgAccuracy 1e-3; %d-step simulations" % (512, len(sizes) - 512, sim_steps),
+            "scenes": len(sizes), "cells": info["cells"], "tiles": info["tiles"], "device_bytes": info["bytes"],
+            "batched": batched, "plain_per_scene": plain, "speedup_sims_per_hour":
+                batched["sims_per_hour"] / plain["sims_per_hour"]}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -347,6 +431,9 @@ def main():
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--precision-size", type=int, default=64, help="grid side of the precision-form sample (0: skip)")
     ap.add_argument("--precision-steps", type=int, default=10)
+    ap.add_argument("--batched-steps", type=int, default=10, help="timed steps of the config-4 batch (0: skip)")
+    ap.add_argument("--plain-steps", type=int, default=3, help="timed steps per sampled scene of the plain path")
+    ap.add_argument("--plain-scenes", type=int, default=16)
     ap.add_argument("--refined-steps", type=int, default=5,
                     help="timed 256^3 steps of the FP64-refined form reported beside the headline (0: skip)")
     args = ap.parse_args()
@@ -515,6 +602,9 @@ def main():
                    "value": n ** 3 * KR / (msr.value / 1e3), "unit": "cells/s", "ms_per_step": msr.value / KR,
                    "steps": KR, "warmup": 3, "refine_stats": rp.refine_stats[-KR:]}
         del noise_r, ng, rp
+    batched = None
+    if args.batched_steps > 0 and rank == 0:
+        batched = batched_form(m, args.batched_steps, args.seed + 13, args.plain_steps, args.plain_scenes)
     precision = None
     if args.precision_size > 0 and rank == 0 and world == 1:
         precision = precision_form(m, args.precision_size, args.precision_steps, args.seed + 5)
@@ -545,7 +635,8 @@ def main():
                "gpu_launches": int(cnt1.value - cnt0.value),
                "clocks": clk, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])},
-               "same_scene_pc_mic": alt, "precision_form": {"refined_256": refined, "errors_vs_fp64": precision}}
+               "same_scene_pc_mic": alt, "precision_form": {"refined_256": refined, "errors_vs_fp64": precision},
+               "batched_form": batched}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
