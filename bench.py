@@ -313,11 +313,13 @@ def batched_form(m, steps, seed, plain_steps, plain_scenes, sim_steps=100):
         st = b.step()
         lat.append(time.perf_counter() - t0)
         sweeps.append(st["sweeps"])
+    tune = b.tuning()
     b.close()
     per_step = statistics.mean(lat)
     batched = {"sims_per_hour": len(sizes) * 3600.0 / (per_step * sim_steps), "step_ms_mean": 1e3 * per_step,
                "step_ms_p50": 1e3 * float(np.percentile(lat, 50)), "step_ms_p99": 1e3 * float(np.percentile(lat, 99)),
-               "cells_per_s": info["cells"] / per_step, "cg_sweeps_per_step": sweeps, "steps_timed": steps}
+               "cells_per_s": info["cells"] / per_step, "cg_sweeps_per_step": sweeps, "steps_timed": steps,
+               "autotuned_sweep_tile": {"rows": tune[0], "ms_per_8_sweeps_for_8_16_32_64_rows": tune[1]}}
     # plain: every k-th scene in size order (2D and 3D separately)
     order2 = sorted(range(512), key=lambda i: sizes[i][0])
     order3 = sorted(range(512, len(sizes)), key=lambda i: sizes[i][0])

@@ -258,6 +258,9 @@ int mg_batch_download(mg_batch b, int scene, int what, void* host, size_t bytes)
  * cell (host computation, for feeding the same inflow to a single scene) */
 int mg_batch_noise(unsigned long long seed, int step, long long cells, float* out);
 int mg_batch_info(mg_batch b, int* count, long long* cells, long long* tiles, size_t* bytes);
+/* the CG sweep tile height the batch's autotuner chose on its first solve
+ * (0 before) and the four timings (ms per lag sweeps, 8/16/32/64 rows) */
+int mg_batch_tuning(mg_batch b, int* sweepRows, float* ms);
 int mg_batch_sync(mg_batch b);
 
 /* ---- timing (CUDA events on the solver's stream) ------------------------- */

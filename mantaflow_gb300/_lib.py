@@ -91,6 +91,7 @@ SIGNATURES = [
     ("mg_batch_info", _I, [_P, C.POINTER(_I), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                            C.POINTER(C.c_size_t)]),
     ("mg_batch_sync", _I, [_P]),
+    ("mg_batch_tuning", _I, [_P, C.POINTER(_I), _FP]),
     ("mg_compute_pressure_rhs", _I, [_P, _P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P, _P]),
     ("mg_solve_pressure_system", _I, [_P, _P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P,
                                       C.POINTER(PressureResult)]),

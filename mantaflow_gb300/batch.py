@@ -81,6 +81,13 @@ class BatchedPlumes:
         check(self._L.mg_batch_info(self._h, C.byref(c), C.byref(cells), C.byref(tiles), C.byref(nbytes)))
         return {"scenes": c.value, "cells": cells.value, "tiles": tiles.value, "bytes": nbytes.value}
 
+    def tuning(self):
+        """(CG sweep tile height chosen by the autotuner, timings per candidate)"""
+        rows = C.c_int()
+        ms = (C.c_float * 4)()
+        check(self._L.mg_batch_tuning(self._h, C.byref(rows), ms))
+        return rows.value, list(ms)
+
     def sync(self):
         check(self._L.mg_batch_sync(self._h))
 

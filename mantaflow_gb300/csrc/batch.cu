@@ -35,10 +35,16 @@ struct mg_batch_s {
   size_t arenaBytes = 0;
   std::vector<BScene> scenes;     // host copy of the table
   BScene* dScenes = nullptr;
-  std::vector<BTile> tiles;       // all tiles, scene-major
+  std::vector<BTile> tiles;       // all 32 x 8 tiles, scene-major
   std::vector<int> tileStart;     // first tile of each scene
   BTile* dTiles = nullptr;
-  BTile* dActive = nullptr;       // tiles of the scenes still iterating
+  // CG sweep tiles 32 x 8R cells for R = 1, 2, 4, 8 (rowsK[k] = 1 << k)
+  std::vector<BTile> tilesR[4];
+  std::vector<int> startR[4];
+  BTile* dActive = nullptr;       // sweep tiles of the scenes still iterating
+  int rowsK = -1;                 // autotuned sweep tile height (index), -1 until chosen
+  float tuneMs[4] = {0.f, 0.f, 0.f, 0.f};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
   CgScalars* dSc = nullptr;
   std::vector<CgScalars> hSc;
   int* dDone = nullptr;
@@ -160,9 +166,21 @@ extern "C" int mg_batch_create(int count, const int* sizes, const float* gravity
     int local = 0;
     for (int z = 0; z < nz; z++)
       for (int y = 0; y < ny; y += kBTY)
-        for (int x = 0; x < nx; x += kBTX) b->tiles.push_back(BTile{q, x, y, z, local++});
+        for (int x = 0; x < nx; x += kBTX) b->tiles.push_back(BTile{q, x, y, z, local++, ntiles});
+    for (int kk = 0; kk < 4; kk++) {
+      const int rows = kBTY << kk;
+      const int cnt = ((nx + kBTX - 1) / kBTX) * ((ny + rows - 1) / rows) * nz;
+      b->startR[kk].push_back((int)b->tilesR[kk].size());
+      int l = 0;
+      for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y += rows)
+          for (int x = 0; x < nx; x += kBTX) b->tilesR[kk].push_back(BTile{q, x, y, z, l++, cnt});
+    }
   }
   b->tileStart.push_back((int)b->tiles.size());
+  for (int kk = 0; kk < 4; kk++) b->startR[kk].push_back((int)b->tilesR[kk].size());
+  CKB(cudaEventCreate(&b->ev[0]));
+  CKB(cudaEventCreate(&b->ev[1]));
   CKB(cudaMalloc(&b->dScenes, sizeof(BScene) * count));
   CKB(cudaMemcpyAsync(b->dScenes, b->scenes.data(), sizeof(BScene) * count, cudaMemcpyHostToDevice, b->stream));
   CKB(cudaMalloc(&b->dTiles, sizeof(BTile) * b->tiles.size()));
@@ -183,6 +201,8 @@ extern "C" int mg_batch_destroy(mg_batch b) {
   cudaFree(b->dActive);
   cudaFree(b->dSc);
   cudaFree(b->dDone);
+  if (b->ev[0]) cudaEventDestroy(b->ev[0]);
+  if (b->ev[1]) cudaEventDestroy(b->ev[1]);
   cudaStreamDestroy(b->stream);
   delete b;
   return MG_OK;
@@ -218,27 +238,59 @@ extern "C" int mg_batch_step(mg_batch b, mg_batch_stats* stats) {
   CKB(cudaMemcpyAsync(b->dSc, b->hSc.data(), sizeof(CgScalars) * b->count, cudaMemcpyHostToDevice, st));
   CKB(cudaMemsetAsync(b->dDone, 0, sizeof(int), st));
   launch_b_pressure_setup(b->dTiles, nt, b->dScenes, nxt, st);
-  CKB(cudaMemcpyAsync(b->dActive, b->dTiles, sizeof(BTile) * nt, cudaMemcpyDeviceToDevice, st));
-  int active = nt, doneSeen = 0, sweeps = 0;
+  // CG sweeps over the tiles of the scenes still iterating.  Autotuner: the
+  // first solve runs its first 4 x lag sweeps with tiles 8, 16, 32 and 64
+  // rows tall (lag sweeps each, timed with events) and keeps the fastest;
+  // results do not depend on the choice.
+  int kk = b->rowsK >= 0 ? b->rowsK : 0;
+  int active = 0, doneSeen = -1, sweeps = 0;
   std::vector<BTile> list;
+  auto rebuild = [&](bool all) -> int {
+    list.clear();
+    for (int q = 0; q < b->count; q++)
+      if (all || !b->hSc[q].done)
+        list.insert(list.end(), b->tilesR[kk].begin() + b->startR[kk][q], b->tilesR[kk].begin() + b->startR[kk][q + 1]);
+    active = (int)list.size();
+    if (active) CKB(cudaMemcpyAsync(b->dActive, list.data(), sizeof(BTile) * active, cudaMemcpyHostToDevice, st));
+    return MG_OK;
+  };
+  if (rebuild(true)) return MG_ERR_CUDA;
+  const bool tuning = b->rowsK < 0;
+  if (tuning) CKB(cudaEventRecord(b->ev[0], st));
   while (active > 0 && sweeps < maxIterAll) {
-    launch_b_pcg_iteration(b->dActive, active, b->dScenes, b->dDone, st);
+    launch_b_pcg_iteration(b->dActive, active, b->dScenes, 1 << kk, b->dDone, st);
     sweeps++;
     if (sweeps % b->lag == 0 || sweeps == maxIterAll) {
+      bool relist = false;
+      if (tuning && b->rowsK < 0 && sweeps <= 4 * b->lag) {
+        CKB(cudaEventRecord(b->ev[1], st));
+        CKB(cudaEventSynchronize(b->ev[1]));
+        float ms = 0.f;
+        CKB(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+        b->tuneMs[kk] = ms;
+        if (kk < 3) {
+          kk++;
+          relist = true;
+        } else {
+          int best = 0;
+          for (int q = 1; q < 4; q++)
+            if (b->tuneMs[q] < b->tuneMs[best]) best = q;
+          b->rowsK = best;
+          relist = kk != best;
+          kk = best;
+        }
+      }
       int nd = 0;
       CKB(cudaMemcpyAsync(&nd, b->dDone, sizeof(int), cudaMemcpyDeviceToHost, st));
       CKB(cudaStreamSynchronize(st));
       if (nd >= b->count) break;
-      if (nd != doneSeen) {
+      if (nd != doneSeen || relist) {
         doneSeen = nd;
         CKB(cudaMemcpyAsync(b->hSc.data(), b->dSc, sizeof(CgScalars) * b->count, cudaMemcpyDeviceToHost, st));
         CKB(cudaStreamSynchronize(st));
-        list.clear();
-        for (int q = 0; q < b->count; q++)
-          if (!b->hSc[q].done) list.insert(list.end(), b->tiles.begin() + b->tileStart[q], b->tiles.begin() + b->tileStart[q + 1]);
-        active = (int)list.size();
-        if (active) CKB(cudaMemcpyAsync(b->dActive, list.data(), sizeof(BTile) * active, cudaMemcpyHostToDevice, st));
+        if (rebuild(false)) return MG_ERR_CUDA;
       }
+      if (tuning && b->rowsK < 0) CKB(cudaEventRecord(b->ev[0], st));
     }
   }
   launch_b_correct(b->dTiles, nt, b->dScenes, nxt, st);
@@ -308,6 +360,14 @@ extern "C" int mg_batch_download(mg_batch b, int scene, int what, void* host, si
 extern "C" int mg_batch_noise(unsigned long long seed, int step, long long cells, float* out) {
   if (!out || cells < 0) return set_error(MG_ERR_ARG, "mg_batch_noise: invalid argument");
   for (long long i = 0; i < cells; i++) out[i] = batch_noise(seed, step, i);
+  return MG_OK;
+}
+
+extern "C" int mg_batch_tuning(mg_batch b, int* sweepRows, float* ms) {
+  if (!b) return set_error(MG_ERR_ARG, "mg_batch_tuning: null batch");
+  if (sweepRows) *sweepRows = b->rowsK < 0 ? 0 : kBTY << b->rowsK;
+  if (ms)
+    for (int q = 0; q < 4; q++) ms[q] = b->tuneMs[q];
   return MG_OK;
 }
 

@@ -26,7 +26,8 @@ void cylinder_axis(const float* z, float* zn, float* mZ);
 struct BTile {
   int scene;
   int x0, y0, z;
-  int local;  // index of the tile within its scene
+  int local;  // index of the tile within its scene (32 x 8 tiles)
+  int count;  // tiles of this scene in the list the tile belongs to
 };
 
 // one scene of a batch (device pointers; MAC grids are 3 planes of n floats)
@@ -60,7 +61,8 @@ void launch_b_advect_density(const BTile* t, int nt, const BScene* s, int cur, c
 void launch_b_advect_velocity(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_forces(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
 void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
-void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, cudaStream_t st);
+// one CG sweep over tiles 32 x 8*rows cells tall (rows 1, 2, 4 or 8)
+void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int rows, int* ndone, cudaStream_t st);
 void launch_b_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
 // uniform [0,1) inflow noise of a scene's cell at a step (the batch's
 // per-scene seeded source); also used to fill single-scene grids for

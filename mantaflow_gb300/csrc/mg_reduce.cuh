@@ -68,6 +68,21 @@ __device__ __forceinline__ void minmax_partials(const float* part, int n, float&
   block_minmax(mn, mx);
 }
 
+// all threads of a block: max of part[0..n), result valid in thread 0
+__device__ __forceinline__ double max_partials(const double* part, int n) {
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  double v = 0.;
+  for (int q = lin_tid(); q < n; q += nt) v = fmax(v, __ldcg(part + q));
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((lin_tid() & 31) == 0) sh[lin_tid() >> 5] = v;
+  __syncthreads();
+  if (lin_tid() == 0)
+    for (int q = 0; q < nwarps(); q++) v = fmax(v, sh[q]);
+  return v;
+}
+
 // "last block" ticket: true in every thread of the block that finishes last
 __device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int total) {
   __shared__ bool last;
@@ -80,6 +95,66 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, unsigned int t
   }
   __syncthreads();
   return last;
+}
+
+// Double-float ("ff") arithmetic: a value is the unevaluated sum h + l of
+// two floats (48-bit significand), built from Knuth's exact two-sum and the
+// FMA-exact product.  GB300 runs FP64 at a small fraction of its FP32 rate,
+// so sums and scalars that need more than float precision use these.
+struct ff {
+  float h, l;
+};
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return ff{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ ff quick_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return ff{s, b - (s - a)};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  const float p = a * b;
+  return ff{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = two_sum(a.h, b.h);
+  const ff t = two_sum(a.l, b.l);
+  s.l = s.l + t.h;
+  s = quick_two_sum(s.h, s.l);
+  s.l = s.l + t.l;
+  return quick_two_sum(s.h, s.l);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  ff p = two_prod(a.h, b.h);
+  p.l = p.l + (a.h * b.l + a.l * b.h);
+  return quick_two_sum(p.h, p.l);
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+  ff p = two_prod(a.h, b);
+  p.l = p.l + a.l * b;
+  return quick_two_sum(p.h, p.l);
+}
+__device__ __forceinline__ ff ff_div_f(ff a, float b) {
+  const float q1 = a.h / b;
+  const ff p = two_prod(q1, b);
+  ff r = two_sum(a.h, -p.h);
+  r.l = (r.l - p.l) + a.l;
+  const float q2 = (r.h + r.l) / b;
+  return quick_two_sum(q1, q2);
+}
+__device__ __forceinline__ double ff_d(ff a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ ff d_ff(double d) {
+  const float h = (float)d;
+  return ff{h, (float)(d - (double)h)};
+}
+__device__ __forceinline__ ff warp_sum_ff(ff v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const ff w{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+    v = ff_add(v, w);
+  }
+  return v;
 }
 
 // Per-thread sum of float products as an unevaluated pair h + l: each

@@ -616,61 +616,6 @@ __global__ void __launch_bounds__(256, 3) k_mg0_up(Lev0 F, const float* __restri
 // CTA.  The iterates agree with an IEEE-double CG to ~1e-14 relative, far
 // below the float resolution of the result; the stopping rule, iteration
 // limit and order of operations are the reference's.
-struct ff {
-  float h, l;
-};
-__device__ __forceinline__ ff two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  return ff{s, (a - (s - bb)) + (b - bb)};
-}
-__device__ __forceinline__ ff quick_two_sum(float a, float b) {  // |a| >= |b|
-  const float s = a + b;
-  return ff{s, b - (s - a)};
-}
-__device__ __forceinline__ ff two_prod(float a, float b) {
-  const float p = a * b;
-  return ff{p, fmaf(a, b, -p)};
-}
-__device__ __forceinline__ ff ff_add(ff a, ff b) {
-  ff s = two_sum(a.h, b.h);
-  const ff t = two_sum(a.l, b.l);
-  s.l = s.l + t.h;
-  s = quick_two_sum(s.h, s.l);
-  s.l = s.l + t.l;
-  return quick_two_sum(s.h, s.l);
-}
-__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
-__device__ __forceinline__ ff ff_mul(ff a, ff b) {
-  ff p = two_prod(a.h, b.h);
-  p.l = p.l + (a.h * b.l + a.l * b.h);
-  return quick_two_sum(p.h, p.l);
-}
-__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
-  ff p = two_prod(a.h, b);
-  p.l = p.l + a.l * b;
-  return quick_two_sum(p.h, p.l);
-}
-__device__ __forceinline__ ff ff_div_f(ff a, float b) {
-  const float q1 = a.h / b;
-  const ff p = two_prod(q1, b);
-  ff r = two_sum(a.h, -p.h);
-  r.l = (r.l - p.l) + a.l;
-  const float q2 = (r.h + r.l) / b;
-  return quick_two_sum(q1, q2);
-}
-__device__ __forceinline__ double ff_d(ff a) { return (double)a.h + (double)a.l; }
-__device__ __forceinline__ ff d_ff(double d) {
-  const float h = (float)d;
-  return ff{h, (float)(d - (double)h)};
-}
-__device__ __forceinline__ ff warp_sum_ff(ff v) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const ff w{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
-    v = ff_add(v, w);
-  }
-  return v;
-}
 // CTA sum of NV pairs per thread in a fixed order; the sums are valid in
 // thread 0 after the call (the caller publishes derived scalars)
 template <int NV>

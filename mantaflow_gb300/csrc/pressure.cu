@@ -1009,40 +1009,89 @@ __global__ void __launch_bounds__(256) k_b_pcg_init(const BTile* __restrict__ ti
   }
   const double b = block_sum(acc.value());
   if (lin_tid() == 0) sc.part[tl.local] = b;
-  if (last_block(&sc.sc->counters[0], sc.ntiles)) {
+  if (last_block(&sc.sc->counters[0], tl.count)) {
     const double s2 = sum_partials(sc.part, sc.ntiles);
     if (lin_tid() == 0) sc.sc->sigma = (float)s2;
   }
 }
 
+// The CG sweep kernels take tiles R row-groups tall (32 x 8R cells per CTA,
+// R chosen by the batch's autotuner).  Reductions stay on the 32 x 8
+// sub-tile grid of R = 1: sub-tile r of a tile writes the slot the R = 1
+// tile at that place would, summed over the same thread order, so results
+// do not depend on R.
+#define BATCH_ROWS                                                        \
+  const BTile tl = tiles[blockIdx.x];                                     \
+  const BScene& sc = S[tl.scene];                                         \
+  const Dims d = sc.d;                                                    \
+  const int txc = (d.nx + kBTX - 1) / kBTX, tyc = (d.ny + kBTY - 1) / kBTY; \
+  const int i = tl.x0 + threadIdx.x, k = tl.z;                            \
+  const int yt0 = tl.y0 / kBTY;
+
+__device__ __forceinline__ int sub_slot(int txc, int tyc, int x0, int yt, int z) { return x0 / kBTX + txc * (yt + tyc * z); }
+
+// per 32 x 8 sub-tile sums of one float per thread: warp sums in
+// double-float, the 8 warp sums added in warp order by thread r, written
+// to slot[r] as a double.  Sub-tiles past the grid (valid[r] false) write
+// nothing.
+template <int R>
+__device__ __forceinline__ void subtile_sums(const float* v, double* part, const int* slot, const bool* valid) {
+  __shared__ ff wsum[R][8];
+  const int lane = lin_tid() & 31, wid = lin_tid() >> 5;
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const ff a = warp_sum_ff(ff{v[r], 0.f});
+    if (lane == 0) wsum[r][wid] = a;
+  }
+  __syncthreads();
+  if (lin_tid() < R) {
+    const int r = lin_tid();
+    if (valid[r]) {
+      ff t{0.f, 0.f};
+      for (int w = 0; w < 8; w++) t = ff_add(t, wsum[r][w]);
+      part[slot[r]] = ff_d(t);
+    }
+  }
+}
+
 // tmp = A s (ApplyMatrix) and dot(tmp, s) -> alpha
+template <int R>
 __global__ void __launch_bounds__(256) k_b_pcg_spmv(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
-  BATCH_TILE
+  BATCH_ROWS
   CgScalars* g = sc.sc;
   if (g->done) return;
-  FSum acc;
-  if (in) {
-    const int c = sc.code[idx];
-    const float* x = sc.search;
-    const float xc = x[idx];
-    float v;
-    if (!(c & kCodeFluid)) {
-      v = xc;
-    } else {
-      v = xc * (float)(c & 7);
-      if (c & kLowX) v = v - x[idx - 1];
-      if (c & kHighX) v = v - x[idx + 1];
-      if (c & kLowY) v = v - x[idx - d.sy];
-      if (c & kHighY) v = v - x[idx + d.sy];
-      if (c & kLowZ) v = v - x[idx - d.sz];
-      if (c & kHighZ) v = v - x[idx + d.sz];
+  float pv[R];
+  int slot[R];
+  bool valid[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    valid[r] = yt0 + r < tyc;
+    slot[r] = sub_slot(txc, tyc, tl.x0, yt0 + r, k);
+    const int j = tl.y0 + kBTY * r + threadIdx.y;
+    pv[r] = 0.f;
+    if (valid[r] && i < d.nx && j < d.ny) {
+      const long long idx = ix(d, i, j, k);
+      const int c = sc.code[idx];
+      const float* x = sc.search;
+      const float xc = x[idx];
+      float v;
+      if (!(c & kCodeFluid)) {
+        v = xc;
+      } else {
+        v = xc * (float)(c & 7);
+        if (c & kLowX) v = v - x[idx - 1];
+        if (c & kHighX) v = v - x[idx + 1];
+        if (c & kLowY) v = v - x[idx - d.sy];
+        if (c & kHighY) v = v - x[idx + d.sy];
+        if (c & kLowZ) v = v - x[idx - d.sz];
+        if (c & kHighZ) v = v - x[idx + d.sz];
+      }
+      sc.tmp[idx] = v;
+      pv[r] = v * xc;
     }
-    sc.tmp[idx] = v;
-    acc.add(v * xc);
   }
-  const double b = block_sum(acc.value());
-  if (lin_tid() == 0) sc.part[tl.local] = b;
-  if (last_block(&g->counters[1], sc.ntiles)) {
+  subtile_sums<R>(pv, sc.part, slot, valid);
+  if (last_block(&g->counters[1], tl.count)) {
     const double s2 = sum_partials(sc.part, sc.ntiles);
     if (lin_tid() == 0) {
       const float dp = (float)s2;
@@ -1054,38 +1103,54 @@ __global__ void __launch_bounds__(256) k_b_pcg_spmv(const BTile* __restrict__ ti
 
 // x += alpha s, r -= alpha tmp, z = r (PcNone), resNorm = max|r| and the
 // convergence test; then sigmaNew = dot(z, r) and beta (GridCg::iterate)
+template <int R>
 __global__ void __launch_bounds__(256) k_b_pcg_axpy(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
                                                     int* ndone) {
-  BATCH_TILE
+  BATCH_ROWS
   CgScalars* g = sc.sc;
   if (g->done) return;
   const float alpha = g->alpha, na = -alpha;
-  float mx = 0.f;
-  FSum acc;
-  if (in) {
-    sc.pres[idx] = sc.pres[idx] + alpha * sc.search[idx];
-    const float rv = sc.res[idx] + na * sc.tmp[idx];
-    sc.res[idx] = rv;
-    sc.tmp[idx] = rv;
-    mx = fabsf(rv);
-    acc.add(rv * rv);
+  float sq[R], mx[R];
+  int slot[R];
+  bool valid[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    valid[r] = yt0 + r < tyc;
+    slot[r] = sub_slot(txc, tyc, tl.x0, yt0 + r, k);
+    const int j = tl.y0 + kBTY * r + threadIdx.y;
+    sq[r] = 0.f;
+    mx[r] = 0.f;
+    if (valid[r] && i < d.nx && j < d.ny) {
+      const long long idx = ix(d, i, j, k);
+      sc.pres[idx] = sc.pres[idx] + alpha * sc.search[idx];
+      const float rv = sc.res[idx] + na * sc.tmp[idx];
+      sc.res[idx] = rv;
+      sc.tmp[idx] = rv;
+      mx[r] = fabsf(rv);
+      sq[r] = rv * rv;
+    }
   }
-  const double b = block_sum(acc.value());
-  __shared__ float smx[32];
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((lin_tid() & 31) == 0) smx[lin_tid() >> 5] = mx;
-  __syncthreads();
-  if (lin_tid() == 0) {
+  // max |r| per sub-tile, then the dot sums
+  __shared__ float smx[R][8];
+  const int lane = lin_tid() & 31, wid = lin_tid() >> 5;
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    float m = mx[r];
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) smx[r][wid] = m;
+  }
+  subtile_sums<R>(sq, sc.part, slot, valid);  // its barrier also publishes smx
+  if (lin_tid() < R && valid[lin_tid()]) {
+    const int r = lin_tid();
     float m = 0.f;
-    for (int q = 0; q < nwarps(); q++) m = fmaxf(m, smx[q]);
-    sc.part[tl.local] = b;
-    sc.part[sc.ntiles + tl.local] = (double)m;
+    for (int w = 0; w < 8; w++) m = fmaxf(m, smx[r][w]);
+    sc.part[sc.ntiles + slot[r]] = (double)m;
   }
-  if (last_block(&g->counters[2], sc.ntiles)) {
+  if (last_block(&g->counters[2], tl.count)) {
     const double s2 = sum_partials(sc.part, sc.ntiles);
+    const double mxp = max_partials(sc.part + sc.ntiles, sc.ntiles);
     if (lin_tid() != 0) return;
-    float res = 0.f;
-    for (int q = 0; q < sc.ntiles; q++) res = fmaxf(res, (float)__ldcg(sc.part + sc.ntiles + q));
+    const float res = (float)mxp;
     g->iterations += 1;
     g->resNorm = res;
     if (res < g->accuracy) {
@@ -1109,12 +1174,23 @@ __global__ void __launch_bounds__(256) k_b_pcg_axpy(const BTile* __restrict__ ti
 }
 
 // s = z + beta s (UpdateSearchVec)
+template <int R>
 __global__ void __launch_bounds__(256) k_b_pcg_update(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
-  BATCH_TILE
-  if (!in || sc.sc->done) return;
+  BATCH_ROWS
+  (void)txc;
+  if (sc.sc->done) return;
   const float beta = sc.sc->beta;
-  sc.search[idx] = sc.tmp[idx] + beta * sc.search[idx];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    if (yt0 + r >= tyc) break;
+    const int j = tl.y0 + kBTY * r + threadIdx.y;
+    if (i < d.nx && j < d.ny) {
+      const long long idx = ix(d, i, j, k);
+      sc.search[idx] = sc.tmp[idx] + beta * sc.search[idx];
+    }
+  }
 }
+#undef BATCH_ROWS
 
 __global__ void __launch_bounds__(256) k_b_correct(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int nxt) {
   BATCH_TILE
@@ -1130,14 +1206,23 @@ void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, c
   count_launch();
   k_b_pcg_init<<<nt, b, 0, st>>>(t, s);
 }
-void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, cudaStream_t st) {
+template <int R>
+static void pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, cudaStream_t st) {
   const dim3 b(kBTX, kBTY, 1);
   count_launch();
-  k_b_pcg_spmv<<<nt, b, 0, st>>>(t, s);
+  k_b_pcg_spmv<R><<<nt, b, 0, st>>>(t, s);
   count_launch();
-  k_b_pcg_axpy<<<nt, b, 0, st>>>(t, s, ndone);
+  k_b_pcg_axpy<R><<<nt, b, 0, st>>>(t, s, ndone);
   count_launch();
-  k_b_pcg_update<<<nt, b, 0, st>>>(t, s);
+  k_b_pcg_update<R><<<nt, b, 0, st>>>(t, s);
+}
+void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int rows, int* ndone, cudaStream_t st) {
+  switch (rows) {
+    case 1: pcg_iteration<1>(t, nt, s, ndone, st); break;
+    case 2: pcg_iteration<2>(t, nt, s, ndone, st); break;
+    case 4: pcg_iteration<4>(t, nt, s, ndone, st); break;
+    default: pcg_iteration<8>(t, nt, s, ndone, st); break;
+  }
 }
 void launch_b_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
   count_launch();

@@ -66,11 +66,8 @@ __global__ void __launch_bounds__(256) k_residual64(Dims d, const code_t* __rest
     part[blockIdx.x] = m;
   }
   if (last_block(counter, gridDim.x)) {
-    if (threadIdx.x == 0) {
-      double m = 0.;
-      for (unsigned int q = 0; q < gridDim.x; q++) m = fmax(m, __ldcg(part + q));
-      *norm = m;
-    }
+    const double m = max_partials(part, gridDim.x);
+    if (threadIdx.x == 0) *norm = m;
   }
 }
 
