@@ -263,6 +263,42 @@ int mg_batch_info(mg_batch b, int* count, long long* cells, long long* tiles, si
 int mg_batch_tuning(mg_batch b, int* sweepRows, float* ms);
 int mg_batch_sync(mg_batch b);
 
+/* ---- served form (no counterpart in the reference) ----------------------- */
+/* A request loop for plume jobs (the batched form's scene, run for a number
+ * of steps): jobs arrive at given times and are admitted in arrival order
+ * once arrived and once their device memory (mg_serve_job_bytes) fits the
+ * budget; every tick advances all resident jobs by one step in one batched
+ * step; a finished job leaves and frees its memory for the next.  A job's
+ * results depend only on its own scene: the same alone and in any mix. */
+typedef struct mg_server_s* mg_server;
+typedef struct {
+  int jobs;
+  long long ticks;
+  double wallSeconds;        /* from the start of mg_serve_run to the last job's end */
+  long long cellSteps;       /* sum over jobs of cells x steps */
+  size_t peakBytes;          /* largest device memory held by resident jobs */
+} mg_serve_stats;
+typedef struct {
+  double arrival, admitted, finished;  /* seconds after the start of the run */
+  int steps;
+  double meanStepMs;         /* mean tick duration over the job's steps */
+} mg_serve_job;
+int mg_serve_create(size_t budgetBytes, float dt, mg_server* out);
+int mg_serve_destroy(mg_server s);
+int mg_serve_set_solver(mg_server s, float cgAccuracy, float cgMaxIterFac);
+size_t mg_serve_job_bytes(int nx, int ny, int nz);
+/* a job of `steps` plume steps on an nx x ny x nz grid (nz = 1: 2D) arriving
+ * `arrival` seconds after mg_serve_run starts; keepResult copies its final
+ * density, velocity and pressure to the host when it finishes */
+int mg_serve_submit(mg_server s, int nx, int ny, int nz, const float* gravity, unsigned long long seed, int steps,
+                    double arrival, int keepResult, int* job);
+/* run until every submitted job has finished */
+int mg_serve_run(mg_server s, mg_serve_stats* stats);
+int mg_serve_job_info(mg_server s, int job, mg_serve_job* info);
+int mg_serve_job_result(mg_server s, int job, int what, void* host, size_t bytes);
+/* tick durations and resident job counts (count: in capacity, out total) */
+int mg_serve_ticks(mg_server s, int* count, float* ms, int* jobs);
+
 /* ---- timing (CUDA events on the solver's stream) ------------------------- */
 /* per-kernel-family device time accumulated while profiling is on */
 int mg_profile_enable(mg_solver s, int on);

@@ -29,6 +29,16 @@ class BatchStats(C.Structure):
                 ("diverged", C.c_int)]
 
 
+class ServeStats(C.Structure):
+    _fields_ = [("jobs", C.c_int), ("ticks", C.c_longlong), ("wallSeconds", C.c_double), ("cellSteps", C.c_longlong),
+                ("peakBytes", C.c_size_t)]
+
+
+class ServeJob(C.Structure):
+    _fields_ = [("arrival", C.c_double), ("admitted", C.c_double), ("finished", C.c_double), ("steps", C.c_int),
+                ("meanStepMs", C.c_double)]
+
+
 class RefineParams(C.Structure):
     _fields_ = [("refineAccuracy", C.c_double), ("innerAccuracy", C.c_double), ("maxRefine", C.c_int)]
 
@@ -92,6 +102,15 @@ SIGNATURES = [
                            C.POINTER(C.c_size_t)]),
     ("mg_batch_sync", _I, [_P]),
     ("mg_batch_tuning", _I, [_P, C.POINTER(_I), _FP]),
+    ("mg_serve_create", _I, [C.c_size_t, _F, C.POINTER(_P)]),
+    ("mg_serve_destroy", _I, [_P]),
+    ("mg_serve_set_solver", _I, [_P, _F, _F]),
+    ("mg_serve_job_bytes", C.c_size_t, [_I, _I, _I]),
+    ("mg_serve_submit", _I, [_P, _I, _I, _I, _FP, C.c_ulonglong, _I, C.c_double, _I, C.POINTER(_I)]),
+    ("mg_serve_run", _I, [_P, C.POINTER(ServeStats)]),
+    ("mg_serve_job_info", _I, [_P, _I, C.POINTER(ServeJob)]),
+    ("mg_serve_job_result", _I, [_P, _I, _I, _P, C.c_size_t]),
+    ("mg_serve_ticks", _I, [_P, C.POINTER(_I), _FP, C.POINTER(_I)]),
     ("mg_compute_pressure_rhs", _I, [_P, _P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P, _P]),
     ("mg_solve_pressure_system", _I, [_P, _P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P,
                                       C.POINTER(PressureResult)]),

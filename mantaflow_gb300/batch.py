@@ -101,3 +101,69 @@ class BatchedPlumes:
             self.close()
         except Exception:
             pass
+
+
+class PlumeServer:
+    """Served form: a request loop for plume jobs with device-memory
+    admission and continuous batching (mg_serve_* of include/mantagpu.h)."""
+
+    def __init__(self, budget_bytes=150 * 10 ** 9, dt=1.0, cgAccuracy=1e-3, cgMaxIterFac=1.5):
+        ensure_init()
+        self._L = _lib.load()
+        h = C.c_void_p()
+        check(self._L.mg_serve_create(int(budget_bytes), float(dt), C.byref(h)))
+        self._h = h
+        check(self._L.mg_serve_set_solver(h, float(cgAccuracy), float(cgMaxIterFac)))
+        self.shapes = []
+
+    @staticmethod
+    def job_bytes(size):
+        nx, ny, nz = (tuple(size) + (1,))[:3]
+        return int(_lib.load().mg_serve_job_bytes(nx, ny, nz))
+
+    def submit(self, size, gravity, seed, steps, arrival=0.0, keep=False):
+        nx, ny, nz = (tuple(int(v) for v in size) + (1,))[:3]
+        g = (C.c_float * 3)(*[float(v) for v in gravity])
+        jid = C.c_int()
+        check(self._L.mg_serve_submit(self._h, nx, ny, nz, g, C.c_ulonglong(int(seed)), int(steps), float(arrival),
+                                      int(bool(keep)), C.byref(jid)))
+        self.shapes.append((nz, ny, nx))
+        return jid.value
+
+    def run(self):
+        st = _lib.ServeStats()
+        check(self._L.mg_serve_run(self._h, C.byref(st)))
+        return {"jobs": st.jobs, "ticks": st.ticks, "wall_s": st.wallSeconds, "cell_steps": st.cellSteps,
+                "peak_bytes": st.peakBytes}
+
+    def job(self, jid):
+        j = _lib.ServeJob()
+        check(self._L.mg_serve_job_info(self._h, int(jid), C.byref(j)))
+        return {"arrival": j.arrival, "admitted": j.admitted, "finished": j.finished, "steps": j.steps,
+                "mean_step_ms": j.meanStepMs}
+
+    def result(self, jid, what):
+        shape = self.shapes[jid] + ((3,) if what == VELOCITY else ())
+        a = np.empty(shape, np.float32)
+        check(self._L.mg_serve_job_result(self._h, int(jid), int(what), a.ctypes.data_as(C.c_void_p), a.nbytes))
+        return a
+
+    def ticks(self):
+        n = C.c_int(0)
+        check(self._L.mg_serve_ticks(self._h, C.byref(n), None, None))
+        ms = (C.c_float * max(1, n.value))()
+        jobs = (C.c_int * max(1, n.value))()
+        cap = C.c_int(n.value)
+        check(self._L.mg_serve_ticks(self._h, C.byref(cap), ms, jobs))
+        return list(ms)[: n.value], list(jobs)[: n.value]
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.mg_serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

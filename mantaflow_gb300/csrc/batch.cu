@@ -1,25 +1,38 @@
-// Batched form of the plume step: many independent scenes of uneven sizes,
-// each stage one launch over all scenes' tiles (mg_batch.h).
+// Batched and served forms of the plume step: many independent scenes of
+// uneven sizes, each stage one launch over all scenes' tiles (mg_batch.h).
 //
-// Memory: one arena per batch.  Per scene (n cells): flags, two velocity
-// buffers (3n, ping-pong), two density buffers, 4n forward/scratch values,
-// the inflow mask, pressure and the CG vectors rhs / residual / search / tmp,
-// plus 2-byte stencil codes: ~80 bytes per cell.  Scenes start on 256-byte
-// boundaries.
+// Engine.  A set of member scenes, each with its own device block: flags,
+// two velocity buffers (3n, ping-pong), two density buffers, 4n forward /
+// scratch values, the inflow mask, pressure, the CG vectors rhs / residual /
+// search / tmp, 2-byte stencil codes and the per-tile partial sums -- about
+// 80 bytes per cell.  Freed blocks are kept in a size-keyed pool.  Members
+// can join and leave between steps (the served form); the tile lists are
+// rebuilt when they do.
 //
 // Step: inflow, advection (forward SL of density and velocity in one pass,
 // MacCormack correction + clamp in the next, outflow BC), setWallBcs +
-// addBuoyancy, then solvePressure: MakeRhs + codes, CG init, CG iterations
-// until every scene has converged, correctVelocity.  CG iterations run over
-// the tiles of the scenes still iterating: the host reads the number of
-// finished scenes every few iterations and, when it changed, drops their
-// tiles from the list.
+// addBuoyancy, then solvePressure: MakeRhs + codes, CG init, CG sweeps until
+// every member has converged, correctVelocity.  Sweeps run over the tiles of
+// the members still iterating: the host reads the number of finished scenes
+// every few sweeps and, when it changed, drops their tiles.  A scene's
+// results depend only on its own data, so it computes the same alone and in
+// any mix.
+//
+// Served form.  Jobs (a plume scene run for a number of steps) arrive at
+// given times; a job is admitted in arrival order once it has arrived and
+// its block fits the device-memory budget; every tick advances all resident
+// jobs by one step together (continuous batching); a finished job leaves
+// (its final fields copied to the host if requested) and its block returns
+// to the pool for the next one.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mantagpu.h"
@@ -27,33 +40,7 @@
 
 using namespace mgpu;
 
-struct mg_batch_s {
-  int count = 0;
-  float dt = 1.f;
-  cudaStream_t stream = nullptr;
-  unsigned char* arena = nullptr;
-  size_t arenaBytes = 0;
-  std::vector<BScene> scenes;     // host copy of the table
-  BScene* dScenes = nullptr;
-  std::vector<BTile> tiles;       // all 32 x 8 tiles, scene-major
-  std::vector<int> tileStart;     // first tile of each scene
-  BTile* dTiles = nullptr;
-  // CG sweep tiles 32 x 8R cells for R = 1, 2, 4, 8 (rowsK[k] = 1 << k)
-  std::vector<BTile> tilesR[4];
-  std::vector<int> startR[4];
-  BTile* dActive = nullptr;       // sweep tiles of the scenes still iterating
-  int rowsK = -1;                 // autotuned sweep tile height (index), -1 until chosen
-  float tuneMs[4] = {0.f, 0.f, 0.f, 0.f};
-  cudaEvent_t ev[2] = {nullptr, nullptr};
-  CgScalars* dSc = nullptr;
-  std::vector<CgScalars> hSc;
-  int* dDone = nullptr;
-  int cur = 0;
-  int step = 0;
-  float cgAccuracy = 1e-3f;
-  float cgMaxIterFac = 1.5f;
-  int lag = 8;
-};
+namespace {
 
 #define CKB(call)                                                                                  \
   do {                                                                                             \
@@ -61,250 +48,343 @@ struct mg_batch_s {
     if (e_ != cudaSuccess) return set_error(MG_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
   } while (0)
 
-static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-extern "C" int mg_batch_create(int count, const int* sizes, const float* gravity, const unsigned long long* seeds, float dt,
-                               mg_batch* out) {
-  if (!library_ready()) return set_error(MG_ERR_STATE, "mg_init has not been called");
-  if (count < 1 || !sizes || !gravity || !seeds || !out) return set_error(MG_ERR_ARG, "mg_batch_create: invalid argument");
-  auto b = new mg_batch_s();
-  b->count = count;
-  b->dt = dt;
-  // layout
-  std::vector<size_t> off(count);
-  size_t total = 0;
-  for (int q = 0; q < count; q++) {
-    const int nx = sizes[3 * q], ny = sizes[3 * q + 1], nz = sizes[3 * q + 2];
-    if (nx < 3 || ny < 3 || nz < 1 || (nz > 1 && nz < 3)) {
-      delete b;
-      return set_error(MG_ERR_ARG, "mg_batch_create: scene " + std::to_string(q) + " is too small");
+int tiles_of(int nx, int ny, int nz, int rows) { return ((nx + kBTX - 1) / kBTX) * ((ny + rows - 1) / rows) * nz; }
+
+// bytes of one scene's device block
+size_t scene_bytes(int nx, int ny, int nz) {
+  const size_t n = (size_t)nx * ny * nz;
+  return align256(n * sizeof(int)) + 2 * align256(3 * n * sizeof(float)) + 2 * align256(n * sizeof(float)) +
+         align256(4 * n * sizeof(float)) + 6 * align256(n * sizeof(float)) + align256(n * sizeof(code_t)) +
+         align256(2 * (size_t)tiles_of(nx, ny, nz, kBTY) * sizeof(double));
+}
+
+struct SceneRec {
+  BScene s;
+  void* mem = nullptr;
+  size_t bytes = 0;
+  int step = 0;  // steps taken: the inflow noise index
+  int cur = 0;   // which ping-pong buffers are current
+};
+
+struct Engine {
+  cudaStream_t stream = nullptr;
+  float dt = 1.f;
+  float cgAccuracy = 1e-3f, cgMaxIterFac = 1.5f;
+  int lag = 8;
+  std::vector<SceneRec*> members;
+  std::multimap<size_t, void*> pool;
+  size_t liveBytes = 0;
+  // device tables
+  BScene* dScenes = nullptr;
+  size_t scenesCap = 0;
+  CgScalars* dSc = nullptr;
+  size_t scCap = 0;
+  std::vector<CgScalars> hSc;
+  std::vector<BScene> hScenes;
+  // tiles: 32 x 8 for the stages; 32 x 8R (R = 1 << k) for the CG sweeps
+  std::vector<BTile> tiles1;
+  std::vector<BTile> tilesR[4];
+  std::vector<int> startR[4];
+  BTile* dTiles = nullptr;
+  size_t tilesCap = 0;
+  BTile* dActive = nullptr;
+  size_t activeCap = 0;
+  bool dirty = true;
+  int rowsK = -1;
+  float tuneMs[4] = {0.f, 0.f, 0.f, 0.f};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  int* dDone = nullptr;
+
+  ~Engine() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto* m : members) {
+      cudaFree(m->mem);
+      delete m;
     }
-    const size_t n = (size_t)nx * ny * nz;
-    const int ntiles = ((nx + kBTX - 1) / kBTX) * ((ny + kBTY - 1) / kBTY) * nz;
-    off[q] = total;
-    total += align256(n * sizeof(int));                  // flags
-    total += 2 * align256(3 * n * sizeof(float));        // vel[2]
-    total += 2 * align256(n * sizeof(float));            // dens[2]
-    total += align256(4 * n * sizeof(float));            // fwd
-    total += 6 * align256(n * sizeof(float));            // mask, pres, rhs, res, search, tmp
-    total += align256(n * sizeof(code_t));               // code
-    total += align256(2 * (size_t)ntiles * sizeof(double));  // part
+    for (auto& kv : pool) cudaFree(kv.second);
+    cudaFree(dScenes);
+    cudaFree(dSc);
+    cudaFree(dTiles);
+    cudaFree(dActive);
+    cudaFree(dDone);
+    if (ev[0]) cudaEventDestroy(ev[0]);
+    if (ev[1]) cudaEventDestroy(ev[1]);
+    if (stream) cudaStreamDestroy(stream);
   }
-  b->arenaBytes = total;
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&b->arena, total) != cudaSuccess) {
-    if (b->stream) cudaStreamDestroy(b->stream);
-    delete b;
+};
+
+int engine_init(Engine& e, float dt) {
+  e.dt = dt;
+  CKB(cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking));
+  CKB(cudaEventCreate(&e.ev[0]));
+  CKB(cudaEventCreate(&e.ev[1]));
+  CKB(cudaMalloc(&e.dDone, sizeof(int)));
+  return MG_OK;
+}
+
+void* pool_take(Engine& e, size_t bytes) {
+  auto it = e.pool.find(bytes);
+  if (it != e.pool.end()) {
+    void* p = it->second;
+    e.pool.erase(it);
+    return p;
+  }
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
     cudaGetLastError();
-    return set_error(MG_ERR_NOMEM, "mg_batch_create: out of device memory");
-  }
-  cudaMemsetAsync(b->arena, 0, total, b->stream);
-  CKB(cudaMalloc(&b->dSc, sizeof(CgScalars) * count));
-  CKB(cudaMemset(b->dSc, 0, sizeof(CgScalars) * count));
-  CKB(cudaMalloc(&b->dDone, sizeof(int)));
-  b->hSc.assign(count, CgScalars{});
-  b->scenes.resize(count);
-  for (int q = 0; q < count; q++) {
-    const int nx = sizes[3 * q], ny = sizes[3 * q + 1], nz = sizes[3 * q + 2];
-    BScene& s = b->scenes[q];
-    s.d.nx = nx;
-    s.d.ny = ny;
-    s.d.nz = nz;
-    s.d.is3d = nz > 1;
-    s.d.n = (long long)nx * ny * nz;
-    s.d.sy = nx;
-    s.d.sz = s.d.is3d ? (long long)nx * ny : 0;
-    const size_t n = (size_t)s.d.n;
-    const int ntiles = ((nx + kBTX - 1) / kBTX) * ((ny + kBTY - 1) / kBTY) * nz;
-    unsigned char* p = b->arena + off[q];
-    auto take = [&](size_t bytes) {
-      unsigned char* r = p;
-      p += align256(bytes);
-      return r;
-    };
-    s.flags = (int*)take(n * sizeof(int));
-    s.vel[0] = (float*)take(3 * n * sizeof(float));
-    s.vel[1] = (float*)take(3 * n * sizeof(float));
-    s.dens[0] = (float*)take(n * sizeof(float));
-    s.dens[1] = (float*)take(n * sizeof(float));
-    s.fwd = (float*)take(4 * n * sizeof(float));
-    s.mask = (float*)take(n * sizeof(float));
-    s.pres = (float*)take(n * sizeof(float));
-    s.rhs = (float*)take(n * sizeof(float));
-    s.res = (float*)take(n * sizeof(float));
-    s.search = (float*)take(n * sizeof(float));
-    s.tmp = (float*)take(n * sizeof(float));
-    s.code = (code_t*)take(n * sizeof(code_t));
-    s.part = (double*)take(2 * (size_t)ntiles * sizeof(double));
-    s.sc = b->dSc + q;
-    s.dt = dt;
-    s.seed = seeds[q];
-    s.ntiles = ntiles;
-    // addBuoyancy(gravity, scale=True, coefficient=1): f = -g*dt/dx, 0.5*f
-    const int m = std::max(nx, std::max(ny, nz));
-    const float gridScale = (float)(1.0 / (double)m);
-    s.bx = 0.5f * (((-gravity[3 * q]) * dt) / gridScale * 1.f);
-    s.by = 0.5f * (((-gravity[3 * q + 1]) * dt) / gridScale * 1.f);
-    s.bz = 0.5f * (((-gravity[3 * q + 2]) * dt) / gridScale * 1.f);
-    // scene setup: initDomain(boundaryWidth=0) walls, fillGrid,
-    // setOpenBound(0, 'Y', Outflow|Empty), the cylinder source
-    const int wz = s.d.is3d ? kObstacle : 0;  // initDomain sets no z sides in 2D
-    const int types[6] = {kObstacle, kObstacle, kObstacle, kObstacle, wz, wz};
-    launch_init_domain(s.d, s.flags, 0, types, b->stream);
-    launch_fill_grid(s.d, s.flags, kFluid, b->stream);
-    const int lo[3] = {0, 0, 0}, up[3] = {0, 1, 0};
-    launch_set_open_bound(s.d, s.flags, 0, lo, up, kOutflow | kEmpty, b->stream);
-    // Cylinder(center = gs*(0.5,0.1,0.5), radius = 0.14*nx, z = gs*(0,0.02,0))
-    const float gs[3] = {(float)nx, (float)ny, (float)nz};
-    const float center[3] = {gs[0] * 0.5f, gs[1] * 0.1f, gs[2] * 0.5f};
-    const float zdir[3] = {gs[0] * 0.f, gs[1] * 0.02f, gs[2] * 0.f};
-    float zn[3], mZ;
-    cylinder_axis(zdir, zn, &mZ);
-    const float one[3] = {1.f, 0.f, 0.f};
-    launch_shape_apply(s.d, 1, s.mask, nullptr, nullptr, one, 0, nullptr, center, zn, (float)(nx * 0.14), mZ, b->stream);
-    b->tileStart.push_back((int)b->tiles.size());
-    int local = 0;
-    for (int z = 0; z < nz; z++)
-      for (int y = 0; y < ny; y += kBTY)
-        for (int x = 0; x < nx; x += kBTX) b->tiles.push_back(BTile{q, x, y, z, local++, ntiles});
-    for (int kk = 0; kk < 4; kk++) {
-      const int rows = kBTY << kk;
-      const int cnt = ((nx + kBTX - 1) / kBTX) * ((ny + rows - 1) / rows) * nz;
-      b->startR[kk].push_back((int)b->tilesR[kk].size());
-      int l = 0;
-      for (int z = 0; z < nz; z++)
-        for (int y = 0; y < ny; y += rows)
-          for (int x = 0; x < nx; x += kBTX) b->tilesR[kk].push_back(BTile{q, x, y, z, l++, cnt});
+    // return the pooled blocks to the device and retry once
+    cudaStreamSynchronize(e.stream);
+    for (auto& kv : e.pool) cudaFree(kv.second);
+    e.pool.clear();
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
     }
   }
-  b->tileStart.push_back((int)b->tiles.size());
-  for (int kk = 0; kk < 4; kk++) b->startR[kk].push_back((int)b->tilesR[kk].size());
-  CKB(cudaEventCreate(&b->ev[0]));
-  CKB(cudaEventCreate(&b->ev[1]));
-  CKB(cudaMalloc(&b->dScenes, sizeof(BScene) * count));
-  CKB(cudaMemcpyAsync(b->dScenes, b->scenes.data(), sizeof(BScene) * count, cudaMemcpyHostToDevice, b->stream));
-  CKB(cudaMalloc(&b->dTiles, sizeof(BTile) * b->tiles.size()));
-  CKB(cudaMalloc(&b->dActive, sizeof(BTile) * b->tiles.size()));
-  CKB(cudaMemcpyAsync(b->dTiles, b->tiles.data(), sizeof(BTile) * b->tiles.size(), cudaMemcpyHostToDevice, b->stream));
-  CKB(cudaStreamSynchronize(b->stream));
+  return p;
+}
+
+// a plume scene joins the engine: device block, flags and source set up
+int scene_add(Engine& e, int nx, int ny, int nz, const float* gravity, unsigned long long seed, SceneRec** out) {
+  if (nx < 3 || ny < 3 || nz < 1 || (nz > 1 && nz < 3)) return set_error(MG_ERR_ARG, "plume scene is too small");
+  auto r = new SceneRec();
+  r->bytes = scene_bytes(nx, ny, nz);
+  r->mem = pool_take(e, r->bytes);
+  if (!r->mem) {
+    delete r;
+    return set_error(MG_ERR_NOMEM, "plume scene: out of device memory");
+  }
+  e.liveBytes += r->bytes;
+  CKB(cudaMemsetAsync(r->mem, 0, r->bytes, e.stream));
+  BScene& s = r->s;
+  s.d.nx = nx;
+  s.d.ny = ny;
+  s.d.nz = nz;
+  s.d.is3d = nz > 1;
+  s.d.n = (long long)nx * ny * nz;
+  s.d.sy = nx;
+  s.d.sz = s.d.is3d ? (long long)nx * ny : 0;
+  const size_t n = (size_t)s.d.n;
+  unsigned char* p = (unsigned char*)r->mem;
+  auto take = [&](size_t bytes) {
+    unsigned char* q = p;
+    p += align256(bytes);
+    return q;
+  };
+  s.flags = (int*)take(n * sizeof(int));
+  s.vel[0] = (float*)take(3 * n * sizeof(float));
+  s.vel[1] = (float*)take(3 * n * sizeof(float));
+  s.dens[0] = (float*)take(n * sizeof(float));
+  s.dens[1] = (float*)take(n * sizeof(float));
+  s.fwd = (float*)take(4 * n * sizeof(float));
+  s.mask = (float*)take(n * sizeof(float));
+  s.pres = (float*)take(n * sizeof(float));
+  s.rhs = (float*)take(n * sizeof(float));
+  s.res = (float*)take(n * sizeof(float));
+  s.search = (float*)take(n * sizeof(float));
+  s.tmp = (float*)take(n * sizeof(float));
+  s.code = (code_t*)take(n * sizeof(code_t));
+  s.ntiles = tiles_of(nx, ny, nz, kBTY);
+  s.part = (double*)take(2 * (size_t)s.ntiles * sizeof(double));
+  s.sc = nullptr;
+  s.dt = e.dt;
+  s.seed = seed;
+  s.step = 0;
+  // addBuoyancy(gravity, scale=True, coefficient=1): f = -g*dt/dx, 0.5*f
+  const int m = std::max(nx, std::max(ny, nz));
+  const float gridScale = (float)(1.0 / (double)m);
+  const float dt = e.dt;
+  s.bx = 0.5f * (((-gravity[0]) * dt) / gridScale * 1.f);
+  s.by = 0.5f * (((-gravity[1]) * dt) / gridScale * 1.f);
+  s.bz = 0.5f * (((-gravity[2]) * dt) / gridScale * 1.f);
+  // initDomain(boundaryWidth=0) walls, fillGrid, setOpenBound(0, 'Y',
+  // Outflow|Empty), Cylinder(center = gs*(0.5,0.1,0.5), radius = 0.14*nx,
+  // z = gs*(0,0.02,0)).applyToGrid(mask, 1)
+  const int wz = s.d.is3d ? kObstacle : 0;  // initDomain sets no z sides in 2D
+  const int types[6] = {kObstacle, kObstacle, kObstacle, kObstacle, wz, wz};
+  launch_init_domain(s.d, s.flags, 0, types, e.stream);
+  launch_fill_grid(s.d, s.flags, kFluid, e.stream);
+  const int lo[3] = {0, 0, 0}, up[3] = {0, 1, 0};
+  launch_set_open_bound(s.d, s.flags, 0, lo, up, kOutflow | kEmpty, e.stream);
+  const float gs[3] = {(float)nx, (float)ny, (float)nz};
+  const float center[3] = {gs[0] * 0.5f, gs[1] * 0.1f, gs[2] * 0.5f};
+  const float zdir[3] = {gs[0] * 0.f, gs[1] * 0.02f, gs[2] * 0.f};
+  float zn[3], mZ;
+  cylinder_axis(zdir, zn, &mZ);
+  const float one[3] = {1.f, 0.f, 0.f};
+  launch_shape_apply(s.d, 1, s.mask, nullptr, nullptr, one, 0, nullptr, center, zn, (float)(nx * 0.14), mZ, e.stream);
   CKB(cudaGetLastError());
-  *out = b;
+  e.members.push_back(r);
+  e.dirty = true;
+  *out = r;
   return MG_OK;
 }
 
-extern "C" int mg_batch_destroy(mg_batch b) {
-  if (!b) return MG_OK;
-  cudaStreamSynchronize(b->stream);
-  cudaFree(b->arena);
-  cudaFree(b->dScenes);
-  cudaFree(b->dTiles);
-  cudaFree(b->dActive);
-  cudaFree(b->dSc);
-  cudaFree(b->dDone);
-  if (b->ev[0]) cudaEventDestroy(b->ev[0]);
-  if (b->ev[1]) cudaEventDestroy(b->ev[1]);
-  cudaStreamDestroy(b->stream);
-  delete b;
+void scene_remove(Engine& e, SceneRec* r) {
+  e.members.erase(std::find(e.members.begin(), e.members.end(), r));
+  e.pool.emplace(r->bytes, r->mem);
+  e.liveBytes -= r->bytes;
+  delete r;
+  e.dirty = true;
+}
+
+template <typename T>
+int ensure_cap(T** p, size_t* cap, size_t want) {
+  if (*cap >= want) return MG_OK;
+  const size_t c = std::max(want, *cap * 2);
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  CKB(cudaMalloc(p, sizeof(T) * c));
+  *cap = c;
   return MG_OK;
 }
 
-extern "C" int mg_batch_set_solver(mg_batch b, float cgAccuracy, float cgMaxIterFac) {
-  if (!b || !(cgAccuracy > 0.f) || !(cgMaxIterFac > 0.f)) return set_error(MG_ERR_ARG, "mg_batch_set_solver: invalid argument");
-  b->cgAccuracy = cgAccuracy;
-  b->cgMaxIterFac = cgMaxIterFac;
+// scene table (each scene's current buffers presented as index 0, its step
+// index) and, after a membership change, the tile lists
+int engine_tables(Engine& e) {
+  const size_t nm = e.members.size();
+  if (ensure_cap(&e.dScenes, &e.scenesCap, nm) || ensure_cap(&e.dSc, &e.scCap, nm)) return MG_ERR_CUDA;
+  e.hScenes.resize(nm);
+  e.hSc.resize(nm);
+  for (size_t q = 0; q < nm; q++) {
+    BScene s = e.members[q]->s;
+    s.sc = e.dSc + q;
+    s.step = e.members[q]->step;
+    if (e.members[q]->cur) {
+      std::swap(s.vel[0], s.vel[1]);
+      std::swap(s.dens[0], s.dens[1]);
+    }
+    e.hScenes[q] = s;
+  }
+  CKB(cudaMemcpyAsync(e.dScenes, e.hScenes.data(), sizeof(BScene) * nm, cudaMemcpyHostToDevice, e.stream));
+  if (!e.dirty) return MG_OK;
+  e.tiles1.clear();
+  for (int k = 0; k < 4; k++) {
+    e.tilesR[k].clear();
+    e.startR[k].clear();
+  }
+  for (size_t q = 0; q < nm; q++) {
+    const Dims& d = e.members[q]->s.d;
+    const int cnt1 = tiles_of(d.nx, d.ny, d.nz, kBTY);
+    int local = 0;
+    for (int z = 0; z < d.nz; z++)
+      for (int y = 0; y < d.ny; y += kBTY)
+        for (int x = 0; x < d.nx; x += kBTX) e.tiles1.push_back(BTile{(int)q, x, y, z, local++, cnt1});
+    for (int k = 0; k < 4; k++) {
+      const int rows = kBTY << k;
+      const int cnt = tiles_of(d.nx, d.ny, d.nz, rows);
+      e.startR[k].push_back((int)e.tilesR[k].size());
+      int l = 0;
+      for (int z = 0; z < d.nz; z++)
+        for (int y = 0; y < d.ny; y += rows)
+          for (int x = 0; x < d.nx; x += kBTX) e.tilesR[k].push_back(BTile{(int)q, x, y, z, l++, cnt});
+    }
+  }
+  for (int k = 0; k < 4; k++) e.startR[k].push_back((int)e.tilesR[k].size());
+  if (ensure_cap(&e.dTiles, &e.tilesCap, e.tiles1.size()) || ensure_cap(&e.dActive, &e.activeCap, e.tiles1.size()))
+    return MG_ERR_CUDA;
+  CKB(cudaMemcpyAsync(e.dTiles, e.tiles1.data(), sizeof(BTile) * e.tiles1.size(), cudaMemcpyHostToDevice, e.stream));
+  e.dirty = false;
   return MG_OK;
 }
 
-extern "C" int mg_batch_step(mg_batch b, mg_batch_stats* stats) {
-  if (!b) return set_error(MG_ERR_ARG, "mg_batch_step: null batch");
-  const int cur = b->cur, nxt = 1 - cur;
-  const int nt = (int)b->tiles.size();
-  cudaStream_t st = b->stream;
-  launch_b_inflow(b->dTiles, nt, b->dScenes, cur, b->step, st);
-  launch_b_advect_velocity(b->dTiles, nt, b->dScenes, cur, st);
-  launch_b_forces(b->dTiles, nt, b->dScenes, nxt, st);
+// one plume step of every member
+int engine_step(Engine& e, mg_batch_stats* stats) {
+  if (e.members.empty()) return MG_OK;
+  if (engine_tables(e)) return MG_ERR_CUDA;
+  const int nm = (int)e.members.size();
+  const int nt = (int)e.tiles1.size();
+  cudaStream_t st = e.stream;
+  const int cur = 0, nxt = 1;  // the table presents every scene's current buffers as 0
+  launch_b_inflow(e.dTiles, nt, e.dScenes, cur, st);
+  launch_b_advect_velocity(e.dTiles, nt, e.dScenes, cur, st);
+  launch_b_forces(e.dTiles, nt, e.dScenes, nxt, st);
   // GridCg setup of every scene: PcNone with the reference's 2D iteration
   // limit, (int)(cgMaxIterFac * max size) * 4 (pressure.cpp:407-409)
   int maxIterAll = 0;
-  for (int q = 0; q < b->count; q++) {
-    const Dims& d = b->scenes[q].d;
+  for (int q = 0; q < nm; q++) {
+    const Dims& d = e.members[q]->s.d;
     CgScalars c{};
-    c.accuracy = b->cgAccuracy;
-    c.maxIter = (int)(b->cgMaxIterFac * (float)std::max(d.nx, std::max(d.ny, d.nz))) * 4;
+    c.accuracy = e.cgAccuracy;
+    c.maxIter = (int)(e.cgMaxIterFac * (float)std::max(d.nx, std::max(d.ny, d.nz))) * 4;
     c.resNorm = 1e20f;
-    b->hSc[q] = c;
+    e.hSc[q] = c;
     maxIterAll = std::max(maxIterAll, c.maxIter);
   }
-  CKB(cudaMemcpyAsync(b->dSc, b->hSc.data(), sizeof(CgScalars) * b->count, cudaMemcpyHostToDevice, st));
-  CKB(cudaMemsetAsync(b->dDone, 0, sizeof(int), st));
-  launch_b_pressure_setup(b->dTiles, nt, b->dScenes, nxt, st);
+  CKB(cudaMemcpyAsync(e.dSc, e.hSc.data(), sizeof(CgScalars) * nm, cudaMemcpyHostToDevice, st));
+  CKB(cudaMemsetAsync(e.dDone, 0, sizeof(int), st));
+  launch_b_pressure_setup(e.dTiles, nt, e.dScenes, nxt, st);
   // CG sweeps over the tiles of the scenes still iterating.  Autotuner: the
   // first solve runs its first 4 x lag sweeps with tiles 8, 16, 32 and 64
   // rows tall (lag sweeps each, timed with events) and keeps the fastest;
   // results do not depend on the choice.
-  int kk = b->rowsK >= 0 ? b->rowsK : 0;
+  int kk = e.rowsK >= 0 ? e.rowsK : 0;
   int active = 0, doneSeen = -1, sweeps = 0;
   std::vector<BTile> list;
   auto rebuild = [&](bool all) -> int {
     list.clear();
-    for (int q = 0; q < b->count; q++)
-      if (all || !b->hSc[q].done)
-        list.insert(list.end(), b->tilesR[kk].begin() + b->startR[kk][q], b->tilesR[kk].begin() + b->startR[kk][q + 1]);
+    for (int q = 0; q < nm; q++)
+      if (all || !e.hSc[q].done)
+        list.insert(list.end(), e.tilesR[kk].begin() + e.startR[kk][q], e.tilesR[kk].begin() + e.startR[kk][q + 1]);
     active = (int)list.size();
-    if (active) CKB(cudaMemcpyAsync(b->dActive, list.data(), sizeof(BTile) * active, cudaMemcpyHostToDevice, st));
+    if (active) CKB(cudaMemcpyAsync(e.dActive, list.data(), sizeof(BTile) * active, cudaMemcpyHostToDevice, st));
     return MG_OK;
   };
   if (rebuild(true)) return MG_ERR_CUDA;
-  const bool tuning = b->rowsK < 0;
-  if (tuning) CKB(cudaEventRecord(b->ev[0], st));
+  const bool tuning = e.rowsK < 0;
+  if (tuning) CKB(cudaEventRecord(e.ev[0], st));
   while (active > 0 && sweeps < maxIterAll) {
-    launch_b_pcg_iteration(b->dActive, active, b->dScenes, 1 << kk, b->dDone, st);
+    launch_b_pcg_iteration(e.dActive, active, e.dScenes, 1 << kk, e.dDone, st);
     sweeps++;
-    if (sweeps % b->lag == 0 || sweeps == maxIterAll) {
+    if (sweeps % e.lag == 0 || sweeps == maxIterAll) {
       bool relist = false;
-      if (tuning && b->rowsK < 0 && sweeps <= 4 * b->lag) {
-        CKB(cudaEventRecord(b->ev[1], st));
-        CKB(cudaEventSynchronize(b->ev[1]));
+      if (tuning && e.rowsK < 0 && sweeps <= 4 * e.lag) {
+        CKB(cudaEventRecord(e.ev[1], st));
+        CKB(cudaEventSynchronize(e.ev[1]));
         float ms = 0.f;
-        CKB(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
-        b->tuneMs[kk] = ms;
+        CKB(cudaEventElapsedTime(&ms, e.ev[0], e.ev[1]));
+        e.tuneMs[kk] = ms;
         if (kk < 3) {
           kk++;
           relist = true;
         } else {
           int best = 0;
           for (int q = 1; q < 4; q++)
-            if (b->tuneMs[q] < b->tuneMs[best]) best = q;
-          b->rowsK = best;
+            if (e.tuneMs[q] < e.tuneMs[best]) best = q;
+          e.rowsK = best;
           relist = kk != best;
           kk = best;
         }
       }
       int nd = 0;
-      CKB(cudaMemcpyAsync(&nd, b->dDone, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CKB(cudaMemcpyAsync(&nd, e.dDone, sizeof(int), cudaMemcpyDeviceToHost, st));
       CKB(cudaStreamSynchronize(st));
-      if (nd >= b->count) break;
+      if (nd >= nm) break;
       if (nd != doneSeen || relist) {
         doneSeen = nd;
-        CKB(cudaMemcpyAsync(b->hSc.data(), b->dSc, sizeof(CgScalars) * b->count, cudaMemcpyDeviceToHost, st));
+        CKB(cudaMemcpyAsync(e.hSc.data(), e.dSc, sizeof(CgScalars) * nm, cudaMemcpyDeviceToHost, st));
         CKB(cudaStreamSynchronize(st));
         if (rebuild(false)) return MG_ERR_CUDA;
       }
-      if (tuning && b->rowsK < 0) CKB(cudaEventRecord(b->ev[0], st));
+      if (tuning && e.rowsK < 0) CKB(cudaEventRecord(e.ev[0], st));
     }
   }
-  launch_b_correct(b->dTiles, nt, b->dScenes, nxt, st);
-  CKB(cudaMemcpyAsync(b->hSc.data(), b->dSc, sizeof(CgScalars) * b->count, cudaMemcpyDeviceToHost, st));
+  launch_b_correct(e.dTiles, nt, e.dScenes, nxt, st);
+  CKB(cudaMemcpyAsync(e.hSc.data(), e.dSc, sizeof(CgScalars) * nm, cudaMemcpyDeviceToHost, st));
   CKB(cudaStreamSynchronize(st));
   CKB(cudaGetLastError());
-  b->cur = nxt;
-  b->step++;
+  for (auto* m : e.members) {
+    m->cur = 1 - m->cur;
+    m->step++;
+  }
   if (stats) {
     stats->sweeps = sweeps;
-    int mx = 0;
+    int mx = 0, diverged = 0;
     long long sum = 0;
-    int diverged = 0;
-    for (auto& c : b->hSc) {
+    for (auto& c : e.hSc) {
       mx = std::max(mx, c.iterations);
       sum += c.iterations;
       diverged += c.status == 2;
@@ -313,35 +393,27 @@ extern "C" int mg_batch_step(mg_batch b, mg_batch_stats* stats) {
     stats->totalIterations = sum;
     stats->diverged = diverged;
   }
-  for (auto& c : b->hSc)
+  for (auto& c : e.hSc)
     if (c.status == 2)
       return set_error(MG_ERR_SOLVER, "GridCg::iterate: The CG solver diverged, residual norm > 1e30, stopping.");
   return MG_OK;
 }
 
-extern "C" int mg_batch_scene_iterations(mg_batch b, int scene, int* iterations, float* resNorm) {
-  if (!b || scene < 0 || scene >= b->count) return set_error(MG_ERR_ARG, "mg_batch_scene_iterations: invalid scene");
-  if (iterations) *iterations = b->hSc[scene].iterations;
-  if (resNorm) *resNorm = b->hSc[scene].resNorm;
-  return MG_OK;
-}
-
-extern "C" int mg_batch_download(mg_batch b, int scene, int what, void* host, size_t bytes) {
-  if (!b || scene < 0 || scene >= b->count || !host) return set_error(MG_ERR_ARG, "mg_batch_download: invalid argument");
-  const BScene& s = b->scenes[scene];
+int scene_download(Engine& e, SceneRec* r, int what, void* host, size_t bytes) {
+  const BScene& s = r->s;
   const size_t n = (size_t)s.d.n;
   const size_t want = what == MG_BATCH_VELOCITY ? 3 * n * sizeof(float) : n * sizeof(float);
-  if (bytes != want) return set_error(MG_ERR_ARG, "mg_batch_download: byte count does not match the scene");
-  cudaStream_t st = b->stream;
+  if (bytes != want) return set_error(MG_ERR_ARG, "download: byte count does not match the scene");
+  cudaStream_t st = e.stream;
   switch (what) {
-    case MG_BATCH_DENSITY: CKB(cudaMemcpyAsync(host, s.dens[b->cur], want, cudaMemcpyDeviceToHost, st)); break;
+    case MG_BATCH_DENSITY: CKB(cudaMemcpyAsync(host, s.dens[r->cur], want, cudaMemcpyDeviceToHost, st)); break;
     case MG_BATCH_PRESSURE: CKB(cudaMemcpyAsync(host, s.pres, want, cudaMemcpyDeviceToHost, st)); break;
     case MG_BATCH_FLAGS: CKB(cudaMemcpyAsync(host, s.flags, want, cudaMemcpyDeviceToHost, st)); break;
     case MG_BATCH_SOURCE: CKB(cudaMemcpyAsync(host, s.mask, want, cudaMemcpyDeviceToHost, st)); break;
     case MG_BATCH_VELOCITY: {
       // SoA planes -> the reference's AoS Vec3 on the host
       std::vector<float> h(3 * n);
-      CKB(cudaMemcpyAsync(h.data(), s.vel[b->cur], want, cudaMemcpyDeviceToHost, st));
+      CKB(cudaMemcpyAsync(h.data(), s.vel[r->cur], want, cudaMemcpyDeviceToHost, st));
       CKB(cudaStreamSynchronize(st));
       float* o = (float*)host;
       for (size_t i = 0; i < n; i++) {
@@ -351,10 +423,70 @@ extern "C" int mg_batch_download(mg_batch b, int scene, int what, void* host, si
       }
       return MG_OK;
     }
-    default: return set_error(MG_ERR_ARG, "mg_batch_download: unknown field");
+    default: return set_error(MG_ERR_ARG, "download: unknown field");
   }
   CKB(cudaStreamSynchronize(st));
   return MG_OK;
+}
+
+}  // namespace
+
+// ============================================================== batched form
+struct mg_batch_s {
+  Engine e;
+  std::vector<SceneRec*> scenes;  // creation order
+};
+
+extern "C" int mg_batch_create(int count, const int* sizes, const float* gravity, const unsigned long long* seeds, float dt,
+                               mg_batch* out) {
+  if (!library_ready()) return set_error(MG_ERR_STATE, "mg_init has not been called");
+  if (count < 1 || !sizes || !gravity || !seeds || !out) return set_error(MG_ERR_ARG, "mg_batch_create: invalid argument");
+  auto b = new mg_batch_s();
+  int st = engine_init(b->e, dt);
+  for (int q = 0; q < count && !st; q++) {
+    SceneRec* r = nullptr;
+    st = scene_add(b->e, sizes[3 * q], sizes[3 * q + 1], sizes[3 * q + 2], gravity + 3 * q, seeds[q], &r);
+    if (!st) b->scenes.push_back(r);
+  }
+  if (!st && cudaStreamSynchronize(b->e.stream) != cudaSuccess) st = set_error(MG_ERR_CUDA, "mg_batch_create: setup failed");
+  if (st) {
+    delete b;
+    return st;
+  }
+  *out = b;
+  return MG_OK;
+}
+
+extern "C" int mg_batch_destroy(mg_batch b) {
+  delete b;
+  return MG_OK;
+}
+
+extern "C" int mg_batch_set_solver(mg_batch b, float cgAccuracy, float cgMaxIterFac) {
+  if (!b || !(cgAccuracy > 0.f) || !(cgMaxIterFac > 0.f)) return set_error(MG_ERR_ARG, "mg_batch_set_solver: invalid argument");
+  b->e.cgAccuracy = cgAccuracy;
+  b->e.cgMaxIterFac = cgMaxIterFac;
+  return MG_OK;
+}
+
+extern "C" int mg_batch_step(mg_batch b, mg_batch_stats* stats) {
+  if (!b) return set_error(MG_ERR_ARG, "mg_batch_step: null batch");
+  return engine_step(b->e, stats);
+}
+
+extern "C" int mg_batch_scene_iterations(mg_batch b, int scene, int* iterations, float* resNorm) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size()) return set_error(MG_ERR_ARG, "mg_batch_scene_iterations: invalid scene");
+  const auto& m = b->e.members;
+  const size_t q = std::find(m.begin(), m.end(), b->scenes[scene]) - m.begin();
+  const bool have = q < b->e.hSc.size();
+  if (iterations) *iterations = have ? b->e.hSc[q].iterations : 0;
+  if (resNorm) *resNorm = have ? b->e.hSc[q].resNorm : 0.f;
+  return MG_OK;
+}
+
+extern "C" int mg_batch_download(mg_batch b, int scene, int what, void* host, size_t bytes) {
+  if (!b || scene < 0 || scene >= (int)b->scenes.size() || !host) return set_error(MG_ERR_ARG, "mg_batch_download: invalid argument");
+  return scene_download(b->e, b->scenes[scene], what, host, bytes);
 }
 
 extern "C" int mg_batch_noise(unsigned long long seed, int step, long long cells, float* out) {
@@ -365,25 +497,219 @@ extern "C" int mg_batch_noise(unsigned long long seed, int step, long long cells
 
 extern "C" int mg_batch_tuning(mg_batch b, int* sweepRows, float* ms) {
   if (!b) return set_error(MG_ERR_ARG, "mg_batch_tuning: null batch");
-  if (sweepRows) *sweepRows = b->rowsK < 0 ? 0 : kBTY << b->rowsK;
+  if (sweepRows) *sweepRows = b->e.rowsK < 0 ? 0 : kBTY << b->e.rowsK;
   if (ms)
-    for (int q = 0; q < 4; q++) ms[q] = b->tuneMs[q];
+    for (int q = 0; q < 4; q++) ms[q] = b->e.tuneMs[q];
   return MG_OK;
 }
 
 extern "C" int mg_batch_info(mg_batch b, int* count, long long* cells, long long* tiles, size_t* bytes) {
   if (!b) return set_error(MG_ERR_ARG, "mg_batch_info: null batch");
-  long long c = 0;
-  for (auto& s : b->scenes) c += s.d.n;
-  if (count) *count = b->count;
+  long long c = 0, t = 0;
+  for (auto* r : b->scenes) {
+    c += r->s.d.n;
+    t += r->s.ntiles;
+  }
+  if (count) *count = (int)b->scenes.size();
   if (cells) *cells = c;
-  if (tiles) *tiles = (long long)b->tiles.size();
-  if (bytes) *bytes = b->arenaBytes;
+  if (tiles) *tiles = t;
+  if (bytes) *bytes = b->e.liveBytes;
   return MG_OK;
 }
 
 extern "C" int mg_batch_sync(mg_batch b) {
   if (!b) return set_error(MG_ERR_ARG, "mg_batch_sync: null batch");
-  CKB(cudaStreamSynchronize(b->stream));
+  CKB(cudaStreamSynchronize(b->e.stream));
+  return MG_OK;
+}
+
+// =============================================================== served form
+namespace {
+struct Job {
+  int nx, ny, nz;
+  float gravity[3];
+  unsigned long long seed;
+  int steps;
+  double arrival;  // seconds after the run starts
+  int keep;        // copy the final fields to the host
+  // outcome
+  double admitted = -1., finished = -1.;
+  int stepsDone = 0;
+  double stepMsSum = 0.;
+  std::vector<float> dens, vel, pres;
+  SceneRec* rec = nullptr;
+};
+}  // namespace
+
+struct mg_server_s {
+  Engine e;
+  size_t budget = 0;
+  std::vector<Job> jobs;
+  std::vector<float> tickMs;
+  std::vector<int> tickJobs;
+  double wall = 0.;
+  long long cellSteps = 0;
+  size_t peakBytes = 0;
+};
+
+extern "C" int mg_serve_create(size_t budgetBytes, float dt, mg_server* out) {
+  if (!library_ready()) return set_error(MG_ERR_STATE, "mg_init has not been called");
+  if (!out || budgetBytes == 0) return set_error(MG_ERR_ARG, "mg_serve_create: invalid argument");
+  auto s = new mg_server_s();
+  s->budget = budgetBytes;
+  const int st = engine_init(s->e, dt);
+  if (st) {
+    delete s;
+    return st;
+  }
+  *out = s;
+  return MG_OK;
+}
+
+extern "C" int mg_serve_destroy(mg_server s) {
+  delete s;
+  return MG_OK;
+}
+
+extern "C" int mg_serve_set_solver(mg_server s, float cgAccuracy, float cgMaxIterFac) {
+  if (!s || !(cgAccuracy > 0.f) || !(cgMaxIterFac > 0.f)) return set_error(MG_ERR_ARG, "mg_serve_set_solver: invalid argument");
+  s->e.cgAccuracy = cgAccuracy;
+  s->e.cgMaxIterFac = cgMaxIterFac;
+  return MG_OK;
+}
+
+extern "C" size_t mg_serve_job_bytes(int nx, int ny, int nz) { return scene_bytes(nx, ny, nz); }
+
+extern "C" int mg_serve_submit(mg_server s, int nx, int ny, int nz, const float* gravity, unsigned long long seed, int steps,
+                               double arrival, int keepResult, int* job) {
+  if (!s || !gravity || steps < 1 || arrival < 0.) return set_error(MG_ERR_ARG, "mg_serve_submit: invalid argument");
+  if (nx < 3 || ny < 3 || nz < 1 || (nz > 1 && nz < 3)) return set_error(MG_ERR_ARG, "mg_serve_submit: scene is too small");
+  if (scene_bytes(nx, ny, nz) > s->budget) return set_error(MG_ERR_ARG, "mg_serve_submit: the job alone exceeds the memory budget");
+  Job j;
+  j.nx = nx;
+  j.ny = ny;
+  j.nz = nz;
+  std::memcpy(j.gravity, gravity, sizeof j.gravity);
+  j.seed = seed;
+  j.steps = steps;
+  j.arrival = arrival;
+  j.keep = keepResult;
+  s->jobs.push_back(std::move(j));
+  if (job) *job = (int)s->jobs.size() - 1;
+  return MG_OK;
+}
+
+// run until every submitted job has finished.  Arrival times are honoured
+// against the wall clock: with nothing resident the loop waits for the next
+// arrival.
+extern "C" int mg_serve_run(mg_server s, mg_serve_stats* stats) {
+  if (!s) return set_error(MG_ERR_ARG, "mg_serve_run: null server");
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
+  auto now = [&]() { return std::chrono::duration<double>(clk::now() - t0).count(); };
+  std::vector<int> order;
+  for (size_t q = 0; q < s->jobs.size(); q++)
+    if (s->jobs[q].finished < 0.) order.push_back((int)q);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return s->jobs[a].arrival < s->jobs[b].arrival; });
+  size_t next = 0, finished = 0;
+  std::vector<int> resident;
+  while (finished < order.size()) {
+    // admission in arrival order while the next job has arrived and fits
+    const double tn = now();
+    while (next < order.size()) {
+      Job& j = s->jobs[order[next]];
+      if (j.arrival > tn) break;
+      if (s->e.liveBytes + scene_bytes(j.nx, j.ny, j.nz) > s->budget) break;
+      SceneRec* r = nullptr;
+      const int st = scene_add(s->e, j.nx, j.ny, j.nz, j.gravity, j.seed, &r);
+      if (st) return st;
+      j.rec = r;
+      j.admitted = now();
+      resident.push_back(order[next]);
+      next++;
+    }
+    s->peakBytes = std::max(s->peakBytes, s->e.liveBytes);
+    if (resident.empty()) {
+      const double wait = s->jobs[order[next]].arrival - now();
+      if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
+      continue;
+    }
+    const double ta = now();
+    const int st = engine_step(s->e, nullptr);
+    if (st) return st;
+    const double dtick = now() - ta;
+    s->tickMs.push_back((float)(1e3 * dtick));
+    s->tickJobs.push_back((int)resident.size());
+    std::vector<int> still;
+    for (int id : resident) {
+      Job& j = s->jobs[id];
+      j.stepsDone++;
+      j.stepMsSum += 1e3 * dtick;
+      s->cellSteps += (long long)j.nx * j.ny * j.nz;
+      if (j.stepsDone < j.steps) {
+        still.push_back(id);
+        continue;
+      }
+      if (j.keep) {
+        const size_t n = (size_t)j.nx * j.ny * j.nz;
+        j.dens.resize(n);
+        j.pres.resize(n);
+        j.vel.resize(3 * n);
+        int e1 = scene_download(s->e, j.rec, MG_BATCH_DENSITY, j.dens.data(), n * sizeof(float));
+        if (!e1) e1 = scene_download(s->e, j.rec, MG_BATCH_PRESSURE, j.pres.data(), n * sizeof(float));
+        if (!e1) e1 = scene_download(s->e, j.rec, MG_BATCH_VELOCITY, j.vel.data(), 3 * n * sizeof(float));
+        if (e1) return e1;
+      }
+      scene_remove(s->e, j.rec);
+      j.rec = nullptr;
+      j.finished = now();
+      finished++;
+    }
+    resident.swap(still);
+  }
+  s->wall = now();
+  if (stats) {
+    stats->jobs = (int)order.size();
+    stats->ticks = (long long)s->tickMs.size();
+    stats->wallSeconds = s->wall;
+    stats->cellSteps = s->cellSteps;
+    stats->peakBytes = s->peakBytes;
+  }
+  return MG_OK;
+}
+
+extern "C" int mg_serve_job_info(mg_server s, int job, mg_serve_job* info) {
+  if (!s || job < 0 || job >= (int)s->jobs.size() || !info) return set_error(MG_ERR_ARG, "mg_serve_job_info: invalid job");
+  const Job& j = s->jobs[job];
+  info->arrival = j.arrival;
+  info->admitted = j.admitted;
+  info->finished = j.finished;
+  info->steps = j.stepsDone;
+  info->meanStepMs = j.stepsDone ? j.stepMsSum / j.stepsDone : 0.;
+  return MG_OK;
+}
+
+extern "C" int mg_serve_job_result(mg_server s, int job, int what, void* host, size_t bytes) {
+  if (!s || job < 0 || job >= (int)s->jobs.size() || !host) return set_error(MG_ERR_ARG, "mg_serve_job_result: invalid job");
+  const Job& j = s->jobs[job];
+  const std::vector<float>* v = what == MG_BATCH_DENSITY    ? &j.dens
+                                : what == MG_BATCH_VELOCITY ? &j.vel
+                                : what == MG_BATCH_PRESSURE ? &j.pres
+                                                            : nullptr;
+  if (!v) return set_error(MG_ERR_ARG, "mg_serve_job_result: density, velocity or pressure only");
+  if (v->empty()) return set_error(MG_ERR_STATE, "mg_serve_job_result: the job kept no result (or has not finished)");
+  if (bytes != v->size() * sizeof(float)) return set_error(MG_ERR_ARG, "mg_serve_job_result: byte count does not match");
+  std::memcpy(host, v->data(), bytes);
+  return MG_OK;
+}
+
+extern "C" int mg_serve_ticks(mg_server s, int* count, float* ms, int* jobs) {
+  if (!s || !count) return set_error(MG_ERR_ARG, "mg_serve_ticks: invalid argument");
+  const int n = std::min(*count, (int)s->tickMs.size());
+  for (int q = 0; q < n; q++) {
+    if (ms) ms[q] = s->tickMs[q];
+    if (jobs) jobs[q] = s->tickJobs[q];
+  }
+  *count = (int)s->tickMs.size();
   return MG_OK;
 }

@@ -467,11 +467,10 @@ int launch_minmax_partial(long long n, const float* a, float* part, cudaStream_t
   if (i >= d.nx || j >= d.ny) return;
 
 // inflow: density = max(density, U[0,1) * source) (Grid::join, grid.cpp:303-311)
-__global__ void __launch_bounds__(256) k_b_inflow(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur,
-                                                  int step) {
+__global__ void __launch_bounds__(256) k_b_inflow(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
   BATCH_CELL
   const long long idx = ix(d, i, j, k);
-  const float b = batch_noise(sc.seed, step, idx) * sc.mask[idx];
+  const float b = batch_noise(sc.seed, sc.step, idx) * sc.mask[idx];
   float* a = sc.dens[cur];
   const float x = a[idx];
   a[idx] = x < b ? b : x;
@@ -486,9 +485,9 @@ __global__ void __launch_bounds__(256) k_b_forces(const BTile* __restrict__ tile
 }
 #undef BATCH_CELL
 
-void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, int step, cudaStream_t st) {
+void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st) {
   count_launch();
-  k_b_inflow<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, cur, step);
+  k_b_inflow<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, cur);
 }
 void launch_b_forces(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
   count_launch();

@@ -49,6 +49,7 @@ struct BScene {
   float dt;
   float bx, by, bz;  // buoyancy factors -gravity*dt/dx*coefficient (KnAddBuoyancy), 0.5 applied in-kernel
   unsigned long long seed;
+  int step;        // steps this scene has taken: the inflow noise index
   int ntiles;
 };
 
@@ -56,7 +57,7 @@ __host__ __device__ inline Mac bmac(float* p, long long n) { return Mac{p, p + n
 __host__ __device__ inline CMac bcmac(const float* p, long long n) { return CMac{p, p + n, p + 2 * n}; }
 
 // stages (cur: index of the current vel/dens buffers; results go to 1-cur)
-void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, int step, cudaStream_t st);
+void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_advect_density(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_advect_velocity(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_forces(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
