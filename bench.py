@@ -371,6 +371,77 @@ def batched_form(m, steps, seed, plain_steps, plain_scenes, sim_steps=100):
                 batched["sims_per_hour"] / plain["sims_per_hour"]}
 
 
+def served_form(m, seed, njobs, step_scale, rate=20.0, budget=150 * 10 ** 9):
+    """Config 5 on a bounded sample: a Poisson stream (rate jobs/s) of 3D
+    plume jobs with sides U{32..128} and U{100..400} steps (divided by
+    step_scale to bound the run), per-job seeds; served (continuous batching
+    under the HBM budget) against the plain sequential path (each job alone
+    through the scene API, first come first served, PcMIC as in config 1)."""
+    from mantaflow_gb300 import batch as mb
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs))
+    sides = rng.integers(32, 129, njobs)
+    steps = np.maximum(1, rng.integers(100, 401, njobs) // step_scale)
+    grav = rng.uniform(1e-3, 8e-3, njobs)
+    seeds = rng.integers(1, 2 ** 62, njobs)
+    srv = mb.PlumeServer(budget_bytes=budget)
+    ids = [srv.submit((int(n),) * 3, (0.0, -float(g), 0.0), int(sd), int(k), float(a))
+           for n, g, sd, k, a in zip(sides, grav, seeds, steps, arrivals)]
+    st = srv.run()
+    infos = [srv.job(q) for q in ids]
+    tick_ms, tick_jobs = srv.ticks()
+    srv.close()
+    step_lat = np.repeat(tick_ms, tick_jobs)  # every resident job's step took the tick
+    job_lat = np.array([i["finished"] - i["arrival"] for i in infos])
+    served = {"cells_per_s": st["cell_steps"] / st["wall_s"], "wall_s": st["wall_s"], "ticks": st["ticks"],
+              "step_ms_p50": float(np.percentile(step_lat, 50)), "step_ms_p99": float(np.percentile(step_lat, 99)),
+              "job_s_p50": float(np.percentile(job_lat, 50)), "job_s_p99": float(np.percentile(job_lat, 99)),
+              "peak_device_bytes": st["peak_bytes"], "max_resident_jobs": int(max(tick_jobs))}
+    # plain sequential path: one job at a time, in arrival order
+    t0 = time.perf_counter()
+    plain_steps, plain_jobs, cell_steps = [], [], 0
+    for n, g, sd, k, a in zip(sides, grav, seeds, steps, arrivals):
+        while time.perf_counter() - t0 < a:
+            time.sleep(min(0.005, a - (time.perf_counter() - t0)))
+        n = int(n)
+        s = m.Solver(name="job", gridSize=m.vec3(n, n, n), dim=3)
+        flags = s.create(m.FlagGrid)
+        flags.initDomain(boundaryWidth=0)
+        flags.fillGrid()
+        m.setOpenBound(flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
+        vel, dens, pres, src = s.create(m.MACGrid), s.create(m.RealGrid), s.create(m.RealGrid), s.create(m.RealGrid)
+        gs = m.vec3(n, n, n)
+        mask = s.create(m.RealGrid)
+        s.create(m.Cylinder, center=gs * m.vec3(0.5, 0.1, 0.5), radius=n * 0.14,
+                 z=gs * m.vec3(0, 0.02, 0)).applyToGrid(grid=mask, value=1.0)
+        mk = mask.numpy()
+        r = np.random.default_rng(int(sd) % (2 ** 32))
+        for t in range(int(k)):
+            m.copyArrayToGridReal((r.random(mk.shape, dtype=np.float32) * mk).astype(np.float32), src)
+            ts = time.perf_counter()
+            dens.join(src)
+            m.advectSemiLagrange(flags=flags, vel=vel, grid=dens, order=2, clampMode=2)
+            m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=2, clampMode=2)
+            m.setWallBcs(flags=flags, vel=vel)
+            m.addBuoyancy(density=dens, vel=vel, gravity=m.vec3(0, -float(g), 0), flags=flags)
+            m.solvePressure(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, preconditioner=m.PcMIC)
+            s.sync()
+            plain_steps.append(time.perf_counter() - ts)
+            cell_steps += n ** 3
+        plain_jobs.append(time.perf_counter() - t0 - a)
+        del s
+    wall = time.perf_counter() - t0
+    plain = {"cells_per_s": cell_steps / wall, "wall_s": wall,
+             "step_ms_p50": 1e3 * float(np.percentile(plain_steps, 50)),
+             "step_ms_p99": 1e3 * float(np.percentile(plain_steps, 99)),
+             "job_s_p50": float(np.percentile(plain_jobs, 50)), "job_s_p99": float(np.percentile(plain_jobs, 99))}
+    return {"workload": "config 5 sample: %d 3D plume jobs, Poisson arrivals %.0f/s, sides U{32..128}, steps "
+                        "U{100..400}/%d, HBM budget %.0f GB; dam-break jobs are not in the served form"
+                        % (njobs, rate, step_scale, budget / 1e9),
+            "served": served, "plain_sequential": plain,
+            "throughput_ratio": served["cells_per_s"] / plain["cells_per_s"]}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -436,6 +507,8 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=10, help="timed steps of the config-4 batch (0: skip)")
     ap.add_argument("--plain-steps", type=int, default=3, help="timed steps per sampled scene of the plain path")
     ap.add_argument("--plain-scenes", type=int, default=16)
+    ap.add_argument("--served-jobs", type=int, default=24, help="jobs of the config-5 served sample (0: skip)")
+    ap.add_argument("--served-step-scale", type=int, default=10)
     ap.add_argument("--refined-steps", type=int, default=5,
                     help="timed 256^3 steps of the FP64-refined form reported beside the headline (0: skip)")
     args = ap.parse_args()
@@ -607,6 +680,9 @@ def main():
     batched = None
     if args.batched_steps > 0 and rank == 0:
         batched = batched_form(m, args.batched_steps, args.seed + 13, args.plain_steps, args.plain_scenes)
+    served = None
+    if args.served_jobs > 0 and rank == 0:
+        served = served_form(m, args.seed + 17, args.served_jobs, args.served_step_scale)
     precision = None
     if args.precision_size > 0 and rank == 0 and world == 1:
         precision = precision_form(m, args.precision_size, args.precision_steps, args.seed + 5)
@@ -638,7 +714,7 @@ def main():
                "clocks": clk, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])},
                "same_scene_pc_mic": alt, "precision_form": {"refined_256": refined, "errors_vs_fp64": precision},
-               "batched_form": batched}
+               "batched_form": batched, "served_form": served}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
