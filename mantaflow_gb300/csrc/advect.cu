@@ -297,7 +297,23 @@ __device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __
   const bool inner = i >= 1 && i < d.nx - 1 && j >= 1 && j < d.ny - 1 && (!d.is3d || (k >= 1 && k < d.nz - 1));
   const float hs = strength * 0.5f;
   float bwd[3] = {0.f, 0.f, 0.f};
-  if (inner) sl_mac_cell<kTrace>(d, vel, fwd, i, j, k, -dt, bwd);
+  // face velocities, shared by the backward trace (order-1 trace) and the
+  // clamp, which both sample vel at the cell's faces
+  V3 ax{0.f, 0.f, 0.f}, ay{0.f, 0.f, 0.f}, az{0.f, 0.f, 0.f};
+  if (inner) {
+    ax = mac_at_x(d, vel, idx);
+    ay = mac_at_y(d, vel, idx);
+    az = mac_at_z(d, vel, idx);
+    if (kTrace == 1) {
+      // SemiLagrangeMAC(fwd, -dt), as sl_mac_cell<1> forms it
+      const float mdt = -dt;
+      bwd[0] = interp(d, fwd.u, (i + 0.5f) - ax.x * mdt, (j + 0.5f) - ax.y * mdt, (k + 0.5f) - ax.z * mdt);
+      bwd[1] = interp(d, fwd.v, (i + 0.5f) - ay.x * mdt, (j + 0.5f) - ay.y * mdt, (k + 0.5f) - ay.z * mdt);
+      bwd[2] = interp(d, fwd.w, (i + 0.5f) - az.x * mdt, (j + 0.5f) - az.y * mdt, (k + 0.5f) - az.z * mdt);
+    } else {
+      sl_mac_cell<kTrace>(d, vel, fwd, i, j, k, -dt, bwd);
+    }
+  }
   float fw[3], val[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
@@ -305,14 +321,10 @@ __device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __
     val[c] = skip[c] ? fw[c] : fmaf(hs, __ldg(orig.c(c) + idx) - bwd[c], fw[c]);
   }
   if (inner) {
-    const V3 ax = mac_at_x(d, vel, idx);
     val[0] = clamp_component_mac(d, flags, val[0], orig.u, fw[0], 0, i, j, k, V3{ax.x * dt, ax.y * dt, ax.z * dt}, clampMode);
-    const V3 ay = mac_at_y(d, vel, idx);
     val[1] = clamp_component_mac(d, flags, val[1], orig.v, fw[1], 1, i, j, k, V3{ay.x * dt, ay.y * dt, ay.z * dt}, clampMode);
-    if (d.is3d) {
-      const V3 az = mac_at_z(d, vel, idx);
+    if (d.is3d)
       val[2] = clamp_component_mac(d, flags, val[2], orig.w, fw[2], 2, i, j, k, V3{az.x * dt, az.y * dt, az.z * dt}, clampMode);
-    }
   }
   dst.u[idx] = val[0];
   dst.v[idx] = val[1];

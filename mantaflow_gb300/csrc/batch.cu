@@ -149,6 +149,7 @@ void* pool_take(Engine& e, size_t bytes) {
 // a plume scene joins the engine: device block, flags and source set up
 int scene_add(Engine& e, int nx, int ny, int nz, const float* gravity, unsigned long long seed, SceneRec** out) {
   if (nx < 3 || ny < 3 || nz < 1 || (nz > 1 && nz < 3)) return set_error(MG_ERR_ARG, "plume scene is too small");
+  if ((long long)nx * ny * nz >= (1LL << 31)) return set_error(MG_ERR_ARG, "plume scene exceeds 2^31 - 1 cells");
   auto r = new SceneRec();
   r->bytes = scene_bytes(nx, ny, nz);
   r->mem = pool_take(e, r->bytes);

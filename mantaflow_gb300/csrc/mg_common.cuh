@@ -60,31 +60,35 @@ struct V3 {
 
 // MACGrid::getCentered / getAtMACX/Y/Z (source/grid.h:424-470).  0.5*(a+b)
 // and 0.25*(((a+b)+c)+d) are exact scalings of float sums.
-__device__ __forceinline__ V3 mac_centered(const Dims& d, CMac m, long long i) {
+__device__ __forceinline__ V3 mac_centered(const Dims& d, CMac m, long long i64) {
+  const int i = (int)i64;  // grids stay below 2^31 cells (checked at creation)
   V3 r;
   r.x = 0.5f * (__ldg(m.u + i) + __ldg(m.u + i + 1));
-  r.y = 0.5f * (__ldg(m.v + i) + __ldg(m.v + i + d.sy));
-  r.z = d.is3d ? 0.5f * (__ldg(m.w + i) + __ldg(m.w + i + d.sz)) : 0.f;
+  r.y = 0.5f * (__ldg(m.v + i) + __ldg(m.v + i + (int)d.sy));
+  r.z = d.is3d ? 0.5f * (__ldg(m.w + i) + __ldg(m.w + i + (int)d.sz)) : 0.f;
   return r;
 }
-__device__ __forceinline__ V3 mac_at_x(const Dims& d, CMac m, long long i) {
-  const long long Y = d.sy, Z = d.sz;
+__device__ __forceinline__ V3 mac_at_x(const Dims& d, CMac m, long long i64) {
+  const int i = (int)i64;  // grids stay below 2^31 cells (checked at creation)
+  const int Y = (int)d.sy, Z = (int)d.sz;
   V3 r;
   r.x = __ldg(m.u + i);
   r.y = 0.25f * (__ldg(m.v + i) + __ldg(m.v + i - 1) + __ldg(m.v + i + Y) + __ldg(m.v + i + Y - 1));
   r.z = d.is3d ? 0.25f * (__ldg(m.w + i) + __ldg(m.w + i - 1) + __ldg(m.w + i + Z) + __ldg(m.w + i + Z - 1)) : 0.f;
   return r;
 }
-__device__ __forceinline__ V3 mac_at_y(const Dims& d, CMac m, long long i) {
-  const long long Y = d.sy, Z = d.sz;
+__device__ __forceinline__ V3 mac_at_y(const Dims& d, CMac m, long long i64) {
+  const int i = (int)i64;  // grids stay below 2^31 cells (checked at creation)
+  const int Y = (int)d.sy, Z = (int)d.sz;
   V3 r;
   r.x = 0.25f * (__ldg(m.u + i) + __ldg(m.u + i - Y) + __ldg(m.u + i + 1) + __ldg(m.u + i + 1 - Y));
   r.y = __ldg(m.v + i);
   r.z = d.is3d ? 0.25f * (__ldg(m.w + i) + __ldg(m.w + i - Y) + __ldg(m.w + i + Z) + __ldg(m.w + i + Z - Y)) : 0.f;
   return r;
 }
-__device__ __forceinline__ V3 mac_at_z(const Dims& d, CMac m, long long i) {
-  const long long Y = d.sy, Z = d.sz;
+__device__ __forceinline__ V3 mac_at_z(const Dims& d, CMac m, long long i64) {
+  const int i = (int)i64;  // grids stay below 2^31 cells (checked at creation)
+  const int Y = (int)d.sy, Z = (int)d.sz;
   V3 r;
   r.x = 0.25f * (__ldg(m.u + i) + __ldg(m.u + i - Z) + __ldg(m.u + i + 1) + __ldg(m.u + i + 1 - Z));
   r.y = 0.25f * (__ldg(m.v + i) + __ldg(m.v + i - Z) + __ldg(m.v + i + Y) + __ldg(m.v + i + Y - Z));
@@ -123,8 +127,8 @@ __device__ __forceinline__ Wts build_index(const Dims& d, float x, float y, floa
 // interpol<T> for one float plane (util/interpol.h:68-78)
 __device__ __forceinline__ float interp(const Dims& d, const float* __restrict__ a, float x, float y, float z) {
   const Wts w = build_index<false>(d, x, y, z);
-  const long long X = 1, Y = d.sy, Z = d.sz;
-  const long long b = (long long)w.xi + Y * w.yi + Z * w.zi;
+  const int X = 1, Y = (int)d.sy, Z = (int)d.sz;
+  const int b = w.xi + Y * w.yi + Z * w.zi;
   const float* p = a + b;
   return ((__ldg(p) * w.t0 + __ldg(p + Y) * w.t1) * w.s0 + (__ldg(p + X) * w.t0 + __ldg(p + X + Y) * w.t1) * w.s1) * w.f0 +
          ((__ldg(p + Z) * w.t0 + __ldg(p + Y + Z) * w.t1) * w.s0 +
@@ -135,22 +139,22 @@ __device__ __forceinline__ float interp(const Dims& d, const float* __restrict__
 __device__ __forceinline__ V3 interp_mac(const Dims& d, CMac m, float x, float y, float z) {
   const Wts w = build_index<false>(d, x, y, z);
   const Wts s = build_index<true>(d, x, y, z);
-  const long long X = 1, Y = d.sy, Z = d.sz;
+  const int X = 1, Y = (int)d.sy, Z = (int)d.sz;
   V3 r;
   {
-    const float* p = m.u + (((long long)w.zi * d.ny + w.yi) * d.nx + s.xi);
+    const float* p = m.u + ((w.zi * d.ny + w.yi) * d.nx + s.xi);
     r.x = w.f0 * ((__ldg(p) * w.t0 + __ldg(p + Y) * w.t1) * s.s0 + (__ldg(p + X) * w.t0 + __ldg(p + X + Y) * w.t1) * s.s1) +
           w.f1 * ((__ldg(p + Z) * w.t0 + __ldg(p + Z + Y) * w.t1) * s.s0 +
                   (__ldg(p + X + Z) * w.t0 + __ldg(p + X + Y + Z) * w.t1) * s.s1);
   }
   {
-    const float* p = m.v + (((long long)w.zi * d.ny + s.yi) * d.nx + w.xi);
+    const float* p = m.v + ((w.zi * d.ny + s.yi) * d.nx + w.xi);
     r.y = w.f0 * ((__ldg(p) * s.t0 + __ldg(p + Y) * s.t1) * w.s0 + (__ldg(p + X) * s.t0 + __ldg(p + X + Y) * s.t1) * w.s1) +
           w.f1 * ((__ldg(p + Z) * s.t0 + __ldg(p + Z + Y) * s.t1) * w.s0 +
                   (__ldg(p + X + Z) * s.t0 + __ldg(p + X + Y + Z) * s.t1) * w.s1);
   }
   {
-    const float* p = m.w + (((long long)s.zi * d.ny + w.yi) * d.nx + w.xi);
+    const float* p = m.w + ((s.zi * d.ny + w.yi) * d.nx + w.xi);
     r.z = s.f0 * ((__ldg(p) * w.t0 + __ldg(p + Y) * w.t1) * w.s0 + (__ldg(p + X) * w.t0 + __ldg(p + X + Y) * w.t1) * w.s1) +
           s.f1 * ((__ldg(p + Z) * w.t0 + __ldg(p + Z + Y) * w.t1) * w.s0 +
                   (__ldg(p + X + Z) * w.t0 + __ldg(p + X + Y + Z) * w.t1) * w.s1);

@@ -304,6 +304,8 @@ extern "C" int mg_solver_create(int nx, int ny, int nz, int dim, mg_solver* out)
   if (dim != 2 && dim != 3) return fail(MG_ERR_ARG, "mg_solver_create: dim must be 2 or 3");
   if (dim == 2 && nz != 1) return fail(MG_ERR_ARG, "mg_solver_create: 2D solvers need nz == 1");
   if (nx < 3 || ny < 3 || (dim == 3 && nz < 3)) return fail(MG_ERR_ARG, "mg_solver_create: grid must be >= 3 cells per axis");
+  if ((long long)nx * ny * nz >= (1LL << 31))
+    return fail(MG_ERR_ARG, "mg_solver_create: grids are limited to 2^31 - 1 cells (32-bit cell offsets in the kernels)");
   auto s = new mg_solver_s();
   s->dim = dim;
   s->d.nx = nx;
