@@ -37,8 +37,11 @@
 #include "mg_multigrid.h"
 #include "mg_reduce.cuh"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -94,6 +97,7 @@ constexpr int kMaxPaths = 512;
 __constant__ Path c_paths[2][kMaxPaths];  // [0] 2D, [1] 3D
 int g_npaths[2] = {0, 0};
 bool g_pathsReady = false;
+int g_tailCta = 0;  // CTAs of the cluster V-cycle tail (0: per-level launches)
 
 __host__ __device__ __forceinline__ int parity3(int a, int b, int c) { return (a & 1) + (b & 1) + (c & 1); }
 __host__ __device__ __forceinline__ float inv_pow2(int e) { return 1.f / (float)(1 << e); }
@@ -257,7 +261,15 @@ __global__ void k_mg_coarse_op(Lev C, Lev F, int S) {
 // their terms subtract zero and need no type test.  The loads of one z-plane
 // of the stencil (9 matrix entries, 9 values) are issued together before
 // its subtractions; the chain of float operations is the reference's.
-template <bool IS3D, bool SKIP_CENTER>
+// vectors that other CTAs of the same launch write (the cluster V-cycle
+// below) are read at L2, past the SM's non-coherent L1
+template <bool CG>
+__device__ __forceinline__ float ldv(const float* p) {
+  if (CG) return __ldcg(p);
+  return *p;
+}
+
+template <bool IS3D, bool SKIP_CENTER, bool CG = false>
 __device__ __forceinline__ float stencil_sub(const Lev& L, int vx, int vy, int vz, long long v, float sum) {
   constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
   constexpr int S = IS3D ? 14 : 5;
@@ -275,7 +287,7 @@ __device__ __forceinline__ float stencil_sub(const Lev& L, int vx, int vy, int v
         in[q] = inside(L, nx, ny, nz) && !(SKIP_CENTER && s == S - 1);
         const long long nn = in[q] ? lin(L, nx, ny, nz) : v;
         a[q] = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
-        xv[q] = L.x[nn];
+        xv[q] = ldv<CG>(&L.x[nn]);
       }
 #pragma unroll
     for (int q = 0; q < 9; q++)
@@ -284,93 +296,156 @@ __device__ __forceinline__ float stencil_sub(const Lev& L, int vx, int vy, int v
   return sum;
 }
 
-// knSmoothColor on a coarse level: colour offset (ox, oy, oz) in 2x2x2 blocks
+// The same sum with every load of the stencil (and of the centre's type,
+// right-hand side and diagonal) issued before any arithmetic: one memory
+// round trip per vertex, for the cluster tail, whose passes have about one
+// vertex per thread and nothing else to overlap the latency with.
+// Levels in the tail have few slots (kTailSlots): offsets are 32-bit.
+template <bool IS3D, bool SKIP_CENTER>
+__device__ __forceinline__ float stencil_sub_flat(const Lev& L, int vx, int vy, int vz, int v, float sum) {
+  constexpr int NZ = IS3D ? 3 : 1, ZL = IS3D ? -1 : 0;
+  constexpr int S = IS3D ? 14 : 5;
+  const int n = (int)L.n;
+  float a[NZ * 9], xv[NZ * 9];
+  unsigned inm = 0;
+#pragma unroll
+  for (int s = 0; s < NZ * 9; s++) {
+    const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = s / 9 + ZL;
+    const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
+    const bool in = inside(L, nx, ny, nz) && !(SKIP_CENTER && s == S - 1);
+    inm |= in ? 1u << s : 0u;
+    const int nn = in ? (int)lin(L, nx, ny, nz) : v;
+    a[s] = s < S ? L.A[(S - 1 - s) * n + nn] : L.A[(s - S + 1) * n + v];
+    xv[s] = __ldcg(&L.x[nn]);
+  }
+#pragma unroll
+  for (int s = 0; s < NZ * 9; s++)
+    if (inm & (1u << s)) sum = sum - a[s] * xv[s];
+  return sum;
+}
+
+// knSmoothColor on a coarse level, one vertex: block bi of colour offset
+// (ox, oy, oz) in 2x2x2 blocks, bx x by blocks per z-plane
+template <bool IS3D, bool CG>
+__device__ __forceinline__ void smooth_vertex(const Lev& L, long long bi, int ox, int oy, int oz, int bx, int by) {
+  const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
+  if (!inside(L, vx, vy, vz)) return;
+  const long long v = L.colored ? (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi : lin(L, vx, vy, vz);
+  if (L.type[v] == kVtInactive) return;
+  const float sum = stencil_sub<IS3D, true, CG>(L, vx, vy, vz, v, ldv<CG>(&L.b[v]));
+  L.x[v] = sum / L.A[v];
+}
+
+// smooth_vertex for the cluster tail: the vertex type is tested after all
+// loads were issued (inactive vertices only cost loads)
+template <bool IS3D>
+__device__ __forceinline__ void smooth_vertex_flat(const Lev& L, long long bi, int ox, int oy, int oz, int bx, int by) {
+  const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
+  if (!inside(L, vx, vy, vz)) return;
+  const long long v = L.colored ? (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi : lin(L, vx, vy, vz);
+  const int8_t ty = L.type[v];
+  const float diag = L.A[v];
+  const float sum = stencil_sub_flat<IS3D, true>(L, vx, vy, vz, (int)v, __ldcg(&L.b[v]));
+  if (ty != kVtInactive) L.x[v] = sum / diag;
+}
+
+template <bool IS3D>
+__device__ __forceinline__ void residual_vertex_flat(const Lev& L, long long v) {
+  int vx, vy, vz;
+  coords(L, v, vx, vy, vz);
+  const int8_t ty = L.type[v];
+  const float r = stencil_sub_flat<IS3D, false>(L, vx, vy, vz, (int)v, __ldcg(&L.b[v]));
+  if (ty != kVtInactive) L.r[v] = r;
+}
+
+// knCalcResidual on a coarse level, one storage slot
+template <bool IS3D, bool CG>
+__device__ __forceinline__ void residual_vertex(const Lev& L, long long v) {
+  if (L.type[v] == kVtInactive) return;
+  int vx, vy, vz;
+  coords(L, v, vx, vy, vz);
+  L.r[v] = stencil_sub<IS3D, false, CG>(L, vx, vy, vz, v, ldv<CG>(&L.b[v]));
+}
+
+// knRestrict into slot v of level D from the level below (level 0 when
+// FROM0), plus knSet(x[D], 0) of the next smoothing's initial guess
+template <bool FROM0, bool CG>
+__device__ __forceinline__ void restrict_vertex(const Lev& D, const Lev& S, const Lev0& F, long long v) {
+  const int sx = FROM0 ? F.d.nx : S.sx, sy = FROM0 ? F.d.ny : S.sy, sz = FROM0 ? F.d.nz : S.sz;
+  const long long py = F.d.sy, pz = F.d.sz;
+  D.x[v] = 0.f;
+  if (D.type[v] == kVtInactive) return;
+  int vx, vy, vz;
+  coords(D, v, vx, vy, vz);
+  // the fine vertices 2V-1 .. 2V+1 inside the level, in the reference's
+  // loop order; all loads first
+  float rv[27];
+  bool in[27];
+#pragma unroll
+  for (int q = 0; q < 27; q++) {
+    const int rx = 2 * vx - 1 + q % 3, ry = 2 * vy - 1 + (q / 3) % 3, rz = 2 * vz - 1 + q / 9;
+    in[q] = rx >= 0 && ry >= 0 && rz >= 0 && rx < sx && ry < sy && rz < sz;
+    // inactive fine vertices hold r = 0: adding their term adds zero
+    rv[q] = in[q] ? (FROM0 ? F.r[rx + py * ry + pz * rz] : ldv<CG>(&S.r[lin(S, rx, ry, rz)])) : 0.f;
+  }
+  float sum = 0.f;
+#pragma unroll
+  for (int q = 0; q < 27; q++) {
+    const int rx = 2 * vx - 1 + q % 3, ry = 2 * vy - 1 + (q / 3) % 3, rz = 2 * vz - 1 + q / 9;
+    if (in[q]) sum = sum + inv_pow2(parity3(rx, ry, rz)) * rv[q];
+  }
+  D.b[v] = sum;
+}
+
+// knInterpolate from level S = D+1 and knAddAssign: x[D] += I * x[S]
+template <bool IS3D, bool CG>
+__device__ __forceinline__ void interp_vertex(const Lev& D, const Lev& S, long long v) {
+  if (D.type[v] == kVtInactive) return;
+  int vx, vy, vz;
+  coords(D, v, vx, vy, vz);
+  // coarse parents V/2 .. (V+1)/2 per axis (one or two), in the
+  // reference's loop order; inactive coarse vertices hold x = 0
+  const int hx = (vx + 1) / 2 - vx / 2, hy = (vy + 1) / 2 - vy / 2, hz = (vz + 1) / 2 - vz / 2;
+  float cv[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
+    const bool use = (ox <= hx) && (oy <= hy) && (oz <= hz);
+    cv[q] = use ? ldv<CG>(&S.x[lin(S, vx / 2 + ox, vy / 2 + oy, vz / 2 + oz)]) : 0.f;
+  }
+  float sum = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
+    if ((ox <= hx) && (oy <= hy) && (oz <= hz)) sum = sum + cv[q];
+  }
+  D.x[v] = ldv<CG>(&D.x[v]) + inv_pow2(parity3(vx, vy, vz)) * sum;
+}
+
 template <bool IS3D>
 __global__ void __launch_bounds__(256, 3) k_mg_smooth(Lev L, int S, int ox, int oy, int oz, const CgScalars* sc) {
   if (sc->done) return;
   const int bx = (L.sx + 1) / 2, by = (L.sy + 1) / 2, bz = (L.sz + 1) / 2;
   const long long nb = (long long)bx * by * bz;
-  GRID_STRIDE(bi, nb) {
-    const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
-    if (!inside(L, vx, vy, vz)) continue;
-    const long long v = L.colored ? (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi : lin(L, vx, vy, vz);
-    if (L.type[v] == kVtInactive) continue;
-    const float sum = stencil_sub<IS3D, true>(L, vx, vy, vz, v, L.b[v]);
-    L.x[v] = sum / L.A[v];
-  }
+  GRID_STRIDE(bi, nb) smooth_vertex<IS3D, false>(L, bi, ox, oy, oz, bx, by);
 }
 
-// knCalcResidual on a coarse level
 template <bool IS3D>
 __global__ void __launch_bounds__(256, 3) k_mg_residual(Lev L, int S, const CgScalars* sc) {
   if (sc->done) return;
-  GRID_STRIDE(v, L.n) {
-    if (L.type[v] == kVtInactive) continue;
-    int vx, vy, vz;
-    coords(L, v, vx, vy, vz);
-    L.r[v] = stencil_sub<IS3D, false>(L, vx, vy, vz, v, L.b[v]);
-  }
+  GRID_STRIDE(v, L.n) residual_vertex<IS3D, false>(L, v);
 }
 
-// knRestrict into level D from the level below (level 0 when FROM0), plus
-// knSet(x[D], 0) of the next smoothing's initial guess
 template <bool FROM0>
 __global__ void __launch_bounds__(256) k_mg_restrict(Lev D, Lev S, Lev0 F, const CgScalars* sc) {
   if (sc->done) return;
-  const int sx = FROM0 ? F.d.nx : S.sx, sy = FROM0 ? F.d.ny : S.sy, sz = FROM0 ? F.d.nz : S.sz;
-  const long long py = F.d.sy, pz = F.d.sz;
-  GRID_STRIDE(v, D.n) {
-    D.x[v] = 0.f;
-    if (D.type[v] == kVtInactive) continue;
-    int vx, vy, vz;
-    coords(D, v, vx, vy, vz);
-    // the fine vertices 2V-1 .. 2V+1 inside the level, in the reference's
-    // loop order; all loads first
-    float rv[27];
-    bool in[27];
-#pragma unroll
-    for (int q = 0; q < 27; q++) {
-      const int rx = 2 * vx - 1 + q % 3, ry = 2 * vy - 1 + (q / 3) % 3, rz = 2 * vz - 1 + q / 9;
-      in[q] = rx >= 0 && ry >= 0 && rz >= 0 && rx < sx && ry < sy && rz < sz;
-      // inactive fine vertices hold r = 0: adding their term adds zero
-      rv[q] = in[q] ? (FROM0 ? F.r[rx + py * ry + pz * rz] : S.r[lin(S, rx, ry, rz)]) : 0.f;
-    }
-    float sum = 0.f;
-#pragma unroll
-    for (int q = 0; q < 27; q++) {
-      const int rx = 2 * vx - 1 + q % 3, ry = 2 * vy - 1 + (q / 3) % 3, rz = 2 * vz - 1 + q / 9;
-      if (in[q]) sum = sum + inv_pow2(parity3(rx, ry, rz)) * rv[q];
-    }
-    D.b[v] = sum;
-  }
+  GRID_STRIDE(v, D.n) restrict_vertex<FROM0, false>(D, S, F, v);
 }
 
-// knInterpolate from level S = D+1 and knAddAssign: x[D] += I * x[S]
 template <bool IS3D>
 __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev S, const CgScalars* sc) {
   if (sc->done) return;
-  GRID_STRIDE(v, D.n) {
-    if (D.type[v] == kVtInactive) continue;
-    int vx, vy, vz;
-    coords(D, v, vx, vy, vz);
-    // coarse parents V/2 .. (V+1)/2 per axis (one or two), in the
-    // reference's loop order; inactive coarse vertices hold x = 0
-    const int hx = (vx + 1) / 2 - vx / 2, hy = (vy + 1) / 2 - vy / 2, hz = (vz + 1) / 2 - vz / 2;
-    float cv[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
-      const bool use = (ox <= hx) && (oy <= hy) && (oz <= hz);
-      cv[q] = use ? S.x[lin(S, vx / 2 + ox, vy / 2 + oy, vz / 2 + oz)] : 0.f;
-    }
-    float sum = 0.f;
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
-      if ((ox <= hx) && (oy <= hy) && (oz <= hz)) sum = sum + cv[q];
-    }
-    D.x[v] = D.x[v] + inv_pow2(parity3(vx, vy, vz)) * sum;
-  }
+  GRID_STRIDE(v, D.n) interp_vertex<IS3D, false>(D, S, v);
 }
 
 // ---- fused level-0 passes.  A CTA of 32 x 8 threads owns a 28 x 12 x 8
@@ -763,6 +838,263 @@ __global__ void __launch_bounds__(kCgThreads) k_mg_coarse_cg(Lev L, Lev0 F, cons
 }
 constexpr size_t kCgDynSmem = (size_t)kCgNb * kCgThreads * (sizeof(float) + sizeof(short));
 
+// ---- the coarse end of the V-cycle in one launch: one thread-block
+// cluster (16 CTAs, 8 where 16 cannot be co-scheduled) runs the levels from
+// `first` down, the coarsest-level CG and the levels back up.  The colour
+// passes of these levels have a few thousand to a few hundred thousand
+// vertices; as separate launches each costs a launch and a cold pipeline,
+// here a hardware cluster barrier.  Every pass does the per-vertex float
+// operations of the separate kernels above (the same device functions), so
+// the levels' results are bit-identical to them; vectors written inside
+// the launch are read at L2 (ldv<true>).
+constexpr int kTailThreads = 384;
+constexpr int kTailMaxCta = 16;
+constexpr int kTailVpc = 128;  // coarsest-level vertices per CTA (<= 1024 over >= 8 CTAs)
+constexpr long long kTailSlots = 100000;  // largest level run inside the cluster (33^3 and below)
+
+struct TailSmem {
+  float coef[kCgNb][kTailVpc];  // own vertices' stencils (applyAStencil order)
+  short nbr[kCgNb][kTailVpc];
+  unsigned char nn[kTailVpc];
+  float ph[kCgThreads], pl[kCgThreads];  // the whole search vector p
+  float zh[kCgThreads], zl[kCgThreads];  // the whole z: every CTA stores its share into every CTA
+  ff wpart[kTailThreads / 32][2];        // per-warp partial dot products
+  ff cpart[kTailMaxCta][3];              // per-CTA partials (rr, rz | pq), stored by each CTA into every CTA
+};
+
+// f1 < f2 for normalised pairs
+__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+// a / b for pairs (long division: a float quotient and a correction)
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  const float q1 = a.h / b.h;
+  const ff r = ff_add(a, ff_neg(ff_mul(b, ff{q1, 0.f})));
+  const float q2 = r.h / b.h;
+  return quick_two_sum(q1, q2);
+}
+
+// The CTA's sums of NV pairs held by the lanes with sub == 0 (zero
+// elsewhere), stored into cpart[rank][slot..] of every CTA of the cluster;
+// the caller's cluster barrier publishes them.  The pq slot is apart from
+// the rr / rz slots: a CTA may store the next phase's sums while another
+// still reads this phase's.
+template <int NV>
+__device__ __forceinline__ void tail_push_sums(cooperative_groups::cluster_group& cl, TailSmem& sm, ff* v, int tpv,
+                                               int slot) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 16; o >= tpv; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      const ff w{__shfl_xor_sync(0xffffffffu, v[q].h, o), __shfl_xor_sync(0xffffffffu, v[q].l, o)};
+      v[q] = ff_add(v[q], w);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++) sm.wpart[wid][q] = v[q];
+  __syncthreads();
+  if (wid == 0) {
+    const int ncta = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      ff t = lane < nw ? sm.wpart[lane][q] : ff{0.f, 0.f};
+      for (int o = 16; o > 0; o >>= 1) {
+        const ff w{__shfl_xor_sync(0xffffffffu, t.h, o), __shfl_xor_sync(0xffffffffu, t.l, o)};
+        t = ff_add(t, w);
+      }
+      if (lane < ncta) *cl.map_shared_rank(&sm.cpart[rank][slot + q], lane) = t;
+    }
+  }
+}
+
+// after the cluster barrier: the cluster's sum of cpart[.][q], summed in
+// the same order in every warp of every CTA (identical bits everywhere)
+__device__ __forceinline__ ff tail_total(const TailSmem& sm, int q, int ncta) {
+  const int lane = threadIdx.x & 31;
+  ff t = lane < ncta ? sm.cpart[lane][q] : ff{0.f, 0.f};
+  for (int o = 16; o > 0; o >>= 1) {
+    const ff w{__shfl_xor_sync(0xffffffffu, t.h, o), __shfl_xor_sync(0xffffffffu, t.l, o)};
+    t = ff_add(t, w);
+  }
+  return t;
+}
+
+// this CTA's z values into zh/zl of every CTA (the tpv lanes of a vertex
+// hold the same z and share its stores)
+__device__ __forceinline__ void tail_push_z(cooperative_groups::cluster_group& cl, TailSmem& sm, bool own, int v, int sub,
+                                            int tpv, ff z) {
+  if (!own) return;
+  const int ncta = (int)cl.num_blocks();
+  for (int rk = sub; rk < ncta; rk += tpv) {
+    *cl.map_shared_rank(&sm.zh[v], rk) = z.h;
+    *cl.map_shared_rank(&sm.zl[v], rk) = z.l;
+  }
+}
+
+// GridMg::solveCG (multigrid.cpp:793-902) on the coarsest level across the
+// cluster: CTA c owns vertices [c*vpc, (c+1)*vpc), tpv threads per vertex
+// split its stencil.  Each CTA stores its partial dot products and its z
+// values into the shared memory of every CTA before a cluster barrier, so
+// every CTA then holds the whole z (and rebuilds the whole p) and all
+// partials; an iteration has two barriers and no remote loads.  Vectors,
+// dot products and scalars are double-float pairs on the FP32 pipe (the
+// stencil product is a compensated sum of exact float products); the
+// iterates follow an IEEE-double CG to ~1e-14 relative.  Every warp forms
+// the scalars from the same rank-ordered sums, so all CTAs take the same
+// branches.
+template <bool IS3D>
+__device__ void tail_coarse_cg(cooperative_groups::cluster_group& cl, const Lev& L, int S, float accuracy, TailSmem& sm) {
+  const int ncta = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int n = (int)L.n;
+  const int vpc = (n + ncta - 1) / ncta;
+  int tpv = 8;
+  while (tpv > 1 && tpv * vpc > (int)blockDim.x) tpv >>= 1;
+  const int lv = threadIdx.x / tpv, sub = threadIdx.x % tpv;
+  const int v = rank * vpc + lv;
+  const bool own = lv < vpc && v < n;
+  bool act = false;
+  float diag = 1.f, bv = 0.f;
+  if (own) {
+    act = L.type[v] != kVtInactive;
+    if (act) {
+      diag = L.A[v];
+      bv = __ldcg(&L.b[v]);
+    }
+    if (sub == 0) {
+      int nn = 0;
+      if (act) {
+        constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
+        int vx, vy, vz;
+        coords(L, v, vx, vy, vz);
+        int s = 0;
+        for (int dz = ZL; dz <= ZH; dz++)
+          for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++, s++) {
+              const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
+              if (!inside(L, nx, ny, nz)) continue;
+              const int q = (int)lin(L, nx, ny, nz);
+              if (L.type[q] == kVtInactive) continue;
+              sm.coef[nn][lv] = s < S ? L.A[(long long)(S - 1 - s) * L.n + q] : L.A[(long long)(s - S + 1) * L.n + v];
+              sm.nbr[nn][lv] = (short)q;
+              nn++;
+            }
+      }
+      sm.nn[lv] = (unsigned char)nn;
+    }
+  }
+  const bool lead = act && sub == 0;
+  // x = 0, so r = b - A*0 = b
+  ff x{0.f, 0.f}, r{0.f, 0.f}, z{0.f, 0.f};
+  if (act) {
+    r = ff{bv, 0.f};
+    z = ff_div_f(r, diag);
+  }
+  tail_push_z(cl, sm, own, v, sub, tpv, z);
+  {
+    ff t[2] = {lead ? ff_mul(r, r) : ff{0.f, 0.f}, lead ? ff_mul(r, z) : ff{0.f, 0.f}};
+    tail_push_sums<2>(cl, sm, t, tpv, 0);
+  }
+  cl.sync();
+  const ff rr0 = tail_total(sm, 0, ncta);
+  ff alphaTop = tail_total(sm, 1, ncta);
+  // residual / initialResidual < accuracy  <=>  rr < rr0 * accuracy^2
+  const ff stopAt = ff_mul(rr0, two_prod(accuracy, accuracy));
+  for (int u = threadIdx.x; u < n; u += blockDim.x) {  // p = z
+    sm.ph[u] = sm.zh[u];
+    sm.pl[u] = sm.zl[u];
+  }
+  __syncthreads();
+  const int nn = own ? sm.nn[lv] : 0;
+  // initialResidual > 1e-12
+  for (int iter = 0; iter < 10000 && rr0.h > 1e-24f; iter++) {
+    // q = A p: this lane's share of the stencil as a compensated sum, then
+    // the vertex's lanes
+    float qs = 0.f, qe = 0.f;
+    for (int e = sub; e < nn; e += tpv) {
+      const int k = sm.nbr[e][lv];
+      const float c = sm.coef[e][lv];
+      const ff pr = two_prod(c, sm.ph[k]);
+      const ff t = two_sum(qs, pr.h);
+      qs = t.h;
+      qe = qe + (t.l + (pr.l + c * sm.pl[k]));
+    }
+    ff q = two_sum(qs, qe);
+    for (int o = tpv >> 1; o > 0; o >>= 1) {
+      const ff w{__shfl_xor_sync(0xffffffffu, q.h, o), __shfl_xor_sync(0xffffffffu, q.l, o)};
+      q = ff_add(q, w);
+    }
+    const ff p = own ? ff{sm.ph[v], sm.pl[v]} : ff{0.f, 0.f};
+    {
+      ff t[1] = {lead ? ff_mul(p, q) : ff{0.f, 0.f}};
+      tail_push_sums<1>(cl, sm, t, tpv, 2);
+    }
+    cl.sync();
+    const ff alpha = ff_div(alphaTop, tail_total(sm, 2, ncta));
+    ff t[2] = {ff{0.f, 0.f}, ff{0.f, 0.f}};
+    if (act) {
+      x = ff_add(x, ff_mul(alpha, p));
+      r = ff_add(r, ff_neg(ff_mul(alpha, q)));
+      z = ff_div_f(r, diag);
+      if (sub == 0) {
+        t[0] = ff_mul(r, r);
+        t[1] = ff_mul(r, z);
+      }
+    }
+    tail_push_z(cl, sm, own, v, sub, tpv, z);
+    tail_push_sums<2>(cl, sm, t, tpv, 0);
+    cl.sync();
+    const ff rr = tail_total(sm, 0, ncta);
+    const ff atn = tail_total(sm, 1, ncta);
+    if (ff_lt(rr, stopAt)) break;
+    const ff beta = ff_div(atn, alphaTop);
+    alphaTop = atn;
+    for (int u = threadIdx.x; u < n; u += blockDim.x) {
+      const ff pu = ff_add(ff{sm.zh[u], sm.zl[u]}, ff_mul(beta, ff{sm.ph[u], sm.pl[u]}));
+      sm.ph[u] = pu.h;
+      sm.pl[u] = pu.l;
+    }
+    __syncthreads();
+  }
+  if (own && sub == 0) L.x[v] = x.h + x.l;
+}
+
+template <bool IS3D>
+__global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(const Lev* __restrict__ levs, int first, int last, int S,
+                                                             float accuracy, const CgScalars* sc) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  if (sc->done) return;  // the same for every CTA of the cluster
+  __shared__ TailSmem sm;
+  const long long T = (long long)cl.num_blocks() * blockDim.x;
+  const long long t0 = (long long)cl.block_rank() * blockDim.x + threadIdx.x;
+  constexpr int ncol = IS3D ? 8 : 4;
+  for (int l = first; l < last; l++) {
+    const Lev L = levs[l];
+    const int bx = (L.sx + 1) / 2, by = (L.sy + 1) / 2;
+    const long long nb = (long long)bx * by * ((L.sz + 1) / 2);
+    for (int c = 0; c < ncol; c++) {
+      for (long long bi = t0; bi < nb; bi += T) smooth_vertex_flat<IS3D>(L, bi, c & 1, (c >> 1) & 1, c >> 2, bx, by);
+      cl.sync();
+    }
+    for (long long v = t0; v < L.n; v += T) residual_vertex_flat<IS3D>(L, v);
+    cl.sync();
+    const Lev D = levs[l + 1];
+    for (long long v = t0; v < D.n; v += T) restrict_vertex<false, true>(D, L, Lev0{}, v);
+    cl.sync();
+  }
+  tail_coarse_cg<IS3D>(cl, levs[last], S, accuracy, sm);
+  cl.sync();  // x of the coarsest level written; no CTA reads another's shared memory any more
+  for (int l = last - 1; l >= first; l--) {
+    const Lev D = levs[l], Sv = levs[l + 1];
+    for (long long v = t0; v < D.n; v += T) interp_vertex<IS3D, true>(D, Sv, v);
+    cl.sync();
+    const int bx = (D.sx + 1) / 2, by = (D.sy + 1) / 2;
+    const long long nb = (long long)bx * by * ((D.sz + 1) / 2);
+    for (int c = ncol - 1; c >= 0; c--) {
+      for (long long bi = t0; bi < nb; bi += T) smooth_vertex_flat<IS3D>(D, bi, c & 1, (c >> 1) & 1, c >> 2, bx, by);
+      cl.sync();
+    }
+  }
+}
+
 // sigmaNew = dot(tmp, residual) and beta (GridCg::iterate after the
 // preconditioner, conjugategrad.cpp:277-299)
 __global__ void __launch_bounds__(256) k_mg_dot_beta(long long n, const float* __restrict__ t, const float* __restrict__ r,
@@ -860,6 +1192,26 @@ int ensure_paths() {
       cudaFuncSetAttribute(k_mg0_up<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t2) != cudaSuccess ||
       cudaFuncSetAttribute(k_mg0_up<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t2) != cudaSuccess)
     return 1;
+  // the cluster V-cycle tail: 16 CTAs where the GPU can co-schedule them
+  g_tailCta = 0;
+  if (cudaFuncSetAttribute(k_mg_tail<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+      cudaFuncSetAttribute(k_mg_tail<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    for (int c = 16; c >= 8 && !g_tailCta; c /= 2) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = c;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(c);
+      cfg.blockDim = dim3(kTailThreads);
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nc = 0;
+      if (cudaOccupancyMaxActiveClusters(&nc, k_mg_tail<true>, &cfg) == cudaSuccess && nc >= 1) g_tailCta = c;
+    }
+  }
+  cudaGetLastError();  // a GPU without clusters keeps the per-level launches
   g_pathsReady = true;
   return 0;
 }
@@ -972,6 +1324,8 @@ struct MgHierarchy {
   MgProfHook hook = nullptr;
   void* hookCtx = nullptr;
   float coarseAcc = 1e-8f;
+  Lev* dlev = nullptr;  // lev[] on the device, for the cluster tail
+  int tailFirst = 0;    // first level of the cluster tail (0: none)
   size_t bytes = 0;
   std::vector<void*> allocs;
   bool ok = true;
@@ -1038,6 +1392,17 @@ MgHierarchy* mg_hierarchy_create(const Dims& d) {
   }
   const long long nc = L > 1 ? h->lev[L - 1].n : n0;
   if (nc > kCgThreads) h->ok = false;  // the level loop guarantees <= 1000
+  // the levels of at most kTailSlots storage slots (and the coarsest) run in
+  // one cluster launch
+  if (h->ok && L > 1 && g_tailCta && nc <= (long long)g_tailCta * kTailVpc) {
+    long long lim = kTailSlots;
+    if (const char* e = std::getenv("MANTAGPU_MG_TAIL_SLOTS")) lim = std::atoll(e);
+    int f = L - 1;
+    while (f > 1 && h->lev[f - 1].n <= lim) f--;
+    h->tailFirst = f;
+    h->dlev = h->alloc<Lev>(L);
+    if (h->ok && cudaMemcpy(h->dlev, h->lev, sizeof(Lev) * (size_t)L, cudaMemcpyHostToDevice) != cudaSuccess) h->ok = false;
+  }
   if (!h->ok) {
     mg_hierarchy_destroy(h);
     return nullptr;
@@ -1194,7 +1559,9 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       count_launch();
       k_mg_restrict<true><<<blocks_for(h->lev[1].n), kThreads1, 0, s>>>(h->lev[1], none, l0, sc);
     }
-    for (int l = 1; l < L; l++) {
+    // levels below the cluster tail (all of them without one)
+    const int first = h->tailFirst ? h->tailFirst : L;
+    for (int l = 1; l < first; l++) {
       smooth(l, false);
       Fam f(h, "mg_transfer_coarse");
       count_launch();
@@ -1203,13 +1570,31 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       count_launch();
       k_mg_restrict<false><<<blocks_for(h->lev[l + 1].n), kThreads1, 0, s>>>(h->lev[l + 1], h->lev[l], l0, sc);
     }
-    {
+    if (h->tailFirst) {
+      Fam f(h, "mg_tail");
+      count_launch();
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = g_tailCta;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(g_tailCta);
+      cfg.blockDim = dim3(kTailThreads);
+      cfg.stream = s;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      const Lev* dl = h->dlev;
+      const float acc = h->coarseAcc;
+      if (h->is3d) cudaLaunchKernelEx(&cfg, k_mg_tail<true>, dl, first, L, S, acc, sc);
+      else cudaLaunchKernelEx(&cfg, k_mg_tail<false>, dl, first, L, S, acc, sc);
+    } else {
       Fam f(h, "mg_coarse_cg");
       count_launch();
       if (h->is3d) k_mg_coarse_cg<true, false><<<1, kCgThreads, kCgDynSmem, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
       else k_mg_coarse_cg<false, false><<<1, kCgThreads, kCgDynSmem, s>>>(h->lev[L], l0, res, x0, S, h->coarseAcc, sc);
     }
-    for (int l = L - 1; l >= 1; l--) {
+    for (int l = first - 1; l >= 1; l--) {
       {
       Fam f(h, "mg_transfer_coarse");
       count_launch();

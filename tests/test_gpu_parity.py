@@ -318,16 +318,23 @@ def test_multigrid_ghost_fluid_against_oracle():
     assert np.max(np.abs(vel.numpy() - vo)) <= 1e-4
 
 
-@pytest.mark.parametrize("shape,liquid", [((40, 36, 30), False), ((37, 29, 41), True), ((90, 70, 1), False),
-                                          ((24, 20, 18), False)])
-def test_multigrid_vcycle_against_oracle(shape, liquid):
+@pytest.mark.parametrize("shape,liquid,tail", [((40, 36, 30), False, None), ((37, 29, 41), True, None),
+                                               ((90, 70, 1), False, None), ((24, 20, 18), False, None),
+                                               ((40, 36, 30), False, "0"), ((90, 70, 1), False, "0"),
+                                               ((37, 29, 41), True, "5000"), ((90, 70, 1), False, "700")])
+def test_multigrid_vcycle_against_oracle(shape, liquid, tail, monkeypatch):
     """One V-cycle of the multigrid preconditioner (GridMg::setA + setRhs +
     doVCycle) on a random residual against the oracle's restatement of the
     reference.  Smoothing, restriction, interpolation and the Galerkin
     operators repeat the reference's float operations, so the cells must
     agree bit for bit; only the coarsest-level CG (double-float, tree sums)
-    may move a last bit, which the smoothers then spread a little."""
+    may move a last bit, which the smoothers then spread a little.  `tail`
+    moves the boundary of the single-launch cluster tail (levels of at most
+    that many slots): "0" leaves only the coarsest CG in it, the default
+    takes every level of these grids."""
     import ctypes as C
+    if tail is not None:
+        monkeypatch.setenv("MANTAGPU_MG_TAIL_SLOTS", tail)
     f, _ = _obstacle_scene(shape, 31, liquid=liquid)
     nx, ny, nz = shape
     rng = np.random.default_rng(5)
