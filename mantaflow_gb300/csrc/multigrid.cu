@@ -448,136 +448,166 @@ __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev S, const CgSca
   GRID_STRIDE(v, D.n) interp_vertex<IS3D, false>(D, S, v);
 }
 
-// ---- fused level-0 passes.  A CTA of 32 x 8 threads owns a 28 x 12 x 8
-// box of fine cells (28 x 12 in 2D) and stages code and residual of the box
-// plus a 2-cell halo -- a 32 x 16 x 12 region, one warp per region row -- in
-// shared memory.  Every cell goes through exactly the float operations of
-// the per-colour Gauss-Seidel passes, in the same order; halo cells are
-// recomputed by each CTA that needs them.
-constexpr int kTX = 28, kTY = 12, kTZ = 8;
-template <bool IS3D>
-struct Tile0 {
-  static constexpr int tz = IS3D ? kTZ : 1, hz = IS3D ? 2 : 0;
-  static constexpr int RX = 32, RY = 16, RZ = tz + 2 * hz;
-  static constexpr int NR = RX * RY * RZ;
-  static constexpr int PER = RZ * 2;  // region cells per thread: (ty, ty+8) x RZ planes
-  static constexpr size_t smem = (size_t)NR * (sizeof(uint16_t) + 2 * sizeof(float));
-  // level-1 parents of the region (the region starts at an even coordinate)
-  static constexpr int CX = RX / 2 + 1, CY = RY / 2 + 1, CZ = IS3D ? RZ / 2 + 1 : 1;
-  static constexpr int CN = CX * CY * CZ;
+// ---- fused level-0 passes, streamed along z.  A CTA of 32 x 8 threads
+// owns a 28 x 12 column of fine cells over kZC planes (28 x 12 cells in 2D)
+// and walks the column's region -- the owned cells plus a 2-cell halo,
+// 32 x 16 cells per plane, one warp per two rows -- plane by plane, keeping
+// the last four planes of code, right-hand side, diagonal and x in shared
+// memory.  In each step plane p is staged (stage A), plane p-1 gets its
+// colour-1 pass (B) and plane p-2 its last pass (C), so every cell goes
+// through exactly the float operations of the per-colour Gauss-Seidel
+// passes, in the same order; halo cells are recomputed by each CTA that
+// needs them.  The next plane's loads are issued before the current
+// plane's passes.
+constexpr int kTX = 28, kTY = 12, kZC = 32;
+constexpr int kRX = 32, kRY = 16;
+
+struct Ring0 {  // four planes of the region
+  float res[4][kRY][kRX];
+  float x[4][kRY][kRX];
+  float diag[4][kRY][kRX];
+  uint16_t code[4][kRY][kRX];
 };
-// region cell k of this thread: x = lane, y = ty + 8 (k & 1), z = k >> 1
-#define T0_CELL(k, lx, ly, lz, q)                          \
-  const int lx = threadIdx.x & 31;                         \
-  const int ly = (threadIdx.x >> 5) + 8 * ((k) & 1);       \
-  const int lz = (k) >> 1;                                 \
-  const int q = lx + T::RX * (ly + T::RY * lz);
+__device__ __forceinline__ int ring0(int p) { return (p + 8) & 3; }  // p >= -2
 
-// the linked neighbours (kLow/kHigh order of the reference's sums) added
-template <bool IS3D>
-__device__ __forceinline__ float add_links(int c, const float* __restrict__ sx, int q, float sum) {
-  constexpr int RX = 32, RXY = 32 * 16;
-  if (c & kLowX) sum = sum + sx[q - 1];
-  if (c & kHighX) sum = sum + sx[q + 1];
-  if (c & kLowY) sum = sum + sx[q - RX];
-  if (c & kHighY) sum = sum + sx[q + RX];
-  if (IS3D) {
-    if (c & kLowZ) sum = sum + sx[q - RXY];
-    if (c & kHighZ) sum = sum + sx[q + RXY];
-  }
-  return sum;
-}
-
-// stage code and residual (masked to active cells) of the region; the
-// loads of one chunk are all issued before its stores
-template <bool IS3D>
-__device__ __forceinline__ void tile0_load(const Lev0& F, const float* __restrict__ res, uint16_t* scode, float* sres,
-                                           const float* __restrict__ xsrc, float* sx, int ox, int oy, int oz) {
-  using T = Tile0<IS3D>;
-  constexpr int CH = 8;
+// one plane of this thread's two region cells (rows ty and ty + 8)
+struct Plane0 {
+  int c[2];
+  float r[2], a[2], xd[2];
+};
+template <bool UP>
+__device__ __forceinline__ void load_plane0(const Lev0& F, const float* __restrict__ res, int ox, int oy, int p, Plane0& P) {
   const Dims& d = F.d;
-#pragma unroll 1
-  for (int k0 = 0; k0 < T::PER; k0 += CH) {
-    int cv[CH];
-    float rv[CH], xv[CH];
+  const int gx = ox + (int)(threadIdx.x & 31);
 #pragma unroll
-    for (int j = 0; j < CH; j++) {
-      const int k = k0 + j;
-      T0_CELL(k, lx, ly, lz, q)
-      (void)q;
-      const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-      const bool in = k < T::PER && gx >= 0 && gy >= 0 && gz >= 0 && gx < d.nx && gy < d.ny && gz < d.nz;
-      const long long g = in ? ix(d, gx, gy, gz) : 0;
-      cv[j] = in ? F.code[g] : 0;
-      rv[j] = in ? res[g] : 0.f;
-      xv[j] = (in && xsrc) ? xsrc[g] : 0.f;
-    }
-#pragma unroll
-    for (int j = 0; j < CH; j++) {
-      const int k = k0 + j;
-      if (k >= T::PER) continue;
-      T0_CELL(k, lx, ly, lz, q)
-      (void)lx; (void)ly; (void)lz;
-      scode[q] = (uint16_t)cv[j];
-      sres[q] = (cv[j] & kMgActive) ? rv[j] : 0.f;
-      if (xsrc) sx[q] = xv[j];
-    }
+  for (int k = 0; k < 2; k++) {
+    const int gy = oy + (int)(threadIdx.x >> 5) + 8 * k;
+    const bool in = p >= 0 && p < d.nz && gx >= 0 && gy >= 0 && gx < d.nx && gy < d.ny;
+    const long long g = in ? ix(d, gx, gy, p) : 0;
+    P.c[k] = in ? F.code[g] : 0;
+    P.r[k] = in ? res[g] : 0.f;
+    P.a[k] = (in && F.a0f) ? F.a0f[g] : 0.f;
+    if (UP) P.xd[k] = in ? F.xd[g] : 0.f;
   }
 }
 
 __device__ __forceinline__ float scaled_b(int c, float r) { return (c & kMgTrivial) ? r * kTrivialScale : r; }
 
+// stage A: the plane into the ring; x is the colour-0 value from the zero
+// guess (down) or x + I * x[1] (up, from the two coarse planes in cx)
+template <bool IS3D, bool UP>
+__device__ __forceinline__ void stage0_a(Ring0& R, const Plane0& P, bool hasA0f, int ox, int oy, int p, int cx0, int cy0,
+                                         const float (*cx)[kRY / 2 + 1][kRX / 2 + 1]) {
+  const int sl = ring0(p);
+  const int lx = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int row = (threadIdx.x >> 5) + 8 * k;
+    const int c = P.c[k];
+    const bool act = (c & kMgActive) != 0;
+    const float diag = hasA0f ? P.a[k] : ((c & kMgTrivial) ? kTrivialScale : (float)(c & 7));
+    const float r = act ? P.r[k] : 0.f;
+    float x = 0.f;
+    if (!UP) {
+      if (((ox + lx + oy + row + p) & 1) == 0 && act) x = scaled_b(c, r) / diag;
+    } else {
+      x = P.xd[k];
+      if (act) {
+        const int vx = ox + lx, vy = oy + row, vz = p;
+        const int hx = vx & 1, hy = vy & 1, hz = vz & 1;  // two parents along odd axes
+        const int bx = vx / 2 - cx0, by = vy / 2 - cy0;
+        float sum = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int ax = j & 1, ay = (j >> 1) & 1, az = j >> 2;
+          if (ax <= hx && ay <= hy && az <= hz) sum = sum + cx[(vz / 2 + az) & 1][by + ay][bx + ax];
+        }
+        x = x + inv_pow2(hx + hy + hz) * sum;
+      }
+    }
+    R.code[sl][row][lx] = (uint16_t)c;
+    R.res[sl][row][lx] = r;
+    R.diag[sl][row][lx] = diag;
+    R.x[sl][row][lx] = x;
+  }
+}
+
+// the linked neighbours (kLow/kHigh order of the reference's sums) added
+template <bool IS3D>
+__device__ __forceinline__ float add_links0(const Ring0& R, int c, int q, int row, int lx, float sum) {
+  const int sl = ring0(q);
+  if (c & kLowX) sum = sum + R.x[sl][row][lx - 1];
+  if (c & kHighX) sum = sum + R.x[sl][row][lx + 1];
+  if (c & kLowY) sum = sum + R.x[sl][row - 1][lx];
+  if (c & kHighY) sum = sum + R.x[sl][row + 1][lx];
+  if (IS3D) {
+    if (c & kLowZ) sum = sum + R.x[ring0(q - 1)][row][lx];
+    if (c & kHighZ) sum = sum + R.x[ring0(q + 1)][row][lx];
+  }
+  return sum;
+}
+
+// stage B: colour 1 on plane q, region minus its outer ring (reads
+// colour-0 values only)
+template <bool IS3D>
+__device__ __forceinline__ void stage0_b(Ring0& R, int ox, int oy, int q) {
+  const int sl = ring0(q);
+  const int lx = threadIdx.x & 31;
+  if (lx < 1 || lx > kRX - 2) return;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int row = (threadIdx.x >> 5) + 8 * k;
+    if (row < 1 || row > kRY - 2) continue;
+    const int c = R.code[sl][row][lx];
+    if (((ox + lx + oy + row + q) & 1) == 0 || !(c & kMgActive)) continue;
+    R.x[sl][row][lx] = add_links0<IS3D>(R, c, q, row, lx, scaled_b(c, R.res[sl][row][lx])) / R.diag[sl][row][lx];
+  }
+}
+
 // V-cycle entry on level 0: colour 0 from x = 0, colour 1, then the
 // residual (knSmoothColor x2 + knCalcResidual); writes x (to F.xd) and r of
-// the box
+// the owned cells
 template <bool IS3D>
-__global__ void __launch_bounds__(256, 3) k_mg0_down(Lev0 F, const float* __restrict__ res, const CgScalars* sc) {
+__global__ void __launch_bounds__(256, 4) k_mg0_down(Lev0 F, const float* __restrict__ res, const CgScalars* sc) {
   if (sc->done) return;
-  using T = Tile0<IS3D>;
-  extern __shared__ __align__(16) unsigned char t0_smem[];
-  float* sres = (float*)t0_smem;
-  float* sx = sres + T::NR;
-  uint16_t* scode = (uint16_t*)(sx + T::NR);
+  __shared__ Ring0 R;
   const Dims& d = F.d;
-  const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2, oz = blockIdx.z * T::tz - T::hz;
-  tile0_load<IS3D>(F, res, scode, sres, nullptr, sx, ox, oy, oz);
-  __syncthreads();
-  // colour 0 from the zero guess: x = b / A0, over the whole region
-#pragma unroll 4
-  for (int k = 0; k < T::PER; k++) {
-    T0_CELL(k, lx, ly, lz, q)
-    const int c = scode[q];
-    float v = 0.f;
-    if ((((ox + lx) + (oy + ly) + (oz + lz)) & 1) == 0 && (c & kMgActive))
-      v = scaled_b(c, sres[q]) / l0_diag(c, F.a0f, ix(d, ox + lx, oy + ly, oz + lz));
-    sx[q] = v;
-  }
-  __syncthreads();
-  // colour 1 on the region minus its outer ring (reads colour-0 values only)
-#pragma unroll 4
-  for (int k = 0; k < T::PER; k++) {
-    T0_CELL(k, lx, ly, lz, q)
-    if (lx < 1 || lx > T::RX - 2 || ly < 1 || ly > T::RY - 2) continue;
-    if (IS3D && (lz < 1 || lz > T::RZ - 2)) continue;
-    const int c = scode[q];
-    if ((((ox + lx) + (oy + ly) + (oz + lz)) & 1) == 0 || !(c & kMgActive)) continue;
-    sx[q] = add_links<IS3D>(c, sx, q, scaled_b(c, sres[q])) / l0_diag(c, F.a0f, ix(d, ox + lx, oy + ly, oz + lz));
-  }
-  __syncthreads();
-  // residual and x of the owned box
-#pragma unroll 4
-  for (int k = 0; k < T::PER; k++) {
-    T0_CELL(k, lx, ly, lz, q)
-    if (lx < 2 || lx >= 2 + kTX || ly < 2 || ly >= 2 + kTY || lz < T::hz || lz >= T::hz + T::tz) continue;
-    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-    if (gx >= d.nx || gy >= d.ny || gz >= d.nz) continue;
-    const long long g = ix(d, gx, gy, gz);
-    const int c = scode[q];
-    F.xd[g] = sx[q];
-    if (!(c & kMgActive)) continue;
-    float sum = add_links<IS3D>(c, sx, q, scaled_b(c, sres[q]));
-    sum = sum - l0_diag(c, F.a0f, g) * sx[q];
-    F.r[g] = sum;
+  constexpr int ZH = IS3D ? 1 : 0;
+  const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2;
+  const int zb = IS3D ? blockIdx.z * kZC : 0, ze = IS3D ? min(zb + kZC, d.nz) : 1;
+  const int pbeg = zb - 2 * ZH, pend = ze - 1 + 2 * ZH;
+  const bool hasA0f = F.a0f != nullptr;
+  const int lx = threadIdx.x & 31;
+  Plane0 P;
+  load_plane0<false>(F, res, ox, oy, pbeg, P);
+  for (int p = pbeg; p <= pend; p++) {
+    stage0_a<IS3D, false>(R, P, hasA0f, ox, oy, p, 0, 0, nullptr);
+    if (p < pend) load_plane0<false>(F, res, ox, oy, p + 1, P);
+    __syncthreads();
+    const int q = p - ZH;
+    if (q >= zb - ZH && q <= ze - 1 + ZH) stage0_b<IS3D>(R, ox, oy, q);
+    __syncthreads();
+    // stage C: residual and x of the owned cells of plane s
+    const int s = p - 2 * ZH;
+    if (s >= zb && s < ze) {
+      const int sl = ring0(s);
+      const int gx = ox + lx;
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const int row = (threadIdx.x >> 5) + 8 * k;
+        const int gy = oy + row;
+        if (lx < 2 || lx >= 2 + kTX || row < 2 || row >= 2 + kTY || gx >= d.nx || gy >= d.ny) continue;
+        const long long g = ix(d, gx, gy, s);
+        const int c = R.code[sl][row][lx];
+        const float xv = R.x[sl][row][lx];
+        F.xd[g] = xv;
+        if (!(c & kMgActive)) continue;
+        float sum = add_links0<IS3D>(R, c, s, row, lx, scaled_b(c, R.res[sl][row][lx]));
+        sum = sum - R.diag[sl][row][lx] * xv;
+        F.r[g] = sum;
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -587,81 +617,67 @@ __global__ void __launch_bounds__(256, 3) k_mg0_down(Lev0 F, const float* __rest
 // from F.xd, halo included, and writes the result to x0: reading and writing
 // one array would race with the neighbouring CTAs' writes.
 template <bool IS3D, bool DOT>
-__global__ void __launch_bounds__(256, 3) k_mg0_up(Lev0 F, const float* __restrict__ res, float* x0, Lev C, double* part,
+__global__ void __launch_bounds__(256, 4) k_mg0_up(Lev0 F, const float* __restrict__ res, float* x0, Lev C, double* part,
                                                    CgScalars* sc) {
   if (sc->done) return;
-  using T = Tile0<IS3D>;
-  extern __shared__ __align__(16) unsigned char t0_smem[];
-  float* sres = (float*)t0_smem;
-  float* sx = sres + T::NR;
-  uint16_t* scode = (uint16_t*)(sx + T::NR);
-  __shared__ float scx[T::CN];
+  constexpr int CX = kRX / 2 + 1, CY = kRY / 2 + 1;
+  __shared__ Ring0 R;
+  __shared__ float scx[2][CY][CX];  // level-1 parents of the region, two coarse planes
   const Dims& d = F.d;
-  const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2, oz = blockIdx.z * T::tz - T::hz;
-  tile0_load<IS3D>(F, res, scode, sres, F.xd, sx, ox, oy, oz);
-  // coarse parents of the region: level-1 vertices c*0 .. c*0 + C* - 1
-  const int cx0 = ox >> 1, cy0 = oy >> 1, cz0 = oz >> 1;
-  {
-    constexpr int NIT = (T::CN + 255) / 256;
-    float cv[NIT];
-#pragma unroll
-    for (int k = 0; k < NIT; k++) {
-      const int q = threadIdx.x + 256 * k;
-      const int ax = cx0 + q % T::CX, ay = cy0 + (q / T::CX) % T::CY, az = cz0 + q / (T::CX * T::CY);
-      const bool in = q < T::CN && ax >= 0 && ay >= 0 && az >= 0 && ax < C.sx && ay < C.sy && az < C.sz;
-      cv[k] = in ? C.x[lin(C, ax, ay, az)] : 0.f;
-    }
-#pragma unroll
-    for (int k = 0; k < NIT; k++) {
-      const int q = threadIdx.x + 256 * k;
-      if (q < T::CN) scx[q] = cv[k];
-    }
-  }
-  __syncthreads();
-  // x + I * x[1] over the whole region (inactive cells keep x = 0;
-  // inactive coarse vertices hold x = 0)
-#pragma unroll 4
-  for (int k = 0; k < T::PER; k++) {
-    T0_CELL(k, lx, ly, lz, q)
-    if (!(scode[q] & kMgActive)) continue;
-    const int vx = ox + lx, vy = oy + ly, vz = oz + lz;
-    const int hx = vx & 1, hy = vy & 1, hz = vz & 1;  // two parents along odd axes
-    const int b0 = (vx / 2 - cx0) + T::CX * ((vy / 2 - cy0) + T::CY * (vz / 2 - cz0));
-    float sum = 0.f;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const int ax = j & 1, ay = (j >> 1) & 1, az = j >> 2;
-      if (ax <= hx && ay <= hy && az <= hz) sum = sum + scx[b0 + ax + T::CX * (ay + T::CY * az)];
-    }
-    sx[q] = sx[q] + inv_pow2(hx + hy + hz) * sum;
-  }
-  __syncthreads();
-  // colour 1 on the region minus its outer ring
-#pragma unroll 4
-  for (int k = 0; k < T::PER; k++) {
-    T0_CELL(k, lx, ly, lz, q)
-    if (lx < 1 || lx > T::RX - 2 || ly < 1 || ly > T::RY - 2) continue;
-    if (IS3D && (lz < 1 || lz > T::RZ - 2)) continue;
-    const int c = scode[q];
-    if ((((ox + lx) + (oy + ly) + (oz + lz)) & 1) == 0 || !(c & kMgActive)) continue;
-    sx[q] = add_links<IS3D>(c, sx, q, scaled_b(c, sres[q])) / l0_diag(c, F.a0f, ix(d, ox + lx, oy + ly, oz + lz));
-  }
-  __syncthreads();
-  // colour 0 of the owned box (reads colour-1 values only), store, dot
+  constexpr int ZH = IS3D ? 1 : 0;
+  const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2;
+  const int zb = IS3D ? blockIdx.z * kZC : 0, ze = IS3D ? min(zb + kZC, d.nz) : 1;
+  const int pbeg = zb - 2 * ZH, pend = ze - 1 + 2 * ZH;  // pbeg is even
+  const bool hasA0f = F.a0f != nullptr;
+  const int lx = threadIdx.x & 31;
+  // coarse parents of the region: level-1 vertices (cx0 .. cx0 + CX - 1) x
+  // (cy0 .. cy0 + CY - 1) of coarse plane cz, one per thread
+  const int cx0 = ox >> 1, cy0 = oy >> 1;
+  const int cq = threadIdx.x;
+  const int cax = cx0 + cq % CX, cay = cy0 + cq / CX;
+  auto coarse = [&](int cz) -> float {
+    const bool in = cq < CX * CY && cz >= 0 && cz < C.sz && cax >= 0 && cay >= 0 && cax < C.sx && cay < C.sy;
+    return in ? C.x[lin(C, cax, cay, cz)] : 0.f;
+  };
+  if (cq < CX * CY) scx[(pbeg / 2 + 8) & 1][cq / CX][cq % CX] = coarse(pbeg / 2);
+  Plane0 P;
+  load_plane0<true>(F, res, ox, oy, pbeg, P);
   FSum acc;
-#pragma unroll 4
-  for (int k = 0; k < T::PER; k++) {
-    T0_CELL(k, lx, ly, lz, q)
-    if (lx < 2 || lx >= 2 + kTX || ly < 2 || ly >= 2 + kTY || lz < T::hz || lz >= T::hz + T::tz) continue;
-    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-    if (gx >= d.nx || gy >= d.ny || gz >= d.nz) continue;
-    const long long g = ix(d, gx, gy, gz);
-    const int c = scode[q];
-    float v = sx[q];
-    if (((gx + gy + gz) & 1) == 0 && (c & kMgActive))
-      v = add_links<IS3D>(c, sx, q, scaled_b(c, sres[q])) / l0_diag(c, F.a0f, g);
-    x0[g] = v;
-    if (DOT) acc.add(v * sres[q]);  // inactive cells: x = 0
+  __syncthreads();
+  for (int p = pbeg; p <= pend; p++) {
+    // coarse plane p/2 + 1 is first read at fine plane p + 1; its slot held
+    // coarse plane p/2 - 1, last read at fine plane p - 1.  It is loaded
+    // here and stored after stage B.
+    const bool even = ((p + 8) & 1) == 0;
+    const float cnext = even ? coarse(p / 2 + 1) : 0.f;
+    stage0_a<IS3D, true>(R, P, hasA0f, ox, oy, p, cx0, cy0, scx);
+    if (p < pend) load_plane0<true>(F, res, ox, oy, p + 1, P);
+    __syncthreads();
+    const int q = p - ZH;
+    if (q >= zb - ZH && q <= ze - 1 + ZH) stage0_b<IS3D>(R, ox, oy, q);
+    if (even && cq < CX * CY) scx[(p / 2 + 1 + 8) & 1][cq / CX][cq % CX] = cnext;
+    __syncthreads();
+    // stage C: colour 0 of the owned cells of plane s (reads colour-1
+    // values only), store, dot
+    const int s = p - 2 * ZH;
+    if (s >= zb && s < ze) {
+      const int sl = ring0(s);
+      const int gx = ox + lx;
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const int row = (threadIdx.x >> 5) + 8 * k;
+        const int gy = oy + row;
+        if (lx < 2 || lx >= 2 + kTX || row < 2 || row >= 2 + kTY || gx >= d.nx || gy >= d.ny) continue;
+        const long long g = ix(d, gx, gy, s);
+        const int c = R.code[sl][row][lx];
+        float v = R.x[sl][row][lx];
+        if (((gx + gy + s) & 1) == 0 && (c & kMgActive))
+          v = add_links0<IS3D>(R, c, s, row, lx, scaled_b(c, R.res[sl][row][lx])) / R.diag[sl][row][lx];
+        x0[g] = v;
+        if (DOT) acc.add(v * R.res[sl][row][lx]);  // inactive cells: x = 0
+      }
+    }
+    __syncthreads();
   }
   if (!DOT) return;
   const double bsum = block_sum(acc.value());
@@ -680,7 +696,6 @@ __global__ void __launch_bounds__(256, 3) k_mg0_up(Lev0 F, const float* __restri
     }
   }
 }
-#undef T0_CELL
 
 // ---- coarsest level: GridMg::solveCG in double-float arithmetic
 // GB300 executes FP64 at a small fraction of its FP32 rate, and a CG on
@@ -1184,14 +1199,6 @@ int ensure_paths() {
       cudaFuncSetAttribute(k_mg_coarse_cg<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(k_mg_coarse_cg<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
     return 1;
-  const int t3 = (int)Tile0<true>::smem, t2 = (int)Tile0<false>::smem;
-  if (cudaFuncSetAttribute(k_mg0_down<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t3) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_down<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t2) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_up<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t3) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_up<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t3) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_up<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t2) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_up<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t2) != cudaSuccess)
-    return 1;
   // the cluster V-cycle tail: 16 CTAs where the GPU can co-schedule them
   g_tailCta = 0;
   if (cudaFuncSetAttribute(k_mg_tail<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
@@ -1526,7 +1533,7 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   float* x0 = b.tmp;
   const float* res = b.residual;
   const Lev none{};
-  const dim3 gt((d.nx + kTX - 1) / kTX, (d.ny + kTY - 1) / kTY, d.is3d ? (d.nz + kTZ - 1) / kTZ : 1);
+  const dim3 gt((d.nx + kTX - 1) / kTX, (d.ny + kTY - 1) / kTY, d.is3d ? (d.nz + kZC - 1) / kZC : 1);
   static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
   const int ncol = h->is3d ? 8 : 4;
   auto smooth = [&](int l, bool reversed) {
@@ -1551,8 +1558,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
     {
       Fam f(h, "mg_down_l0");
       count_launch();
-      if (h->is3d) k_mg0_down<true><<<gt, kThreads1, Tile0<true>::smem, s>>>(l0, res, sc);
-      else k_mg0_down<false><<<gt, kThreads1, Tile0<false>::smem, s>>>(l0, res, sc);
+      if (h->is3d) k_mg0_down<true><<<gt, kThreads1, 0, s>>>(l0, res, sc);
+      else k_mg0_down<false><<<gt, kThreads1, 0, s>>>(l0, res, sc);
     }
     {
       Fam f(h, "mg_restrict_l0");
@@ -1607,11 +1614,11 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       Fam f(h, "mg_up_l0");
       count_launch();
       if (h->is3d) {
-        if (init) k_mg0_up<true, false><<<gt, kThreads1, Tile0<true>::smem, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
-        else k_mg0_up<true, true><<<gt, kThreads1, Tile0<true>::smem, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+        if (init) k_mg0_up<true, false><<<gt, kThreads1, 0, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+        else k_mg0_up<true, true><<<gt, kThreads1, 0, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
       } else {
-        if (init) k_mg0_up<false, false><<<gt, kThreads1, Tile0<false>::smem, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
-        else k_mg0_up<false, true><<<gt, kThreads1, Tile0<false>::smem, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+        if (init) k_mg0_up<false, false><<<gt, kThreads1, 0, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+        else k_mg0_up<false, true><<<gt, kThreads1, 0, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
       }
     }
   }
