@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev S, const CgSca
 // passes, in the same order; halo cells are recomputed by each CTA that
 // needs them.  The next plane's loads are issued before the current
 // plane's passes.
-constexpr int kTX = 28, kTY = 12, kZC = 32;
+constexpr int kTX = 28, kTY = 12, kZC = 32;  // kZC: default planes per CTA (even)
 constexpr int kRX = 32, kRY = 16;
 
 struct Ring0 {  // four planes of the region
@@ -568,13 +568,13 @@ __device__ __forceinline__ void stage0_b(Ring0& R, int ox, int oy, int q) {
 // residual (knSmoothColor x2 + knCalcResidual); writes x (to F.xd) and r of
 // the owned cells
 template <bool IS3D>
-__global__ void __launch_bounds__(256, 4) k_mg0_down(Lev0 F, const float* __restrict__ res, const CgScalars* sc) {
+__global__ void __launch_bounds__(256, 4) k_mg0_down(Lev0 F, const float* __restrict__ res, int zc, const CgScalars* sc) {
   if (sc->done) return;
   __shared__ Ring0 R;
   const Dims& d = F.d;
   constexpr int ZH = IS3D ? 1 : 0;
   const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2;
-  const int zb = IS3D ? blockIdx.z * kZC : 0, ze = IS3D ? min(zb + kZC, d.nz) : 1;
+  const int zb = IS3D ? blockIdx.z * zc : 0, ze = IS3D ? min(zb + zc, d.nz) : 1;
   const int pbeg = zb - 2 * ZH, pend = ze - 1 + 2 * ZH;
   const bool hasA0f = F.a0f != nullptr;
   const int lx = threadIdx.x & 31;
@@ -617,8 +617,8 @@ __global__ void __launch_bounds__(256, 4) k_mg0_down(Lev0 F, const float* __rest
 // from F.xd, halo included, and writes the result to x0: reading and writing
 // one array would race with the neighbouring CTAs' writes.
 template <bool IS3D, bool DOT>
-__global__ void __launch_bounds__(256, 4) k_mg0_up(Lev0 F, const float* __restrict__ res, float* x0, Lev C, double* part,
-                                                   CgScalars* sc) {
+__global__ void __launch_bounds__(256, 4) k_mg0_up(Lev0 F, const float* __restrict__ res, int zc, float* x0, Lev C,
+                                                   double* part, CgScalars* sc) {
   if (sc->done) return;
   constexpr int CX = kRX / 2 + 1, CY = kRY / 2 + 1;
   __shared__ Ring0 R;
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(256, 4) k_mg0_up(Lev0 F, const float* __restri
   const Dims& d = F.d;
   constexpr int ZH = IS3D ? 1 : 0;
   const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2;
-  const int zb = IS3D ? blockIdx.z * kZC : 0, ze = IS3D ? min(zb + kZC, d.nz) : 1;
+  const int zb = IS3D ? blockIdx.z * zc : 0, ze = IS3D ? min(zb + zc, d.nz) : 1;
   const int pbeg = zb - 2 * ZH, pend = ze - 1 + 2 * ZH;  // pbeg is even
   const bool hasA0f = F.a0f != nullptr;
   const int lx = threadIdx.x & 31;
@@ -1333,6 +1333,7 @@ struct MgHierarchy {
   float coarseAcc = 1e-8f;
   Lev* dlev = nullptr;  // lev[] on the device, for the cluster tail
   int tailFirst = 0;    // first level of the cluster tail (0: none)
+  int zc = kZC;         // planes per CTA of the level-0 passes
   size_t bytes = 0;
   std::vector<void*> allocs;
   bool ok = true;
@@ -1399,6 +1400,7 @@ MgHierarchy* mg_hierarchy_create(const Dims& d) {
   }
   const long long nc = L > 1 ? h->lev[L - 1].n : n0;
   if (nc > kCgThreads) h->ok = false;  // the level loop guarantees <= 1000
+  if (const char* e = std::getenv("MANTAGPU_MG0_PLANES")) h->zc = std::max(2, std::atoi(e) & ~1);
   // the levels of at most kTailSlots storage slots (and the coarsest) run in
   // one cluster launch
   if (h->ok && L > 1 && g_tailCta && nc <= (long long)g_tailCta * kTailVpc) {
@@ -1533,7 +1535,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   float* x0 = b.tmp;
   const float* res = b.residual;
   const Lev none{};
-  const dim3 gt((d.nx + kTX - 1) / kTX, (d.ny + kTY - 1) / kTY, d.is3d ? (d.nz + kZC - 1) / kZC : 1);
+  const int zc = h->zc;
+  const dim3 gt((d.nx + kTX - 1) / kTX, (d.ny + kTY - 1) / kTY, d.is3d ? (d.nz + zc - 1) / zc : 1);
   static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
   const int ncol = h->is3d ? 8 : 4;
   auto smooth = [&](int l, bool reversed) {
@@ -1558,8 +1561,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
     {
       Fam f(h, "mg_down_l0");
       count_launch();
-      if (h->is3d) k_mg0_down<true><<<gt, kThreads1, 0, s>>>(l0, res, sc);
-      else k_mg0_down<false><<<gt, kThreads1, 0, s>>>(l0, res, sc);
+      if (h->is3d) k_mg0_down<true><<<gt, kThreads1, 0, s>>>(l0, res, zc, sc);
+      else k_mg0_down<false><<<gt, kThreads1, 0, s>>>(l0, res, zc, sc);
     }
     {
       Fam f(h, "mg_restrict_l0");
@@ -1614,11 +1617,11 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       Fam f(h, "mg_up_l0");
       count_launch();
       if (h->is3d) {
-        if (init) k_mg0_up<true, false><<<gt, kThreads1, 0, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
-        else k_mg0_up<true, true><<<gt, kThreads1, 0, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+        if (init) k_mg0_up<true, false><<<gt, kThreads1, 0, s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
+        else k_mg0_up<true, true><<<gt, kThreads1, 0, s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
       } else {
-        if (init) k_mg0_up<false, false><<<gt, kThreads1, 0, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
-        else k_mg0_up<false, true><<<gt, kThreads1, 0, s>>>(l0, res, x0, h->lev[1], b.part, b.sc);
+        if (init) k_mg0_up<false, false><<<gt, kThreads1, 0, s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
+        else k_mg0_up<false, true><<<gt, kThreads1, 0, s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
       }
     }
   }
