@@ -202,6 +202,19 @@ int mg_release_mg(mg_solver s);
  * (conjugategrad.cpp:100-106, 162-167).  A diagnostic entry for checking
  * the preconditioner on its own; solvePressure does not need it. */
 int mg_multigrid_vcycle(mg_grid flags, mg_grid phi, mg_grid src, mg_grid dst, float gfClamp, float coarseAccuracy);
+/* How the multigrid hierarchy for flags is laid out and run: level sizes
+ * (GridMg ctor, multigrid.cpp:240-265), the first level of the coarse end
+ * that runs as one cluster launch, and per level the number of distinct
+ * stencils when the level reads a stencil dictionary (0: stencil planes).
+ * Builds a fresh hierarchy like mg_multigrid_vcycle; diagnostic only. */
+typedef struct mg_multigrid_layout {
+  int levels;
+  int tailFirst;
+  int tailCtas;
+  int size[32][3];
+  int dictStencils[32];
+} mg_multigrid_layout;
+int mg_multigrid_describe(mg_grid flags, mg_multigrid_layout* out);
 
 /* ---- scene setup (source/grid.cpp, source/shapes.cpp) -------------------- */
 /* FlagGrid::initDomain (grid.cpp:732-822); phiWalls must be NULL */

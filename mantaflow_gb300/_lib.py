@@ -47,6 +47,11 @@ class RefineResult(C.Structure):
     _fields_ = [("refinements", C.c_int), ("iterations", C.c_int), ("resNorm", C.c_double)]
 
 
+class MultigridLayout(C.Structure):
+    _fields_ = [("levels", C.c_int), ("tailFirst", C.c_int), ("tailCtas", C.c_int),
+                ("size", (C.c_int * 3) * 32), ("dictStencils", C.c_int * 32)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _P = C.c_void_p
 _I = C.c_int
@@ -117,6 +122,7 @@ SIGNATURES = [
     ("mg_correct_velocity", _I, [_P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P]),
     ("mg_release_mg", _I, [_P]),
     ("mg_multigrid_vcycle", _I, [_P, _P, _P, _P, _F, _F]),
+    ("mg_multigrid_describe", _I, [_P, _P]),
     ("mg_flags_init_domain", _I, [_P, _I, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, _P]),
     ("mg_flags_fill_grid", _I, [_P, _I]),
     ("mg_flags_update_from_levelset", _I, [_P, _P]),

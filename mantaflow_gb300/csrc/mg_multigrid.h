@@ -17,6 +17,15 @@ void mg_hierarchy_destroy(MgHierarchy* h);
 void mg_hierarchy_reset(MgHierarchy* h);
 size_t mg_hierarchy_bytes(const MgHierarchy* h);
 int mg_hierarchy_levels(const MgHierarchy* h);
+// level sizes and how each level is run (after mg_setup)
+struct MgLayout {
+  int levels;
+  int tailFirst;  // first level of the single-launch cluster tail (0: none)
+  int tailCtas;   // CTAs of that cluster
+  int size[32][3];
+  int dictStencils[32];  // distinct stencils of a dictionary level (0: planes)
+};
+void mg_hierarchy_describe(const MgHierarchy* h, MgLayout* out);
 // changes whenever the kernel parameters of mg_apply change (rebuild,
 // coarsest-level accuracy, ghost-fluid diagonal): a captured graph of
 // mg_apply stays valid while the signature and the PcgBuffers are the same

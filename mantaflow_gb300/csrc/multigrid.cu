@@ -72,6 +72,10 @@ struct Lev {
   float* x;
   float* b;
   float* r;
+  // stencil dictionary (null: none): the full 27 (2D: 9) coefficients of
+  // vertex v, in applyAStencil's order, are T[sid[v] * kDictStride + s]
+  const uint16_t* sid;
+  const float* T;
 };
 
 // level 0: snapshot of the Poisson matrix taken by setA
@@ -324,6 +328,159 @@ __device__ __forceinline__ float stencil_sub_flat(const Lev& L, int vx, int vy, 
   return sum;
 }
 
+// ---- stencil dictionary.  A coarse level's Galerkin stencils repeat:
+// away from walls, obstacles and free surfaces every vertex of a level has
+// the same 27 coefficients.  The dictionary holds each distinct tuple once;
+// a vertex keeps a 16-bit id, so a colour pass reads 2 bytes of matrix per
+// vertex instead of 108.  The tuples are compared bit for bit when the
+// dictionary is built (a level with a hash collision or more than
+// kDictCap distinct stencils keeps reading its planes), so smoothing and
+// residual do exactly the same float operations on the same values.
+constexpr int kDictCap = 65535;  // ids 1..kDictCap; id 0: inactive vertices
+constexpr int kDictStride = 28;
+constexpr int kDictTableBits = 17;
+constexpr int kDictTable = 1 << kDictTableBits;
+constexpr int kDictProbes = 256;
+
+// the coefficient tuple of slot v (zero outside the level)
+template <bool IS3D>
+__device__ __forceinline__ void dict_tuple(const Lev& L, long long v, float* a) {
+  constexpr int NZ = IS3D ? 3 : 1, ZL = IS3D ? -1 : 0;
+  constexpr int S = IS3D ? 14 : 5;
+  int vx, vy, vz;
+  coords(L, v, vx, vy, vz);
+#pragma unroll
+  for (int s = 0; s < NZ * 9; s++) {
+    const int nx = vx + s % 3 - 1, ny = vy + (s / 3) % 3 - 1, nz = vz + s / 9 + ZL;
+    const bool in = inside(L, nx, ny, nz);
+    const long long nn = in ? lin(L, nx, ny, nz) : v;
+    const float c = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
+    a[s] = in ? c : 0.f;
+  }
+}
+template <int NS>
+__device__ __forceinline__ unsigned long long dict_hash(const float* a) {
+  unsigned long long h = 0x9E3779B97F4A7C15ull;
+#pragma unroll
+  for (int s = 0; s < NS; s++) {
+    h ^= (unsigned long long)__float_as_uint(a[s]) + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    h *= 0xBF58476D1CE4E5B9ull;
+  }
+  return (h ^ (h >> 31)) | 1ull;  // 0 marks an empty table slot
+}
+// the table slot of hash hv (inserting it when ins); -1 after kDictProbes
+__device__ __forceinline__ int dict_slot(unsigned long long* keys, unsigned long long hv, bool ins) {
+  int slot = (int)(hv & (kDictTable - 1));
+  for (int k = 0; k < kDictProbes; k++) {
+    const unsigned long long cur = ins ? atomicCAS(&keys[slot], 0ull, hv) : keys[slot];
+    if (cur == hv || (ins && cur == 0ull)) return slot;
+    if (!ins && cur == 0ull) return -1;
+    slot = (slot + 1) & (kDictTable - 1);
+  }
+  return -1;
+}
+// flags: [0] table overflow, [1] tuple mismatch, [2] distinct tuples
+template <bool IS3D>
+__global__ void __launch_bounds__(256) k_dict_insert(Lev L, unsigned long long* keys, int* rep, int* flags) {
+  constexpr int NS = IS3D ? 27 : 9;
+  GRID_STRIDE(v, L.n) {
+    if (L.type[v] == kVtInactive) continue;
+    float a[NS];
+    dict_tuple<IS3D>(L, v, a);
+    const int slot = dict_slot(keys, dict_hash<NS>(a), true);
+    if (slot < 0) flags[0] = 1;
+    else atomicMin(&rep[slot], (int)v);  // the lowest slot index represents the tuple
+  }
+}
+// ids in table order: one CTA of 1024 threads, 128 table slots per thread
+__global__ void __launch_bounds__(1024) k_dict_ids(const unsigned long long* keys, int* slotId, int* flags) {
+  constexpr int PER = kDictTable / 1024;
+  __shared__ int scan[1024];
+  const int t = threadIdx.x;
+  int cnt = 0;
+  for (int k = 0; k < PER; k++) cnt += keys[t * PER + k] != 0ull;
+  scan[t] = cnt;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
+    const int add = t >= o ? scan[t - o] : 0;
+    __syncthreads();
+    scan[t] += add;
+    __syncthreads();
+  }
+  int id = scan[t] - cnt + 1;
+  for (int k = 0; k < PER; k++) {
+    const int q = t * PER + k;
+    slotId[q] = keys[q] != 0ull ? id++ : 0;
+  }
+  if (t == 1023) flags[2] = scan[1023];
+}
+template <bool IS3D>
+__global__ void __launch_bounds__(256) k_dict_fill(Lev L, unsigned long long* keys, const int* rep, const int* slotId,
+                                                   uint16_t* sid, float* T, int* flags) {
+  constexpr int NS = IS3D ? 27 : 9;
+  GRID_STRIDE(v, L.n) {
+    if (L.type[v] == kVtInactive) {
+      sid[v] = 0;
+      continue;
+    }
+    float a[NS];
+    dict_tuple<IS3D>(L, v, a);
+    const int slot = dict_slot(keys, dict_hash<NS>(a), false);
+    const int id = slot < 0 ? 0 : slotId[slot];
+    if (slot < 0 || id > kDictCap) {
+      flags[0] = 1;
+      sid[v] = 0;
+      continue;
+    }
+    sid[v] = (uint16_t)id;
+    if (rep[slot] == (int)v)
+#pragma unroll
+      for (int s = 0; s < NS; s++) T[(long long)id * kDictStride + s] = a[s];
+  }
+}
+template <bool IS3D>
+__global__ void __launch_bounds__(256) k_dict_verify(Lev L, const uint16_t* sid, const float* T, int* flags) {
+  constexpr int NS = IS3D ? 27 : 9;
+  GRID_STRIDE(v, L.n) {
+    if (L.type[v] == kVtInactive) continue;
+    float a[NS];
+    dict_tuple<IS3D>(L, v, a);
+    const float* t = T + (long long)sid[v] * kDictStride;
+    bool same = sid[v] != 0;
+#pragma unroll
+    for (int s = 0; s < NS; s++) same = same && __float_as_uint(a[s]) == __float_as_uint(t[s]);
+    if (!same) flags[1] = 1;
+  }
+}
+
+// stencil_sub with the coefficients from the dictionary tuple t
+template <bool IS3D, bool SKIP_CENTER>
+__device__ __forceinline__ float stencil_sub_dict(const Lev& L, const float* __restrict__ t, int vx, int vy, int vz,
+                                                  float sum) {
+  constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
+  constexpr int S = IS3D ? 14 : 5;
+#pragma unroll
+  for (int dz = ZL; dz <= ZH; dz++) {
+    float a[9], xv[9];
+    bool in[9];
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+      for (int dx = -1; dx <= 1; dx++) {
+        const int q = (dy + 1) * 3 + (dx + 1);
+        const int s = (dz - ZL) * 9 + q;
+        const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
+        in[q] = inside(L, nx, ny, nz) && !(SKIP_CENTER && s == S - 1);
+        a[q] = t[s];
+        xv[q] = in[q] ? L.x[lin(L, nx, ny, nz)] : 0.f;
+      }
+#pragma unroll
+    for (int q = 0; q < 9; q++)
+      if (in[q]) sum = sum - a[q] * xv[q];
+  }
+  return sum;
+}
+
 // knSmoothColor on a coarse level, one vertex: block bi of colour offset
 // (ox, oy, oz) in 2x2x2 blocks, bx x by blocks per z-plane
 template <bool IS3D, bool CG>
@@ -434,6 +591,36 @@ template <bool IS3D>
 __global__ void __launch_bounds__(256, 3) k_mg_residual(Lev L, int S, const CgScalars* sc) {
   if (sc->done) return;
   GRID_STRIDE(v, L.n) residual_vertex<IS3D, false>(L, v);
+}
+
+// the same passes on a level with a stencil dictionary
+template <bool IS3D>
+__global__ void __launch_bounds__(256, 4) k_mg_smooth_dict(Lev L, int ox, int oy, int oz, const CgScalars* sc) {
+  if (sc->done) return;
+  const int bx = (L.sx + 1) / 2, by = (L.sy + 1) / 2, bz = (L.sz + 1) / 2;
+  const long long nb = (long long)bx * by * bz;
+  constexpr int S = IS3D ? 14 : 5;
+  GRID_STRIDE(bi, nb) {
+    const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
+    if (!inside(L, vx, vy, vz)) continue;
+    const long long v = (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi;
+    if (L.type[v] == kVtInactive) continue;
+    const float* t = L.T + (int)L.sid[v] * kDictStride;
+    const float sum = stencil_sub_dict<IS3D, true>(L, t, vx, vy, vz, L.b[v]);
+    L.x[v] = sum / t[S - 1];
+  }
+}
+
+template <bool IS3D>
+__global__ void __launch_bounds__(256, 4) k_mg_residual_dict(Lev L, const CgScalars* sc) {
+  if (sc->done) return;
+  GRID_STRIDE(v, L.n) {
+    if (L.type[v] == kVtInactive) continue;
+    int vx, vy, vz;
+    coords(L, v, vx, vy, vz);
+    const float* t = L.T + (int)L.sid[v] * kDictStride;
+    L.r[v] = stencil_sub_dict<IS3D, false>(L, t, vx, vy, vz, L.b[v]);
+  }
 }
 
 template <bool FROM0>
@@ -1334,6 +1521,14 @@ struct MgHierarchy {
   Lev* dlev = nullptr;  // lev[] on the device, for the cluster tail
   int tailFirst = 0;    // first level of the cluster tail (0: none)
   int zc = kZC;         // planes per CTA of the level-0 passes
+  // stencil dictionaries of the levels run by per-level launches
+  uint16_t* dsid[kMaxLevels] = {};
+  float* dT[kMaxLevels] = {};
+  unsigned long long* dkeys = nullptr;
+  int* drep = nullptr;
+  int* dslot = nullptr;
+  int* dflags = nullptr;  // 3 ints per level
+  int ndict[kMaxLevels] = {};  // distinct stencils of the level (0: planes)
   size_t bytes = 0;
   std::vector<void*> allocs;
   bool ok = true;
@@ -1412,6 +1607,21 @@ MgHierarchy* mg_hierarchy_create(const Dims& d) {
     h->dlev = h->alloc<Lev>(L);
     if (h->ok && cudaMemcpy(h->dlev, h->lev, sizeof(Lev) * (size_t)L, cudaMemcpyHostToDevice) != cudaSuccess) h->ok = false;
   }
+  // dictionary buffers for the colour-blocked levels outside the tail
+  if (h->ok && !std::getenv("MANTAGPU_MG_NO_DICT")) {
+    bool any = false;
+    for (int l = 1; l < L - 1 && (!h->tailFirst || l < h->tailFirst); l++) {
+      h->dsid[l] = h->alloc<uint16_t>(h->lev[l].n);
+      h->dT[l] = h->alloc<float>((long long)(kDictCap + 1) * kDictStride);
+      any = true;
+    }
+    if (any) {
+      h->dkeys = h->alloc<unsigned long long>(kDictTable);
+      h->drep = h->alloc<int>(kDictTable);
+      h->dslot = h->alloc<int>(kDictTable);
+      h->dflags = h->alloc<int>(3 * kMaxLevels);
+    }
+  }
   if (!h->ok) {
     mg_hierarchy_destroy(h);
     return nullptr;
@@ -1437,6 +1647,17 @@ unsigned long long mg_hierarchy_signature(const MgHierarchy* h) {
   return (h->gen << 34) ^ ((unsigned long long)h->useA0f << 33) ^ (unsigned long long)acc;
 }
 int mg_hierarchy_levels(const MgHierarchy* h) { return h ? h->nlev : 0; }
+void mg_hierarchy_describe(const MgHierarchy* h, MgLayout* out) {
+  *out = MgLayout{};
+  if (!h) return;
+  out->levels = h->nlev;
+  out->tailFirst = h->tailFirst;
+  out->tailCtas = h->tailFirst ? g_tailCta : 0;
+  for (int l = 0; l < h->nlev && l < 32; l++) {
+    for (int c = 0; c < 3; c++) out->size[l][c] = h->size[l][c];
+    out->dictStencils[l] = h->ndict[l];
+  }
+}
 
 int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStream_t s) {
   h->coarseAcc = coarseAccuracy;
@@ -1502,6 +1723,49 @@ int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStre
       }
       if (cudaGetLastError() != cudaSuccess) return 1;
     }
+    // stencil dictionaries (a level keeps its planes unless every tuple was
+    // found and verified bit for bit)
+    bool anyDict = false;
+    for (int l = 1; l < h->nlev; l++) {
+      h->lev[l].sid = nullptr;
+      h->lev[l].T = nullptr;
+      h->ndict[l] = 0;
+      if (!h->dsid[l]) continue;
+      anyDict = true;
+      const Lev& v = h->lev[l];
+      int* fl = h->dflags + 3 * l;
+      if (cudaMemsetAsync(h->dkeys, 0, sizeof(unsigned long long) * kDictTable, s) != cudaSuccess ||
+          cudaMemsetAsync(h->drep, 0x7f, sizeof(int) * kDictTable, s) != cudaSuccess ||
+          cudaMemsetAsync(fl, 0, sizeof(int) * 3, s) != cudaSuccess ||
+          cudaMemsetAsync(h->dT[l], 0, sizeof(float) * kDictStride, s) != cudaSuccess)
+        return 1;
+      count_launch();
+      if (h->is3d) k_dict_insert<true><<<blocks_for(v.n), kThreads1, 0, s>>>(v, h->dkeys, h->drep, fl);
+      else k_dict_insert<false><<<blocks_for(v.n), kThreads1, 0, s>>>(v, h->dkeys, h->drep, fl);
+      count_launch();
+      k_dict_ids<<<1, 1024, 0, s>>>(h->dkeys, h->dslot, fl);
+      count_launch();
+      if (h->is3d) k_dict_fill<true><<<blocks_for(v.n), kThreads1, 0, s>>>(v, h->dkeys, h->drep, h->dslot, h->dsid[l], h->dT[l], fl);
+      else k_dict_fill<false><<<blocks_for(v.n), kThreads1, 0, s>>>(v, h->dkeys, h->drep, h->dslot, h->dsid[l], h->dT[l], fl);
+      count_launch();
+      if (h->is3d) k_dict_verify<true><<<blocks_for(v.n), kThreads1, 0, s>>>(v, h->dsid[l], h->dT[l], fl);
+      else k_dict_verify<false><<<blocks_for(v.n), kThreads1, 0, s>>>(v, h->dsid[l], h->dT[l], fl);
+      if (cudaGetLastError() != cudaSuccess) return 1;
+    }
+    if (anyDict) {
+      int hf[3 * kMaxLevels];
+      if (cudaMemcpyAsync(hf, h->dflags, sizeof hf, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess)
+        return 1;
+      for (int l = 1; l < h->nlev; l++) {
+        if (!h->dsid[l]) continue;
+        const int* f = hf + 3 * l;
+        if (f[0] || f[1] || f[2] > kDictCap) continue;
+        h->lev[l].sid = h->dsid[l];
+        h->lev[l].T = h->dT[l];
+        h->ndict[l] = f[2];
+      }
+    }
   }
   h->isASet = true;
   return 0;
@@ -1546,8 +1810,13 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
     for (int q = 0; q < ncol; q++) {
       const int c = reversed ? ncol - 1 - q : q;
       count_launch();
-      if (h->is3d) k_mg_smooth<true><<<nb, kThreads1, 0, s>>>(v, S, off[c][0], off[c][1], off[c][2], sc);
-      else k_mg_smooth<false><<<nb, kThreads1, 0, s>>>(v, S, off[c][0], off[c][1], off[c][2], sc);
+      if (v.sid) {
+        if (h->is3d) k_mg_smooth_dict<true><<<nb, kThreads1, 0, s>>>(v, off[c][0], off[c][1], off[c][2], sc);
+        else k_mg_smooth_dict<false><<<nb, kThreads1, 0, s>>>(v, off[c][0], off[c][1], off[c][2], sc);
+      } else {
+        if (h->is3d) k_mg_smooth<true><<<nb, kThreads1, 0, s>>>(v, S, off[c][0], off[c][1], off[c][2], sc);
+        else k_mg_smooth<false><<<nb, kThreads1, 0, s>>>(v, S, off[c][0], off[c][1], off[c][2], sc);
+      }
     }
   };
   if (L == 0) {
@@ -1575,8 +1844,14 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       smooth(l, false);
       Fam f(h, "mg_transfer_coarse");
       count_launch();
-      if (h->is3d) k_mg_residual<true><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], S, sc);
-      else k_mg_residual<false><<<blocks_for(h->lev[l].n), kThreads1, 0, s>>>(h->lev[l], S, sc);
+      const Lev& v = h->lev[l];
+      if (v.sid) {
+        if (h->is3d) k_mg_residual_dict<true><<<blocks_for(v.n), kThreads1, 0, s>>>(v, sc);
+        else k_mg_residual_dict<false><<<blocks_for(v.n), kThreads1, 0, s>>>(v, sc);
+      } else {
+        if (h->is3d) k_mg_residual<true><<<blocks_for(v.n), kThreads1, 0, s>>>(v, S, sc);
+        else k_mg_residual<false><<<blocks_for(v.n), kThreads1, 0, s>>>(v, S, sc);
+      }
       count_launch();
       k_mg_restrict<false><<<blocks_for(h->lev[l + 1].n), kThreads1, 0, s>>>(h->lev[l + 1], h->lev[l], l0, sc);
     }

@@ -1429,6 +1429,33 @@ extern "C" int mg_multigrid_vcycle(mg_grid flags, mg_grid phi, mg_grid src, mg_g
   return MG_OK;
 }
 
+extern "C" int mg_multigrid_describe(mg_grid flags, mg_multigrid_layout* out) {
+  NEED_GRID(flags, "mg_multigrid_describe");
+  if (!out) return fail(MG_ERR_ARG, "mg_multigrid_describe: out is NULL");
+  mg_solver s = flags->s;
+  int st = ensure_cg_state(s);
+  if (st) return st;
+  PcgBuffers b = cg_buffers(s, flags, nullptr, nullptr);
+  launch_make_codes(b, s->stream);
+  CKL();
+  mgpu::MgHierarchy* h = mg_hierarchy_create(s->d);
+  if (!h) return fail(MG_ERR_NOMEM, "mg_multigrid_describe: multigrid allocation failed");
+  const int e = mg_setup(h, b, 1e-8f, s->stream);
+  cudaStreamSynchronize(s->stream);
+  mgpu::MgLayout L;
+  mgpu::mg_hierarchy_describe(h, &L);
+  mg_hierarchy_destroy(h);
+  if (e) return fail(MG_ERR_CUDA, "mg_multigrid_describe: multigrid setup failed");
+  out->levels = L.levels;
+  out->tailFirst = L.tailFirst;
+  out->tailCtas = L.tailCtas;
+  for (int l = 0; l < 32; l++) {
+    for (int c = 0; c < 3; c++) out->size[l][c] = L.size[l][c];
+    out->dictStencils[l] = L.dictStencils[l];
+  }
+  return MG_OK;
+}
+
 extern "C" int mg_release_mg(mg_solver s) {
   if (!s) {
     for (auto x : g_ctx.solvers)

@@ -366,6 +366,42 @@ def test_multigrid_vcycle_against_oracle(shape, liquid, tail, monkeypatch):
     assert np.mean(got == want) >= 0.999, np.mean(got == want)
 
 
+@pytest.mark.parametrize("shape,liquid", [((40, 36, 30), False), ((37, 29, 41), True), ((90, 70, 1), False)])
+def test_multigrid_dictionary_bitwise(shape, liquid, monkeypatch):
+    """Levels run by per-level launches read their Galerkin stencils from a
+    dictionary of distinct coefficient tuples (verified bit for bit when it
+    is built).  With every level but the coarsest outside the cluster tail,
+    a V-cycle must give the same bits with the dictionary and with the
+    stencil planes, and the dictionary levels must hold few stencils."""
+    import ctypes as C
+    from mantaflow_gb300 import _lib as mlib
+    lib = mlib.load()
+    f, _ = _obstacle_scene(shape, 31, liquid=liquid)
+    nx, ny, nz = shape
+    rng = np.random.default_rng(9)
+    src = (rng.random(f.shape, dtype=np.float32) - 0.5).astype(np.float32)
+    src[(f & og.FLUID) == 0] = 0
+    monkeypatch.setenv("MANTAGPU_MG_TAIL_SLOTS", "0")
+    out = []
+    for nodict in (False, True):
+        if nodict:
+            monkeypatch.setenv("MANTAGPU_MG_NO_DICT", "1")
+        s = m.Solver(name="dict", gridSize=m.vec3(nx, ny, nz), dim=3 if nz > 1 else 2)
+        flags = grid_from(s, m.FlagGrid, f)
+        sg = grid_from(s, m.RealGrid, src)
+        dg = s.create(m.RealGrid)
+        lay = mlib.MultigridLayout()
+        mlib.check(lib.mg_multigrid_describe(flags._h, C.byref(lay)))
+        mlib.check(lib.mg_multigrid_vcycle(flags._h, None, sg._h, dg._h, C.c_float(1e-4), C.c_float(1e-7)))
+        out.append(dg.numpy().copy())
+        dicts = [lay.dictStencils[l] for l in range(1, lay.levels - 1)]
+        if nodict:
+            assert all(d == 0 for d in dicts), dicts
+        else:
+            assert lay.levels >= 3 and all(0 < d < 2000 for d in dicts), dicts
+    assert np.array_equal(out[0], out[1])
+
+
 def test_pcnone_rejected_like_reference():
     g = load("pressure_3d")
     s = make_solver(g["flags_smoke"].shape)
