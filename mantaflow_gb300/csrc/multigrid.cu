@@ -146,6 +146,31 @@ __device__ __forceinline__ void coords(const Lev& L, long long v, int& x, int& y
   z = (int)(v / L.pz);
 }
 
+// The 27 neighbours of a vertex of a colour-blocked level: slot offsets and
+// in-level flags separate per axis.  A step d along x moves to colour bit
+// (x+d)&1 and block column (x+d)>>1 (likewise y, z), so the neighbour's
+// slot is v + ox[dx+1] + oy[dy+1] + oz[dz+1]: nine offsets and nine flags
+// per vertex instead of an index computation per neighbour.
+struct Nb3 {
+  int ox[3], oy[3], oz[3];
+  bool ix[3], iy[3], iz[3];
+};
+__device__ __forceinline__ Nb3 nb3(const Lev& L, int vx, int vy, int vz) {
+  Nb3 r;
+  const int cx = vx & 1, cy = vy & 1, cz = vz & 1;
+  const int nb = (int)L.nb, bx = L.bx, bxy = L.bx * L.by;
+#pragma unroll
+  for (int d = -1; d <= 1; d++) {
+    r.ox[d + 1] = (((cx + d) & 1) - cx) * nb + ((cx + d) >> 1);
+    r.oy[d + 1] = 2 * (((cy + d) & 1) - cy) * nb + bx * ((cy + d) >> 1);
+    r.oz[d + 1] = 4 * (((cz + d) & 1) - cz) * nb + bxy * ((cz + d) >> 1);
+    r.ix[d + 1] = (unsigned)(vx + d) < (unsigned)L.sx;
+    r.iy[d + 1] = (unsigned)(vy + d) < (unsigned)L.sy;
+    r.iz[d + 1] = (unsigned)(vz + d) < (unsigned)L.sz;
+  }
+  return r;
+}
+
 #define GRID_STRIDE(v, n) \
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < (n); v += (long long)gridDim.x * blockDim.x)
 
@@ -277,6 +302,8 @@ template <bool IS3D, bool SKIP_CENTER, bool CG = false>
 __device__ __forceinline__ float stencil_sub(const Lev& L, int vx, int vy, int vz, long long v, float sum) {
   constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
   constexpr int S = IS3D ? 14 : 5;
+  const Nb3 o = nb3(L, vx, vy, vz);  // L is colour-blocked
+  const int vi = (int)v;
 #pragma unroll
   for (int dz = ZL; dz <= ZH; dz++) {
     float a[9], xv[9];
@@ -287,10 +314,9 @@ __device__ __forceinline__ float stencil_sub(const Lev& L, int vx, int vy, int v
       for (int dx = -1; dx <= 1; dx++) {
         const int q = (dy + 1) * 3 + (dx + 1);
         const int s = (dz - ZL) * 9 + q;
-        const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
-        in[q] = inside(L, nx, ny, nz) && !(SKIP_CENTER && s == S - 1);
-        const long long nn = in[q] ? lin(L, nx, ny, nz) : v;
-        a[q] = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
+        in[q] = o.ix[dx + 1] && o.iy[dy + 1] && o.iz[dz + 1] && !(SKIP_CENTER && s == S - 1);
+        const int nn = in[q] ? vi + o.ox[dx + 1] + o.oy[dy + 1] + o.oz[dz + 1] : vi;
+        a[q] = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + vi];
         xv[q] = ldv<CG>(&L.x[nn]);
       }
 #pragma unroll
@@ -310,15 +336,15 @@ __device__ __forceinline__ float stencil_sub_flat(const Lev& L, int vx, int vy, 
   constexpr int NZ = IS3D ? 3 : 1, ZL = IS3D ? -1 : 0;
   constexpr int S = IS3D ? 14 : 5;
   const int n = (int)L.n;
+  const Nb3 o = nb3(L, vx, vy, vz);  // L is colour-blocked
   float a[NZ * 9], xv[NZ * 9];
   unsigned inm = 0;
 #pragma unroll
   for (int s = 0; s < NZ * 9; s++) {
-    const int dx = s % 3 - 1, dy = (s / 3) % 3 - 1, dz = s / 9 + ZL;
-    const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
-    const bool in = inside(L, nx, ny, nz) && !(SKIP_CENTER && s == S - 1);
+    const int dx = s % 3, dy = (s / 3) % 3, dz = s / 9 + ZL + 1;
+    const bool in = o.ix[dx] && o.iy[dy] && o.iz[dz] && !(SKIP_CENTER && s == S - 1);
     inm |= in ? 1u << s : 0u;
-    const int nn = in ? (int)lin(L, nx, ny, nz) : v;
+    const int nn = in ? v + o.ox[dx] + o.oy[dy] + o.oz[dz] : v;
     a[s] = s < S ? L.A[(S - 1 - s) * n + nn] : L.A[(s - S + 1) * n + v];
     xv[s] = __ldcg(&L.x[nn]);
   }
@@ -349,12 +375,14 @@ __device__ __forceinline__ void dict_tuple(const Lev& L, long long v, float* a) 
   constexpr int S = IS3D ? 14 : 5;
   int vx, vy, vz;
   coords(L, v, vx, vy, vz);
+  const Nb3 o = nb3(L, vx, vy, vz);  // L is colour-blocked
+  const int vi = (int)v;
 #pragma unroll
   for (int s = 0; s < NZ * 9; s++) {
-    const int nx = vx + s % 3 - 1, ny = vy + (s / 3) % 3 - 1, nz = vz + s / 9 + ZL;
-    const bool in = inside(L, nx, ny, nz);
-    const long long nn = in ? lin(L, nx, ny, nz) : v;
-    const float c = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + v];
+    const int dx = s % 3, dy = (s / 3) % 3, dz = s / 9 + ZL + 1;
+    const bool in = o.ix[dx] && o.iy[dy] && o.iz[dz];
+    const int nn = in ? vi + o.ox[dx] + o.oy[dy] + o.oz[dz] : vi;
+    const float c = s < S ? L.A[(long long)(S - 1 - s) * L.n + nn] : L.A[(long long)(s - S + 1) * L.n + vi];
     a[s] = in ? c : 0.f;
   }
 }
@@ -459,6 +487,8 @@ __device__ __forceinline__ float stencil_sub_dict(const Lev& L, const float* __r
                                                   float sum) {
   constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
   constexpr int S = IS3D ? 14 : 5;
+  const Nb3 o = nb3(L, vx, vy, vz);  // L is colour-blocked
+  const int vi = (int)lin(L, vx, vy, vz);
 #pragma unroll
   for (int dz = ZL; dz <= ZH; dz++) {
     float a[9], xv[9];
@@ -469,10 +499,9 @@ __device__ __forceinline__ float stencil_sub_dict(const Lev& L, const float* __r
       for (int dx = -1; dx <= 1; dx++) {
         const int q = (dy + 1) * 3 + (dx + 1);
         const int s = (dz - ZL) * 9 + q;
-        const int nx = vx + dx, ny = vy + dy, nz = vz + dz;
-        in[q] = inside(L, nx, ny, nz) && !(SKIP_CENTER && s == S - 1);
+        in[q] = o.ix[dx + 1] && o.iy[dy + 1] && o.iz[dz + 1] && !(SKIP_CENTER && s == S - 1);
         a[q] = t[s];
-        xv[q] = in[q] ? L.x[lin(L, nx, ny, nz)] : 0.f;
+        xv[q] = in[q] ? L.x[vi + o.ox[dx + 1] + o.oy[dy + 1] + o.oz[dz + 1]] : 0.f;
       }
 #pragma unroll
     for (int q = 0; q < 9; q++)
@@ -635,29 +664,30 @@ __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev S, const CgSca
   GRID_STRIDE(v, D.n) interp_vertex<IS3D, false>(D, S, v);
 }
 
-// ---- fused level-0 passes, streamed along z.  A CTA of 32 x 8 threads
-// owns a 28 x 12 column of fine cells over kZC planes (28 x 12 cells in 2D)
-// and walks the column's region -- the owned cells plus a 2-cell halo,
-// 32 x 16 cells per plane, one warp per two rows -- plane by plane, keeping
-// the last four planes of code, right-hand side, diagonal and x in shared
-// memory.  In each step plane p is staged (stage A), plane p-1 gets its
-// colour-1 pass (B) and plane p-2 its last pass (C), so every cell goes
-// through exactly the float operations of the per-colour Gauss-Seidel
-// passes, in the same order; halo cells are recomputed by each CTA that
-// needs them.  The next plane's loads are issued before the current
-// plane's passes.
-constexpr int kTX = 28, kTY = 12, kZC = 32;  // kZC: default planes per CTA (even)
-constexpr int kRX = 32, kRY = 16;
+// ---- fused level-0 passes, streamed along z.  A CTA of 512 threads owns
+// a 28 x 28 column of fine cells over zc planes (28 x 28 cells in 2D) and
+// walks the column's region -- the owned cells plus a 2-cell halo, 32 x 32
+// cells per plane -- plane by plane, keeping the last five planes of code,
+// right-hand side, diagonal and x in shared memory.  In each step plane p
+// is staged (stage A, two cells per thread), plane p-1 gets its colour-1
+// pass (B, one colour-1 cell per thread) and plane p-2 its last pass (C), so
+// every cell goes through exactly the float operations of the per-colour
+// Gauss-Seidel passes, in the same order; halo cells are recomputed by each
+// CTA that needs them.  With five planes in the ring, stage A of the next
+// step writes a plane no thread still reads, so a step needs two barriers.
+constexpr int kTX = 28, kTY = 28, kZC = 32;  // kZC: default planes per CTA (even)
+constexpr int kRX = 32, kRY = 32, kRing = 5;
+constexpr int kT0 = 512;  // threads of a level-0 CTA: rows w and w + 16 of warp w
 
-struct Ring0 {  // four planes of the region
-  float res[4][kRY][kRX];
-  float x[4][kRY][kRX];
-  float diag[4][kRY][kRX];
-  uint16_t code[4][kRY][kRX];
+struct Ring0 {  // five planes of the region (dynamic shared memory)
+  float res[kRing][kRY][kRX];
+  float x[kRing][kRY][kRX];
+  float diag[kRing][kRY][kRX];
+  uint16_t code[kRing][kRY][kRX];
 };
-__device__ __forceinline__ int ring0(int p) { return (p + 8) & 3; }  // p >= -2
+__device__ __forceinline__ int ring0(int p) { return (p + 10) % kRing; }  // p >= -2
 
-// one plane of this thread's two region cells (rows ty and ty + 8)
+// one plane of this thread's two region cells (rows w and w + 16)
 struct Plane0 {
   int c[2];
   float r[2], a[2], xd[2];
@@ -668,7 +698,7 @@ __device__ __forceinline__ void load_plane0(const Lev0& F, const float* __restri
   const int gx = ox + (int)(threadIdx.x & 31);
 #pragma unroll
   for (int k = 0; k < 2; k++) {
-    const int gy = oy + (int)(threadIdx.x >> 5) + 8 * k;
+    const int gy = oy + (int)(threadIdx.x >> 5) + 16 * k;
     const bool in = p >= 0 && p < d.nz && gx >= 0 && gy >= 0 && gx < d.nx && gy < d.ny;
     const long long g = in ? ix(d, gx, gy, p) : 0;
     P.c[k] = in ? F.code[g] : 0;
@@ -689,7 +719,7 @@ __device__ __forceinline__ void stage0_a(Ring0& R, const Plane0& P, bool hasA0f,
   const int lx = threadIdx.x & 31;
 #pragma unroll
   for (int k = 0; k < 2; k++) {
-    const int row = (threadIdx.x >> 5) + 8 * k;
+    const int row = (threadIdx.x >> 5) + 16 * k;
     const int c = P.c[k];
     const bool act = (c & kMgActive) != 0;
     const float diag = hasA0f ? P.a[k] : ((c & kMgTrivial) ? kTrivialScale : (float)(c & 7));
@@ -735,29 +765,29 @@ __device__ __forceinline__ float add_links0(const Ring0& R, int c, int q, int ro
 }
 
 // stage B: colour 1 on plane q, region minus its outer ring (reads
-// colour-0 values only)
+// colour-0 values only).  A region row holds 16 colour-1 cells: thread t
+// takes cell t & 15 of row 1 + (t >> 4), so no lane idles on colour 0.
 template <bool IS3D>
 __device__ __forceinline__ void stage0_b(Ring0& R, int ox, int oy, int q) {
-  const int sl = ring0(q);
-  const int lx = threadIdx.x & 31;
+  const int t = threadIdx.x;
+  if (t >= 16 * (kRY - 2)) return;
+  const int row = 1 + (t >> 4);
+  const int lx = ((1 + ox + oy + row + q) & 1) + 2 * (t & 15);
   if (lx < 1 || lx > kRX - 2) return;
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
-    const int row = (threadIdx.x >> 5) + 8 * k;
-    if (row < 1 || row > kRY - 2) continue;
-    const int c = R.code[sl][row][lx];
-    if (((ox + lx + oy + row + q) & 1) == 0 || !(c & kMgActive)) continue;
-    R.x[sl][row][lx] = add_links0<IS3D>(R, c, q, row, lx, scaled_b(c, R.res[sl][row][lx])) / R.diag[sl][row][lx];
-  }
+  const int sl = ring0(q);
+  const int c = R.code[sl][row][lx];
+  if (!(c & kMgActive)) return;
+  R.x[sl][row][lx] = add_links0<IS3D>(R, c, q, row, lx, scaled_b(c, R.res[sl][row][lx])) / R.diag[sl][row][lx];
 }
 
 // V-cycle entry on level 0: colour 0 from x = 0, colour 1, then the
 // residual (knSmoothColor x2 + knCalcResidual); writes x (to F.xd) and r of
 // the owned cells
 template <bool IS3D>
-__global__ void __launch_bounds__(256, 4) k_mg0_down(Lev0 F, const float* __restrict__ res, int zc, const CgScalars* sc) {
+__global__ void __launch_bounds__(kT0, 2) k_mg0_down(Lev0 F, const float* __restrict__ res, int zc, const CgScalars* sc) {
   if (sc->done) return;
-  __shared__ Ring0 R;
+  extern __shared__ __align__(16) unsigned char t0_smem[];
+  Ring0& R = *reinterpret_cast<Ring0*>(t0_smem);
   const Dims& d = F.d;
   constexpr int ZH = IS3D ? 1 : 0;
   const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2;
@@ -781,7 +811,7 @@ __global__ void __launch_bounds__(256, 4) k_mg0_down(Lev0 F, const float* __rest
       const int gx = ox + lx;
 #pragma unroll
       for (int k = 0; k < 2; k++) {
-        const int row = (threadIdx.x >> 5) + 8 * k;
+        const int row = (threadIdx.x >> 5) + 16 * k;
         const int gy = oy + row;
         if (lx < 2 || lx >= 2 + kTX || row < 2 || row >= 2 + kTY || gx >= d.nx || gy >= d.ny) continue;
         const long long g = ix(d, gx, gy, s);
@@ -794,7 +824,6 @@ __global__ void __launch_bounds__(256, 4) k_mg0_down(Lev0 F, const float* __rest
         F.r[g] = sum;
       }
     }
-    __syncthreads();
   }
 }
 
@@ -804,11 +833,12 @@ __global__ void __launch_bounds__(256, 4) k_mg0_down(Lev0 F, const float* __rest
 // from F.xd, halo included, and writes the result to x0: reading and writing
 // one array would race with the neighbouring CTAs' writes.
 template <bool IS3D, bool DOT>
-__global__ void __launch_bounds__(256, 4) k_mg0_up(Lev0 F, const float* __restrict__ res, int zc, float* x0, Lev C,
+__global__ void __launch_bounds__(kT0, 2) k_mg0_up(Lev0 F, const float* __restrict__ res, int zc, float* x0, Lev C,
                                                    double* part, CgScalars* sc) {
   if (sc->done) return;
   constexpr int CX = kRX / 2 + 1, CY = kRY / 2 + 1;
-  __shared__ Ring0 R;
+  extern __shared__ __align__(16) unsigned char t0_smem[];
+  Ring0& R = *reinterpret_cast<Ring0*>(t0_smem);
   __shared__ float scx[2][CY][CX];  // level-1 parents of the region, two coarse planes
   const Dims& d = F.d;
   constexpr int ZH = IS3D ? 1 : 0;
@@ -852,7 +882,7 @@ __global__ void __launch_bounds__(256, 4) k_mg0_up(Lev0 F, const float* __restri
       const int gx = ox + lx;
 #pragma unroll
       for (int k = 0; k < 2; k++) {
-        const int row = (threadIdx.x >> 5) + 8 * k;
+        const int row = (threadIdx.x >> 5) + 16 * k;
         const int gy = oy + row;
         if (lx < 2 || lx >= 2 + kTX || row < 2 || row >= 2 + kTY || gx >= d.nx || gy >= d.ny) continue;
         const long long g = ix(d, gx, gy, s);
@@ -864,7 +894,6 @@ __global__ void __launch_bounds__(256, 4) k_mg0_up(Lev0 F, const float* __restri
         if (DOT) acc.add(v * R.res[sl][row][lx]);  // inactive cells: x = 0
       }
     }
-    __syncthreads();
   }
   if (!DOT) return;
   const double bsum = block_sum(acc.value());
@@ -1386,6 +1415,14 @@ int ensure_paths() {
       cudaFuncSetAttribute(k_mg_coarse_cg<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(k_mg_coarse_cg<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
     return 1;
+  const int r0 = (int)sizeof(Ring0);
+  if (cudaFuncSetAttribute(k_mg0_down<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_down<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess)
+    return 1;
   // the cluster V-cycle tail: 16 CTAs where the GPU can co-schedule them
   g_tailCta = 0;
   if (cudaFuncSetAttribute(k_mg_tail<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
@@ -1830,8 +1867,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
     {
       Fam f(h, "mg_down_l0");
       count_launch();
-      if (h->is3d) k_mg0_down<true><<<gt, kThreads1, 0, s>>>(l0, res, zc, sc);
-      else k_mg0_down<false><<<gt, kThreads1, 0, s>>>(l0, res, zc, sc);
+      if (h->is3d) k_mg0_down<true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, sc);
+      else k_mg0_down<false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, sc);
     }
     {
       Fam f(h, "mg_restrict_l0");
@@ -1892,11 +1929,11 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       Fam f(h, "mg_up_l0");
       count_launch();
       if (h->is3d) {
-        if (init) k_mg0_up<true, false><<<gt, kThreads1, 0, s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
-        else k_mg0_up<true, true><<<gt, kThreads1, 0, s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
+        if (init) k_mg0_up<true, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
+        else k_mg0_up<true, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
       } else {
-        if (init) k_mg0_up<false, false><<<gt, kThreads1, 0, s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
-        else k_mg0_up<false, true><<<gt, kThreads1, 0, s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
+        if (init) k_mg0_up<false, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
+        else k_mg0_up<false, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
       }
     }
   }
