@@ -54,12 +54,11 @@ BYTES_PER_CELL = {
     "make_codes": 4 + 2 + 2 + 2,
     "correct_velocity": 4 + 4 + 12 + 12,
     "join": 4 + 4 + 4,
-    # multigrid V-cycle, level 0 (bytes per fine cell)
-    "mg_smooth_l0": 2 + 4 + 4 + 2,          # code, residual, x (every cell a neighbour or updated) -> x (half)
-    "mg_smooth_l0_first": 2 + 4 + 4,        # code, residual -> x (all cells, from a zero guess)
-    "mg_residual_l0": 2 + 4 + 4 + 4,        # code, residual, x -> r
-    "mg_restrict_l0": 4 + 0.5,              # r -> coarse b (1/8 of the cells)
-    "mg_interp_l0": 2 + 4 + 4 + 0.5,        # code, x, coarse x -> x
+    # multigrid V-cycle, level 0 (bytes per fine cell; the level-1 vectors
+    # are 1/8 of the cells)
+    "mg_down_l0": 2 + 4 + 4 + 4,            # code, residual -> x (pre-smoothed), r
+    "mg_up_l0": 2 + 4 + 4 + 0.5 + 4,        # code, residual, x, level-1 x -> x (+dot)
+    "mg_restrict_l0": 4 + 0.5,              # r -> level-1 b
     "mg_dot": 4 + 4,                        # z, residual (+dot)
 }
 
