@@ -245,17 +245,14 @@ __global__ void __launch_bounds__(256) k_sl_mac(Dims d, CMac vel, CMac src, Mac 
 }
 
 // doClampComponentMAC (advection.cpp:191-235)
-__device__ __forceinline__ float clamp_component_mac(const Dims& d, const int* __restrict__ flags, float dst,
-                                                     const float* __restrict__ orig, float fwd, int c, int i, int j, int k,
-                                                     V3 vel, int clampMode) {
+__device__ __forceinline__ float clamp_component_mac(const Dims& d, int fo, int fnb, float dst, const float* __restrict__ orig,
+                                                     float fwd, int i, int j, int k, V3 vel, int clampMode) {
+  // fo, fnb: flags of the cell and of its lower neighbour along the component
   float mn = FLT_MAX, mx = -FLT_MAX;
   const float posx = (float)i, posy = (float)j, posz = (float)k;
-  if (clampMode == 2) {
-    const long long o = ix(d, i, j, k);
-    const long long nb = o - (c == 0 ? 1 : (c == 1 ? d.sy : d.sz));
-    if (!((__ldg(flags + o) & (kFluid | kEmpty)) && (__ldg(flags + nb) & (kFluid | kEmpty)))) return fwd;
-  }
+  if (clampMode == 2 && !((fo & (kFluid | kEmpty)) && (fnb & (kFluid | kEmpty)))) return fwd;
   const int np = clampMode == 1 ? 2 : 1;
+  const int Y = (int)d.sy, Z = (int)d.sz;  // grids hold < 2^31 cells
   for (int l = 0; l < np; l++) {
     const int qx = (int)(l == 0 ? posx - vel.x : posx + vel.x);
     const int qy = (int)(l == 0 ? posy - vel.y : posy + vel.y);
@@ -263,11 +260,12 @@ __device__ __forceinline__ float clamp_component_mac(const Dims& d, const int* _
     const int i0 = min(max(qx, 0), d.nx - 2);
     const int j0 = min(max(qy, 0), d.ny - 2);
     const int k0 = min(max(qz, 0), d.is3d ? d.nz - 2 : 0);
+    const float* p = orig + (i0 + Y * j0 + Z * k0);
     const int nk = d.is3d ? 2 : 1;
     for (int kk = 0; kk < nk; kk++) {
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        const float v = __ldg(orig + ix(d, i0 + (q & 1), j0 + (q >> 1), k0 + kk));
+        const float v = __ldg(p + (q & 1) + Y * (q >> 1) + Z * kk);
         if (v < mn) mn = v;
         if (v > mx) mx = v;
       }
@@ -289,11 +287,13 @@ __device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __
                                                         CMac fwd, Mac dst, float dt, float strength, int clampMode, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   bool skip[3];
-  const bool fl = isF(flags, idx);
-  skip[0] = skip[1] = skip[2] = !fl;
-  if (i > 0 && !isF(flags, idx - 1)) skip[0] = true;
-  if (j > 0 && !isF(flags, idx - d.sy)) skip[1] = true;
-  if (k > 0 && !isF(flags, idx - d.sz)) skip[2] = true;
+  const int f0 = __ldg(flags + idx);
+  const int fm[3] = {i > 0 ? __ldg(flags + idx - 1) : 0, j > 0 ? __ldg(flags + idx - d.sy) : 0,
+                     k > 0 ? __ldg(flags + idx - d.sz) : 0};
+  skip[0] = skip[1] = skip[2] = !(f0 & kFluid);
+  if (i > 0 && !(fm[0] & kFluid)) skip[0] = true;
+  if (j > 0 && !(fm[1] & kFluid)) skip[1] = true;
+  if (k > 0 && !(fm[2] & kFluid)) skip[2] = true;
   const bool inner = i >= 1 && i < d.nx - 1 && j >= 1 && j < d.ny - 1 && (!d.is3d || (k >= 1 && k < d.nz - 1));
   const float hs = strength * 0.5f;
   float bwd[3] = {0.f, 0.f, 0.f};
@@ -321,10 +321,10 @@ __device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __
     val[c] = skip[c] ? fw[c] : fmaf(hs, __ldg(orig.c(c) + idx) - bwd[c], fw[c]);
   }
   if (inner) {
-    val[0] = clamp_component_mac(d, flags, val[0], orig.u, fw[0], 0, i, j, k, V3{ax.x * dt, ax.y * dt, ax.z * dt}, clampMode);
-    val[1] = clamp_component_mac(d, flags, val[1], orig.v, fw[1], 1, i, j, k, V3{ay.x * dt, ay.y * dt, ay.z * dt}, clampMode);
+    val[0] = clamp_component_mac(d, f0, fm[0], val[0], orig.u, fw[0], i, j, k, V3{ax.x * dt, ax.y * dt, ax.z * dt}, clampMode);
+    val[1] = clamp_component_mac(d, f0, fm[1], val[1], orig.v, fw[1], i, j, k, V3{ay.x * dt, ay.y * dt, ay.z * dt}, clampMode);
     if (d.is3d)
-      val[2] = clamp_component_mac(d, flags, val[2], orig.w, fw[2], 2, i, j, k, V3{az.x * dt, az.y * dt, az.z * dt}, clampMode);
+      val[2] = clamp_component_mac(d, f0, fm[2], val[2], orig.w, fw[2], i, j, k, V3{az.x * dt, az.y * dt, az.z * dt}, clampMode);
   }
   dst.u[idx] = val[0];
   dst.v[idx] = val[1];

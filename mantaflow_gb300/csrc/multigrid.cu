@@ -556,13 +556,12 @@ __device__ __forceinline__ void residual_vertex(const Lev& L, long long v) {
 // knRestrict into slot v of level D from the level below (level 0 when
 // FROM0), plus knSet(x[D], 0) of the next smoothing's initial guess
 template <bool FROM0, bool CG>
-__device__ __forceinline__ void restrict_vertex(const Lev& D, const Lev& S, const Lev0& F, long long v) {
+__device__ __forceinline__ void restrict_vertex_at(const Lev& D, const Lev& S, const Lev0& F, long long v, int vx, int vy,
+                                                   int vz) {
   const int sx = FROM0 ? F.d.nx : S.sx, sy = FROM0 ? F.d.ny : S.sy, sz = FROM0 ? F.d.nz : S.sz;
   const long long py = F.d.sy, pz = F.d.sz;
   D.x[v] = 0.f;
   if (D.type[v] == kVtInactive) return;
-  int vx, vy, vz;
-  coords(D, v, vx, vy, vz);
   // the fine vertices 2V-1 .. 2V+1 inside the level, in the reference's
   // loop order; all loads first
   float rv[27];
@@ -581,6 +580,12 @@ __device__ __forceinline__ void restrict_vertex(const Lev& D, const Lev& S, cons
     if (in[q]) sum = sum + inv_pow2(parity3(rx, ry, rz)) * rv[q];
   }
   D.b[v] = sum;
+}
+template <bool FROM0, bool CG>
+__device__ __forceinline__ void restrict_vertex(const Lev& D, const Lev& S, const Lev0& F, long long v) {
+  int vx, vy, vz;
+  coords(D, v, vx, vy, vz);
+  restrict_vertex_at<FROM0, CG>(D, S, F, v, vx, vy, vz);
 }
 
 // knInterpolate from level S = D+1 and knAddAssign: x[D] += I * x[S]
@@ -656,6 +661,15 @@ template <bool FROM0>
 __global__ void __launch_bounds__(256) k_mg_restrict(Lev D, Lev S, Lev0 F, const CgScalars* sc) {
   if (sc->done) return;
   GRID_STRIDE(v, D.n) restrict_vertex<FROM0, false>(D, S, F, v);
+}
+
+// restriction from level 0 with threads in x-fastest coarse order (a warp's
+// 27 gathers then cover 64 neighbouring fine cells per row instead of 128)
+__global__ void __launch_bounds__(256) k_mg_restrict0(Lev D, Lev0 F, const CgScalars* sc) {
+  if (sc->done) return;
+  const int vx = blockIdx.x * 32 + (threadIdx.x & 31), vy = blockIdx.y * 8 + (threadIdx.x >> 5), vz = blockIdx.z;
+  if (vx >= D.sx || vy >= D.sy) return;
+  restrict_vertex_at<true, false>(D, D, F, lin(D, vx, vy, vz), vx, vy, vz);
 }
 
 template <bool IS3D>
@@ -1873,7 +1887,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
     {
       Fam f(h, "mg_restrict_l0");
       count_launch();
-      k_mg_restrict<true><<<blocks_for(h->lev[1].n), kThreads1, 0, s>>>(h->lev[1], none, l0, sc);
+      const Lev& v1 = h->lev[1];
+      k_mg_restrict0<<<dim3((v1.sx + 31) / 32, (v1.sy + 7) / 8, v1.sz), kThreads1, 0, s>>>(v1, l0, sc);
     }
     // levels below the cluster tail (all of them without one)
     const int first = h->tailFirst ? h->tailFirst : L;
