@@ -86,6 +86,18 @@ int mg_grid_destroy(mg_grid g);
 /* host <-> device in the reference layout; bytes must equal the grid size */
 int mg_grid_upload(mg_grid g, const void* host, size_t bytes);
 int mg_grid_download(mg_grid g, void* host, size_t bytes);
+/* Asynchronous forms of mg_grid_upload / mg_grid_download for pipelined
+ * hosts (no counterpart in the reference, whose copies are synchronous).
+ * They return at once; the host buffer (pinned: mg_host_alloc) must stay
+ * untouched until mg_solver_wait_copies returns.  The transfer runs on the
+ * solver's copy stream through a device staging copy of the grid, ordered
+ * against the solver's kernels: an upload lands before any kernel queued
+ * after it, a download takes the grid as it is after the kernels queued
+ * before it, and the next step's kernels may run while it streams out. */
+int mg_grid_upload_async(mg_grid g, const void* host, size_t bytes);
+int mg_grid_download_async(mg_grid g, void* host, size_t bytes);
+/* Block until every asynchronous transfer and kernel of the solver is done. */
+int mg_solver_wait_copies(mg_solver s);
 /* Grid<T>::swap (grid.cpp:99-110): exchanges the storage of two grids */
 int mg_grid_swap(mg_grid a, mg_grid b);
 /* Grid<T>::copyFrom */

@@ -73,6 +73,9 @@ SIGNATURES = [
     ("mg_grid_destroy", _I, [_P]),
     ("mg_grid_upload", _I, [_P, _P, C.c_size_t]),
     ("mg_grid_download", _I, [_P, _P, C.c_size_t]),
+    ("mg_grid_upload_async", _I, [_P, _P, C.c_size_t]),
+    ("mg_grid_download_async", _I, [_P, _P, C.c_size_t]),
+    ("mg_solver_wait_copies", _I, [_P]),
     ("mg_grid_swap", _I, [_P, _P]),
     ("mg_grid_copy", _I, [_P, _P]),
     ("mg_grid_set_const", _I, [_P, _F, _F, _F]),

@@ -89,6 +89,7 @@ struct mg_solver_s {
   int dim;
   float dt = 1.f;
   cudaStream_t stream = nullptr;
+  cudaStream_t copyStream = nullptr;  // asynchronous grid transfers (created on first use)
   std::multimap<size_t, void*> pool;  // free device buffers by size
   std::set<mg_grid> grids;
   size_t poolBytes = 0;
@@ -135,6 +136,11 @@ struct mg_grid_s {
   mg_solver s;
   int kind;
   void* data;   // device: n floats / ints, or 3n floats (SoA) for Vec3/MAC
+  // asynchronous transfers: a device staging copy of the grid (AoS for
+  // Vec3/MAC), ready / free events, allocated on first use
+  void* stage = nullptr;
+  cudaEvent_t stageReady = nullptr, stageFree = nullptr;
+  bool stageUsed = false;
   int comps() const { return (kind == MG_VEC3 || kind == MG_MAC) ? 3 : 1; }
   size_t bytes() const { return sizeof(float) * (size_t)comps() * (size_t)s->d.n; }
   float* f() const { return (float*)data; }
@@ -343,10 +349,20 @@ static void free_cg_state(mg_solver s) {
   s->micWave = MicWavePlan{};
 }
 
+static void free_stage(mg_grid g) {
+  if (g->stage) cudaFree(g->stage);
+  if (g->stageReady) cudaEventDestroy(g->stageReady);
+  if (g->stageFree) cudaEventDestroy(g->stageFree);
+  g->stage = nullptr;
+  g->stageReady = g->stageFree = nullptr;
+}
+
 extern "C" int mg_solver_destroy(mg_solver s) {
   if (!valid_solver(s)) return fail(MG_ERR_ARG, "mg_solver_destroy: invalid solver");
+  if (s->copyStream) cudaStreamSynchronize(s->copyStream);
   cudaStreamSynchronize(s->stream);
   for (auto g : s->grids) {
+    free_stage(g);
     cudaFree(g->data);
     delete g;
   }
@@ -359,6 +375,7 @@ extern "C" int mg_solver_destroy(mg_solver s) {
   prof_collect(s);
   for (auto e : s->evFree) cudaEventDestroy(e);
   for (auto e : s->marks) cudaEventDestroy(e);
+  if (s->copyStream) cudaStreamDestroy(s->copyStream);
   cudaStreamDestroy(s->stream);
   g_ctx.solvers.erase(s);
   delete s;
@@ -413,7 +430,9 @@ extern "C" int mg_grid_create(mg_solver s, int kind, mg_grid* out) {
 
 extern "C" int mg_grid_destroy(mg_grid g) {
   NEED_GRID(g, "mg_grid_destroy");
+  if (g->s->copyStream) cudaStreamSynchronize(g->s->copyStream);
   cudaStreamSynchronize(g->s->stream);
+  free_stage(g);
   cudaFree(g->data);
   g->s->grids.erase(g);
   delete g;
@@ -454,6 +473,78 @@ extern "C" int mg_grid_download(mg_grid g, void* host, size_t bytes) {
     CK(cudaStreamSynchronize(s->stream));
     return MG_OK;
   }
+  CK(cudaStreamSynchronize(s->stream));
+  return MG_OK;
+}
+
+// ---- asynchronous transfers.  An upload copies host -> staging on the
+// solver's copy stream, then staging -> grid on the compute stream; a
+// download snapshots grid -> staging on the compute stream, then staging ->
+// host on the copy stream.  Events order the two streams and keep a grid's
+// staging buffer from being refilled before its previous transfer is done,
+// so a caller can queue step t+1 while step t's results are still leaving.
+static int ensure_stage(mg_grid g) {
+  mg_solver s = g->s;
+  if (!s->copyStream) CK(cudaStreamCreateWithFlags(&s->copyStream, cudaStreamNonBlocking));
+  if (!g->stage) {
+    if (cudaMalloc(&g->stage, g->bytes()) != cudaSuccess) {
+      cudaGetLastError();
+      g->stage = nullptr;
+      return fail(MG_ERR_NOMEM, "asynchronous transfer: out of device memory");
+    }
+    CK(cudaEventCreateWithFlags(&g->stageReady, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&g->stageFree, cudaEventDisableTiming));
+  }
+  return MG_OK;
+}
+
+extern "C" int mg_grid_upload_async(mg_grid g, const void* host, size_t bytes) {
+  NEED_GRID(g, "mg_grid_upload_async");
+  if (!host || bytes != g->bytes()) return fail(MG_ERR_ARG, "mg_grid_upload_async: host buffer size does not match the grid");
+  const int st = ensure_stage(g);
+  if (st) return st;
+  mg_solver s = g->s;
+  ProfScope ps(s, "h2d");
+  if (g->stageUsed) CK(cudaStreamWaitEvent(s->copyStream, g->stageFree, 0));
+  CK(cudaMemcpyAsync(g->stage, host, bytes, cudaMemcpyHostToDevice, s->copyStream));
+  CK(cudaEventRecord(g->stageReady, s->copyStream));
+  CK(cudaStreamWaitEvent(s->stream, g->stageReady, 0));
+  if (is_vec(g)) {
+    launch_aos_to_soa(s->d.n, (const float*)g->stage, g->mac(), s->stream);
+    CKL();
+  } else {
+    CK(cudaMemcpyAsync(g->data, g->stage, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  }
+  CK(cudaEventRecord(g->stageFree, s->stream));
+  g->stageUsed = true;
+  return MG_OK;
+}
+
+extern "C" int mg_grid_download_async(mg_grid g, void* host, size_t bytes) {
+  NEED_GRID(g, "mg_grid_download_async");
+  if (!host || bytes != g->bytes()) return fail(MG_ERR_ARG, "mg_grid_download_async: host buffer size does not match the grid");
+  const int st = ensure_stage(g);
+  if (st) return st;
+  mg_solver s = g->s;
+  ProfScope ps(s, "d2h");
+  if (g->stageUsed) CK(cudaStreamWaitEvent(s->stream, g->stageFree, 0));
+  if (is_vec(g)) {
+    launch_soa_to_aos(s->d.n, g->cmac(), (float*)g->stage, s->stream);
+    CKL();
+  } else {
+    CK(cudaMemcpyAsync(g->stage, g->data, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  }
+  CK(cudaEventRecord(g->stageReady, s->stream));
+  CK(cudaStreamWaitEvent(s->copyStream, g->stageReady, 0));
+  CK(cudaMemcpyAsync(host, g->stage, bytes, cudaMemcpyDeviceToHost, s->copyStream));
+  CK(cudaEventRecord(g->stageFree, s->copyStream));
+  g->stageUsed = true;
+  return MG_OK;
+}
+
+extern "C" int mg_solver_wait_copies(mg_solver s) {
+  if (!valid_solver(s)) return fail(MG_ERR_ARG, "mg_solver_wait_copies: invalid solver");
+  if (s->copyStream) CK(cudaStreamSynchronize(s->copyStream));
   CK(cudaStreamSynchronize(s->stream));
   return MG_OK;
 }
