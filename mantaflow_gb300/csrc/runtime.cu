@@ -89,7 +89,12 @@ struct mg_solver_s {
   int dim;
   float dt = 1.f;
   cudaStream_t stream = nullptr;
-  cudaStream_t copyStream = nullptr;  // asynchronous grid transfers (created on first use)
+  // asynchronous grid transfers: copy streams, created on first use; a
+  // transfer is split into one chunk per stream so several copy engines
+  // move it at once
+  static constexpr int kMaxCopyStreams = 8;
+  int ncopy = 0;
+  cudaStream_t copyStream[kMaxCopyStreams] = {};
   std::multimap<size_t, void*> pool;  // free device buffers by size
   std::set<mg_grid> grids;
   size_t poolBytes = 0;
@@ -139,8 +144,9 @@ struct mg_grid_s {
   // asynchronous transfers: a device staging copy of the grid (AoS for
   // Vec3/MAC), ready / free events, allocated on first use
   void* stage = nullptr;
-  cudaEvent_t stageReady = nullptr, stageFree = nullptr;
-  bool stageUsed = false;
+  cudaEvent_t stageReady = nullptr;
+  cudaEvent_t stageFree[mg_solver_s::kMaxCopyStreams] = {};  // one per stream the last transfer used
+  int nFree = 0;
   int comps() const { return (kind == MG_VEC3 || kind == MG_MAC) ? 3 : 1; }
   size_t bytes() const { return sizeof(float) * (size_t)comps() * (size_t)s->d.n; }
   float* f() const { return (float*)data; }
@@ -352,14 +358,20 @@ static void free_cg_state(mg_solver s) {
 static void free_stage(mg_grid g) {
   if (g->stage) cudaFree(g->stage);
   if (g->stageReady) cudaEventDestroy(g->stageReady);
-  if (g->stageFree) cudaEventDestroy(g->stageFree);
+  for (auto& e : g->stageFree)
+    if (e) cudaEventDestroy(e);
   g->stage = nullptr;
-  g->stageReady = g->stageFree = nullptr;
+  g->stageReady = nullptr;
+  for (auto& e : g->stageFree) e = nullptr;
+  g->nFree = 0;
+}
+static void sync_copies(mg_solver s) {
+  for (int k = 0; k < s->ncopy; k++) cudaStreamSynchronize(s->copyStream[k]);
 }
 
 extern "C" int mg_solver_destroy(mg_solver s) {
   if (!valid_solver(s)) return fail(MG_ERR_ARG, "mg_solver_destroy: invalid solver");
-  if (s->copyStream) cudaStreamSynchronize(s->copyStream);
+  sync_copies(s);
   cudaStreamSynchronize(s->stream);
   for (auto g : s->grids) {
     free_stage(g);
@@ -375,7 +387,7 @@ extern "C" int mg_solver_destroy(mg_solver s) {
   prof_collect(s);
   for (auto e : s->evFree) cudaEventDestroy(e);
   for (auto e : s->marks) cudaEventDestroy(e);
-  if (s->copyStream) cudaStreamDestroy(s->copyStream);
+  for (int k = 0; k < s->ncopy; k++) cudaStreamDestroy(s->copyStream[k]);
   cudaStreamDestroy(s->stream);
   g_ctx.solvers.erase(s);
   delete s;
@@ -430,7 +442,7 @@ extern "C" int mg_grid_create(mg_solver s, int kind, mg_grid* out) {
 
 extern "C" int mg_grid_destroy(mg_grid g) {
   NEED_GRID(g, "mg_grid_destroy");
-  if (g->s->copyStream) cudaStreamSynchronize(g->s->copyStream);
+  sync_copies(g->s);
   cudaStreamSynchronize(g->s->stream);
   free_stage(g);
   cudaFree(g->data);
@@ -485,7 +497,13 @@ extern "C" int mg_grid_download(mg_grid g, void* host, size_t bytes) {
 // so a caller can queue step t+1 while step t's results are still leaving.
 static int ensure_stage(mg_grid g) {
   mg_solver s = g->s;
-  if (!s->copyStream) CK(cudaStreamCreateWithFlags(&s->copyStream, cudaStreamNonBlocking));
+  if (!s->ncopy) {
+    int n = 4;
+    if (const char* e = std::getenv("MANTAGPU_COPY_STREAMS")) n = std::atoi(e);
+    n = std::max(1, std::min(n, (int)mg_solver_s::kMaxCopyStreams));
+    for (int k = 0; k < n; k++) CK(cudaStreamCreateWithFlags(&s->copyStream[k], cudaStreamNonBlocking));
+    s->ncopy = n;
+  }
   if (!g->stage) {
     if (cudaMalloc(&g->stage, g->bytes()) != cudaSuccess) {
       cudaGetLastError();
@@ -493,41 +511,64 @@ static int ensure_stage(mg_grid g) {
       return fail(MG_ERR_NOMEM, "asynchronous transfer: out of device memory");
     }
     CK(cudaEventCreateWithFlags(&g->stageReady, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&g->stageFree, cudaEventDisableTiming));
+    for (int k = 0; k < mg_solver_s::kMaxCopyStreams; k++)
+      CK(cudaEventCreateWithFlags(&g->stageFree[k], cudaEventDisableTiming));
   }
+  return MG_OK;
+}
+// wait on stream st until the grid's staging copy is free
+static int wait_stage_free(mg_grid g, cudaStream_t st) {
+  for (int k = 0; k < g->nFree; k++) CK(cudaStreamWaitEvent(st, g->stageFree[k], 0));
+  return MG_OK;
+}
+// the copy split into one 256-byte-aligned chunk per copy stream, each after
+// `ready`; records the grid's free events on the streams it used
+static int chunked_copy(mg_grid g, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaEvent_t ready) {
+  mg_solver s = g->s;
+  const size_t per = ((bytes + s->ncopy - 1) / s->ncopy + 255) & ~(size_t)255;
+  int used = 0;
+  for (int k = 0; k < s->ncopy && (size_t)k * per < bytes; k++) {
+    const size_t off = (size_t)k * per, len = std::min(per, bytes - off);
+    if (ready) CK(cudaStreamWaitEvent(s->copyStream[k], ready, 0));
+    CK(cudaMemcpyAsync((char*)dst + off, (const char*)src + off, len, kind, s->copyStream[k]));
+    CK(cudaEventRecord(g->stageFree[k], s->copyStream[k]));
+    used++;
+  }
+  g->nFree = used;
   return MG_OK;
 }
 
 extern "C" int mg_grid_upload_async(mg_grid g, const void* host, size_t bytes) {
   NEED_GRID(g, "mg_grid_upload_async");
   if (!host || bytes != g->bytes()) return fail(MG_ERR_ARG, "mg_grid_upload_async: host buffer size does not match the grid");
-  const int st = ensure_stage(g);
+  int st = ensure_stage(g);
   if (st) return st;
   mg_solver s = g->s;
   ProfScope ps(s, "h2d");
-  if (g->stageUsed) CK(cudaStreamWaitEvent(s->copyStream, g->stageFree, 0));
-  CK(cudaMemcpyAsync(g->stage, host, bytes, cudaMemcpyHostToDevice, s->copyStream));
-  CK(cudaEventRecord(g->stageReady, s->copyStream));
-  CK(cudaStreamWaitEvent(s->stream, g->stageReady, 0));
+  for (int k = 0; k < s->ncopy; k++)
+    if ((st = wait_stage_free(g, s->copyStream[k]))) return st;
+  if ((st = chunked_copy(g, g->stage, host, bytes, cudaMemcpyHostToDevice, nullptr))) return st;
+  // the compute stream waits for every chunk, then moves staging -> grid
+  for (int k = 0; k < g->nFree; k++) CK(cudaStreamWaitEvent(s->stream, g->stageFree[k], 0));
   if (is_vec(g)) {
     launch_aos_to_soa(s->d.n, (const float*)g->stage, g->mac(), s->stream);
     CKL();
   } else {
     CK(cudaMemcpyAsync(g->data, g->stage, bytes, cudaMemcpyDeviceToDevice, s->stream));
   }
-  CK(cudaEventRecord(g->stageFree, s->stream));
-  g->stageUsed = true;
+  CK(cudaEventRecord(g->stageFree[0], s->stream));
+  g->nFree = 1;
   return MG_OK;
 }
 
 extern "C" int mg_grid_download_async(mg_grid g, void* host, size_t bytes) {
   NEED_GRID(g, "mg_grid_download_async");
   if (!host || bytes != g->bytes()) return fail(MG_ERR_ARG, "mg_grid_download_async: host buffer size does not match the grid");
-  const int st = ensure_stage(g);
+  int st = ensure_stage(g);
   if (st) return st;
   mg_solver s = g->s;
   ProfScope ps(s, "d2h");
-  if (g->stageUsed) CK(cudaStreamWaitEvent(s->stream, g->stageFree, 0));
+  if ((st = wait_stage_free(g, s->stream))) return st;
   if (is_vec(g)) {
     launch_soa_to_aos(s->d.n, g->cmac(), (float*)g->stage, s->stream);
     CKL();
@@ -535,16 +576,12 @@ extern "C" int mg_grid_download_async(mg_grid g, void* host, size_t bytes) {
     CK(cudaMemcpyAsync(g->stage, g->data, bytes, cudaMemcpyDeviceToDevice, s->stream));
   }
   CK(cudaEventRecord(g->stageReady, s->stream));
-  CK(cudaStreamWaitEvent(s->copyStream, g->stageReady, 0));
-  CK(cudaMemcpyAsync(host, g->stage, bytes, cudaMemcpyDeviceToHost, s->copyStream));
-  CK(cudaEventRecord(g->stageFree, s->copyStream));
-  g->stageUsed = true;
-  return MG_OK;
+  return chunked_copy(g, host, g->stage, bytes, cudaMemcpyDeviceToHost, g->stageReady);
 }
 
 extern "C" int mg_solver_wait_copies(mg_solver s) {
   if (!valid_solver(s)) return fail(MG_ERR_ARG, "mg_solver_wait_copies: invalid solver");
-  if (s->copyStream) CK(cudaStreamSynchronize(s->copyStream));
+  for (int k = 0; k < s->ncopy; k++) CK(cudaStreamSynchronize(s->copyStream[k]));
   CK(cudaStreamSynchronize(s->stream));
   return MG_OK;
 }
