@@ -25,15 +25,21 @@
 // reference's sorted table of fine-grid paths).
 //
 // V-cycle (doVCycle, :448-504; V(1,1), zero initial guess).  Gauss-Seidel
-// colour passes are one launch per colour: red/black on level 0 (7-point
-// stencil), eight (four in 2D) 2x2x2 block colours on coarse levels.  Within
-// a colour every vertex reads only other colours, so each pass reproduces the
-// reference's float arithmetic exactly; restriction and interpolation sum
-// their terms in the reference's loop order.  The coarsest level is solved by
-// Jacobi-preconditioned CG (solveCG, :793-902) by one CTA with the vectors in
-// shared memory, in double-float arithmetic with tree-summed dot products:
-// it differs from the serial double reference only far below float
-// resolution.
+// uses red/black colours on level 0 (7-point stencil) and eight (four in 2D)
+// 2x2x2 block colours on coarse levels; within a colour every vertex reads
+// only other colours, so each pass reproduces the reference's float
+// arithmetic exactly, and restriction and interpolation sum their terms in
+// the reference's loop order.  Level 0 runs as two fused kernels streamed
+// along z (entry: both pre-smoothing colours and the residual; exit:
+// interpolation, both post-smoothing colours and the outer CG's dot).
+// Coarse levels with many slots run one launch per colour, reading a stencil
+// dictionary where the level's stencils repeat.  The remaining levels and
+// the coarsest solve run as one thread-block-cluster launch; the coarsest
+// level is solved by Jacobi-preconditioned CG (solveCG, :793-902) in
+// double-float arithmetic with tree-summed dot products, which differs from
+// the serial double reference only far below float resolution (a one-CTA
+// kernel solves it when the hierarchy has a single level or the GPU cannot
+// co-schedule the cluster).
 #include "mg_multigrid.h"
 #include "mg_reduce.cuh"
 
