@@ -1858,6 +1858,7 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   const Lev none{};
   const int zc = h->zc;
   const dim3 gt((d.nx + kTX - 1) / kTX, (d.ny + kTY - 1) / kTY, d.is3d ? (d.nz + zc - 1) / zc : 1);
+  if (gt.y > 65535u || gt.z > 65535u) return 1;  // beyond the launch limits (> 1.8 M cells along y or z)
   static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
   const int ncol = h->is3d ? 8 : 4;
   auto smooth = [&](int l, bool reversed) {
@@ -1894,7 +1895,10 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       Fam f(h, "mg_restrict_l0");
       count_launch();
       const Lev& v1 = h->lev[1];
-      k_mg_restrict0<<<dim3((v1.sx + 31) / 32, (v1.sy + 7) / 8, v1.sz), kThreads1, 0, s>>>(v1, l0, sc);
+      if (v1.sz <= 65535 && (v1.sy + 7) / 8 <= 65535)
+        k_mg_restrict0<<<dim3((v1.sx + 31) / 32, (v1.sy + 7) / 8, v1.sz), kThreads1, 0, s>>>(v1, l0, sc);
+      else  // grid dimensions beyond the y / z launch limits: slot order
+        k_mg_restrict<true><<<blocks_for(v1.n), kThreads1, 0, s>>>(v1, none, l0, sc);
     }
     // levels below the cluster tail (all of them without one)
     const int first = h->tailFirst ? h->tailFirst : L;
