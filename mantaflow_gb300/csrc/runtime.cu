@@ -412,7 +412,7 @@ extern "C" int mg_solver_sync(mg_solver s) {
 extern "C" int mg_solver_memory(mg_solver s, size_t* bytes) {
   if (!valid_solver(s) || !bytes) return fail(MG_ERR_ARG, "mg_solver_memory: invalid argument");
   size_t b = s->poolBytes;
-  for (auto g : s->grids) b += g->bytes();
+  for (auto g : s->grids) b += g->bytes() * (g->stage ? 2 : 1);  // + the staging copy of asynchronous transfers
   const size_t n = (size_t)s->d.n;
   if (s->code) b += n * (sizeof(code_t) + 4 * sizeof(float));
   if (s->A0f) b += n * sizeof(float);
