@@ -5,7 +5,8 @@
  * Every entry point replaces one mantaflow Python plugin or one member of the
  * classes those plugins take (paths relative to the mantaflow source tree).
  * A plugin translation unit of the reference (source/plugin/*.cpp) calls
- * these with the grids it receives; INTEGRATION.md shows that binding.
+ * these with the grids it receives, converting a non-zero status into the
+ * reference's errMsg with mg_last_error()'s text.
  *
  * Conventions
  *  - Every function returns MG_OK (0) or an MG_ERR_* code; mg_last_error()
@@ -78,6 +79,19 @@ int mg_solver_get_dt(mg_solver s, float* dt);
 int mg_solver_sync(mg_solver s);
 /* bytes of device memory held by the solver (grids, pool, solver state) */
 int mg_solver_memory(mg_solver s, size_t* bytes);
+/* No counterpart in the reference (its grids come from the host heap).  Caps
+ * the device memory the solver may hold: a grid creation or temporary grid
+ * that would take mg_solver_memory above `bytes` is refused with
+ * MG_ERR_NOMEM and the reference's out-of-memory text, leaving the solver
+ * usable.  0 (the default) removes the cap. */
+int mg_solver_set_memory_limit(mg_solver s, size_t bytes);
+/* No counterpart in the reference (its MIC(0) sweeps are serial loops).  The
+ * device-side waits of the MIC(0) wavefront sweeps give up after
+ * `limitNs` nanoseconds (default 200 ms; 0 restores it); the solve then
+ * returns MG_ERR_TIMEOUT instead of hanging.  With stallNextSolve != 0 the
+ * next MIC(0) solve's sweeps wait for tile words that no tile publishes, so
+ * its first wait runs out: a failure-path test that leaves the GPU usable. */
+int mg_solver_set_wait_limit(mg_solver s, long long limitNs, int stallNextSolve);
 
 /* ---- grids (source/grid.cpp) --------------------------------------------- */
 /* Grid<T>(parent): a zero-initialised grid (grid.cpp:48-58) */

@@ -69,6 +69,8 @@ SIGNATURES = [
     ("mg_solver_get_dt", _I, [_P, _FP]),
     ("mg_solver_sync", _I, [_P]),
     ("mg_solver_memory", _I, [_P, C.POINTER(C.c_size_t)]),
+    ("mg_solver_set_memory_limit", _I, [_P, C.c_size_t]),
+    ("mg_solver_set_wait_limit", _I, [_P, C.c_longlong, _I]),
     ("mg_grid_create", _I, [_P, _I, C.POINTER(_P)]),
     ("mg_grid_destroy", _I, [_P]),
     ("mg_grid_upload", _I, [_P, _P, C.c_size_t]),

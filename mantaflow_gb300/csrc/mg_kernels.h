@@ -142,11 +142,13 @@ int mic_wave_prepare(int* ctasPerSm4, int* ctasPerSm8);
 void launch_mic_wave(const PcgBuffers& b, const MicWavePlan& m, int mode, unsigned int epoch, long long spinLimit,
                      int ctas, cudaStream_t s);
 // tile-dataflow MIC sweeps (micflow.cu): the tiles of a MicPlan, faces
-// published as epoch-tagged words (face: mic_flow_face_words() words)
+// published as epoch-tagged words (face: mic_flow_face_words() words).
+// stall: the sweep waits for an epoch no tile publishes, so its first wait
+// runs out after spinLimit (the timeout path's test)
 int mic_flow_prepare(int* ctasPerSm);
 size_t mic_flow_face_words(int ntiles);
 void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* face, int mode, unsigned int epoch,
-                     long long spinLimit, cudaStream_t s);
+                     long long spinLimit, cudaStream_t s, bool stall = false);
 // sum of nparts per-block dot partials -> beta/sigma (init: sigma only)
 void launch_mic_finish(const PcgBuffers& b, int nparts, bool init, cudaStream_t s);
 

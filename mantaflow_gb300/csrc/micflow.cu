@@ -57,6 +57,7 @@ struct FlowArgs {
   int* error;
   unsigned long long* face;  // [ntiles][3][kT*kT]: downstream faces x, y, z
   unsigned int epoch;
+  unsigned int waitXor;  // 0; non-zero only to make every wait run out (failure-path tests)
   long long spinLimit;
 };
 
@@ -78,10 +79,12 @@ __device__ __forceinline__ unsigned long long make_word(float v, int code, unsig
 }
 __device__ __forceinline__ bool current(unsigned long long w, unsigned ep16) { return (unsigned)(w >> 48) == ep16; }
 
-// the word at p once it carries this sweep's epoch; gives up (and flags the
-// error) after `limit` nanoseconds or once another wait has given up
+// the word at p once it carries this sweep's epoch; gives up after `limit`
+// nanoseconds or once another wait has given up.  Giving up flags the error
+// and ends the CG (done), so the solve's later launches return at once and
+// the host reports the timeout.
 __device__ __noinline__ unsigned long long poll_word(const unsigned long long* p, unsigned ep16, long long limit,
-                                                    int* error) {
+                                                    int* error, CgScalars* sc) {
   unsigned long long v = ld_word(p);
   if (current(v, ep16)) return v;
   const unsigned long long t0 = ftimer();
@@ -89,7 +92,10 @@ __device__ __noinline__ unsigned long long poll_word(const unsigned long long* p
     v = ld_word(p);
     if (current(v, ep16)) return v;
     if ((n & 31) == 0 && (ftimer() - t0 > (unsigned long long)limit || *((volatile int*)error) != 0)) {
-      atomicExch(error, 6);
+      if (atomicExch(error, 6) == 0) {
+        sc->status = 3;
+        sc->done = 1;
+      }
       return v;
     }
   }
@@ -129,6 +135,7 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
   const int hw = (tid - 256) >> 5, hl = tid & 31;  // halo warp 0/1 and its lane
   if (MODE != 0 && a.sc->done) return;
   const unsigned ep16 = a.epoch & 0xffffu;
+  const unsigned wep16 = ep16 ^ a.waitXor;  // the epoch the fill words must carry
   auto gx = [&](int c, int n) { return MODE == 2 ? n - 1 - c : c; };  // global coordinate of a sweep coordinate
 
   for (;;) {
@@ -236,7 +243,7 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
           const int Lh = L + 1;  // fill what level L+1 reads
           if (fOK && Lh >= fLo && Lh < fHi) {
             unsigned long long w = q[u];
-            if (!current(w, ep16)) w = poll_word(fSrc + fSS * Lh, ep16, a.spinLimit, a.error);
+            if (!current(w, wep16)) w = poll_word(fSrc + fSS * Lh, wep16, a.spinLimit, a.error, a.sc);
             const int pe = fDst + fDS * Lh;
             s_n[pe] = __uint_as_float((unsigned)w);
             s_cp[pe] = (code_t)((w >> 32) & 0xffffu);
@@ -350,7 +357,7 @@ size_t mic_flow_face_words(int ntiles) { return (size_t)ntiles * 3 * kT * kT; }
 
 // mode: 0 factor, 1 forward, 2 backward (+beta), 3 backward for doInit (+sigma)
 void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* face, int mode, unsigned int epoch,
-                     long long spinLimit, cudaStream_t s) {
+                     long long spinLimit, cudaStream_t s, bool stall) {
   FlowArgs a;
   a.d = b.d;
   a.code = b.code;
@@ -369,6 +376,7 @@ void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* 
   a.error = m.error;
   a.face = face;
   a.epoch = epoch;
+  a.waitXor = stall ? 0x8000u : 0u;
   a.spinLimit = spinLimit;
   cudaMemsetAsync(m.counter, 0, sizeof(int), s);
   const int n = m.ctas < m.ntiles ? m.ctas : m.ntiles;

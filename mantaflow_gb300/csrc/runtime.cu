@@ -97,7 +97,8 @@ struct mg_solver_s {
   cudaStream_t copyStream[kMaxCopyStreams] = {};
   std::multimap<size_t, void*> pool;  // free device buffers by size
   std::set<mg_grid> grids;
-  size_t poolBytes = 0;
+  size_t poolBytes = 0;  // free buffers in the pool
+  size_t tmpBytes = 0;   // pool buffers handed out to temporaries
   // CG state (allocated on first solve)
   code_t* code = nullptr;
   float* A0f = nullptr;
@@ -120,6 +121,10 @@ struct mg_solver_s {
   unsigned long long* micFace = nullptr;  // tile-dataflow sweeps: face words
   bool useMicFlow = false;
   unsigned int epoch = 0;
+  long long waitNs = kWaitNs;  // limit of each device-side MIC wait
+  bool stallNext = false;      // the next MIC solve's waits run out (test of the timeout path)
+  bool stall = false;          // ... during this solve
+  size_t memLimit = 0;         // cap on the device memory the solver holds (0: none)
   mgpu::MgHierarchy* mg = nullptr;  // static multigrid cache (gMapMG)
   // one MG-PCG iteration captured as a CUDA graph, replayed while the
   // buffers and hierarchy it was captured with are unchanged
@@ -206,25 +211,43 @@ static void prof_collect(mg_solver s) {
 }
 
 // ------------------------------------------------------------------ pool
+// device bytes held by the solver: grids (and their staging copies), the
+// pool, CG state and the multigrid hierarchy
+static size_t held_bytes(mg_solver s) {
+  size_t b = s->poolBytes + s->tmpBytes;
+  for (auto g : s->grids) b += g->bytes() * (g->stage ? 2 : 1);
+  const size_t n = (size_t)s->d.n;
+  if (s->code) b += n * (sizeof(code_t) + 4 * sizeof(float));
+  if (s->A0f) b += n * sizeof(float);
+  if (s->mg) b += mg_hierarchy_bytes(s->mg);
+  return b;
+}
+// a new allocation of `bytes` would exceed the solver's memory cap
+static bool over_limit(mg_solver s, size_t bytes) { return s->memLimit && held_bytes(s) + bytes > s->memLimit; }
+
 static void* pool_get(mg_solver s, size_t bytes) {
   auto it = s->pool.find(bytes);
   if (it != s->pool.end()) {
     void* p = it->second;
     s->pool.erase(it);
     s->poolBytes -= bytes;
+    s->tmpBytes += bytes;
     return p;
   }
+  if (over_limit(s, bytes)) return nullptr;
   void* p = nullptr;
   if (cudaMalloc(&p, bytes) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }
+  s->tmpBytes += bytes;
   return p;
 }
 static void pool_put(mg_solver s, void* p, size_t bytes) {
   if (!p) return;
   s->pool.emplace(bytes, p);
   s->poolBytes += bytes;
+  s->tmpBytes -= bytes;
 }
 
 // RAII temp grid storage (FluidSolver::GridStorage, fluidsolver.cpp:33-50)
@@ -286,11 +309,13 @@ extern "C" int mg_init(int device) {
 }
 
 extern "C" int mg_solver_destroy(mg_solver s);
+static void noalloc_forget();
 
 extern "C" int mg_shutdown(void) {
   if (!g_ctx.init) return MG_OK;
   std::vector<mg_solver> all(g_ctx.solvers.begin(), g_ctx.solvers.end());
   for (auto s : all) mg_solver_destroy(s);
+  noalloc_forget();
   g_ctx.init = false;
   g_ctx.device = -1;
   return MG_OK;
@@ -411,13 +436,20 @@ extern "C" int mg_solver_sync(mg_solver s) {
 }
 extern "C" int mg_solver_memory(mg_solver s, size_t* bytes) {
   if (!valid_solver(s) || !bytes) return fail(MG_ERR_ARG, "mg_solver_memory: invalid argument");
-  size_t b = s->poolBytes;
-  for (auto g : s->grids) b += g->bytes() * (g->stage ? 2 : 1);  // + the staging copy of asynchronous transfers
-  const size_t n = (size_t)s->d.n;
-  if (s->code) b += n * (sizeof(code_t) + 4 * sizeof(float));
-  if (s->A0f) b += n * sizeof(float);
-  if (s->mg) b += mg_hierarchy_bytes(s->mg);
-  *bytes = b;
+  *bytes = held_bytes(s);
+  return MG_OK;
+}
+
+extern "C" int mg_solver_set_memory_limit(mg_solver s, size_t bytes) {
+  if (!valid_solver(s)) return fail(MG_ERR_ARG, "mg_solver_set_memory_limit: invalid solver");
+  s->memLimit = bytes;
+  return MG_OK;
+}
+
+extern "C" int mg_solver_set_wait_limit(mg_solver s, long long limitNs, int stallNextSolve) {
+  if (!valid_solver(s) || limitNs < 0) return fail(MG_ERR_ARG, "mg_solver_set_wait_limit: invalid argument");
+  s->waitNs = limitNs ? limitNs : kWaitNs;
+  s->stallNext = stallNextSolve != 0;
   return MG_OK;
 }
 
@@ -429,6 +461,10 @@ extern "C" int mg_grid_create(mg_solver s, int kind, mg_grid* out) {
   g->s = s;
   g->kind = kind;
   const size_t bytes = g->bytes();
+  if (over_limit(s, bytes)) {
+    delete g;
+    return fail(MG_ERR_NOMEM, "mg_grid_create: the solver's memory limit is reached");
+  }
   if (cudaMalloc(&g->data, bytes) != cudaSuccess) {
     cudaGetLastError();
     delete g;
@@ -695,6 +731,7 @@ extern "C" int mg_advect_semi_lagrange(mg_grid flags, mg_grid vel, mg_grid grid,
     const float ts = (float)std::max(1.0, (double)dt * 4);
     if (order == 1) {
       Tmp dst(s, bytes);
+      if (!dst.p) return fail(MG_ERR_NOMEM, "advectSemiLagrange: out of device memory");
       {
         ProfScope ps(s, "advect_outflow");
         launch_outflow_bc(d, flags->i(), fwd.cmac(), grid->cmac(), dst.mac(), fwd.mac(), ts, s->stream);
@@ -759,6 +796,12 @@ extern "C" int mg_advect_semi_lagrange(mg_grid flags, mg_grid vel, mg_grid grid,
 constexpr size_t kNoAllocSlotFloats = (size_t)3 << 20;
 static __device__ __align__(256) float g_noallocScratch[2 * kNoAllocSlotFloats];
 static float* g_noallocPtr[64] = {};  // per device ordinal, set on first use
+
+// mg_shutdown forgets the resolved addresses: a host may reset the device
+// before the next mg_init, after which the module (and the array) reload
+static void noalloc_forget() {
+  for (auto& p : g_noallocPtr) p = nullptr;
+}
 
 // Resolves the array's device address for the current device.  Runs once per
 // device, on the first call, which should therefore come before any stream
@@ -1137,18 +1180,18 @@ static int apply_precond(mg_solver s, const PcgBuffers& b, int pc, bool init) {
   if (pc == kPcMic) {
     {
       ProfScope ps(s, "mic_forward");
-      if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 1, ++s->epoch, kWaitNs, s->stream);
-      else if (s->useMicWave) launch_mic_wave(b, s->micWave, 1, ++s->epoch, kWaitNs, wave_ctas(s), s->stream);
-      else if (s->useMicCol) launch_mic_col(b, s->micCol, 1, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
-      else launch_mic(b, s->mic, 1, ++s->epoch, kWaitNs, s->stream);
+      if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 1, ++s->epoch, s->waitNs, s->stream, s->stall);
+      else if (s->useMicWave) launch_mic_wave(b, s->micWave, 1, ++s->epoch, s->waitNs, wave_ctas(s), s->stream);
+      else if (s->useMicCol) launch_mic_col(b, s->micCol, 1, ++s->epoch, s->waitNs, g_ctx.sms, s->stream);
+      else launch_mic(b, s->mic, 1, ++s->epoch, s->waitNs, s->stream);
     }
     {
       ProfScope ps(s, "mic_backward");
-      if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, init ? 3 : 2, ++s->epoch, kWaitNs, s->stream);
+      if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, init ? 3 : 2, ++s->epoch, s->waitNs, s->stream, s->stall);
       else if (s->useMicWave)
-        launch_mic_wave(b, s->micWave, init ? 3 : 2, ++s->epoch, kWaitNs, wave_ctas(s), s->stream);
-      else if (s->useMicCol) launch_mic_col(b, s->micCol, init ? 3 : 2, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
-      else launch_mic(b, s->mic, init ? 3 : 2, ++s->epoch, kWaitNs, s->stream);
+        launch_mic_wave(b, s->micWave, init ? 3 : 2, ++s->epoch, s->waitNs, wave_ctas(s), s->stream);
+      else if (s->useMicCol) launch_mic_col(b, s->micCol, init ? 3 : 2, ++s->epoch, s->waitNs, g_ctx.sms, s->stream);
+      else launch_mic(b, s->mic, init ? 3 : 2, ++s->epoch, s->waitNs, s->stream);
     }
   } else if (pc == kPcMg) {
     mg_set_profiler(s->mg, s->prof ? mg_prof_hook : nullptr, s);
@@ -1295,11 +1338,13 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   CKL();
   if (pc == kPcMic) {
     ProfScope ps(s, "mic_init");
+    s->stall = s->stallNext;
+    s->stallNext = false;
     CK(cudaMemsetAsync(s->mic.error, 0, sizeof(int), s->stream));
-    if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 0, ++s->epoch, kWaitNs, s->stream);
-    else if (s->useMicWave) launch_mic_wave(b, s->micWave, 0, ++s->epoch, kWaitNs, wave_ctas(s), s->stream);
-    else if (s->useMicCol) launch_mic_col(b, s->micCol, 0, ++s->epoch, kWaitNs, g_ctx.sms, s->stream);
-    else launch_mic(b, s->mic, 0, ++s->epoch, kWaitNs, s->stream);
+    if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 0, ++s->epoch, s->waitNs, s->stream, s->stall);
+    else if (s->useMicWave) launch_mic_wave(b, s->micWave, 0, ++s->epoch, s->waitNs, wave_ctas(s), s->stream);
+    else if (s->useMicCol) launch_mic_col(b, s->micCol, 0, ++s->epoch, s->waitNs, g_ctx.sms, s->stream);
+    else launch_mic(b, s->mic, 0, ++s->epoch, s->waitNs, s->stream);
     CKL();
   }
   if (pc != kPcNone) {
@@ -1315,8 +1360,10 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   }
   CKL();
   // GridCg::iterate until converged or maxIter; the host polls the device
-  // flag a few iterations behind so the GPU never waits for the CPU
-  const int lag = 4;
+  // flag a few iterations behind so the GPU never waits for the CPU.  While
+  // profiling it polls every iteration, so that every launch it times did
+  // work (launches after convergence return at once)
+  const int lag = s->prof ? 1 : 4;
   std::vector<cudaEvent_t> ev;
   int it = 0;
   bool done = false;
@@ -1348,6 +1395,18 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
       ProfScope ps(s, "pcg_axpy");
       launch_pcg_axpy(b, s->stream);
     }
+    if (s->prof) {
+      // the axpy's residual norm may have converged the solve, after which
+      // the iteration's remaining launches would return at once: leave them
+      // out, so the profile times only launches that did work
+      CKL();
+      CK(cudaMemcpyAsync(s->scHost, s->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s->stream));
+      CK(cudaStreamSynchronize(s->stream));
+      if (s->scHost->done) {
+        it++;
+        break;
+      }
+    }
     st = apply_precond(s, b, pc, false);
     if (st) return st;
     {
@@ -1365,6 +1424,7 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   CK(cudaMemcpyAsync(s->scHost, s->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   if (pc == kPcMic) {
+    s->stall = false;
     int err = 0;
     CK(cudaMemcpy(&err, s->mic.error, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) return fail(MG_ERR_TIMEOUT, "MIC wavefront: a tile wait exceeded its spin limit");

@@ -154,6 +154,16 @@ class Solver:
         check(_lib.load().mg_solver_memory(self._h, C.byref(v)))
         return int(v.value)
 
+    def setMemoryLimit(self, nbytes):
+        """Cap the device memory this solver may hold (0: no cap)."""
+        check(_lib.load().mg_solver_set_memory_limit(self._h, int(nbytes)))
+
+    def setWaitLimit(self, ns, stallNextSolve=False):
+        """Limit of each device-side MIC(0) wavefront wait in nanoseconds (0:
+        the default 200 ms).  stallNextSolve makes the next MIC(0) solve's
+        waits run out, to exercise the timeout path."""
+        check(_lib.load().mg_solver_set_wait_limit(self._h, int(ns), 1 if stallNextSolve else 0))
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and _lib._lib is not None:
