@@ -198,17 +198,31 @@ __global__ void __launch_bounds__(256) k_maccormack_cell(Dims d, const int* __re
 }
 
 // ------------------------------------------------------------------- MAC SL
+// MACGrid::getInterpolatedComponentHi<c> (grid.h:268-274): orderSpace 1 is
+// trilinear on the component's plane; orderSpace 2 is interpolCubicMAC's
+// component (interpolHigh.h:171-178), the Vec3 Catmull-Rom sample half a
+// cell further along the component's axis (0 for z in 2D).
+template <int kOS>
+__device__ __forceinline__ float sample_mac_comp(const Dims& d, const float* __restrict__ plane, int c, float x, float y,
+                                                 float z) {
+  if (kOS == 1) return interp(d, plane, x, y, z);
+  if (c == 0) return interp_cubic<true>(d, plane, x + 0.5f, y, z);
+  if (c == 1) return interp_cubic<true>(d, plane, x, y + 0.5f, z);
+  if (!d.is3d) return 0.f;
+  return interp_cubic<true>(d, plane, x, y, z + 0.5f);
+}
+
 // SemiLagrangeMAC (advection.cpp:44-77), src sampled per component.
-template <int kTrace>
+template <int kTrace, int kOS>
 __device__ __forceinline__ void sl_mac_cell(const Dims& d, CMac vel, CMac src, int i, int j, int k, float dt, float* out) {
   const long long idx = ix(d, i, j, k);
   if (kTrace == 1) {
     const V3 ax = mac_at_x(d, vel, idx);
-    out[0] = interp(d, src.u, (i + 0.5f) - ax.x * dt, (j + 0.5f) - ax.y * dt, (k + 0.5f) - ax.z * dt);
+    out[0] = sample_mac_comp<kOS>(d, src.u, 0, (i + 0.5f) - ax.x * dt, (j + 0.5f) - ax.y * dt, (k + 0.5f) - ax.z * dt);
     const V3 ay = mac_at_y(d, vel, idx);
-    out[1] = interp(d, src.v, (i + 0.5f) - ay.x * dt, (j + 0.5f) - ay.y * dt, (k + 0.5f) - ay.z * dt);
+    out[1] = sample_mac_comp<kOS>(d, src.v, 1, (i + 0.5f) - ay.x * dt, (j + 0.5f) - ay.y * dt, (k + 0.5f) - ay.z * dt);
     const V3 az = mac_at_z(d, vel, idx);
-    out[2] = interp(d, src.w, (i + 0.5f) - az.x * dt, (j + 0.5f) - az.y * dt, (k + 0.5f) - az.z * dt);
+    out[2] = sample_mac_comp<kOS>(d, src.w, 2, (i + 0.5f) - az.x * dt, (j + 0.5f) - az.y * dt, (k + 0.5f) - az.z * dt);
   } else {
     // the midpoint trace samples src, as the reference does
     const float p0x = i + 0.5f, p0y = j + 0.5f, p0z = k + 0.5f;
@@ -219,29 +233,29 @@ __device__ __forceinline__ void sl_mac_cell(const Dims& d, CMac vel, CMac src, i
       const float qz = c == 2 ? (float)k : k + 0.5f;
       const V3 a = c == 0 ? mac_at_x(d, src, idx) : (c == 1 ? mac_at_y(d, src, idx) : mac_at_z(d, src, idx));
       const V3 vi = interp_mac(d, src, qx - (a.x * dt) * 0.5f, qy - (a.y * dt) * 0.5f, qz - (a.z * dt) * 0.5f);
-      out[c] = interp(d, src.c(c), p0x - vi.x * dt, p0y - vi.y * dt, p0z - vi.z * dt);
+      out[c] = sample_mac_comp<kOS>(d, src.c(c), c, p0x - vi.x * dt, p0y - vi.y * dt, p0z - vi.z * dt);
     }
   }
 }
 
-template <int kTrace>
+template <int kTrace, int kOS>
 __device__ __forceinline__ void sl_mac_grid_cell(const Dims& d, CMac vel, CMac src, Mac dst, float dt, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   const bool inner = i >= 1 && i < d.nx - 1 && j >= 1 && j < d.ny - 1 && (!d.is3d || (k >= 1 && k < d.nz - 1));
   float out[3] = {0.f, 0.f, 0.f};
-  if (inner) sl_mac_cell<kTrace>(d, vel, src, i, j, k, dt, out);
+  if (inner) sl_mac_cell<kTrace, kOS>(d, vel, src, i, j, k, dt, out);
   dst.u[idx] = out[0];
   dst.v[idx] = out[1];
   dst.w[idx] = out[2];
 }
 
-template <int kTrace>
+template <int kTrace, int kOS>
 __global__ void __launch_bounds__(256) k_sl_mac(Dims d, CMac vel, CMac src, Mac dst, float dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= d.nx || j >= d.ny) return;
-  sl_mac_grid_cell<kTrace>(d, vel, src, dst, dt, i, j, k);
+  sl_mac_grid_cell<kTrace, kOS>(d, vel, src, dst, dt, i, j, k);
 }
 
 // doClampComponentMAC (advection.cpp:191-235)
@@ -282,7 +296,7 @@ __device__ __forceinline__ float clamp_component_mac(const Dims& d, int fo, int 
 
 // bwd = SLMAC(fwd, -dt) on the fly, MacCormackCorrectMAC (advection.cpp:94-115),
 // MacCormackClampMAC (:270-287).  orig is the grid being advected.
-template <int kTrace>
+template <int kTrace, int kOS>
 __device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __restrict__ flags, CMac vel, CMac orig,
                                                         CMac fwd, Mac dst, float dt, float strength, int clampMode, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
@@ -307,11 +321,11 @@ __device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __
     if (kTrace == 1) {
       // SemiLagrangeMAC(fwd, -dt), as sl_mac_cell<1> forms it
       const float mdt = -dt;
-      bwd[0] = interp(d, fwd.u, (i + 0.5f) - ax.x * mdt, (j + 0.5f) - ax.y * mdt, (k + 0.5f) - ax.z * mdt);
-      bwd[1] = interp(d, fwd.v, (i + 0.5f) - ay.x * mdt, (j + 0.5f) - ay.y * mdt, (k + 0.5f) - ay.z * mdt);
-      bwd[2] = interp(d, fwd.w, (i + 0.5f) - az.x * mdt, (j + 0.5f) - az.y * mdt, (k + 0.5f) - az.z * mdt);
+      bwd[0] = sample_mac_comp<kOS>(d, fwd.u, 0, (i + 0.5f) - ax.x * mdt, (j + 0.5f) - ax.y * mdt, (k + 0.5f) - ax.z * mdt);
+      bwd[1] = sample_mac_comp<kOS>(d, fwd.v, 1, (i + 0.5f) - ay.x * mdt, (j + 0.5f) - ay.y * mdt, (k + 0.5f) - ay.z * mdt);
+      bwd[2] = sample_mac_comp<kOS>(d, fwd.w, 2, (i + 0.5f) - az.x * mdt, (j + 0.5f) - az.y * mdt, (k + 0.5f) - az.z * mdt);
     } else {
-      sl_mac_cell<kTrace>(d, vel, fwd, i, j, k, -dt, bwd);
+      sl_mac_cell<kTrace, kOS>(d, vel, fwd, i, j, k, -dt, bwd);
     }
   }
   float fw[3], val[3];
@@ -331,14 +345,14 @@ __device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __
   dst.w[idx] = val[2];
 }
 
-template <int kTrace>
+template <int kTrace, int kOS>
 __global__ void __launch_bounds__(256) k_maccormack_mac(Dims d, const int* __restrict__ flags, CMac vel, CMac orig,
                                                         CMac fwd, Mac dst, float dt, float strength, int clampMode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= d.nx || j >= d.ny) return;
-  maccormack_mac_cell<kTrace>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode, i, j, k);
+  maccormack_mac_cell<kTrace, kOS>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode, i, j, k);
 }
 
 // extrapolateVelConvectiveBC (advection.cpp:346-381): velDst for outflow
@@ -461,14 +475,14 @@ __global__ void __launch_bounds__(256) k_b_advect_fwd(const BTile* __restrict__ 
   BATCH_CELL
   const CMac v = bcmac(sc.vel[cur], d.n);
   sl_real_cell<1, 1, 1>(d, v, sc.dens[cur], sc.fwd + 3 * d.n, sc.dt, i, j, k);
-  sl_mac_grid_cell<1>(d, v, v, bmac(sc.fwd, d.n), sc.dt, i, j, k);
+  sl_mac_grid_cell<1, 1>(d, v, v, bmac(sc.fwd, d.n), sc.dt, i, j, k);
 }
 // MacCormack correction and clamp of both into the next buffers
 __global__ void __launch_bounds__(256) k_b_advect_mc(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
   BATCH_CELL
   const CMac v = bcmac(sc.vel[cur], d.n);
   maccormack_real_cell<1, 1, 1>(d, sc.flags, v, sc.dens[cur], sc.fwd + 3 * d.n, sc.dens[1 - cur], sc.dt, 1.f, 2, i, j, k);
-  maccormack_mac_cell<1>(d, sc.flags, v, v, bcmac(sc.fwd, d.n), bmac(sc.vel[1 - cur], d.n), sc.dt, 1.f, 2, i, j, k);
+  maccormack_mac_cell<1, 1>(d, sc.flags, v, v, bcmac(sc.fwd, d.n), bmac(sc.vel[1 - cur], d.n), sc.dt, 1.f, 2, i, j, k);
 }
 // applyOutflowBC (advection.cpp:387-391): convective values into the scratch
 __global__ void __launch_bounds__(256) k_b_outflow(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
@@ -541,18 +555,30 @@ void launch_advect_maccormack(const Dims& d, int ch, const int* flags, CMac vel,
   else dispatch_mc<3>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode, orderSpace, orderTrace, s);
 }
 
-void launch_advect_sl_mac(const Dims& d, CMac vel, CMac src, Mac dst, float dt, int orderTrace, cudaStream_t s) {
-  if (orderTrace == 1) { count_launch(); k_sl_mac<1><<<grid3(d, kBlk), kBlk, 0, s>>>(d, vel, src, dst, dt); }
-  else { count_launch(); k_sl_mac<2><<<grid3(d, kBlk), kBlk, 0, s>>>(d, vel, src, dst, dt); }
+void launch_advect_sl_mac(const Dims& d, CMac vel, CMac src, Mac dst, float dt, int orderSpace, int orderTrace,
+                         cudaStream_t s) {
+  count_launch();
+  const dim3 g = grid3(d, kBlk);
+  if (orderSpace == 1) {
+    if (orderTrace == 1) k_sl_mac<1, 1><<<g, kBlk, 0, s>>>(d, vel, src, dst, dt);
+    else k_sl_mac<2, 1><<<g, kBlk, 0, s>>>(d, vel, src, dst, dt);
+  } else {
+    if (orderTrace == 1) k_sl_mac<1, 2><<<g, kBlk, 0, s>>>(d, vel, src, dst, dt);
+    else k_sl_mac<2, 2><<<g, kBlk, 0, s>>>(d, vel, src, dst, dt);
+  }
 }
 
 void launch_advect_maccormack_mac(const Dims& d, const int* flags, CMac vel, CMac orig, CMac fwd, Mac dst, float dt,
-                                  float strength, int clampMode, int orderTrace, cudaStream_t s) {
+                                  float strength, int clampMode, int orderSpace, int orderTrace, cudaStream_t s) {
   count_launch();
-  if (orderTrace == 1)
-    k_maccormack_mac<1><<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode);
-  else
-    k_maccormack_mac<2><<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode);
+  const dim3 g = grid3(d, kBlk);
+  if (orderSpace == 1) {
+    if (orderTrace == 1) k_maccormack_mac<1, 1><<<g, kBlk, 0, s>>>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode);
+    else k_maccormack_mac<2, 1><<<g, kBlk, 0, s>>>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode);
+  } else {
+    if (orderTrace == 1) k_maccormack_mac<1, 2><<<g, kBlk, 0, s>>>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode);
+    else k_maccormack_mac<2, 2><<<g, kBlk, 0, s>>>(d, flags, vel, orig, fwd, dst, dt, strength, clampMode);
+  }
 }
 
 void launch_outflow_bc(const Dims& d, const int* flags, CMac vel, CMac velPrev, Mac velDst, Mac velOut, float timeStep,

@@ -17,9 +17,10 @@ void launch_advect_sl(const Dims& d, int ch, CMac vel, const float* src, float* 
 void launch_advect_maccormack(const Dims& d, int ch, const int* flags, CMac vel, const float* orig, const float* fwd,
                               float* dst, float dt, float strength, int clampMode, int orderSpace, int orderTrace,
                               cudaStream_t s);
-void launch_advect_sl_mac(const Dims& d, CMac vel, CMac src, Mac dst, float dt, int orderTrace, cudaStream_t s);
+void launch_advect_sl_mac(const Dims& d, CMac vel, CMac src, Mac dst, float dt, int orderSpace, int orderTrace,
+                         cudaStream_t s);
 void launch_advect_maccormack_mac(const Dims& d, const int* flags, CMac vel, CMac orig, CMac fwd, Mac dst, float dt,
-                                  float strength, int clampMode, int orderTrace, cudaStream_t s);
+                                  float strength, int clampMode, int orderSpace, int orderTrace, cudaStream_t s);
 void launch_outflow_bc(const Dims& d, const int* flags, CMac vel, CMac velPrev, Mac velDst, Mac velOut, float timeStep,
                        cudaStream_t s);
 void launch_reset_phi_in_obs(const Dims& d, const int* flags, float* sdf, cudaStream_t s);
@@ -149,6 +150,9 @@ int mic_flow_prepare(int* ctasPerSm);
 size_t mic_flow_face_words(int ntiles);
 void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* face, int mode, unsigned int epoch,
                      long long spinLimit, cudaStream_t s, bool stall = false);
+// once per device: the streamed SpMV's shared-memory size (MANTAGPU_SPMV=quad
+// selects the per-quad gather kernel instead)
+int pcg_prepare(int sms);
 // sum of nparts per-block dot partials -> beta/sigma (init: sigma only)
 void launch_mic_finish(const PcgBuffers& b, int nparts, bool init, cudaStream_t s);
 

@@ -19,11 +19,14 @@
 //    the serial loop would, so the result is the reference's bit for bit.
 #include "mg_common.cuh"
 #include "mg_kernels.h"
+#include "mg_tma.cuh"
 #include "mg_reduce.cuh"
 #include "mg_batch.h"
 
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
+#include <string>
 
 namespace mgpu {
 
@@ -388,48 +391,85 @@ __global__ void k_pcg_update(long long n, const float* __restrict__ t, float* s,
 // the same float operations as the scalar kernels above.
 __device__ __forceinline__ float fget(const float4& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
 
-__global__ void __launch_bounds__(256) k_pcg_spmv4(Dims d, const code_t* __restrict__ code,
+// The inputs of one quad (four x-consecutive cells): its stencil codes, x
+// at the quad and its four y/z neighbour quads, and the x neighbours of its
+// end cells.  Loaded before any arithmetic so that a thread keeps two quads'
+// loads in flight.
+struct SpmvQuad {
+  uint2 cw;
+  float4 xc, ylo, yhi, zlo, zhi, A0;
+  float xl, xr;
+};
+
+__device__ __forceinline__ void spmv_load(const Dims& d, const code_t* __restrict__ code, const float* __restrict__ A0f,
+                                          const float* __restrict__ x, long long q, SpmvQuad& Q) {
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  Q.cw = __ldg(reinterpret_cast<const uint2*>(code) + q);
+  const int any = (int)((Q.cw.x | Q.cw.y | (Q.cw.x >> 16) | (Q.cw.y >> 16)) & 0xffffu);
+  Q.xc = __ldg(x4 + q);
+  Q.ylo = (any & kLowY) ? __ldg(x4 + q - (d.sy >> 2)) : z4;
+  Q.yhi = (any & kHighY) ? __ldg(x4 + q + (d.sy >> 2)) : z4;
+  Q.zlo = (any & kLowZ) ? __ldg(x4 + q - (d.sz >> 2)) : z4;
+  Q.zhi = (any & kHighZ) ? __ldg(x4 + q + (d.sz >> 2)) : z4;
+  Q.xl = (Q.cw.x & kLowX) ? __ldg(x + (q << 2) - 1) : 0.f;
+  Q.xr = ((Q.cw.y >> 16) & kHighX) ? __ldg(x + (q << 2) + 4) : 0.f;
+  if (A0f) Q.A0 = __ldg(reinterpret_cast<const float4*>(A0f) + q);
+  else
+    Q.A0 = make_float4((float)(Q.cw.x & 7), (float)((Q.cw.x >> 16) & 7), (float)(Q.cw.y & 7),
+                       (float)((Q.cw.y >> 16) & 7));
+}
+
+// ApplyMatrix (conjugategrad.h:118-151) on one quad, and its part of the
+// fused dot(y, x)
+__device__ __forceinline__ float4 spmv_apply(const SpmvQuad& Q, FSum& acc) {
+  const int c[4] = {(int)(Q.cw.x & 0xffffu), (int)(Q.cw.x >> 16), (int)(Q.cw.y & 0xffffu), (int)(Q.cw.y >> 16)};
+  float out[4];
+#pragma unroll
+  for (int e = 0; e < 4; e++) {
+    const int ce = c[e];
+    const float xv = fget(Q.xc, e);
+    float v;
+    if (!(ce & kCodeFluid)) {
+      v = xv;
+    } else {
+      v = xv * fget(Q.A0, e);
+      if (ce & kLowX) v = v - (e == 0 ? Q.xl : fget(Q.xc, e - 1));
+      if (ce & kHighX) v = v - (e == 3 ? Q.xr : fget(Q.xc, e + 1));
+      if (ce & kLowY) v = v - fget(Q.ylo, e);
+      if (ce & kHighY) v = v - fget(Q.yhi, e);
+      if (ce & kLowZ) v = v - fget(Q.zlo, e);
+      if (ce & kHighZ) v = v - fget(Q.zhi, e);
+    }
+    out[e] = v;
+    acc.add(v * xv);
+  }
+  return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// A thread takes the quads q, q + stride, q + 2 stride, ... two per loop
+// trip, in that order (the dot's summation order does not depend on the
+// pairing).
+__global__ void __launch_bounds__(256, 4) k_pcg_spmv4(Dims d, const code_t* __restrict__ code,
                                                    const float* __restrict__ A0f, const float* __restrict__ x,
                                                    float* y, double* part, CgScalars* sc) {
   if (sc->done) return;
   FSum acc;
   const long long nq = d.n >> 2;
-  const float4* x4 = reinterpret_cast<const float4*>(x);
-  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
-    const long long idx = q << 2;
-    const uint2 cw = __ldg(reinterpret_cast<const uint2*>(code) + q);
-    const int c[4] = {(int)(cw.x & 0xffffu), (int)(cw.x >> 16), (int)(cw.y & 0xffffu), (int)(cw.y >> 16)};
-    const int any = c[0] | c[1] | c[2] | c[3];
-    const float4 xc = __ldg(x4 + q);
-    const float4 ylo = (any & kLowY) ? __ldg(x4 + q - (d.sy >> 2)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 yhi = (any & kHighY) ? __ldg(x4 + q + (d.sy >> 2)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 zlo = (any & kLowZ) ? __ldg(x4 + q - (d.sz >> 2)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 zhi = (any & kHighZ) ? __ldg(x4 + q + (d.sz >> 2)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float xl = (c[0] & kLowX) ? __ldg(x + idx - 1) : 0.f;
-    const float xr = (c[3] & kHighX) ? __ldg(x + idx + 4) : 0.f;
-    float4 A0 = make_float4((float)(c[0] & 7), (float)(c[1] & 7), (float)(c[2] & 7), (float)(c[3] & 7));
-    if (A0f) A0 = __ldg(reinterpret_cast<const float4*>(A0f) + q);
-    float out[4];
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      const int ce = c[e];
-      const float xv = fget(xc, e);
-      float v;
-      if (!(ce & kCodeFluid)) {
-        v = xv;
-      } else {
-        v = xv * fget(A0, e);
-        if (ce & kLowX) v = v - (e == 0 ? xl : fget(xc, e - 1));
-        if (ce & kHighX) v = v - (e == 3 ? xr : fget(xc, e + 1));
-        if (ce & kLowY) v = v - fget(ylo, e);
-        if (ce & kHighY) v = v - fget(yhi, e);
-        if (ce & kLowZ) v = v - fget(zlo, e);
-        if (ce & kHighZ) v = v - fget(zhi, e);
-      }
-      out[e] = v;
-      acc.add(v * xv);
-    }
-    reinterpret_cast<float4*>(y)[q] = make_float4(out[0], out[1], out[2], out[3]);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  float4* y4 = reinterpret_cast<float4*>(y);
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; q + stride < nq; q += 2 * stride) {
+    SpmvQuad Q0, Q1;
+    spmv_load(d, code, A0f, x, q, Q0);
+    spmv_load(d, code, A0f, x, q + stride, Q1);
+    y4[q] = spmv_apply(Q0, acc);
+    y4[q + stride] = spmv_apply(Q1, acc);
+  }
+  if (q < nq) {
+    SpmvQuad Q0;
+    spmv_load(d, code, A0f, x, q, Q0);
+    y4[q] = spmv_apply(Q0, acc);
   }
   const double b = block_sum(acc.value());
   if (threadIdx.x == 0) part[blockIdx.x] = b;
@@ -443,6 +483,167 @@ __global__ void __launch_bounds__(256) k_pcg_spmv4(Dims d, const code_t* __restr
       sc->alpha = alpha;
     }
   }
+}
+
+// ---- the same SpMV streamed plane by plane through shared memory.  A CTA
+// owns a slab of TY full-width rows and a run of z planes.  Its ring of
+// kStreamSlots planes is filled by bulk asynchronous copies (one copy of the
+// slab's rows plus their y halo per plane, one of the plane's stencil codes),
+// completed on one mbarrier per slot; while plane z is computed from planes
+// z-1, z and z+1, plane z+2 is on its way.  x is read from DRAM once per
+// plane (the y halo rows come from L2), and no neighbour is re-read from L2
+// by a gather.  Same cell arithmetic as k_pcg_spmv4.
+constexpr int kStreamSlots = 4;
+constexpr int kStreamSlotBudget = 16384;         // bytes of one ring slot at most
+constexpr long long kStreamWaitNs = 100000000LL;  // bound of one copy wait
+
+struct StreamGeom {
+  int TY, zc;                  // rows per slab, planes per CTA
+  unsigned slotBytes, xBytes;  // ring slot size, offset of the code rows in a slot
+};
+
+__global__ void __launch_bounds__(256, 3) k_pcg_spmv_stream(Dims d, StreamGeom g, const code_t* __restrict__ code,
+                                                           const float* __restrict__ A0f, const float* __restrict__ x,
+                                                           float* y, double* part, CgScalars* sc) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bars[kStreamSlots];
+  if (sc->done) return;
+  const int nx = d.nx;
+  const int y0 = blockIdx.x * g.TY, ty = min(g.TY, d.ny - y0);
+  const int ya = max(y0 - 1, 0), yb = min(y0 + g.TY + 1, d.ny);
+  const int zs = blockIdx.y * g.zc, ze = min(zs + g.zc, d.nz);
+  const int p0 = zs - 1;        // plane of ring index 0
+  const int np = ze + 1 - p0;   // ring indices 0 .. np-1: planes zs-1 .. ze
+  const long long sz = d.sz;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < kStreamSlots; k++) mbar_init(&bars[k]);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto slotX = [&](int i) { return reinterpret_cast<float*>(smem + (size_t)(i % kStreamSlots) * g.slotBytes); };
+  auto slotC = [&](int i) {
+    return reinterpret_cast<const code_t*>(smem + (size_t)(i % kStreamSlots) * g.slotBytes + g.xBytes);
+  };
+  // thread 0: fill the slot of ring index i (planes outside the grid only
+  // complete the slot's phase)
+  auto issue = [&](int i) {
+    const int p = p0 + i;
+    uint64_t* bar = &bars[i % kStreamSlots];
+    if (p < 0 || p >= d.nz) {
+      mbar_arrive_expect(bar, 0);
+      return;
+    }
+    const unsigned xb = (unsigned)((yb - ya) * nx) * 4u;
+    const bool withCode = p >= zs && p < ze;
+    const unsigned cb = withCode ? (unsigned)(ty * nx) * 2u : 0u;
+    mbar_arrive_expect(bar, xb + cb);
+    bulk_g2s(slotX(i), x + p * sz + (long long)ya * nx, xb, bar);
+    if (withCode) bulk_g2s(smem + (size_t)(i % kStreamSlots) * g.slotBytes + g.xBytes, code + p * sz + (long long)y0 * nx, cb, bar);
+  };
+  int issued = 0;
+  if (threadIdx.x == 0)
+    for (; issued < kStreamSlots && issued < np; issued++) issue(issued);
+  const int nq4 = nx >> 2, quads = ty * nq4;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4* A4 = reinterpret_cast<const float4*>(A0f);
+  float4* y4 = reinterpret_cast<float4*>(y);
+  FSum acc;
+  bool ok = true;
+  int waited = 0;  // ring indices below this one have been waited for
+  for (int z = zs; z < ze && ok; z++) {
+    const int ic = z - p0;
+    for (; waited <= ic + 1; waited++)
+      if (!mbar_wait(&bars[waited % kStreamSlots], (unsigned)(waited / kStreamSlots) & 1u, kStreamWaitNs)) ok = false;
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    const float* xm = slotX(ic - 1);
+    const float* xcen = slotX(ic);
+    const float* xp = slotX(ic + 1);
+    const code_t* cs = slotC(ic);
+    for (int e = threadIdx.x; e < quads; e += blockDim.x) {
+      const int r = e / nq4, xq = e - r * nq4;
+      const int yy = y0 + r;
+      const int ro = (yy - ya) * nx + 4 * xq;  // the quad in the slot's x rows
+      SpmvQuad Q;
+      Q.cw = *reinterpret_cast<const uint2*>(cs + r * nx + 4 * xq);
+      const int any = (int)((Q.cw.x | Q.cw.y | (Q.cw.x >> 16) | (Q.cw.y >> 16)) & 0xffffu);
+      Q.xc = *reinterpret_cast<const float4*>(xcen + ro);
+      Q.ylo = (any & kLowY) ? *reinterpret_cast<const float4*>(xcen + ro - nx) : z4;
+      Q.yhi = (any & kHighY) ? *reinterpret_cast<const float4*>(xcen + ro + nx) : z4;
+      Q.zlo = (any & kLowZ) ? *reinterpret_cast<const float4*>(xm + ro) : z4;
+      Q.zhi = (any & kHighZ) ? *reinterpret_cast<const float4*>(xp + ro) : z4;
+      Q.xl = (Q.cw.x & kLowX) ? xcen[ro - 1] : 0.f;
+      Q.xr = ((Q.cw.y >> 16) & kHighX) ? xcen[ro + 4] : 0.f;
+      const long long q = ((long long)z * sz + (long long)yy * nx) / 4 + xq;
+      if (A0f) Q.A0 = __ldg(A4 + q);
+      else
+        Q.A0 = make_float4((float)(Q.cw.x & 7), (float)((Q.cw.x >> 16) & 7), (float)(Q.cw.y & 7),
+                           (float)((Q.cw.y >> 16) & 7));
+      y4[q] = spmv_apply(Q, acc);
+    }
+    __syncthreads();  // the slot of plane z-1 is read for the last time
+    if (threadIdx.x == 0 && issued < np) issue(issued++);
+  }
+  if (!ok) {
+    // a copy wait ran out: let the copies in flight land (bounded) before the
+    // block's shared memory is given up, and end the solve with an error
+    if (threadIdx.x == 0) {
+      for (int i = std::max(0, issued - kStreamSlots); i < issued; i++)
+        mbar_wait(&bars[i % kStreamSlots], (unsigned)(i / kStreamSlots) & 1u, kStreamWaitNs);
+      sc->status = 4;
+      sc->done = 1;
+    }
+    return;
+  }
+  const double b = block_sum(acc.value());
+  const unsigned nb = gridDim.x * gridDim.y;
+  if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = b;
+  if (last_block(&sc->counters[1], nb)) {
+    const double s = sum_partials(part, (int)nb);
+    if (threadIdx.x == 0) {
+      const float dp = (float)s;
+      sc->dp = dp;
+      float alpha = 0.f;
+      if (fabsf(dp) > 0.f) alpha = sc->sigma / dp;
+      sc->alpha = alpha;
+    }
+  }
+}
+
+// Slab height and z run for the streamed SpMV, or false where it does not
+// apply (2D, rows not a multiple of 8 cells, rows too long for a slab of 4).
+static bool stream_geom(const Dims& d, int maxBlocks, int sms, StreamGeom* g, dim3* grid) {
+  if (!d.is3d || d.nx % 8 != 0) return false;
+  int TY = 16;
+  while (TY >= 4 && (size_t)(TY + 2) * d.nx * 4 + (size_t)TY * d.nx * 2 > (size_t)kStreamSlotBudget) TY--;
+  if (TY < 4) return false;
+  g->TY = TY;
+  g->xBytes = (unsigned)((TY + 2) * d.nx * 4);
+  g->slotBytes = (unsigned)(((size_t)g->xBytes + (size_t)TY * d.nx * 2 + 127) / 128 * 128);
+  const int slabs = (d.ny + TY - 1) / TY;
+  const int target = std::min(maxBlocks, 3 * sms);
+  // at least 6 planes per CTA: the two halo planes of a run cost extra reads
+  int chunks = std::max(1, std::min(std::max(1, d.nz / 6), target / std::max(1, slabs)));
+  g->zc = (d.nz + chunks - 1) / chunks;
+  chunks = (d.nz + g->zc - 1) / g->zc;
+  if (slabs * chunks > maxBlocks) return false;
+  *grid = dim3((unsigned)slabs, (unsigned)chunks, 1);
+  return true;
+}
+
+static int g_sms = 0;
+static bool g_spmvStream = true;
+
+int pcg_prepare(int sms) {
+  g_sms = sms;
+  const char* e = getenv("MANTAGPU_SPMV");
+  g_spmvStream = !(e && std::string(e) == "quad");
+  const size_t smem = (size_t)kStreamSlots * kStreamSlotBudget;
+  return cudaFuncSetAttribute(k_pcg_spmv_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess
+             ? 0
+             : 1;
 }
 
 __global__ void __launch_bounds__(256) k_pcg_axpy4(long long n, float* p, const float* __restrict__ s, float* r,
@@ -878,6 +1079,13 @@ static int vec4_blocks(const PcgBuffers& b) {
 }
 void launch_pcg_spmv(const PcgBuffers& b, cudaStream_t s) {
   count_launch();
+  StreamGeom g;
+  dim3 grid;
+  if (g_spmvStream && stream_geom(b.d, 2 * b.nblocks, g_sms, &g, &grid)) {
+    k_pcg_spmv_stream<<<grid, kThreads, (size_t)kStreamSlots * g.slotBytes, s>>>(b.d, g, b.code, b.A0f, b.search,
+                                                                               b.tmp, b.part, b.sc);
+    return;
+  }
   if (vec4_ok(b.d))
     k_pcg_spmv4<<<vec4_blocks(b), kThreads, 0, s>>>(b.d, b.code, b.A0f, b.search, b.tmp, b.part, b.sc);
   else

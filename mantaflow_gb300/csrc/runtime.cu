@@ -301,7 +301,7 @@ extern "C" int mg_init(int device) {
   g_ctx.sms = prop.multiProcessorCount;
   g_ctx.micCtasPerSm = mic_ctas_per_sm();
   if (mic_col_prepare() || mic_wave_prepare(&g_ctx.waveCtasPerSm4, &g_ctx.waveCtasPerSm8) ||
-      mic_flow_prepare(&g_ctx.flowCtasPerSm))
+      mic_flow_prepare(&g_ctx.flowCtasPerSm) || pcg_prepare(g_ctx.sms))
     return fail(MG_ERR_CUDA, "mg_init: cannot configure the MIC kernels");
   g_ctx.device = device;
   g_ctx.init = true;
@@ -719,13 +719,12 @@ extern "C" int mg_advect_semi_lagrange(mg_grid flags, mg_grid vel, mg_grid grid,
   if (grid->kind == MG_INT || grid->kind == MG_FLAGS)
     return fail(MG_ERR_SOLVER, "AdvectSemiLagrange: Grid Type is not supported (only Real, Vec3, MAC, Levelset)");
   if (grid->kind == MG_MAC) {
-    if (orderSpace != 1) return fail(MG_ERR_UNSUPPORTED, "advectSemiLagrange: cubic (orderSpace=2) MAC advection is not supported");
     const size_t bytes = grid->bytes();
     Tmp fwd(s, bytes);
     if (!fwd.p) return fail(MG_ERR_NOMEM, "advectSemiLagrange: out of device memory");
     {
       ProfScope ps(s, "advect_mac_fwd");
-      launch_advect_sl_mac(d, vel->cmac(), grid->cmac(), fwd.mac(), dt, orderTrace, s->stream);
+      launch_advect_sl_mac(d, vel->cmac(), grid->cmac(), fwd.mac(), dt, orderSpace, orderTrace, s->stream);
     }
     CKL();
     const float ts = (float)std::max(1.0, (double)dt * 4);
@@ -744,7 +743,7 @@ extern "C" int mg_advect_semi_lagrange(mg_grid flags, mg_grid vel, mg_grid grid,
       {
         ProfScope ps(s, "advect_mac_maccormack");
         launch_advect_maccormack_mac(d, flags->i(), vel->cmac(), grid->cmac(), fwd.cmac(), nw.mac(), dt, strength, clampMode,
-                                     orderTrace, s->stream);
+                                     orderSpace, orderTrace, s->stream);
       }
       CKL();
       {
@@ -836,8 +835,6 @@ extern "C" int mg_advect_semi_lagrange_noalloc(mg_grid flags, mg_grid vel, mg_gr
   if (orderSpace != 1 && orderSpace != 2) return fail(MG_ERR_SOLVER, "Unknown interpolation order " + std::to_string(orderSpace));
   if (grid->kind == MG_INT || grid->kind == MG_FLAGS)
     return fail(MG_ERR_SOLVER, "AdvectSemiLagrange: Grid Type is not supported (only Real, Vec3, MAC, Levelset)");
-  if (grid->kind == MG_MAC && orderSpace != 1)
-    return fail(MG_ERR_UNSUPPORTED, "advectSemiLagrange: cubic (orderSpace=2) MAC advection is not supported");
   mg_solver s = flags->s;
   const Dims& d = s->d;
   const float dt = s->dt;
@@ -855,15 +852,15 @@ extern "C" int mg_advect_semi_lagrange_noalloc(mg_grid flags, mg_grid vel, mg_gr
   const CMac cA{A, A + d.n, A + 2 * d.n}, cB{B, B + d.n, B + 2 * d.n};
   const float* result;
   if (grid->kind == MG_MAC) {
-    launch_advect_sl_mac(d, vel->cmac(), grid->cmac(), mA, dt, orderTrace, s->stream);
+    launch_advect_sl_mac(d, vel->cmac(), grid->cmac(), mA, dt, orderSpace, orderTrace, s->stream);
     CKL();
     const float ts = (float)std::max(1.0, (double)dt * 4);
     if (order == 1) {
       launch_outflow_bc(d, flags->i(), cA, grid->cmac(), mB, mA, ts, s->stream);
       result = A;
     } else {
-      launch_advect_maccormack_mac(d, flags->i(), vel->cmac(), grid->cmac(), cA, mB, dt, strength, clampMode, orderTrace,
-                                   s->stream);
+      launch_advect_maccormack_mac(d, flags->i(), vel->cmac(), grid->cmac(), cA, mB, dt, strength, clampMode, orderSpace,
+                                   orderTrace, s->stream);
       CKL();
       launch_outflow_bc(d, flags->i(), cB, grid->cmac(), mA, mB, ts, s->stream);
       result = B;
@@ -1435,6 +1432,7 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   }
   if (s->scHost->status == 2)
     return fail(MG_ERR_SOLVER, "GridCg::iterate: The CG solver diverged, residual norm > 1e30, stopping.");
+  if (s->scHost->status == 4) return fail(MG_ERR_TIMEOUT, "PCG: a plane copy of the streamed SpMV exceeded its wait limit");
   if (s->mg && preconditioner == MG_PC_MG_DYNAMIC) mg_hierarchy_reset(s->mg);
   return MG_OK;
 }

@@ -80,6 +80,26 @@ def test_advection(tag):
 
 
 @pytest.mark.parametrize("tag", ["3d", "2d"])
+@pytest.mark.parametrize("order,clamp,trace", [(1, 2, 1), (2, 1, 1), (2, 2, 1), (2, 2, 2)])
+def test_advection_mac_cubic_against_oracle(tag, order, clamp, trace):
+    """Cubic (orderSpace=2) MAC advection -- interpolCubicMAC's per-component
+    Catmull-Rom samples (util/interpolHigh.h:171-178) -- against the
+    oracle's restatement on the golden scene's inputs (the reference's golden
+    set has no cubic MAC case, so this comparison is with the oracle only)."""
+    g = load("advect_" + tag)
+    flags_a, vel_a, dt = g["flags"], g["vel"], float(g["dt"])
+    s = make_solver(flags_a.shape, dt)
+    flags = grid_from(s, m.FlagGrid, flags_a)
+    vel = grid_from(s, m.MACGrid, vel_a)
+    m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=order, orderSpace=2, clampMode=clamp,
+                         orderTrace=trace)
+    want = vel_a.copy()
+    og.advect_semi_lagrange(flags_a, want, want, og.KIND_MAC, order=order, orderSpace=2, clampMode=clamp,
+                            orderTrace=trace, dt=dt)
+    close_bitwise(vel.numpy(), want, "cubic MAC %s order %d clamp %d trace %d" % (tag, order, clamp, trace))
+
+
+@pytest.mark.parametrize("tag", ["3d", "2d"])
 def test_forces_and_walls(tag):
     g = load("forces_" + tag)
     s = make_solver(g["flags"].shape, float(g["dt"]))
