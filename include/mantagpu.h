@@ -164,6 +164,8 @@ int mg_reset_outflow(mg_grid flags, mg_grid phi, mg_grid real);
 /* ---- plugins: simple extrapolation (fastmarch.cpp) ----------------------- */
 /* extrapolateMACSimple (:337-375); phiObs must be NULL */
 int mg_extrapolate_mac_simple(mg_grid flags, mg_grid vel, int distance, mg_grid phiObs, int intoObs);
+/* extrapolateLsSimple (fastmarch.cpp:470-507): phi is a Real or Levelset grid */
+int mg_extrapolate_ls_simple(mg_grid phi, int distance, int inside);
 
 /* ---- plugins: pressure (plugin/pressure.cpp) ----------------------------- */
 typedef struct {

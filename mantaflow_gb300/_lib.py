@@ -95,6 +95,7 @@ SIGNATURES = [
     ("mg_set_open_bound", _I, [_P, _I, C.c_char_p, _I]),
     ("mg_reset_outflow", _I, [_P, _P, _P]),
     ("mg_extrapolate_mac_simple", _I, [_P, _P, _I, _P, _I]),
+    ("mg_extrapolate_ls_simple", _I, [_P, _I, _I]),
     ("mg_pressure_params_default", None, [C.POINTER(PressureParams)]),
     ("mg_solve_pressure", _I, [_P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P, _P, _P,
                                C.POINTER(PressureResult)]),

@@ -155,6 +155,54 @@ __global__ void k_extrap_into_bnd(Dims d, const int* __restrict__ flags, Mac vel
   }
 }
 
+// ------------------------------------------------------- levelset extrapolation
+// extrapolateLsSimple (fastmarch.cpp:470-507).  Pass 1 marks the inside
+// (phi < 0; phi > 0 for inside marching) with 1, pass 2 the first layer
+// around it with 2 (tmp 1 -> 2 never feeds pass 2 itself, so the reference's
+// serial loop is order independent).  Both skip the outermost layer.
+__global__ void k_els_mark(Dims d, const float* __restrict__ phi, int* tmp, int inside) {
+  CELL_IJK
+  int t = 0;
+  if (INNER) t = inside ? (phi[idx] > 0.f) : (phi[idx] < 0.f);
+  tmp[idx] = t;
+}
+__global__ void k_els_first(Dims d, const int* __restrict__ mark, int* tmp) {
+  CELL_IJK
+  if (!INNER || mark[idx]) return;
+  const long long nb[6] = {1, -1, d.sy, -d.sy, d.sz, -d.sz};
+  const int dim = d.is3d ? 3 : 2;
+  for (int q = 0; q < 2 * dim; q++)
+    if (mark[idx + nb[q]] == 1) {
+      tmp[idx] = 2;
+      return;
+    }
+}
+// knExtrapolateLsSimple (fastmarch.cpp:443-461): the float average of the
+// layer-d neighbours (+x,-x,+y,-y,+z,-z order) divided by their count, plus
+// the marching direction; in place like the MAC layers above.
+__global__ void k_els_layer(Dims d, float* phi, int* tmp, int layer, float direction) {
+  CELL_IJK
+  if (!INNER || tmp[idx] != 0) return;
+  const long long nb[6] = {1, -1, d.sy, -d.sy, d.sz, -d.sz};
+  const int dim = d.is3d ? 3 : 2;
+  int nbs = 0;
+  float avg = 0.f;
+  for (int q = 0; q < 2 * dim; q++)
+    if (tmp[idx + nb[q]] == layer) {
+      avg += phi[idx + nb[q]];
+      nbs++;
+    }
+  if (nbs > 0) {
+    tmp[idx] = layer + 1;
+    phi[idx] = avg / (float)nbs + direction;
+  }
+}
+// knSetRemaining (fastmarch.cpp:464-468)
+__global__ void k_els_remaining(Dims d, float* phi, const int* __restrict__ tmp, float value) {
+  CELL_IJK
+  if (INNER && tmp[idx] == 0) phi[idx] = value;
+}
+
 // ------------------------------------------------------------------ setup
 // FlagGrid::initDomain -> setConst(TypeEmpty) + initBoundaries (grid.cpp:824-842)
 __global__ void k_init_domain(Dims d, int* flags, int w, int t0, int t1, int t2, int t3, int t4, int t5) {
@@ -400,6 +448,21 @@ void launch_extrapolate_mac_simple(const Dims& d, const int* flags, Mac vel, int
   cudaMemcpyAsync(snap.w, vel.w, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s);
   count_launch();
   k_extrap_into_bnd<<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, CMac{snap.u, snap.v, snap.w});
+}
+void launch_extrapolate_ls_simple(const Dims& d, float* phi, int* tmp, int* mark, int distance, int inside,
+                                  cudaStream_t s) {
+  const float direction = inside ? -1.f : 1.f;
+  count_launch();
+  k_els_mark<<<grid3(d, kBlk), kBlk, 0, s>>>(d, phi, mark, inside);
+  cudaMemcpyAsync(tmp, mark, sizeof(int) * d.n, cudaMemcpyDeviceToDevice, s);
+  count_launch();
+  k_els_first<<<grid3(d, kBlk), kBlk, 0, s>>>(d, mark, tmp);
+  for (int l = 2; l < 1 + distance; l++) {
+    count_launch();
+    k_els_layer<<<grid3(d, kBlk), kBlk, 0, s>>>(d, phi, tmp, l, direction);
+  }
+  count_launch();
+  k_els_remaining<<<grid3(d, kBlk), kBlk, 0, s>>>(d, phi, tmp, direction * (float)(distance + 2));
 }
 void launch_init_domain(const Dims& d, int* flags, int bw, const int* types, cudaStream_t s) {
   count_launch();

@@ -33,6 +33,9 @@ void launch_add_force(const Dims& d, const int* flags, Mac vel, float fx, float 
                       cudaStream_t s);
 void launch_extrapolate_mac_simple(const Dims& d, const int* flags, Mac vel, int* tmp, Mac snap, int distance, int intoObs,
                                    cudaStream_t s);
+// extrapolateLsSimple; tmp, mark: int scratch grids
+void launch_extrapolate_ls_simple(const Dims& d, float* phi, int* tmp, int* mark, int distance, int inside,
+                                  cudaStream_t s);
 void launch_init_domain(const Dims& d, int* flags, int bw, const int* types, cudaStream_t s);
 void launch_fill_grid(const Dims& d, int* flags, int type, cudaStream_t s);
 void launch_set_open_bound(const Dims& d, int* flags, int bw, const int* lo, const int* up, int type, cudaStream_t s);

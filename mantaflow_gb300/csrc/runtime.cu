@@ -1002,6 +1002,18 @@ extern "C" int mg_extrapolate_mac_simple(mg_grid flags, mg_grid vel, int distanc
   return MG_OK;
 }
 
+extern "C" int mg_extrapolate_ls_simple(mg_grid phi, int distance, int inside) {
+  NEED_GRID(phi, "extrapolateLsSimple");
+  if (!is_real(phi)) return fail(MG_ERR_ARG, "extrapolateLsSimple: phi must be a Real or Levelset grid");
+  mg_solver s = phi->s;
+  Tmp tmp(s, sizeof(int) * (size_t)s->d.n), mark(s, sizeof(int) * (size_t)s->d.n);
+  if (!tmp.p || !mark.p) return fail(MG_ERR_NOMEM, "extrapolateLsSimple: out of device memory");
+  ProfScope ps(s, "extrapolate_ls_simple");
+  launch_extrapolate_ls_simple(s->d, phi->f(), tmp.i(), mark.i(), distance, inside, s->stream);
+  CKL();
+  return MG_OK;
+}
+
 // ================================================================ pressure
 extern "C" void mg_pressure_params_default(mg_pressure_params* p) {
   if (!p) return;

@@ -445,6 +445,11 @@ def extrapolateMACSimple(flags, vel, distance=4, phiObs=None, intoObs=False):
     check(_lib.load().mg_extrapolate_mac_simple(flags._h, vel._h, int(distance), _h(phiObs), int(bool(intoObs))))
 
 
+def extrapolateLsSimple(phi, distance=4, inside=False):
+    """fastmarch.cpp:470-507"""
+    check(_lib.load().mg_extrapolate_ls_simple(phi._h, int(distance), int(bool(inside))))
+
+
 def _params(cgAccuracy, gfClamp, cgMaxIterFac, precondition, preconditioner, enforceCompatibility, useL2Norm,
             zeroPressureFixing, surfTens):
     return PressureParams(float(cgAccuracy), float(gfClamp), float(cgMaxIterFac), int(bool(precondition)),

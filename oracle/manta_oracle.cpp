@@ -800,6 +800,58 @@ void og_extrapolate_mac_simple(og_dims d, const int* flags, og_real* vel, int di
   free(tmp);
 }
 
+/* extrapolateLsSimple (fastmarch.cpp:470-507): mark the inside (phi < 0, or
+ * phi > 0 with inside), the first layer around it (tmp = 2, values kept),
+ * then layers d = 2..distance by knExtrapolateLsSimple (:443-461; a cell
+ * reads only neighbours of layer d, so the in-place pass is order
+ * independent: avg over +x,-x,+y,-y,+z,-z in float, then avg / nbs +
+ * direction), and knSetRemaining (:464-468) for cells never reached.  All
+ * passes skip the outermost layer (bnd = 1). */
+void og_extrapolate_ls_simple(og_dims d, og_real* phi, int distance, int inside) {
+  const ll n = NCELL(d);
+  int* tmp = (int*)calloc((size_t)n, sizeof(int));
+  const int dim = d.is3d ? 3 : 2;
+  const og_real direction = inside ? OG_R(-1.) : OG_R(1.);
+  const ll nbo[6] = {1, -1, SY(d), -SY(d), SZ(d), -SZ(d)};
+  for (int k = KLO(d, 1); k < KHI(d, 1); k++)
+    for (int j = 1; j < d.ny - 1; j++)
+      for (int i = 1; i < d.nx - 1; i++) {
+        const ll idx = IX(d, i, j, k);
+        if (inside ? phi[idx] > OG_R(0.) : phi[idx] < OG_R(0.)) tmp[idx] = 1;
+      }
+  for (int k = KLO(d, 1); k < KHI(d, 1); k++)
+    for (int j = 1; j < d.ny - 1; j++)
+      for (int i = 1; i < d.nx - 1; i++) {
+        const ll idx = IX(d, i, j, k);
+        if (tmp[idx]) continue;
+        for (int q = 0; q < 2 * dim; q++)
+          if (tmp[idx + nbo[q]] == 1) { tmp[idx] = 2; break; }
+      }
+  for (int dd = 2; dd < 1 + distance; dd++)
+    for (int k = KLO(d, 1); k < KHI(d, 1); k++)
+      for (int j = 1; j < d.ny - 1; j++)
+        for (int i = 1; i < d.nx - 1; i++) {
+          const ll idx = IX(d, i, j, k);
+          if (tmp[idx] != 0) continue;
+          int nbs = 0;
+          og_real avg = OG_R(0.);
+          for (int q = 0; q < 2 * dim; q++)
+            if (tmp[idx + nbo[q]] == dd) { avg += phi[idx + nbo[q]]; nbs++; }
+          if (nbs > 0) {
+            tmp[idx] = dd + 1;
+            phi[idx] = avg / (og_real)nbs + direction;
+          }
+        }
+  const og_real rem = (og_real)(direction * (og_real)(distance + 2));
+  for (int k = KLO(d, 1); k < KHI(d, 1); k++)
+    for (int j = 1; j < d.ny - 1; j++)
+      for (int i = 1; i < d.nx - 1; i++) {
+        const ll idx = IX(d, i, j, k);
+        if (tmp[idx] == 0) phi[idx] = rem;
+      }
+  free(tmp);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Pressure projection, plugin/pressure.cpp + conjugategrad.*               */
 

@@ -75,6 +75,7 @@ void og_add_gravity(og_dims d, const int* flags, og_real* vel, og_real gx, og_re
 
 /* extrapolateMACSimple (fastmarch.cpp:337-375), phiObs unsupported (NULL). */
 void og_extrapolate_mac_simple(og_dims d, const int* flags, og_real* vel, int distance, int intoObs);
+void og_extrapolate_ls_simple(og_dims d, og_real* phi, int distance, int inside);
 
 typedef struct {
   og_real cgAccuracy;        /* 1e-3 */

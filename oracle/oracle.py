@@ -80,6 +80,7 @@ def lib(dtype=np.float32):
         L.og_add_buoyancy.argtypes = [Dims, ip, fp, fp, F, F, F, F, I, F]
         L.og_add_gravity.argtypes = [Dims, ip, fp, F, F, F, C.c_void_p, I, F]
         L.og_extrapolate_mac_simple.argtypes = [Dims, ip, fp, I, I]
+        L.og_extrapolate_ls_simple.argtypes = [Dims, fp, I, I]
         L.og_mg_create.argtypes = [Dims]
         L.og_mg_create.restype = C.c_void_p
         L.og_mg_destroy.argtypes = [C.c_void_p]
@@ -153,6 +154,10 @@ def add_gravity(flags, vel, gravity, exclude=None, scale=True, dt=1.0):
 
 def extrapolate_mac_simple(flags, vel, distance=4, intoObs=False):
     lib(vel.dtype).og_extrapolate_mac_simple(dims(flags.shape), flags, vel, distance, int(intoObs))
+
+
+def extrapolate_ls_simple(phi, distance=4, inside=False):
+    lib(phi.dtype).og_extrapolate_ls_simple(dims(phi.shape), phi, int(distance), int(bool(inside)))
 
 
 def params(cgAccuracy=1e-3, gfClamp=1e-4, cgMaxIterFac=1.5, preconditioner=PC_MIC, enforceCompatibility=False,

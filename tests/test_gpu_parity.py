@@ -136,6 +136,32 @@ def test_extrapolate_mac_simple(tag):
     close_bitwise(v.numpy(), g["ext2_obs"], "extrap 2 intoObs")
 
 
+@pytest.mark.parametrize("shape", [(30, 34, 28), (48, 40, 1)])
+@pytest.mark.parametrize("distance,inside", [(4, False), (3, True), (6, False)])
+def test_extrapolate_ls_simple_against_oracle(shape, distance, inside):
+    """extrapolateLsSimple (fastmarch.cpp:470-507) on a box levelset that has
+    been advected (so it is no longer a distance field) against the oracle's
+    restatement (the golden set holds no case of it: oracle only)."""
+    nx, ny, nz = shape
+    f = np.zeros((nz, ny, nx), np.int32)
+    og.init_domain(f, 0)
+    og.fill_grid(f)
+    phi = np.zeros((nz, ny, nx), np.float32)
+    og.box_sdf(phi, (0, 0, 0), (0.4 * nx, 0.55 * ny, nz))
+    rng = np.random.default_rng(11)
+    v = ((rng.random((nz, ny, nx, 3), dtype=np.float32) - 0.5) * 1.5).astype(np.float32)
+    if nz == 1:
+        v[..., 2] = 0
+    og.advect_semi_lagrange(f, v, phi, og.KIND_REAL, order=1)
+    s = make_solver(phi.shape)
+    g = grid_from(s, m.LevelsetGrid, phi)
+    m.extrapolateLsSimple(phi=g, distance=distance, inside=inside)
+    want = phi.copy()
+    og.extrapolate_ls_simple(want, distance, inside)
+    assert not np.array_equal(want, phi)
+    close_bitwise(g.numpy(), want, "extrapolateLsSimple %s d=%d inside=%s" % (shape, distance, inside), min_exact=1.0)
+
+
 def test_setup():
     g = load("setup_3d")
     nx, ny, nz = [int(x) for x in g["size"]]
