@@ -112,6 +112,15 @@ int mg_grid_upload_async(mg_grid g, const void* host, size_t bytes);
 int mg_grid_download_async(mg_grid g, void* host, size_t bytes);
 /* Block until every asynchronous transfer and kernel of the solver is done. */
 int mg_solver_wait_copies(mg_solver s);
+/* Grid<T>::getSizeX/Y/Z and getType: the grid's dimensions and kind */
+int mg_grid_get_info(mg_grid g, int* nx, int* ny, int* nz, int* kind);
+/* Grid<T>::save (grid.cpp:135-156) for .uni (writeGridUni, fileio/iogrids.cpp:
+ * 386-432), .raw (writeGridRaw, :255-271) and .npz (writeGridNumpy,
+ * :836-884), written from the device mirror.  The gzip streams of .uni/.raw
+ * hold stored (uncompressed) deflate blocks, which every gzip reader
+ * accepts; .npz is an uncompressed zip of arr_0.npy, shape (nz, ny, nx, 1|3).
+ * Other extensions: MG_ERR_UNSUPPORTED with the reference's message. */
+int mg_grid_save(mg_grid g, const char* path);
 /* Grid<T>::swap (grid.cpp:99-110): exchanges the storage of two grids */
 int mg_grid_swap(mg_grid a, mg_grid b);
 /* Grid<T>::copyFrom */

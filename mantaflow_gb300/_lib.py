@@ -78,6 +78,8 @@ SIGNATURES = [
     ("mg_grid_upload_async", _I, [_P, _P, C.c_size_t]),
     ("mg_grid_download_async", _I, [_P, _P, C.c_size_t]),
     ("mg_solver_wait_copies", _I, [_P]),
+    ("mg_grid_get_info", _I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
+    ("mg_grid_save", _I, [_P, C.c_char_p]),
     ("mg_grid_swap", _I, [_P, _P]),
     ("mg_grid_copy", _I, [_P, _P]),
     ("mg_grid_set_const", _I, [_P, _F, _F, _F]),

@@ -476,6 +476,15 @@ extern "C" int mg_grid_create(mg_solver s, int kind, mg_grid* out) {
   return MG_OK;
 }
 
+extern "C" int mg_grid_get_info(mg_grid g, int* nx, int* ny, int* nz, int* kind) {
+  NEED_GRID(g, "mg_grid_get_info");
+  if (nx) *nx = g->s->d.nx;
+  if (ny) *ny = g->s->d.ny;
+  if (nz) *nz = g->s->d.nz;
+  if (kind) *kind = g->kind;
+  return MG_OK;
+}
+
 extern "C" int mg_grid_destroy(mg_grid g) {
   NEED_GRID(g, "mg_grid_destroy");
   sync_copies(g->s);

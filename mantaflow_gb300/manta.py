@@ -225,6 +225,12 @@ class GridBase:
         """Download the grid as a numpy array in the reference layout."""
         return self._download()
 
+    def save(self, name):
+        """Grid<T>::save (grid.cpp:135-156): .uni, .raw or .npz, written from
+        the device mirror."""
+        check(_lib.load().mg_grid_save(self._h, str(name).encode()))
+        return 1
+
     def copyFrom(self, other, copyType=True):
         check(_lib.load().mg_grid_copy(self._h, other._h))
         return self
