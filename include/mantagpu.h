@@ -112,6 +112,13 @@ int mg_grid_upload_async(mg_grid g, const void* host, size_t bytes);
 int mg_grid_download_async(mg_grid g, void* host, size_t bytes);
 /* Block until every asynchronous transfer and kernel of the solver is done. */
 int mg_solver_wait_copies(mg_solver s);
+/* FluidSolver::getGridSize */
+int mg_solver_size(mg_solver s, int* nx, int* ny, int* nz);
+/* The grid's device storage (n floats / ints, or three planes of n floats for
+ * Vec3/MAC) and its solver's CUDA stream (a cudaStream_t), for callers that
+ * launch their own kernels on a grid.  Valid until the grid is destroyed or
+ * swapped. */
+int mg_grid_device(mg_grid g, void** data, void** stream);
 /* Grid<T>::getSizeX/Y/Z and getType: the grid's dimensions and kind */
 int mg_grid_get_info(mg_grid g, int* nx, int* ny, int* nz, int* kind);
 /* Grid<T>::save (grid.cpp:135-156) for .uni (writeGridUni, fileio/iogrids.cpp:
@@ -175,6 +182,37 @@ int mg_reset_outflow(mg_grid flags, mg_grid phi, mg_grid real);
 int mg_extrapolate_mac_simple(mg_grid flags, mg_grid vel, int distance, mg_grid phiObs, int intoObs);
 /* extrapolateLsSimple (fastmarch.cpp:470-507): phi is a Real or Levelset grid */
 int mg_extrapolate_ls_simple(mg_grid phi, int distance, int inside);
+
+/* ---- wavelet noise and the density source (noisefield.h, noisefield.cpp,
+ * plugin/initplugins.cpp) ---------------------------------------------------- */
+typedef struct mg_noise_s* mg_noise; /* WaveletNoiseField, Python name NoiseField */
+/* the NoiseField properties posOffset, posScale, valOffset, valScale, clamp,
+ * clampNeg, clampPos, timeAnim (noisefield.h:52-63) */
+typedef struct {
+  float posOffset[3], posScale[3];
+  float valOffset, valScale;
+  int clamp;
+  float clampNeg, clampPos;
+  float timeAnim;
+} mg_noise_params;
+void mg_noise_params_default(mg_noise_params* p);
+/* WaveletNoiseField(parent, fixedSeed=-1) (noisefield.cpp:61-78): the shared
+ * 3 x 128^3 noise tile is generated on the host (generateTile, :94-190) on
+ * first use and kept in device memory until mg_shutdown */
+int mg_noise_create(mg_solver s, int fixedSeed, mg_noise* out);
+int mg_noise_destroy(mg_noise n);
+int mg_noise_set_params(mg_noise n, const mg_noise_params* p);
+/* mSeedOffset, the normalized random offset into the tile */
+int mg_noise_seed_offset(mg_noise n, float* out3);
+/* out(i,j,k) = evaluate(Vec3(i,j,k)) (noisefield.h:332-357) at the solver time
+ * solverTime (FluidSolver::getTime, for timeAnim) */
+int mg_noise_evaluate_grid(mg_noise n, mg_grid out, float solverTime);
+/* densityInflow(flags, density, noise, shape, scale, sigma) (initplugins.cpp:
+ * 38-43) with sdf = shape->computeLevelset() computed by the caller */
+int mg_density_inflow(mg_grid flags, mg_grid density, mg_noise noise, mg_grid sdf, float scale, float sigma,
+                      float solverTime);
+/* Cylinder::computeLevelset (CylinderSDF, shapes.cpp:367-388) */
+int mg_shape_cylinder_levelset(mg_grid phi, const float* center, float radius, const float* z);
 
 /* ---- plugins: pressure (plugin/pressure.cpp) ----------------------------- */
 typedef struct {

@@ -39,6 +39,12 @@ class ServeJob(C.Structure):
                 ("meanStepMs", C.c_double)]
 
 
+class NoiseParams(C.Structure):
+    _fields_ = [("posOffset", C.c_float * 3), ("posScale", C.c_float * 3), ("valOffset", C.c_float),
+                ("valScale", C.c_float), ("clamp", C.c_int), ("clampNeg", C.c_float), ("clampPos", C.c_float),
+                ("timeAnim", C.c_float)]
+
+
 class RefineParams(C.Structure):
     _fields_ = [("refineAccuracy", C.c_double), ("innerAccuracy", C.c_double), ("maxRefine", C.c_int)]
 
@@ -78,6 +84,8 @@ SIGNATURES = [
     ("mg_grid_upload_async", _I, [_P, _P, C.c_size_t]),
     ("mg_grid_download_async", _I, [_P, _P, C.c_size_t]),
     ("mg_solver_wait_copies", _I, [_P]),
+    ("mg_solver_size", _I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
+    ("mg_grid_device", _I, [_P, C.POINTER(_P), C.POINTER(_P)]),
     ("mg_grid_get_info", _I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     ("mg_grid_save", _I, [_P, C.c_char_p]),
     ("mg_grid_swap", _I, [_P, _P]),
@@ -98,6 +106,14 @@ SIGNATURES = [
     ("mg_reset_outflow", _I, [_P, _P, _P]),
     ("mg_extrapolate_mac_simple", _I, [_P, _P, _I, _P, _I]),
     ("mg_extrapolate_ls_simple", _I, [_P, _I, _I]),
+    ("mg_noise_params_default", None, [C.POINTER(NoiseParams)]),
+    ("mg_noise_create", _I, [_P, _I, C.POINTER(_P)]),
+    ("mg_noise_destroy", _I, [_P]),
+    ("mg_noise_set_params", _I, [_P, C.POINTER(NoiseParams)]),
+    ("mg_noise_seed_offset", _I, [_P, _FP]),
+    ("mg_noise_evaluate_grid", _I, [_P, _P, _F]),
+    ("mg_density_inflow", _I, [_P, _P, _P, _P, _F, _F, _F]),
+    ("mg_shape_cylinder_levelset", _I, [_P, _FP, _F, _FP]),
     ("mg_pressure_params_default", None, [C.POINTER(PressureParams)]),
     ("mg_solve_pressure", _I, [_P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P, _P, _P,
                                C.POINTER(PressureResult)]),

@@ -187,7 +187,7 @@ __device__ __forceinline__ void maccormack_real_cell(const Dims& d, const int* _
 }
 
 template <int CH, int kOrderSpace, int kTrace>
-__global__ void __launch_bounds__(256) k_maccormack_cell(Dims d, const int* __restrict__ flags, CMac vel,
+__global__ void __launch_bounds__(256, 6) k_maccormack_cell(Dims d, const int* __restrict__ flags, CMac vel,
                                                          const float* __restrict__ orig, const float* __restrict__ fwd,
                                                          float* __restrict__ dst, float dt, float strength, int clampMode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -346,7 +346,7 @@ __device__ __forceinline__ void maccormack_mac_cell(const Dims& d, const int* __
 }
 
 template <int kTrace, int kOS>
-__global__ void __launch_bounds__(256) k_maccormack_mac(Dims d, const int* __restrict__ flags, CMac vel, CMac orig,
+__global__ void __launch_bounds__(256, 5) k_maccormack_mac(Dims d, const int* __restrict__ flags, CMac vel, CMac orig,
                                                         CMac fwd, Mac dst, float dt, float strength, int clampMode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;

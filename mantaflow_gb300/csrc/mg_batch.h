@@ -22,6 +22,8 @@ int set_error(int code, const std::string& msg);
 bool library_ready();
 // Cylinder's axis: the unit direction and the length of the z vector
 void cylinder_axis(const float* z, float* zn, float* mZ);
+// noise.cu: frees the device noise tile (mg_shutdown)
+void noise_release();
 
 struct BTile {
   int scene;

@@ -490,11 +490,13 @@ __global__ void __launch_bounds__(256, 4) k_pcg_spmv4(Dims d, const code_t* __re
 // kStreamSlots planes is filled by bulk asynchronous copies (one copy of the
 // slab's rows plus their y halo per plane, one of the plane's stencil codes),
 // completed on one mbarrier per slot; while plane z is computed from planes
-// z-1, z and z+1, plane z+2 is on its way.  x is read from DRAM once per
-// plane (the y halo rows come from L2), and no neighbour is re-read from L2
-// by a gather.  Same cell arithmetic as k_pcg_spmv4.
-constexpr int kStreamSlots = 4;
-constexpr int kStreamSlotBudget = 16384;         // bytes of one ring slot at most
+// z-1, z and z+1, the next kStreamSlots - 3 planes are on their way, so each
+// SM keeps ~100 KB of loads in flight.  x is read from DRAM once per plane
+// (the y halo rows come from L2), and no neighbour is re-read from L2 by a
+// gather.  Same cell arithmetic as k_pcg_spmv4.
+constexpr int kStreamSlots = 8;
+constexpr int kStreamSlotBudget = 12288;         // bytes of one ring slot at most
+constexpr int kStreamQuads = 2;                  // quads per thread and plane at most
 constexpr long long kStreamWaitNs = 100000000LL;  // bound of one copy wait
 
 struct StreamGeom {
@@ -502,7 +504,7 @@ struct StreamGeom {
   unsigned slotBytes, xBytes;  // ring slot size, offset of the code rows in a slot
 };
 
-__global__ void __launch_bounds__(256, 3) k_pcg_spmv_stream(Dims d, StreamGeom g, const code_t* __restrict__ code,
+__global__ void __launch_bounds__(256, 2) k_pcg_spmv_stream(Dims d, StreamGeom g, const code_t* __restrict__ code,
                                                            const float* __restrict__ A0f, const float* __restrict__ x,
                                                            float* y, double* part, CgScalars* sc) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -520,10 +522,7 @@ __global__ void __launch_bounds__(256, 3) k_pcg_spmv_stream(Dims d, StreamGeom g
     mbar_fence_init();
   }
   __syncthreads();
-  auto slotX = [&](int i) { return reinterpret_cast<float*>(smem + (size_t)(i % kStreamSlots) * g.slotBytes); };
-  auto slotC = [&](int i) {
-    return reinterpret_cast<const code_t*>(smem + (size_t)(i % kStreamSlots) * g.slotBytes + g.xBytes);
-  };
+  auto slotBase = [&](int i) { return smem + (size_t)(i % kStreamSlots) * g.slotBytes; };
   // thread 0: fill the slot of ring index i (planes outside the grid only
   // complete the slot's phase)
   auto issue = [&](int i) {
@@ -537,20 +536,29 @@ __global__ void __launch_bounds__(256, 3) k_pcg_spmv_stream(Dims d, StreamGeom g
     const bool withCode = p >= zs && p < ze;
     const unsigned cb = withCode ? (unsigned)(ty * nx) * 2u : 0u;
     mbar_arrive_expect(bar, xb + cb);
-    bulk_g2s(slotX(i), x + p * sz + (long long)ya * nx, xb, bar);
-    if (withCode) bulk_g2s(smem + (size_t)(i % kStreamSlots) * g.slotBytes + g.xBytes, code + p * sz + (long long)y0 * nx, cb, bar);
+    bulk_g2s(slotBase(i), x + p * sz + (long long)ya * nx, xb, bar);
+    if (withCode) bulk_g2s(slotBase(i) + g.xBytes, code + p * sz + (long long)y0 * nx, cb, bar);
   };
   int issued = 0;
   if (threadIdx.x == 0)
     for (; issued < kStreamSlots && issued < np; issued++) issue(issued);
+  // this thread's quads of a plane: rows and x offsets fixed for the CTA
   const int nq4 = nx >> 2, quads = ty * nq4;
+  int nmine = 0, ro[kStreamQuads], co[kStreamQuads], go[kStreamQuads];
+  for (int e = threadIdx.x; e < quads && nmine < kStreamQuads; e += blockDim.x) {
+    const int r = e / nq4, xq = e - r * nq4;
+    ro[nmine] = (y0 + r - ya) * nx + 4 * xq;  // the quad in a slot's x rows
+    co[nmine] = r * nx + 4 * xq;              // its codes in the slot's code rows
+    go[nmine] = (y0 + r) * nq4 + xq;          // its float4 index within a plane
+    nmine++;
+  }
   const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
   const float4* A4 = reinterpret_cast<const float4*>(A0f);
   float4* y4 = reinterpret_cast<float4*>(y);
   FSum acc;
   bool ok = true;
   int waited = 0;  // ring indices below this one have been waited for
-  for (int z = zs; z < ze && ok; z++) {
+  for (int z = zs; z < ze; z++) {
     const int ic = z - p0;
     for (; waited <= ic + 1; waited++)
       if (!mbar_wait(&bars[waited % kStreamSlots], (unsigned)(waited / kStreamSlots) & 1u, kStreamWaitNs)) ok = false;
@@ -558,30 +566,32 @@ __global__ void __launch_bounds__(256, 3) k_pcg_spmv_stream(Dims d, StreamGeom g
       ok = false;
       break;
     }
-    const float* xm = slotX(ic - 1);
-    const float* xcen = slotX(ic);
-    const float* xp = slotX(ic + 1);
-    const code_t* cs = slotC(ic);
-    for (int e = threadIdx.x; e < quads; e += blockDim.x) {
-      const int r = e / nq4, xq = e - r * nq4;
-      const int yy = y0 + r;
-      const int ro = (yy - ya) * nx + 4 * xq;  // the quad in the slot's x rows
-      SpmvQuad Q;
-      Q.cw = *reinterpret_cast<const uint2*>(cs + r * nx + 4 * xq);
-      const int any = (int)((Q.cw.x | Q.cw.y | (Q.cw.x >> 16) | (Q.cw.y >> 16)) & 0xffffu);
-      Q.xc = *reinterpret_cast<const float4*>(xcen + ro);
-      Q.ylo = (any & kLowY) ? *reinterpret_cast<const float4*>(xcen + ro - nx) : z4;
-      Q.yhi = (any & kHighY) ? *reinterpret_cast<const float4*>(xcen + ro + nx) : z4;
-      Q.zlo = (any & kLowZ) ? *reinterpret_cast<const float4*>(xm + ro) : z4;
-      Q.zhi = (any & kHighZ) ? *reinterpret_cast<const float4*>(xp + ro) : z4;
-      Q.xl = (Q.cw.x & kLowX) ? xcen[ro - 1] : 0.f;
-      Q.xr = ((Q.cw.y >> 16) & kHighX) ? xcen[ro + 4] : 0.f;
-      const long long q = ((long long)z * sz + (long long)yy * nx) / 4 + xq;
-      if (A0f) Q.A0 = __ldg(A4 + q);
-      else
-        Q.A0 = make_float4((float)(Q.cw.x & 7), (float)((Q.cw.x >> 16) & 7), (float)(Q.cw.y & 7),
-                           (float)((Q.cw.y >> 16) & 7));
-      y4[q] = spmv_apply(Q, acc);
+    const float* xm = reinterpret_cast<const float*>(slotBase(ic - 1));
+    const float* xcen = reinterpret_cast<const float*>(slotBase(ic));
+    const float* xp = reinterpret_cast<const float*>(slotBase(ic + 1));
+    const code_t* cs = reinterpret_cast<const code_t*>(slotBase(ic) + g.xBytes);
+    const long long planeQ = ((long long)z * sz) >> 2;
+#pragma unroll
+    for (int u = 0; u < kStreamQuads; u++) {
+      if (u < nmine) {
+        const int o = ro[u];
+        SpmvQuad Q;
+        Q.cw = *reinterpret_cast<const uint2*>(cs + co[u]);
+        const int any = (int)((Q.cw.x | Q.cw.y | (Q.cw.x >> 16) | (Q.cw.y >> 16)) & 0xffffu);
+        Q.xc = *reinterpret_cast<const float4*>(xcen + o);
+        Q.ylo = (any & kLowY) ? *reinterpret_cast<const float4*>(xcen + o - nx) : z4;
+        Q.yhi = (any & kHighY) ? *reinterpret_cast<const float4*>(xcen + o + nx) : z4;
+        Q.zlo = (any & kLowZ) ? *reinterpret_cast<const float4*>(xm + o) : z4;
+        Q.zhi = (any & kHighZ) ? *reinterpret_cast<const float4*>(xp + o) : z4;
+        Q.xl = (Q.cw.x & kLowX) ? xcen[o - 1] : 0.f;
+        Q.xr = ((Q.cw.y >> 16) & kHighX) ? xcen[o + 4] : 0.f;
+        const long long q = planeQ + go[u];
+        if (A0f) Q.A0 = __ldg(A4 + q);
+        else
+          Q.A0 = make_float4((float)(Q.cw.x & 7), (float)((Q.cw.x >> 16) & 7), (float)(Q.cw.y & 7),
+                             (float)((Q.cw.y >> 16) & 7));
+        y4[q] = spmv_apply(Q, acc);
+      }
     }
     __syncthreads();  // the slot of plane z-1 is read for the last time
     if (threadIdx.x == 0 && issued < np) issue(issued++);
@@ -613,17 +623,17 @@ __global__ void __launch_bounds__(256, 3) k_pcg_spmv_stream(Dims d, StreamGeom g
 }
 
 // Slab height and z run for the streamed SpMV, or false where it does not
-// apply (2D, rows not a multiple of 8 cells, rows too long for a slab of 4).
+// apply (2D, rows not a multiple of 8 cells, rows too long for a slab of 2).
 static bool stream_geom(const Dims& d, int maxBlocks, int sms, StreamGeom* g, dim3* grid) {
   if (!d.is3d || d.nx % 8 != 0) return false;
   int TY = 16;
-  while (TY >= 4 && (size_t)(TY + 2) * d.nx * 4 + (size_t)TY * d.nx * 2 > (size_t)kStreamSlotBudget) TY--;
-  if (TY < 4) return false;
+  while (TY >= 2 && (size_t)(TY + 2) * d.nx * 4 + (size_t)TY * d.nx * 2 > (size_t)kStreamSlotBudget) TY--;
+  if (TY < 2 || (size_t)TY * (d.nx / 4) > (size_t)kStreamQuads * 256) return false;
   g->TY = TY;
   g->xBytes = (unsigned)((TY + 2) * d.nx * 4);
   g->slotBytes = (unsigned)(((size_t)g->xBytes + (size_t)TY * d.nx * 2 + 127) / 128 * 128);
   const int slabs = (d.ny + TY - 1) / TY;
-  const int target = std::min(maxBlocks, 3 * sms);
+  const int target = std::min(maxBlocks, 2 * sms);
   // at least 6 planes per CTA: the two halo planes of a run cost extra reads
   int chunks = std::max(1, std::min(std::max(1, d.nz / 6), target / std::max(1, slabs)));
   g->zc = (d.nz + chunks - 1) / chunks;

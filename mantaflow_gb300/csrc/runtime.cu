@@ -316,6 +316,7 @@ extern "C" int mg_shutdown(void) {
   std::vector<mg_solver> all(g_ctx.solvers.begin(), g_ctx.solvers.end());
   for (auto s : all) mg_solver_destroy(s);
   noalloc_forget();
+  noise_release();
   g_ctx.init = false;
   g_ctx.device = -1;
   return MG_OK;
@@ -473,6 +474,21 @@ extern "C" int mg_grid_create(mg_solver s, int kind, mg_grid* out) {
   CK(cudaMemsetAsync(g->data, 0, bytes, s->stream));
   s->grids.insert(g);
   *out = g;
+  return MG_OK;
+}
+
+extern "C" int mg_solver_size(mg_solver s, int* nx, int* ny, int* nz) {
+  if (!valid_solver(s)) return fail(MG_ERR_ARG, "mg_solver_size: invalid solver");
+  if (nx) *nx = s->d.nx;
+  if (ny) *ny = s->d.ny;
+  if (nz) *nz = s->d.nz;
+  return MG_OK;
+}
+
+extern "C" int mg_grid_device(mg_grid g, void** data, void** stream) {
+  NEED_GRID(g, "mg_grid_device");
+  if (data) *data = g->data;
+  if (stream) *stream = (void*)g->s->stream;
   return MG_OK;
 }
 

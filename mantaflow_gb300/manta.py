@@ -372,6 +372,62 @@ class Cylinder(Shape):
         check(_lib.load().mg_shape_cylinder_apply(grid._h, fptr(self.center), float(self.radius), fptr(self.z),
                                                   fptr(v), iv, _h(respectFlags)))
 
+    def computeLevelset(self):
+        phi = LevelsetGrid(self._parent)
+        check(_lib.load().mg_shape_cylinder_levelset(phi._h, fptr(self.center), float(self.radius), fptr(self.z)))
+        return phi
+
+
+# -------------------------------------------------------------- noise field
+class NoiseField:
+    """WaveletNoiseField (source/noisefield.h:27-98), Python name NoiseField:
+    the shared 128^3 wavelet noise tile (generated on first use, kept on the
+    device) sampled with the properties below."""
+
+    def __init__(self, parent, fixedSeed=-1, loadFromFile=False):
+        self._parent = parent
+        h = C.c_void_p()
+        check(_lib.load().mg_noise_create(parent._h, int(fixedSeed), C.byref(h)))
+        self._h = h
+        self.posOffset = vec3(0.0)
+        self.posScale = vec3(1.0)
+        self.valOffset = 0.0
+        self.valScale = 1.0
+        self.clamp = False
+        self.clampNeg = 0.0
+        self.clampPos = 1.0
+        self.timeAnim = 0.0
+
+    def _sync(self):
+        p = _lib.NoiseParams()
+        p.posOffset[:] = [float(x) for x in _vec(self.posOffset)]
+        p.posScale[:] = [float(x) for x in _vec(self.posScale)]
+        p.valOffset, p.valScale = float(self.valOffset), float(self.valScale)
+        p.clamp, p.clampNeg, p.clampPos = int(bool(self.clamp)), float(self.clampNeg), float(self.clampPos)
+        p.timeAnim = float(self.timeAnim)
+        check(_lib.load().mg_noise_set_params(self._h, C.byref(p)))
+
+    def seedOffset(self):
+        out = (C.c_float * 3)()
+        check(_lib.load().mg_noise_seed_offset(self._h, out))
+        return vec3(out[0], out[1], out[2])
+
+    def evaluateGrid(self, grid):
+        """grid(i,j,k) = evaluate(Vec3(i,j,k)) at the solver's time"""
+        self._sync()
+        check(_lib.load().mg_noise_evaluate_grid(self._h, grid._h, float(self._parent.timeTotal)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            try:
+                _lib._lib.mg_noise_destroy(h)
+            except Exception:
+                pass
+
+
+WaveletNoiseField = NoiseField
+
 
 # ------------------------------------------------------------- numpy bridge
 # plugin/numpyconvert.cpp:145-182
@@ -449,6 +505,14 @@ def resetOutflow(flags, phi=None, parts=None, real=None, index=None, indexSys=No
 def extrapolateMACSimple(flags, vel, distance=4, phiObs=None, intoObs=False):
     """fastmarch.cpp:337-375"""
     check(_lib.load().mg_extrapolate_mac_simple(flags._h, vel._h, int(distance), _h(phiObs), int(bool(intoObs))))
+
+
+def densityInflow(flags, density, noise, shape, scale=1.0, sigma=0.0):
+    """plugin/initplugins.cpp:38-43"""
+    sdf = shape.computeLevelset()
+    noise._sync()
+    check(_lib.load().mg_density_inflow(flags._h, density._h, noise._h, sdf._h, float(scale), float(sigma),
+                                        float(noise._parent.timeTotal)))
 
 
 def extrapolateLsSimple(phi, distance=4, inside=False):

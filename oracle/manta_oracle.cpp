@@ -2104,3 +2104,210 @@ void og_box_apply(og_dims d, og_real* grid, og_real p0x, og_real p0y, og_real p0
 void og_join_real(ll n, og_real* a, const og_real* b, int keepMax) {
   for (ll i = 0; i < n; i++) a[i] = keepMax ? fmaxf_(a[i], b[i]) : fminf_(a[i], b[i]);
 }
+
+/* ------------------------------------------------------------------ noise */
+/* MTRand (util/randomstream.h): MT19937 with the reference's seeding,
+ * tempering and double conversions; RandomStream's getRandNorm and
+ * getVec3Norm on top. */
+typedef struct {
+  unsigned int st[624];
+  int left, next;
+} og_mt;
+
+static void og_mt_reload(og_mt* m) {
+  unsigned int* s = m->st;
+  for (int i = 0; i < 624; i++) {
+    const unsigned int y = (s[i] & 0x80000000u) | (s[(i + 1) % 624] & 0x7fffffffu);
+    s[i] = s[(i + 397) % 624] ^ (y >> 1) ^ ((s[(i + 1) % 624] & 1u) ? 0x9908b0dfu : 0u);
+  }
+  m->left = 624;
+  m->next = 0;
+}
+static void og_mt_seed(og_mt* m, unsigned int seed) {
+  m->st[0] = seed;
+  for (int i = 1; i < 624; i++) m->st[i] = 1812433253u * (m->st[i - 1] ^ (m->st[i - 1] >> 30)) + (unsigned int)i;
+  og_mt_reload(m);
+}
+static unsigned int og_mt_int(og_mt* m) {
+  if (m->left == 0) og_mt_reload(m);
+  m->left--;
+  unsigned int y = m->st[m->next++];
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  return y ^ (y >> 18);
+}
+static double og_mt_rand(og_mt* m) { return (double)og_mt_int(m) * (1.0 / 4294967295.0); }
+static double og_mt_norm(og_mt* m, double mean, double variance) {
+  const double u = ((double)og_mt_int(m) + 0.5) * (1.0 / 4294967296.0);
+  const double r = sqrt(-2.0 * log(1.0 - u)) * variance;
+  const double phi = 2.0 * 3.14159265358979323846264338328 * ((double)og_mt_int(m) * (1.0 / 4294967296.0));
+  return mean + r * cos(phi);
+}
+
+/* WaveletNoiseField::generateTile (noisefield.cpp:94-190) for the float build:
+ * 3 tiles of 128^3 normal noise, minus their down/up-sampled version along x,
+ * y and z (periodic), plus the result read at a (65,65,65) offset. */
+static const float og_aco[32] = {
+    0.000334f, -0.001528f, 0.000410f, 0.003545f, -0.000938f, -0.008233f, 0.002172f, 0.019120f,
+    -0.005040f, -0.044412f, 0.011655f, 0.103311f, -0.025936f, -0.243780f, 0.033979f, 0.655340f,
+    0.655340f, 0.033979f, -0.243780f, -0.025936f, 0.103311f, 0.011655f, -0.044412f, -0.005040f,
+    0.019120f, 0.002172f, -0.008233f, -0.000938f, 0.003546f, 0.000410f, -0.001528f, 0.000334f};
+static const float og_pco[4] = {0.25f, 0.75f, 0.75f, 0.25f};
+
+static void og_noise_down(const float* from, float* to, int n, int stride) {
+  for (int i = 0; i < n / 2; i++) {
+    float acc = 0.f;
+    for (int k = 2 * i - 16; k < 2 * i + 16; k++) acc += og_aco[16 + k - 2 * i] * from[(k & 127) * stride];
+    to[i * stride] = acc;
+  }
+}
+static void og_noise_up(const float* from, float* to, int n, int stride) {
+  for (int i = 0; i < n; i++) {
+    float acc = 0.f;
+    for (int k = i / 2 - 1; k < i / 2 + 3; k++) {
+      int mm = k % (n / 2);
+      if (mm < 0) mm += n / 2;
+      acc = (float)((double)acc + 0.5 * (double)og_pco[1 + k - i / 2] * (double)from[mm * stride]);
+    }
+    to[i * stride] = acc;
+  }
+}
+
+void og_noise_tile(float* noise) {
+  const int n = 128, n3 = n * n * n;
+  og_mt mt;
+  og_mt_seed(&mt, 13322223u);
+  for (int i = 0; i < 3 * n3; i++) noise[i] = (float)og_mt_norm(&mt, 0.0, 1.0);
+  float* t1 = (float*)calloc((size_t)3 * n3, sizeof(float));
+  float* t2 = (float*)calloc((size_t)3 * n3, sizeof(float));
+  for (int tile = 0; tile < 3; tile++) {
+    for (int iy = 0; iy < n; iy++)
+      for (int iz = 0; iz < n; iz++) {
+        const int i = iy * n + iz * n * n + tile * n3;
+        og_noise_down(noise + i, t1 + i, n, 1);
+        og_noise_up(t1 + i, t2 + i, n, 1);
+      }
+    for (int ix = 0; ix < n; ix++)
+      for (int iz = 0; iz < n; iz++) {
+        const int i = ix + iz * n * n + tile * n3;
+        og_noise_down(t2 + i, t1 + i, n, n);
+        og_noise_up(t1 + i, t2 + i, n, n);
+      }
+    for (int ix = 0; ix < n; ix++)
+      for (int iy = 0; iy < n; iy++) {
+        const int i = ix + iy * n + tile * n3;
+        og_noise_down(t2 + i, t1 + i, n, n * n);
+        og_noise_up(t1 + i, t2 + i, n, n * n);
+      }
+  }
+  for (int i = 0; i < 3 * n3; i++) noise[i] -= t2[i];
+  const int off = 65;
+  int c = 0;
+  for (int tile = 0; tile < 3; tile++)
+    for (int ix = 0; ix < n; ix++)
+      for (int iy = 0; iy < n; iy++)
+        for (int iz = 0; iz < n; iz++)
+          t1[c++] = noise[((ix + off) & 127) + ((iy + off) & 127) * n + ((iz + off) & 127) * n * n + tile * n3];
+  for (int i = 0; i < 3 * n3; i++) noise[i] += t1[i];
+  free(t1);
+  free(t2);
+}
+
+/* WaveletNoiseField(parent, fixedSeed): mSeedOffset = normalized getVec3 of
+ * RandomStream(fixedSeed) (noisefield.cpp:61-78; seed -1 -> 13322223 + 123) */
+void og_noise_seed_offset(int fixedSeed, float* out) {
+  og_mt mt;
+  og_mt_seed(&mt, (unsigned int)(fixedSeed == -1 ? 13322223 + 123 : fixedSeed));
+  float v[3];
+  for (int c = 0; c < 3; c++) v[c] = (float)og_mt_rand(&mt);
+  const float l = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  if (fabs((double)l - 1.) < (double)(1e-6f * 1e-6f)) {
+  } else if (l > 1e-6f * 1e-6f) {
+    const float norm = sqrtf(l);
+    const float s = (float)(1. / (double)norm);
+    for (int c = 0; c < 3; c++) v[c] = v[c] * s;
+  } else {
+    v[0] = v[1] = v[2] = 0.f;
+  }
+  for (int c = 0; c < 3; c++) out[c] = v[c];
+}
+
+/* WaveletNoiseField::evaluate (noisefield.h:332-357) with WNoise (:155-196):
+ * quadratic B-spline weights around ceil(p - 0.5), 27 tile samples summed x
+ * fastest, then z. */
+static float og_wnoise(const float* p, const float* data) {
+  float w[3][3];
+  int mid[3];
+  for (int a = 0; a < 3; a++) {
+    mid[a] = (int)ceilf(p[a] - 0.5f);
+    const float t = (float)mid[a] - (p[a] - 0.5f);
+    w[a][0] = t * t * 0.5f;
+    w[a][2] = (1.f - t) * (1.f - t) * 0.5f;
+    w[a][1] = 1.f - w[a][0] - w[a][2];
+  }
+  float result = 0.f;
+  for (int z = -1; z <= 1; z++)
+    for (int y = -1; y <= 1; y++)
+      for (int x = -1; x <= 1; x++) {
+        float weight = 1.0f;
+        weight *= w[0][x + 1];
+        weight *= w[1][y + 1];
+        weight *= w[2][z + 1];
+        const int xC = (mid[0] + x) & 127, yC = (mid[1] + y) & 127, zC = (mid[2] + z) & 127;
+        result += weight * data[(zC * 128 + yC) * 128 + xC];
+      }
+  return result;
+}
+
+float og_noise_evaluate(const og_noise_params* q, const float* tile, float x, float y, float z) {
+  float p[3] = {x, y, z};
+  p[0] *= q->gsInv[0];
+  p[1] *= q->gsInv[1];
+  p[2] *= q->gsInv[2];
+  for (int c = 0; c < 3; c++) p[c] += q->seedOffset[c];
+  for (int c = 0; c < 3; c++) p[c] += q->timeOffset;
+  for (int c = 0; c < 3; c++) p[c] *= q->posScale[c];
+  for (int c = 0; c < 3; c++) p[c] += q->posOffset[c];
+  float v = og_wnoise(p, tile);
+  v += q->valOffset;
+  v *= q->valScale;
+  if (q->clamp) {
+    if (v < q->clampNeg) v = q->clampNeg;
+    if (v > q->clampPos) v = q->clampPos;
+  }
+  return v;
+}
+
+/* CylinderSDF (shapes.cpp:367-385), the Cylinder's levelset */
+void og_cylinder_sdf(og_dims d, float* phi, const float* center, float radius, const float* zaxis, float maxz) {
+  for (int k = 0; k < d.nz; k++)
+    for (int j = 0; j < d.ny; j++)
+      for (int i = 0; i < d.nx; i++) {
+        const float px = (float)(i + 0.5) - center[0], py = (float)(j + 0.5) - center[1], pz = (float)(k + 0.5) - center[2];
+        const float z = fabsf(px * zaxis[0] + py * zaxis[1] + pz * zaxis[2]);
+        const float r = sqrtf((px * px + py * py + pz * pz) - z * z);
+        float v;
+        if (z < maxz) v = r < radius ? fmaxf_(r - radius, z - maxz) : r - radius;
+        else if (r < radius) v = fabsf(z - maxz);
+        else v = sqrtf((z - maxz) * (z - maxz) + (r - radius) * (r - radius));
+        phi[IX(d, i, j, k)] = v;
+      }
+}
+
+/* densityInflow (initplugins.cpp:38-43) with KnApplyNoiseInfl (:27-36) */
+void og_density_inflow(og_dims d, const int* flags, float* density, const float* sdf, const og_noise_params* q,
+                       const float* tile, float scale, float sigma) {
+  for (int k = 0; k < d.nz; k++)
+    for (int j = 0; j < d.ny; j++)
+      for (int i = 0; i < d.nx; i++) {
+        const ll idx = IX(d, i, j, k);
+        if (!isF(flags, idx) || sdf[idx] > sigma) continue;
+        double f = 1.0 - 0.5 / (double)sigma * (double)(sdf[idx] + sigma);
+        if (f < 0.0) f = 0.0;
+        else if (f > 1.0) f = 1.0;
+        const float factor = (float)f;
+        const float target = og_noise_evaluate(q, tile, (float)i, (float)j, (float)k) * scale * factor;
+        if (density[idx] < target) density[idx] = target;
+      }
+}

@@ -162,6 +162,22 @@ og_real og_get_max_abs(long long n, const og_real* a);
 void og_set_num_threads(int n);
 int og_get_num_threads(void);
 
+/* wavelet noise (noisefield.h/.cpp), float build */
+typedef struct {
+  float gsInv[3];      /* 1/max(grid size); z: 1 in 2D */
+  float seedOffset[3]; /* mSeedOffset */
+  float timeOffset;    /* getTime(): solver time * dx * timeAnim */
+  float posScale[3], posOffset[3];
+  float valOffset, valScale, clampNeg, clampPos;
+  int clamp;
+} og_noise_params;
+void og_noise_tile(float* tile3x128cubed);
+void og_noise_seed_offset(int fixedSeed, float* out3);
+float og_noise_evaluate(const og_noise_params* q, const float* tile, float x, float y, float z);
+void og_cylinder_sdf(og_dims d, float* phi, const float* center, float radius, const float* zaxis, float maxz);
+void og_density_inflow(og_dims d, const int* flags, float* density, const float* sdf, const og_noise_params* q,
+                       const float* tile, float scale, float sigma);
+
 #ifdef __cplusplus
 }
 #endif

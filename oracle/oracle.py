@@ -26,6 +26,12 @@ class Dims(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("is3d", C.c_int)]
 
 
+class NoiseParams(C.Structure):
+    _fields_ = [("gsInv", C.c_float * 3), ("seedOffset", C.c_float * 3), ("timeOffset", C.c_float),
+                ("posScale", C.c_float * 3), ("posOffset", C.c_float * 3), ("valOffset", C.c_float),
+                ("valScale", C.c_float), ("clampNeg", C.c_float), ("clampPos", C.c_float), ("clamp", C.c_int)]
+
+
 def _structs(R):
     class PressureParams(C.Structure):
         _fields_ = [("cgAccuracy", R), ("gfClamp", R), ("cgMaxIterFac", R),
@@ -111,6 +117,14 @@ def lib(dtype=np.float32):
         L.og_join_real.argtypes = [C.c_longlong, fp, fp, I]
         L.og_get_max_abs.argtypes = [C.c_longlong, fp]
         L.og_get_max_abs.restype = F
+        if t is np.float32:
+            f32 = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+            L.og_noise_tile.argtypes = [f32]
+            L.og_noise_seed_offset.argtypes = [I, f32]
+            L.og_noise_evaluate.argtypes = [C.POINTER(NoiseParams), f32, C.c_float, C.c_float, C.c_float]
+            L.og_noise_evaluate.restype = C.c_float
+            L.og_cylinder_sdf.argtypes = [Dims, f32, f32, C.c_float, f32, C.c_float]
+            L.og_density_inflow.argtypes = [Dims, ip, f32, f32, C.POINTER(NoiseParams), f32, C.c_float, C.c_float]
         L.og_set_num_threads.argtypes = [I]
         L.og_get_num_threads.restype = I
         _libs[t] = L
@@ -158,6 +172,47 @@ def extrapolate_mac_simple(flags, vel, distance=4, intoObs=False):
 
 def extrapolate_ls_simple(phi, distance=4, inside=False):
     lib(phi.dtype).og_extrapolate_ls_simple(dims(phi.shape), phi, int(distance), int(bool(inside)))
+
+
+_TILE = None
+
+
+def noise_tile():
+    """WaveletNoiseField's 3 x 128^3 tile (generated once per process)"""
+    global _TILE
+    if _TILE is None:
+        t = np.zeros(3 * 128 ** 3, np.float32)
+        lib().og_noise_tile(t)
+        _TILE = t
+    return _TILE
+
+
+def noise_params(shape, fixedSeed=-1, time=0.0, posScale=(1, 1, 1), posOffset=(0, 0, 0), valOffset=0.0,
+                 valScale=1.0, clamp=False, clampNeg=0.0, clampPos=1.0, timeAnim=0.0):
+    """the evaluate() parameters of a NoiseField on a grid of shape (nz, ny, nx)"""
+    nz, ny, nx = shape[:3]
+    q = NoiseParams()
+    scale = np.float32(1.0 / max(nx, ny, nz))
+    q.gsInv[:] = [scale, scale, scale if nz > 1 else np.float32(1.0)]
+    so = np.zeros(3, np.float32)
+    lib().og_noise_seed_offset(int(fixedSeed), so)
+    q.seedOffset[:] = list(so)
+    dx = np.float32(1.0 / max(nx, ny, nz))
+    q.timeOffset = float(np.float32(np.float32(time) * dx) * np.float32(timeAnim))
+    q.posScale[:] = [float(np.float32(v)) for v in posScale]
+    q.posOffset[:] = [float(np.float32(v)) for v in posOffset]
+    q.valOffset, q.valScale = float(valOffset), float(valScale)
+    q.clamp, q.clampNeg, q.clampPos = int(bool(clamp)), float(clampNeg), float(clampPos)
+    return q
+
+
+def cylinder_sdf(phi, center, radius, zaxis, maxz):
+    lib().og_cylinder_sdf(dims(phi.shape), phi, np.asarray(center, np.float32), float(radius),
+                          np.asarray(zaxis, np.float32), float(maxz))
+
+
+def density_inflow(flags, density, sdf, q, scale=1.0, sigma=0.0):
+    lib().og_density_inflow(dims(flags.shape), flags, density, sdf, C.byref(q), noise_tile(), float(scale), float(sigma))
 
 
 def params(cgAccuracy=1e-3, gfClamp=1e-4, cgMaxIterFac=1.5, preconditioner=PC_MIC, enforceCompatibility=False,
