@@ -337,6 +337,11 @@ int mg_batch_create(int count, const int* sizes, const float* gravity, const uns
 int mg_batch_destroy(mg_batch b);
 /* solvePressure's cgAccuracy (1e-3) and cgMaxIterFac (1.5) */
 int mg_batch_set_solver(mg_batch b, float cgAccuracy, float cgMaxIterFac);
+/* MG_PC_MIC (the default): 3D scenes precondition with MIC(0), whose
+ * dataflow sweeps run over the tiles of all 3D scenes in one launch; 2D
+ * scenes run GridCg without a preconditioner, as the reference does in 2D.
+ * MG_PC_NONE: no scene is preconditioned. */
+int mg_batch_set_preconditioner(mg_batch b, int preconditioner);
 /* one plume step of every scene; stats may be NULL */
 int mg_batch_step(mg_batch b, mg_batch_stats* stats);
 int mg_batch_scene_iterations(mg_batch b, int scene, int* iterations, float* resNorm);

@@ -18,7 +18,9 @@ DENSITY, VELOCITY, PRESSURE, FLAGS, SOURCE = 0, 1, 2, 3, 4
 
 
 class BatchedPlumes:
-    def __init__(self, sizes, gravity, seeds, dt=1.0, cgAccuracy=1e-3, cgMaxIterFac=1.5):
+    def __init__(self, sizes, gravity, seeds, dt=1.0, cgAccuracy=1e-3, cgMaxIterFac=1.5, preconditioner=1):
+        """preconditioner: 1 (PcMIC, the default: MIC(0) for the 3D scenes, none
+        in 2D as the reference's GridCg) or 0 (no scene preconditioned)"""
         ensure_init()
         self._L = _lib.load()
         sizes = [tuple(int(v) for v in s) + ((1,) if len(s) == 2 else ()) for s in sizes]
@@ -32,6 +34,7 @@ class BatchedPlumes:
         check(self._L.mg_batch_create(n, sz, gr, sd, float(dt), C.byref(h)))
         self._h = h
         check(self._L.mg_batch_set_solver(h, float(cgAccuracy), float(cgMaxIterFac)))
+        check(self._L.mg_batch_set_preconditioner(h, int(preconditioner)))
         self.steps = 0
 
     def __len__(self):

@@ -52,12 +52,20 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int tiles_of(int nx, int ny, int nz, int rows) { return ((nx + kBTX - 1) / kBTX) * ((ny + rows - 1) / rows) * nz; }
 
-// bytes of one scene's device block
+constexpr int kMicTile = 16;  // edge of the MIC dataflow tiles
+int mic_tiles(int n) { return (n + kMicTile - 1) / kMicTile; }
+
+// bytes of one scene's device block (3D scenes also hold the MIC diagonal
+// and the face words of the dataflow sweeps)
 size_t scene_bytes(int nx, int ny, int nz) {
   const size_t n = (size_t)nx * ny * nz;
-  return align256(n * sizeof(int)) + 2 * align256(3 * n * sizeof(float)) + 2 * align256(n * sizeof(float)) +
-         align256(4 * n * sizeof(float)) + 6 * align256(n * sizeof(float)) + align256(n * sizeof(code_t)) +
-         align256(2 * (size_t)tiles_of(nx, ny, nz, kBTY) * sizeof(double));
+  size_t b = align256(n * sizeof(int)) + 2 * align256(3 * n * sizeof(float)) + 2 * align256(n * sizeof(float)) +
+             align256(4 * n * sizeof(float)) + 6 * align256(n * sizeof(float)) + align256(n * sizeof(code_t)) +
+             align256(2 * (size_t)tiles_of(nx, ny, nz, kBTY) * sizeof(double));
+  if (nz > 1)
+    b += align256(n * sizeof(float)) +
+         align256(mic_flow_face_words(mic_tiles(nx) * mic_tiles(ny) * mic_tiles(nz)) * sizeof(unsigned long long));
+  return b;
 }
 
 struct SceneRec {
@@ -84,6 +92,20 @@ struct Engine {
   std::vector<CgScalars> hSc;
   std::vector<BScene> hScenes;
   // tiles: 32 x 8 for the stages; 32 x 8R (R = 1 << k) for the CG sweeps
+  // MIC(0) for 3D scenes (the reference's PcMIC; 2D scenes run without a
+  // preconditioner, as GridCg does in 2D): flow table, dispatch order
+  bool micFor3D = true;
+  std::vector<FlowScene> hFlow;
+  std::vector<int2> hOrder2;
+  std::vector<int> hMicScene;
+  FlowScene* dFlow = nullptr;
+  size_t flowCap = 0;
+  int2* dOrder2 = nullptr;
+  size_t orderCap = 0;
+  int* dMicScene = nullptr;
+  size_t micSceneCap = 0;
+  int* dMicCounter = nullptr;  // [0] tile counter, [1] wait error
+  unsigned int micEpoch = 0;
   std::vector<BTile> tiles1;
   std::vector<BTile> tilesR[4];
   std::vector<int> startR[4];
@@ -109,6 +131,10 @@ struct Engine {
     cudaFree(dTiles);
     cudaFree(dActive);
     cudaFree(dDone);
+    cudaFree(dFlow);
+    cudaFree(dOrder2);
+    cudaFree(dMicScene);
+    cudaFree(dMicCounter);
     if (ev[0]) cudaEventDestroy(ev[0]);
     if (ev[1]) cudaEventDestroy(ev[1]);
     if (stream) cudaStreamDestroy(stream);
@@ -121,6 +147,8 @@ int engine_init(Engine& e, float dt) {
   CKB(cudaEventCreate(&e.ev[0]));
   CKB(cudaEventCreate(&e.ev[1]));
   CKB(cudaMalloc(&e.dDone, sizeof(int)));
+  CKB(cudaMalloc(&e.dMicCounter, 2 * sizeof(int)));
+  CKB(cudaMemset(e.dMicCounter, 0, 2 * sizeof(int)));
   return MG_OK;
 }
 
@@ -189,6 +217,16 @@ int scene_add(Engine& e, int nx, int ny, int nz, const float* gravity, unsigned 
   s.code = (code_t*)take(n * sizeof(code_t));
   s.ntiles = tiles_of(nx, ny, nz, kBTY);
   s.part = (double*)take(2 * (size_t)s.ntiles * sizeof(double));
+  s.P = nullptr;
+  s.face = nullptr;
+  s.tx = mic_tiles(nx);
+  s.ty = mic_tiles(ny);
+  s.tz = mic_tiles(nz);
+  if (nz > 1) {
+    s.P = (float*)take(n * sizeof(float));
+    s.face = (unsigned long long*)take(mic_flow_face_words(s.tx * s.ty * s.tz) * sizeof(unsigned long long));
+  }
+  s.mic = (nz > 1 && e.micFor3D) ? 1 : 0;
   s.sc = nullptr;
   s.dt = e.dt;
   s.seed = seed;
@@ -285,6 +323,51 @@ int engine_tables(Engine& e) {
     }
   }
   for (int k = 0; k < 4; k++) e.startR[k].push_back((int)e.tilesR[k].size());
+  // MIC scenes: one FlowScene each; tiles ordered by wavefront level (a+b+c
+  // within the scene) and then scene, so a tile comes after every tile it
+  // waits for
+  e.hFlow.clear();
+  e.hOrder2.clear();
+  e.hMicScene.clear();
+  int maxLevel = 0;
+  for (size_t q = 0; q < nm; q++) {
+    const BScene& b = e.hScenes[q];
+    if (!b.mic) continue;
+    FlowScene f;
+    f.d = b.d;
+    f.code = b.code;
+    f.A0f = nullptr;
+    f.P = b.P;
+    f.r = b.res;
+    f.z = b.tmp;
+    f.part = b.part;
+    f.sc = b.sc;
+    f.tx = b.tx;
+    f.ty = b.ty;
+    f.tz = b.tz;
+    f.face = b.face;
+    e.hFlow.push_back(f);
+    e.hMicScene.push_back((int)q);
+    maxLevel = std::max(maxLevel, b.tx + b.ty + b.tz - 3);
+  }
+  for (int L = 0; L <= maxLevel; L++)
+    for (size_t m = 0; m < e.hFlow.size(); m++) {
+      const FlowScene& f = e.hFlow[m];
+      for (int c = 0; c < f.tz; c++)
+        for (int b = 0; b < f.ty; b++) {
+          const int a = L - b - c;
+          if (a >= 0 && a < f.tx) e.hOrder2.push_back(make_int2((int)m, a + f.tx * (b + f.ty * c)));
+        }
+    }
+  if (!e.hFlow.empty()) {
+    if (ensure_cap(&e.dFlow, &e.flowCap, e.hFlow.size()) || ensure_cap(&e.dOrder2, &e.orderCap, e.hOrder2.size()) ||
+        ensure_cap(&e.dMicScene, &e.micSceneCap, e.hMicScene.size()))
+      return MG_ERR_CUDA;
+    CKB(cudaMemcpyAsync(e.dFlow, e.hFlow.data(), sizeof(FlowScene) * e.hFlow.size(), cudaMemcpyHostToDevice, e.stream));
+    CKB(cudaMemcpyAsync(e.dOrder2, e.hOrder2.data(), sizeof(int2) * e.hOrder2.size(), cudaMemcpyHostToDevice, e.stream));
+    CKB(cudaMemcpyAsync(e.dMicScene, e.hMicScene.data(), sizeof(int) * e.hMicScene.size(), cudaMemcpyHostToDevice,
+                        e.stream));
+  }
   if (ensure_cap(&e.dTiles, &e.tilesCap, e.tiles1.size()) || ensure_cap(&e.dActive, &e.activeCap, e.tiles1.size()))
     return MG_ERR_CUDA;
   CKB(cudaMemcpyAsync(e.dTiles, e.tiles1.data(), sizeof(BTile) * e.tiles1.size(), cudaMemcpyHostToDevice, e.stream));
@@ -303,14 +386,16 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
   launch_b_inflow(e.dTiles, nt, e.dScenes, cur, st);
   launch_b_advect_velocity(e.dTiles, nt, e.dScenes, cur, st);
   launch_b_forces(e.dTiles, nt, e.dScenes, nxt, st);
-  // GridCg setup of every scene: PcNone with the reference's 2D iteration
-  // limit, (int)(cgMaxIterFac * max size) * 4 (pressure.cpp:407-409)
+  // GridCg setup of every scene (pressure.cpp:407-419): PcMIC in 3D with
+  // (int)(cgMaxIterFac * max size) iterations at most; in 2D GridCg drops
+  // MIC (conjugategrad.cpp:315-321) and allows 4 times as many
   int maxIterAll = 0;
   for (int q = 0; q < nm; q++) {
-    const Dims& d = e.members[q]->s.d;
+    const BScene& b = e.members[q]->s;
+    const Dims& d = b.d;
     CgScalars c{};
     c.accuracy = e.cgAccuracy;
-    c.maxIter = (int)(e.cgMaxIterFac * (float)std::max(d.nx, std::max(d.ny, d.nz))) * 4;
+    c.maxIter = (int)(e.cgMaxIterFac * (float)std::max(d.nx, std::max(d.ny, d.nz))) * (d.is3d ? 1 : 4);
     c.resNorm = 1e20f;
     e.hSc[q] = c;
     maxIterAll = std::max(maxIterAll, c.maxIter);
@@ -318,6 +403,21 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
   CKB(cudaMemcpyAsync(e.dSc, e.hSc.data(), sizeof(CgScalars) * nm, cudaMemcpyHostToDevice, st));
   CKB(cudaMemsetAsync(e.dDone, 0, sizeof(int), st));
   launch_b_pressure_setup(e.dTiles, nt, e.dScenes, nxt, st);
+  BatchMic mic;
+  mic.flow = e.dFlow;
+  mic.order = e.dOrder2;
+  mic.ntiles = (int)e.hOrder2.size();
+  mic.nscenes = (int)e.hFlow.size();
+  mic.ctas = mic_flow_device_ctas();
+  mic.sceneOf = e.dMicScene;
+  mic.counter = e.dMicCounter;
+  mic.error = e.dMicCounter + 1;
+  mic.epoch = &e.micEpoch;
+  mic.spinLimit = 200000000LL;
+  if (mic.nscenes > 0) {
+    CKB(cudaMemsetAsync(mic.error, 0, sizeof(int), st));
+    launch_b_mic_init(e.dTiles, nt, e.dScenes, mic, st);
+  }
   // CG sweeps over the tiles of the scenes still iterating.  Autotuner: the
   // first solve runs its first 4 x lag sweeps with tiles 8, 16, 32 and 64
   // rows tall (lag sweeps each, timed with events) and keeps the fastest;
@@ -338,7 +438,7 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
   const bool tuning = e.rowsK < 0;
   if (tuning) CKB(cudaEventRecord(e.ev[0], st));
   while (active > 0 && sweeps < maxIterAll) {
-    launch_b_pcg_iteration(e.dActive, active, e.dScenes, 1 << kk, e.dDone, st);
+    launch_b_pcg_iteration(e.dActive, active, e.dScenes, 1 << kk, e.dDone, &mic, st);
     sweeps++;
     if (sweeps % e.lag == 0 || sweeps == maxIterAll) {
       bool relist = false;
@@ -393,6 +493,11 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
     stats->maxIterations = mx;
     stats->totalIterations = sum;
     stats->diverged = diverged;
+  }
+  if (mic.nscenes > 0) {
+    int err = 0;
+    CKB(cudaMemcpy(&err, mic.error, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return set_error(MG_ERR_TIMEOUT, "MIC wavefront (batched): a tile wait exceeded its spin limit");
   }
   for (auto& c : e.hSc)
     if (c.status == 2)
@@ -467,6 +572,15 @@ extern "C" int mg_batch_set_solver(mg_batch b, float cgAccuracy, float cgMaxIter
   if (!b || !(cgAccuracy > 0.f) || !(cgMaxIterFac > 0.f)) return set_error(MG_ERR_ARG, "mg_batch_set_solver: invalid argument");
   b->e.cgAccuracy = cgAccuracy;
   b->e.cgMaxIterFac = cgMaxIterFac;
+  return MG_OK;
+}
+
+extern "C" int mg_batch_set_preconditioner(mg_batch b, int preconditioner) {
+  if (!b || (preconditioner != MG_PC_NONE && preconditioner != MG_PC_MIC))
+    return set_error(MG_ERR_ARG, "mg_batch_set_preconditioner: PcNone or PcMIC");
+  b->e.micFor3D = preconditioner == MG_PC_MIC;
+  for (auto* m : b->e.members) m->s.mic = (m->s.d.is3d && b->e.micFor3D) ? 1 : 0;
+  b->e.dirty = true;
   return MG_OK;
 }
 

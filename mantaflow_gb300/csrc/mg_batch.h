@@ -48,6 +48,13 @@ struct BScene {
   code_t* code;
   CgScalars* sc;
   double* part;    // per-tile partials (ntiles doubles, 2 per tile for max-abs)
+  // MIC(0) preconditioning (3D scenes, the reference's PcMIC): the
+  // diagonal P and the 16^3 tile grid of the dataflow sweeps with its face
+  // words; mic 0 runs GridCg without a preconditioner (the reference's 2D
+  // path)
+  float* P;
+  unsigned long long* face;
+  int mic, tx, ty, tz;
   float dt;
   float bx, by, bz;  // buoyancy factors -gravity*dt/dx*coefficient (KnAddBuoyancy), 0.5 applied in-kernel
   unsigned long long seed;
@@ -64,8 +71,26 @@ void launch_b_advect_density(const BTile* t, int nt, const BScene* s, int cur, c
 void launch_b_advect_velocity(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_forces(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
 void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
-// one CG sweep over tiles 32 x 8*rows cells tall (rows 1, 2, 4 or 8)
-void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int rows, int* ndone, cudaStream_t st);
+// the MIC(0) sweeps of a batch: the FlowScene table of its MIC scenes, the
+// (scene, tile) dispatch order, and the BScene index of each MIC scene
+struct BatchMic {
+  const FlowScene* flow;
+  const int2* order;
+  int ntiles, nscenes, ctas;
+  const int* sceneOf;  // [nscenes]: index into the BScene table
+  int* counter;
+  int* error;
+  unsigned int* epoch;  // host counter, advanced per sweep launch
+  long long spinLimit;
+};
+// doInit's preconditioner application for the MIC scenes: P, z = M^-1 r,
+// sigma = dot(z, r), search = z
+void launch_b_mic_init(const BTile* t, int nt, const BScene* s, const BatchMic& m, cudaStream_t st);
+// one CG sweep over tiles 32 x 8*rows cells tall (rows 1, 2, 4 or 8); with
+// mic, the MIC scenes apply their preconditioner between the residual
+// update and the search-vector update
+void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int rows, int* ndone, const BatchMic* mic,
+                            cudaStream_t st);
 void launch_b_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
 // uniform [0,1) inflow noise of a scene's cell at a step (the batch's
 // per-scene seeded source); also used to fill single-scene grids for

@@ -145,6 +145,24 @@ void mic_wave_order(int nyb, int nzb, int* order);
 int mic_wave_prepare(int* ctasPerSm4, int* ctasPerSm8);
 void launch_mic_wave(const PcgBuffers& b, const MicWavePlan& m, int mode, unsigned int epoch, long long spinLimit,
                      int ctas, cudaStream_t s);
+// one scene of a tile-dataflow MIC sweep: its grids, its 16^3 tile grid and
+// its face words (mic_flow_face_words(tx*ty*tz) of them)
+struct FlowScene {
+  Dims d;
+  const code_t* code;
+  const float* A0f;
+  float* P;
+  const float* r;
+  float* z;
+  double* part;
+  CgScalars* sc;
+  int tx, ty, tz;
+  unsigned long long* face;
+};
+void launch_mic_flow_batch(const FlowScene* scenes, const int2* order2, int ntiles, int ctas, int* counter, int* error,
+                           int mode, unsigned int epoch, long long spinLimit, cudaStream_t s);
+// resident CTAs of one MIC sweep launch on the device (after mic_flow_prepare)
+int mic_flow_device_ctas();
 // tile-dataflow MIC sweeps (micflow.cu): the tiles of a MicPlan, faces
 // published as epoch-tagged words (face: mic_flow_face_words() words).
 // stall: the sweep waits for an epoch no tile publishes, so its first wait

@@ -30,6 +30,8 @@
 //    the residency.
 //
 // The backward sweep runs the same schedule in mirrored coordinates.
+#include <cstring>
+
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 
@@ -43,19 +45,13 @@ constexpr int kNL = 3 * kT - 2;      // cell levels per tile
 constexpr int kQ = 4;                // halo prefetch distance (levels)
 
 struct FlowArgs {
-  Dims d;
-  const code_t* code;
-  const float* A0f;
-  float* P;
-  const float* r;
-  float* z;
-  double* part;
-  CgScalars* sc;
-  int tx, ty, tz, ntiles;
-  const int* order;
+  FlowScene one;              // the scene of a single-scene launch
+  const FlowScene* scenes;    // batched launch: the scene table
+  int ntiles;
+  const int* order;           // single scene: tile indices in dispatch order
+  const int2* order2;         // batched: (scene, tile) pairs in dispatch order
   int* counter;
   int* error;
-  unsigned long long* face;  // [ntiles][3][kT*kT]: downstream faces x, y, z
   unsigned int epoch;
   unsigned int waitXor;  // 0; non-zero only to make every wait run out (failure-path tests)
   long long spinLimit;
@@ -119,21 +115,20 @@ __host__ __device__ constexpr size_t flow_smem() {
 
 // MODE 0: factor (P).  MODE 1: forward substitution r -> z.  MODE 2:
 // backward substitution z -> z with the fused dot(z, r) per tile.
-template <int MODE>
+template <int MODE, bool kBatch>
 __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   float* s_n = reinterpret_cast<float*>(smem);                                  // [kPad] value neighbours use
   code_t* s_cp = reinterpret_cast<code_t*>(smem + (size_t)kPad * 4);             // [kPad] stencil codes
   float* s_P = reinterpret_cast<float*>(smem + (size_t)kPad * 4 + (size_t)((kPad * 2 + 15) / 16 * 16));  // [kTC]
   float* s_v = s_P + kTC;                                   // [kTC] forward: r -> z; backward: r
-  __shared__ int s_tile;
+  __shared__ int s_tile, s_scene;
   __shared__ double s_red[8];
-  const Dims& d = a.d;
   const int tid = threadIdx.x;
   const bool haloWarp = tid >= 256;
   const int ly = tid & (kT - 1), lz = (tid >> 4) & (kT - 1);
   const int hw = (tid - 256) >> 5, hl = tid & 31;  // halo warp 0/1 and its lane
-  if (MODE != 0 && a.sc->done) return;
+  if (!kBatch && MODE != 0 && a.one.sc->done) return;
   const unsigned ep16 = a.epoch & 0xffffu;
   const unsigned wep16 = ep16 ^ a.waitXor;  // the epoch the fill words must carry
   auto gx = [&](int c, int n) { return MODE == 2 ? n - 1 - c : c; };  // global coordinate of a sweep coordinate
@@ -141,12 +136,26 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
   for (;;) {
     if (tid == 0) {
       const int q = atomicAdd(a.counter, 1);
-      s_tile = q < a.ntiles ? a.order[q] : -1;
+      if (kBatch) {
+        const int2 e = q < a.ntiles ? a.order2[q] : make_int2(-1, -1);
+        s_scene = e.x;
+        s_tile = e.y;
+      } else {
+        s_scene = 0;
+        s_tile = q < a.ntiles ? a.order[q] : -1;
+      }
     }
     __syncthreads();
     const int tile = s_tile;
     if (tile < 0) return;
-    const int ta = tile % a.tx, tb = (tile / a.tx) % a.ty, tc = tile / (a.tx * a.ty);
+    const FlowScene& S = kBatch ? a.scenes[s_scene] : a.one;
+    // a converged scene's tiles are skipped whole (its downstream tiles too)
+    if (kBatch && MODE != 0 && S.sc->done) {
+      __syncthreads();
+      continue;
+    }
+    const Dims& d = S.d;
+    const int ta = tile % S.tx, tb = (tile / S.tx) % S.ty, tc = tile / (S.tx * S.ty);
     const int x0 = ta * kT, y0 = tb * kT, z0 = tc * kT;
     const int nxT = min(kT, d.nx - x0), nyT = min(kT, d.ny - y0), nzT = min(kT, d.nz - z0);  // tile extents
 
@@ -160,13 +169,13 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
         float v = 0.f, p = 0.f, rv = 0.f;
         if (x < nxT && y < nyT && zc < nzT) {
           const long long g = ix(d, gx(x0 + x, d.nx), gx(y0 + y, d.ny), gx(z0 + zc, d.nz));
-          c = a.code[g];
+          c = S.code[g];
           if (MODE == 0) {
-            v = a.A0f ? a.A0f[g] : 0.f;
+            v = S.A0f ? S.A0f[g] : 0.f;
           } else {
-            p = a.P[g];
-            rv = a.r[g];
-            if (MODE == 2) v = a.z[g];
+            p = S.P[g];
+            rv = S.r[g];
+            if (MODE == 2) v = S.z[g];
           }
         }
         const int pe = pad(x, y, zc);
@@ -192,36 +201,36 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
     //   warp 1, lanes 0-15:  y-face fill and publish (hi = z)
     bool fOK = false, pOK = false;
     int fLo = 0, fHi = 0, fSS = 0, fDst = 0, fDS = 0, pLo = 0, pHi = 0, pSrc = 0, pSS = 0, pDS = 0;
-    const unsigned long long* fSrc = a.face;
-    unsigned long long* pDst = a.face;
+    const unsigned long long* fSrc = S.face;
+    unsigned long long* pDst = S.face;
     if (haloWarp) {
       const int hi = hl & 15;
       if (hw == 0 && hl < 16) {           // x: thread (hi, zz) reads (-1, hi, zz) at level hi + zz
         fOK = ta > 0 && hi < nyT;
         fLo = hi; fHi = hi + nzT;
-        fSrc = a.face + ((long long)(tile - 1) * 3 + 0) * (kT * kT) + hi - kT * hi; fSS = kT;
+        fSrc = S.face + ((long long)(tile - 1) * 3 + 0) * (kT * kT) + hi - kT * hi; fSS = kT;
         fDst = pad(-1, hi, -hi); fDS = kSZ;
-        pOK = ta + 1 < a.tx && hi < nyT && nxT == kT;  // cell (15, hi, zz) at level 15 + hi + zz
+        pOK = ta + 1 < S.tx && hi < nyT && nxT == kT;  // cell (15, hi, zz) at level 15 + hi + zz
         pLo = kT - 1 + hi; pHi = pLo + nzT;
-        pDst = a.face + (long long)tile * 3 * (kT * kT) + hi - kT * (kT - 1 + hi); pDS = kT;
+        pDst = S.face + (long long)tile * 3 * (kT * kT) + hi - kT * (kT - 1 + hi); pDS = kT;
         pSrc = pad(kT - 1, hi, -(kT - 1) - hi); pSS = kSZ;
       } else if (hw == 0) {               // z: thread (hi, 0) reads (x, hi, -1) at level x + hi
         fOK = tc > 0 && hi < nyT;
         fLo = hi; fHi = hi + nxT;
-        fSrc = a.face + ((long long)(tile - a.tx * a.ty) * 3 + 2) * (kT * kT) + (kT - 1) * hi; fSS = 1;
+        fSrc = S.face + ((long long)(tile - S.tx * S.ty) * 3 + 2) * (kT * kT) + (kT - 1) * hi; fSS = 1;
         fDst = pad(-hi, hi, -1); fDS = 1;
-        pOK = tc + 1 < a.tz && hi < nyT && nzT == kT;  // cell (x, hi, 15) at level x + hi + 15
+        pOK = tc + 1 < S.tz && hi < nyT && nzT == kT;  // cell (x, hi, 15) at level x + hi + 15
         pLo = kT - 1 + hi; pHi = pLo + nxT;
-        pDst = a.face + (long long)tile * 3 * (kT * kT) + 2 * kT * kT + (kT - 1) * hi - (kT - 1); pDS = 1;
+        pDst = S.face + (long long)tile * 3 * (kT * kT) + 2 * kT * kT + (kT - 1) * hi - (kT - 1); pDS = 1;
         pSrc = pad(-(kT - 1) - hi, hi, kT - 1); pSS = 1;
       } else if (hl < 16) {               // y: thread (0, hi) reads (x, -1, hi) at level x + hi
         fOK = tb > 0 && hi < nzT;
         fLo = hi; fHi = hi + nxT;
-        fSrc = a.face + ((long long)(tile - a.tx) * 3 + 1) * (kT * kT) + (kT - 1) * hi; fSS = 1;
+        fSrc = S.face + ((long long)(tile - S.tx) * 3 + 1) * (kT * kT) + (kT - 1) * hi; fSS = 1;
         fDst = pad(-hi, -1, hi); fDS = 1;
-        pOK = tb + 1 < a.ty && hi < nzT && nyT == kT;  // cell (x, 15, hi) at level x + 15 + hi
+        pOK = tb + 1 < S.ty && hi < nzT && nyT == kT;  // cell (x, 15, hi) at level x + 15 + hi
         pLo = kT - 1 + hi; pHi = pLo + nxT;
-        pDst = a.face + (long long)tile * 3 * (kT * kT) + kT * kT + (kT - 1) * hi - (kT - 1); pDS = 1;
+        pDst = S.face + (long long)tile * 3 * (kT * kT) + kT * kT + (kT - 1) * hi - (kT - 1); pDS = 1;
         pSrc = pad(-(kT - 1) - hi, kT - 1, hi); pSS = 1;
       }
     }
@@ -243,7 +252,7 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
           const int Lh = L + 1;  // fill what level L+1 reads
           if (fOK && Lh >= fLo && Lh < fHi) {
             unsigned long long w = q[u];
-            if (!current(w, wep16)) w = poll_word(fSrc + fSS * Lh, wep16, a.spinLimit, a.error, a.sc);
+            if (!current(w, wep16)) w = poll_word(fSrc + fSS * Lh, wep16, a.spinLimit, a.error, S.sc);
             const int pe = fDst + fDS * Lh;
             s_n[pe] = __uint_as_float((unsigned)w);
             s_cp[pe] = (code_t)((w >> 32) & 0xffffu);
@@ -262,7 +271,7 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
               if (cd & kCodeFluid) {
                 const float px = s_n[pe - 1], py = s_n[pe - kSY], pz = s_n[pe - kSZ];
                 const int cx = s_cp[pe - 1], cy = s_cp[pe - kSY], cz = s_cp[pe - kSZ];
-                const float A0 = a.A0f ? s_n[pe] : (float)(cd & 7);
+                const float A0 = S.A0f ? s_n[pe] : (float)(cd & 7);
                 float ev = A0;
                 if (cd & kLowX) ev = ev - px * px;
                 if (cd & kLowY) ev = ev - py * py;
@@ -320,8 +329,8 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
         if (x < nxT && y < nyT && zc < nzT) {
           const long long g = ix(d, gx(x0 + x, d.nx), gx(y0 + y, d.ny), gx(z0 + zc, d.nz));
           const float v = MODE == 1 ? s_v[e] : s_n[pad(x, y, zc)];
-          if (MODE == 0) a.P[g] = v;
-          else a.z[g] = v;
+          if (MODE == 0) S.P[g] = v;
+          else S.z[g] = v;
           if (MODE == 2) acc += (double)(v * s_v[e]);
         }
       }
@@ -333,7 +342,7 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
       if (tid == 0) {
         double t = 0.;
         for (int w = 0; w < 8; w++) t += s_red[w];
-        a.part[tile] = t;
+        S.part[tile] = t;
       }
     }
     __syncthreads();
@@ -341,50 +350,92 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
 }
 
 // ---------------------------------------------------------------- host side
+template <bool kB>
+static cudaError_t flow_attrs() {
+  cudaError_t e = cudaFuncSetAttribute(k_mic_flow<0, kB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flow_smem<0>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mic_flow<1, kB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flow_smem<1>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mic_flow<2, kB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flow_smem<2>());
+  return e;
+}
+
+static int g_flowCtas = 0;  // resident CTAs of a sweep on the whole device
+
 int mic_flow_prepare(int* ctasPerSm) {
-  cudaError_t e = cudaFuncSetAttribute(k_mic_flow<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flow_smem<0>());
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_mic_flow<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flow_smem<1>());
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_mic_flow<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flow_smem<2>());
+  cudaError_t e = flow_attrs<false>();
+  if (e == cudaSuccess) e = flow_attrs<true>();
   int n = 0;
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mic_flow<1>, 320, flow_smem<1>());
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mic_flow<1, false>, 320, flow_smem<1>());
   *ctasPerSm = n > 0 ? n : 1;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  g_flowCtas = *ctasPerSm * (sms > 0 ? sms : 1);
   return e == cudaSuccess ? 0 : 1;
 }
 
+int mic_flow_device_ctas() { return g_flowCtas > 0 ? g_flowCtas : 1; }
+
 size_t mic_flow_face_words(int ntiles) { return (size_t)ntiles * 3 * kT * kT; }
+
+template <bool kB>
+static void flow_launch(const FlowArgs& a, int mode, int ctas, cudaStream_t s) {
+  count_launch();
+  if (mode == 0) k_mic_flow<0, kB><<<ctas, 320, flow_smem<0>(), s>>>(a);
+  else if (mode == 1) k_mic_flow<1, kB><<<ctas, 320, flow_smem<1>(), s>>>(a);
+  else k_mic_flow<2, kB><<<ctas, 320, flow_smem<2>(), s>>>(a);
+}
 
 // mode: 0 factor, 1 forward, 2 backward (+beta), 3 backward for doInit (+sigma)
 void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* face, int mode, unsigned int epoch,
                      long long spinLimit, cudaStream_t s, bool stall) {
   FlowArgs a;
-  a.d = b.d;
-  a.code = b.code;
-  a.A0f = b.A0f;
-  a.P = b.P;
-  a.r = b.residual;
-  a.z = b.tmp;
-  a.part = b.part;
-  a.sc = b.sc;
-  a.tx = m.tx;
-  a.ty = m.ty;
-  a.tz = m.tz;
+  a.one.d = b.d;
+  a.one.code = b.code;
+  a.one.A0f = b.A0f;
+  a.one.P = b.P;
+  a.one.r = b.residual;
+  a.one.z = b.tmp;
+  a.one.part = b.part;
+  a.one.sc = b.sc;
+  a.one.tx = m.tx;
+  a.one.ty = m.ty;
+  a.one.tz = m.tz;
+  a.one.face = face;
+  a.scenes = nullptr;
   a.ntiles = m.ntiles;
   a.order = m.order;
+  a.order2 = nullptr;
   a.counter = m.counter;
   a.error = m.error;
-  a.face = face;
   a.epoch = epoch;
   a.waitXor = stall ? 0x8000u : 0u;
   a.spinLimit = spinLimit;
   cudaMemsetAsync(m.counter, 0, sizeof(int), s);
-  const int n = m.ctas < m.ntiles ? m.ctas : m.ntiles;
-  count_launch();
-  if (mode == 0) k_mic_flow<0><<<n, 320, flow_smem<0>(), s>>>(a);
-  else if (mode == 1) k_mic_flow<1><<<n, 320, flow_smem<1>(), s>>>(a);
-  else k_mic_flow<2><<<n, 320, flow_smem<2>(), s>>>(a);
+  flow_launch<false>(a, mode, m.ctas < m.ntiles ? m.ctas : m.ntiles, s);
   if (mode >= 2) launch_mic_finish(b, m.ntiles, mode == 3, s);
+}
+
+// the sweep over the tiles of several scenes in one launch: order2 lists
+// (scene, tile) pairs so that each tile comes after the tiles it waits for
+// (wavefront level first); the backward modes leave each scene's per-tile
+// dot partials in its part[] for the caller's per-scene reduction
+void launch_mic_flow_batch(const FlowScene* scenes, const int2* order2, int ntiles, int ctas, int* counter, int* error,
+                           int mode, unsigned int epoch, long long spinLimit, cudaStream_t s) {
+  FlowArgs a;
+  memset(&a.one, 0, sizeof(a.one));
+  a.scenes = scenes;
+  a.ntiles = ntiles;
+  a.order = nullptr;
+  a.order2 = order2;
+  a.counter = counter;
+  a.error = error;
+  a.epoch = epoch;
+  a.waitXor = 0u;
+  a.spinLimit = spinLimit;
+  cudaMemsetAsync(counter, 0, sizeof(int), s);
+  flow_launch<true>(a, mode == 3 ? 2 : mode, ctas < ntiles ? ctas : ntiles, s);
 }
 
 }  // namespace mgpu

@@ -1343,7 +1343,7 @@ __global__ void __launch_bounds__(256) k_b_pcg_axpy(const BTile* __restrict__ ti
       sc.pres[idx] = sc.pres[idx] + alpha * sc.search[idx];
       const float rv = sc.res[idx] + na * sc.tmp[idx];
       sc.res[idx] = rv;
-      sc.tmp[idx] = rv;
+      if (!sc.mic) sc.tmp[idx] = rv;  // z = r without a preconditioner
       mx[r] = fabsf(rv);
       sq[r] = rv * rv;
     }
@@ -1375,6 +1375,14 @@ __global__ void __launch_bounds__(256) k_b_pcg_axpy(const BTile* __restrict__ ti
       g->sigma = res;
       g->done = 1;
       atomicAdd(ndone, 1);
+      return;
+    }
+    if (sc.mic) {
+      // beta and the divergence test follow the MIC sweeps (k_b_mic_finish)
+      if (g->iterations >= g->maxIter) {
+        g->done = 1;
+        atomicAdd(ndone, 1);
+      }
       return;
     }
     const float sigmaNew = (float)s2;
@@ -1415,7 +1423,50 @@ __global__ void __launch_bounds__(256) k_b_correct(const BTile* __restrict__ til
   if (!in) return;
   correct_velocity_cell(d, sc.flags, bmac(sc.vel[nxt], d.n), sc.pres, i, j, k);
 }
+// search = z for the MIC scenes after doInit's preconditioner application
+__global__ void __launch_bounds__(256) k_b_mic_search(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
+  BATCH_TILE
+  if (!in || !sc.mic) return;
+  sc.search[idx] = sc.tmp[idx];
+}
+
 #undef BATCH_TILE
+
+// sigma (doInit) or beta (iterate) of each MIC scene from the per-tile
+// dot(z, r) partials its backward sweep left, summed in tile order; the
+// divergence test of GridCg::iterate (conjugategrad.cpp:288-295)
+template <bool kInit>
+__global__ void k_b_mic_finish(const BScene* __restrict__ S, const int* __restrict__ sceneOf, const FlowScene* F,
+                               int* ndone) {
+  const BScene& sc = S[sceneOf[blockIdx.x]];
+  CgScalars* g = sc.sc;
+  if (!kInit && g->done) return;
+  const double s2 = sum_partials(sc.part, F[blockIdx.x].tx * F[blockIdx.x].ty * F[blockIdx.x].tz);
+  if (threadIdx.x != 0) return;
+  const float sigmaNew = (float)s2;
+  if (kInit) {
+    g->sigma = sigmaNew;
+    return;
+  }
+  g->beta = sigmaNew / g->sigma;
+  g->sigma = sigmaNew;
+  if (!(g->resNorm < 1e35f)) {
+    g->status = 2;
+    g->done = 1;
+    atomicAdd(ndone, 1);
+  }
+}
+
+void launch_b_mic_init(const BTile* t, int nt, const BScene* s, const BatchMic& m, cudaStream_t st) {
+  if (m.nscenes == 0) return;
+  for (int mode = 0; mode <= 2; mode++)
+    launch_mic_flow_batch(m.flow, m.order, m.ntiles, m.ctas, m.counter, m.error, mode == 2 ? 3 : mode, ++*m.epoch,
+                          m.spinLimit, st);
+  count_launch();
+  k_b_mic_finish<true><<<m.nscenes, 256, 0, st>>>(s, m.sceneOf, m.flow, nullptr);
+  count_launch();
+  k_b_mic_search<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s);
+}
 
 void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
   const dim3 b(kBTX, kBTY, 1);
@@ -1425,21 +1476,30 @@ void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, c
   k_b_pcg_init<<<nt, b, 0, st>>>(t, s);
 }
 template <int R>
-static void pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, cudaStream_t st) {
+static void pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, const BatchMic* mic, cudaStream_t st) {
   const dim3 b(kBTX, kBTY, 1);
   count_launch();
   k_b_pcg_spmv<R><<<nt, b, 0, st>>>(t, s);
   count_launch();
   k_b_pcg_axpy<R><<<nt, b, 0, st>>>(t, s, ndone);
+  if (mic && mic->nscenes > 0) {
+    launch_mic_flow_batch(mic->flow, mic->order, mic->ntiles, mic->ctas, mic->counter, mic->error, 1, ++*mic->epoch,
+                          mic->spinLimit, st);
+    launch_mic_flow_batch(mic->flow, mic->order, mic->ntiles, mic->ctas, mic->counter, mic->error, 2, ++*mic->epoch,
+                          mic->spinLimit, st);
+    count_launch();
+    k_b_mic_finish<false><<<mic->nscenes, 256, 0, st>>>(s, mic->sceneOf, mic->flow, ndone);
+  }
   count_launch();
   k_b_pcg_update<R><<<nt, b, 0, st>>>(t, s);
 }
-void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int rows, int* ndone, cudaStream_t st) {
+void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int rows, int* ndone, const BatchMic* mic,
+                            cudaStream_t st) {
   switch (rows) {
-    case 1: pcg_iteration<1>(t, nt, s, ndone, st); break;
-    case 2: pcg_iteration<2>(t, nt, s, ndone, st); break;
-    case 4: pcg_iteration<4>(t, nt, s, ndone, st); break;
-    default: pcg_iteration<8>(t, nt, s, ndone, st); break;
+    case 1: pcg_iteration<1>(t, nt, s, ndone, mic, st); break;
+    case 2: pcg_iteration<2>(t, nt, s, ndone, mic, st); break;
+    case 4: pcg_iteration<4>(t, nt, s, ndone, mic, st); break;
+    default: pcg_iteration<8>(t, nt, s, ndone, mic, st); break;
   }
 }
 void launch_b_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
