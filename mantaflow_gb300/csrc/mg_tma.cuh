@@ -22,9 +22,16 @@ __device__ __forceinline__ unsigned long long gtimer() {
   return t;
 }
 
-// one thread: an mbarrier expecting a single arrival per phase
-__device__ __forceinline__ void mbar_init(uint64_t* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+// one thread: an mbarrier expecting `count` arrivals per phase
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count = 1) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// a plain arrival (no transaction bytes)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  uint64_t state;
+  asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(smem_addr(bar)) : "memory");
+  (void)state;
 }
 
 // after every mbar_init of the block, before any thread uses the barriers

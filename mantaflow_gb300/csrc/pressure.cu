@@ -486,17 +486,20 @@ __global__ void __launch_bounds__(256, 4) k_pcg_spmv4(Dims d, const code_t* __re
 }
 
 // ---- the same SpMV streamed plane by plane through shared memory.  A CTA
-// owns a slab of TY full-width rows and a run of z planes.  Its ring of
-// kStreamSlots planes is filled by bulk asynchronous copies (one copy of the
-// slab's rows plus their y halo per plane, one of the plane's stencil codes),
-// completed on one mbarrier per slot; while plane z is computed from planes
-// z-1, z and z+1, the next kStreamSlots - 3 planes are on their way, so each
-// SM keeps ~100 KB of loads in flight.  x is read from DRAM once per plane
-// (the y halo rows come from L2), and no neighbour is re-read from L2 by a
-// gather.  Same cell arithmetic as k_pcg_spmv4.
+// owns a slab of TY full-width rows and a run of z planes, and keeps a ring
+// of kStreamSlots planes in shared memory.  One producer warp fills the ring
+// with bulk asynchronous copies (per plane: the slab's rows plus their y
+// halo, and the plane's stencil codes), each completing a "full" mbarrier;
+// eight consumer warps compute plane z from planes z-1, z and z+1 and hand
+// the slot of plane z-1 back through an "empty" mbarrier.  No block-wide
+// barrier runs per plane, so warps drift freely and the producer keeps up to
+// kStreamSlots - 3 planes in flight.  x is read from DRAM once per plane (the
+// y halo rows come from L2) and no neighbour is re-read from L2 by a gather.
+// Same cell arithmetic as k_pcg_spmv4.
 constexpr int kStreamSlots = 8;
 constexpr int kStreamSlotBudget = 12288;         // bytes of one ring slot at most
-constexpr int kStreamQuads = 2;                  // quads per thread and plane at most
+constexpr int kStreamQuads = 2;                  // quads per consumer thread and plane at most
+constexpr int kStreamConsumers = 256;            // consumer threads (8 warps); + 1 producer warp
 constexpr long long kStreamWaitNs = 100000000LL;  // bound of one copy wait
 
 struct StreamGeom {
@@ -504,11 +507,12 @@ struct StreamGeom {
   unsigned slotBytes, xBytes;  // ring slot size, offset of the code rows in a slot
 };
 
-__global__ void __launch_bounds__(256, 2) k_pcg_spmv_stream(Dims d, StreamGeom g, const code_t* __restrict__ code,
-                                                           const float* __restrict__ A0f, const float* __restrict__ x,
-                                                           float* y, double* part, CgScalars* sc) {
+__global__ void __launch_bounds__(kStreamConsumers + 32, 2)
+    k_pcg_spmv_stream(Dims d, StreamGeom g, const code_t* __restrict__ code, const float* __restrict__ A0f,
+                      const float* __restrict__ x, float* y, double* part, CgScalars* sc) {
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bars[kStreamSlots];
+  __shared__ __align__(8) uint64_t full[kStreamSlots], empty[kStreamSlots];
+  __shared__ int s_fail, s_issued;
   if (sc->done) return;
   const int nx = d.nx;
   const int y0 = blockIdx.x * g.TY, ty = min(g.TY, d.ny - y0);
@@ -517,91 +521,110 @@ __global__ void __launch_bounds__(256, 2) k_pcg_spmv_stream(Dims d, StreamGeom g
   const int p0 = zs - 1;        // plane of ring index 0
   const int np = ze + 1 - p0;   // ring indices 0 .. np-1: planes zs-1 .. ze
   const long long sz = d.sz;
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < kStreamSlots; k++) mbar_init(&bars[k]);
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int k = 0; k < kStreamSlots; k++) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], kStreamConsumers / 32);
+    }
+    s_fail = 0;
+    s_issued = 0;
     mbar_fence_init();
   }
   __syncthreads();
   auto slotBase = [&](int i) { return smem + (size_t)(i % kStreamSlots) * g.slotBytes; };
-  // thread 0: fill the slot of ring index i (planes outside the grid only
-  // complete the slot's phase)
-  auto issue = [&](int i) {
-    const int p = p0 + i;
-    uint64_t* bar = &bars[i % kStreamSlots];
-    if (p < 0 || p >= d.nz) {
-      mbar_arrive_expect(bar, 0);
-      return;
-    }
-    const unsigned xb = (unsigned)((yb - ya) * nx) * 4u;
-    const bool withCode = p >= zs && p < ze;
-    const unsigned cb = withCode ? (unsigned)(ty * nx) * 2u : 0u;
-    mbar_arrive_expect(bar, xb + cb);
-    bulk_g2s(slotBase(i), x + p * sz + (long long)ya * nx, xb, bar);
-    if (withCode) bulk_g2s(slotBase(i) + g.xBytes, code + p * sz + (long long)y0 * nx, cb, bar);
-  };
-  int issued = 0;
-  if (threadIdx.x == 0)
-    for (; issued < kStreamSlots && issued < np; issued++) issue(issued);
-  // this thread's quads of a plane: rows and x offsets fixed for the CTA
-  const int nq4 = nx >> 2, quads = ty * nq4;
-  int nmine = 0, ro[kStreamQuads], co[kStreamQuads], go[kStreamQuads];
-  for (int e = threadIdx.x; e < quads && nmine < kStreamQuads; e += blockDim.x) {
-    const int r = e / nq4, xq = e - r * nq4;
-    ro[nmine] = (y0 + r - ya) * nx + 4 * xq;  // the quad in a slot's x rows
-    co[nmine] = r * nx + 4 * xq;              // its codes in the slot's code rows
-    go[nmine] = (y0 + r) * nq4 + xq;          // its float4 index within a plane
-    nmine++;
-  }
-  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4* A4 = reinterpret_cast<const float4*>(A0f);
-  float4* y4 = reinterpret_cast<float4*>(y);
   FSum acc;
-  bool ok = true;
-  int waited = 0;  // ring indices below this one have been waited for
-  for (int z = zs; z < ze; z++) {
-    const int ic = z - p0;
-    for (; waited <= ic + 1; waited++)
-      if (!mbar_wait(&bars[waited % kStreamSlots], (unsigned)(waited / kStreamSlots) & 1u, kStreamWaitNs)) ok = false;
-    if (!__syncthreads_and(ok)) {
-      ok = false;
-      break;
-    }
-    const float* xm = reinterpret_cast<const float*>(slotBase(ic - 1));
-    const float* xcen = reinterpret_cast<const float*>(slotBase(ic));
-    const float* xp = reinterpret_cast<const float*>(slotBase(ic + 1));
-    const code_t* cs = reinterpret_cast<const code_t*>(slotBase(ic) + g.xBytes);
-    const long long planeQ = ((long long)z * sz) >> 2;
-#pragma unroll
-    for (int u = 0; u < kStreamQuads; u++) {
-      if (u < nmine) {
-        const int o = ro[u];
-        SpmvQuad Q;
-        Q.cw = *reinterpret_cast<const uint2*>(cs + co[u]);
-        const int any = (int)((Q.cw.x | Q.cw.y | (Q.cw.x >> 16) | (Q.cw.y >> 16)) & 0xffffu);
-        Q.xc = *reinterpret_cast<const float4*>(xcen + o);
-        Q.ylo = (any & kLowY) ? *reinterpret_cast<const float4*>(xcen + o - nx) : z4;
-        Q.yhi = (any & kHighY) ? *reinterpret_cast<const float4*>(xcen + o + nx) : z4;
-        Q.zlo = (any & kLowZ) ? *reinterpret_cast<const float4*>(xm + o) : z4;
-        Q.zhi = (any & kHighZ) ? *reinterpret_cast<const float4*>(xp + o) : z4;
-        Q.xl = (Q.cw.x & kLowX) ? xcen[o - 1] : 0.f;
-        Q.xr = ((Q.cw.y >> 16) & kHighX) ? xcen[o + 4] : 0.f;
-        const long long q = planeQ + go[u];
-        if (A0f) Q.A0 = __ldg(A4 + q);
-        else
-          Q.A0 = make_float4((float)(Q.cw.x & 7), (float)((Q.cw.x >> 16) & 7), (float)(Q.cw.y & 7),
-                             (float)((Q.cw.y >> 16) & 7));
-        y4[q] = spmv_apply(Q, acc);
+  if (tid >= kStreamConsumers) {
+    // ---- producer warp: lane 0 fills ring index i once its slot's previous
+    // plane (ring index i - kStreamSlots) has been handed back
+    if (tid == kStreamConsumers) {
+      for (int i = 0; i < np; i++) {
+        if (i >= kStreamSlots &&
+            !mbar_wait(&empty[i % kStreamSlots], (unsigned)((i - kStreamSlots) / kStreamSlots) & 1u, kStreamWaitNs)) {
+          atomicExch(&s_fail, 1);
+          break;
+        }
+        if (*((volatile int*)&s_fail)) break;
+        const int p = p0 + i;
+        uint64_t* bar = &full[i % kStreamSlots];
+        s_issued = i + 1;
+        if (p < 0 || p >= d.nz) {
+          mbar_arrive_expect(bar, 0);  // completes the slot's phase
+          continue;
+        }
+        const unsigned xb = (unsigned)((yb - ya) * nx) * 4u;
+        const bool withCode = p >= zs && p < ze;
+        const unsigned cb = withCode ? (unsigned)(ty * nx) * 2u : 0u;
+        mbar_arrive_expect(bar, xb + cb);
+        bulk_g2s(slotBase(i), x + p * sz + (long long)ya * nx, xb, bar);
+        if (withCode) bulk_g2s(slotBase(i) + g.xBytes, code + p * sz + (long long)y0 * nx, cb, bar);
       }
     }
-    __syncthreads();  // the slot of plane z-1 is read for the last time
-    if (threadIdx.x == 0 && issued < np) issue(issued++);
+  } else {
+    // ---- consumers: this thread's quads of a plane (fixed for the CTA)
+    const int nq4 = nx >> 2, quads = ty * nq4;
+    int nmine = 0, ro[kStreamQuads], co[kStreamQuads], go[kStreamQuads];
+    for (int e = tid; e < quads && nmine < kStreamQuads; e += kStreamConsumers) {
+      const int r = e / nq4, xq = e - r * nq4;
+      ro[nmine] = (y0 + r - ya) * nx + 4 * xq;  // the quad in a slot's x rows
+      co[nmine] = r * nx + 4 * xq;              // its codes in the slot's code rows
+      go[nmine] = (y0 + r) * nq4 + xq;          // its float4 index within a plane
+      nmine++;
+    }
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4* A4 = reinterpret_cast<const float4*>(A0f);
+    float4* y4 = reinterpret_cast<float4*>(y);
+    const bool leader = (tid & 31) == 0;
+    int waited = 0;  // ring indices below this one have been waited for
+    for (int z = zs; z < ze; z++) {
+      const int ic = z - p0;
+      bool ok = true;
+      for (; waited <= ic + 1 && ok; waited++)
+        ok = mbar_wait(&full[waited % kStreamSlots], (unsigned)(waited / kStreamSlots) & 1u, kStreamWaitNs);
+      if (!__all_sync(0xffffffffu, ok) || *((volatile int*)&s_fail)) {
+        if (leader) atomicExch(&s_fail, 1);
+        break;
+      }
+      const float* xm = reinterpret_cast<const float*>(slotBase(ic - 1));
+      const float* xcen = reinterpret_cast<const float*>(slotBase(ic));
+      const float* xp = reinterpret_cast<const float*>(slotBase(ic + 1));
+      const code_t* cs = reinterpret_cast<const code_t*>(slotBase(ic) + g.xBytes);
+      const long long planeQ = ((long long)z * sz) >> 2;
+#pragma unroll
+      for (int u = 0; u < kStreamQuads; u++) {
+        if (u < nmine) {
+          const int o = ro[u];
+          SpmvQuad Q;
+          Q.cw = *reinterpret_cast<const uint2*>(cs + co[u]);
+          const int any = (int)((Q.cw.x | Q.cw.y | (Q.cw.x >> 16) | (Q.cw.y >> 16)) & 0xffffu);
+          Q.xc = *reinterpret_cast<const float4*>(xcen + o);
+          Q.ylo = (any & kLowY) ? *reinterpret_cast<const float4*>(xcen + o - nx) : z4;
+          Q.yhi = (any & kHighY) ? *reinterpret_cast<const float4*>(xcen + o + nx) : z4;
+          Q.zlo = (any & kLowZ) ? *reinterpret_cast<const float4*>(xm + o) : z4;
+          Q.zhi = (any & kHighZ) ? *reinterpret_cast<const float4*>(xp + o) : z4;
+          Q.xl = (Q.cw.x & kLowX) ? xcen[o - 1] : 0.f;
+          Q.xr = ((Q.cw.y >> 16) & kHighX) ? xcen[o + 4] : 0.f;
+          const long long q = planeQ + go[u];
+          if (A0f) Q.A0 = __ldg(A4 + q);
+          else
+            Q.A0 = make_float4((float)(Q.cw.x & 7), (float)((Q.cw.x >> 16) & 7), (float)(Q.cw.y & 7),
+                               (float)((Q.cw.y >> 16) & 7));
+          y4[q] = spmv_apply(Q, acc);
+        }
+      }
+      // the warp is done with plane z-1 (read for the last time)
+      __syncwarp();
+      if (leader) mbar_arrive(&empty[(ic - 1) % kStreamSlots]);
+    }
   }
-  if (!ok) {
-    // a copy wait ran out: let the copies in flight land (bounded) before the
+  __syncthreads();
+  if (s_fail) {
+    // a copy wait ran out: let every copy in flight land (bounded) before the
     // block's shared memory is given up, and end the solve with an error
-    if (threadIdx.x == 0) {
-      for (int i = std::max(0, issued - kStreamSlots); i < issued; i++)
-        mbar_wait(&bars[i % kStreamSlots], (unsigned)(i / kStreamSlots) & 1u, kStreamWaitNs);
+    if (tid == 0) {
+      const int issued = s_issued;
+      for (int i = issued > kStreamSlots ? issued - kStreamSlots : 0; i < issued; i++)
+        mbar_wait(&full[i % kStreamSlots], (unsigned)(i / kStreamSlots) & 1u, kStreamWaitNs);
       sc->status = 4;
       sc->done = 1;
     }
@@ -609,11 +632,11 @@ __global__ void __launch_bounds__(256, 2) k_pcg_spmv_stream(Dims d, StreamGeom g
   }
   const double b = block_sum(acc.value());
   const unsigned nb = gridDim.x * gridDim.y;
-  if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = b;
+  if (tid == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = b;
   if (last_block(&sc->counters[1], nb)) {
-    const double s = sum_partials(part, (int)nb);
-    if (threadIdx.x == 0) {
-      const float dp = (float)s;
+    const double s2 = sum_partials(part, (int)nb);
+    if (tid == 0) {
+      const float dp = (float)s2;
       sc->dp = dp;
       float alpha = 0.f;
       if (fabsf(dp) > 0.f) alpha = sc->sigma / dp;
@@ -628,7 +651,7 @@ static bool stream_geom(const Dims& d, int maxBlocks, int sms, StreamGeom* g, di
   if (!d.is3d || d.nx % 8 != 0) return false;
   int TY = 16;
   while (TY >= 2 && (size_t)(TY + 2) * d.nx * 4 + (size_t)TY * d.nx * 2 > (size_t)kStreamSlotBudget) TY--;
-  if (TY < 2 || (size_t)TY * (d.nx / 4) > (size_t)kStreamQuads * 256) return false;
+  if (TY < 2 || (size_t)TY * (d.nx / 4) > (size_t)kStreamQuads * kStreamConsumers) return false;
   g->TY = TY;
   g->xBytes = (unsigned)((TY + 2) * d.nx * 4);
   g->slotBytes = (unsigned)(((size_t)g->xBytes + (size_t)TY * d.nx * 2 + 127) / 128 * 128);
@@ -1092,8 +1115,8 @@ void launch_pcg_spmv(const PcgBuffers& b, cudaStream_t s) {
   StreamGeom g;
   dim3 grid;
   if (g_spmvStream && stream_geom(b.d, 2 * b.nblocks, g_sms, &g, &grid)) {
-    k_pcg_spmv_stream<<<grid, kThreads, (size_t)kStreamSlots * g.slotBytes, s>>>(b.d, g, b.code, b.A0f, b.search,
-                                                                               b.tmp, b.part, b.sc);
+    k_pcg_spmv_stream<<<grid, kStreamConsumers + 32, (size_t)kStreamSlots * g.slotBytes, s>>>(
+        b.d, g, b.code, b.A0f, b.search, b.tmp, b.part, b.sc);
     return;
   }
   if (vec4_ok(b.d))
