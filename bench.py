@@ -300,11 +300,87 @@ def batch_config(seed, n2=512, n3=64):
     return sizes, grav, seeds
 
 
-def batched_form(m, steps, seed, plain_steps, plain_scenes, sim_steps=100):
+def _plain_plume(m, size, grav):
+    """one plume scene on the plain per-scene path"""
+    nx, ny, nz = size
+    s = m.Solver(name="plain", gridSize=m.vec3(nx, ny, nz), dim=3 if nz > 1 else 2)
+    flags = s.create(m.FlagGrid)
+    flags.initDomain(boundaryWidth=0)
+    flags.fillGrid()
+    m.setOpenBound(flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
+    g = {"s": s, "flags": flags, "vel": s.create(m.MACGrid), "dens": s.create(m.RealGrid),
+         "pres": s.create(m.RealGrid), "src": s.create(m.RealGrid), "grav": m.vec3(*grav)}
+    gs = m.vec3(nx, ny, nz)
+    mask = s.create(m.RealGrid)
+    s.create(m.Cylinder, center=gs * m.vec3(0.5, 0.1, 0.5), radius=nx * 0.14,
+             z=gs * m.vec3(0, 0.02, 0)).applyToGrid(grid=mask, value=1.0)
+    g["mask"] = mask.numpy()
+    return g
+
+
+def _plain_step(m, g, inflow):
+    m.copyArrayToGridReal(inflow, g["src"])
+    g["dens"].join(g["src"])
+    m.advectSemiLagrange(flags=g["flags"], vel=g["vel"], grid=g["dens"], order=2, clampMode=2)
+    m.advectSemiLagrange(flags=g["flags"], vel=g["vel"], grid=g["vel"], order=2, clampMode=2)
+    m.setWallBcs(flags=g["flags"], vel=g["vel"])
+    m.addBuoyancy(density=g["dens"], vel=g["vel"], gravity=g["grav"], flags=g["flags"])
+    m.solvePressure(flags=g["flags"], vel=g["vel"], pressure=g["pres"], cgAccuracy=1e-3, preconditioner=m.PcMIC)
+
+
+def batch_accuracy(m, sizes, grav, seeds, pick, steps):
+    """Batched and plain results of a few scenes after `steps` steps from
+    rest (same inflow), each against the FP64 oracle (the reference's double
+    build restated, cgAccuracy 1e-5): per-field relative L2 errors."""
+    from mantaflow_gb300 import batch as mb
+    from oracle import oracle as og
+    og.set_num_threads(os.cpu_count() or 1)
+    b = mb.BatchedPlumes([sizes[i] for i in pick], [grav[i] for i in pick], [seeds[i] for i in pick])
+    for _ in range(steps):
+        b.step()
+    rows = []
+    for q, i in enumerate(pick):
+        nx, ny, nz = sizes[i]
+        inflow = [b.inflow(q, t) for t in range(steps)]
+        g = _plain_plume(m, sizes[i], grav[i])
+        for t in range(steps):
+            _plain_step(m, g, inflow[t])
+        f = g["flags"].numpy()
+        d64 = np.zeros(f.shape, np.float64)
+        v64 = np.zeros(f.shape + (3,), np.float64)
+        p64 = np.zeros(f.shape, np.float64)
+        for t in range(steps):
+            og.join_real(d64, inflow[t].astype(np.float64))
+            og.advect_semi_lagrange(f, v64, d64, og.KIND_REAL, order=2, clampMode=2)
+            og.advect_semi_lagrange(f, v64, v64, og.KIND_MAC, order=2, clampMode=2)
+            og.set_wall_bcs(f, v64)
+            og.add_buoyancy(f, d64, v64, grav[i])
+            og.solve_pressure(f, v64, p64, cgAccuracy=1e-5, preconditioner=og.PC_MIC)
+
+        def rel(a, ref):
+            a = np.asarray(a, np.float64)
+            return float(np.linalg.norm(a - ref) / max(np.linalg.norm(ref), 1e-30))
+
+        rows.append({"size": [nx, ny, nz],
+                     "batched_rel_l2": {"density": rel(b.download(q, mb.DENSITY), d64),
+                                        "velocity": rel(b.download(q, mb.VELOCITY), v64),
+                                        "pressure": rel(b.download(q, mb.PRESSURE), p64)},
+                     "plain_rel_l2": {"density": rel(g["dens"].numpy(), d64), "velocity": rel(g["vel"].numpy(), v64),
+                                      "pressure": rel(g["pres"].numpy(), p64)}})
+        del g
+    b.close()
+    og.set_num_threads(1)
+    return {"steps": steps, "fp64_oracle": "oracle restatement compiled as the reference's double build, PcMIC, "
+                                           "cgAccuracy 1e-5", "scenes": rows}
+
+
+def batched_form(m, steps, seed, plain_steps, acc_steps, sim_steps=100):
     """Config 4, batched against plain: the whole batch for `steps` steps,
     and the plain per-scene path (one solver per scene, scenes one after
-    another) on a stratified sample of the same scenes; sims/hour for
-    `sim_steps`-step simulations and per-step latency percentiles."""
+    another) on every scene of the batch with the same solver (PcMIC in 3D,
+    no preconditioner in 2D as GridCg); sims/hour for `sim_steps`-step
+    simulations, per-step latency percentiles, and the accuracy of both
+    paths against the FP64 oracle on a few scenes."""
     from mantaflow_gb300 import batch as mb
     sizes, grav, seeds = batch_config(seed)
     b = mb.BatchedPlumes(sizes, grav, seeds)
@@ -323,56 +399,40 @@ def batched_form(m, steps, seed, plain_steps, plain_scenes, sim_steps=100):
     batched = {"sims_per_hour": len(sizes) * 3600.0 / (per_step * sim_steps), "step_ms_mean": 1e3 * per_step,
                "step_ms_p50": 1e3 * float(np.percentile(lat, 50)), "step_ms_p99": 1e3 * float(np.percentile(lat, 99)),
                "cells_per_s": info["cells"] / per_step, "cg_sweeps_per_step": sweeps, "steps_timed": steps,
+               "preconditioner": "MIC(0) in 3D scenes (one dataflow launch over all 3D scenes), none in 2D",
                "autotuned_sweep_tile": {"rows": tune[0], "ms_per_8_sweeps_for_8_16_32_64_rows": tune[1]}}
-    # plain: every k-th scene in size order (2D and 3D separately)
-    order2 = sorted(range(512), key=lambda i: sizes[i][0])
-    order3 = sorted(range(512, len(sizes)), key=lambda i: sizes[i][0])
-    k2 = max(1, len(order2) // max(1, plain_scenes - 4))
-    pick = order2[k2 // 2::k2][: plain_scenes - 4] + order3[len(order3) // 8::len(order3) // 4][:4]
+    # plain: every scene, one after another
     per_scene, plain_lat = [], []
-    for i in pick:
-        nx, ny, nz = sizes[i]
-        s = m.Solver(name="plain", gridSize=m.vec3(nx, ny, nz), dim=3 if nz > 1 else 2)
-        flags = s.create(m.FlagGrid)
-        flags.initDomain(boundaryWidth=0)
-        flags.fillGrid()
-        m.setOpenBound(flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
-        vel, dens, pres, src = s.create(m.MACGrid), s.create(m.RealGrid), s.create(m.RealGrid), s.create(m.RealGrid)
-        gs = m.vec3(nx, ny, nz)
-        mask = s.create(m.RealGrid)
-        s.create(m.Cylinder, center=gs * m.vec3(0.5, 0.1, 0.5), radius=nx * 0.14,
-                 z=gs * m.vec3(0, 0.02, 0)).applyToGrid(grid=mask, value=1.0)
-        mk = mask.numpy()
+    for i in range(len(sizes)):
+        g = _plain_plume(m, sizes[i], grav[i])
         rng = np.random.default_rng(seeds[i] % (2 ** 32))
+        nx, ny, nz = sizes[i]
         ts = []
         for t in range(plain_steps + 1):
-            m.copyArrayToGridReal((rng.random(mk.shape, dtype=np.float32) * mk).astype(np.float32), src)
-            s.sync()
+            a = (rng.random((nz, ny, nx), dtype=np.float32) * g["mask"]).astype(np.float32)
+            g["s"].sync()
             t0 = time.perf_counter()
-            dens.join(src)
-            m.advectSemiLagrange(flags=flags, vel=vel, grid=dens, order=2, clampMode=2)
-            m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=2, clampMode=2)
-            m.setWallBcs(flags=flags, vel=vel)
-            m.addBuoyancy(density=dens, vel=vel, gravity=m.vec3(*grav[i]), flags=flags)
-            m.solvePressure(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, preconditioner=m.PcMIC)
-            s.sync()
+            _plain_step(m, g, a)
+            g["s"].sync()
             if t > 0:
                 ts.append(time.perf_counter() - t0)
         per_scene.append(statistics.mean(ts))
         plain_lat += ts
-        del s
-    w2 = 512 / (len(pick) - 4)
-    w3 = (len(sizes) - 512) / 4
-    est = sum(t * (w2 if i < 512 else w3) for t, i in zip(per_scene, pick))  # seconds per step of all scenes
+        del g
+    est = sum(per_scene)  # seconds per step of all scenes, one after another
     plain = {"sims_per_hour": len(sizes) * 3600.0 / (est * sim_steps), "step_ms_p50": 1e3 * float(np.percentile(plain_lat, 50)),
-             "step_ms_p99": 1e3 * float(np.percentile(plain_lat, 99)), "all_scenes_step_s_estimate": est,
-             "sample": "%d scenes (every %d-th 2D scene by size, 4 of the 3D scenes), %d timed steps each after one "
-                       "untimed; per-step time extrapolated by scene class" % (len(pick), k2, plain_steps)}
+             "step_ms_p99": 1e3 * float(np.percentile(plain_lat, 99)), "all_scenes_step_s": est,
+             "sample": "every scene, %d timed steps each after one untimed (seeded uniform inflow noise in the "
+                       "cylinder source; solver identical to the batch's)" % plain_steps}
+    order2 = sorted(range(512), key=lambda i: sizes[i][0])
+    order3 = sorted(range(512, len(sizes)), key=lambda i: sizes[i][0])
+    pick = [order2[len(order2) // 4], order2[len(order2) // 2], order3[len(order3) // 4], order3[len(order3) // 2]]
+    acc = batch_accuracy(m, sizes, grav, seeds, pick, acc_steps) if acc_steps > 0 else None
     return {"workload": "config 4: %d 2D plume scenes (sides log-uniform in [64,512]) + %d 3D (sides U{32..96}), "
                         "buoyancy U[1e-3,8e-3], cgAccuracy 1e-3; %d-step simulations" % (512, len(sizes) - 512, sim_steps),
             "scenes": len(sizes), "cells": info["cells"], "tiles": info["tiles"], "device_bytes": info["bytes"],
             "batched": batched, "plain_per_scene": plain, "speedup_sims_per_hour":
-                batched["sims_per_hour"] / plain["sims_per_hour"]}
+                batched["sims_per_hour"] / plain["sims_per_hour"], "accuracy_vs_fp64": acc}
 
 
 def served_form(m, seed, njobs, step_scale, rate=20.0, budget=150 * 10 ** 9):
@@ -511,8 +571,9 @@ def main():
     ap.add_argument("--precision-size", type=int, default=64, help="grid side of the precision-form sample (0: skip)")
     ap.add_argument("--precision-steps", type=int, default=10)
     ap.add_argument("--batched-steps", type=int, default=10, help="timed steps of the config-4 batch (0: skip)")
-    ap.add_argument("--plain-steps", type=int, default=3, help="timed steps per sampled scene of the plain path")
-    ap.add_argument("--plain-scenes", type=int, default=16)
+    ap.add_argument("--plain-steps", type=int, default=2, help="timed steps per scene of the plain path")
+    ap.add_argument("--accuracy-steps", type=int, default=5,
+                    help="steps of the batched/plain accuracy sample against the FP64 oracle (0: skip)")
     ap.add_argument("--served-jobs", type=int, default=24, help="jobs of the config-5 served sample (0: skip)")
     ap.add_argument("--served-step-scale", type=int, default=10)
     ap.add_argument("--refined-steps", type=int, default=5,
@@ -700,7 +761,7 @@ def main():
         del noise_r, ng, rp
     batched = None
     if args.batched_steps > 0 and rank == 0:
-        batched = batched_form(m, args.batched_steps, args.seed + 13, args.plain_steps, args.plain_scenes)
+        batched = batched_form(m, args.batched_steps, args.seed + 13, args.plain_steps, args.accuracy_steps)
     served = None
     if args.served_jobs > 0 and rank == 0:
         served = served_form(m, args.seed + 17, args.served_jobs, args.served_step_scale)

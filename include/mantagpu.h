@@ -385,6 +385,16 @@ size_t mg_serve_job_bytes(int nx, int ny, int nz);
  * density, velocity and pressure to the host when it finishes */
 int mg_serve_submit(mg_server s, int nx, int ny, int nz, const float* gravity, unsigned long long seed, int steps,
                     double arrival, int keepResult, int* job);
+/* mg_serve_submit for a job of a given kind: 0 the smoke plume, 1 the dam
+ * break of the free-surface liquid scene (initDomain closed box, phi of the
+ * box x < 0.4 nx, y < 0.6 ny; per step extrapolateMACSimple(vel, 4), advect
+ * phi and vel (SL order 1), updateFromLevelset, addGravity, setWallBcs,
+ * ghost-fluid solvePressure(phi), setWallBcs).  A dam-break job's "density"
+ * result is its levelset phi; 3D jobs of both kinds precondition with MIC(0). */
+int mg_serve_submit_kind(mg_server s, int kind, int nx, int ny, int nz, const float* gravity, unsigned long long seed,
+                         int steps, double arrival, int keepResult, int* job);
+/* device bytes a job of that kind and size holds while resident */
+size_t mg_serve_job_bytes_kind(int kind, int nx, int ny, int nz);
 /* run until every submitted job has finished */
 int mg_serve_run(mg_server s, mg_serve_stats* stats);
 int mg_serve_job_info(mg_server s, int job, mg_serve_job* info);

@@ -137,6 +137,8 @@ SIGNATURES = [
     ("mg_serve_set_solver", _I, [_P, _F, _F]),
     ("mg_serve_job_bytes", C.c_size_t, [_I, _I, _I]),
     ("mg_serve_submit", _I, [_P, _I, _I, _I, _FP, C.c_ulonglong, _I, C.c_double, _I, C.POINTER(_I)]),
+    ("mg_serve_submit_kind", _I, [_P, _I, _I, _I, _I, C.POINTER(C.c_float), C.c_ulonglong, _I, C.c_double, _I, C.POINTER(_I)]),
+    ("mg_serve_job_bytes_kind", C.c_size_t, [_I, _I, _I, _I]),
     ("mg_serve_run", _I, [_P, C.POINTER(ServeStats)]),
     ("mg_serve_job_info", _I, [_P, _I, C.POINTER(ServeJob)]),
     ("mg_serve_job_result", _I, [_P, _I, _I, _P, C.c_size_t]),

@@ -106,9 +106,13 @@ class BatchedPlumes:
             pass
 
 
+PLUME, DAM_BREAK = 0, 1
+
+
 class PlumeServer:
-    """Served form: a request loop for plume jobs with device-memory
-    admission and continuous batching (mg_serve_* of include/mantagpu.h)."""
+    """Served form: a request loop for plume and dam-break jobs with
+    device-memory admission and continuous batching (mg_serve_* of
+    include/mantagpu.h)."""
 
     def __init__(self, budget_bytes=150 * 10 ** 9, dt=1.0, cgAccuracy=1e-3, cgMaxIterFac=1.5):
         ensure_init()
@@ -120,16 +124,18 @@ class PlumeServer:
         self.shapes = []
 
     @staticmethod
-    def job_bytes(size):
+    def job_bytes(size, kind=PLUME):
         nx, ny, nz = (tuple(size) + (1,))[:3]
-        return int(_lib.load().mg_serve_job_bytes(nx, ny, nz))
+        return int(_lib.load().mg_serve_job_bytes_kind(int(kind), nx, ny, nz))
 
-    def submit(self, size, gravity, seed, steps, arrival=0.0, keep=False):
+    def submit(self, size, gravity, seed, steps, arrival=0.0, keep=False, kind=PLUME):
+        """kind PLUME (0) or DAM_BREAK (1); a dam-break job's DENSITY result is
+        its levelset phi"""
         nx, ny, nz = (tuple(int(v) for v in size) + (1,))[:3]
         g = (C.c_float * 3)(*[float(v) for v in gravity])
         jid = C.c_int()
-        check(self._L.mg_serve_submit(self._h, nx, ny, nz, g, C.c_ulonglong(int(seed)), int(steps), float(arrival),
-                                      int(bool(keep)), C.byref(jid)))
+        check(self._L.mg_serve_submit_kind(self._h, int(kind), nx, ny, nz, g, C.c_ulonglong(int(seed)), int(steps),
+                                           float(arrival), int(bool(keep)), C.byref(jid)))
         self.shapes.append((nz, ny, nx))
         return jid.value
 

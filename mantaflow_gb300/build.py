@@ -3,7 +3,10 @@
 The library is a plain C-ABI shared object (include/mantagpu.h); Python
 reaches it through ctypes.  -fmad=false keeps a*b+c uncontracted so the
 kernels repeat the reference's float arithmetic exactly; the few places that
-emulate the reference's double-rounded expressions call fmaf explicitly.
+emulate the reference's double-rounded expressions call fmaf explicitly.  The
+host compiler gets -ffp-contract=off for the same reason: the host-side set-up
+arithmetic (the wavelet noise tile, shape axes, force factors) must not be
+contracted into fused multiply-adds, which aarch64 gcc does by default.
 """
 import os
 import shutil
@@ -17,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmantagpu.so")
 SOURCES = ["runtime.cu", "advect.cu", "forces.cu", "pressure.cu", "mic.cu", "micwave.cu", "micflow.cu", "multigrid.cu", "refine.cu", "batch.cu", "gridio.cu", "noise.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 
 def nvcc():

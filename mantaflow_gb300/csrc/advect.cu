@@ -473,6 +473,7 @@ __global__ void k_reset_phi_in_obs(Dims d, const int* __restrict__ flags, float*
 // forward SL of density (into sc.fwd plane 3) and velocity (sc.fwd planes 0-2)
 __global__ void __launch_bounds__(256) k_b_advect_fwd(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
   BATCH_CELL
+  if (sc.kind != 0) return;  // plume scenes only
   const CMac v = bcmac(sc.vel[cur], d.n);
   sl_real_cell<1, 1, 1>(d, v, sc.dens[cur], sc.fwd + 3 * d.n, sc.dt, i, j, k);
   sl_mac_grid_cell<1, 1>(d, v, v, bmac(sc.fwd, d.n), sc.dt, i, j, k);
@@ -480,6 +481,7 @@ __global__ void __launch_bounds__(256) k_b_advect_fwd(const BTile* __restrict__ 
 // MacCormack correction and clamp of both into the next buffers
 __global__ void __launch_bounds__(256) k_b_advect_mc(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
   BATCH_CELL
+  if (sc.kind != 0) return;  // plume scenes only
   const CMac v = bcmac(sc.vel[cur], d.n);
   maccormack_real_cell<1, 1, 1>(d, sc.flags, v, sc.dens[cur], sc.fwd + 3 * d.n, sc.dens[1 - cur], sc.dt, 1.f, 2, i, j, k);
   maccormack_mac_cell<1, 1>(d, sc.flags, v, v, bcmac(sc.fwd, d.n), bmac(sc.vel[1 - cur], d.n), sc.dt, 1.f, 2, i, j, k);
@@ -487,14 +489,36 @@ __global__ void __launch_bounds__(256) k_b_advect_mc(const BTile* __restrict__ t
 // applyOutflowBC (advection.cpp:387-391): convective values into the scratch
 __global__ void __launch_bounds__(256) k_b_outflow(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
   BATCH_CELL
+  if (sc.kind != 0) return;  // plume scenes only
   const float ts = fmaxf(1.f, sc.dt * 4.f);
   outflow_bc_cell(d, sc.flags, bcmac(sc.vel[1 - cur], d.n), bcmac(sc.vel[cur], d.n), bmac(sc.fwd, d.n), ts, i, j, k);
 }
 __global__ void __launch_bounds__(256) k_b_outflow_copy(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
   BATCH_CELL
+  if (sc.kind != 0) return;  // plume scenes only
   copy_outflow_cell(d, sc.flags, bcmac(sc.fwd, d.n), bmac(sc.vel[1 - cur], d.n), i, j, k);
 }
+// dam break: advectSemiLagrange(phi, order 1) into the next buffer
+__global__ void __launch_bounds__(256) k_b_dam_advect_phi(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                          int cur) {
+  BATCH_CELL
+  sl_real_cell<1, 1, 1>(d, bcmac(sc.vel[cur], d.n), sc.dens[cur], sc.dens[1 - cur], sc.dt, i, j, k);
+}
+// dam break: advectSemiLagrange(vel, order 1) into the next buffer (a closed
+// box has no outflow cells, so applyOutflowBC changes nothing)
+__global__ void __launch_bounds__(256) k_b_dam_advect_vel(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                          int cur) {
+  BATCH_CELL
+  const CMac v = bcmac(sc.vel[cur], d.n);
+  sl_mac_grid_cell<1, 1>(d, v, v, bmac(sc.vel[1 - cur], d.n), sc.dt, i, j, k);
+}
 #undef BATCH_CELL
+
+void launch_b_dam_advect_sl(const BTile* t, int nt, const BScene* s, int cur, bool vel, cudaStream_t st) {
+  count_launch();
+  if (vel) k_b_dam_advect_vel<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, cur);
+  else k_b_dam_advect_phi<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, cur);
+}
 
 void launch_b_advect_density(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st) {
   (void)t; (void)nt; (void)s; (void)cur; (void)st;  // density and velocity advect together (launch_b_advect_velocity)

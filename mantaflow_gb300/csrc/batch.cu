@@ -56,8 +56,9 @@ constexpr int kMicTile = 16;  // edge of the MIC dataflow tiles
 int mic_tiles(int n) { return (n + kMicTile - 1) / kMicTile; }
 
 // bytes of one scene's device block (3D scenes also hold the MIC diagonal
-// and the face words of the dataflow sweeps)
-size_t scene_bytes(int nx, int ny, int nz) {
+// and the face words of the dataflow sweeps; dam-break scenes the
+// ghost-fluid diagonal and the extrapolation marks)
+size_t scene_bytes(int nx, int ny, int nz, int kind = 0) {
   const size_t n = (size_t)nx * ny * nz;
   size_t b = align256(n * sizeof(int)) + 2 * align256(3 * n * sizeof(float)) + 2 * align256(n * sizeof(float)) +
              align256(4 * n * sizeof(float)) + 6 * align256(n * sizeof(float)) + align256(n * sizeof(code_t)) +
@@ -65,6 +66,7 @@ size_t scene_bytes(int nx, int ny, int nz) {
   if (nz > 1)
     b += align256(n * sizeof(float)) +
          align256(mic_flow_face_words(mic_tiles(nx) * mic_tiles(ny) * mic_tiles(nz)) * sizeof(unsigned long long));
+  if (kind == 1) b += align256(n * sizeof(float)) + align256(n * sizeof(int));
   return b;
 }
 
@@ -107,6 +109,9 @@ struct Engine {
   int* dMicCounter = nullptr;  // [0] tile counter, [1] wait error
   unsigned int micEpoch = 0;
   std::vector<BTile> tiles1;
+  std::vector<BTile> tilesDam;  // the 32 x 8 tiles of the dam-break scenes
+  BTile* dTilesDam = nullptr;
+  size_t tilesDamCap = 0;
   std::vector<BTile> tilesR[4];
   std::vector<int> startR[4];
   BTile* dTiles = nullptr;
@@ -132,6 +137,7 @@ struct Engine {
     cudaFree(dActive);
     cudaFree(dDone);
     cudaFree(dFlow);
+    cudaFree(dTilesDam);
     cudaFree(dOrder2);
     cudaFree(dMicScene);
     cudaFree(dMicCounter);
@@ -174,12 +180,16 @@ void* pool_take(Engine& e, size_t bytes) {
   return p;
 }
 
-// a plume scene joins the engine: device block, flags and source set up
-int scene_add(Engine& e, int nx, int ny, int nz, const float* gravity, unsigned long long seed, SceneRec** out) {
-  if (nx < 3 || ny < 3 || nz < 1 || (nz > 1 && nz < 3)) return set_error(MG_ERR_ARG, "plume scene is too small");
-  if ((long long)nx * ny * nz >= (1LL << 31)) return set_error(MG_ERR_ARG, "plume scene exceeds 2^31 - 1 cells");
+// a scene joins the engine: device block, flags and source set up.  kind 0
+// is the smoke plume, kind 1 the dam break (a liquid box x < 0.4 nx,
+// y < 0.6 ny in a closed domain)
+int scene_add(Engine& e, int nx, int ny, int nz, const float* gravity, unsigned long long seed, SceneRec** out,
+              int kind = 0) {
+  if (nx < 3 || ny < 3 || nz < 1 || (nz > 1 && nz < 3)) return set_error(MG_ERR_ARG, "scene is too small");
+  if ((long long)nx * ny * nz >= (1LL << 31)) return set_error(MG_ERR_ARG, "scene exceeds 2^31 - 1 cells");
+  if (kind != 0 && kind != 1) return set_error(MG_ERR_ARG, "scene kind: 0 plume or 1 dam break");
   auto r = new SceneRec();
-  r->bytes = scene_bytes(nx, ny, nz);
+  r->bytes = scene_bytes(nx, ny, nz, kind);
   r->mem = pool_take(e, r->bytes);
   if (!r->mem) {
     delete r;
@@ -227,23 +237,50 @@ int scene_add(Engine& e, int nx, int ny, int nz, const float* gravity, unsigned 
     s.face = (unsigned long long*)take(mic_flow_face_words(s.tx * s.ty * s.tz) * sizeof(unsigned long long));
   }
   s.mic = (nz > 1 && e.micFor3D) ? 1 : 0;
+  s.kind = kind;
+  s.A0f = nullptr;
+  s.itmp = nullptr;
+  if (kind == 1) {
+    s.A0f = (float*)take(n * sizeof(float));
+    s.itmp = (int*)take(n * sizeof(int));
+  }
   s.sc = nullptr;
   s.dt = e.dt;
   s.seed = seed;
   s.step = 0;
-  // addBuoyancy(gravity, scale=True, coefficient=1): f = -g*dt/dx, 0.5*f
   const int m = std::max(nx, std::max(ny, nz));
   const float gridScale = (float)(1.0 / (double)m);
   const float dt = e.dt;
-  s.bx = 0.5f * (((-gravity[0]) * dt) / gridScale * 1.f);
-  s.by = 0.5f * (((-gravity[1]) * dt) / gridScale * 1.f);
-  s.bz = 0.5f * (((-gravity[2]) * dt) / gridScale * 1.f);
+  if (kind == 0) {
+    // addBuoyancy(gravity, scale=True, coefficient=1): f = -g*dt/dx, 0.5*f
+    s.bx = 0.5f * (((-gravity[0]) * dt) / gridScale * 1.f);
+    s.by = 0.5f * (((-gravity[1]) * dt) / gridScale * 1.f);
+    s.bz = 0.5f * (((-gravity[2]) * dt) / gridScale * 1.f);
+  } else {
+    // addGravity(gravity, scale=True): f = g*dt/dx (extforces.cpp:61-65)
+    s.bx = (gravity[0] * dt) / gridScale;
+    s.by = (gravity[1] * dt) / gridScale;
+    s.bz = (gravity[2] * dt) / gridScale;
+  }
   // initDomain(boundaryWidth=0) walls, fillGrid, setOpenBound(0, 'Y',
   // Outflow|Empty), Cylinder(center = gs*(0.5,0.1,0.5), radius = 0.14*nx,
   // z = gs*(0,0.02,0)).applyToGrid(mask, 1)
   const int wz = s.d.is3d ? kObstacle : 0;  // initDomain sets no z sides in 2D
   const int types[6] = {kObstacle, kObstacle, kObstacle, kObstacle, wz, wz};
   launch_init_domain(s.d, s.flags, 0, types, e.stream);
+  if (kind == 1) {
+    // the dam-break scene: phi = Box(p0 = 0, p1 = (0.4 nx, 0.6 ny, nz)).computeLevelset();
+    // flags.updateFromLevelset(phi)
+    const float p0[3] = {0.f, 0.f, 0.f};
+    const float p1[3] = {(float)(0.4 * nx), (float)(0.6 * ny), (float)nz};
+    launch_box_sdf(s.d, s.dens[0], p0, p1, e.stream);
+    launch_update_from_levelset(s.d, s.flags, s.dens[0], e.stream);
+    CKB(cudaGetLastError());
+    e.members.push_back(r);
+    e.dirty = true;
+    *out = r;
+    return MG_OK;
+  }
   launch_fill_grid(s.d, s.flags, kFluid, e.stream);
   const int lo[3] = {0, 0, 0}, up[3] = {0, 1, 0};
   launch_set_open_bound(s.d, s.flags, 0, lo, up, kOutflow | kEmpty, e.stream);
@@ -301,6 +338,7 @@ int engine_tables(Engine& e) {
   CKB(cudaMemcpyAsync(e.dScenes, e.hScenes.data(), sizeof(BScene) * nm, cudaMemcpyHostToDevice, e.stream));
   if (!e.dirty) return MG_OK;
   e.tiles1.clear();
+  e.tilesDam.clear();
   for (int k = 0; k < 4; k++) {
     e.tilesR[k].clear();
     e.startR[k].clear();
@@ -311,7 +349,11 @@ int engine_tables(Engine& e) {
     int local = 0;
     for (int z = 0; z < d.nz; z++)
       for (int y = 0; y < d.ny; y += kBTY)
-        for (int x = 0; x < d.nx; x += kBTX) e.tiles1.push_back(BTile{(int)q, x, y, z, local++, cnt1});
+        for (int x = 0; x < d.nx; x += kBTX) {
+          e.tiles1.push_back(BTile{(int)q, x, y, z, local, cnt1});
+          if (e.members[q]->s.kind == 1) e.tilesDam.push_back(BTile{(int)q, x, y, z, local, cnt1});
+          local++;
+        }
     for (int k = 0; k < 4; k++) {
       const int rows = kBTY << k;
       const int cnt = tiles_of(d.nx, d.ny, d.nz, rows);
@@ -336,7 +378,7 @@ int engine_tables(Engine& e) {
     FlowScene f;
     f.d = b.d;
     f.code = b.code;
-    f.A0f = nullptr;
+    f.A0f = b.A0f;  // ghost-fluid diagonal of dam-break scenes
     f.P = b.P;
     f.r = b.res;
     f.z = b.tmp;
@@ -371,6 +413,11 @@ int engine_tables(Engine& e) {
   if (ensure_cap(&e.dTiles, &e.tilesCap, e.tiles1.size()) || ensure_cap(&e.dActive, &e.activeCap, e.tiles1.size()))
     return MG_ERR_CUDA;
   CKB(cudaMemcpyAsync(e.dTiles, e.tiles1.data(), sizeof(BTile) * e.tiles1.size(), cudaMemcpyHostToDevice, e.stream));
+  if (!e.tilesDam.empty()) {
+    if (ensure_cap(&e.dTilesDam, &e.tilesDamCap, e.tilesDam.size())) return MG_ERR_CUDA;
+    CKB(cudaMemcpyAsync(e.dTilesDam, e.tilesDam.data(), sizeof(BTile) * e.tilesDam.size(), cudaMemcpyHostToDevice,
+                        e.stream));
+  }
   e.dirty = false;
   return MG_OK;
 }
@@ -383,8 +430,10 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
   const int nt = (int)e.tiles1.size();
   cudaStream_t st = e.stream;
   const int cur = 0, nxt = 1;  // the table presents every scene's current buffers as 0
+  const int ntDam = (int)e.tilesDam.size();
   launch_b_inflow(e.dTiles, nt, e.dScenes, cur, st);
   launch_b_advect_velocity(e.dTiles, nt, e.dScenes, cur, st);
+  launch_b_dam_advect(e.dTilesDam, ntDam, e.dScenes, cur, st);
   launch_b_forces(e.dTiles, nt, e.dScenes, nxt, st);
   // GridCg setup of every scene (pressure.cpp:407-419): PcMIC in 3D with
   // (int)(cgMaxIterFac * max size) iterations at most; in 2D GridCg drops
@@ -402,7 +451,7 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
   }
   CKB(cudaMemcpyAsync(e.dSc, e.hSc.data(), sizeof(CgScalars) * nm, cudaMemcpyHostToDevice, st));
   CKB(cudaMemsetAsync(e.dDone, 0, sizeof(int), st));
-  launch_b_pressure_setup(e.dTiles, nt, e.dScenes, nxt, st);
+  launch_b_pressure_setup(e.dTiles, nt, e.dScenes, nxt, st, e.dTilesDam, ntDam);
   BatchMic mic;
   mic.flow = e.dFlow;
   mic.order = e.dOrder2;
@@ -474,6 +523,7 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
     }
   }
   launch_b_correct(e.dTiles, nt, e.dScenes, nxt, st);
+  launch_b_dam_correct(e.dTilesDam, ntDam, e.dScenes, nxt, st);
   CKB(cudaMemcpyAsync(e.hSc.data(), e.dSc, sizeof(CgScalars) * nm, cudaMemcpyDeviceToHost, st));
   CKB(cudaStreamSynchronize(st));
   CKB(cudaGetLastError());
@@ -641,6 +691,7 @@ extern "C" int mg_batch_sync(mg_batch b) {
 // =============================================================== served form
 namespace {
 struct Job {
+  int kind = 0;  // 0 plume, 1 dam break
   int nx, ny, nz;
   float gravity[3];
   unsigned long long seed;
@@ -694,13 +745,17 @@ extern "C" int mg_serve_set_solver(mg_server s, float cgAccuracy, float cgMaxIte
 }
 
 extern "C" size_t mg_serve_job_bytes(int nx, int ny, int nz) { return scene_bytes(nx, ny, nz); }
+extern "C" size_t mg_serve_job_bytes_kind(int kind, int nx, int ny, int nz) { return scene_bytes(nx, ny, nz, kind); }
 
-extern "C" int mg_serve_submit(mg_server s, int nx, int ny, int nz, const float* gravity, unsigned long long seed, int steps,
-                               double arrival, int keepResult, int* job) {
+extern "C" int mg_serve_submit_kind(mg_server s, int kind, int nx, int ny, int nz, const float* gravity,
+                                    unsigned long long seed, int steps, double arrival, int keepResult, int* job) {
   if (!s || !gravity || steps < 1 || arrival < 0.) return set_error(MG_ERR_ARG, "mg_serve_submit: invalid argument");
+  if (kind != 0 && kind != 1) return set_error(MG_ERR_ARG, "mg_serve_submit: kind is 0 (plume) or 1 (dam break)");
   if (nx < 3 || ny < 3 || nz < 1 || (nz > 1 && nz < 3)) return set_error(MG_ERR_ARG, "mg_serve_submit: scene is too small");
-  if (scene_bytes(nx, ny, nz) > s->budget) return set_error(MG_ERR_ARG, "mg_serve_submit: the job alone exceeds the memory budget");
+  if (scene_bytes(nx, ny, nz, kind) > s->budget)
+    return set_error(MG_ERR_ARG, "mg_serve_submit: the job alone exceeds the memory budget");
   Job j;
+  j.kind = kind;
   j.nx = nx;
   j.ny = ny;
   j.nz = nz;
@@ -712,6 +767,11 @@ extern "C" int mg_serve_submit(mg_server s, int nx, int ny, int nz, const float*
   s->jobs.push_back(std::move(j));
   if (job) *job = (int)s->jobs.size() - 1;
   return MG_OK;
+}
+
+extern "C" int mg_serve_submit(mg_server s, int nx, int ny, int nz, const float* gravity, unsigned long long seed, int steps,
+                               double arrival, int keepResult, int* job) {
+  return mg_serve_submit_kind(s, 0, nx, ny, nz, gravity, seed, steps, arrival, keepResult, job);
 }
 
 // run until every submitted job has finished.  Arrival times are honoured
@@ -734,9 +794,9 @@ extern "C" int mg_serve_run(mg_server s, mg_serve_stats* stats) {
     while (next < order.size()) {
       Job& j = s->jobs[order[next]];
       if (j.arrival > tn) break;
-      if (s->e.liveBytes + scene_bytes(j.nx, j.ny, j.nz) > s->budget) break;
+      if (s->e.liveBytes + scene_bytes(j.nx, j.ny, j.nz, j.kind) > s->budget) break;
       SceneRec* r = nullptr;
-      const int st = scene_add(s->e, j.nx, j.ny, j.nz, j.gravity, j.seed, &r);
+      const int st = scene_add(s->e, j.nx, j.ny, j.nz, j.gravity, j.seed, &r, j.kind);
       if (st) return st;
       j.rec = r;
       j.admitted = now();

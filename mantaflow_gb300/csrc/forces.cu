@@ -84,9 +84,9 @@ __global__ void k_add_buoyancy(Dims d, const int* __restrict__ flags, const floa
 }
 
 // KnApplyForce additive (extforces.cpp:46-58)
-__global__ void k_add_force(Dims d, const int* __restrict__ flags, Mac vel, float fx, float fy, float fz,
-                            const float* __restrict__ exclude) {
-  CELL_IJK
+__device__ __forceinline__ void add_force_cell(const Dims& d, const int* __restrict__ flags, Mac vel, float fx, float fy,
+                                               float fz, const float* __restrict__ exclude, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   if (!INNER) return;
   const int f = __ldg(flags + idx);
   const bool curFluid = f & kFluid, curEmpty = f & kEmpty;
@@ -96,11 +96,18 @@ __global__ void k_add_force(Dims d, const int* __restrict__ flags, Mac vel, floa
   if (isF(flags, idx - d.sy) || (curFluid && isE(flags, idx - d.sy))) vel.v[idx] = vel.v[idx] + fy;
   if (d.is3d && (isF(flags, idx - d.sz) || (curFluid && isE(flags, idx - d.sz)))) vel.w[idx] = vel.w[idx] + fz;
 }
+__global__ void k_add_force(Dims d, const int* __restrict__ flags, Mac vel, float fx, float fy, float fz,
+                            const float* __restrict__ exclude) {
+  CELL_IJK
+  (void)idx;
+  add_force_cell(d, flags, vel, fx, fy, fz, exclude, i, j, k);
+}
 
 // extrapolateMACSimple marking (fastmarch.cpp:350-362): tmp = 1 on faces of
 // component c next to fluid, 0 elsewhere (also clears the border)
-__global__ void k_extrap_mark(Dims d, const int* __restrict__ flags, int* tmp, int c, int intoObs) {
-  CELL_IJK
+__device__ __forceinline__ void extrap_mark_cell(const Dims& d, const int* __restrict__ flags, int* tmp, int c, int intoObs,
+                                                 int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   int mark = 0;
   if (INNER) {
     const long long nb = idx - (c == 0 ? 1 : (c == 1 ? d.sy : d.sz));
@@ -109,12 +116,17 @@ __global__ void k_extrap_mark(Dims d, const int* __restrict__ flags, int* tmp, i
   }
   tmp[idx] = mark;
 }
+__global__ void k_extrap_mark(Dims d, const int* __restrict__ flags, int* tmp, int c, int intoObs) {
+  CELL_IJK
+  (void)idx;
+  extrap_mark_cell(d, flags, tmp, c, intoObs, i, j, k);
+}
 
 // knExtrapolateMACSimple (fastmarch.cpp:230-258).  The reference updates in
 // place; a cell only reads neighbours marked with layer d and writes d+1,
 // so the result does not depend on the visiting order.
-__global__ void k_extrap_layer(Dims d, float* comp, int* tmp, int layer) {
-  CELL_IJK
+__device__ __forceinline__ void extrap_layer_cell(const Dims& d, float* comp, int* tmp, int layer, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   if (!INNER) return;
   if (tmp[idx] != 0) return;
   const long long nb[6] = {1, -1, d.sy, -d.sy, d.sz, -d.sz};
@@ -131,10 +143,16 @@ __global__ void k_extrap_layer(Dims d, float* comp, int* tmp, int layer) {
     comp[idx] = avg / (float)nbs;
   }
 }
+__global__ void k_extrap_layer(Dims d, float* comp, int* tmp, int layer) {
+  CELL_IJK
+  (void)idx;
+  extrap_layer_cell(d, comp, tmp, layer, i, j, k);
+}
 
 // knExtrapolateIntoBnd (fastmarch.cpp:260-300) reading a snapshot
-__global__ void k_extrap_into_bnd(Dims d, const int* __restrict__ flags, Mac vel, CMac vt) {
-  CELL_IJK
+__device__ __forceinline__ void extrap_into_bnd_cell(const Dims& d, const int* __restrict__ flags, Mac vel, CMac vt, int i,
+                                                     int j, int k) {
+  const long long idx = ix(d, i, j, k);
   int cc = 0;
   float v0 = 0.f, v1 = 0.f, v2 = 0.f;
   const bool obs = isO(flags, idx);
@@ -153,6 +171,11 @@ __global__ void k_extrap_into_bnd(Dims d, const int* __restrict__ flags, Mac vel
     vel.v[idx] = v1 / (float)cc;
     vel.w[idx] = v2 / (float)cc;
   }
+}
+__global__ void k_extrap_into_bnd(Dims d, const int* __restrict__ flags, Mac vel, CMac vt) {
+  CELL_IJK
+  (void)idx;
+  extrap_into_bnd_cell(d, flags, vel, vt, i, j, k);
 }
 
 // ------------------------------------------------------- levelset extrapolation
@@ -258,14 +281,17 @@ __global__ void k_reset_outflow(Dims d, int* flags, float* phi, float* real) {
 }
 
 // FlagGrid::updateFromLevelset (grid.cpp:844-854), invalid time -1000
-__global__ void k_update_from_levelset(Dims d, int* flags, const float* __restrict__ phi) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= d.n) return;
+__device__ __forceinline__ void update_from_levelset_cell(int* flags, const float* __restrict__ phi, long long idx) {
   const int f = flags[idx];
   if ((f & kObstacle) || (f & kOutflow)) return;
   const float p = phi[idx];
   if (p <= -1000.f) return;
   flags[idx] = (f & ~(kEmpty | kFluid)) | (p <= 0.f ? kFluid : kEmpty);
+}
+__global__ void k_update_from_levelset(Dims d, int* flags, const float* __restrict__ phi) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= d.n) return;
+  update_from_levelset_cell(flags, phi, idx);
 }
 
 __device__ __forceinline__ float smax(float a, float b) { return a < b ? b : a; }
@@ -532,6 +558,7 @@ int launch_minmax_partial(long long n, const float* a, float* part, cudaStream_t
 // inflow: density = max(density, U[0,1) * source) (Grid::join, grid.cpp:303-311)
 __global__ void __launch_bounds__(256) k_b_inflow(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int cur) {
   BATCH_CELL
+  if (sc.kind != 0) return;  // plume scenes only
   const long long idx = ix(d, i, j, k);
   const float b = batch_noise(sc.seed, sc.step, idx) * sc.mask[idx];
   float* a = sc.dens[cur];
@@ -540,13 +567,87 @@ __global__ void __launch_bounds__(256) k_b_inflow(const BTile* __restrict__ tile
 }
 // setWallBcs then addBuoyancy: both read and write only their own cell's
 // velocity, so one pass applies them in the reference's order
+// (dam break: addGravity, then setWallBcs; also one pass)
 __global__ void __launch_bounds__(256) k_b_forces(const BTile* __restrict__ tiles, const BScene* __restrict__ S, int nxt) {
   BATCH_CELL
   const Mac v = bmac(sc.vel[nxt], d.n);
-  set_wall_bcs_cell(d, sc.flags, v, CMac{nullptr, nullptr, nullptr}, 0, i, j, k);
-  add_buoyancy_cell(d, sc.flags, sc.dens[nxt], v, sc.bx, sc.by, sc.bz, i, j, k);
+  if (sc.kind == 0) {
+    set_wall_bcs_cell(d, sc.flags, v, CMac{nullptr, nullptr, nullptr}, 0, i, j, k);
+    add_buoyancy_cell(d, sc.flags, sc.dens[nxt], v, sc.bx, sc.by, sc.bz, i, j, k);
+  } else {
+    add_force_cell(d, sc.flags, v, sc.bx, sc.by, sc.bz, nullptr, i, j, k);
+    set_wall_bcs_cell(d, sc.flags, v, CMac{nullptr, nullptr, nullptr}, 0, i, j, k);
+  }
+}
+
+// ---- dam-break passes over the dam scenes' tiles
+// extrapolateMACSimple(flags, vel, distance=4) (fastmarch.cpp:337-375) on
+// the current velocity: marks and layers per component, then the domain
+// sides from a snapshot (in the scene's forward scratch)
+__global__ void __launch_bounds__(256) k_b_dam_extrap_mark(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                           int c) {
+  BATCH_CELL
+  if (c >= (d.is3d ? 3 : 2)) return;  // 2D: x and y only
+  extrap_mark_cell(d, sc.flags, sc.itmp, c, 0, i, j, k);
+}
+__global__ void __launch_bounds__(256) k_b_dam_extrap_layer(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                            int cur, int c, int layer) {
+  BATCH_CELL
+  if (c >= (d.is3d ? 3 : 2)) return;
+  extrap_layer_cell(d, sc.vel[cur] + (long long)c * d.n, sc.itmp, layer, i, j, k);
+}
+__global__ void __launch_bounds__(256) k_b_dam_snapshot(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                        int cur) {
+  BATCH_CELL
+  const long long idx = ix(d, i, j, k);
+  for (int c = 0; c < 3; c++) sc.fwd[c * d.n + idx] = sc.vel[cur][c * d.n + idx];
+}
+__global__ void __launch_bounds__(256) k_b_dam_extrap_bnd(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                          int cur) {
+  BATCH_CELL
+  extrap_into_bnd_cell(d, sc.flags, bmac(sc.vel[cur], d.n), bcmac(sc.fwd, d.n), i, j, k);
+}
+// FlagGrid::updateFromLevelset (grid.cpp:844-854) from the advected phi
+__global__ void __launch_bounds__(256) k_b_dam_flags(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                     int nxt) {
+  BATCH_CELL
+  update_from_levelset_cell(sc.flags, sc.dens[nxt], ix(d, i, j, k));
+}
+// the final setWallBcs of the dam-break step
+__global__ void __launch_bounds__(256) k_b_dam_walls(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                     int nxt) {
+  BATCH_CELL
+  set_wall_bcs_cell(d, sc.flags, bmac(sc.vel[nxt], d.n), CMac{nullptr, nullptr, nullptr}, 0, i, j, k);
 }
 #undef BATCH_CELL
+
+void launch_b_dam_advect_sl(const BTile* t, int nt, const BScene* s, int cur, bool vel, cudaStream_t st);
+
+void launch_b_dam_advect(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st) {
+  if (nt == 0) return;
+  const dim3 b(kBTX, kBTY, 1);
+  for (int c = 0; c < 3; c++) {  // 2D scenes skip c = 2 in the kernels
+    count_launch();
+    k_b_dam_extrap_mark<<<nt, b, 0, st>>>(t, s, c);
+    for (int l = 1; l <= 4; l++) {
+      count_launch();
+      k_b_dam_extrap_layer<<<nt, b, 0, st>>>(t, s, cur, c, l);
+    }
+  }
+  count_launch();
+  k_b_dam_snapshot<<<nt, b, 0, st>>>(t, s, cur);
+  count_launch();
+  k_b_dam_extrap_bnd<<<nt, b, 0, st>>>(t, s, cur);
+  launch_b_dam_advect_sl(t, nt, s, cur, false, st);
+  count_launch();
+  k_b_dam_flags<<<nt, b, 0, st>>>(t, s, 1 - cur);
+  launch_b_dam_advect_sl(t, nt, s, cur, true, st);
+}
+
+void launch_b_dam_walls(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
+  count_launch();
+  k_b_dam_walls<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, nxt);
+}
 
 void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st) {
   count_launch();

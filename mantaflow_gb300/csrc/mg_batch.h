@@ -55,8 +55,15 @@ struct BScene {
   float* P;
   unsigned long long* face;
   int mic, tx, ty, tz;
+  // kind 0: smoke plume.  kind 1: dam break (free-surface liquid; dens[]
+  // holds the levelset phi, A0f the ghost-fluid diagonal, itmp the marks of
+  // the MAC extrapolation)
+  int kind;
+  float* A0f;
+  int* itmp;
   float dt;
-  float bx, by, bz;  // buoyancy factors -gravity*dt/dx*coefficient (KnAddBuoyancy), 0.5 applied in-kernel
+  float bx, by, bz;  // plume: buoyancy factors -gravity*dt/dx (KnAddBuoyancy), 0.5 applied in-kernel;
+                     // dam break: the gravity force gravity*dt/dx (KnApplyForce)
   unsigned long long seed;
   int step;        // steps this scene has taken: the inflow noise index
   int ntiles;
@@ -70,7 +77,10 @@ void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, cudaStrea
 void launch_b_advect_density(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_advect_velocity(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_forces(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
-void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
+// MakeRhs + codes, the dam scenes' ghost-fluid diagonal (their own tile
+// list), GridCg::doInit
+void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st, const BTile* tDam,
+                             int ntDam);
 // the MIC(0) sweeps of a batch: the FlowScene table of its MIC scenes, the
 // (scene, tile) dispatch order, and the BScene index of each MIC scene
 struct BatchMic {
@@ -92,6 +102,12 @@ void launch_b_mic_init(const BTile* t, int nt, const BScene* s, const BatchMic& 
 void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int rows, int* ndone, const BatchMic* mic,
                             cudaStream_t st);
 void launch_b_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
+// dam-break scenes (over their own tiles): extrapolateMACSimple(vel, 4),
+// advect phi and velocity (SL order 1), updateFromLevelset; after the
+// solve's velocity update, the ghost-fluid corrections and setWallBcs
+void launch_b_dam_advect(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
+void launch_b_dam_gf_diag(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
+void launch_b_dam_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
 // uniform [0,1) inflow noise of a scene's cell at a step (the batch's
 // per-scene seeded source); also used to fill single-scene grids for
 // comparisons

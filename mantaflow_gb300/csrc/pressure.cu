@@ -194,9 +194,10 @@ __global__ void k_make_codes_low(Dims d, code_t* code) {
 }
 
 // ApplyGhostFluidDiagonal (pressure.cpp:136-151): float diagonal
-__global__ void k_ghost_fluid_diag(Dims d, const int* __restrict__ flags, const code_t* __restrict__ code,
-                                   const float* __restrict__ phi, float gfClamp, float* A0f) {
-  CELL_IJK
+__device__ __forceinline__ void ghost_fluid_diag_cell(const Dims& d, const int* __restrict__ flags,
+                                                      const code_t* __restrict__ code, const float* __restrict__ phi,
+                                                      float gfClamp, float* A0f, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   float a = (float)(code[idx] & 7);
   if (INNER && isF(flags, idx)) {
     const long long X = 1, Y = d.sy, Z = d.sz;
@@ -210,6 +211,12 @@ __global__ void k_ghost_fluid_diag(Dims d, const int* __restrict__ flags, const 
     }
   }
   A0f[idx] = a;
+}
+__global__ void k_ghost_fluid_diag(Dims d, const int* __restrict__ flags, const code_t* __restrict__ code,
+                                   const float* __restrict__ phi, float gfClamp, float* A0f) {
+  CELL_IJK
+  (void)idx;
+  ghost_fluid_diag_cell(d, flags, code, phi, gfClamp, A0f, i, j, k);
 }
 
 // CountEmptyCells (pressure.cpp:217-220)
@@ -1016,9 +1023,11 @@ __global__ void k_correct_velocity(Dims d, const int* __restrict__ flags, Mac ve
 }
 
 // knCorrectVelocityGhostFluid (pressure.cpp:154-187)
-__global__ void k_correct_velocity_gf(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ p,
-                                      const float* __restrict__ phi, float gfc, const float* __restrict__ curv, float st) {
-  CELL_IJK
+__device__ __forceinline__ void correct_velocity_gf_cell(const Dims& d, const int* __restrict__ flags, Mac vel,
+                                                         const float* __restrict__ p, const float* __restrict__ phi,
+                                                         float gfc, const float* __restrict__ curv, float st, int i,
+                                                         int j, int k) {
+  const long long idx = ix(d, i, j, k);
   if (!INNER) return;
   const long long X = 1, Y = d.sy, Z = d.sz;
   float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
@@ -1047,8 +1056,16 @@ __global__ void k_correct_velocity_gf(Dims d, const int* __restrict__ flags, Mac
 
 // knReplaceClampedGhostFluidVels (pressure.cpp:198-214): writes only empty
 // cells and reads only fluid ones, so it is race free in place.
-__global__ void k_replace_clamped_gf(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ phi, float gfc) {
+__global__ void k_correct_velocity_gf(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ p,
+                                      const float* __restrict__ phi, float gfc, const float* __restrict__ curv, float st) {
   CELL_IJK
+  (void)idx;
+  correct_velocity_gf_cell(d, flags, vel, p, phi, gfc, curv, st, i, j, k);
+}
+
+__device__ __forceinline__ void replace_clamped_gf_cell(const Dims& d, const int* __restrict__ flags, Mac vel,
+                                                        const float* __restrict__ phi, float gfc, int i, int j, int k) {
+  const long long idx = ix(d, i, j, k);
   if (!INNER) return;
   if (!isE(flags, idx)) return;
   const long long X = 1, Y = d.sy, Z = d.sz;
@@ -1060,6 +1077,11 @@ __global__ void k_replace_clamped_gf(Dims d, const int* __restrict__ flags, Mac 
   if (isF(flags, idx + Y) && CLAMPED(idx + Y, -Y)) vel.v[idx] = vel.v[idx + Y];
   if (d.is3d && isF(flags, idx + Z) && CLAMPED(idx + Z, -Z)) vel.w[idx] = vel.w[idx + Z];
 #undef CLAMPED
+}
+__global__ void k_replace_clamped_gf(Dims d, const int* __restrict__ flags, Mac vel, const float* __restrict__ phi, float gfc) {
+  CELL_IJK
+  (void)idx;
+  replace_clamped_gf_cell(d, flags, vel, phi, gfc, i, j, k);
 }
 
 // ------------------------------------------------------------- launchers
@@ -1319,7 +1341,7 @@ __global__ void __launch_bounds__(256) k_b_pcg_spmv(const BTile* __restrict__ ti
       if (!(c & kCodeFluid)) {
         v = xc;
       } else {
-        v = xc * (float)(c & 7);
+        v = xc * (sc.A0f ? sc.A0f[idx] : (float)(c & 7));
         if (c & kLowX) v = v - x[idx - 1];
         if (c & kHighX) v = v - x[idx + 1];
         if (c & kLowY) v = v - x[idx - d.sy];
@@ -1453,6 +1475,32 @@ __global__ void __launch_bounds__(256) k_b_mic_search(const BTile* __restrict__ 
   sc.search[idx] = sc.tmp[idx];
 }
 
+// dam break: ApplyGhostFluidDiagonal from the advected phi (pass-1 codes)
+__global__ void __launch_bounds__(256) k_b_dam_gf_diag(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                       int nxt) {
+  BATCH_TILE
+  if (!in) return;
+  (void)idx;
+  ghost_fluid_diag_cell(d, sc.flags, sc.code, sc.dens[nxt], 1e-4f, sc.A0f, i, j, k);
+}
+// dam break: knCorrectVelocityGhostFluid, then knReplaceClampedGhostFluidVels
+// (pressure.cpp:154-214), each a pass of its own (the second reads
+// neighbours' corrected velocities)
+__global__ void __launch_bounds__(256) k_b_dam_correct_gf(const BTile* __restrict__ tiles, const BScene* __restrict__ S,
+                                                          int nxt) {
+  BATCH_TILE
+  if (!in) return;
+  (void)idx;
+  correct_velocity_gf_cell(d, sc.flags, bmac(sc.vel[nxt], d.n), sc.pres, sc.dens[nxt], 1e-4f, nullptr, 0.f, i, j, k);
+}
+__global__ void __launch_bounds__(256) k_b_dam_replace_clamped(const BTile* __restrict__ tiles,
+                                                               const BScene* __restrict__ S, int nxt) {
+  BATCH_TILE
+  if (!in) return;
+  (void)idx;
+  replace_clamped_gf_cell(d, sc.flags, bmac(sc.vel[nxt], d.n), sc.dens[nxt], 1e-4f, i, j, k);
+}
+
 #undef BATCH_TILE
 
 // sigma (doInit) or beta (iterate) of each MIC scene from the per-tile
@@ -1491,10 +1539,13 @@ void launch_b_mic_init(const BTile* t, int nt, const BScene* s, const BatchMic& 
   k_b_mic_search<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s);
 }
 
-void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
+void launch_b_dam_gf_diag(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
+void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st, const BTile* tDam,
+                             int ntDam) {
   const dim3 b(kBTX, kBTY, 1);
   count_launch();
   k_b_rhs_codes<<<nt, b, 0, st>>>(t, s, nxt);
+  launch_b_dam_gf_diag(tDam, ntDam, s, nxt, st);
   count_launch();
   k_b_pcg_init<<<nt, b, 0, st>>>(t, s);
 }
@@ -1528,6 +1579,20 @@ void launch_b_pcg_iteration(const BTile* t, int nt, const BScene* s, int rows, i
 void launch_b_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
   count_launch();
   k_b_correct<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, nxt);
+}
+void launch_b_dam_gf_diag(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
+  if (nt == 0) return;
+  count_launch();
+  k_b_dam_gf_diag<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, nxt);
+}
+void launch_b_dam_walls(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
+void launch_b_dam_correct(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st) {
+  if (nt == 0) return;
+  count_launch();
+  k_b_dam_correct_gf<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, nxt);
+  count_launch();
+  k_b_dam_replace_clamped<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s, nxt);
+  launch_b_dam_walls(t, nt, s, nxt, st);
 }
 
 }  // namespace mgpu
