@@ -435,22 +435,49 @@ def batched_form(m, steps, seed, plain_steps, acc_steps, sim_steps=100):
                 batched["sims_per_hour"] / plain["sims_per_hour"], "accuracy_vs_fp64": acc}
 
 
-def served_form(m, seed, njobs, step_scale, rate=20.0, budget=150 * 10 ** 9):
-    """Config 5 on a bounded sample: a Poisson stream (rate jobs/s) of 3D
-    plume jobs with sides U{32..128} and U{100..400} steps (divided by
-    step_scale to bound the run), per-job seeds; served (continuous batching
-    under the HBM budget) against the plain sequential path (each job alone
-    through the scene API, first come first served, PcMIC as in config 1)."""
+def _plain_dam(m, n):
+    """the dam-break scene (config 3's setup) on the plain per-scene path"""
+    s = m.Solver(name="dam", gridSize=m.vec3(n, n, n), dim=3)
+    s.timestep = 1.0
+    flags = s.create(m.FlagGrid)
+    flags.initDomain(boundaryWidth=0)
+    box = s.create(m.Box, p0=m.vec3(0, 0, 0), p1=m.vec3(n * 0.4, n * 0.6, n))
+    phi = box.computeLevelset()
+    flags.updateFromLevelset(phi)
+    return {"s": s, "flags": flags, "phi": phi, "vel": s.create(m.MACGrid), "pres": s.create(m.RealGrid)}
+
+
+def _plain_dam_step(m, g):
+    m.extrapolateMACSimple(flags=g["flags"], vel=g["vel"], distance=4)
+    m.advectSemiLagrange(flags=g["flags"], vel=g["vel"], grid=g["phi"], order=1)
+    g["flags"].updateFromLevelset(g["phi"])
+    m.advectSemiLagrange(flags=g["flags"], vel=g["vel"], grid=g["vel"], order=1)
+    m.addGravity(flags=g["flags"], vel=g["vel"], gravity=m.vec3(0, -1e-3, 0))
+    m.setWallBcs(flags=g["flags"], vel=g["vel"])
+    m.solvePressure(flags=g["flags"], vel=g["vel"], pressure=g["pres"], phi=g["phi"])
+    m.setWallBcs(flags=g["flags"], vel=g["vel"])
+
+
+def served_form(m, seed, njobs, plain_sample, rate=20.0, budget=150 * 10 ** 9):
+    """Config 5: a Poisson stream (rate jobs/s) of 3D jobs, half smoke plume
+    and half dam break, sides U{32..128}, steps U{100..400}, per-job seeds;
+    served (continuous batching under the HBM budget) against the plain
+    sequential path (each job alone through the scene API, first come first
+    served).  The plain path's time per job is its measured step time
+    (`plain_sample` steps after one untimed) times the job's steps; its job
+    latencies follow from the arrivals in first-come order."""
     from mantaflow_gb300 import batch as mb
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs))
     sides = rng.integers(32, 129, njobs)
-    steps = np.maximum(1, rng.integers(100, 401, njobs) // step_scale)
+    steps = rng.integers(100, 401, njobs)
+    kinds = rng.integers(0, 2, njobs)
     grav = rng.uniform(1e-3, 8e-3, njobs)
     seeds = rng.integers(1, 2 ** 62, njobs)
     srv = mb.PlumeServer(budget_bytes=budget)
-    ids = [srv.submit((int(n),) * 3, (0.0, -float(g), 0.0), int(sd), int(k), float(a))
-           for n, g, sd, k, a in zip(sides, grav, seeds, steps, arrivals)]
+    ids = [srv.submit((int(n),) * 3, (0.0, -(float(g) if kd == 0 else 1e-3), 0.0), int(sd), int(k), float(a),
+                      kind=int(kd))
+           for n, g, sd, k, a, kd in zip(sides, grav, seeds, steps, arrivals, kinds)]
     st = srv.run()
     infos = [srv.job(q) for q in ids]
     tick_ms, tick_jobs = srv.ticks()
@@ -461,47 +488,45 @@ def served_form(m, seed, njobs, step_scale, rate=20.0, budget=150 * 10 ** 9):
               "step_ms_p50": float(np.percentile(step_lat, 50)), "step_ms_p99": float(np.percentile(step_lat, 99)),
               "job_s_p50": float(np.percentile(job_lat, 50)), "job_s_p99": float(np.percentile(job_lat, 99)),
               "peak_device_bytes": st["peak_bytes"], "max_resident_jobs": int(max(tick_jobs))}
-    # plain sequential path: one job at a time, in arrival order
-    t0 = time.perf_counter()
-    plain_steps, plain_jobs, cell_steps = [], [], 0
-    for n, g, sd, k, a in zip(sides, grav, seeds, steps, arrivals):
-        while time.perf_counter() - t0 < a:
-            time.sleep(min(0.005, a - (time.perf_counter() - t0)))
+    # plain sequential path: each job's step time measured, one job at a time
+    job_time, plain_steps, cell_steps = [], [], 0
+    for n, g, sd, k, kd in zip(sides, grav, seeds, steps, kinds):
         n = int(n)
-        s = m.Solver(name="job", gridSize=m.vec3(n, n, n), dim=3)
-        flags = s.create(m.FlagGrid)
-        flags.initDomain(boundaryWidth=0)
-        flags.fillGrid()
-        m.setOpenBound(flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
-        vel, dens, pres, src = s.create(m.MACGrid), s.create(m.RealGrid), s.create(m.RealGrid), s.create(m.RealGrid)
-        gs = m.vec3(n, n, n)
-        mask = s.create(m.RealGrid)
-        s.create(m.Cylinder, center=gs * m.vec3(0.5, 0.1, 0.5), radius=n * 0.14,
-                 z=gs * m.vec3(0, 0.02, 0)).applyToGrid(grid=mask, value=1.0)
-        mk = mask.numpy()
-        r = np.random.default_rng(int(sd) % (2 ** 32))
-        for t in range(int(k)):
-            m.copyArrayToGridReal((r.random(mk.shape, dtype=np.float32) * mk).astype(np.float32), src)
-            ts = time.perf_counter()
-            dens.join(src)
-            m.advectSemiLagrange(flags=flags, vel=vel, grid=dens, order=2, clampMode=2)
-            m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=2, clampMode=2)
-            m.setWallBcs(flags=flags, vel=vel)
-            m.addBuoyancy(density=dens, vel=vel, gravity=m.vec3(0, -float(g), 0), flags=flags)
-            m.solvePressure(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, preconditioner=m.PcMIC)
-            s.sync()
-            plain_steps.append(time.perf_counter() - ts)
-            cell_steps += n ** 3
-        plain_jobs.append(time.perf_counter() - t0 - a)
-        del s
-    wall = time.perf_counter() - t0
-    plain = {"cells_per_s": cell_steps / wall, "wall_s": wall,
+        ts = []
+        if kd == 0:
+            pg = _plain_plume(m, (n, n, n), (0.0, -float(g), 0.0))
+            r = np.random.default_rng(int(sd) % (2 ** 32))
+        else:
+            pg = _plain_dam(m, n)
+        for t in range(plain_sample + 1):
+            if kd == 0:
+                a = (r.random((n, n, n), dtype=np.float32) * pg["mask"]).astype(np.float32)
+            pg["s"].sync()
+            t0 = time.perf_counter()
+            if kd == 0:
+                _plain_step(m, pg, a)
+            else:
+                _plain_dam_step(m, pg)
+            pg["s"].sync()
+            if t > 0:
+                ts.append(time.perf_counter() - t0)
+        plain_steps += ts
+        job_time.append(statistics.mean(ts) * int(k))
+        cell_steps += n ** 3 * int(k)
+        del pg
+    end, plain_lat = 0.0, []
+    for a, jt in zip(arrivals, job_time):
+        end = max(end, float(a)) + jt
+        plain_lat.append(end - float(a))
+    plain = {"cells_per_s": cell_steps / end, "wall_s": end,
              "step_ms_p50": 1e3 * float(np.percentile(plain_steps, 50)),
              "step_ms_p99": 1e3 * float(np.percentile(plain_steps, 99)),
-             "job_s_p50": float(np.percentile(plain_jobs, 50)), "job_s_p99": float(np.percentile(plain_jobs, 99))}
-    return {"workload": "config 5 sample: %d 3D plume jobs, Poisson arrivals %.0f/s, sides U{32..128}, steps "
-                        "U{100..400}/%d, HBM budget %.0f GB; dam-break jobs are not in the served form"
-                        % (njobs, rate, step_scale, budget / 1e9),
+             "job_s_p50": float(np.percentile(plain_lat, 50)), "job_s_p99": float(np.percentile(plain_lat, 99)),
+             "sample": "each job's step time measured over %d steps after one untimed, times its steps; "
+                       "first-come-first-served schedule from the arrivals" % plain_sample}
+    return {"workload": "config 5: %d 3D jobs (%d plume, %d dam break), Poisson arrivals %.0f/s, sides U{32..128}, "
+                        "steps U{100..400}, HBM budget %.0f GB" % (njobs, int((kinds == 0).sum()),
+                                                                    int((kinds == 1).sum()), rate, budget / 1e9),
             "served": served, "plain_sequential": plain,
             "throughput_ratio": served["cells_per_s"] / plain["cells_per_s"]}
 
@@ -574,8 +599,9 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps per scene of the plain path")
     ap.add_argument("--accuracy-steps", type=int, default=5,
                     help="steps of the batched/plain accuracy sample against the FP64 oracle (0: skip)")
-    ap.add_argument("--served-jobs", type=int, default=24, help="jobs of the config-5 served sample (0: skip)")
-    ap.add_argument("--served-step-scale", type=int, default=10)
+    ap.add_argument("--served-jobs", type=int, default=32, help="jobs of the config-5 served run (0: skip)")
+    ap.add_argument("--served-plain-sample", type=int, default=3,
+                    help="timed steps per job measuring the plain sequential path")
     ap.add_argument("--refined-steps", type=int, default=5,
                     help="timed 256^3 steps of the FP64-refined form reported beside the headline (0: skip)")
     args = ap.parse_args()
@@ -764,7 +790,7 @@ def main():
         batched = batched_form(m, args.batched_steps, args.seed + 13, args.plain_steps, args.accuracy_steps)
     served = None
     if args.served_jobs > 0 and rank == 0:
-        served = served_form(m, args.seed + 17, args.served_jobs, args.served_step_scale)
+        served = served_form(m, args.seed + 17, args.served_jobs, args.served_plain_sample)
     precision = None
     if args.precision_size > 0 and rank == 0 and world == 1:
         precision = precision_form(m, args.precision_size, args.precision_steps, args.seed + 5)
