@@ -233,8 +233,11 @@ typedef struct {
 } mg_pressure_result;
 
 void mg_pressure_params_default(mg_pressure_params* p);
-/* solvePressure (:480-521).  phi, perCellCorr, curv, retRhs may be NULL;
- * fractions and obvel must be NULL.  out may be NULL. */
+/* solvePressure (:480-521).  phi, perCellCorr, fractions, obvel, curv,
+ * retRhs may be NULL; out may be NULL.  With fractions (a MACGrid of face
+ * fractions, MakeLaplaceMatrix's float form) the matrix is stored as floats
+ * and MIC(0) runs plane by plane; fractions with PcMGStatic/PcMGDynamic or
+ * with pressure fixing return MG_ERR_UNSUPPORTED. */
 int mg_solve_pressure(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p, mg_grid phi,
                       mg_grid perCellCorr, mg_grid fractions, mg_grid obvel, mg_grid curv, mg_grid retRhs,
                       mg_pressure_result* out);

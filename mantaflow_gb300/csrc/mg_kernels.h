@@ -76,7 +76,10 @@ struct PcgBuffers {
   Dims d;
   const int* flags;
   code_t* code;
-  float* A0f;       // non-null with ghost fluid: float diagonal
+  float* A0f;       // non-null with ghost fluid or fractions: float diagonal
+  float* Aif;       // non-null with fractions: float off-diagonals (the
+  float* Ajf;       // reference's stored Ai, Aj, Ak; the codes still carry
+  float* Akf;       // the fluid bit and the links)
   float* rhs;
   float* pressure;
   float* residual;
@@ -100,8 +103,16 @@ struct MicPlan {
 };
 
 // sums: also the per-block sums of rhs and fluid cells (enforceCompatibility)
+// frac / obvel: the fractions and obstacle-velocity MAC grids (three planes
+// of n floats each) or null
 void launch_make_rhs(const PcgBuffers& b, const float* vu, const float* vv, const float* vw, const float* perCellCorr,
-                     const float* phi, const float* curv, float surfTens, float gfClamp, bool sums, cudaStream_t s);
+                     const float* phi, const float* curv, float surfTens, float gfClamp, bool sums, cudaStream_t s,
+                     const float* frac = nullptr, const float* obvel = nullptr);
+// MakeLaplaceMatrix with fractions: b.A0f and b.Aif/Ajf/Akf
+void launch_make_frac_matrix(const PcgBuffers& b, const float* frac, cudaStream_t s);
+// the stored-coefficient MIC(0) (fractions): one launch per i+j+k plane;
+// mode 0 factor, 1 forward, 2 backward (+beta), 3 backward for doInit (+sigma)
+void launch_mic_planes(const PcgBuffers& b, int mode, cudaStream_t s);
 void launch_compat_shift(const PcgBuffers& b, cudaStream_t s);
 void launch_make_codes(const PcgBuffers& b, cudaStream_t s);
 void launch_ghost_fluid_diag(const PcgBuffers& b, const float* phi, float gfClamp, cudaStream_t s);

@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict_
                                                   const float* __restrict__ vv, const float* __restrict__ vw,
                                                   const float* __restrict__ corr, const float* __restrict__ phi,
                                                   const float* __restrict__ curv, float surfTens, float gfClamp,
-                                                  double* part, CgScalars* sc, unsigned int nblk);
+                                                  double* part, CgScalars* sc, unsigned int nblk,
+                                                  const float* __restrict__ frac, const float* __restrict__ obv);
 
 __device__ __forceinline__ float theta_helper(float inside, float outside) {
   const float denom = inside - outside;
@@ -81,7 +82,8 @@ __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict_
                                                   const float* __restrict__ vv, const float* __restrict__ vw,
                                                   const float* __restrict__ corr, const float* __restrict__ phi,
                                                   const float* __restrict__ curv, float surfTens, float gfClamp,
-                                                  double* part, CgScalars* sc, unsigned int nblk) {
+                                                  double* part, CgScalars* sc, unsigned int nblk,
+                                                  const float* __restrict__ frac, const float* __restrict__ obv) {
   double sum = 0.;
   double cnt = 0.;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,7 +95,23 @@ __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict_
       if (!isF(flags, idx)) {
         rhs[idx] = 0.f;
       } else {
-        float set = mac_neg_div(d, vu, vv, vw, idx);
+        float set;
+        if (!frac) {
+          set = mac_neg_div(d, vu, vv, vw, idx);
+        } else {
+          // the fraction-weighted divergence, and the obstacle velocity's
+          // share of the faces (pressure.cpp:50-60)
+          const float *fu = frac, *fv = frac + d.n, *fw = frac + 2 * d.n;
+          const long long X = 1, Y = d.sy, Z = d.sz;
+          set = fu[idx] * vu[idx] - fu[idx + X] * vu[idx + X] + fv[idx] * vv[idx] - fv[idx + Y] * vv[idx + Y];
+          if (d.is3d) set += fw[idx] * vw[idx] - fw[idx + Z] * vw[idx + Z];
+          if (obv) {
+            const float *ou = obv, *ov = obv + d.n, *ow = obv + 2 * d.n;
+            set += (1.f - fu[idx]) * ou[idx] - (1.f - fu[idx + X]) * ou[idx + X] + (1.f - fv[idx]) * ov[idx] -
+                   (1.f - fv[idx + Y]) * ov[idx + Y];
+            if (d.is3d) set += (1.f - fw[idx]) * ow[idx] - (1.f - fw[idx + Z]) * ow[idx + Z];
+          }
+        }
         if (phi && curv) {
           const long long X = 1, Y = d.sy, Z = d.sz;
           if (isE(flags, idx - X)) set += surf_tens_helper(phi, curv, idx, -X, surfTens, gfClamp);
@@ -196,9 +214,10 @@ __global__ void k_make_codes_low(Dims d, code_t* code) {
 // ApplyGhostFluidDiagonal (pressure.cpp:136-151): float diagonal
 __device__ __forceinline__ void ghost_fluid_diag_cell(const Dims& d, const int* __restrict__ flags,
                                                       const code_t* __restrict__ code, const float* __restrict__ phi,
-                                                      float gfClamp, float* A0f, int i, int j, int k) {
+                                                      float gfClamp, float* A0f, int i, int j, int k,
+                                                      const float* base = nullptr) {
   const long long idx = ix(d, i, j, k);
-  float a = (float)(code[idx] & 7);
+  float a = base ? base[idx] : (float)(code[idx] & 7);  // base: the fractions' diagonal
   if (INNER && isF(flags, idx)) {
     const long long X = 1, Y = d.sy, Z = d.sz;
     if (isE(flags, idx - X)) a -= gf_helper(phi, idx, -X, gfClamp);
@@ -213,10 +232,10 @@ __device__ __forceinline__ void ghost_fluid_diag_cell(const Dims& d, const int* 
   A0f[idx] = a;
 }
 __global__ void k_ghost_fluid_diag(Dims d, const int* __restrict__ flags, const code_t* __restrict__ code,
-                                   const float* __restrict__ phi, float gfClamp, float* A0f) {
+                                   const float* __restrict__ phi, float gfClamp, float* A0f, int inPlace) {
   CELL_IJK
   (void)idx;
-  ghost_fluid_diag_cell(d, flags, code, phi, gfClamp, A0f, i, j, k);
+  ghost_fluid_diag_cell(d, flags, code, phi, gfClamp, A0f, i, j, k, inPlace ? A0f : nullptr);
 }
 
 // CountEmptyCells (pressure.cpp:217-220)
@@ -1084,13 +1103,188 @@ __global__ void k_replace_clamped_gf(Dims d, const int* __restrict__ flags, Mac 
   replace_clamped_gf_cell(d, flags, vel, phi, gfc, i, j, k);
 }
 
+// ---------------------------------------------------- stored coefficients
+// With fractions the Poisson matrix has float off-diagonals: it is stored as
+// the reference stores it (A0, Ai, Aj, Ak), and the SpMV and MIC(0) read the
+// floats.  The stencil codes still carry the fluid bit and the links.
+
+// MakeLaplaceMatrix with fractions (conjugategrad.h:172-186)
+__global__ void k_make_frac_matrix(Dims d, const int* __restrict__ flags, const float* __restrict__ frac, float* A0,
+                                   float* Ai, float* Aj, float* Ak) {
+  CELL_IJK
+  float a0 = 0.f, ai = 0.f, aj = 0.f, ak = 0.f;
+  if (INNER && isF(flags, idx)) {
+    const float *fu = frac, *fv = frac + d.n, *fw = frac + 2 * d.n;
+    const long long X = 1, Y = d.sy, Z = d.sz;
+    a0 += fu[idx];
+    a0 += fu[idx + X];
+    a0 += fv[idx];
+    a0 += fv[idx + Y];
+    if (d.is3d) {
+      a0 += fw[idx];
+      a0 += fw[idx + Z];
+    }
+    if (isF(flags, idx + X)) ai = -fu[idx + X];
+    if (isF(flags, idx + Y)) aj = -fv[idx + Y];
+    if (d.is3d && isF(flags, idx + Z)) ak = -fw[idx + Z];
+  }
+  A0[idx] = a0;
+  Ai[idx] = ai;
+  Aj[idx] = aj;
+  Ak[idx] = ak;
+}
+
+// ApplyMatrix (conjugategrad.h:118-132) with the stored floats: the terms of
+// absent links (zero coefficients) are left out, which adds nothing; fused
+// dot(tmp, search) -> alpha as in k_pcg_spmv4
+__global__ void __launch_bounds__(256) k_pcg_spmv_stored(Dims d, const code_t* __restrict__ code,
+                                                         const float* __restrict__ A0, const float* __restrict__ Ai,
+                                                         const float* __restrict__ Aj, const float* __restrict__ Ak,
+                                                         const float* __restrict__ x, float* y, double* part,
+                                                         CgScalars* sc) {
+  if (sc->done) return;
+  FSum acc;
+  const long long Y = d.sy, Z = d.sz;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < d.n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int c = code[idx];
+    const float xv = x[idx];
+    float v = xv;
+    if (c & kCodeFluid) {
+      v = xv * A0[idx];
+      if (c & kLowX) v = v + x[idx - 1] * Ai[idx - 1];
+      if (c & kHighX) v = v + x[idx + 1] * Ai[idx];
+      if (c & kLowY) v = v + x[idx - Y] * Aj[idx - Y];
+      if (c & kHighY) v = v + x[idx + Y] * Aj[idx];
+      if (c & kLowZ) v = v + x[idx - Z] * Ak[idx - Z];
+      if (c & kHighZ) v = v + x[idx + Z] * Ak[idx];
+    }
+    y[idx] = v;
+    acc.add(v * xv);
+  }
+  const double b = block_sum(acc.value());
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
+  if (last_block(&sc->counters[1], gridDim.x)) {
+    const double s2 = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      const float dp = (float)s2;
+      sc->dp = dp;
+      sc->alpha = fabsf(dp) > 0.f ? sc->sigma / dp : 0.f;
+    }
+  }
+}
+
+// InitPreconditionModifiedIncompCholesky2 / ApplyPreconditionModifiedIncomp-
+// Cholesky2 (conjugategrad.cpp:66-97, 135-160) on the cells of one plane
+// i + j + k = L, with the stored floats.  The cells of a plane depend only
+// on the plane before (forward) or after (backward), so plane by plane is the
+// reference's lexicographic result.  MODE 0 factor, 1 forward, 2 backward.
+template <int MODE>
+__global__ void k_mic_plane(Dims d, int L, const code_t* __restrict__ code, const float* __restrict__ A0,
+                            const float* __restrict__ Ai, const float* __restrict__ Aj, const float* __restrict__ Ak,
+                            float* P, const float* __restrict__ r, float* z, const CgScalars* sc) {
+  if (MODE != 0 && sc->done) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+  const int i = L - j - k;
+  if (j >= d.ny || i < 0 || i >= d.nx) return;
+  const long long idx = ix(d, i, j, k), Y = d.sy, Z = d.sz;
+  const bool fl = (code[idx] & kCodeFluid) != 0;
+  if (MODE == 0) {
+    float pv = 0.f;
+    if (fl) {
+      float e = A0[idx];
+      float S = 0.f;
+      if (i > 0) {
+        const long long q = idx - 1;
+        const float t = Ai[q] * P[q];
+        e = e - t * t;
+        S = S + Ai[q] * (Aj[q] + Ak[q]) * (P[q] * P[q]);
+      }
+      if (j > 0) {
+        const long long q = idx - Y;
+        const float t = Aj[q] * P[q];
+        e = e - t * t;
+        S = S + Aj[q] * (Ai[q] + Ak[q]) * (P[q] * P[q]);
+      }
+      if (k > 0) {
+        const long long q = idx - Z;
+        const float t = Ak[q] * P[q];
+        e = e - t * t;
+        S = S + Ak[q] * (Ai[q] + Aj[q]) * (P[q] * P[q]);
+      }
+      // e -= tau * (...): the sum is widened to double by its "+ 0."
+      e = (float)((double)e - (double)0.97f * (double)S);
+      if (e < 0.25f * A0[idx]) e = A0[idx];
+      pv = 1.f / sqrtf(e);
+    }
+    P[idx] = pv;
+  } else if (MODE == 1) {
+    float zv = 0.f;
+    if (fl) {
+      float t = r[idx];
+      if (i > 0) t = t - z[idx - 1] * Ai[idx - 1] * P[idx - 1];
+      if (j > 0) t = t - z[idx - Y] * Aj[idx - Y] * P[idx - Y];
+      if (k > 0) t = t - z[idx - Z] * Ak[idx - Z] * P[idx - Z];
+      zv = P[idx] * t;
+    }
+    z[idx] = zv;
+  } else {
+    if (fl) {
+      const float p = P[idx];
+      float t = z[idx];
+      if (i < d.nx - 1) t = t - z[idx + 1] * Ai[idx] * p;
+      if (j < d.ny - 1) t = t - z[idx + Y] * Aj[idx] * p;
+      if (k < d.nz - 1) t = t - z[idx + Z] * Ak[idx] * p;
+      z[idx] = p * t;
+    }
+  }
+}
+
+// dot(z, r) per block after the backward sweep
+__global__ void __launch_bounds__(256) k_dot_partials(long long n, const float* __restrict__ a,
+                                                      const float* __restrict__ b, double* part, const CgScalars* sc,
+                                                      int init) {
+  if (!init && sc->done) return;
+  FSum acc;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x)
+    acc.add(a[idx] * b[idx]);
+  const double s2 = block_sum(acc.value());
+  if (threadIdx.x == 0) part[blockIdx.x] = s2;
+}
+
+void launch_make_frac_matrix(const PcgBuffers& b, const float* frac, cudaStream_t s) {
+  count_launch();
+  k_make_frac_matrix<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.flags, frac, b.A0f, b.Aif, b.Ajf, b.Akf);
+}
+
+void launch_mic_planes(const PcgBuffers& b, int mode, cudaStream_t s) {
+  const int last = b.d.nx + b.d.ny + b.d.nz - 3;
+  const dim3 g((unsigned)((b.d.ny + 127) / 128), (unsigned)b.d.nz);
+  for (int q = 0; q <= last; q++) {
+    count_launch();
+    if (mode == 0)
+      k_mic_plane<0><<<g, 128, 0, s>>>(b.d, q, b.code, b.A0f, b.Aif, b.Ajf, b.Akf, b.P, b.residual, b.tmp, b.sc);
+    else if (mode == 1)
+      k_mic_plane<1><<<g, 128, 0, s>>>(b.d, q, b.code, b.A0f, b.Aif, b.Ajf, b.Akf, b.P, b.residual, b.tmp, b.sc);
+    else
+      k_mic_plane<2><<<g, 128, 0, s>>>(b.d, last - q, b.code, b.A0f, b.Aif, b.Ajf, b.Akf, b.P, b.residual, b.tmp,
+                                       b.sc);
+  }
+  if (mode >= 2) {
+    count_launch();
+    k_dot_partials<<<b.nblocks, kThreads, 0, s>>>(b.d.n, b.tmp, b.residual, b.part, b.sc, mode == 3);
+    launch_mic_finish(b, b.nblocks, mode == 3, s);
+  }
+}
+
 // ------------------------------------------------------------- launchers
 void launch_make_rhs(const PcgBuffers& b, const float* vu, const float* vv, const float* vw, const float* perCellCorr,
-                     const float* phi, const float* curv, float surfTens, float gfClamp, bool sums, cudaStream_t s) {
+                     const float* phi, const float* curv, float surfTens, float gfClamp, bool sums, cudaStream_t s,
+                     const float* frac, const float* obvel) {
   const dim3 g = grid3(b.d, kBlk);
   count_launch();
   k_make_rhs<<<g, kBlk, 0, s>>>(b.d, b.flags, b.rhs, vu, vv, vw, perCellCorr, phi, curv, surfTens, gfClamp, b.part, b.sc,
-                                sums ? g.x * g.y * g.z : 0u);
+                                sums ? g.x * g.y * g.z : 0u, frac, obvel);
 }
 void launch_compat_shift(const PcgBuffers& b, cudaStream_t s) {
   const dim3 g = grid3(b.d, kBlk);
@@ -1107,7 +1301,8 @@ void launch_make_codes(const PcgBuffers& b, cudaStream_t s) {
 }
 void launch_ghost_fluid_diag(const PcgBuffers& b, const float* phi, float gfClamp, cudaStream_t s) {
   count_launch();
-  k_ghost_fluid_diag<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.flags, b.code, phi, gfClamp, b.A0f);
+  // with fractions the diagonal already holds their sum: adjust it in place
+  k_ghost_fluid_diag<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.flags, b.code, phi, gfClamp, b.A0f, b.Aif ? 1 : 0);
 }
 void launch_count_empty(const PcgBuffers& b, int* out, cudaStream_t s) {
   cudaMemsetAsync(out, 0, sizeof(int), s);
@@ -1134,6 +1329,11 @@ static int vec4_blocks(const PcgBuffers& b) {
 }
 void launch_pcg_spmv(const PcgBuffers& b, cudaStream_t s) {
   count_launch();
+  if (b.Aif) {
+    k_pcg_spmv_stored<<<b.nblocks, kThreads, 0, s>>>(b.d, b.code, b.A0f, b.Aif, b.Ajf, b.Akf, b.search, b.tmp, b.part,
+                                                    b.sc);
+    return;
+  }
   StreamGeom g;
   dim3 grid;
   if (g_spmvStream && stream_geom(b.d, 2 * b.nblocks, g_sms, &g, &grid)) {

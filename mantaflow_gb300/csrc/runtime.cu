@@ -106,6 +106,7 @@ struct mg_solver_s {
   float* search = nullptr;
   float* tmp = nullptr;
   float* P = nullptr;
+  float* Aoff = nullptr;  // fractions: the stored off-diagonals Ai | Aj | Ak (3n floats)
   double* part = nullptr;
   float* partf = nullptr;
   CgScalars* sc = nullptr;
@@ -219,6 +220,7 @@ static size_t held_bytes(mg_solver s) {
   const size_t n = (size_t)s->d.n;
   if (s->code) b += n * (sizeof(code_t) + 4 * sizeof(float));
   if (s->A0f) b += n * sizeof(float);
+  if (s->Aoff) b += 3 * n * sizeof(float);
   if (s->mg) b += mg_hierarchy_bytes(s->mg);
   return b;
 }
@@ -376,6 +378,8 @@ static void free_cg_state(mg_solver s) {
   cudaFree(s->micWave.order); cudaFree(s->micWave.counter); cudaFree(s->micWave.exchange);
   cudaFree(s->micFace);
   s->micFace = nullptr;
+  cudaFree(s->Aoff);
+  s->Aoff = nullptr;
   cudaGetLastError();  // a failed free must not surface as a later launch error
   s->micCol = MicColPlan{};
   s->micWave = MicWavePlan{};
@@ -1152,6 +1156,7 @@ static PcgBuffers cg_buffers(mg_solver s, mg_grid flags, float* rhs, mg_grid pre
   b.flags = flags->i();
   b.code = s->code;
   b.A0f = nullptr;
+  b.Aif = b.Ajf = b.Akf = nullptr;
   b.rhs = rhs;
   b.pressure = pressure ? pressure->f() : nullptr;
   b.residual = s->residual;
@@ -1175,7 +1180,10 @@ extern "C" int mg_compute_pressure_rhs(mg_grid rhs, mg_grid vel, mg_grid pressur
   NEED_GRID(flags, "computePressureRhs");
   (void)pressure;
   if (!check_params(p)) return fail(MG_ERR_ARG, "computePressureRhs: null params");
-  if (fractions || obvel) return fail(MG_ERR_UNSUPPORTED, "computePressureRhs: fractions/obvel are not supported");
+  if (fractions && (!valid_grid(fractions) || fractions->kind != MG_MAC))
+    return fail(MG_ERR_ARG, "computePressureRhs: fractions must be a MACGrid");
+  if (obvel && (!valid_grid(obvel) || obvel->kind != MG_MAC))
+    return fail(MG_ERR_ARG, "computePressureRhs: obvel must be a MACGrid");
   mg_solver s = flags->s;
   int st = ensure_cg_state(s);
   if (st) return st;
@@ -1183,8 +1191,10 @@ extern "C" int mg_compute_pressure_rhs(mg_grid rhs, mg_grid vel, mg_grid pressur
   Mac v = vel->mac();
   {
     ProfScope ps(s, "make_rhs");
+    // obvel enters MakeRhs only together with fractions (pressure.cpp:56-60)
     launch_make_rhs(b, v.u, v.v, v.w, perCellCorr ? perCellCorr->f() : nullptr, phi ? phi->f() : nullptr,
-                    curv ? curv->f() : nullptr, p->surfTens, p->gfClamp, p->enforceCompatibility != 0, s->stream);
+                    curv ? curv->f() : nullptr, p->surfTens, p->gfClamp, p->enforceCompatibility != 0, s->stream,
+                    fractions ? fractions->f() : nullptr, (fractions && obvel) ? obvel->f() : nullptr);
   }
   CKL();
   if (p->enforceCompatibility) {
@@ -1211,7 +1221,17 @@ static void mg_prof_hook(void* ctx, const char* family, int begin) {
 
 // doInit's preconditioner application: r -> tmp
 static int apply_precond(mg_solver s, const PcgBuffers& b, int pc, bool init) {
-  if (pc == kPcMic) {
+  if (pc == kPcMic && b.Aif) {
+    // fractions: the stored-coefficient MIC(0), plane by plane
+    {
+      ProfScope ps(s, "mic_forward");
+      launch_mic_planes(b, 1, s->stream);
+    }
+    {
+      ProfScope ps(s, "mic_backward");
+      launch_mic_planes(b, init ? 3 : 2, s->stream);
+    }
+  } else if (pc == kPcMic) {
     {
       ProfScope ps(s, "mic_forward");
       if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 1, ++s->epoch, s->waitNs, s->stream, s->stall);
@@ -1293,7 +1313,8 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   (void)perCellCorr;
   (void)curv;
   if (!check_params(p)) return fail(MG_ERR_ARG, "solvePressureSystem: null params");
-  if (fractions) return fail(MG_ERR_UNSUPPORTED, "solvePressureSystem: fractions are not supported");
+  if (fractions && (!valid_grid(fractions) || fractions->kind != MG_MAC))
+    return fail(MG_ERR_ARG, "solvePressureSystem: fractions must be a MACGrid");
   mg_solver s = flags->s;
   const Dims& d = s->d;
   int preconditioner = p->precondition ? p->preconditioner : MG_PC_NONE;
@@ -1301,6 +1322,10 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
     return fail(MG_ERR_SOLVER, "GridCg<APPLYMAT>::setICPreconditioner: Invalid method specified.");
   if (preconditioner < 0 || preconditioner > MG_PC_MG_STATIC)
     return fail(MG_ERR_ARG, "solvePressureSystem: unknown preconditioner");
+  if (fractions && (preconditioner == MG_PC_MG_STATIC || preconditioner == MG_PC_MG_DYNAMIC))
+    return fail(MG_ERR_UNSUPPORTED, "solvePressureSystem: fractions with the multigrid preconditioner are not supported");
+  if (fractions && (p->zeroPressureFixing || p->cgAccuracy < 1e-07))
+    return fail(MG_ERR_UNSUPPORTED, "solvePressureSystem: fractions with pressure fixing are not supported");
   int st = ensure_cg_state(s);
   if (st) return st;
   PcgBuffers b = cg_buffers(s, flags, rhs->f(), pressure);
@@ -1309,9 +1334,20 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
     launch_make_codes(b, s->stream);
   }
   CKL();
-  if (phi) {
+  if (fractions || phi) {
     if (!s->A0f) CK(cudaMalloc(&s->A0f, sizeof(float) * (size_t)d.n));
     b.A0f = s->A0f;
+  }
+  if (fractions) {
+    // MakeLaplaceMatrix with fractions: the float matrix as the reference stores it
+    if (!s->Aoff) CK(cudaMalloc(&s->Aoff, 3 * sizeof(float) * (size_t)d.n));
+    b.Aif = s->Aoff;
+    b.Ajf = s->Aoff + d.n;
+    b.Akf = s->Aoff + 2 * d.n;
+    launch_make_frac_matrix(b, fractions->f(), s->stream);
+    CKL();
+  }
+  if (phi) {
     launch_ghost_fluid_diag(b, phi->f(), p->gfClamp, s->stream);
     CKL();
   }
@@ -1375,7 +1411,8 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
     s->stall = s->stallNext;
     s->stallNext = false;
     CK(cudaMemsetAsync(s->mic.error, 0, sizeof(int), s->stream));
-    if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 0, ++s->epoch, s->waitNs, s->stream, s->stall);
+    if (b.Aif) launch_mic_planes(b, 0, s->stream);
+    else if (s->useMicFlow) launch_mic_flow(b, flow_plan(s), s->micFace, 0, ++s->epoch, s->waitNs, s->stream, s->stall);
     else if (s->useMicWave) launch_mic_wave(b, s->micWave, 0, ++s->epoch, s->waitNs, wave_ctas(s), s->stream);
     else if (s->useMicCol) launch_mic_col(b, s->micCol, 0, ++s->epoch, s->waitNs, g_ctx.sms, s->stream);
     else launch_mic(b, s->mic, 0, ++s->epoch, s->waitNs, s->stream);
@@ -1592,7 +1629,6 @@ extern "C" int mg_solve_pressure(mg_grid vel, mg_grid pressure, mg_grid flags, c
     mg_pressure_params_default(&def);
     p = &def;
   }
-  if (fractions || obvel) return fail(MG_ERR_UNSUPPORTED, "solvePressure: fractions/obvel are not supported");
   mg_solver s = flags->s;
   Tmp rhs(s, sizeof(float) * (size_t)s->d.n);
   if (!rhs.p) return fail(MG_ERR_NOMEM, "solvePressure: out of device memory");
@@ -1606,9 +1642,9 @@ extern "C" int mg_solve_pressure(mg_grid vel, mg_grid pressure, mg_grid flags, c
     mg_grid g;
     ~Unreg() { s->grids.erase(g); }
   } unreg{s, &rg};
-  int st = mg_compute_pressure_rhs(&rg, vel, pressure, flags, p, phi, perCellCorr, nullptr, nullptr, curv);
+  int st = mg_compute_pressure_rhs(&rg, vel, pressure, flags, p, phi, perCellCorr, fractions, obvel, curv);
   if (st) return st;
-  st = mg_solve_pressure_system(&rg, vel, pressure, flags, p, phi, perCellCorr, nullptr, curv, out);
+  st = mg_solve_pressure_system(&rg, vel, pressure, flags, p, phi, perCellCorr, fractions, curv, out);
   if (st) return st;
   st = mg_correct_velocity(vel, pressure, flags, p, phi, perCellCorr, nullptr, curv);
   if (st) return st;

@@ -873,7 +873,17 @@ static inline og_real surf_tens_helper(const og_real* phi, const og_real* curv, 
   return surfTens * (curv[idx + off] - gf_helper(phi, idx, off, gfClamp) * curv[idx]);
 }
 
-/* MakeRhs (pressure.cpp:32-84) without fractions/obvel; returns sum, cnt */
+/* Face fractions and obstacle velocity of the next MakeRhs /
+ * MakeLaplaceMatrix (MAC grids in the reference layout, or NULL): set
+ * around a call, test infrastructure only. */
+static const og_real* g_fractions = NULL;
+static const og_real* g_obvel = NULL;
+void og_set_fractions(const og_real* fractions, const og_real* obvel) {
+  g_fractions = fractions;
+  g_obvel = obvel;
+}
+
+/* MakeRhs (pressure.cpp:32-84); returns sum, cnt */
 static void make_rhs(og_dims d, const int* flags, og_real* rhs, const og_real* vel, const og_real* perCellCorr,
                      const og_real* phi, const og_real* curv, og_real surfTens, og_real gfClamp, double* sumOut, int* cntOut) {
   double sum = 0;
@@ -884,8 +894,22 @@ static void make_rhs(og_dims d, const int* flags, og_real* rhs, const og_real* v
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
         if (!isF(flags, idx)) { rhs[idx] = OG_R(0.); continue; }
-        og_real set = vel[3 * idx] - vel[3 * (idx + X)] + vel[3 * idx + 1] - vel[3 * (idx + Y) + 1];
-        if (d.is3d) set += vel[3 * idx + 2] - vel[3 * (idx + Z) + 2];
+        og_real set;
+        if (!g_fractions) {
+          set = vel[3 * idx] - vel[3 * (idx + X)] + vel[3 * idx + 1] - vel[3 * (idx + Y) + 1];
+          if (d.is3d) set += vel[3 * idx + 2] - vel[3 * (idx + Z) + 2];
+        } else {
+          const og_real* f = g_fractions;
+          set = f[3 * idx] * vel[3 * idx] - f[3 * (idx + X)] * vel[3 * (idx + X)] + f[3 * idx + 1] * vel[3 * idx + 1] -
+                f[3 * (idx + Y) + 1] * vel[3 * (idx + Y) + 1];
+          if (d.is3d) set += f[3 * idx + 2] * vel[3 * idx + 2] - f[3 * (idx + Z) + 2] * vel[3 * (idx + Z) + 2];
+          if (g_obvel) {
+            const og_real* o = g_obvel;
+            set += (1 - f[3 * idx]) * o[3 * idx] - (1 - f[3 * (idx + X)]) * o[3 * (idx + X)] +
+                   (1 - f[3 * idx + 1]) * o[3 * idx + 1] - (1 - f[3 * (idx + Y) + 1]) * o[3 * (idx + Y) + 1];
+            if (d.is3d) set += (1 - f[3 * idx + 2]) * o[3 * idx + 2] - (1 - f[3 * (idx + Z) + 2]) * o[3 * (idx + Z) + 2];
+          }
+        }
         if (phi && curv) {
           if (isE(flags, idx - X)) set += surf_tens_helper(phi, curv, idx, -X, surfTens, gfClamp);
           if (isE(flags, idx + X)) set += surf_tens_helper(phi, curv, idx, +X, surfTens, gfClamp);
@@ -930,6 +954,20 @@ void og_make_laplace_matrix(og_dims d, const int* flags, og_real* A0, og_real* A
       for (int i = 1; i < d.nx - 1; i++) {
         const ll idx = IX(d, i, j, k);
         if (!isF(flags, idx)) continue;
+        if (g_fractions) {
+          /* the fractions form (conjugategrad.h:172-186) */
+          const og_real* f = g_fractions;
+          A0[idx] += f[3 * idx];
+          A0[idx] += f[3 * (idx + X)];
+          A0[idx] += f[3 * idx + 1];
+          A0[idx] += f[3 * (idx + Y) + 1];
+          if (d.is3d) A0[idx] += f[3 * idx + 2];
+          if (d.is3d) A0[idx] += f[3 * (idx + Z) + 2];
+          if (isF(flags, idx + X)) Ai[idx] = -f[3 * (idx + X)];
+          if (isF(flags, idx + Y)) Aj[idx] = -f[3 * (idx + Y) + 1];
+          if (d.is3d && isF(flags, idx + Z)) Ak[idx] = -f[3 * (idx + Z) + 2];
+          continue;
+        }
         if (!isO(flags, idx - X)) A0[idx] += OG_R(1.);
         if (!isO(flags, idx + X)) A0[idx] += OG_R(1.);
         if (!isO(flags, idx - Y)) A0[idx] += OG_R(1.);

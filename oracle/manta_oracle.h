@@ -178,6 +178,9 @@ void og_cylinder_sdf(og_dims d, float* phi, const float* center, float radius, c
 void og_density_inflow(og_dims d, const int* flags, float* density, const float* sdf, const og_noise_params* q,
                        const float* tile, float scale, float sigma);
 
+/* fractions / obstacle velocity (MAC grids) for the next pressure calls */
+void og_set_fractions(const og_real* fractions, const og_real* obvel);
+
 #ifdef __cplusplus
 }
 #endif

@@ -125,6 +125,7 @@ def lib(dtype=np.float32):
             L.og_noise_evaluate.restype = C.c_float
             L.og_cylinder_sdf.argtypes = [Dims, f32, f32, C.c_float, f32, C.c_float]
             L.og_density_inflow.argtypes = [Dims, ip, f32, f32, C.POINTER(NoiseParams), f32, C.c_float, C.c_float]
+        L.og_set_fractions.argtypes = [C.c_void_p, C.c_void_p]
         L.og_set_num_threads.argtypes = [I]
         L.og_get_num_threads.restype = I
         _libs[t] = L
@@ -247,9 +248,18 @@ def compute_pressure_rhs(rhs, vel, flags, phi=None, perCellCorr=None, curv=None,
                                   C.byref(p))
 
 
-def solve_pressure(flags, vel, pressure, phi=None, perCellCorr=None, curv=None, mg_cache=None, retRhs=None, **kw):
+def solve_pressure(flags, vel, pressure, phi=None, perCellCorr=None, curv=None, mg_cache=None, retRhs=None,
+                   fractions=None, obvel=None, **kw):
     """solvePressure; returns (iterations, resNorm, fixPidx)."""
     t = _prec(vel.dtype)
+    lib(t).og_set_fractions(_ptr(fractions), _ptr(obvel))
+    try:
+        return _solve_pressure(t, flags, vel, pressure, phi, perCellCorr, curv, mg_cache, retRhs, **kw)
+    finally:
+        lib(t).og_set_fractions(None, None)
+
+
+def _solve_pressure(t, flags, vel, pressure, phi, perCellCorr, curv, mg_cache, retRhs, **kw):
     p = params(dtype=t, **kw)
     res = _STRUCTS[t][1]()
     cache = mg_cache if mg_cache is not None else MGCache()
