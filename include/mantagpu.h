@@ -318,15 +318,18 @@ int mg_shape_box_levelset(mg_grid phi, const float* p0, const float* p1);
  * advection, setWallBcs, addBuoyancy, solvePressure) stepped together: every
  * stage is one launch over all scenes' tiles, and the pressure solve iterates
  * until every scene has converged, each with its own CG scalars.  The
- * pressure solve is GridCg with PcNone -- the reference's 2D path
- * (conjugategrad.cpp:315-321) -- for 2D and 3D scenes alike, with the 2D
- * iteration limit (int)(cgMaxIterFac * max size) * 4. */
+ * pressure solve is the reference's GridCg with PcMIC: MIC(0) for 3D scenes
+ * with (int)(cgMaxIterFac * max size) iterations at most, no preconditioner
+ * for 2D scenes with 4 times as many (conjugategrad.cpp:315-321,
+ * pressure.cpp:407-419).  Once the CG tile height is tuned, the sweeps run
+ * as CUDA graphs of 8 sweeps between convergence polls. */
 typedef struct mg_batch_s* mg_batch;
 typedef struct {
   int sweeps;                  /* CG iterations launched (the slowest scene's count) */
   int maxIterations;           /* largest per-scene iteration count */
   long long totalIterations;   /* sum over scenes */
   int diverged;                /* scenes whose residual exceeded 1e35 */
+  long long graphLaunches;     /* CUDA graph launches of CG sweeps in this step */
 } mg_batch_stats;
 #define MG_BATCH_DENSITY 0
 #define MG_BATCH_VELOCITY 1    /* AoS Vec3, 3 floats per cell */

@@ -26,7 +26,7 @@ class PressureResult(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("sweeps", C.c_int), ("maxIterations", C.c_int), ("totalIterations", C.c_longlong),
-                ("diverged", C.c_int)]
+                ("diverged", C.c_int), ("graphLaunches", C.c_longlong)]
 
 
 class ServeStats(C.Structure):

@@ -44,7 +44,8 @@ class BatchedPlumes:
         st = _lib.BatchStats()
         check(self._L.mg_batch_step(self._h, C.byref(st)))
         self.steps += 1
-        return {"sweeps": st.sweeps, "max_iterations": st.maxIterations, "total_iterations": st.totalIterations}
+        return {"sweeps": st.sweeps, "max_iterations": st.maxIterations, "total_iterations": st.totalIterations,
+                "graph_launches": st.graphLaunches}
 
     def iterations(self, scene):
         it = C.c_int()

@@ -78,6 +78,20 @@ struct SceneRec {
   int cur = 0;   // which ping-pong buffers are current
 };
 
+// the kernel arguments a captured sweep graph depends on
+struct GraphKey {
+  const void* tiles;
+  int active, rowsK;
+  const void* scenes;
+  const void* flow;
+  const void* order;
+  int micTiles, micScenes;
+  bool operator==(const GraphKey& o) const {
+    return tiles == o.tiles && active == o.active && rowsK == o.rowsK && scenes == o.scenes && flow == o.flow &&
+           order == o.order && micTiles == o.micTiles && micScenes == o.micScenes;
+  }
+};
+
 struct Engine {
   cudaStream_t stream = nullptr;
   float dt = 1.f;
@@ -106,8 +120,12 @@ struct Engine {
   size_t orderCap = 0;
   int* dMicScene = nullptr;
   size_t micSceneCap = 0;
-  int* dMicCounter = nullptr;  // [0] tile counter, [1] wait error
-  unsigned int micEpoch = 0;
+  int* dMicCounter = nullptr;  // [0] tile counter, [1] wait error, [2] sweep epoch
+  // `lag` CG sweeps captured as a CUDA graph, and what it was captured with
+  cudaGraphExec_t sweepGraph = nullptr;
+  GraphKey graphKey{};
+  unsigned long long graphNodes = 0;
+  long long graphLaunches = 0;
   std::vector<BTile> tiles1;
   std::vector<BTile> tilesDam;  // the 32 x 8 tiles of the dam-break scenes
   BTile* dTilesDam = nullptr;
@@ -141,6 +159,7 @@ struct Engine {
     cudaFree(dOrder2);
     cudaFree(dMicScene);
     cudaFree(dMicCounter);
+    if (sweepGraph) cudaGraphExecDestroy(sweepGraph);
     if (ev[0]) cudaEventDestroy(ev[0]);
     if (ev[1]) cudaEventDestroy(ev[1]);
     if (stream) cudaStreamDestroy(stream);
@@ -153,8 +172,8 @@ int engine_init(Engine& e, float dt) {
   CKB(cudaEventCreate(&e.ev[0]));
   CKB(cudaEventCreate(&e.ev[1]));
   CKB(cudaMalloc(&e.dDone, sizeof(int)));
-  CKB(cudaMalloc(&e.dMicCounter, 2 * sizeof(int)));
-  CKB(cudaMemset(e.dMicCounter, 0, 2 * sizeof(int)));
+  CKB(cudaMalloc(&e.dMicCounter, 3 * sizeof(int)));
+  CKB(cudaMemset(e.dMicCounter, 0, 3 * sizeof(int)));
   return MG_OK;
 }
 
@@ -461,7 +480,7 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
   mic.sceneOf = e.dMicScene;
   mic.counter = e.dMicCounter;
   mic.error = e.dMicCounter + 1;
-  mic.epoch = &e.micEpoch;
+  mic.epochDev = (unsigned int*)(e.dMicCounter + 2);
   mic.spinLimit = 200000000LL;
   if (mic.nscenes > 0) {
     CKB(cudaMemsetAsync(mic.error, 0, sizeof(int), st));
@@ -485,10 +504,44 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
   };
   if (rebuild(true)) return MG_ERR_CUDA;
   const bool tuning = e.rowsK < 0;
+  const long long graphLaunches0 = e.graphLaunches;
   if (tuning) CKB(cudaEventRecord(e.ev[0], st));
   while (active > 0 && sweeps < maxIterAll) {
-    launch_b_pcg_iteration(e.dActive, active, e.dScenes, 1 << kk, e.dDone, &mic, st);
-    sweeps++;
+    // once the tile height is tuned, `lag` sweeps run as one CUDA graph,
+    // captured for the current sweep list and captured again when it changes
+    const bool useGraph = !(tuning && e.rowsK < 0) && sweeps % e.lag == 0 && sweeps + e.lag <= maxIterAll;
+    if (useGraph) {
+      const GraphKey key{e.dActive, active, kk, e.dScenes, mic.flow, mic.order, mic.ntiles, mic.nscenes};
+      if (!e.sweepGraph || !(key == e.graphKey)) {
+        if (e.sweepGraph) cudaGraphExecDestroy(e.sweepGraph);
+        e.sweepGraph = nullptr;
+        const unsigned long long before = g_launches;
+        cudaGraph_t g = nullptr;
+        CKB(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int q = 0; q < e.lag; q++) launch_b_pcg_iteration(e.dActive, active, e.dScenes, 1 << kk, e.dDone, &mic, st);
+        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+        e.graphNodes = g_launches - before;
+        g_launches = before;
+        if (ce != cudaSuccess) {
+          if (g) cudaGraphDestroy(g);
+          return set_error(MG_ERR_CUDA, std::string("capturing the batched CG sweeps failed: ") + cudaGetErrorString(ce));
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&e.sweepGraph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+          e.sweepGraph = nullptr;
+          return set_error(MG_ERR_CUDA, std::string("instantiating the batched CG sweeps failed: ") + cudaGetErrorString(ie));
+        }
+        e.graphKey = key;
+      }
+      CKB(cudaGraphLaunch(e.sweepGraph, st));
+      g_launches += e.graphNodes;
+      e.graphLaunches++;
+      sweeps += e.lag;
+    } else {
+      launch_b_pcg_iteration(e.dActive, active, e.dScenes, 1 << kk, e.dDone, &mic, st);
+      sweeps++;
+    }
     if (sweeps % e.lag == 0 || sweeps == maxIterAll) {
       bool relist = false;
       if (tuning && e.rowsK < 0 && sweeps <= 4 * e.lag) {
@@ -533,6 +586,7 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
   }
   if (stats) {
     stats->sweeps = sweeps;
+    stats->graphLaunches = e.graphLaunches - graphLaunches0;
     int mx = 0, diverged = 0;
     long long sum = 0;
     for (auto& c : e.hSc) {

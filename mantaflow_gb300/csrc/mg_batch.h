@@ -90,7 +90,7 @@ struct BatchMic {
   const int* sceneOf;  // [nscenes]: index into the BScene table
   int* counter;
   int* error;
-  unsigned int* epoch;  // host counter, advanced per sweep launch
+  unsigned int* epochDev;  // device word, advanced on the device before each sweep
   long long spinLimit;
 };
 // doInit's preconditioner application for the MIC scenes: P, z = M^-1 r,

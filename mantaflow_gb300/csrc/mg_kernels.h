@@ -170,8 +170,10 @@ struct FlowScene {
   int tx, ty, tz;
   unsigned long long* face;
 };
+// epochDev: a device word the launch advances before sweeping (so that a
+// captured CUDA graph replays with new epochs)
 void launch_mic_flow_batch(const FlowScene* scenes, const int2* order2, int ntiles, int ctas, int* counter, int* error,
-                           int mode, unsigned int epoch, long long spinLimit, cudaStream_t s);
+                           int mode, unsigned int* epochDev, long long spinLimit, cudaStream_t s);
 // resident CTAs of one MIC sweep launch on the device (after mic_flow_prepare)
 int mic_flow_device_ctas();
 // tile-dataflow MIC sweeps (micflow.cu): the tiles of a MicPlan, faces

@@ -53,6 +53,7 @@ struct FlowArgs {
   int* counter;
   int* error;
   unsigned int epoch;
+  const unsigned int* epochDev;  // batched launches: the epoch in device memory (set by k_flow_prep)
   unsigned int waitXor;  // 0; non-zero only to make every wait run out (failure-path tests)
   long long spinLimit;
 };
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(320) k_mic_flow(FlowArgs a) {
   const int ly = tid & (kT - 1), lz = (tid >> 4) & (kT - 1);
   const int hw = (tid - 256) >> 5, hl = tid & 31;  // halo warp 0/1 and its lane
   if (!kBatch && MODE != 0 && a.one.sc->done) return;
-  const unsigned ep16 = a.epoch & 0xffffu;
+  const unsigned ep16 = (kBatch ? *((volatile const unsigned int*)a.epochDev) : a.epoch) & 0xffffu;
   const unsigned wep16 = ep16 ^ a.waitXor;  // the epoch the fill words must carry
   auto gx = [&](int c, int n) { return MODE == 2 ? n - 1 - c : c; };  // global coordinate of a sweep coordinate
 
@@ -410,6 +411,7 @@ void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* 
   a.counter = m.counter;
   a.error = m.error;
   a.epoch = epoch;
+  a.epochDev = nullptr;
   a.waitXor = stall ? 0x8000u : 0u;
   a.spinLimit = spinLimit;
   cudaMemsetAsync(m.counter, 0, sizeof(int), s);
@@ -417,12 +419,22 @@ void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* 
   if (mode >= 2) launch_mic_finish(b, m.ntiles, mode == 3, s);
 }
 
+// before each batched sweep: the tile counter back to zero and the next
+// epoch (never 0 in its low 16 bits, the value of freshly cleared face
+// words).  On the device, so that a captured graph replays new epochs.
+__global__ void k_flow_prep(int* counter, unsigned int* epoch) {
+  *counter = 0;
+  unsigned int e = *epoch + 1u;
+  if ((e & 0xffffu) == 0u) e++;
+  *epoch = e;
+}
+
 // the sweep over the tiles of several scenes in one launch: order2 lists
 // (scene, tile) pairs so that each tile comes after the tiles it waits for
 // (wavefront level first); the backward modes leave each scene's per-tile
 // dot partials in its part[] for the caller's per-scene reduction
 void launch_mic_flow_batch(const FlowScene* scenes, const int2* order2, int ntiles, int ctas, int* counter, int* error,
-                           int mode, unsigned int epoch, long long spinLimit, cudaStream_t s) {
+                           int mode, unsigned int* epochDev, long long spinLimit, cudaStream_t s) {
   FlowArgs a;
   memset(&a.one, 0, sizeof(a.one));
   a.scenes = scenes;
@@ -431,10 +443,12 @@ void launch_mic_flow_batch(const FlowScene* scenes, const int2* order2, int ntil
   a.order2 = order2;
   a.counter = counter;
   a.error = error;
-  a.epoch = epoch;
+  a.epoch = 0u;
+  a.epochDev = epochDev;
   a.waitXor = 0u;
   a.spinLimit = spinLimit;
-  cudaMemsetAsync(counter, 0, sizeof(int), s);
+  count_launch();
+  k_flow_prep<<<1, 1, 0, s>>>(counter, epochDev);
   flow_launch<true>(a, mode == 3 ? 2 : mode, ctas < ntiles ? ctas : ntiles, s);
 }
 

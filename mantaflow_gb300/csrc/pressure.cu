@@ -1731,7 +1731,7 @@ __global__ void k_b_mic_finish(const BScene* __restrict__ S, const int* __restri
 void launch_b_mic_init(const BTile* t, int nt, const BScene* s, const BatchMic& m, cudaStream_t st) {
   if (m.nscenes == 0) return;
   for (int mode = 0; mode <= 2; mode++)
-    launch_mic_flow_batch(m.flow, m.order, m.ntiles, m.ctas, m.counter, m.error, mode == 2 ? 3 : mode, ++*m.epoch,
+    launch_mic_flow_batch(m.flow, m.order, m.ntiles, m.ctas, m.counter, m.error, mode == 2 ? 3 : mode, m.epochDev,
                           m.spinLimit, st);
   count_launch();
   k_b_mic_finish<true><<<m.nscenes, 256, 0, st>>>(s, m.sceneOf, m.flow, nullptr);
@@ -1757,9 +1757,9 @@ static void pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, c
   count_launch();
   k_b_pcg_axpy<R><<<nt, b, 0, st>>>(t, s, ndone);
   if (mic && mic->nscenes > 0) {
-    launch_mic_flow_batch(mic->flow, mic->order, mic->ntiles, mic->ctas, mic->counter, mic->error, 1, ++*mic->epoch,
+    launch_mic_flow_batch(mic->flow, mic->order, mic->ntiles, mic->ctas, mic->counter, mic->error, 1, mic->epochDev,
                           mic->spinLimit, st);
-    launch_mic_flow_batch(mic->flow, mic->order, mic->ntiles, mic->ctas, mic->counter, mic->error, 2, ++*mic->epoch,
+    launch_mic_flow_batch(mic->flow, mic->order, mic->ntiles, mic->ctas, mic->counter, mic->error, 2, mic->epochDev,
                           mic->spinLimit, st);
     count_launch();
     k_b_mic_finish<false><<<mic->nscenes, 256, 0, st>>>(s, mic->sceneOf, mic->flow, ndone);

@@ -28,8 +28,10 @@ STEPS = 3
 def _run_batch(idx, preconditioner=1):
     b = mb.BatchedPlumes([SIZES[i] for i in idx], [GRAV[i] for i in idx], [SEEDS[i] for i in idx],
                          preconditioner=preconditioner)
+    graphs = 0
     for _ in range(STEPS):
-        b.step()
+        graphs += b.step()["graph_launches"]
+    _run_batch.graphs = graphs
     out = [(b.download(q, mb.DENSITY), b.download(q, mb.VELOCITY), b.download(q, mb.PRESSURE)) for q in range(len(idx))]
     inflows = [[b.inflow(q, t) for t in range(STEPS)] for q in range(len(idx))]
     its = [b.iterations(q)[0] for q in range(len(idx))]
@@ -39,6 +41,7 @@ def _run_batch(idx, preconditioner=1):
 
 def test_batch_scene_alone_equals_in_mix():
     mix, _, its_mix = _run_batch(list(range(len(SIZES))))
+    assert _run_batch.graphs > 0  # the sweeps ran as CUDA graphs after the tile tuning
     for q in (0, 3):
         alone, _, its_alone = _run_batch([q])
         assert its_alone[0] == its_mix[q]
