@@ -348,6 +348,13 @@ int mg_batch_set_solver(mg_batch b, float cgAccuracy, float cgMaxIterFac);
  * scenes run GridCg without a preconditioner, as the reference does in 2D.
  * MG_PC_NONE: no scene is preconditioned. */
 int mg_batch_set_preconditioner(mg_batch b, int preconditioner);
+/* The precision form for a batch (mg_solve_pressure_refined per scene):
+ * after the FP32 solve each scene's pressure is accumulated in double, its
+ * residual max|b - A p| formed in double, and FP32 solves of A delta = r to
+ * innerAccuracy * max|r| repeat until it is below refineAccuracy (maxRefine
+ * rounds at most).  refineAccuracy 0 switches the refinement off (the
+ * default).  Each scene holds 16 more bytes per cell while it refines. */
+int mg_batch_set_refinement(mg_batch b, double refineAccuracy, double innerAccuracy, int maxRefine);
 /* one plume step of every scene; stats may be NULL */
 int mg_batch_step(mg_batch b, mg_batch_stats* stats);
 int mg_batch_scene_iterations(mg_batch b, int scene, int* iterations, float* resNorm);

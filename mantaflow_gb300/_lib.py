@@ -123,6 +123,7 @@ SIGNATURES = [
     ("mg_batch_create", _I, [_I, C.POINTER(_I), _FP, C.POINTER(C.c_ulonglong), _F, C.POINTER(_P)]),
     ("mg_batch_destroy", _I, [_P]),
     ("mg_batch_set_solver", _I, [_P, _F, _F]),
+    ("mg_batch_set_refinement", _I, [_P, C.c_double, C.c_double, _I]),
     ("mg_batch_set_preconditioner", _I, [_P, _I]),
     ("mg_batch_step", _I, [_P, C.POINTER(BatchStats)]),
     ("mg_batch_scene_iterations", _I, [_P, _I, C.POINTER(_I), _FP]),

@@ -37,6 +37,11 @@ class BatchedPlumes:
         check(self._L.mg_batch_set_preconditioner(h, int(preconditioner)))
         self.steps = 0
 
+    def set_refinement(self, refineAccuracy=1e-5, innerAccuracy=1e-2, maxRefine=10):
+        """FP64 residual refinement of every scene's pressure solve
+        (refineAccuracy 0: off)"""
+        check(self._L.mg_batch_set_refinement(self._h, float(refineAccuracy), float(innerAccuracy), int(maxRefine)))
+
     def __len__(self):
         return len(self.sizes)
 

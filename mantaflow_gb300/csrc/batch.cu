@@ -73,6 +73,7 @@ size_t scene_bytes(int nx, int ny, int nz, int kind = 0) {
 struct SceneRec {
   BScene s;
   void* mem = nullptr;
+  void* refMem = nullptr;  // p64 | b64 of the FP64 refinement, allocated when first used
   size_t bytes = 0;
   int step = 0;  // steps taken: the inflow noise index
   int cur = 0;   // which ping-pong buffers are current
@@ -111,6 +112,10 @@ struct Engine {
   // MIC(0) for 3D scenes (the reference's PcMIC; 2D scenes run without a
   // preconditioner, as GridCg does in 2D): flow table, dispatch order
   bool micFor3D = true;
+  // FP64 residual refinement of every scene's solve (off by default)
+  bool refine = false;
+  double refineAccuracy = 1e-5, innerAccuracy = 1e-2;
+  int maxRefine = 10;
   std::vector<FlowScene> hFlow;
   std::vector<int2> hOrder2;
   std::vector<int> hMicScene;
@@ -146,6 +151,7 @@ struct Engine {
     if (stream) cudaStreamSynchronize(stream);
     for (auto* m : members) {
       cudaFree(m->mem);
+      cudaFree(m->refMem);
       delete m;
     }
     for (auto& kv : pool) cudaFree(kv.second);
@@ -259,6 +265,8 @@ int scene_add(Engine& e, int nx, int ny, int nz, const float* gravity, unsigned 
   s.kind = kind;
   s.A0f = nullptr;
   s.itmp = nullptr;
+  s.p64 = nullptr;
+  s.b64 = nullptr;
   if (kind == 1) {
     s.A0f = (float*)take(n * sizeof(float));
     s.itmp = (int*)take(n * sizeof(int));
@@ -319,6 +327,10 @@ int scene_add(Engine& e, int nx, int ny, int nz, const float* gravity, unsigned 
 
 void scene_remove(Engine& e, SceneRec* r) {
   e.members.erase(std::find(e.members.begin(), e.members.end(), r));
+  if (r->refMem) {
+    cudaStreamSynchronize(e.stream);
+    cudaFree(r->refMem);
+  }
   e.pool.emplace(r->bytes, r->mem);
   e.liveBytes -= r->bytes;
   delete r;
@@ -441,57 +453,62 @@ int engine_tables(Engine& e) {
   return MG_OK;
 }
 
-// one plume step of every member
-int engine_step(Engine& e, mg_batch_stats* stats) {
-  if (e.members.empty()) return MG_OK;
-  if (engine_tables(e)) return MG_ERR_CUDA;
+int engine_tables(Engine& e);
+
+// the double pressure and right-hand side of every member (FP64 refinement),
+// allocated on first use; the scene table is uploaded again
+int engine_refine_buffers(Engine& e) {
+  bool changed = false;
+  for (auto* m : e.members) {
+    if (m->refMem) continue;
+    const size_t n = (size_t)m->s.d.n;
+    if (cudaMalloc(&m->refMem, 2 * n * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      m->refMem = nullptr;
+      return set_error(MG_ERR_NOMEM, "batched refinement: out of device memory");
+    }
+    m->s.p64 = (double*)m->refMem;
+    m->s.b64 = (double*)m->refMem + n;
+    changed = true;
+  }
+  return changed ? engine_tables(e) : MG_OK;
+}
+
+// One batched GridCg solve (pressure.cpp:407-419) of every scene not
+// skipped, each to its own accuracy: PcMIC in 3D with (int)(cgMaxIterFac *
+// max size) iterations at most; in 2D GridCg drops MIC (conjugategrad.cpp:
+// 315-321) and allows 4 times as many.  The right-hand side is in rhs.
+int engine_cg(Engine& e, const BatchMic& mic, const std::vector<float>& acc, const std::vector<char>& skip,
+              int* sweepsOut) {
   const int nm = (int)e.members.size();
   const int nt = (int)e.tiles1.size();
   cudaStream_t st = e.stream;
-  const int cur = 0, nxt = 1;  // the table presents every scene's current buffers as 0
-  const int ntDam = (int)e.tilesDam.size();
-  launch_b_inflow(e.dTiles, nt, e.dScenes, cur, st);
-  launch_b_advect_velocity(e.dTiles, nt, e.dScenes, cur, st);
-  launch_b_dam_advect(e.dTilesDam, ntDam, e.dScenes, cur, st);
-  launch_b_forces(e.dTiles, nt, e.dScenes, nxt, st);
-  // GridCg setup of every scene (pressure.cpp:407-419): PcMIC in 3D with
-  // (int)(cgMaxIterFac * max size) iterations at most; in 2D GridCg drops
-  // MIC (conjugategrad.cpp:315-321) and allows 4 times as many
-  int maxIterAll = 0;
+  int maxIterAll = 0, nskip = 0;
   for (int q = 0; q < nm; q++) {
-    const BScene& b = e.members[q]->s;
-    const Dims& d = b.d;
+    const Dims& d = e.members[q]->s.d;
     CgScalars c{};
-    c.accuracy = e.cgAccuracy;
+    c.accuracy = acc[q];
     c.maxIter = (int)(e.cgMaxIterFac * (float)std::max(d.nx, std::max(d.ny, d.nz))) * (d.is3d ? 1 : 4);
     c.resNorm = 1e20f;
+    c.refNorm = e.hSc[q].refNorm;
+    if (skip[q]) {
+      c.done = 1;
+      nskip++;
+    }
     e.hSc[q] = c;
-    maxIterAll = std::max(maxIterAll, c.maxIter);
+    if (!skip[q]) maxIterAll = std::max(maxIterAll, c.maxIter);
   }
   CKB(cudaMemcpyAsync(e.dSc, e.hSc.data(), sizeof(CgScalars) * nm, cudaMemcpyHostToDevice, st));
-  CKB(cudaMemsetAsync(e.dDone, 0, sizeof(int), st));
-  launch_b_pressure_setup(e.dTiles, nt, e.dScenes, nxt, st, e.dTilesDam, ntDam);
-  BatchMic mic;
-  mic.flow = e.dFlow;
-  mic.order = e.dOrder2;
-  mic.ntiles = (int)e.hOrder2.size();
-  mic.nscenes = (int)e.hFlow.size();
-  mic.ctas = mic_flow_device_ctas();
-  mic.sceneOf = e.dMicScene;
-  mic.counter = e.dMicCounter;
-  mic.error = e.dMicCounter + 1;
-  mic.epochDev = (unsigned int*)(e.dMicCounter + 2);
-  mic.spinLimit = 200000000LL;
-  if (mic.nscenes > 0) {
-    CKB(cudaMemsetAsync(mic.error, 0, sizeof(int), st));
-    launch_b_mic_init(e.dTiles, nt, e.dScenes, mic, st);
-  }
+  CKB(cudaMemcpyAsync(e.dDone, &nskip, sizeof(int), cudaMemcpyHostToDevice, st));
+  launch_b_pcg_init(e.dTiles, nt, e.dScenes, st);
+  if (mic.nscenes > 0) launch_b_mic_init(e.dTiles, nt, e.dScenes, mic, st);
   // CG sweeps over the tiles of the scenes still iterating.  Autotuner: the
   // first solve runs its first 4 x lag sweeps with tiles 8, 16, 32 and 64
   // rows tall (lag sweeps each, timed with events) and keeps the fastest;
   // results do not depend on the choice.
   int kk = e.rowsK >= 0 ? e.rowsK : 0;
   int active = 0, doneSeen = -1, sweeps = 0;
+  (void)nt;
   std::vector<BTile> list;
   auto rebuild = [&](bool all) -> int {
     list.clear();
@@ -502,9 +519,8 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
     if (active) CKB(cudaMemcpyAsync(e.dActive, list.data(), sizeof(BTile) * active, cudaMemcpyHostToDevice, st));
     return MG_OK;
   };
-  if (rebuild(true)) return MG_ERR_CUDA;
+  if (rebuild(false)) return MG_ERR_CUDA;
   const bool tuning = e.rowsK < 0;
-  const long long graphLaunches0 = e.graphLaunches;
   if (tuning) CKB(cudaEventRecord(e.ev[0], st));
   while (active > 0 && sweeps < maxIterAll) {
     // once the tile height is tuned, `lag` sweeps run as one CUDA graph,
@@ -574,6 +590,70 @@ int engine_step(Engine& e, mg_batch_stats* stats) {
       }
       if (tuning && e.rowsK < 0) CKB(cudaEventRecord(e.ev[0], st));
     }
+  }
+  *sweepsOut = sweeps;
+  CKB(cudaStreamSynchronize(st));
+  return MG_OK;
+}
+
+// one plume step of every member
+int engine_step(Engine& e, mg_batch_stats* stats) {
+  if (e.members.empty()) return MG_OK;
+  if (engine_tables(e)) return MG_ERR_CUDA;
+  const int nm = (int)e.members.size();
+  const int nt = (int)e.tiles1.size();
+  cudaStream_t st = e.stream;
+  const int cur = 0, nxt = 1;  // the table presents every scene's current buffers as 0
+  const int ntDam = (int)e.tilesDam.size();
+  launch_b_inflow(e.dTiles, nt, e.dScenes, cur, st);
+  launch_b_advect_velocity(e.dTiles, nt, e.dScenes, cur, st);
+  launch_b_dam_advect(e.dTilesDam, ntDam, e.dScenes, cur, st);
+  launch_b_forces(e.dTiles, nt, e.dScenes, nxt, st);
+  launch_b_pressure_setup(e.dTiles, nt, e.dScenes, nxt, st, e.dTilesDam, ntDam);
+  BatchMic mic;
+  mic.flow = e.dFlow;
+  mic.order = e.dOrder2;
+  mic.ntiles = (int)e.hOrder2.size();
+  mic.nscenes = (int)e.hFlow.size();
+  mic.ctas = mic_flow_device_ctas();
+  mic.sceneOf = e.dMicScene;
+  mic.counter = e.dMicCounter;
+  mic.error = e.dMicCounter + 1;
+  mic.epochDev = (unsigned int*)(e.dMicCounter + 2);
+  mic.spinLimit = 200000000LL;
+  if (mic.nscenes > 0) CKB(cudaMemsetAsync(mic.error, 0, sizeof(int), st));
+  std::vector<char> skip(nm, 0);
+  std::vector<float> acc(nm, e.cgAccuracy);
+  const long long graphLaunches0 = e.graphLaunches;
+  int sweeps = 0, st1 = engine_cg(e, mic, acc, skip, &sweeps);
+  if (st1) return st1;
+  int refinements = 0;
+  if (e.refine) {
+    // FP64 residual refinement (the precision form, refine.cu) per scene:
+    // p64 accumulates the FP32 solutions, r = b - A p64 in double; scenes
+    // whose max|r| is below refineAccuracy stop, the others solve A delta = r
+    // in FP32 to innerAccuracy * max|r|
+    if (engine_refine_buffers(e)) return MG_ERR_NOMEM;
+    launch_b_ref_first(e.dTiles, nt, e.dScenes, st);
+    for (refinements = 1; refinements <= e.maxRefine; refinements++) {
+      launch_b_ref_residual(e.dTiles, nt, e.dScenes, st);
+      CKB(cudaMemcpyAsync(e.hSc.data(), e.dSc, sizeof(CgScalars) * nm, cudaMemcpyDeviceToHost, st));
+      CKB(cudaStreamSynchronize(st));
+      int open = 0;
+      for (int q = 0; q < nm; q++) {
+        skip[q] = !(e.hSc[q].refNorm >= e.refineAccuracy);
+        acc[q] = (float)(e.innerAccuracy * e.hSc[q].refNorm);
+        if (!skip[q] && !(acc[q] > 1e-30f)) skip[q] = 1;
+        open += !skip[q];
+      }
+      if (!open || refinements == e.maxRefine) break;
+      int sw = 0;
+      st1 = engine_cg(e, mic, acc, skip, &sw);
+      if (st1) return st1;
+      sweeps += sw;
+      launch_b_ref_add(e.dTiles, nt, e.dScenes, st);
+    }
+    launch_b_ref_finish(e.dTiles, nt, e.dScenes, st);
   }
   launch_b_correct(e.dTiles, nt, e.dScenes, nxt, st);
   launch_b_dam_correct(e.dTilesDam, ntDam, e.dScenes, nxt, st);
@@ -676,6 +756,16 @@ extern "C" int mg_batch_set_solver(mg_batch b, float cgAccuracy, float cgMaxIter
   if (!b || !(cgAccuracy > 0.f) || !(cgMaxIterFac > 0.f)) return set_error(MG_ERR_ARG, "mg_batch_set_solver: invalid argument");
   b->e.cgAccuracy = cgAccuracy;
   b->e.cgMaxIterFac = cgMaxIterFac;
+  return MG_OK;
+}
+
+extern "C" int mg_batch_set_refinement(mg_batch b, double refineAccuracy, double innerAccuracy, int maxRefine) {
+  if (!b || refineAccuracy < 0. || !(innerAccuracy > 0.) || maxRefine < 1)
+    return set_error(MG_ERR_ARG, "mg_batch_set_refinement: invalid argument");
+  b->e.refine = refineAccuracy > 0.;
+  b->e.refineAccuracy = refineAccuracy;
+  b->e.innerAccuracy = innerAccuracy;
+  b->e.maxRefine = maxRefine;
   return MG_OK;
 }
 

@@ -61,6 +61,10 @@ struct BScene {
   int kind;
   float* A0f;
   int* itmp;
+  // FP64 refinement (when the batch refines): the pressure accumulated in
+  // double and the double right-hand side
+  double* p64;
+  double* b64;
   float dt;
   float bx, by, bz;  // plume: buoyancy factors -gravity*dt/dx (KnAddBuoyancy), 0.5 applied in-kernel;
                      // dam break: the gravity force gravity*dt/dx (KnApplyForce)
@@ -77,10 +81,19 @@ void launch_b_inflow(const BTile* t, int nt, const BScene* s, int cur, cudaStrea
 void launch_b_advect_density(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_advect_velocity(const BTile* t, int nt, const BScene* s, int cur, cudaStream_t st);
 void launch_b_forces(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st);
-// MakeRhs + codes, the dam scenes' ghost-fluid diagonal (their own tile
-// list), GridCg::doInit
+// MakeRhs + codes and the dam scenes' ghost-fluid diagonal (their own tile
+// list)
 void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, cudaStream_t st, const BTile* tDam,
                              int ntDam);
+// GridCg::doInit without a preconditioner: x = 0, r = rhs, z = s = r, sigma
+// (MIC scenes then apply theirs: launch_b_mic_init)
+void launch_b_pcg_init(const BTile* t, int nt, const BScene* s, cudaStream_t st);
+// FP64 refinement: b64 = rhs, p64 = pres; r = b64 - A p64 in double into rhs
+// (as float) with max|r| into the scene's refNorm; p64 += pres; pres = p64
+void launch_b_ref_first(const BTile* t, int nt, const BScene* s, cudaStream_t st);
+void launch_b_ref_residual(const BTile* t, int nt, const BScene* s, cudaStream_t st);
+void launch_b_ref_add(const BTile* t, int nt, const BScene* s, cudaStream_t st);
+void launch_b_ref_finish(const BTile* t, int nt, const BScene* s, cudaStream_t st);
 // the MIC(0) sweeps of a batch: the FlowScene table of its MIC scenes, the
 // (scene, tile) dispatch order, and the BScene index of each MIC scene
 struct BatchMic {

@@ -66,6 +66,7 @@ struct CgScalars {
   int iterations, done, status, maxIter;
   int useL2, pad;
   double sum;   // MakeRhs sum (enforceCompatibility)
+  double refNorm;  // batched FP64 refinement: max|b - A p64| of the scene
   int cnt, pad2;
   unsigned int counters[8];  // last-block tickets
 };

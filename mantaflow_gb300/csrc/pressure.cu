@@ -1701,6 +1701,61 @@ __global__ void __launch_bounds__(256) k_b_dam_replace_clamped(const BTile* __re
   replace_clamped_gf_cell(d, sc.flags, bmac(sc.vel[nxt], d.n), sc.dens[nxt], 1e-4f, i, j, k);
 }
 
+// ---- batched FP64 refinement (the precision form of refine.cu per scene)
+__global__ void __launch_bounds__(256) k_b_ref_first(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
+  BATCH_TILE
+  if (!in) return;
+  sc.b64[idx] = (double)sc.rhs[idx];
+  sc.p64[idx] = (double)sc.pres[idx];
+}
+// r = b - A p64 in double (identity rows off the fluid), rhs = (float) r,
+// max|r| per 32 x 8 tile, reduced by the scene's last tile into refNorm
+__global__ void __launch_bounds__(256) k_b_ref_residual(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
+  BATCH_TILE
+  double m = 0.;
+  if (in) {
+    const int c = sc.code[idx];
+    const double* p = sc.p64;
+    const double pc = p[idx];
+    double ap = pc;
+    if (c & kCodeFluid) {
+      ap = (double)(sc.A0f ? sc.A0f[idx] : (float)(c & 7)) * pc;
+      if (c & kLowX) ap -= p[idx - 1];
+      if (c & kHighX) ap -= p[idx + 1];
+      if (c & kLowY) ap -= p[idx - d.sy];
+      if (c & kHighY) ap -= p[idx + d.sy];
+      if (c & kLowZ) ap -= p[idx - d.sz];
+      if (c & kHighZ) ap -= p[idx + d.sz];
+    }
+    const double r = sc.b64[idx] - ap;
+    sc.rhs[idx] = (float)r;
+    m = fabs(r);
+  }
+  __shared__ double sh[8];
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((lin_tid() & 31) == 0) sh[lin_tid() >> 5] = m;
+  __syncthreads();
+  if (lin_tid() == 0) {
+    double t = 0.;
+    for (int w = 0; w < 8; w++) t = fmax(t, sh[w]);
+    sc.part[tl.local] = t;
+  }
+  if (last_block(&sc.sc->counters[4], tl.count)) {
+    const double mx = max_partials(sc.part, sc.ntiles);
+    if (lin_tid() == 0) sc.sc->refNorm = mx;
+  }
+}
+__global__ void __launch_bounds__(256) k_b_ref_add(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
+  BATCH_TILE
+  if (!in) return;
+  sc.p64[idx] += (double)sc.pres[idx];
+}
+__global__ void __launch_bounds__(256) k_b_ref_finish(const BTile* __restrict__ tiles, const BScene* __restrict__ S) {
+  BATCH_TILE
+  if (!in) return;
+  sc.pres[idx] = (float)sc.p64[idx];
+}
+
 #undef BATCH_TILE
 
 // sigma (doInit) or beta (iterate) of each MIC scene from the per-tile
@@ -1746,8 +1801,26 @@ void launch_b_pressure_setup(const BTile* t, int nt, const BScene* s, int nxt, c
   count_launch();
   k_b_rhs_codes<<<nt, b, 0, st>>>(t, s, nxt);
   launch_b_dam_gf_diag(tDam, ntDam, s, nxt, st);
+}
+void launch_b_ref_first(const BTile* t, int nt, const BScene* s, cudaStream_t st) {
   count_launch();
-  k_b_pcg_init<<<nt, b, 0, st>>>(t, s);
+  k_b_ref_first<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s);
+}
+void launch_b_ref_residual(const BTile* t, int nt, const BScene* s, cudaStream_t st) {
+  count_launch();
+  k_b_ref_residual<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s);
+}
+void launch_b_ref_add(const BTile* t, int nt, const BScene* s, cudaStream_t st) {
+  count_launch();
+  k_b_ref_add<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s);
+}
+void launch_b_ref_finish(const BTile* t, int nt, const BScene* s, cudaStream_t st) {
+  count_launch();
+  k_b_ref_finish<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s);
+}
+void launch_b_pcg_init(const BTile* t, int nt, const BScene* s, cudaStream_t st) {
+  count_launch();
+  k_b_pcg_init<<<nt, dim3(kBTX, kBTY, 1), 0, st>>>(t, s);
 }
 template <int R>
 static void pcg_iteration(const BTile* t, int nt, const BScene* s, int* ndone, const BatchMic* mic, cudaStream_t st) {

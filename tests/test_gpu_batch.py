@@ -83,3 +83,37 @@ def test_batch_against_single_scene_path(preconditioner):
         else:
             assert np.max(np.abs(d - dens.numpy())) <= 1e-3, q
             assert np.max(np.abs(v - vel.numpy())) <= 5e-3, q
+
+
+def test_batch_fp64_refined_against_single_scene_refined():
+    """The batched precision form: every scene's FP32 solve refined in FP64
+    to max|b - A p| < 1e-5, against the single-scene refined solve
+    (solvePressureRefined) fed the same inflow: 1e-5 absolute in pressure and
+    velocity (both are within 1e-5 of the exact solution's residual)."""
+    sizes, grav, seeds = [(48, 40, 1), (24, 20, 22)], [(0.0, -4e-3, 0.0), (0.0, -6e-3, 0.0)], [21, 22]
+    b = mb.BatchedPlumes(sizes, grav, seeds)
+    b.set_refinement(1e-5)
+    steps = 3
+    for _ in range(steps):
+        b.step()
+    for q, (nx, ny, nz) in enumerate(sizes):
+        s = m.Solver(name="ref", gridSize=m.vec3(nx, ny, nz), dim=3 if nz > 1 else 2)
+        s.timestep = 1.0
+        flags = s.create(m.FlagGrid)
+        flags.initDomain(boundaryWidth=0)
+        flags.fillGrid()
+        m.setOpenBound(flags, 0, "Y", m.FlagOutflow | m.FlagEmpty)
+        vel, dens, pres, src = s.create(m.MACGrid), s.create(m.RealGrid), s.create(m.RealGrid), s.create(m.RealGrid)
+        for t in range(steps):
+            m.copyArrayToGridReal(b.inflow(q, t), src)
+            dens.join(src)
+            m.advectSemiLagrange(flags=flags, vel=vel, grid=dens, order=2, clampMode=2)
+            m.advectSemiLagrange(flags=flags, vel=vel, grid=vel, order=2, clampMode=2)
+            m.setWallBcs(flags=flags, vel=vel)
+            m.addBuoyancy(density=dens, vel=vel, gravity=m.vec3(*grav[q]), flags=flags)
+            m.solvePressureRefined(flags=flags, vel=vel, pressure=pres, cgAccuracy=1e-3, refineAccuracy=1e-5,
+                                   preconditioner=m.PcMIC)
+        assert np.max(np.abs(b.download(q, mb.PRESSURE) - pres.numpy())) <= 1e-5, q
+        assert np.max(np.abs(b.download(q, mb.VELOCITY) - vel.numpy())) <= 1e-5, q
+        assert np.max(np.abs(b.download(q, mb.DENSITY) - dens.numpy())) <= 1e-5, q
+    b.close()
