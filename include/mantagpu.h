@@ -214,6 +214,54 @@ int mg_density_inflow(mg_grid flags, mg_grid density, mg_noise noise, mg_grid sd
 /* Cylinder::computeLevelset (CylinderSDF, shapes.cpp:367-388) */
 int mg_shape_cylinder_levelset(mg_grid phi, const float* center, float radius, const float* z);
 
+/* ---- particles and the FLIP transfers (source/particle.h,
+ * source/plugin/flip.cpp) ----------------------------------------------------- */
+/* BasicParticleSystem (particle.h:193-230) of one solver, holding up to
+ * `capacity` particles in device memory; ParticleDataImpl<Real|Vec3|int>
+ * (particle.h:306) per-particle data of one particle system.  Destroying a
+ * particle system destroys its data; destroying the solver destroys both. */
+typedef struct mg_particles_s* mg_particles;
+typedef struct mg_pdata_s* mg_pdata;
+/* ParticleBase::PDELETE (particle.h:41): a deleted particle, skipped */
+#define MG_PARTICLE_DELETED 1024
+int mg_particles_create(mg_solver s, long long capacity, mg_particles* out);
+int mg_particles_destroy(mg_particles p);
+/* `count` records in the layout of BasicParticleData (particle.h:182-191):
+ * float pos[3], int flag -- 16 bytes each.  Upload sets the particle count
+ * (at most the capacity); download takes exactly the particle count. */
+int mg_particles_upload(mg_particles p, const void* host, long long count);
+int mg_particles_download(mg_particles p, void* host, long long count);
+int mg_particles_size(mg_particles p, long long* count);
+/* kind MG_REAL (float), MG_VEC3 (3 floats per particle) or MG_INT (int32);
+ * transfers take exactly the particle count; created zeroed */
+int mg_pdata_create(mg_particles p, int kind, mg_pdata* out);
+int mg_pdata_destroy(mg_pdata d);
+int mg_pdata_upload(mg_pdata d, const void* host, long long count);
+int mg_pdata_download(mg_pdata d, void* host, long long count);
+/* mapPartsToMAC (flip.cpp:573-595): vel = the particle velocities splatted
+ * with their trilinear MAC weights, divided by the summed weights; velOld =
+ * vel; weight (a Vec3 grid, may be NULL) receives the summed weights.
+ * ptype (an MG_INT particle data, may be NULL) and exclude skip particles
+ * whose type has an excluded bit.  Results equal the reference's
+ * particle-order sums bit for bit.  In 2D the particles of the slab
+ * 0 <= z < 1 match the reference; others are taken to lie in the slab (the
+ * reference indexes outside the grid for them), here and in the transfers
+ * below. */
+int mg_map_parts_to_mac(mg_grid flags, mg_grid vel, mg_grid velOld, mg_particles parts, mg_pdata partVel,
+                        mg_grid weight, mg_pdata ptype, int exclude);
+/* mapMACToParts (flip.cpp:651-655): partVel = vel interpolated (PIC) */
+int mg_map_mac_to_parts(mg_grid flags, mg_grid vel, mg_particles parts, mg_pdata partVel, mg_pdata ptype,
+                        int exclude);
+/* flipVelocityUpdate (flip.cpp:669-673): partVel = flipRatio * (partVel +
+ * vel(p) - velOld(p)) + (1 - flipRatio) * vel(p) */
+int mg_flip_velocity_update(mg_grid flags, mg_grid vel, mg_grid velOld, mg_particles parts, mg_pdata partVel,
+                            float flipRatio, mg_pdata ptype, int exclude);
+/* mapPartsToGrid / mapPartsToGridVec3 (flip.cpp:599-622): target is a Real
+ * grid with MG_REAL data or a Vec3 grid with MG_VEC3 data */
+int mg_map_parts_to_grid(mg_grid flags, mg_grid target, mg_particles parts, mg_pdata source);
+/* mapGridToParts / mapGridToPartsVec3 (flip.cpp:625-638) */
+int mg_map_grid_to_parts(mg_grid source, mg_particles parts, mg_pdata target);
+
 /* ---- plugins: pressure (plugin/pressure.cpp) ----------------------------- */
 typedef struct {
   float cgAccuracy;          /* 1e-3 */

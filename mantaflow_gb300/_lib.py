@@ -114,6 +114,20 @@ SIGNATURES = [
     ("mg_noise_evaluate_grid", _I, [_P, _P, _F]),
     ("mg_density_inflow", _I, [_P, _P, _P, _P, _F, _F, _F]),
     ("mg_shape_cylinder_levelset", _I, [_P, _FP, _F, _FP]),
+    ("mg_particles_create", _I, [_P, C.c_longlong, C.POINTER(_P)]),
+    ("mg_particles_destroy", _I, [_P]),
+    ("mg_particles_upload", _I, [_P, _P, C.c_longlong]),
+    ("mg_particles_download", _I, [_P, _P, C.c_longlong]),
+    ("mg_particles_size", _I, [_P, C.POINTER(C.c_longlong)]),
+    ("mg_pdata_create", _I, [_P, _I, C.POINTER(_P)]),
+    ("mg_pdata_destroy", _I, [_P]),
+    ("mg_pdata_upload", _I, [_P, _P, C.c_longlong]),
+    ("mg_pdata_download", _I, [_P, _P, C.c_longlong]),
+    ("mg_map_parts_to_mac", _I, [_P, _P, _P, _P, _P, _P, _P, _I]),
+    ("mg_map_mac_to_parts", _I, [_P, _P, _P, _P, _P, _I]),
+    ("mg_flip_velocity_update", _I, [_P, _P, _P, _P, _P, _F, _P, _I]),
+    ("mg_map_parts_to_grid", _I, [_P, _P, _P, _P]),
+    ("mg_map_grid_to_parts", _I, [_P, _P, _P]),
     ("mg_pressure_params_default", None, [C.POINTER(PressureParams)]),
     ("mg_solve_pressure", _I, [_P, _P, _P, C.POINTER(PressureParams), _P, _P, _P, _P, _P, _P,
                                C.POINTER(PressureResult)]),

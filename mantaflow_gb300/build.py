@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmantagpu.so")
-SOURCES = ["runtime.cu", "advect.cu", "forces.cu", "pressure.cu", "mic.cu", "micwave.cu", "micflow.cu", "multigrid.cu", "refine.cu", "batch.cu", "gridio.cu", "noise.cu"]
+SOURCES = ["runtime.cu", "advect.cu", "forces.cu", "pressure.cu", "mic.cu", "micwave.cu", "micflow.cu", "multigrid.cu", "refine.cu", "batch.cu", "gridio.cu", "noise.cu", "particles.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr"]
 

@@ -11,6 +11,7 @@
 #pragma once
 #include <string>
 
+#include "../../include/mantagpu.h"
 #include "mg_kernels.h"
 
 namespace mgpu {
@@ -24,6 +25,11 @@ bool library_ready();
 void cylinder_axis(const float* z, float* zn, float* mZ);
 // noise.cu: frees the device noise tile (mg_shutdown)
 void noise_release();
+// particles.cu: frees the particle systems of a solver (all of them for
+// nullptr) and their particle data, whose handles become invalid
+void particles_release(mg_solver s);
+// runtime.cu: a solver's dimensions and stream (MG_ERR_ARG for a bad handle)
+int solver_info(mg_solver s, Dims* d, cudaStream_t* st);
 
 struct BTile {
   int scene;

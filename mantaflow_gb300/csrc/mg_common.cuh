@@ -135,10 +135,15 @@ __device__ __forceinline__ float interp(const Dims& d, const float* __restrict__
           (__ldg(p + X + Z) * w.t0 + __ldg(p + X + Y + Z) * w.t1) * w.s1) * w.f1;
 }
 
-// interpolMAC (util/interpol.h:127-157): per component, one axis shifted
+// interpolMAC (util/interpol.h:127-157): per component, one axis shifted.
+// kSlab: in 2D, read the z = 0 slab whatever z is (for arbitrary particle
+// positions; the reference's 2D particles stay in 0 <= z < 1, where this
+// changes nothing)
+template <bool kSlab = false>
 __device__ __forceinline__ V3 interp_mac(const Dims& d, CMac m, float x, float y, float z) {
-  const Wts w = build_index<false>(d, x, y, z);
-  const Wts s = build_index<true>(d, x, y, z);
+  Wts w = build_index<false>(d, x, y, z);
+  Wts s = build_index<true>(d, x, y, z);
+  if (kSlab && !d.is3d) w.zi = s.zi = 0;
   const int X = 1, Y = (int)d.sy, Z = (int)d.sz;
   V3 r;
   {

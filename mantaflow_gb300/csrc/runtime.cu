@@ -403,6 +403,7 @@ extern "C" int mg_solver_destroy(mg_solver s) {
   if (!valid_solver(s)) return fail(MG_ERR_ARG, "mg_solver_destroy: invalid solver");
   sync_copies(s);
   cudaStreamSynchronize(s->stream);
+  particles_release(s);
   for (auto g : s->grids) {
     free_stage(g);
     cudaFree(g->data);
@@ -486,6 +487,13 @@ extern "C" int mg_solver_size(mg_solver s, int* nx, int* ny, int* nz) {
   if (nx) *nx = s->d.nx;
   if (ny) *ny = s->d.ny;
   if (nz) *nz = s->d.nz;
+  return MG_OK;
+}
+
+int mgpu::solver_info(mg_solver s, Dims* d, cudaStream_t* st) {
+  if (!valid_solver(s)) return fail(MG_ERR_ARG, "invalid solver");
+  *d = s->d;
+  *st = s->stream;
   return MG_OK;
 }
 

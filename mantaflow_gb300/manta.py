@@ -170,6 +170,10 @@ class Solver:
             try:
                 for g in self._grids:
                     g._h = None
+                for ps in getattr(self, "_particles", []):
+                    ps._h = None
+                    for d in ps._data:
+                        d._h = None
                 _lib._lib.mg_solver_destroy(h)
             except Exception:
                 pass
@@ -612,5 +616,258 @@ def setDebugLevel(level=1):
     """fluidsolver.cpp:213-215 (messages of the GPU path are not printed)"""
     return None
 
+
+
+# ----------------------------------------------------------------- particles
+ParticleDelete = 1 << 10  # ParticleBase::PDELETE (source/particle.h:41)
+
+
+class BasicParticleSystem:
+    """BasicParticleSystem (source/particle.h:193-230): particle positions and
+    status flags in device memory.  addParticle collects particles on the
+    host; they reach the device (and every particle data of the system grows
+    by zeros, as ParticleDataImpl does) before the next transfer."""
+
+    def __init__(self, parent, show=True, name=None):
+        self._parent = parent
+        self.name = name
+        self._h = None
+        self._cap = 0
+        self._n = 0
+        self._pending = []
+        self._data = []
+        parent._particles = getattr(parent, "_particles", [])
+        parent._particles.append(self)
+
+    def create(self, cls, **kwargs):
+        """ParticleBase::create: particle data of this system"""
+        d = cls(self, **kwargs)
+        return d
+
+    def addParticle(self, pos):
+        self._pending.append([float(x) for x in _vec(pos)])
+
+    def pySize(self):
+        return self._n + len(self._pending)
+
+    def size(self):
+        return self.pySize()
+
+    def _records(self):
+        rec = np.zeros(self._n, dtype=[("pos", np.float32, 3), ("flag", np.int32)])
+        if self._n:
+            check(_lib.load().mg_particles_download(self._h, rec.ctypes.data_as(C.c_void_p), self._n))
+        return rec
+
+    def _set_records(self, rec):
+        """replace every particle (positions and flags); data keeps its values
+        for the first min(old, new) particles and is zero beyond"""
+        L = _lib.load()
+        n = len(rec)
+        saved = [(d, d._download()) for d in self._data]
+        if self._h is None or n > self._cap:
+            cap = max(1024, n, 2 * self._cap)
+            if self._h is not None:
+                for d in self._data:
+                    d._h = None  # destroyed with the system
+                check(L.mg_particles_destroy(self._h))
+                self._h = None
+            h = C.c_void_p()
+            check(L.mg_particles_create(self._parent._h, cap, C.byref(h)))
+            self._h, self._cap = h, cap
+            for d in self._data:
+                d._alloc()
+        rec = np.ascontiguousarray(rec)
+        check(L.mg_particles_upload(self._h, rec.ctypes.data_as(C.c_void_p), n))
+        self._n = n
+        for d, old in saved:
+            new = np.zeros((n,) + old.shape[1:], old.dtype)
+            m = min(n, len(old))
+            new[:m] = old[:m]
+            d._upload(new)
+
+    def _flush(self):
+        if not self._pending and self._h is not None:
+            return
+        rec = self._records()
+        add = np.zeros(len(self._pending), dtype=rec.dtype)
+        if self._pending:
+            add["pos"] = np.asarray(self._pending, np.float32)
+        self._pending = []
+        self._set_records(np.concatenate([rec, add]))
+
+    def setPositions(self, pos, flags=None):
+        """all particles at once from an (n, 3) array (flags: (n,) int32, 0 if
+        omitted); a bulk form of addParticle"""
+        pos = np.asarray(pos, np.float32).reshape(-1, 3)
+        rec = np.zeros(len(pos), dtype=[("pos", np.float32, 3), ("flag", np.int32)])
+        rec["pos"] = pos
+        if flags is not None:
+            rec["flag"] = np.asarray(flags, np.int32)
+        self._pending = []
+        self._set_records(rec)
+
+    def positions(self):
+        """(positions (n, 3), flags (n,)) from the device"""
+        self._flush()
+        rec = self._records()
+        return np.ascontiguousarray(rec["pos"]), np.ascontiguousarray(rec["flag"])
+
+    def getPosPdata(self, target):
+        target._upload(self.positions()[0])
+
+    def setPosPdata(self, source):
+        self._flush()
+        rec = self._records()
+        rec["pos"] = source._download()
+        self._set_records(rec)
+
+    def kill(self, idx):
+        """ParticleBase::kill: mark particle idx deleted"""
+        self._flush()
+        rec = self._records()
+        rec["flag"][idx] |= ParticleDelete
+        self._set_records(rec)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            try:
+                _lib._lib.mg_particles_destroy(h)
+            except Exception:
+                pass
+
+
+class _Pdata:
+    """ParticleDataImpl<T> (source/particle.h:306-360) of one particle system"""
+    _kind = None
+    _comps = 1
+    _dtype = np.float32
+
+    def __init__(self, parts, show=True, name=None):
+        self._parts = parts
+        self.name = name
+        self._h = None
+        parts._data.append(self)
+        parts._flush()  # creates the device system (and this data) if needed
+        if self._h is None:
+            self._alloc()
+
+    def _alloc(self):
+        h = C.c_void_p()
+        check(_lib.load().mg_pdata_create(self._parts._h, self._kind, C.byref(h)))
+        self._h = h
+
+    def _shape(self):
+        n = self._parts._n
+        return (n, 3) if self._comps == 3 else (n,)
+
+    def _upload(self, a):
+        self._parts._flush()
+        a = np.ascontiguousarray(a, dtype=self._dtype).reshape(self._shape())
+        check(_lib.load().mg_pdata_upload(self._h, a.ctypes.data_as(C.c_void_p), self._parts._n))
+
+    def _download(self):
+        a = np.zeros(self._shape(), self._dtype)
+        if self._parts._n:
+            check(_lib.load().mg_pdata_download(self._h, a.ctypes.data_as(C.c_void_p), self._parts._n))
+        return a
+
+    def numpy(self):
+        self._parts._flush()
+        return self._download()
+
+    def setConst(self, s):
+        v = np.broadcast_to(np.asarray(_vec(s) if self._comps == 3 else s, self._dtype), self._shape())
+        self._upload(v)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            try:
+                _lib._lib.mg_pdata_destroy(h)
+            except Exception:
+                pass
+
+
+class PdataReal(_Pdata):
+    _kind = _KIND_REAL
+
+
+class PdataVec3(_Pdata):
+    _kind = _KIND_VEC3
+    _comps = 3
+
+
+class PdataInt(_Pdata):
+    _kind = _KIND_INT
+    _dtype = np.int32
+
+
+# plugin/numpyconvert.cpp:202-223
+def copyArrayToPdataInt(source, target):
+    target._upload(source)
+
+
+def copyPdataToArrayInt(source, target):
+    target[...] = source.numpy().reshape(target.shape)
+
+
+def copyArrayToPdataReal(source, target):
+    target._upload(source)
+
+
+def copyPdataToArrayReal(source, target):
+    target[...] = source.numpy().reshape(target.shape)
+
+
+def copyArrayToPdataVec3(source, target):
+    target._upload(source)
+
+
+def copyPdataToArrayVec3(source, target):
+    target[...] = source.numpy().reshape(target.shape)
+
+
+def mapPartsToMAC(flags, vel, velOld, parts, partVel, weight=None, ptype=None, exclude=0):
+    """plugin/flip.cpp:573-595"""
+    parts._flush()
+    check(_lib.load().mg_map_parts_to_mac(flags._h, vel._h, velOld._h, parts._h, partVel._h, _h(weight), _h(ptype),
+                                          int(exclude)))
+
+
+def mapMACToParts(flags, vel, parts, partVel, ptype=None, exclude=0):
+    """plugin/flip.cpp:651-655"""
+    parts._flush()
+    check(_lib.load().mg_map_mac_to_parts(flags._h, vel._h, parts._h, partVel._h, _h(ptype), int(exclude)))
+
+
+def flipVelocityUpdate(flags, vel, velOld, parts, partVel, flipRatio, ptype=None, exclude=0):
+    """plugin/flip.cpp:669-673"""
+    parts._flush()
+    check(_lib.load().mg_flip_velocity_update(flags._h, vel._h, velOld._h, parts._h, partVel._h, float(flipRatio),
+                                              _h(ptype), int(exclude)))
+
+
+def mapPartsToGrid(flags, target, parts, source):
+    """plugin/flip.cpp:617-619"""
+    parts._flush()
+    check(_lib.load().mg_map_parts_to_grid(flags._h, target._h, parts._h, source._h))
+
+
+def mapPartsToGridVec3(flags, target, parts, source):
+    """plugin/flip.cpp:620-622"""
+    mapPartsToGrid(flags, target, parts, source)
+
+
+def mapGridToParts(source, parts, target):
+    """plugin/flip.cpp:633-635"""
+    parts._flush()
+    check(_lib.load().mg_map_grid_to_parts(source._h, parts._h, target._h))
+
+
+def mapGridToPartsVec3(source, parts, target):
+    """plugin/flip.cpp:636-638"""
+    mapGridToParts(source, parts, target)
 
 __all__ = [n for n in dir() if not n.startswith("_") and n not in ("C", "np")]

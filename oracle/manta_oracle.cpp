@@ -49,6 +49,7 @@ typedef long long ll;
 #define SZ(d) ((d).is3d ? (ll)(d).nx * (d).ny : (ll)0)
 #define NCELL(d) ((ll)(d).nx * (d).ny * (d).nz)
 #define IX(d, i, j, k) ((ll)(i) + SY(d) * (j) + SZ(d) * (k))
+#define CELLS(d) ((ll)(d).nx * (d).ny * (d).nz)
 
 /* loop helpers: reference KERNEL ijk range with boundary width b */
 #define KLO(d, b) ((d).is3d ? (b) : 0)
@@ -2348,4 +2349,156 @@ void og_density_inflow(og_dims d, const int* flags, float* density, const float*
         const float target = og_noise_evaluate(q, tile, (float)i, (float)j, (float)k) * scale * factor;
         if (density[idx] < target) density[idx] = target;
       }
+}
+
+/* ------------------------------------------------------------------------ */
+/* FLIP transfers (plugin/flip.cpp:549-673).  Particles: pos[3*i] (Vec3
+ * records), flag[i] (BasicParticleData::flag, particle.h:182-191); a particle
+ * is active unless flag has ParticleBase::PDELETE (particle.h:41, :122).     */
+
+#define OG_PDELETE (1 << 10)
+
+static inline int part_skipped(const int* pflag, const int* ptype, int exclude, ll p) {
+  return (pflag[p] & OG_PDELETE) != 0 || (ptype && (ptype[p] & exclude) != 0);
+}
+
+/* setInterpolMAC (util/interpol.h:159-195): every component's 8 faces get the
+ * weight into sum and weight * value into data, in the reference's order
+ * (in 2D the z stride is 0 and both z layers land on one face) */
+static void set_interpol_mac(og_dims d, og_real* data, og_real* sum, og_real x, og_real y, og_real z,
+                             const og_real* val) {
+  const wts w = build_index(d, x, y, z);
+  const wts s = build_index_shift(d, x, y, z);
+  const ll X = 1, Y = SY(d), Z = SZ(d);
+#define ADD(arr, o, c, v) (arr)[3 * (o) + (c)] += (v)
+  { /* X: x shifted */
+    const ll b = ((ll)w.zi * d.ny + w.yi) * d.nx + s.xi;
+    og_real* ref = data + 3 * b;
+    og_real* sm = sum + 3 * b;
+    const og_real s0f0 = s.s0 * w.f0, s1f0 = s.s1 * w.f0, s0f1 = s.s0 * w.f1, s1f1 = s.s1 * w.f1;
+    const og_real w0 = w.t0 * s0f0, wx = w.t0 * s1f0, wy = w.t1 * s0f0, wxy = w.t1 * s1f0;
+    const og_real wz = w.t0 * s0f1, wxz = w.t0 * s1f1, wyz = w.t1 * s0f1, wxyz = w.t1 * s1f1;
+    const og_real v = val[0];
+    ADD(sm, Z, 0, wz); ADD(sm, X + Z, 0, wxz); ADD(sm, Y + Z, 0, wyz); ADD(sm, X + Y + Z, 0, wxyz);
+    ADD(ref, Z, 0, wz * v); ADD(ref, X + Z, 0, wxz * v); ADD(ref, Y + Z, 0, wyz * v); ADD(ref, X + Y + Z, 0, wxyz * v);
+    ADD(sm, 0, 0, w0); ADD(sm, X, 0, wx); ADD(sm, Y, 0, wy); ADD(sm, X + Y, 0, wxy);
+    ADD(ref, 0, 0, w0 * v); ADD(ref, X, 0, wx * v); ADD(ref, Y, 0, wy * v); ADD(ref, X + Y, 0, wxy * v);
+  }
+  { /* Y: y shifted */
+    const ll b = ((ll)w.zi * d.ny + s.yi) * d.nx + w.xi;
+    og_real* ref = data + 3 * b;
+    og_real* sm = sum + 3 * b;
+    const og_real s0f0 = w.s0 * w.f0, s1f0 = w.s1 * w.f0, s0f1 = w.s0 * w.f1, s1f1 = w.s1 * w.f1;
+    const og_real w0 = s.t0 * s0f0, wx = s.t0 * s1f0, wy = s.t1 * s0f0, wxy = s.t1 * s1f0;
+    const og_real wz = s.t0 * s0f1, wxz = s.t0 * s1f1, wyz = s.t1 * s0f1, wxyz = s.t1 * s1f1;
+    const og_real v = val[1];
+    ADD(sm, Z, 1, wz); ADD(sm, X + Z, 1, wxz); ADD(sm, Y + Z, 1, wyz); ADD(sm, X + Y + Z, 1, wxyz);
+    ADD(ref, Z, 1, wz * v); ADD(ref, X + Z, 1, wxz * v); ADD(ref, Y + Z, 1, wyz * v); ADD(ref, X + Y + Z, 1, wxyz * v);
+    ADD(sm, 0, 1, w0); ADD(sm, X, 1, wx); ADD(sm, Y, 1, wy); ADD(sm, X + Y, 1, wxy);
+    ADD(ref, 0, 1, w0 * v); ADD(ref, X, 1, wx * v); ADD(ref, Y, 1, wy * v); ADD(ref, X + Y, 1, wxy * v);
+  }
+  { /* Z: z shifted; the z = 0 layer first */
+    const ll b = ((ll)s.zi * d.ny + w.yi) * d.nx + w.xi;
+    og_real* ref = data + 3 * b;
+    og_real* sm = sum + 3 * b;
+    const og_real s0f0 = w.s0 * s.f0, s1f0 = w.s1 * s.f0, s0f1 = w.s0 * s.f1, s1f1 = w.s1 * s.f1;
+    const og_real w0 = w.t0 * s0f0, wx = w.t0 * s1f0, wy = w.t1 * s0f0, wxy = w.t1 * s1f0;
+    const og_real wz = w.t0 * s0f1, wxz = w.t0 * s1f1, wyz = w.t1 * s0f1, wxyz = w.t1 * s1f1;
+    const og_real v = val[2];
+    ADD(sm, 0, 2, w0); ADD(sm, X, 2, wx); ADD(sm, Y, 2, wy); ADD(sm, X + Y, 2, wxy);
+    ADD(sm, Z, 2, wz); ADD(sm, X + Z, 2, wxz); ADD(sm, Y + Z, 2, wyz); ADD(sm, X + Y + Z, 2, wxyz);
+    ADD(ref, 0, 2, w0 * v); ADD(ref, X, 2, wx * v); ADD(ref, Y, 2, wy * v); ADD(ref, X + Y, 2, wxy * v);
+    ADD(ref, Z, 2, wz * v); ADD(ref, X + Z, 2, wxz * v); ADD(ref, Y + Z, 2, wyz * v); ADD(ref, X + Y + Z, 2, wxyz * v);
+  }
+#undef ADD
+}
+
+/* mapPartsToMAC (flip.cpp:573-595) with knMapLinearVec3ToMACGrid (:561-570)
+ * run serially in particle order; weight (AoS Vec3) may be NULL */
+void og_map_parts_to_mac(og_dims d, og_real* vel, og_real* velOld, og_real* weight, ll np, const og_real* pos,
+                         const int* pflag, const og_real* pvel, const int* ptype, int exclude) {
+  const ll n3 = 3 * CELLS(d);
+  og_real* w = weight ? weight : (og_real*)malloc(sizeof(og_real) * n3);
+  for (ll i = 0; i < n3; i++) { w[i] = OG_R(0.); vel[i] = OG_R(0.); }
+  for (ll p = 0; p < np; p++) {
+    if (part_skipped(pflag, ptype, exclude, p)) continue;
+    set_interpol_mac(d, vel, w, pos[3 * p], pos[3 * p + 1], pos[3 * p + 2], pvel + 3 * p);
+  }
+  /* Grid<Vec3>::stomp (grid.cpp:224-226), then MACGrid::safeDivide
+   * (safeDivide, general.h:150) */
+  for (ll i = 0; i < n3; i++) {
+    if (w[i] < OG_R(OG_VEC_EPS)) w[i] = OG_R(0.);
+    if (w[i] != OG_R(0.)) vel[i] = vel[i] / w[i];
+    velOld[i] = vel[i];
+  }
+  if (!weight) free(w);
+}
+
+/* mapPartsToGrid / mapPartsToGridVec3 (flip.cpp:599-622): setInterpol
+ * (util/interpol.h:93-112) per particle, then knSafeDivReal (:549-557);
+ * comps 1 (Real) or 3 (Vec3, AoS) */
+void og_map_parts_to_grid(og_dims d, og_real* target, int comps, ll np, const og_real* pos, const int* pflag,
+                          const og_real* src) {
+  const ll n = CELLS(d);
+  og_real* sum = (og_real*)calloc((size_t)n, sizeof(og_real));
+  for (ll i = 0; i < n * comps; i++) target[i] = OG_R(0.);
+  const ll X = 1, Y = SY(d), Z = SZ(d);
+  for (ll p = 0; p < np; p++) {
+    if (pflag[p] & OG_PDELETE) continue;
+    const wts w = build_index(d, pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]);
+    const ll b = (ll)w.xi + Y * w.yi + Z * w.zi;
+    const og_real s0f0 = w.s0 * w.f0, s1f0 = w.s1 * w.f0, s0f1 = w.s0 * w.f1, s1f1 = w.s1 * w.f1;
+    const og_real w0 = w.t0 * s0f0, wx = w.t0 * s1f0, wy = w.t1 * s0f0, wxy = w.t1 * s1f0;
+    const og_real wz = w.t0 * s0f1, wxz = w.t0 * s1f1, wyz = w.t1 * s0f1, wxyz = w.t1 * s1f1;
+    const og_real* v = src + (ll)comps * p;
+    og_real* sm = sum + b;
+    og_real* ref = target + (ll)comps * b;
+#define ADDV(o, wt)                                                  \
+  for (int c = 0; c < comps; c++) ref[(ll)comps * (o) + c] += (wt) * v[c];
+    sm[Z] += wz; sm[X + Z] += wxz; sm[Y + Z] += wyz; sm[X + Y + Z] += wxyz;
+    ADDV(Z, wz) ADDV(X + Z, wxz) ADDV(Y + Z, wyz) ADDV(X + Y + Z, wxyz)
+    sm[0] += w0; sm[X] += wx; sm[Y] += wy; sm[X + Y] += wxy;
+    ADDV(0, w0) ADDV(X, wx) ADDV(Y, wy) ADDV(X + Y, wxy)
+#undef ADDV
+  }
+  for (ll i = 0; i < n; i++) {
+    for (int c = 0; c < comps; c++) {
+      og_real* t = target + (ll)comps * i + c;
+      if (sum[i] < OG_R(OG_VEC_EPS)) *t = OG_R(0.);
+      else if (sum[i] != OG_R(0.)) *t = *t / sum[i];
+    }
+  }
+  free(sum);
+}
+
+/* mapMACToParts (flip.cpp:643-655); with velOld, flipVelocityUpdate
+ * (:659-673): pvel = flipRatio * (pvel + delta) + (1.0 - flipRatio) * v,
+ * whose second product the reference forms in double */
+void og_map_mac_to_parts(og_dims d, const og_real* vel, const og_real* velOld, og_real flipRatio, ll np,
+                         const og_real* pos, const int* pflag, og_real* pvel, const int* ptype, int exclude) {
+  for (ll p = 0; p < np; p++) {
+    if (part_skipped(pflag, ptype, exclude, p)) continue;
+    const og_real x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
+    const v3 v = interp_mac(d, vel, x, y, z);
+    og_real* pv = pvel + 3 * p;
+    if (!velOld) {
+      pv[0] = v.x; pv[1] = v.y; pv[2] = v.z;
+      continue;
+    }
+    const v3 o = interp_mac(d, velOld, x, y, z);
+    const og_real dl[3] = {v.x - o.x, v.y - o.y, v.z - o.z};
+    const og_real vv[3] = {v.x, v.y, v.z};
+    const double keep = 1.0 - (double)flipRatio;
+    for (int c = 0; c < 3; c++) pv[c] = flipRatio * (pv[c] + dl[c]) + (og_real)(keep * (double)vv[c]);
+  }
+}
+
+/* mapGridToParts / mapGridToPartsVec3 (knMapFromGrid, flip.cpp:625-638) */
+void og_map_grid_to_parts(og_dims d, const og_real* grid, int comps, ll np, const og_real* pos, const int* pflag,
+                          og_real* target) {
+  for (ll p = 0; p < np; p++) {
+    if (pflag[p] & OG_PDELETE) continue;
+    for (int c = 0; c < comps; c++)
+      target[(ll)comps * p + c] = interp_ch(d, grid, comps, c, pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]);
+  }
 }

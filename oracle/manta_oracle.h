@@ -181,6 +181,18 @@ void og_density_inflow(og_dims d, const int* flags, float* density, const float*
 /* fractions / obstacle velocity (MAC grids) for the next pressure calls */
 void og_set_fractions(const og_real* fractions, const og_real* obvel);
 
+/* FLIP transfers (plugin/flip.cpp:549-673).  Particles are pos[3*i] and
+ * flag[i] (BasicParticleData, particle.h:182-191); ptype may be NULL; Vec3
+ * data and grids are array-of-structs. */
+void og_map_parts_to_mac(og_dims d, og_real* vel, og_real* velOld, og_real* weight, long long np, const og_real* pos,
+                         const int* pflag, const og_real* pvel, const int* ptype, int exclude);
+void og_map_parts_to_grid(og_dims d, og_real* target, int comps, long long np, const og_real* pos, const int* pflag,
+                          const og_real* src);
+void og_map_mac_to_parts(og_dims d, const og_real* vel, const og_real* velOld, og_real flipRatio, long long np,
+                         const og_real* pos, const int* pflag, og_real* pvel, const int* ptype, int exclude);
+void og_map_grid_to_parts(og_dims d, const og_real* grid, int comps, long long np, const og_real* pos,
+                          const int* pflag, og_real* target);
+
 #ifdef __cplusplus
 }
 #endif

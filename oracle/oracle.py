@@ -125,6 +125,11 @@ def lib(dtype=np.float32):
             L.og_noise_evaluate.restype = C.c_float
             L.og_cylinder_sdf.argtypes = [Dims, f32, f32, C.c_float, f32, C.c_float]
             L.og_density_inflow.argtypes = [Dims, ip, f32, f32, C.POINTER(NoiseParams), f32, C.c_float, C.c_float]
+        LL = C.c_longlong
+        L.og_map_parts_to_mac.argtypes = [Dims, fp, fp, C.c_void_p, LL, fp, ip, fp, C.c_void_p, I]
+        L.og_map_parts_to_grid.argtypes = [Dims, fp, I, LL, fp, ip, fp]
+        L.og_map_mac_to_parts.argtypes = [Dims, fp, C.c_void_p, F, LL, fp, ip, fp, C.c_void_p, I]
+        L.og_map_grid_to_parts.argtypes = [Dims, fp, I, LL, fp, ip, fp]
         L.og_set_fractions.argtypes = [C.c_void_p, C.c_void_p]
         L.og_set_num_threads.argtypes = [I]
         L.og_get_num_threads.restype = I
@@ -173,6 +178,41 @@ def extrapolate_mac_simple(flags, vel, distance=4, intoObs=False):
 
 def extrapolate_ls_simple(phi, distance=4, inside=False):
     lib(phi.dtype).og_extrapolate_ls_simple(dims(phi.shape), phi, int(distance), int(bool(inside)))
+
+
+# -------------------------------------------------- FLIP transfers
+# particles: pos (np, 3) and flag (np,) int32 -- BasicParticleData; ptype an
+# int32 (np,) array or None; Vec3 particle data (np, 3); grids as elsewhere
+
+
+def map_parts_to_mac(flags, vel, velOld, pos, pflag, pvel, weight=None, ptype=None, exclude=0):
+    """mapPartsToMAC (flip.cpp:573-595): vel, velOld (and weight) in place"""
+    lib(vel.dtype).og_map_parts_to_mac(dims(flags.shape), vel, velOld, _ptr(weight), len(pflag), pos, pflag, pvel,
+                                       _ptr(ptype), int(exclude))
+
+
+def map_parts_to_grid(flags, target, pos, pflag, src):
+    """mapPartsToGrid / mapPartsToGridVec3 (flip.cpp:599-622)"""
+    comps = 3 if target.ndim == 4 else 1
+    lib(target.dtype).og_map_parts_to_grid(dims(flags.shape), target, comps, len(pflag), pos, pflag, src)
+
+
+def map_mac_to_parts(flags, vel, pos, pflag, pvel, ptype=None, exclude=0):
+    """mapMACToParts (flip.cpp:651-655): pvel in place"""
+    lib(vel.dtype).og_map_mac_to_parts(dims(flags.shape), vel, None, 0.0, len(pflag), pos, pflag, pvel, _ptr(ptype),
+                                       int(exclude))
+
+
+def flip_velocity_update(flags, vel, velOld, pos, pflag, pvel, flipRatio, ptype=None, exclude=0):
+    """flipVelocityUpdate (flip.cpp:669-673): pvel in place"""
+    lib(vel.dtype).og_map_mac_to_parts(dims(flags.shape), vel, _ptr(velOld), flipRatio, len(pflag), pos, pflag, pvel,
+                                       _ptr(ptype), int(exclude))
+
+
+def map_grid_to_parts(grid, pos, pflag, target):
+    """mapGridToParts / mapGridToPartsVec3 (flip.cpp:625-638): target in place"""
+    comps = 3 if grid.ndim == 4 else 1
+    lib(grid.dtype).og_map_grid_to_parts(dims(grid.shape), grid, comps, len(pflag), pos, pflag, target)
 
 
 _TILE = None
