@@ -581,6 +581,66 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(out), flush=True)
 
 
+def flip_form(m, n, ppc, reps, seed):
+    """The FLIP transfers (plugin/flip.cpp:573-673) at n^3 with ppc particles
+    per cell, seeded cell by cell with jitter as a fresh FLIP scene seeds
+    them: device time per call of mapPartsToMAC, mapMACToParts and
+    flipVelocityUpdate (CUDA events on the solver's stream), against the
+    oracle's serial loops (the reference's single-threaded splat) on the
+    same particles."""
+    from mantaflow_gb300 import _lib
+    from oracle import oracle as og
+    L = _lib.load()
+    s = m.Solver(name="flip", gridSize=m.vec3(n, n, n), dim=3)
+    flags = s.create(m.FlagGrid)
+    flags.initDomain(boundaryWidth=0)
+    flags.fillGrid()
+    rng = np.random.default_rng(seed)
+    cells = np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")[::-1], -1).reshape(-1, 3)
+    pos = (np.repeat(cells, ppc, axis=0) + rng.random((n ** 3 * ppc, 3))).astype(np.float32)
+    count = len(pos)
+    pv = rng.standard_normal((count, 3)).astype(np.float32)
+    pp = s.create(m.BasicParticleSystem)
+    pp.setPositions(pos)
+    pvel = pp.create(m.PdataVec3)
+    m.copyArrayToPdataVec3(pv, pvel)
+    vel, velOld = s.create(m.MACGrid), s.create(m.MACGrid)
+    out = {"workload": "%d^3 grid, %d particles per cell (%d particles) seeded cell by cell with jitter" % (n, ppc, count),
+           "particles": count}
+
+    def timed(fn):
+        fn()
+        s.sync()
+        _lib.check(L.mg_mark(s._h, 0))
+        for _ in range(reps):
+            fn()
+        _lib.check(L.mg_mark(s._h, 1))
+        ms = C.c_float()
+        _lib.check(L.mg_elapsed(s._h, 0, 1, C.byref(ms)))
+        return ms.value / reps
+
+    t_p2g = timed(lambda: m.mapPartsToMAC(flags=flags, vel=vel, velOld=velOld, parts=pp, partVel=pvel))
+    t_g2p = timed(lambda: m.mapMACToParts(flags=flags, vel=vel, parts=pp, partVel=pvel))
+    t_flip = timed(lambda: m.flipVelocityUpdate(flags=flags, vel=vel, velOld=velOld, parts=pp, partVel=pvel,
+                                                flipRatio=0.95))
+    f = flags.numpy()
+    pflag = np.zeros(count, np.int32)
+    v0, v1 = np.zeros(f.shape + (3,), np.float32), np.zeros(f.shape + (3,), np.float32)
+    t0 = time.perf_counter()
+    og.map_parts_to_mac(f, v0, v1, pos, pflag, pv)
+    c_p2g = 1e3 * (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    og.map_mac_to_parts(f, v0, pos, pflag, pv)
+    c_g2p = 1e3 * (time.perf_counter() - t0)
+    out.update({"map_parts_to_mac_ms": t_p2g, "map_mac_to_parts_ms": t_g2p, "flip_velocity_update_ms": t_flip,
+                "map_parts_to_mac_particles_per_s": count / (t_p2g / 1e3),
+                "cpu_oracle": {"map_parts_to_mac_ms": c_p2g, "map_mac_to_parts_ms": c_g2p, "cores": 1,
+                               "kind": "port", "sample": "one call each on the same particles, serial as the reference"},
+                "speedup_map_parts_to_mac": c_p2g / t_p2g, "reps": reps})
+    del pp, pvel, vel, velOld, flags, s
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -602,6 +662,7 @@ def main():
     ap.add_argument("--served-jobs", type=int, default=32, help="jobs of the config-5 served run (0: skip)")
     ap.add_argument("--served-plain-sample", type=int, default=3,
                     help="timed steps per job measuring the plain sequential path")
+    ap.add_argument("--flip-size", type=int, default=128, help="grid side of the FLIP transfer measurement (0: skip)")
     ap.add_argument("--refined-steps", type=int, default=5,
                     help="timed 256^3 steps of the FP64-refined form reported beside the headline (0: skip)")
     args = ap.parse_args()
@@ -791,6 +852,9 @@ def main():
     served = None
     if args.served_jobs > 0 and rank == 0:
         served = served_form(m, args.seed + 17, args.served_jobs, args.served_plain_sample)
+    flip = None
+    if args.flip_size > 0 and rank == 0:
+        flip = flip_form(m, args.flip_size, 8, 10, args.seed + 23)
     precision = None
     if args.precision_size > 0 and rank == 0 and world == 1:
         precision = precision_form(m, args.precision_size, args.precision_steps, args.seed + 5)
@@ -822,7 +886,7 @@ def main():
                "clocks": clk, "e2e": e2e, "roofline": roofline, "rooflines": rooflines, "cpu_baseline": cpu,
                "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])},
                "same_scene_pc_mic": alt, "precision_form": {"refined_256": refined, "errors_vs_fp64": precision},
-               "batched_form": batched, "served_form": served}
+               "batched_form": batched, "served_form": served, "flip_transfers": flip}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()

@@ -48,7 +48,30 @@ class FlagGrid : public Grid<int> {
                   TypeOpen = 32, TypeStick = 64 };
 };
 class LevelsetGrid : public Grid<Real> {};
-class BasicParticleSystem;
+typedef long long IndexInt;
+// particle.h:182-191, 193, 276, 306
+struct BasicParticleData {
+  Vec3 pos;
+  int flag;
+};
+class BasicParticleSystem {
+ public:
+  BasicParticleData& operator[](IndexInt idx);
+  const BasicParticleData& operator[](IndexInt idx) const;
+  IndexInt size() const;
+  FluidSolver* getParent() const;
+};
+class ParticleDataBase {
+ public:
+  virtual ~ParticleDataBase();
+};
+template <class T>
+class ParticleDataImpl : public ParticleDataBase {
+ public:
+  T& operator[](IndexInt idx);
+  const T& operator[](IndexInt idx) const;
+  IndexInt size() const;
+};
 class ParticleIndexSystem;
 
 [[noreturn]] inline void errMsgText(const std::string& s) { throw std::runtime_error(s); }
