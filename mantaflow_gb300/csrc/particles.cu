@@ -263,6 +263,31 @@ __global__ void k_bucket_starts(const unsigned* __restrict__ keys, long long n, 
 namespace {
 
 // ----------------------------------------------------- particle -> grid
+// Positions and values copied into bucket order after a sort, so that the
+// faces' merges read them in sequence instead of gathering each particle
+// from its own index (every particle is read by up to 8 faces per sort).
+struct SortedParts {
+  const float* x;
+  const float* y;
+  const float* z;
+  const float* v[3];
+};
+__global__ void k_sorted_copy(long long n, const unsigned* __restrict__ sorted, PartView p, const float* __restrict__ v0,
+                              const float* __restrict__ v1, const float* __restrict__ v2, float* sx, float* sy,
+                              float* sz, float* s0, float* s1, float* s2) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned k = sorted[i];
+  sx[i] = p.x[k];
+  sy[i] = p.y[k];
+  sz[i] = p.z[k];
+  s0[i] = __ldg(v0 + k);
+  if (v1) {
+    s1[i] = __ldg(v1 + k);
+    s2[i] = __ldg(v2 + k);
+  }
+}
+
 // The weights setInterpol / setInterpolMAC give the stencil corner (dx, dy,
 // dz) of a particle: T[dy] * (S[dx] * F[dz]) (util/interpol.h:93-112,
 // 159-195), with the axis of MAC component comp shifted.
@@ -293,8 +318,7 @@ __device__ __forceinline__ CornerW corner_weights(const Dims& d, float px, float
 // written.  For cells (mapPartsToGrid, knSafeDivReal, flip.cpp:549-557):
 // weights below VECTOR_EPSILON give 0, others divide.
 template <int kComps>
-__global__ void __launch_bounds__(256) k_p2g_gather(Dims d, int comp, PartView p, const float* __restrict__ v0,
-                                                    const float* __restrict__ v1, const float* __restrict__ v2,
+__global__ void __launch_bounds__(256) k_p2g_gather(Dims d, int comp, SortedParts sp,
                                                     const unsigned* __restrict__ sorted,
                                                     const unsigned* __restrict__ starts, float* o0, float* o1,
                                                     float* o2, float* old, float* wout) {
@@ -329,11 +353,15 @@ __global__ void __launch_bounds__(256) k_p2g_gather(Dims d, int comp, PartView p
         bq = q;
       }
     if (best == kNone) break;
-    const CornerW c = corner_weights(d, p.x[best], p.y[best], p.z[best], comp);
+    unsigned at = cur[0];  // the particle's slot in bucket order
+#pragma unroll
+    for (int q = 1; q < 8; q++)
+      if (q == bq) at = cur[q];
+    const CornerW c = corner_weights(d, __ldg(sp.x + at), __ldg(sp.y + at), __ldg(sp.z + at), comp);
     const int dx = bq & 1, dy = (bq >> 1) & 1, dz = bq >> 2;
-    const float a0 = __ldg(v0 + best);
-    const float a1 = kComps == 3 ? __ldg(v1 + best) : 0.f;
-    const float a2 = kComps == 3 ? __ldg(v2 + best) : 0.f;
+    const float a0 = __ldg(sp.v[0] + at);
+    const float a1 = kComps == 3 ? __ldg(sp.v[1] + at) : 0.f;
+    const float a2 = kComps == 3 ? __ldg(sp.v[2] + at) : 0.f;
     if (d.is3d) {
       const float w = c.T[dy] * (c.S[dx] * c.F[dz]);
       sum += w;
@@ -438,6 +466,7 @@ struct mg_particles_s {
   // counts and their scan's block totals, bucket starts (ncells + 1)
   unsigned *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr};
   unsigned *hist = nullptr, *sums = nullptr, *starts = nullptr;
+  float* sorted[6] = {};  // positions and up to 3 values in bucket order
   void* stage = nullptr;  // 16 bytes per particle for record transfers
 };
 
@@ -467,6 +496,8 @@ void free_parts(mg_particles p) {
   void* bufs[] = {p->x, p->y, p->z, p->flag, p->keys[0], p->keys[1], p->vals[0], p->vals[1], p->hist, p->sums,
                   p->starts, p->stage};
   for (void* b : bufs)
+    if (b) cudaFree(b);
+  for (float* b : p->sorted)
     if (b) cudaFree(b);
 }
 
@@ -522,6 +553,19 @@ const unsigned* sort_stencil(mg_particles p, int comp, const PartView& v) {
   return p->vals[a];
 }
 
+// the live particles' positions and values (1 or 3 planes) in bucket order
+SortedParts sorted_copy(mg_particles p, const unsigned* sorted, const PartView& v, const float* v0, const float* v1,
+                        const float* v2) {
+  const long long n = p->n;
+  if (n > 0) {
+    count_launch();
+    k_sorted_copy<<<blocks_of(n), 256, 0, p->st>>>(n, sorted, v, v0, v1, v2, p->sorted[0], p->sorted[1],
+                                                    p->sorted[2], p->sorted[3], p->sorted[4], p->sorted[5]);
+  }
+  SortedParts sp{p->sorted[0], p->sorted[1], p->sorted[2], {p->sorted[3], p->sorted[4], p->sorted[5]}};
+  return sp;
+}
+
 PartView view_of(mg_particles p, mg_pdata ptype, int exclude) {
   PartView v{p->x, p->y, p->z, p->flag, ptype ? (const int*)ptype->c[0] : nullptr, exclude};
   return v;
@@ -575,6 +619,7 @@ extern "C" int mg_particles_create(mg_solver s, long long capacity, mg_particles
             cudaMalloc(&p->hist, histN * 4) == cudaSuccess &&
             cudaMalloc(&p->sums, ((histN + kRsTile - 1) / kRsTile) * 4) == cudaSuccess &&
             cudaMalloc(&p->starts, (p->d.n + 1) * 4) == cudaSuccess && cudaMalloc(&p->stage, c * 16) == cudaSuccess;
+  for (int q = 0; q < 6 && ok; q++) ok = cudaMalloc(&p->sorted[q], c * 4) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     free_parts(p);
@@ -740,10 +785,10 @@ extern "C" int mg_map_parts_to_mac(mg_grid flags, mg_grid vel, mg_grid velOld, m
   const dim3 b(32, 8, 1);
   for (int c = 0; c < 3; c++) {
     const unsigned* sorted = sort_stencil(parts, c, pv);
+    const SortedParts sp = sorted_copy(parts, sorted, pv, partVel->c[c], nullptr, nullptr);
     count_launch();
-    k_p2g_gather<1><<<grid3(d, b), b, 0, parts->st>>>(d, c, pv, partVel->c[c], nullptr, nullptr, sorted, parts->starts,
-                                                      v + c * d.n, nullptr, nullptr, vo + c * d.n,
-                                                      w ? w + c * d.n : nullptr);
+    k_p2g_gather<1><<<grid3(d, b), b, 0, parts->st>>>(d, c, sp, sorted, parts->starts, v + c * d.n, nullptr, nullptr,
+                                                      vo + c * d.n, w ? w + c * d.n : nullptr);
   }
   return launch_status(what);
 }
@@ -762,14 +807,16 @@ extern "C" int mg_map_parts_to_grid(mg_grid flags, mg_grid target, mg_particles 
   const Dims& d = parts->d;
   const PartView pv = view_of(parts, nullptr, 0);
   const unsigned* sorted = sort_stencil(parts, -1, pv);
+  const SortedParts sp = sorted_copy(parts, sorted, pv, source->c[0], vec ? source->c[1] : nullptr,
+                                     vec ? source->c[2] : nullptr);
   const dim3 b(32, 8, 1);
   count_launch();
   if (vec)
-    k_p2g_gather<3><<<grid3(d, b), b, 0, parts->st>>>(d, -1, pv, source->c[0], source->c[1], source->c[2], sorted,
-                                                      parts->starts, t, t + d.n, t + 2 * d.n, nullptr, nullptr);
+    k_p2g_gather<3><<<grid3(d, b), b, 0, parts->st>>>(d, -1, sp, sorted, parts->starts, t, t + d.n, t + 2 * d.n,
+                                                      nullptr, nullptr);
   else
-    k_p2g_gather<1><<<grid3(d, b), b, 0, parts->st>>>(d, -1, pv, source->c[0], nullptr, nullptr, sorted,
-                                                      parts->starts, t, nullptr, nullptr, nullptr, nullptr);
+    k_p2g_gather<1><<<grid3(d, b), b, 0, parts->st>>>(d, -1, sp, sorted, parts->starts, t, nullptr, nullptr, nullptr,
+                                                      nullptr);
   return launch_status(what);
 }
 
