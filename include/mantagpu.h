@@ -104,10 +104,11 @@ int mg_grid_download(mg_grid g, void* host, size_t bytes);
  * hosts (no counterpart in the reference, whose copies are synchronous).
  * They return at once; the host buffer (pinned: mg_host_alloc) must stay
  * untouched until mg_solver_wait_copies returns.  The transfer runs on the
- * solver's copy stream through a device staging copy of the grid, ordered
- * against the solver's kernels: an upload lands before any kernel queued
- * after it, a download takes the grid as it is after the kernels queued
- * before it, and the next step's kernels may run while it streams out. */
+ * solver's copy streams (uploads and downloads on separate ones) through a
+ * device staging copy of the grid, ordered against the solver's kernels: an
+ * upload lands before any kernel queued after it, a download takes the grid
+ * as it is after the kernels queued before it, and the next step's upload
+ * and kernels may run while it streams out. */
 int mg_grid_upload_async(mg_grid g, const void* host, size_t bytes);
 int mg_grid_download_async(mg_grid g, void* host, size_t bytes);
 /* Block until every asynchronous transfer and kernel of the solver is done. */

@@ -94,7 +94,8 @@ struct mg_solver_s {
   // move it at once
   static constexpr int kMaxCopyStreams = 8;
   int ncopy = 0;
-  cudaStream_t copyStream[kMaxCopyStreams] = {};
+  cudaStream_t copyStream[kMaxCopyStreams] = {};  // device -> host
+  cudaStream_t upStream[kMaxCopyStreams] = {};    // host -> device
   std::multimap<size_t, void*> pool;  // free device buffers by size
   std::set<mg_grid> grids;
   size_t poolBytes = 0;  // free buffers in the pool
@@ -396,7 +397,10 @@ static void free_stage(mg_grid g) {
   g->nFree = 0;
 }
 static void sync_copies(mg_solver s) {
-  for (int k = 0; k < s->ncopy; k++) cudaStreamSynchronize(s->copyStream[k]);
+  for (int k = 0; k < s->ncopy; k++) {
+    cudaStreamSynchronize(s->copyStream[k]);
+    cudaStreamSynchronize(s->upStream[k]);
+  }
 }
 
 extern "C" int mg_solver_destroy(mg_solver s) {
@@ -418,7 +422,10 @@ extern "C" int mg_solver_destroy(mg_solver s) {
   prof_collect(s);
   for (auto e : s->evFree) cudaEventDestroy(e);
   for (auto e : s->marks) cudaEventDestroy(e);
-  for (int k = 0; k < s->ncopy; k++) cudaStreamDestroy(s->copyStream[k]);
+  for (int k = 0; k < s->ncopy; k++) {
+    cudaStreamDestroy(s->copyStream[k]);
+    cudaStreamDestroy(s->upStream[k]);
+  }
   cudaStreamDestroy(s->stream);
   g_ctx.solvers.erase(s);
   delete s;
@@ -574,7 +581,12 @@ static int ensure_stage(mg_grid g) {
     int n = 4;
     if (const char* e = std::getenv("MANTAGPU_COPY_STREAMS")) n = std::atoi(e);
     n = std::max(1, std::min(n, (int)mg_solver_s::kMaxCopyStreams));
-    for (int k = 0; k < n; k++) CK(cudaStreamCreateWithFlags(&s->copyStream[k], cudaStreamNonBlocking));
+    // downloads and uploads on streams of their own: the next step's upload
+    // must not queue behind this step's downloads
+    for (int k = 0; k < n; k++) {
+      CK(cudaStreamCreateWithFlags(&s->copyStream[k], cudaStreamNonBlocking));
+      CK(cudaStreamCreateWithFlags(&s->upStream[k], cudaStreamNonBlocking));
+    }
     s->ncopy = n;
   }
   if (!g->stage) {
@@ -596,15 +608,16 @@ static int wait_stage_free(mg_grid g, cudaStream_t st) {
 }
 // the copy split into one 256-byte-aligned chunk per copy stream, each after
 // `ready`; records the grid's free events on the streams it used
-static int chunked_copy(mg_grid g, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaEvent_t ready) {
+static int chunked_copy(mg_grid g, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaEvent_t ready,
+                        cudaStream_t* streams) {
   mg_solver s = g->s;
   const size_t per = ((bytes + s->ncopy - 1) / s->ncopy + 255) & ~(size_t)255;
   int used = 0;
   for (int k = 0; k < s->ncopy && (size_t)k * per < bytes; k++) {
     const size_t off = (size_t)k * per, len = std::min(per, bytes - off);
-    if (ready) CK(cudaStreamWaitEvent(s->copyStream[k], ready, 0));
-    CK(cudaMemcpyAsync((char*)dst + off, (const char*)src + off, len, kind, s->copyStream[k]));
-    CK(cudaEventRecord(g->stageFree[k], s->copyStream[k]));
+    if (ready) CK(cudaStreamWaitEvent(streams[k], ready, 0));
+    CK(cudaMemcpyAsync((char*)dst + off, (const char*)src + off, len, kind, streams[k]));
+    CK(cudaEventRecord(g->stageFree[k], streams[k]));
     used++;
   }
   g->nFree = used;
@@ -619,8 +632,8 @@ extern "C" int mg_grid_upload_async(mg_grid g, const void* host, size_t bytes) {
   mg_solver s = g->s;
   ProfScope ps(s, "h2d");
   for (int k = 0; k < s->ncopy; k++)
-    if ((st = wait_stage_free(g, s->copyStream[k]))) return st;
-  if ((st = chunked_copy(g, g->stage, host, bytes, cudaMemcpyHostToDevice, nullptr))) return st;
+    if ((st = wait_stage_free(g, s->upStream[k]))) return st;
+  if ((st = chunked_copy(g, g->stage, host, bytes, cudaMemcpyHostToDevice, nullptr, s->upStream))) return st;
   // the compute stream waits for every chunk, then moves staging -> grid
   for (int k = 0; k < g->nFree; k++) CK(cudaStreamWaitEvent(s->stream, g->stageFree[k], 0));
   if (is_vec(g)) {
@@ -649,12 +662,15 @@ extern "C" int mg_grid_download_async(mg_grid g, void* host, size_t bytes) {
     CK(cudaMemcpyAsync(g->stage, g->data, bytes, cudaMemcpyDeviceToDevice, s->stream));
   }
   CK(cudaEventRecord(g->stageReady, s->stream));
-  return chunked_copy(g, host, g->stage, bytes, cudaMemcpyDeviceToHost, g->stageReady);
+  return chunked_copy(g, host, g->stage, bytes, cudaMemcpyDeviceToHost, g->stageReady, s->copyStream);
 }
 
 extern "C" int mg_solver_wait_copies(mg_solver s) {
   if (!valid_solver(s)) return fail(MG_ERR_ARG, "mg_solver_wait_copies: invalid solver");
-  for (int k = 0; k < s->ncopy; k++) CK(cudaStreamSynchronize(s->copyStream[k]));
+  for (int k = 0; k < s->ncopy; k++) {
+    CK(cudaStreamSynchronize(s->copyStream[k]));
+    CK(cudaStreamSynchronize(s->upStream[k]));
+  }
   CK(cudaStreamSynchronize(s->stream));
   return MG_OK;
 }

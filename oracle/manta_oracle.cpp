@@ -2502,3 +2502,24 @@ void og_map_grid_to_parts(og_dims d, const og_real* grid, int comps, ll np, cons
       target[(ll)comps * p + c] = interp_ch(d, grid, comps, c, pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]);
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* resetOutflow (plugin/extforces.cpp:133-160) without particles: outflow
+ * cells lose the fluid flag and gain the empty flag; phi = 0.5, real = 0
+ * there.  phi / real may be NULL. */
+void og_reset_outflow(og_dims d, int* flags, og_real* phi, og_real* real) {
+  const ll n = NCELL(d);
+  for (ll idx = 0; idx < n; idx++) {
+    if (!(flags[idx] & OG_OUTFLOW)) continue;
+    flags[idx] = (flags[idx] | OG_EMPTY) & ~OG_FLUID;
+    if (phi) phi[idx] = OG_R(0.5);
+    if (real) real[idx] = OG_R(0.);
+  }
+}
+
+/* resetPhiInObs (plugin/advection.cpp:396-401) */
+void og_reset_phi_in_obs(og_dims d, const int* flags, og_real* sdf) {
+  const ll n = NCELL(d);
+  for (ll idx = 0; idx < n; idx++)
+    if ((flags[idx] & OG_OBSTACLE) && sdf[idx] < OG_R(0.)) sdf[idx] = OG_R(0.1);
+}

@@ -181,6 +181,12 @@ void og_density_inflow(og_dims d, const int* flags, float* density, const float*
 /* fractions / obstacle velocity (MAC grids) for the next pressure calls */
 void og_set_fractions(const og_real* fractions, const og_real* obvel);
 
+/* resetOutflow (extforces.cpp:133-160) without particles; phi / real may be
+ * NULL */
+void og_reset_outflow(og_dims d, int* flags, og_real* phi, og_real* real);
+/* resetPhiInObs (advection.cpp:396-401) */
+void og_reset_phi_in_obs(og_dims d, const int* flags, og_real* sdf);
+
 /* FLIP transfers (plugin/flip.cpp:549-673).  Particles are pos[3*i] and
  * flag[i] (BasicParticleData, particle.h:182-191); ptype may be NULL; Vec3
  * data and grids are array-of-structs. */

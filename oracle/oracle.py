@@ -130,6 +130,8 @@ def lib(dtype=np.float32):
         L.og_map_parts_to_grid.argtypes = [Dims, fp, I, LL, fp, ip, fp]
         L.og_map_mac_to_parts.argtypes = [Dims, fp, C.c_void_p, F, LL, fp, ip, fp, C.c_void_p, I]
         L.og_map_grid_to_parts.argtypes = [Dims, fp, I, LL, fp, ip, fp]
+        L.og_reset_outflow.argtypes = [Dims, ip, C.c_void_p, C.c_void_p]
+        L.og_reset_phi_in_obs.argtypes = [Dims, ip, fp]
         L.og_set_fractions.argtypes = [C.c_void_p, C.c_void_p]
         L.og_set_num_threads.argtypes = [I]
         L.og_get_num_threads.restype = I
@@ -174,6 +176,17 @@ def add_gravity(flags, vel, gravity, exclude=None, scale=True, dt=1.0):
 
 def extrapolate_mac_simple(flags, vel, distance=4, intoObs=False):
     lib(vel.dtype).og_extrapolate_mac_simple(dims(flags.shape), flags, vel, distance, int(intoObs))
+
+
+def reset_outflow(flags, phi=None, real=None, dtype=np.float32):
+    """resetOutflow (extforces.cpp:133-160) without particles, in place"""
+    lib(phi.dtype if phi is not None else (real.dtype if real is not None else dtype)).og_reset_outflow(
+        dims(flags.shape), flags, _ptr(phi), _ptr(real))
+
+
+def reset_phi_in_obs(flags, sdf):
+    """resetPhiInObs (advection.cpp:396-401), in place"""
+    lib(sdf.dtype).og_reset_phi_in_obs(dims(flags.shape), flags, sdf)
 
 
 def extrapolate_ls_simple(phi, distance=4, inside=False):
