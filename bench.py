@@ -623,6 +623,14 @@ def flip_form(m, n, ppc, reps, seed):
     t_g2p = timed(lambda: m.mapMACToParts(flags=flags, vel=vel, parts=pp, partVel=pvel))
     t_flip = timed(lambda: m.flipVelocityUpdate(flags=flags, vel=vel, velOld=velOld, parts=pp, partVel=pvel,
                                                 flipRatio=0.95))
+    # the same particles in a random order, as a long-running scene leaves
+    # them (particles move between cells; the reference never re-sorts them)
+    perm = rng.permutation(count)
+    pp.setPositions(pos[perm])
+    m.copyArrayToPdataVec3(pv[perm], pvel)
+    t_p2g_shuf = timed(lambda: m.mapPartsToMAC(flags=flags, vel=vel, velOld=velOld, parts=pp, partVel=pvel))
+    t_g2p_shuf = timed(lambda: m.mapMACToParts(flags=flags, vel=vel, parts=pp, partVel=pvel))
+    del perm
     f = flags.numpy()
     pflag = np.zeros(count, np.int32)
     v0, v1 = np.zeros(f.shape + (3,), np.float32), np.zeros(f.shape + (3,), np.float32)
@@ -633,6 +641,7 @@ def flip_form(m, n, ppc, reps, seed):
     og.map_mac_to_parts(f, v0, pos, pflag, pv)
     c_g2p = 1e3 * (time.perf_counter() - t0)
     out.update({"map_parts_to_mac_ms": t_p2g, "map_mac_to_parts_ms": t_g2p, "flip_velocity_update_ms": t_flip,
+                "shuffled_order": {"map_parts_to_mac_ms": t_p2g_shuf, "map_mac_to_parts_ms": t_g2p_shuf},
                 "map_parts_to_mac_particles_per_s": count / (t_p2g / 1e3),
                 "cpu_oracle": {"map_parts_to_mac_ms": c_p2g, "map_mac_to_parts_ms": c_g2p, "cores": 1,
                                "kind": "port", "sample": "one call each on the same particles, serial as the reference"},

@@ -263,6 +263,31 @@ __global__ void k_bucket_starts(const unsigned* __restrict__ keys, long long n, 
 namespace {
 
 // ----------------------------------------------------- particle -> grid
+// Positions and values copied into bucket order after a sort, so that the
+// faces' merges read them in sequence instead of gathering each particle
+// from its own index (every particle is read by up to 8 faces per sort).
+struct SortedParts {
+  const float* x;
+  const float* y;
+  const float* z;
+  const float* v[3];
+};
+__global__ void k_sorted_copy(long long n, const unsigned* __restrict__ sorted, PartView p, const float* __restrict__ v0,
+                              const float* __restrict__ v1, const float* __restrict__ v2, float* sx, float* sy,
+                              float* sz, float* s0, float* s1, float* s2) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned k = sorted[i];
+  sx[i] = p.x[k];
+  sy[i] = p.y[k];
+  sz[i] = p.z[k];
+  s0[i] = __ldg(v0 + k);
+  if (v1) {
+    s1[i] = __ldg(v1 + k);
+    s2[i] = __ldg(v2 + k);
+  }
+}
+
 // The weights setInterpol / setInterpolMAC give the stencil corner (dx, dy,
 // dz) of a particle: T[dy] * (S[dx] * F[dz]) (util/interpol.h:93-112,
 // 159-195), with the axis of MAC component comp shifted.
@@ -279,39 +304,6 @@ __device__ __forceinline__ CornerW corner_weights(const Dims& d, float px, float
     if (comp == 2) { c.F[0] = s.f0; c.F[1] = s.f1; }
   }
   return c;
-}
-
-
-// After a sort, every live particle's stencil weights (S0, S1, T0, T1, F0,
-// F1 for the component being splatted) and values are written in bucket
-// order, so that a face's merge reads each contribution's inputs in
-// sequence, and the weights, which up to 8 faces use, are formed once.
-struct SortedOut {
-  float* w[6];
-  float* v[3];
-};
-struct SortedParts {
-  const float* w[6];
-  const float* v[3];
-};
-__global__ void k_sorted_copy(long long n, const unsigned* __restrict__ sorted, Dims d, int comp, PartView p,
-                              const float* __restrict__ v0, const float* __restrict__ v1,
-                              const float* __restrict__ v2, SortedOut out) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const unsigned k = sorted[i];
-  const CornerW c = corner_weights(d, p.x[k], p.y[k], p.z[k], comp);
-  out.w[0][i] = c.S[0];
-  out.w[1][i] = c.S[1];
-  out.w[2][i] = c.T[0];
-  out.w[3][i] = c.T[1];
-  out.w[4][i] = c.F[0];
-  out.w[5][i] = c.F[1];
-  out.v[0][i] = __ldg(v0 + k);
-  if (v1) {
-    out.v[1][i] = __ldg(v1 + k);
-    out.v[2][i] = __ldg(v2 + k);
-  }
 }
 
 // One thread per face (comp >= 0, MAC component comp) or cell (comp -1):
@@ -365,9 +357,7 @@ __global__ void __launch_bounds__(256) k_p2g_gather(Dims d, int comp, SortedPart
 #pragma unroll
     for (int q = 1; q < 8; q++)
       if (q == bq) at = cur[q];
-    const CornerW c{{__ldg(sp.w[0] + at), __ldg(sp.w[1] + at)},
-                    {__ldg(sp.w[2] + at), __ldg(sp.w[3] + at)},
-                    {__ldg(sp.w[4] + at), __ldg(sp.w[5] + at)}};
+    const CornerW c = corner_weights(d, __ldg(sp.x + at), __ldg(sp.y + at), __ldg(sp.z + at), comp);
     const int dx = bq & 1, dy = (bq >> 1) & 1, dz = bq >> 2;
     const float a0 = __ldg(sp.v[0] + at);
     const float a1 = kComps == 3 ? __ldg(sp.v[1] + at) : 0.f;
@@ -476,7 +466,7 @@ struct mg_particles_s {
   // counts and their scan's block totals, bucket starts (ncells + 1)
   unsigned *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr};
   unsigned *hist = nullptr, *sums = nullptr, *starts = nullptr;
-  float* sorted[9] = {};  // stencil weights (6) and up to 3 values in bucket order
+  float* sorted[6] = {};  // positions and up to 3 values in bucket order
   void* stage = nullptr;  // 16 bytes per particle for record transfers
 };
 
@@ -563,18 +553,16 @@ const unsigned* sort_stencil(mg_particles p, int comp, const PartView& v) {
   return p->vals[a];
 }
 
-// the particles' stencil weights for component comp (-1: cell centred) and
-// their values (1 or 3 planes), in bucket order
-SortedParts sorted_copy(mg_particles p, const unsigned* sorted, int comp, const PartView& v, const float* v0,
-                        const float* v1, const float* v2) {
-  SortedOut o{{p->sorted[0], p->sorted[1], p->sorted[2], p->sorted[3], p->sorted[4], p->sorted[5]},
-              {p->sorted[6], p->sorted[7], p->sorted[8]}};
+// the live particles' positions and values (1 or 3 planes) in bucket order
+SortedParts sorted_copy(mg_particles p, const unsigned* sorted, const PartView& v, const float* v0, const float* v1,
+                        const float* v2) {
   const long long n = p->n;
   if (n > 0) {
     count_launch();
-    k_sorted_copy<<<blocks_of(n), 256, 0, p->st>>>(n, sorted, p->d, comp, v, v0, v1, v2, o);
+    k_sorted_copy<<<blocks_of(n), 256, 0, p->st>>>(n, sorted, v, v0, v1, v2, p->sorted[0], p->sorted[1],
+                                                    p->sorted[2], p->sorted[3], p->sorted[4], p->sorted[5]);
   }
-  SortedParts sp{{o.w[0], o.w[1], o.w[2], o.w[3], o.w[4], o.w[5]}, {o.v[0], o.v[1], o.v[2]}};
+  SortedParts sp{p->sorted[0], p->sorted[1], p->sorted[2], {p->sorted[3], p->sorted[4], p->sorted[5]}};
   return sp;
 }
 
@@ -631,7 +619,7 @@ extern "C" int mg_particles_create(mg_solver s, long long capacity, mg_particles
             cudaMalloc(&p->hist, histN * 4) == cudaSuccess &&
             cudaMalloc(&p->sums, ((histN + kRsTile - 1) / kRsTile) * 4) == cudaSuccess &&
             cudaMalloc(&p->starts, (p->d.n + 1) * 4) == cudaSuccess && cudaMalloc(&p->stage, c * 16) == cudaSuccess;
-  for (int q = 0; q < 9 && ok; q++) ok = cudaMalloc(&p->sorted[q], c * 4) == cudaSuccess;
+  for (int q = 0; q < 6 && ok; q++) ok = cudaMalloc(&p->sorted[q], c * 4) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     free_parts(p);
@@ -797,7 +785,7 @@ extern "C" int mg_map_parts_to_mac(mg_grid flags, mg_grid vel, mg_grid velOld, m
   const dim3 b(32, 8, 1);
   for (int c = 0; c < 3; c++) {
     const unsigned* sorted = sort_stencil(parts, c, pv);
-    const SortedParts sp = sorted_copy(parts, sorted, c, pv, partVel->c[c], nullptr, nullptr);
+    const SortedParts sp = sorted_copy(parts, sorted, pv, partVel->c[c], nullptr, nullptr);
     count_launch();
     k_p2g_gather<1><<<grid3(d, b), b, 0, parts->st>>>(d, c, sp, sorted, parts->starts, v + c * d.n, nullptr, nullptr,
                                                       vo + c * d.n, w ? w + c * d.n : nullptr);
@@ -819,7 +807,7 @@ extern "C" int mg_map_parts_to_grid(mg_grid flags, mg_grid target, mg_particles 
   const Dims& d = parts->d;
   const PartView pv = view_of(parts, nullptr, 0);
   const unsigned* sorted = sort_stencil(parts, -1, pv);
-  const SortedParts sp = sorted_copy(parts, sorted, -1, pv, source->c[0], vec ? source->c[1] : nullptr,
+  const SortedParts sp = sorted_copy(parts, sorted, pv, source->c[0], vec ? source->c[1] : nullptr,
                                      vec ? source->c[2] : nullptr);
   const dim3 b(32, 8, 1);
   count_launch();
