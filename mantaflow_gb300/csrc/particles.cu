@@ -294,15 +294,30 @@ __global__ void k_sorted_copy(long long n, const unsigned* __restrict__ sorted, 
 struct CornerW {
   float S[2], T[2], F[2];
 };
-__device__ __forceinline__ CornerW corner_weights(const Dims& d, float px, float py, float pz, int comp) {
-  const Wts w = build_index<false>(d, px, py, pz);
-  CornerW c{{w.s0, w.s1}, {w.t0, w.t1}, {w.f0, w.f1}};
-  if (comp >= 0) {
-    const Wts s = build_index<true>(d, px, py, pz);
-    if (comp == 0) { c.S[0] = s.s0; c.S[1] = s.s1; }
-    if (comp == 1) { c.T[0] = s.t0; c.T[1] = s.t1; }
-    if (comp == 2) { c.F[0] = s.f0; c.F[1] = s.f1; }
+// One axis of BUILD_INDEX / BUILD_INDEX_SHIFT: the weights of the lower and
+// upper sample for the coordinate q (already shifted by -0.5 or not), with
+// the border clamps (the upper one only where the axis has more than one
+// cell).  The same operations as build_index, one axis at a time, so a
+// component's weights take three axes instead of both full variants.
+__device__ __forceinline__ void axis_weights(float q, int n, bool clampHigh, float* w) {
+  const int i = (int)q;
+  float w1 = q - (float)i, w0 = 1.f - w1;
+  if (q < 0.f) {
+    w0 = 1.f;
+    w1 = 0.f;
   }
+  if (clampHigh && i >= n - 1) {
+    w0 = 0.f;
+    w1 = 1.f;
+  }
+  w[0] = w0;
+  w[1] = w1;
+}
+__device__ __forceinline__ CornerW corner_weights(const Dims& d, float px, float py, float pz, int comp) {
+  CornerW c;
+  axis_weights(comp == 0 ? px : px - 0.5f, d.nx, true, c.S);
+  axis_weights(comp == 1 ? py : py - 0.5f, d.ny, true, c.T);
+  axis_weights(comp == 2 ? pz : pz - 0.5f, d.nz, d.nz > 1, c.F);
   return c;
 }
 
