@@ -1,5 +1,6 @@
 // Host-side launcher declarations for the grid-step kernels.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -7,9 +8,23 @@
 
 namespace mgpu {
 
-// number of kernels this library has launched (the bench's gpu_launches)
-extern unsigned long long g_launches;
-inline void count_launch() { g_launches++; }
+// number of kernels this library has launched (the bench's gpu_launches),
+// and the calling thread's share (graph captures subtract what they
+// recorded, which runs only when the graph is launched)
+extern std::atomic<unsigned long long> g_launches;
+extern thread_local unsigned long long t_launches;
+inline void count_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  t_launches++;
+}
+// after a capture on this thread that began when t_launches was `before`:
+// the number of kernels captured, no longer counted as launched
+inline unsigned long long uncount_captured(unsigned long long before) {
+  const unsigned long long n = t_launches - before;
+  t_launches = before;
+  g_launches.fetch_sub(n, std::memory_order_relaxed);
+  return n;
+}
 
 // ---- advection (advect.cu)
 void launch_advect_sl(const Dims& d, int ch, CMac vel, const float* src, float* dst, float dt, int orderSpace,

@@ -23,7 +23,8 @@
 
 using namespace mgpu;
 
-unsigned long long mgpu::g_launches = 0;
+std::atomic<unsigned long long> mgpu::g_launches{0};
+thread_local unsigned long long mgpu::t_launches = 0;
 
 // upper bound on any single device-side wait in the MIC wavefronts (ns);
 // a wait that runs out flags an error instead of spinning on
@@ -1301,7 +1302,7 @@ static int mg_iteration_graph(mg_solver s, const PcgBuffers& b) {
     cudaGraphExecDestroy(s->iterGraph);
     s->iterGraph = nullptr;
   }
-  const unsigned long long before = g_launches;
+  const unsigned long long before = t_launches;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   launch_pcg_spmv(b, s->stream);
@@ -1309,8 +1310,7 @@ static int mg_iteration_graph(mg_solver s, const PcgBuffers& b) {
   const int e = mg_apply(s->mg, b, false, s->stream);
   launch_pcg_update(b, s->stream);
   const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
-  s->iterNodes = g_launches - before;
-  g_launches = before;
+  s->iterNodes = uncount_captured(before);
   if (e || ce != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
     return fail(MG_ERR_CUDA, std::string("capturing the multigrid iteration failed: ") + cudaGetErrorString(ce));
@@ -1473,7 +1473,7 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
   while (it < maxIter && !done) {
     if (graph) {
       CK(cudaGraphLaunch(s->iterGraph, s->stream));
-      g_launches += s->iterNodes;
+      g_launches.fetch_add(s->iterNodes, std::memory_order_relaxed);
       it++;
       if (it % lag == 0 || it == maxIter) {
         CK(cudaMemcpyAsync(s->scHost, s->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s->stream));
@@ -1915,6 +1915,6 @@ extern "C" int mg_elapsed(mg_solver s, int a, int b, float* ms) {
 
 extern "C" int mg_launch_count(long long* out) {
   if (!out) return fail(MG_ERR_ARG, "mg_launch_count: null out");
-  *out = (long long)g_launches;
+  *out = (long long)g_launches.load();
   return MG_OK;
 }
