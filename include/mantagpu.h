@@ -419,16 +419,12 @@ int mg_batch_tuning(mg_batch b, int* sweepRows, float* ms);
 int mg_batch_sync(mg_batch b);
 
 /* ---- served form (no counterpart in the reference) ----------------------- */
-/* A request loop for plume and dam-break jobs (the batched form's scenes,
- * run for a number of steps): jobs arrive at given times and are admitted
- * in arrival order once arrived and once their device memory
- * (mg_serve_job_bytes_kind) fits the budget.  Admitted jobs join one of
- * three size lanes (fewer than 64^3 cells, fewer than 100^3, larger); each
- * lane is a batched engine with its own CUDA stream and host thread, and
- * every tick of a lane advances all of its resident jobs by one step, so
- * small jobs do not wait for the largest job's solve.  A finished job leaves
- * and frees its memory for the next.  A job's results depend only on its
- * own scene: the same alone, in any mix and in any lane. */
+/* A request loop for plume jobs (the batched form's scene, run for a number
+ * of steps): jobs arrive at given times and are admitted in arrival order
+ * once arrived and once their device memory (mg_serve_job_bytes) fits the
+ * budget; every tick advances all resident jobs by one step in one batched
+ * step; a finished job leaves and frees its memory for the next.  A job's
+ * results depend only on its own scene: the same alone and in any mix. */
 typedef struct mg_server_s* mg_server;
 typedef struct {
   int jobs;

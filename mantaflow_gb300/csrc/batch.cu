@@ -31,7 +31,6 @@
 #include <cmath>
 #include <cstring>
 #include <map>
-#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -851,18 +850,8 @@ struct Job {
 };
 }  // namespace
 
-// Jobs are served in size lanes: each lane is a batched engine of its own,
-// with its own CUDA stream and host thread, so a lane of small jobs ticks
-// at its own pace instead of waiting every step for the largest job's
-// solve.  Admission stays global: in arrival order, against one budget.
-constexpr int kServeLanes = 3;
-static int serve_lane(const Job& j) {
-  const long long c = (long long)j.nx * j.ny * j.nz;
-  return c < 64LL * 64 * 64 ? 0 : (c < 100LL * 100 * 100 ? 1 : 2);
-}
-
 struct mg_server_s {
-  Engine lane[kServeLanes];
+  Engine e;
   size_t budget = 0;
   std::vector<Job> jobs;
   std::vector<float> tickMs;
@@ -877,12 +866,10 @@ extern "C" int mg_serve_create(size_t budgetBytes, float dt, mg_server* out) {
   if (!out || budgetBytes == 0) return set_error(MG_ERR_ARG, "mg_serve_create: invalid argument");
   auto s = new mg_server_s();
   s->budget = budgetBytes;
-  for (Engine& e : s->lane) {
-    const int st = engine_init(e, dt);
-    if (st) {
-      delete s;
-      return st;
-    }
+  const int st = engine_init(s->e, dt);
+  if (st) {
+    delete s;
+    return st;
   }
   *out = s;
   return MG_OK;
@@ -895,10 +882,8 @@ extern "C" int mg_serve_destroy(mg_server s) {
 
 extern "C" int mg_serve_set_solver(mg_server s, float cgAccuracy, float cgMaxIterFac) {
   if (!s || !(cgAccuracy > 0.f) || !(cgMaxIterFac > 0.f)) return set_error(MG_ERR_ARG, "mg_serve_set_solver: invalid argument");
-  for (Engine& e : s->lane) {
-    e.cgAccuracy = cgAccuracy;
-    e.cgMaxIterFac = cgMaxIterFac;
-  }
+  s->e.cgAccuracy = cgAccuracy;
+  s->e.cgMaxIterFac = cgMaxIterFac;
   return MG_OK;
 }
 
@@ -933,9 +918,8 @@ extern "C" int mg_serve_submit(mg_server s, int nx, int ny, int nz, const float*
 }
 
 // run until every submitted job has finished.  Arrival times are honoured
-// against the wall clock.  One host thread per lane: it takes the jobs the
-// shared admission assigned to its lane, steps its engine, and retires
-// finished jobs; an idle lane looks for work every millisecond.
+// against the wall clock: with nothing resident the loop waits for the next
+// arrival.
 extern "C" int mg_serve_run(mg_server s, mg_serve_stats* stats) {
   if (!s) return set_error(MG_ERR_ARG, "mg_serve_run: null server");
   using clk = std::chrono::steady_clock;
@@ -945,104 +929,61 @@ extern "C" int mg_serve_run(mg_server s, mg_serve_stats* stats) {
   for (size_t q = 0; q < s->jobs.size(); q++)
     if (s->jobs[q].finished < 0.) order.push_back((int)q);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return s->jobs[a].arrival < s->jobs[b].arrival; });
-  std::mutex mu;  // guards everything below and the server's statistics
-  size_t next = 0, finished = 0, live = 0;
-  std::vector<int> pending[kServeLanes];
-  int err = 0;
-  std::string errMsg;
-  // admission in arrival order while the next job has arrived and fits
-  auto admit = [&]() {
+  size_t next = 0, finished = 0;
+  std::vector<int> resident;
+  while (finished < order.size()) {
+    // admission in arrival order while the next job has arrived and fits
     const double tn = now();
     while (next < order.size()) {
       Job& j = s->jobs[order[next]];
       if (j.arrival > tn) break;
-      const size_t b = scene_bytes(j.nx, j.ny, j.nz, j.kind);
-      if (live + b > s->budget) break;
-      live += b;
+      if (s->e.liveBytes + scene_bytes(j.nx, j.ny, j.nz, j.kind) > s->budget) break;
+      SceneRec* r = nullptr;
+      const int st = scene_add(s->e, j.nx, j.ny, j.nz, j.gravity, j.seed, &r, j.kind);
+      if (st) return st;
+      j.rec = r;
       j.admitted = now();
-      pending[serve_lane(j)].push_back(order[next]);
+      resident.push_back(order[next]);
       next++;
     }
-    s->peakBytes = std::max(s->peakBytes, live);
-  };
-  auto fail = [&](int code) {
-    std::lock_guard<std::mutex> lk(mu);
-    if (!err) {
-      err = code;
-      errMsg = mg_last_error();
+    s->peakBytes = std::max(s->peakBytes, s->e.liveBytes);
+    if (resident.empty()) {
+      const double wait = s->jobs[order[next]].arrival - now();
+      if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
+      continue;
     }
-  };
-  auto lane_loop = [&](int L) {
-    Engine& e = s->lane[L];
-    std::vector<int> resident;
-    for (;;) {
-      std::vector<int> mine;
-      {
-        std::lock_guard<std::mutex> lk(mu);
-        if (err || finished == order.size()) return;
-        admit();
-        mine.swap(pending[L]);
-      }
-      for (int id : mine) {
-        Job& j = s->jobs[id];
-        SceneRec* r = nullptr;
-        const int st = scene_add(e, j.nx, j.ny, j.nz, j.gravity, j.seed, &r, j.kind);
-        if (st) return fail(st);
-        j.rec = r;
-        resident.push_back(id);
-      }
-      if (resident.empty()) {
-        std::this_thread::sleep_for(std::chrono::milliseconds(1));
+    const double ta = now();
+    const int st = engine_step(s->e, nullptr);
+    if (st) return st;
+    const double dtick = now() - ta;
+    s->tickMs.push_back((float)(1e3 * dtick));
+    s->tickJobs.push_back((int)resident.size());
+    std::vector<int> still;
+    for (int id : resident) {
+      Job& j = s->jobs[id];
+      j.stepsDone++;
+      j.stepMsSum += 1e3 * dtick;
+      s->cellSteps += (long long)j.nx * j.ny * j.nz;
+      if (j.stepsDone < j.steps) {
+        still.push_back(id);
         continue;
       }
-      const double ta = now();
-      const int st = engine_step(e, nullptr);
-      if (st) return fail(st);
-      const double dtick = now() - ta;
-      std::vector<int> still, done;
-      for (int id : resident) {
-        Job& j = s->jobs[id];
-        j.stepsDone++;
-        j.stepMsSum += 1e3 * dtick;
-        (j.stepsDone < j.steps ? still : done).push_back(id);
+      if (j.keep) {
+        const size_t n = (size_t)j.nx * j.ny * j.nz;
+        j.dens.resize(n);
+        j.pres.resize(n);
+        j.vel.resize(3 * n);
+        int e1 = scene_download(s->e, j.rec, MG_BATCH_DENSITY, j.dens.data(), n * sizeof(float));
+        if (!e1) e1 = scene_download(s->e, j.rec, MG_BATCH_PRESSURE, j.pres.data(), n * sizeof(float));
+        if (!e1) e1 = scene_download(s->e, j.rec, MG_BATCH_VELOCITY, j.vel.data(), 3 * n * sizeof(float));
+        if (e1) return e1;
       }
-      for (int id : done) {
-        Job& j = s->jobs[id];
-        if (j.keep) {
-          const size_t n = (size_t)j.nx * j.ny * j.nz;
-          j.dens.resize(n);
-          j.pres.resize(n);
-          j.vel.resize(3 * n);
-          int e1 = scene_download(e, j.rec, MG_BATCH_DENSITY, j.dens.data(), n * sizeof(float));
-          if (!e1) e1 = scene_download(e, j.rec, MG_BATCH_PRESSURE, j.pres.data(), n * sizeof(float));
-          if (!e1) e1 = scene_download(e, j.rec, MG_BATCH_VELOCITY, j.vel.data(), 3 * n * sizeof(float));
-          if (e1) return fail(e1);
-        }
-        scene_remove(e, j.rec);
-        j.rec = nullptr;
-      }
-      {
-        std::lock_guard<std::mutex> lk(mu);
-        s->tickMs.push_back((float)(1e3 * dtick));
-        s->tickJobs.push_back((int)resident.size());
-        for (int id : resident) s->cellSteps += (long long)s->jobs[id].nx * s->jobs[id].ny * s->jobs[id].nz;
-        for (int id : done) {
-          Job& j = s->jobs[id];
-          j.finished = now();
-          live -= scene_bytes(j.nx, j.ny, j.nz, j.kind);
-          finished++;
-        }
-      }
-      resident.swap(still);
+      scene_remove(s->e, j.rec);
+      j.rec = nullptr;
+      j.finished = now();
+      finished++;
     }
-  };
-  std::vector<std::thread> threads;
-  for (int L = 0; L < kServeLanes; L++) threads.emplace_back(lane_loop, L);
-  for (auto& t : threads) t.join();
-  if (err) {
-    // a lane that failed leaves its engine as it was; the server can be
-    // destroyed but not run again
-    return set_error(err, errMsg);
+    resident.swap(still);
   }
   s->wall = now();
   if (stats) {

@@ -112,3 +112,30 @@ def test_dam_break_job_alone_equals_in_mix_and_single_path():
     assert np.max(np.abs(want[1] - vel)) <= 1e-4
     assert np.max(np.abs(want[2] - pres)) <= 1e-4
     assert np.max(np.abs(vel)) > 1e-3  # the liquid moved
+
+
+def test_jobs_of_different_sizes():
+    """Small and large plume and dam-break jobs resident together: every
+    job's result equals its result alone, and admission keeps the arrival
+    order."""
+    jobs = [dict(size=(24, 28, 20), gravity=(0.0, -4e-3, 0.0), seed=11, steps=5),
+            dict(size=(70, 66, 72), gravity=(0.0, -3e-3, 0.0), seed=12, steps=3),
+            dict(size=(100, 104, 100), gravity=(0.0, -2e-3, 0.0), seed=13, steps=2, kind=mb.DAM_BREAK),
+            dict(size=(30, 30, 30), gravity=(0.0, -1e-3, 0.0), seed=14, steps=4, kind=mb.DAM_BREAK)]
+    want = []
+    for jb in jobs:
+        alone = mb.PlumeServer(budget_bytes=20 * 10 ** 9)
+        a = alone.submit(keep=True, **jb)
+        alone.run()
+        want.append(_result(alone, a))
+        alone.close()
+    mix = mb.PlumeServer(budget_bytes=20 * 10 ** 9)
+    ids = [mix.submit(arrival=0.001 * q, keep=True, **jb) for q, jb in enumerate(jobs)]
+    mix.run()
+    for q, w in zip(ids, want):
+        for a, b in zip(w, _result(mix, q)):
+            assert np.array_equal(a, b)
+    adm = [mix.job(q)["admitted"] for q in ids]
+    assert adm == sorted(adm)
+    assert [mix.job(q)["steps"] for q in ids] == [jb["steps"] for jb in jobs]
+    mix.close()
