@@ -179,7 +179,8 @@ int mg_set_open_bound(mg_grid flags, int bWidth, const char* openBound, int type
 int mg_reset_outflow(mg_grid flags, mg_grid phi, mg_grid real);
 
 /* ---- plugins: simple extrapolation (fastmarch.cpp) ----------------------- */
-/* extrapolateMACSimple (:337-375); phiObs must be NULL */
+/* extrapolateMACSimple (:337-375); phiObs (a levelset, may be NULL) adds
+ * knUnprojectNormalComp (:316-330) */
 int mg_extrapolate_mac_simple(mg_grid flags, mg_grid vel, int distance, mg_grid phiObs, int intoObs);
 /* extrapolateLsSimple (fastmarch.cpp:470-507): phi is a Real or Levelset grid */
 int mg_extrapolate_ls_simple(mg_grid phi, int distance, int inside);

@@ -172,6 +172,38 @@ __device__ __forceinline__ void extrap_into_bnd_cell(const Dims& d, const int* _
     vel.w[idx] = v2 / (float)cc;
   }
 }
+// knUnprojectNormalComp (fastmarch.cpp:316-330) with getNormal
+// (:298-314): in the band -maxDist <= phiObs <= 0, a velocity pointing
+// against the levelset's central-difference normal loses that component
+// (normalize as util/vectorbase.h:416-429).  Reads and writes only its own
+// cell's velocity; getNormal's clamps are no-ops on the inner cells.
+__global__ void k_unproject_normal(Dims d, const float* __restrict__ phi, Mac vel, float maxDist) {
+  CELL_IJK
+  if (!INNER) return;
+  const float p = phi[idx];
+  if (p > 0.f || p < -maxDist) return;
+  float nx = phi[idx + 1] - phi[idx - 1];
+  float ny = phi[idx + d.sy] - phi[idx - d.sy];
+  float nz = d.is3d ? phi[idx + d.sz] - phi[idx - d.sz] : p - p;
+  const float vx = vel.u[idx], vy = vel.v[idx], vz = vel.w[idx];
+  if (!(nx * vx + ny * vy + nz * vz < 0.f)) return;
+  const float l = nx * nx + ny * ny + nz * nz;
+  const float eps2 = 1e-6f * 1e-6f;
+  if (fabs((double)l - 1.) < (double)eps2) {
+  } else if (l > eps2) {
+    const float sc = (float)(1. / (double)sqrtf(l));
+    nx = nx * sc;
+    ny = ny * sc;
+    nz = nz * sc;
+  } else {
+    nx = ny = nz = 0.f;
+  }
+  const float dl = nx * vx + ny * vy + nz * vz;
+  vel.u[idx] = vx - nx * dl;
+  vel.v[idx] = vy - ny * dl;
+  vel.w[idx] = vz - nz * dl;
+}
+
 __global__ void k_extrap_into_bnd(Dims d, const int* __restrict__ flags, Mac vel, CMac vt) {
   CELL_IJK
   (void)idx;
@@ -461,13 +493,19 @@ void launch_add_force(const Dims& d, const int* flags, Mac vel, float fx, float 
   k_add_force<<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, fx, fy, fz, exclude);
 }
 void launch_extrapolate_mac_simple(const Dims& d, const int* flags, Mac vel, int* tmp, Mac snap, int distance, int intoObs,
-                                   cudaStream_t s) {
+                                   const float* phiObs, cudaStream_t s) {
   const int dim = d.is3d ? 3 : 2;
   for (int c = 0; c < dim; c++) {
     count_launch();
     k_extrap_mark<<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, tmp, c, intoObs);
+    for (int l = 1; l < 1 + distance; l++) {
+      count_launch();
+      k_extrap_layer<<<grid3(d, kBlk), kBlk, 0, s>>>(d, vel.c(c), tmp, l);
+    }
+  }
+  if (phiObs) {
     count_launch();
-    for (int l = 1; l < 1 + distance; l++) k_extrap_layer<<<grid3(d, kBlk), kBlk, 0, s>>>(d, vel.c(c), tmp, l);
+    k_unproject_normal<<<grid3(d, kBlk), kBlk, 0, s>>>(d, phiObs, vel, (float)distance);
   }
   cudaMemcpyAsync(snap.u, vel.u, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(snap.v, vel.v, sizeof(float) * d.n, cudaMemcpyDeviceToDevice, s);

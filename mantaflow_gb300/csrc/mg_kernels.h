@@ -47,7 +47,7 @@ void launch_add_buoyancy(const Dims& d, const int* flags, const float* rho, Mac 
 void launch_add_force(const Dims& d, const int* flags, Mac vel, float fx, float fy, float fz, const float* exclude,
                       cudaStream_t s);
 void launch_extrapolate_mac_simple(const Dims& d, const int* flags, Mac vel, int* tmp, Mac snap, int distance, int intoObs,
-                                   cudaStream_t s);
+                                   const float* phiObs, cudaStream_t s);
 // extrapolateLsSimple; tmp, mark: int scratch grids
 void launch_extrapolate_ls_simple(const Dims& d, float* phi, int* tmp, int* mark, int distance, int inside,
                                   cudaStream_t s);

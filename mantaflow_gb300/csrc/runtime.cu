@@ -1045,13 +1045,17 @@ extern "C" int mg_reset_outflow(mg_grid flags, mg_grid phi, mg_grid real) {
 extern "C" int mg_extrapolate_mac_simple(mg_grid flags, mg_grid vel, int distance, mg_grid phiObs, int intoObs) {
   NEED_GRID(flags, "extrapolateMACSimple");
   NEED_GRID(vel, "extrapolateMACSimple");
-  if (phiObs) return fail(MG_ERR_UNSUPPORTED, "extrapolateMACSimple: phiObs (knUnprojectNormalComp) is not supported");
   mg_solver s = flags->s;
+  if (phiObs) {
+    NEED_GRID(phiObs, "extrapolateMACSimple");
+    if (!is_real(phiObs) || phiObs->s != s) return fail(MG_ERR_ARG, "extrapolateMACSimple: phiObs must be a levelset of the same solver");
+  }
   Tmp tmp(s, sizeof(int) * (size_t)s->d.n);
   Tmp snap(s, vel->bytes());
   if (!tmp.p || !snap.p) return fail(MG_ERR_NOMEM, "extrapolateMACSimple: out of device memory");
   ProfScope ps(s, "extrapolate_mac_simple");
-  launch_extrapolate_mac_simple(s->d, flags->i(), vel->mac(), tmp.i(), snap.mac(), distance, intoObs, s->stream);
+  launch_extrapolate_mac_simple(s->d, flags->i(), vel->mac(), tmp.i(), snap.mac(), distance, intoObs,
+                                phiObs ? phiObs->f() : nullptr, s->stream);
   CKL();
   return MG_OK;
 }

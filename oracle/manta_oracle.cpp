@@ -736,7 +736,48 @@ void og_add_gravity(og_dims d, const int* flags, og_real* vel, og_real gx, og_re
 /* extrapolateMACSimple (fastmarch.cpp:337-375) with knExtrapolateMACSimple
  * (:230-258, in place: a cell reads neighbours of layer d only, so the
  * in-place update is order independent) and knExtrapolateIntoBnd (:260-300) */
-void og_extrapolate_mac_simple(og_dims d, const int* flags, og_real* vel, int distance, int intoObs) {
+/* knUnprojectNormalComp (fastmarch.cpp:316-330) with getNormal (:298-314)
+ * and normalize (util/vectorbase.h:416-429) */
+static void unproject_normal_comp(og_dims d, og_real* vel, const og_real* phi, og_real maxDist) {
+  for (int k = KLO(d, 1); k < KHI(d, 1); k++)
+    for (int j = 1; j < d.ny - 1; j++)
+      for (int i = 1; i < d.nx - 1; i++) {
+        const ll idx = IX(d, i, j, k);
+        if (phi[idx] > 0. || phi[idx] < -maxDist) continue;
+        int ii = i, jj = j, kk = k, kd = 1;
+        if (ii > d.nx - 2) ii = d.nx - 2;
+        if (ii < 1) ii = 1;
+        if (jj > d.ny - 2) jj = d.ny - 2;
+        if (jj < 1) jj = 1;
+        if (d.is3d) {
+          if (kk > d.nz - 2) kk = d.nz - 2;
+          if (kk < 1) kk = 1;
+        } else {
+          kd = 0;
+        }
+        og_real n[3] = {phi[IX(d, ii + 1, jj, kk)] - phi[IX(d, ii - 1, jj, kk)],
+                        phi[IX(d, ii, jj + 1, kk)] - phi[IX(d, ii, jj - 1, kk)],
+                        phi[IX(d, ii, jj, kk + kd)] - phi[IX(d, ii, jj, kk - kd)]};
+        og_real* v = vel + 3 * idx;
+        if (n[0] * v[0] + n[1] * v[1] + n[2] * v[2] < 0.) {
+          const og_real l = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+          const og_real eps2 = OG_R(OG_VEC_EPS) * OG_R(OG_VEC_EPS);
+          if (fabs(l - 1.) < eps2) {
+          } else if (l > eps2) {
+            const og_real norm = og_sqrt(l);
+            const og_real sc = (og_real)(1. / (double)norm);
+            for (int c = 0; c < 3; c++) n[c] *= sc;
+          } else {
+            n[0] = n[1] = n[2] = OG_R(0.);
+          }
+          const og_real dl = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
+          for (int c = 0; c < 3; c++) v[c] -= n[c] * dl;
+        }
+      }
+}
+
+void og_extrapolate_mac_simple(og_dims d, const int* flags, og_real* vel, int distance, const og_real* phiObs,
+                               int intoObs) {
   const ll n = NCELL(d);
   int* tmp = (int*)malloc(sizeof(int) * (size_t)n);
   const int dim = d.is3d ? 3 : 2;
@@ -773,6 +814,7 @@ void og_extrapolate_mac_simple(og_dims d, const int* flags, og_real* vel, int di
           }
     }
   }
+  if (phiObs) unproject_normal_comp(d, vel, phiObs, (og_real)distance);
   /* copy tangential values into the domain sides from a snapshot */
   og_real* vt = (og_real*)malloc(sizeof(og_real) * 3 * (size_t)n);
   memcpy(vt, vel, sizeof(og_real) * 3 * (size_t)n);

@@ -73,8 +73,9 @@ void og_add_buoyancy(og_dims d, const int* flags, const og_real* density, og_rea
 void og_add_gravity(og_dims d, const int* flags, og_real* vel, og_real gx, og_real gy, og_real gz,
                     const og_real* exclude, int scale, og_real dt);
 
-/* extrapolateMACSimple (fastmarch.cpp:337-375), phiObs unsupported (NULL). */
-void og_extrapolate_mac_simple(og_dims d, const int* flags, og_real* vel, int distance, int intoObs);
+/* extrapolateMACSimple (fastmarch.cpp:337-375); phiObs may be NULL */
+void og_extrapolate_mac_simple(og_dims d, const int* flags, og_real* vel, int distance, const og_real* phiObs,
+                               int intoObs);
 void og_extrapolate_ls_simple(og_dims d, og_real* phi, int distance, int inside);
 
 typedef struct {

@@ -85,7 +85,7 @@ def lib(dtype=np.float32):
         L.og_set_wall_bcs.argtypes = [Dims, ip, fp, C.c_void_p]
         L.og_add_buoyancy.argtypes = [Dims, ip, fp, fp, F, F, F, F, I, F]
         L.og_add_gravity.argtypes = [Dims, ip, fp, F, F, F, C.c_void_p, I, F]
-        L.og_extrapolate_mac_simple.argtypes = [Dims, ip, fp, I, I]
+        L.og_extrapolate_mac_simple.argtypes = [Dims, ip, fp, I, C.c_void_p, I]
         L.og_extrapolate_ls_simple.argtypes = [Dims, fp, I, I]
         L.og_mg_create.argtypes = [Dims]
         L.og_mg_create.restype = C.c_void_p
@@ -174,8 +174,8 @@ def add_gravity(flags, vel, gravity, exclude=None, scale=True, dt=1.0):
     lib(vel.dtype).og_add_gravity(dims(flags.shape), flags, vel, *map(float, gravity), _ptr(exclude), int(scale), dt)
 
 
-def extrapolate_mac_simple(flags, vel, distance=4, intoObs=False):
-    lib(vel.dtype).og_extrapolate_mac_simple(dims(flags.shape), flags, vel, distance, int(intoObs))
+def extrapolate_mac_simple(flags, vel, distance=4, intoObs=False, phiObs=None):
+    lib(vel.dtype).og_extrapolate_mac_simple(dims(flags.shape), flags, vel, distance, _ptr(phiObs), int(intoObs))
 
 
 def reset_outflow(flags, phi=None, real=None, dtype=np.float32):

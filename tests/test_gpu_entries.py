@@ -3,7 +3,8 @@ resetPhiInObs (advection.cpp:396-401), resetOutflow without particles
 (extforces.cpp:133-160), addGravity with an exclude grid and
 addGravityNoScale (extforces.cpp:45-69), and solvePressure's three parts
 computePressureRhs / solvePressureSystem / correctVelocity
-(pressure.cpp:277-476), which together must give solvePressure's result.
+(pressure.cpp:277-476), which together must give solvePressure's result,
+and extrapolateMACSimple with an obstacle levelset (fastmarch.cpp:316-375).
 """
 import numpy as np
 import pytest
@@ -148,3 +149,35 @@ def test_split_solve_equals_solve_pressure(pc, gf):
     assert abs(it_whole - it_ref) <= 1
     assert float(np.max(np.abs(pres2.numpy() - po))) <= 1e-4 * max(1.0, float(np.max(np.abs(po))))
     assert float(np.max(np.abs(vel2.numpy() - vo))) <= 1e-4
+
+
+@pytest.mark.parametrize("shape", [(24, 26, 28), (1, 44, 40)])
+@pytest.mark.parametrize("intoObs", [False, True])
+def test_extrapolate_mac_simple_with_phi_obs(shape, intoObs):
+    """extrapolateMACSimple with an obstacle levelset (fastmarch.cpp:337-375,
+    knUnprojectNormalComp :316-330): velocities inside the obstacle band
+    lose their component against the obstacle normal.  Against the oracle's
+    restatement (the golden set holds no phiObs case: oracle only)."""
+    nz, ny, nx = shape
+    f = np.zeros(shape, np.int32)
+    og.init_domain(f, 0)
+    og.fill_grid(f)
+    z, y, x = np.mgrid[0:nz, 0:ny, 0:nx].astype(np.float32) + 0.5
+    cz = nz / 2 if nz > 1 else 0.5
+    obs = (np.sqrt((x - 0.6 * nx) ** 2 + (y - 0.45 * ny) ** 2 + (z - cz) ** 2) - 0.22 * min(nx, ny)).astype(np.float32)
+    f[(obs < 0) & (f == og.FLUID)] = og.OBSTACLE
+    rng = np.random.default_rng(9)
+    f[(rng.random(shape) < 0.3) & (f == og.FLUID)] = og.EMPTY
+    v = (rng.random(shape + (3,), dtype=np.float32) - 0.5).astype(np.float32)
+    s = _solver(shape)
+    flags, vel, phi = s.create(m.FlagGrid), s.create(m.MACGrid), s.create(m.LevelsetGrid)
+    m.copyArrayToGridReal(f, flags)
+    m.copyArrayToGridReal(v, vel)
+    m.copyArrayToGridReal(obs, phi)
+    m.extrapolateMACSimple(flags=flags, vel=vel, distance=3, phiObs=phi, intoObs=intoObs)
+    want = v.copy()
+    og.extrapolate_mac_simple(f, want, 3, intoObs=intoObs, phiObs=obs)
+    assert np.array_equal(vel.numpy(), want)
+    plain = v.copy()
+    og.extrapolate_mac_simple(f, plain, 3, intoObs=intoObs)
+    assert np.any(plain != want)  # the obstacle band changed something
