@@ -277,7 +277,15 @@ struct Tmp {
 };
 
 static bool valid_solver(mg_solver s) { return s && g_ctx.solvers.count(s); }
-static bool valid_grid(mg_grid g) { return g && valid_solver(g->s) && g->s->grids.count(g); }
+// a grid handle is valid while one of the live solvers holds it; the test
+// never dereferences the handle, so a stale one (after mg_grid_destroy,
+// mg_solver_destroy or mg_shutdown) is refused, not read
+static bool valid_grid(mg_grid g) {
+  if (!g) return false;
+  for (mg_solver s : g_ctx.solvers)
+    if (s->grids.count(g)) return true;
+  return false;
+}
 
 bool mgpu::library_ready() { return g_ctx.init; }
 
