@@ -285,9 +285,10 @@ typedef struct {
 void mg_pressure_params_default(mg_pressure_params* p);
 /* solvePressure (:480-521).  phi, perCellCorr, fractions, obvel, curv,
  * retRhs may be NULL; out may be NULL.  With fractions (a MACGrid of face
- * fractions, MakeLaplaceMatrix's float form) the matrix is stored as floats
- * and MIC(0) runs plane by plane; fractions with PcMGStatic/PcMGDynamic or
- * with pressure fixing return MG_ERR_UNSUPPORTED. */
+ * fractions, MakeLaplaceMatrix's float form) the matrix is stored as floats,
+ * MIC(0) runs plane by plane, the multigrid preconditioners take the stored
+ * off-diagonals into their level 0, and pressure fixing zeroes the fixed
+ * cell's stored entries like fixPressure (:226-245). */
 int mg_solve_pressure(mg_grid vel, mg_grid pressure, mg_grid flags, const mg_pressure_params* p, mg_grid phi,
                       mg_grid perCellCorr, mg_grid fractions, mg_grid obvel, mg_grid curv, mg_grid retRhs,
                       mg_pressure_result* out);

@@ -8,7 +8,9 @@
 // (A0 count, fluid bit, -1 links) plus two bits: vertex active (A0 != 0) and
 // "trivial" (A0 == 1 without links, whose row and right-hand side are scaled
 // by 1e-6, multigrid.cpp:345-347, 377-382).  With ghost fluid the float
-// diagonal is kept beside it.  Coarse levels store their symmetric 27-point
+// diagonal is kept beside it, and with face fractions also the stored float
+// off-diagonals Ai, Aj, Ak (the links then say which entries to use; the
+// level-0 passes subtract A * x instead of adding x).  Coarse levels store their symmetric 27-point
 // (3D) / 9-point (2D) Galerkin stencils as 14 / 5 planes of n floats
 // (structure of arrays, so neighbouring threads read neighbouring words),
 // plus a byte of vertex type and x, b, r vectors.
@@ -88,7 +90,10 @@ struct Lev {
 struct Lev0 {
   Dims d;
   uint16_t* code;  // Poisson code | kMgActive | kMgTrivial
-  float* a0f;      // trivial-scaled float diagonal (ghost fluid) or null
+  float* a0f;      // trivial-scaled float diagonal (ghost fluid, fractions) or null
+  float* ai;       // with fractions: the stored off-diagonals Ai, Aj, Ak
+  float* aj;       // (entries of linked pairs; the code's links still say
+  float* ak;       // which pairs are linked); null: the Poisson -1 links
   float* r;        // residual
   float* xd;       // x after pre-smoothing: read (with halo) by the up pass
 };
@@ -124,6 +129,7 @@ __device__ __forceinline__ float l0_rhs(int c, const float* __restrict__ res, lo
 __device__ __forceinline__ float l0_entry(const Lev0& F, long long u, int sf) {
   const int c = F.code[u];
   if (sf == 0) return l0_diag(c, F.a0f, u);
+  if (F.ai) return (sf == 1 ? F.ai : (sf == 2 ? F.aj : F.ak))[u];
   const int bit = sf == 1 ? kHighX : (sf == 2 ? kHighY : kHighZ);
   return (c & bit) ? -1.f : 0.f;
 }
@@ -181,17 +187,32 @@ __device__ __forceinline__ Nb3 nb3(const Lev& L, int vx, int vy, int vz) {
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < (n); v += (long long)gridDim.x * blockDim.x)
 
 // ---------------------------------------------------------------- setup
-// knCopyA + knActivateVertices (multigrid.cpp:333-384)
-__global__ void k_mg_snapshot0(Dims d, const code_t* __restrict__ code, const float* __restrict__ A0f, uint16_t* code0,
-                               float* a0f0, int8_t* type0) {
+// knCopyA + knActivateVertices (multigrid.cpp:333-384).  With stored
+// off-diagonals (fractions) they are copied too, and an equation is trivial
+// when A0 == 1 and its six entries compare equal to zero (analyzeStencil,
+// :320-347): a linked pair whose face fraction is 0 has an entry of -0.
+__global__ void k_mg_snapshot0(Dims d, const code_t* __restrict__ code, const float* __restrict__ A0f,
+                               const float* __restrict__ Ai, const float* __restrict__ Aj,
+                               const float* __restrict__ Ak, uint16_t* code0, float* a0f0, float* ai0, float* aj0,
+                               float* ak0, int8_t* type0) {
   GRID_STRIDE(v, d.n) {
     int c = code[v] & 0x3ff;
     float a0 = A0f ? A0f[v] : (float)(c & 7);
+    if (Ai) {
+      ai0[v] = Ai[v];
+      aj0[v] = Aj[v];
+      ak0[v] = Ak[v];
+    }
     int8_t t = kVtInactive;
     if (a0 != 0.f) {
       t = kVtActive;
       c |= kMgActive;
-      const int links = c & (kLowX | kLowY | kLowZ | kHighX | kHighY | kHighZ);
+      bool links = (c & (kLowX | kLowY | kLowZ | kHighX | kHighY | kHighZ)) != 0;
+      if (Ai) {
+        const int i = (int)(v % d.nx), j = (int)((v / d.nx) % d.ny), k = d.is3d ? (int)(v / d.sz) : 0;
+        links = Ai[v] != 0.f || Aj[v] != 0.f || (d.is3d && Ak[v] != 0.f) || (i > 0 && Ai[v - 1] != 0.f) ||
+                (j > 0 && Aj[v - d.sy] != 0.f) || (d.is3d && k > 0 && Ak[v - d.sz] != 0.f);
+      }
       if (a0 == 1.f && !links) {
         t = kVtTrivial;
         c |= kMgTrivial;
@@ -769,10 +790,26 @@ __device__ __forceinline__ void stage0_a(Ring0& R, const Plane0& P, bool hasA0f,
   }
 }
 
-// the linked neighbours (kLow/kHigh order of the reference's sums) added
-template <bool IS3D>
-__device__ __forceinline__ float add_links0(const Ring0& R, int c, int q, int row, int lx, float sum) {
+// the linked neighbours' terms in the kLow/kHigh order of the reference's
+// sums (knSmoothColor, knCalcResidual: sum -= A * x[N]).  Poisson links
+// have A = -1, so the term is an exact addition; with fractions (FRAC) the
+// stored entries of cell g's pairs are read at L2 and the product
+// subtracted.  Unlinked pairs have zero entries and are left out.
+template <bool IS3D, bool FRAC>
+__device__ __forceinline__ float add_links0(const Ring0& R, const Lev0& F, long long g, int c, int q, int row, int lx,
+                                            float sum) {
   const int sl = ring0(q);
+  if (FRAC) {
+    if (c & kLowX) sum = sum - F.ai[g - 1] * R.x[sl][row][lx - 1];
+    if (c & kHighX) sum = sum - F.ai[g] * R.x[sl][row][lx + 1];
+    if (c & kLowY) sum = sum - F.aj[g - F.d.sy] * R.x[sl][row - 1][lx];
+    if (c & kHighY) sum = sum - F.aj[g] * R.x[sl][row + 1][lx];
+    if (IS3D) {
+      if (c & kLowZ) sum = sum - F.ak[g - F.d.sz] * R.x[ring0(q - 1)][row][lx];
+      if (c & kHighZ) sum = sum - F.ak[g] * R.x[ring0(q + 1)][row][lx];
+    }
+    return sum;
+  }
   if (c & kLowX) sum = sum + R.x[sl][row][lx - 1];
   if (c & kHighX) sum = sum + R.x[sl][row][lx + 1];
   if (c & kLowY) sum = sum + R.x[sl][row - 1][lx];
@@ -787,8 +824,8 @@ __device__ __forceinline__ float add_links0(const Ring0& R, int c, int q, int ro
 // stage B: colour 1 on plane q, region minus its outer ring (reads
 // colour-0 values only).  A region row holds 16 colour-1 cells: thread t
 // takes cell t & 15 of row 1 + (t >> 4), so no lane idles on colour 0.
-template <bool IS3D>
-__device__ __forceinline__ void stage0_b(Ring0& R, int ox, int oy, int q) {
+template <bool IS3D, bool FRAC>
+__device__ __forceinline__ void stage0_b(Ring0& R, const Lev0& F, int ox, int oy, int q) {
   const int t = threadIdx.x;
   if (t >= 16 * (kRY - 2)) return;
   const int row = 1 + (t >> 4);
@@ -797,13 +834,15 @@ __device__ __forceinline__ void stage0_b(Ring0& R, int ox, int oy, int q) {
   const int sl = ring0(q);
   const int c = R.code[sl][row][lx];
   if (!(c & kMgActive)) return;
-  R.x[sl][row][lx] = add_links0<IS3D>(R, c, q, row, lx, scaled_b(c, R.res[sl][row][lx])) / R.diag[sl][row][lx];
+  // an active cell lies inside the grid
+  const long long g = FRAC ? ix(F.d, ox + lx, oy + row, q) : 0;
+  R.x[sl][row][lx] = add_links0<IS3D, FRAC>(R, F, g, c, q, row, lx, scaled_b(c, R.res[sl][row][lx])) / R.diag[sl][row][lx];
 }
 
 // V-cycle entry on level 0: colour 0 from x = 0, colour 1, then the
 // residual (knSmoothColor x2 + knCalcResidual); writes x (to F.xd) and r of
 // the owned cells
-template <bool IS3D>
+template <bool IS3D, bool FRAC>
 __global__ void __launch_bounds__(kT0, 2) k_mg0_down(Lev0 F, const float* __restrict__ res, int zc, const CgScalars* sc) {
   if (sc->done) return;
   extern __shared__ __align__(16) unsigned char t0_smem[];
@@ -822,7 +861,7 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_down(Lev0 F, const float* __rest
     if (p < pend) load_plane0<false>(F, res, ox, oy, p + 1, P);
     __syncthreads();
     const int q = p - ZH;
-    if (q >= zb - ZH && q <= ze - 1 + ZH) stage0_b<IS3D>(R, ox, oy, q);
+    if (q >= zb - ZH && q <= ze - 1 + ZH) stage0_b<IS3D, FRAC>(R, F, ox, oy, q);
     __syncthreads();
     // stage C: residual and x of the owned cells of plane s
     const int s = p - 2 * ZH;
@@ -839,7 +878,7 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_down(Lev0 F, const float* __rest
         const float xv = R.x[sl][row][lx];
         F.xd[g] = xv;
         if (!(c & kMgActive)) continue;
-        float sum = add_links0<IS3D>(R, c, s, row, lx, scaled_b(c, R.res[sl][row][lx]));
+        float sum = add_links0<IS3D, FRAC>(R, F, g, c, s, row, lx, scaled_b(c, R.res[sl][row][lx]));
         sum = sum - R.diag[sl][row][lx] * xv;
         F.r[g] = sum;
       }
@@ -852,7 +891,7 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_down(Lev0 F, const float* __rest
 // sigmaNew = dot(x, residual) and beta like GridCg::iterate.  It reads x
 // from F.xd, halo included, and writes the result to x0: reading and writing
 // one array would race with the neighbouring CTAs' writes.
-template <bool IS3D, bool DOT>
+template <bool IS3D, bool DOT, bool FRAC>
 __global__ void __launch_bounds__(kT0, 2) k_mg0_up(Lev0 F, const float* __restrict__ res, int zc, float* x0, Lev C,
                                                    double* part, CgScalars* sc) {
   if (sc->done) return;
@@ -891,7 +930,7 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_up(Lev0 F, const float* __restri
     if (p < pend) load_plane0<true>(F, res, ox, oy, p + 1, P);
     __syncthreads();
     const int q = p - ZH;
-    if (q >= zb - ZH && q <= ze - 1 + ZH) stage0_b<IS3D>(R, ox, oy, q);
+    if (q >= zb - ZH && q <= ze - 1 + ZH) stage0_b<IS3D, FRAC>(R, F, ox, oy, q);
     if (even && cq < CX * CY) scx[(p / 2 + 1 + 8) & 1][cq / CX][cq % CX] = cnext;
     __syncthreads();
     // stage C: colour 0 of the owned cells of plane s (reads colour-1
@@ -909,7 +948,7 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_up(Lev0 F, const float* __restri
         const int c = R.code[sl][row][lx];
         float v = R.x[sl][row][lx];
         if (((gx + gy + s) & 1) == 0 && (c & kMgActive))
-          v = add_links0<IS3D>(R, c, s, row, lx, scaled_b(c, R.res[sl][row][lx])) / R.diag[sl][row][lx];
+          v = add_links0<IS3D, FRAC>(R, F, g, c, s, row, lx, scaled_b(c, R.res[sl][row][lx])) / R.diag[sl][row][lx];
         x0[g] = v;
         if (DOT) acc.add(v * R.res[sl][row][lx]);  // inactive cells: x = 0
       }
@@ -993,9 +1032,18 @@ __global__ void __launch_bounds__(kCgThreads) k_mg_coarse_cg(Lev L, Lev0 F, cons
         const Dims& d = F.d;
         const int lo[3] = {kLowX, kLowY, kLowZ}, hi[3] = {kHighX, kHighY, kHighZ};
         const long long st[3] = {1, d.sy, d.sz};
+        const float* st3[3] = {F.ai, F.aj, F.ak};  // stored entries (fractions) or null
         for (int q = 0; q < (IS3D ? 3 : 2); q++) {
-          if (c & lo[q]) { coef[nn * kCgThreads + v] = -1.f; nbr[nn * kCgThreads + v] = (short)(v - st[q]); nn++; }
-          if (c & hi[q]) { coef[nn * kCgThreads + v] = -1.f; nbr[nn * kCgThreads + v] = (short)(v + st[q]); nn++; }
+          if (c & lo[q]) {
+            coef[nn * kCgThreads + v] = F.ai ? st3[q][v - st[q]] : -1.f;
+            nbr[nn * kCgThreads + v] = (short)(v - st[q]);
+            nn++;
+          }
+          if (c & hi[q]) {
+            coef[nn * kCgThreads + v] = F.ai ? st3[q][v] : -1.f;
+            nbr[nn * kCgThreads + v] = (short)(v + st[q]);
+            nn++;
+          }
         }
         coef[nn * kCgThreads + v] = diag;
         nbr[nn * kCgThreads + v] = (short)v;
@@ -1436,12 +1484,19 @@ int ensure_paths() {
       cudaFuncSetAttribute(k_mg_coarse_cg<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
     return 1;
   const int r0 = (int)sizeof(Ring0);
-  if (cudaFuncSetAttribute(k_mg0_down<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_down<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_up<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_up<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_up<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess ||
-      cudaFuncSetAttribute(k_mg0_up<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, r0) != cudaSuccess)
+  const auto ring = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  if (cudaFuncSetAttribute(k_mg0_down<true, false>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_down<false, false>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_down<true, true>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_down<false, true>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<true, true, false>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<true, false, false>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<false, true, false>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<false, false, false>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<true, true, true>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<true, false, true>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<false, true, true>, ring, r0) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg0_up<false, false, true>, ring, r0) != cudaSuccess)
     return 1;
   // the cluster V-cycle tail: 16 CTAs where the GPU can co-schedule them
   g_tailCta = 0;
@@ -1571,7 +1626,8 @@ struct MgHierarchy {
   bool selValid = false;
   bool isASet = false;
   unsigned long long gen = 0;  // bumped by every rebuild
-  bool useA0f = false;  // the snapshot has a float diagonal (ghost fluid)
+  bool useA0f = false;  // the snapshot has a float diagonal (ghost fluid, fractions)
+  bool useFrac = false;  // the snapshot has stored off-diagonals (fractions)
   MgProfHook hook = nullptr;
   void* hookCtx = nullptr;
   float coarseAcc = 1e-8f;
@@ -1629,6 +1685,7 @@ MgHierarchy* mg_hierarchy_create(const Dims& d) {
   h->l0.d = d;
   h->l0.code = h->alloc<uint16_t>(n0);
   h->l0.a0f = nullptr;
+  h->l0.ai = h->l0.aj = h->l0.ak = nullptr;
   h->l0.r = L > 1 ? h->alloc<float>(n0) : nullptr;
   h->l0.xd = L > 1 ? h->alloc<float>(n0) : nullptr;
   h->type0 = h->alloc<int8_t>(n0);
@@ -1701,7 +1758,8 @@ unsigned long long mg_hierarchy_signature(const MgHierarchy* h) {
   if (!h) return 0;
   unsigned int acc;
   std::memcpy(&acc, &h->coarseAcc, sizeof acc);
-  return (h->gen << 34) ^ ((unsigned long long)h->useA0f << 33) ^ (unsigned long long)acc;
+  return (h->gen << 35) ^ ((unsigned long long)h->useFrac << 34) ^ ((unsigned long long)h->useA0f << 33) ^
+         (unsigned long long)acc;
 }
 int mg_hierarchy_levels(const MgHierarchy* h) { return h ? h->nlev : 0; }
 void mg_hierarchy_describe(const MgHierarchy* h, MgLayout* out) {
@@ -1725,6 +1783,12 @@ int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStre
     h->l0.a0f = h->alloc<float>(d.n);
     if (!h->ok) return 1;
   }
+  if (b.Aif && !h->l0.ai) {
+    h->l0.ai = h->alloc<float>(d.n);
+    h->l0.aj = h->alloc<float>(d.n);
+    h->l0.ak = h->alloc<float>(d.n);
+    if (!h->ok) return 1;
+  }
   // inactive vertices keep zero x, b, r and matrix rows: the V-cycle
   // kernels rely on it instead of testing vertex types
   if (h->l0.r && cudaMemsetAsync(h->l0.r, 0, sizeof(float) * (size_t)d.n, s) != cudaSuccess) return 1;
@@ -1737,12 +1801,16 @@ int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStre
       return 1;
   }
   float* a0f = b.A0f ? h->l0.a0f : nullptr;
+  const bool frac = b.Aif != nullptr;
   Lev0 l0 = h->l0;
   l0.a0f = a0f;
+  if (!frac) l0.ai = l0.aj = l0.ak = nullptr;
   count_launch();
-  k_mg_snapshot0<<<blocks_for(d.n), kThreads1, 0, s>>>(d, b.code, b.A0f, h->l0.code, a0f, h->type0);
+  k_mg_snapshot0<<<blocks_for(d.n), kThreads1, 0, s>>>(d, b.code, b.A0f, b.Aif, b.Ajf, b.Akf, h->l0.code, a0f, l0.ai,
+                                                        l0.aj, l0.ak, h->type0);
   if (cudaGetLastError() != cudaSuccess) return 1;
   h->useA0f = a0f != nullptr;
+  h->useFrac = frac;
   if (h->nlev > 1) {
     // vertex selection on the host, reused while the level-0 types repeat
     h->htype[0].resize((size_t)d.n);
@@ -1852,6 +1920,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   const int S = h->S;
   Lev0 l0 = h->l0;
   if (!h->useA0f) l0.a0f = nullptr;
+  if (!h->useFrac) l0.ai = l0.aj = l0.ak = nullptr;
+  const bool frac = h->useFrac;
   const CgScalars* sc = b.sc;
   float* x0 = b.tmp;
   const float* res = b.residual;
@@ -1888,8 +1958,13 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
     {
       Fam f(h, "mg_down_l0");
       count_launch();
-      if (h->is3d) k_mg0_down<true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, sc);
-      else k_mg0_down<false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, sc);
+      if (frac) {
+        if (h->is3d) k_mg0_down<true, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, sc);
+        else k_mg0_down<false, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, sc);
+      } else {
+        if (h->is3d) k_mg0_down<true, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, sc);
+        else k_mg0_down<false, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, sc);
+      }
     }
     {
       Fam f(h, "mg_restrict_l0");
@@ -1953,12 +2028,23 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
     {
       Fam f(h, "mg_up_l0");
       count_launch();
-      if (h->is3d) {
-        if (init) k_mg0_up<true, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
-        else k_mg0_up<true, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
+      const Lev& v1 = h->lev[1];
+      if (frac) {
+        if (h->is3d) {
+          if (init) k_mg0_up<true, false, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, v1, b.part, b.sc);
+          else k_mg0_up<true, true, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, v1, b.part, b.sc);
+        } else {
+          if (init) k_mg0_up<false, false, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, v1, b.part, b.sc);
+          else k_mg0_up<false, true, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, v1, b.part, b.sc);
+        }
       } else {
-        if (init) k_mg0_up<false, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
-        else k_mg0_up<false, true><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, h->lev[1], b.part, b.sc);
+        if (h->is3d) {
+          if (init) k_mg0_up<true, false, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, v1, b.part, b.sc);
+          else k_mg0_up<true, true, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, v1, b.part, b.sc);
+        } else {
+          if (init) k_mg0_up<false, false, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, v1, b.part, b.sc);
+          else k_mg0_up<false, true, false><<<gt, kT0, sizeof(Ring0), s>>>(l0, res, zc, x0, v1, b.part, b.sc);
+        }
       }
     }
   }

@@ -249,11 +249,18 @@ __global__ void k_count_empty(long long n, const int* __restrict__ flags, int* o
 
 // fixPressure(fixPidx, 0, ...) (pressure.cpp:226-245): the rhs updates of
 // the neighbours subtract A*0 and leave them unchanged.
-__global__ void k_fix_pressure(Dims d, long long f, code_t* code, float* A0f, float* rhs) {
+__global__ void k_fix_pressure(Dims d, long long f, code_t* code, float* A0f, float* Ai, float* Aj, float* Ak,
+                               float* rhs) {
   if (threadIdx.x != 0) return;
   rhs[f] = 0.f;
   code[f] = (code_t)((code[f] & kCodeFluid) | 1);
   if (A0f) A0f[f] = 1.f;
+  if (Ai) {  // the stored matrix (fractions): the row's and the column's entries
+    Ai[f] = Aj[f] = Ak[f] = 0.f;
+    Ai[f - 1] = 0.f;
+    Aj[f - d.sy] = 0.f;
+    if (d.is3d) Ak[f - d.sz] = 0.f;
+  }
   code[f - 1] &= (code_t)~kHighX;
   code[f + 1] &= (code_t)~kLowX;
   code[f - d.sy] &= (code_t)~kHighY;
@@ -1315,7 +1322,7 @@ void launch_count_empty(const PcgBuffers& b, int* out, cudaStream_t s) {
 }
 void launch_fix_pressure(const PcgBuffers& b, long long fix, cudaStream_t s) {
   count_launch();
-  k_fix_pressure<<<1, 32, 0, s>>>(b.d, fix, b.code, b.A0f, b.rhs);
+  k_fix_pressure<<<1, 32, 0, s>>>(b.d, fix, b.code, b.A0f, b.Aif, b.Ajf, b.Akf, b.rhs);
 }
 void launch_pcg_init(const PcgBuffers& b, cudaStream_t s) {
   count_launch();

@@ -1358,10 +1358,6 @@ extern "C" int mg_solve_pressure_system(mg_grid rhs, mg_grid vel, mg_grid pressu
     return fail(MG_ERR_SOLVER, "GridCg<APPLYMAT>::setICPreconditioner: Invalid method specified.");
   if (preconditioner < 0 || preconditioner > MG_PC_MG_STATIC)
     return fail(MG_ERR_ARG, "solvePressureSystem: unknown preconditioner");
-  if (fractions && (preconditioner == MG_PC_MG_STATIC || preconditioner == MG_PC_MG_DYNAMIC))
-    return fail(MG_ERR_UNSUPPORTED, "solvePressureSystem: fractions with the multigrid preconditioner are not supported");
-  if (fractions && (p->zeroPressureFixing || p->cgAccuracy < 1e-07))
-    return fail(MG_ERR_UNSUPPORTED, "solvePressureSystem: fractions with pressure fixing are not supported");
   int st = ensure_cg_state(s);
   if (st) return st;
   PcgBuffers b = cg_buffers(s, flags, rhs->f(), pressure);
