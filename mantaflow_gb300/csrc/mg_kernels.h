@@ -200,8 +200,8 @@ int mic_flow_prepare(int* ctasPerSm);
 size_t mic_flow_face_words(int ntiles);
 void launch_mic_flow(const PcgBuffers& b, const MicPlan& m, unsigned long long* face, int mode, unsigned int epoch,
                      long long spinLimit, cudaStream_t s, bool stall = false);
-// once per device: the streamed SpMV's shared-memory size (MANTAGPU_SPMV=quad
-// selects the per-quad gather kernel instead)
+// once per device: the z-marching SpMV's resident CTAs and the streamed
+// SpMV's shared-memory size (MANTAGPU_SPMV selects the kernel per launch)
 int pcg_prepare(int sms);
 // sum of nparts per-block dot partials -> beta/sigma (init: sigma only)
 void launch_mic_finish(const PcgBuffers& b, int nparts, bool init, cudaStream_t s);

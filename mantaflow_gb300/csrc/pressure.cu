@@ -518,6 +518,125 @@ __global__ void __launch_bounds__(256, 4) k_pcg_spmv4(Dims d, const code_t* __re
   }
 }
 
+// ---- the same SpMV marching along z in registers.  A thread owns one quad
+// of one row and walks a run of zc planes; x of the planes below, at and
+// above the quad rotate through registers, so every plane of x and of the
+// codes is read from memory once per run.  While plane z is computed, the
+// loads of plane z+1 (codes, the neighbouring rows' quads, the end cells' x
+// neighbours) and x of plane z+2 are in flight.  The neighbouring rows are
+// the quads of other threads of the CTA (L1) or of the next CTA (L2); their
+// addresses are clamped into the grid so the loads need no test, and a
+// clamped value is only read when the code has the link, which implies the
+// neighbour exists.  Same cell arithmetic as k_pcg_spmv4; 0.63 of the
+// measured copy peak in the plume step at 256^3 against 0.54 for the
+// plane-streamed kernel below, which keeps two CTAs per SM.
+struct ZmGeom {
+  int nq, TY, zc;  // quads per row, rows per CTA, planes per CTA
+};
+
+// spmv_apply without branches: a non-fluid cell (code 0: no diagonal, no
+// links) gives x * 1 = x, the reference's copy; a fluid cell x * A0 minus
+// its linked neighbours in the reference's order.
+__device__ __forceinline__ float4 spmv_apply_sel(const SpmvQuad& Q, FSum& acc) {
+  const unsigned c[4] = {Q.cw.x & 0xffffu, Q.cw.x >> 16, Q.cw.y & 0xffffu, Q.cw.y >> 16};
+  float out[4];
+#pragma unroll
+  for (int e = 0; e < 4; e++) {
+    const unsigned ce = c[e];
+    const float xv = fget(Q.xc, e);
+    float v = xv * ((ce & kCodeFluid) ? fget(Q.A0, e) : 1.f);
+    if (ce & kLowX) v = v - (e == 0 ? Q.xl : fget(Q.xc, e - 1));
+    if (ce & kHighX) v = v - (e == 3 ? Q.xr : fget(Q.xc, e + 1));
+    if (ce & kLowY) v = v - fget(Q.ylo, e);
+    if (ce & kHighY) v = v - fget(Q.yhi, e);
+    if (ce & kLowZ) v = v - fget(Q.zlo, e);
+    if (ce & kHighZ) v = v - fget(Q.zhi, e);
+    out[e] = v;
+    acc.add(v * xv);
+  }
+  return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+__global__ void __launch_bounds__(256, 4) k_pcg_spmv_zm(Dims d, ZmGeom g, const code_t* __restrict__ code,
+                                                      const float* __restrict__ A0f, const float* __restrict__ x,
+                                                      float* y, double* part, CgScalars* sc) {
+  if (sc->done) return;
+  FSum acc;
+  const int r = threadIdx.x / g.nq, xq = threadIdx.x - r * g.nq;
+  const int row = blockIdx.x * g.TY + r;
+  const int zs = blockIdx.y * g.zc, ze = min(zs + g.zc, d.nz);
+  if (r < g.TY && row < d.ny) {
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int pq = (int)(d.sz >> 2);  // quads per plane; grids hold < 2^31 cells
+    const int dn = row > 0 ? g.nq : 0, up = row + 1 < d.ny ? g.nq : 0;
+    const int nlast = (int)d.n - 1;
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    const uint2* c2 = reinterpret_cast<const uint2*>(code);
+    const float4* A4 = reinterpret_cast<const float4*>(A0f);
+    float4* y4 = reinterpret_cast<float4*>(y);
+    int q = zs * pq + row * g.nq + xq;
+    // x below, at and above plane z (and x of plane z+2 in flight), the
+    // codes and the neighbour rows / end cells of plane z
+    float4 cm = zs > 0 ? __ldg(x4 + q - pq) : z4;
+    float4 cc = __ldg(x4 + q);
+    float4 cp = zs + 1 < d.nz ? __ldg(x4 + q + pq) : z4;
+    uint2 cw = __ldg(c2 + q);
+    float4 ylo = __ldg(x4 + q - dn), yhi = __ldg(x4 + q + up);
+    float xl = __ldg(x + max(4 * q - 1, 0)), xr = __ldg(x + min(4 * q + 4, nlast));
+#pragma unroll 2
+    for (int z = zs; z < ze; z++) {
+      const bool more = z + 1 < ze;
+      const int qn = q + pq;
+      float4 cn = z4, nylo = ylo, nyhi = yhi;
+      uint2 ncw = cw;
+      float nxl = xl, nxr = xr;
+      if (more) {
+        ncw = __ldg(c2 + qn);
+        nylo = __ldg(x4 + qn - dn);
+        nyhi = __ldg(x4 + qn + up);
+        nxl = __ldg(x + (4 * qn - 1));  // qn >= pq > 0
+        nxr = __ldg(x + min(4 * qn + 4, nlast));
+        if (z + 2 < d.nz) cn = __ldg(x4 + qn + pq);
+      }
+      SpmvQuad Q;
+      Q.cw = cw;
+      Q.xc = cc;
+      Q.ylo = ylo;
+      Q.yhi = yhi;
+      Q.zlo = cm;
+      Q.zhi = cp;
+      Q.xl = xl;
+      Q.xr = xr;
+      if (A0f) Q.A0 = __ldg(A4 + q);
+      else
+        Q.A0 = make_float4((float)(cw.x & 7u), (float)((cw.x >> 16) & 7u), (float)(cw.y & 7u), (float)((cw.y >> 16) & 7u));
+      y4[q] = spmv_apply_sel(Q, acc);
+      cm = cc;
+      cc = cp;
+      cp = cn;
+      cw = ncw;
+      ylo = nylo;
+      yhi = nyhi;
+      xl = nxl;
+      xr = nxr;
+      q = qn;
+    }
+  }
+  const double b = block_sum(acc.value());
+  const unsigned nb = gridDim.x * gridDim.y;
+  if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = b;
+  if (last_block(&sc->counters[1], nb)) {
+    const double s2 = sum_partials(part, (int)nb);
+    if (threadIdx.x == 0) {
+      const float dp = (float)s2;
+      sc->dp = dp;
+      float alpha = 0.f;
+      if (fabsf(dp) > 0.f) alpha = sc->sigma / dp;
+      sc->alpha = alpha;
+    }
+  }
+}
+
 // ---- the same SpMV streamed plane by plane through shared memory.  A CTA
 // owns a slab of TY full-width rows and a run of z planes, and keeps a ring
 // of kStreamSlots planes in shared memory.  One producer warp fills the ring
@@ -703,13 +822,44 @@ static bool stream_geom(const Dims& d, int maxBlocks, int sms, StreamGeom* g, di
   return true;
 }
 
+// Quads per row, rows per CTA and the z run for the z-marching SpMV, or
+// false where it does not apply (2D, rows not a multiple of 4 cells or
+// longer than 1024 cells, more CTAs than the solver keeps partials for).
+// The z runs are cut so that one wave of CTAs covers the grid.
+static bool zm_geom(const Dims& d, int maxBlocks, int slots, ZmGeom* g, dim3* grid) {
+  if (!d.is3d || (d.nx & 3) != 0 || d.nx / 4 > 256) return false;
+  g->nq = d.nx / 4;
+  g->TY = std::max(1, 256 / g->nq);
+  const int rowsB = (d.ny + g->TY - 1) / g->TY;
+  const int target = std::max(1, std::min(maxBlocks, slots));
+  int chunks = std::max(1, std::min(std::max(1, d.nz / 4), target / rowsB));
+  g->zc = (d.nz + chunks - 1) / chunks;
+  chunks = (d.nz + g->zc - 1) / g->zc;
+  if (rowsB * chunks > maxBlocks || rowsB > 65535) return false;
+  *grid = dim3((unsigned)rowsB, (unsigned)chunks, 1);
+  return true;
+}
+
 static int g_sms = 0;
-static bool g_spmvStream = true;
+enum { kSpmvQuad = 0, kSpmvStream = 1, kSpmvZm = 2 };
+static int g_zmSlots = 0;  // resident CTAs of k_pcg_spmv_zm on the whole GPU
+
+// the PCG matrix-vector kernel: z-marching in registers by default;
+// MANTAGPU_SPMV=stream selects the plane-streamed one (shared-memory ring
+// filled by bulk asynchronous copies), =quad the grid-stride quad kernel.
+// Read at every launch, so a process can switch between solves.
+static int spmv_mode() {
+  const char* e = getenv("MANTAGPU_SPMV");
+  if (e && std::string(e) == "quad") return kSpmvQuad;
+  if (e && std::string(e) == "stream") return kSpmvStream;
+  return kSpmvZm;
+}
 
 int pcg_prepare(int sms) {
   g_sms = sms;
-  const char* e = getenv("MANTAGPU_SPMV");
-  g_spmvStream = !(e && std::string(e) == "quad");
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_spmv_zm, 256, 0) != cudaSuccess || per < 1) per = 1;
+  g_zmSlots = per * sms;
   const size_t smem = (size_t)kStreamSlots * kStreamSlotBudget;
   return cudaFuncSetAttribute(k_pcg_spmv_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess
              ? 0
@@ -1346,8 +1496,14 @@ void launch_pcg_spmv(const PcgBuffers& b, cudaStream_t s) {
     return;
   }
   StreamGeom g;
+  ZmGeom zg;
   dim3 grid;
-  if (g_spmvStream && stream_geom(b.d, 2 * b.nblocks, g_sms, &g, &grid)) {
+  const int mode = spmv_mode();
+  if (mode == kSpmvZm && zm_geom(b.d, 2 * b.nblocks, g_zmSlots, &zg, &grid)) {
+    k_pcg_spmv_zm<<<grid, 256, 0, s>>>(b.d, zg, b.code, b.A0f, b.search, b.tmp, b.part, b.sc);
+    return;
+  }
+  if (mode != kSpmvQuad && stream_geom(b.d, 2 * b.nblocks, g_sms, &g, &grid)) {
     k_pcg_spmv_stream<<<grid, kStreamConsumers + 32, (size_t)kStreamSlots * g.slotBytes, s>>>(
         b.d, g, b.code, b.A0f, b.search, b.tmp, b.part, b.sc);
     return;
