@@ -11,6 +11,7 @@
 #include "mg_kernels.h"
 #include "mg_batch.h"
 
+#include <algorithm>
 #include <cfloat>
 
 namespace mgpu {
@@ -435,6 +436,32 @@ __global__ void k_outflow_bc(Dims d, const int* __restrict__ flags, CMac vel, CM
   outflow_bc_cell(d, flags, vel, velPrev, velDst, timeStep, i, j, k);
 }
 
+// The same over four consecutive cells per thread: outflow cells are a
+// boundary layer, so nearly every thread only reads its four flags (one
+// 16-byte load) and returns.  n is a multiple of 4 (checked by the caller).
+template <bool COPY>
+__global__ void k_outflow_q(Dims d, const int* __restrict__ flags, CMac vel, CMac velPrev, Mac velDst, float timeStep) {
+  const long long nq = d.n >> 2;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
+    const int4 f4 = __ldg(reinterpret_cast<const int4*>(flags) + q);
+    if (!((f4.x | f4.y | f4.z | f4.w) & kOutflow)) continue;
+    const int fl[4] = {f4.x, f4.y, f4.z, f4.w};
+#pragma unroll 1
+    for (int e = 0; e < 4; e++) {
+      if (!(fl[e] & kOutflow)) continue;
+      const long long idx = 4 * q + e;
+      const int i = (int)(idx % d.nx), j = (int)((idx / d.nx) % d.ny), k = (int)(idx / ((long long)d.nx * d.ny));
+      if (COPY) {
+        velDst.u[idx] = vel.u[idx];
+        velDst.v[idx] = vel.v[idx];
+        velDst.w[idx] = vel.w[idx];
+      } else {
+        outflow_bc_cell(d, flags, vel, velPrev, velDst, timeStep, i, j, k);
+      }
+    }
+  }
+}
+
 // copyChangedVels (advection.cpp:384)
 __device__ __forceinline__ void copy_outflow_cell(const Dims& d, const int* __restrict__ flags, CMac src, Mac dst, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
@@ -607,6 +634,15 @@ void launch_advect_maccormack_mac(const Dims& d, const int* flags, CMac vel, CMa
 
 void launch_outflow_bc(const Dims& d, const int* flags, CMac vel, CMac velPrev, Mac velDst, Mac velOut, float timeStep,
                        cudaStream_t s) {
+  if ((d.n & 3) == 0) {
+    const unsigned nb = (unsigned)std::min<long long>((d.n / 4 + 255) / 256, 4096);
+    count_launch();
+    k_outflow_q<false><<<nb, 256, 0, s>>>(d, flags, vel, velPrev, velDst, timeStep);
+    count_launch();
+    k_outflow_q<true><<<nb, 256, 0, s>>>(d, flags, CMac{velDst.u, velDst.v, velDst.w}, CMac{nullptr, nullptr, nullptr},
+                                         velOut, timeStep);
+    return;
+  }
   count_launch();
   k_outflow_bc<<<grid3(d, kBlk), kBlk, 0, s>>>(d, flags, vel, velPrev, velDst, timeStep);
   count_launch();

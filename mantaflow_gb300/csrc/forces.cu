@@ -4,6 +4,7 @@
 #include "mg_kernels.h"
 #include "mg_batch.h"
 
+#include <algorithm>
 #include <cfloat>
 
 namespace mgpu {
@@ -19,34 +20,43 @@ static const dim3 kBlk(32, 8, 1);
 
 #define INNER (i >= 1 && i < d.nx - 1 && j >= 1 && j < d.ny - 1 && (!d.is3d || (k >= 1 && k < d.nz - 1)))
 
-// KnSetWallBcs (extforces.cpp:186-217): every cell, i>0 style checks
+// KnSetWallBcs (extforces.cpp:186-217): every cell, i>0 style checks.
+// Every load is issued first (neighbour addresses clamped into the grid; a
+// clamped value is never used), then the reference's tests in its order.
 __device__ __forceinline__ void set_wall_bcs_cell(const Dims& d, const int* __restrict__ flags, Mac vel, CMac obvel, int hasObvel, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
+  const bool xm = i > 0, xp = i < d.nx - 1, ym = j > 0, yp = j < d.ny - 1, zm = k > 0, zp = k < d.nz - 1;
   const int f = __ldg(flags + idx);
-  const bool curFluid = f & kFluid, curObs = f & kObstacle;
-  if (!curFluid && !curObs) return;
+  const int fxm = __ldg(flags + (xm ? idx - 1 : idx)), fxp = __ldg(flags + (xp ? idx + 1 : idx));
+  const int fym = __ldg(flags + (ym ? idx - d.sy : idx)), fyp = __ldg(flags + (yp ? idx + d.sy : idx));
+  int fzm = 0, fzp = 0;
+  if (d.is3d) {
+    fzm = __ldg(flags + (zm ? idx - d.sz : idx));
+    fzp = __ldg(flags + (zp ? idx + d.sz : idx));
+  }
+  float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
   float bx = 0.f, by = 0.f, bz = 0.f;
   if (hasObvel) {
     bx = obvel.u[idx];
     by = obvel.v[idx];
     if (d.is3d) bz = obvel.w[idx];
   }
-  float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
-  if (i > 0 && isO(flags, idx - 1)) u = bx;
-  if (i > 0 && curObs && isF(flags, idx - 1)) u = bx;
-  if (j > 0 && isO(flags, idx - d.sy)) v = by;
-  if (j > 0 && curObs && isF(flags, idx - d.sy)) v = by;
+  const bool curFluid = f & kFluid, curObs = f & kObstacle;
+  if (!curFluid && !curObs) return;
+  if (xm && (fxm & kObstacle)) u = bx;
+  if (xm && curObs && (fxm & kFluid)) u = bx;
+  if (ym && (fym & kObstacle)) v = by;
+  if (ym && curObs && (fym & kFluid)) v = by;
   if (!d.is3d) {
     w = 0.f;
   } else {
-    if (k > 0 && isO(flags, idx - d.sz)) w = bz;
-    if (k > 0 && curObs && isF(flags, idx - d.sz)) w = bz;
+    if (zm && (fzm & kObstacle)) w = bz;
+    if (zm && curObs && (fzm & kFluid)) w = bz;
   }
   if (curFluid) {
-    if ((i > 0 && (__ldg(flags + idx - 1) & kStick)) || (i < d.nx - 1 && (__ldg(flags + idx + 1) & kStick))) v = w = 0.f;
-    if ((j > 0 && (__ldg(flags + idx - d.sy) & kStick)) || (j < d.ny - 1 && (__ldg(flags + idx + d.sy) & kStick))) u = w = 0.f;
-    if (d.is3d && ((k > 0 && (__ldg(flags + idx - d.sz) & kStick)) || (k < d.nz - 1 && (__ldg(flags + idx + d.sz) & kStick))))
-      u = v = 0.f;
+    if ((xm && (fxm & kStick)) || (xp && (fxp & kStick))) v = w = 0.f;
+    if ((ym && (fym & kStick)) || (yp && (fyp & kStick))) u = w = 0.f;
+    if (d.is3d && ((zm && (fzm & kStick)) || (zp && (fzp & kStick)))) u = v = 0.f;
   }
   vel.u[idx] = u;
   vel.v[idx] = v;
@@ -63,15 +73,20 @@ __global__ void k_set_wall_bcs(Dims d, const int* __restrict__ flags, Mac vel, C
 
 // KnAddBuoyancy (extforces.cpp:72-80).  (0.5*s)*(rho+rho') is formed in
 // double and added in double in the reference: one fmaf rounding here.
+// Every load is issued before the flag tests.
 __device__ __forceinline__ void add_buoyancy_cell(const Dims& d, const int* __restrict__ flags, const float* __restrict__ rho, Mac vel, float hx,
                                float hy, float hz, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   if (!INNER) return;
-  if (!isF(flags, idx)) return;
-  const float r = __ldg(rho + idx);
-  if (isF(flags, idx - 1)) vel.u[idx] = fmaf(hx, r + __ldg(rho + idx - 1), vel.u[idx]);
-  if (isF(flags, idx - d.sy)) vel.v[idx] = fmaf(hy, r + __ldg(rho + idx - d.sy), vel.v[idx]);
-  if (d.is3d && isF(flags, idx - d.sz)) vel.w[idx] = fmaf(hz, r + __ldg(rho + idx - d.sz), vel.w[idx]);
+  const int f = __ldg(flags + idx), fxm = __ldg(flags + idx - 1), fym = __ldg(flags + idx - d.sy);
+  const int fzm = d.is3d ? __ldg(flags + idx - d.sz) : 0;
+  const float r = __ldg(rho + idx), rxm = __ldg(rho + idx - 1), rym = __ldg(rho + idx - d.sy);
+  const float rzm = d.is3d ? __ldg(rho + idx - d.sz) : 0.f;
+  const float u = vel.u[idx], v = vel.v[idx], w = d.is3d ? vel.w[idx] : 0.f;
+  if (!(f & kFluid)) return;
+  if (fxm & kFluid) vel.u[idx] = fmaf(hx, r + rxm, u);
+  if (fym & kFluid) vel.v[idx] = fmaf(hy, r + rym, v);
+  if (d.is3d && (fzm & kFluid)) vel.w[idx] = fmaf(hz, r + rzm, w);
 }
 
 __global__ void k_add_buoyancy(Dims d, const int* __restrict__ flags, const float* __restrict__ rho, Mac vel, float hx,
@@ -439,6 +454,18 @@ __global__ void k_soa_to_aos(long long n, CMac soa, float* __restrict__ aos) {
 }
 
 // Grid<Real>::join (grid.cpp knJoinReal): keep max / min
+// four cells per thread (n a multiple of 4; grids start 256-byte aligned)
+__global__ void k_join4(long long nq, float4* a, const float4* __restrict__ b, int keepMax) {
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
+    const float4 x = a[q], y = __ldg(b + q);
+    float4 o;
+    o.x = keepMax ? (x.x < y.x ? y.x : x.x) : (y.x < x.x ? y.x : x.x);
+    o.y = keepMax ? (x.y < y.y ? y.y : x.y) : (y.y < x.y ? y.y : x.y);
+    o.z = keepMax ? (x.z < y.z ? y.z : x.z) : (y.z < x.z ? y.z : x.z);
+    o.w = keepMax ? (x.w < y.w ? y.w : x.w) : (y.w < x.w ? y.w : x.w);
+    a[q] = o;
+  }
+}
 __global__ void k_join(long long n, float* a, const float* __restrict__ b, int keepMax) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
@@ -572,7 +599,13 @@ void launch_soa_to_aos(long long n, CMac soa, float* aos, cudaStream_t s) {
 }
 void launch_join(long long n, float* a, const float* b, int keepMax, cudaStream_t s) {
   count_launch();
-  k_join<<<nblk(n, 256), 256, 0, s>>>(n, a, b, keepMax);
+  if ((n & 3) == 0 && ((uintptr_t)a & 15) == 0 && ((uintptr_t)b & 15) == 0) {
+    const long long nq = n / 4;
+    k_join4<<<(unsigned)std::min<long long>(nblk(nq, 256), 1 << 16), 256, 0, s>>>(nq, reinterpret_cast<float4*>(a),
+                                                                                reinterpret_cast<const float4*>(b), keepMax);
+  } else {
+    k_join<<<nblk(n, 256), 256, 0, s>>>(n, a, b, keepMax);
+  }
 }
 void launch_set_const(long long n, float* a, float v, cudaStream_t s) {
   count_launch();

@@ -92,12 +92,14 @@ __global__ void __launch_bounds__(256) k_make_rhs(Dims d, const int* __restrict_
   if (i < d.nx && j < d.ny) {
     const long long idx = ix(d, i, j, k);
     if (INNER) {
+      // the divergence's loads are issued with the flag load
+      const float div = frac ? 0.f : mac_neg_div(d, vu, vv, vw, idx);
       if (!isF(flags, idx)) {
         rhs[idx] = 0.f;
       } else {
         float set;
         if (!frac) {
-          set = mac_neg_div(d, vu, vv, vw, idx);
+          set = div;
         } else {
           // the fraction-weighted divergence, and the obstacle velocity's
           // share of the faces (pressure.cpp:50-60)
@@ -166,26 +168,31 @@ __global__ void k_compat_shift(long long n, float* rhs, const CgScalars* sc) {
 // fluid bit and the upward links of interior fluid cells.
 __device__ __forceinline__ void make_codes_cell(const Dims& d, const int* __restrict__ flags, code_t* code, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
-  const bool fl = isF(flags, idx);
-  int c = fl ? kCodeFluid : 0;
-  if (fl && INNER) {
-    int a0 = 0;
-    a0 += !isO(flags, idx - 1);
-    a0 += !isO(flags, idx + 1);
-    a0 += !isO(flags, idx - d.sy);
-    a0 += !isO(flags, idx + d.sy);
-    if (d.is3d) {
-      a0 += !isO(flags, idx - d.sz);
-      a0 += !isO(flags, idx + d.sz);
+  const int f = __ldg(flags + idx);
+  int c = (f & kFluid) ? kCodeFluid : 0;
+  if (INNER) {
+    // the six neighbours' flags are loaded with the cell's own
+    const int fxm = __ldg(flags + idx - 1), fxp = __ldg(flags + idx + 1);
+    const int fym = __ldg(flags + idx - d.sy), fyp = __ldg(flags + idx + d.sy);
+    const int fzm = d.is3d ? __ldg(flags + idx - d.sz) : 0, fzp = d.is3d ? __ldg(flags + idx + d.sz) : 0;
+    if (f & kFluid) {
+      int a0 = 0;
+      a0 += !(fxm & kObstacle);
+      a0 += !(fxp & kObstacle);
+      a0 += !(fym & kObstacle);
+      a0 += !(fyp & kObstacle);
+      if (d.is3d) {
+        a0 += !(fzm & kObstacle);
+        a0 += !(fzp & kObstacle);
+      }
+      c |= a0;
+      if (fxp & kFluid) c |= kHighX;
+      if (fyp & kFluid) c |= kHighY;
+      if (d.is3d && (fzp & kFluid)) c |= kHighZ;
     }
-    c |= a0;
-    if (isF(flags, idx + 1)) c |= kHighX;
-    if (isF(flags, idx + d.sy)) c |= kHighY;
-    if (d.is3d && isF(flags, idx + d.sz)) c |= kHighZ;
   }
   code[idx] = (code_t)c;
 }
-
 __global__ void k_make_codes(Dims d, const int* __restrict__ flags, code_t* code) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -1170,26 +1177,29 @@ __global__ void k_mic_init_sigma(const double* part, int ntiles, CgScalars* sc) 
 }
 
 // ------------------------------------------------------- correctVelocity
-// knCorrectVelocity (pressure.cpp:87-109)
+// knCorrectVelocity (pressure.cpp:87-109); every load is issued before the
+// flag tests
 __device__ __forceinline__ void correct_velocity_cell(const Dims& d, const int* __restrict__ flags, Mac vel, const float* __restrict__ p, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   if (!INNER) return;
   const long long X = 1, Y = d.sy, Z = d.sz;
-  if (isF(flags, idx)) {
-    float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
-    const float pc = p[idx];
-    if (isF(flags, idx - X)) u -= (pc - p[idx - X]);
-    if (isF(flags, idx - Y)) v -= (pc - p[idx - Y]);
-    if (d.is3d && isF(flags, idx - Z)) w -= (pc - p[idx - Z]);
-    if (isE(flags, idx - X)) u -= pc;
-    if (isE(flags, idx - Y)) v -= pc;
-    if (d.is3d && isE(flags, idx - Z)) w -= pc;
+  const int f = __ldg(flags + idx), fxm = __ldg(flags + idx - X), fym = __ldg(flags + idx - Y);
+  const int fzm = d.is3d ? __ldg(flags + idx - Z) : 0;
+  const float pc = p[idx], pxm = p[idx - X], pym = p[idx - Y];
+  const float pzm = d.is3d ? p[idx - Z] : 0.f;
+  float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
+  if (f & kFluid) {
+    if (fxm & kFluid) u -= (pc - pxm);
+    if (fym & kFluid) v -= (pc - pym);
+    if (d.is3d && (fzm & kFluid)) w -= (pc - pzm);
+    if (fxm & kEmpty) u -= pc;
+    if (fym & kEmpty) v -= pc;
+    if (d.is3d && (fzm & kEmpty)) w -= pc;
     vel.u[idx] = u; vel.v[idx] = v; vel.w[idx] = w;
-  } else if (isE(flags, idx) && !isOut(flags, idx)) {
-    float u = vel.u[idx], v = vel.v[idx], w = vel.w[idx];
-    if (isF(flags, idx - X)) u += p[idx - X]; else u = 0.f;
-    if (isF(flags, idx - Y)) v += p[idx - Y]; else v = 0.f;
-    if (d.is3d) { if (isF(flags, idx - Z)) w += p[idx - Z]; else w = 0.f; }
+  } else if ((f & kEmpty) && !(f & kOutflow)) {
+    if (fxm & kFluid) u += pxm; else u = 0.f;
+    if (fym & kFluid) v += pym; else v = 0.f;
+    if (d.is3d) { if (fzm & kFluid) w += pzm; else w = 0.f; }
     vel.u[idx] = u; vel.v[idx] = v; vel.w[idx] = w;
   }
 }
