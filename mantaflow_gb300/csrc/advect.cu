@@ -79,21 +79,28 @@ __device__ __forceinline__ void clamp_component(const Dims& d, const int* __rest
     const int j0 = min(max(qy, 0), d.ny - 2);
     const int k0 = min(max(qz, 0), d.is3d ? d.nz - 2 : 1);
     const int k1 = d.is3d ? k0 + 1 : k0;
-    const int nk = d.is3d ? 2 : 1;
-    for (int kk = 0; kk < nk; kk++) {
-      const int kc = kk == 0 ? k0 : k1;
+    const int nq = d.is3d ? 8 : 4;
+    // the corners' flags and values are loaded together, then visited in
+    // the reference's order (k0 plane first)
+    int fl[8];
+    float ov[8][CH];
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const long long e = ix(d, i0 + (q & 1), j0 + (q >> 1), kc);
-        if (__ldg(flags + e) & (kFluid | kEmpty)) {
+    for (int q = 0; q < 8; q++) {
+      const long long e = ix(d, i0 + (q & 1), j0 + ((q >> 1) & 1), q < 4 ? k0 : k1);
+      fl[q] = __ldg(flags + e);
 #pragma unroll
-          for (int c = 0; c < CH; c++) {
-            const float v = __ldg(orig + c * d.n + e);
-            if (v < mn[c]) mn[c] = v;
-            if (v > mx[c]) mx[c] = v;
-          }
-          haveFl = true;
+      for (int c = 0; c < CH; c++) ov[q][c] = __ldg(orig + c * d.n + e);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      if (q < nq && (fl[q] & (kFluid | kEmpty))) {
+#pragma unroll
+        for (int c = 0; c < CH; c++) {
+          const float v = ov[q][c];
+          if (v < mn[c]) mn[c] = v;
+          if (v > mx[c]) mx[c] = v;
         }
+        haveFl = true;
       }
     }
   }

@@ -115,7 +115,15 @@ bool g_pathsReady = false;
 int g_tailCta = 0;  // CTAs of the cluster V-cycle tail (0: per-level launches)
 
 __host__ __device__ __forceinline__ int parity3(int a, int b, int c) { return (a & 1) + (b & 1) + (c & 1); }
-__host__ __device__ __forceinline__ float inv_pow2(int e) { return 1.f / (float)(1 << e); }
+// 2^-e (0 <= e <= 3), the reference's 1/(1<<e): exact, so the device forms
+// it from its exponent bits instead of a division
+__host__ __device__ __forceinline__ float inv_pow2(int e) {
+#ifdef __CUDA_ARCH__
+  return __int_as_float((127 - e) << 23);
+#else
+  return 1.f / (float)(1 << e);
+#endif
+}
 
 __device__ __forceinline__ float l0_diag(int c, const float* __restrict__ a0f, long long v) {
   if (a0f) return a0f[v];
