@@ -596,9 +596,9 @@ __device__ __forceinline__ void restrict_vertex_at(const Lev& D, const Lev& S, c
   const int sx = FROM0 ? F.d.nx : S.sx, sy = FROM0 ? F.d.ny : S.sy, sz = FROM0 ? F.d.nz : S.sz;
   const long long py = F.d.sy, pz = F.d.sz;
   D.x[v] = 0.f;
-  if (D.type[v] == kVtInactive) return;
+  const int8_t ty = D.type[v];
   // the fine vertices 2V-1 .. 2V+1 inside the level, in the reference's
-  // loop order; all loads first
+  // loop order; all loads first (the type is tested after them)
   float rv[27];
   bool in[27];
 #pragma unroll
@@ -614,7 +614,7 @@ __device__ __forceinline__ void restrict_vertex_at(const Lev& D, const Lev& S, c
     const int rx = 2 * vx - 1 + q % 3, ry = 2 * vy - 1 + (q / 3) % 3, rz = 2 * vz - 1 + q / 9;
     if (in[q]) sum = sum + inv_pow2(parity3(rx, ry, rz)) * rv[q];
   }
-  D.b[v] = sum;
+  if (ty != kVtInactive) D.b[v] = sum;
 }
 template <bool FROM0, bool CG>
 __device__ __forceinline__ void restrict_vertex(const Lev& D, const Lev& S, const Lev0& F, long long v) {
@@ -626,9 +626,10 @@ __device__ __forceinline__ void restrict_vertex(const Lev& D, const Lev& S, cons
 // knInterpolate from level S = D+1 and knAddAssign: x[D] += I * x[S]
 template <bool IS3D, bool CG>
 __device__ __forceinline__ void interp_vertex(const Lev& D, const Lev& S, long long v) {
-  if (D.type[v] == kVtInactive) return;
+  const int8_t ty = D.type[v];
   int vx, vy, vz;
   coords(D, v, vx, vy, vz);
+  if (!inside(D, vx, vy, vz)) return;  // padding slot
   // coarse parents V/2 .. (V+1)/2 per axis (one or two), in the
   // reference's loop order; inactive coarse vertices hold x = 0
   const int hx = (vx + 1) / 2 - vx / 2, hy = (vy + 1) / 2 - vy / 2, hz = (vz + 1) / 2 - vz / 2;
@@ -645,7 +646,8 @@ __device__ __forceinline__ void interp_vertex(const Lev& D, const Lev& S, long l
     const int ox = q & 1, oy = (q >> 1) & 1, oz = q >> 2;
     if ((ox <= hx) && (oy <= hy) && (oz <= hz)) sum = sum + cv[q];
   }
-  D.x[v] = ldv<CG>(&D.x[v]) + inv_pow2(parity3(vx, vy, vz)) * sum;
+  const float xv = ldv<CG>(&D.x[v]) + inv_pow2(parity3(vx, vy, vz)) * sum;
+  if (ty != kVtInactive) D.x[v] = xv;
 }
 
 template <bool IS3D>
@@ -673,10 +675,12 @@ __global__ void __launch_bounds__(256, 4) k_mg_smooth_dict(Lev L, int ox, int oy
     const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
     if (!inside(L, vx, vy, vz)) continue;
     const long long v = (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi;
-    if (L.type[v] == kVtInactive) continue;
+    // the vertex type is tested after every load was issued (an inactive
+    // vertex has id 0, whose table entry exists)
+    const int8_t ty = L.type[v];
     const float* t = L.T + (int)L.sid[v] * kDictStride;
     const float sum = stencil_sub_dict<IS3D, true>(L, t, vx, vy, vz, L.b[v]);
-    L.x[v] = sum / t[S - 1];
+    if (ty != kVtInactive) L.x[v] = sum / t[S - 1];
   }
 }
 
@@ -684,11 +688,13 @@ template <bool IS3D>
 __global__ void __launch_bounds__(256, 4) k_mg_residual_dict(Lev L, const CgScalars* sc) {
   if (sc->done) return;
   GRID_STRIDE(v, L.n) {
-    if (L.type[v] == kVtInactive) continue;
+    const int8_t ty = L.type[v];
     int vx, vy, vz;
     coords(L, v, vx, vy, vz);
+    if (!inside(L, vx, vy, vz)) continue;  // padding slot
     const float* t = L.T + (int)L.sid[v] * kDictStride;
-    L.r[v] = stencil_sub_dict<IS3D, false>(L, t, vx, vy, vz, L.b[v]);
+    const float r = stencil_sub_dict<IS3D, false>(L, t, vx, vy, vz, L.b[v]);
+    if (ty != kVtInactive) L.r[v] = r;
   }
 }
 
