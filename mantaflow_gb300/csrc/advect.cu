@@ -642,7 +642,9 @@ void launch_advect_maccormack_mac(const Dims& d, const int* flags, CMac vel, CMa
 void launch_outflow_bc(const Dims& d, const int* flags, CMac vel, CMac velPrev, Mac velDst, Mac velOut, float timeStep,
                        cudaStream_t s) {
   if ((d.n & 3) == 0) {
-    const unsigned nb = (unsigned)std::min<long long>((d.n / 4 + 255) / 256, 4096);
+    // one quad per thread: a thread of the boundary layer then handles at
+    // most four outflow cells
+    const unsigned nb = (unsigned)((d.n / 4 + 255) / 256);
     count_launch();
     k_outflow_q<false><<<nb, 256, 0, s>>>(d, flags, vel, velPrev, velDst, timeStep);
     count_launch();
