@@ -193,13 +193,6 @@ __device__ __forceinline__ void make_codes_cell(const Dims& d, const int* __rest
   }
   code[idx] = (code_t)c;
 }
-__global__ void k_make_codes(Dims d, const int* __restrict__ flags, code_t* code) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= d.nx || j >= d.ny) return;
-  make_codes_cell(d, flags, code, i, j, k);
-}
 // pass 2: lower links mirror the upper link of the lower neighbour
 __device__ __forceinline__ void make_codes_low_cell(const Dims& d, code_t* code, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
@@ -210,13 +203,56 @@ __device__ __forceinline__ void make_codes_low_cell(const Dims& d, code_t* code,
   code[idx] = (code_t)c;
 }
 
-__global__ void k_make_codes_low(Dims d, code_t* code) {
+// both passes in one: a cell's lower links are its lower neighbours' upper
+// links, which the flags decide directly (the neighbour is an interior
+// fluid cell and this cell is fluid), so one sweep forms the whole code
+__device__ __forceinline__ void make_codes_full_cell(const Dims& d, const int* __restrict__ flags, code_t* code, int i,
+                                                     int j, int k) {
+  const long long idx = ix(d, i, j, k);
+  const bool xm = i > 0, xp = i < d.nx - 1, ym = j > 0, yp = j < d.ny - 1, zm = k > 0, zp = k < d.nz - 1;
+  const int f = __ldg(flags + idx);
+  const int fxm = __ldg(flags + (xm ? idx - 1 : idx)), fxp = __ldg(flags + (xp ? idx + 1 : idx));
+  const int fym = __ldg(flags + (ym ? idx - d.sy : idx)), fyp = __ldg(flags + (yp ? idx + d.sy : idx));
+  int fzm = 0, fzp = 0;
+  if (d.is3d) {
+    fzm = __ldg(flags + (zm ? idx - d.sz : idx));
+    fzp = __ldg(flags + (zp ? idx + d.sz : idx));
+  }
+  const bool fl = f & kFluid;
+  int c = fl ? kCodeFluid : 0;
+  const bool iin = i >= 1 && i < d.nx - 1, jin = j >= 1 && j < d.ny - 1, kin = !d.is3d || (k >= 1 && k < d.nz - 1);
+  if (fl && iin && jin && kin) {
+    int a0 = 0;
+    a0 += !(fxm & kObstacle);
+    a0 += !(fxp & kObstacle);
+    a0 += !(fym & kObstacle);
+    a0 += !(fyp & kObstacle);
+    if (d.is3d) {
+      a0 += !(fzm & kObstacle);
+      a0 += !(fzp & kObstacle);
+    }
+    c |= a0;
+    if (fxp & kFluid) c |= kHighX;
+    if (fyp & kFluid) c |= kHighY;
+    if (d.is3d && (fzp & kFluid)) c |= kHighZ;
+  }
+  if (fl) {
+    // the lower neighbour is interior: its own index inside, the others as here
+    if (i >= 2 && i - 1 < d.nx - 1 && jin && kin && (fxm & kFluid)) c |= kLowX;
+    if (j >= 2 && j - 1 < d.ny - 1 && iin && kin && (fym & kFluid)) c |= kLowY;
+    if (d.is3d && k >= 2 && k - 1 < d.nz - 1 && iin && jin && (fzm & kFluid)) c |= kLowZ;
+  }
+  code[idx] = (code_t)c;
+}
+
+__global__ void k_make_codes_full(Dims d, const int* __restrict__ flags, code_t* code) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= d.nx || j >= d.ny) return;
-  make_codes_low_cell(d, code, i, j, k);
+  make_codes_full_cell(d, flags, code, i, j, k);
 }
+
 
 // ApplyGhostFluidDiagonal (pressure.cpp:136-151): float diagonal
 __device__ __forceinline__ void ghost_fluid_diag_cell(const Dims& d, const int* __restrict__ flags,
@@ -1466,9 +1502,7 @@ void launch_compat_shift(const PcgBuffers& b, cudaStream_t s) {
 }
 void launch_make_codes(const PcgBuffers& b, cudaStream_t s) {
   count_launch();
-  k_make_codes<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.flags, b.code);
-  count_launch();
-  k_make_codes_low<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.code);
+  k_make_codes_full<<<grid3(b.d, kBlk), kBlk, 0, s>>>(b.d, b.flags, b.code);
 }
 void launch_ghost_fluid_diag(const PcgBuffers& b, const float* phi, float gfClamp, cudaStream_t s) {
   count_launch();
