@@ -153,17 +153,28 @@ __device__ __forceinline__ bool inside(const Lev& L, int x, int y, int z) {
 }
 // slot -> vertex; padding slots of a colour-blocked level map outside the
 // grid and have type inactive
+// a block index's block coordinates; 32-bit: a level holds fewer than 2^31
+// slots (the finest grid has fewer than 2^31 cells)
+__device__ __forceinline__ void block_xyz(long long bi64, int bx, int by, int& x, int& y, int& z) {
+  const unsigned bi = (unsigned)bi64, q = bi / (unsigned)bx, r = q / (unsigned)by;
+  x = (int)(bi - q * (unsigned)bx);
+  y = (int)(q - r * (unsigned)by);
+  z = (int)r;
+}
 __device__ __forceinline__ void coords(const Lev& L, long long v, int& x, int& y, int& z) {
   if (L.colored) {
-    const long long c = v / L.nb, bi = v - c * L.nb;
-    x = 2 * (int)(bi % L.bx) + (int)(c & 1);
-    y = 2 * (int)((bi / L.bx) % L.by) + (int)((c >> 1) & 1);
-    z = 2 * (int)(bi / ((long long)L.bx * L.by)) + (int)(c >> 2);
+    const unsigned u = (unsigned)v, c = u / (unsigned)L.nb, bi = u - c * (unsigned)L.nb;
+    int bxi, byi, bzi;
+    block_xyz(bi, L.bx, L.by, bxi, byi, bzi);
+    x = 2 * bxi + (int)(c & 1);
+    y = 2 * byi + (int)((c >> 1) & 1);
+    z = 2 * bzi + (int)(c >> 2);
     return;
   }
-  x = (int)(v % L.sx);
-  y = (int)((v / L.sx) % L.sy);
-  z = (int)(v / L.pz);
+  const unsigned u = (unsigned)v, q = u / (unsigned)L.sx, r = q / (unsigned)L.sy;
+  x = (int)(u - q * (unsigned)L.sx);
+  y = (int)(q - r * (unsigned)L.sy);
+  z = (int)r;
 }
 
 // The 27 neighbours of a vertex of a colour-blocked level: slot offsets and
@@ -549,7 +560,11 @@ __device__ __forceinline__ float stencil_sub_dict(const Lev& L, const float* __r
 // (ox, oy, oz) in 2x2x2 blocks, bx x by blocks per z-plane
 template <bool IS3D, bool CG>
 __device__ __forceinline__ void smooth_vertex(const Lev& L, long long bi, int ox, int oy, int oz, int bx, int by) {
-  const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
+  int vx, vy, vz;
+  block_xyz(bi, bx, by, vx, vy, vz);
+  vx = 2 * vx + ox;
+  vy = 2 * vy + oy;
+  vz = 2 * vz + oz;
   if (!inside(L, vx, vy, vz)) return;
   const long long v = L.colored ? (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi : lin(L, vx, vy, vz);
   if (L.type[v] == kVtInactive) return;
@@ -561,7 +576,11 @@ __device__ __forceinline__ void smooth_vertex(const Lev& L, long long bi, int ox
 // loads were issued (inactive vertices only cost loads)
 template <bool IS3D>
 __device__ __forceinline__ void smooth_vertex_flat(const Lev& L, long long bi, int ox, int oy, int oz, int bx, int by) {
-  const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
+  int vx, vy, vz;
+  block_xyz(bi, bx, by, vx, vy, vz);
+  vx = 2 * vx + ox;
+  vy = 2 * vy + oy;
+  vz = 2 * vz + oz;
   if (!inside(L, vx, vy, vz)) return;
   const long long v = L.colored ? (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi : lin(L, vx, vy, vz);
   const int8_t ty = L.type[v];
@@ -672,7 +691,11 @@ __global__ void __launch_bounds__(256, 4) k_mg_smooth_dict(Lev L, int ox, int oy
   const long long nb = (long long)bx * by * bz;
   constexpr int S = IS3D ? 14 : 5;
   GRID_STRIDE(bi, nb) {
-    const int vx = 2 * (int)(bi % bx) + ox, vy = 2 * (int)((bi / bx) % by) + oy, vz = 2 * (int)(bi / ((long long)bx * by)) + oz;
+    int vx, vy, vz;
+    block_xyz(bi, bx, by, vx, vy, vz);
+    vx = 2 * vx + ox;
+    vy = 2 * vy + oy;
+    vz = 2 * vz + oz;
     if (!inside(L, vx, vy, vz)) continue;
     const long long v = (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi;
     // the vertex type is tested after every load was issued (an inactive
