@@ -457,7 +457,9 @@ __global__ void k_outflow_q(Dims d, const int* __restrict__ flags, CMac vel, CMa
     for (int e = 0; e < 4; e++) {
       if (!(fl[e] & kOutflow)) continue;
       const long long idx = 4 * q + e;
-      const int i = (int)(idx % d.nx), j = (int)((idx / d.nx) % d.ny), k = (int)(idx / ((long long)d.nx * d.ny));
+      // grids hold fewer than 2^31 cells: 32-bit division
+      const unsigned u = (unsigned)idx, q = u / (unsigned)d.nx, r = q / (unsigned)d.ny;
+      const int i = (int)(u - q * (unsigned)d.nx), j = (int)(q - r * (unsigned)d.ny), k = (int)r;
       if (COPY) {
         velDst.u[idx] = vel.u[idx];
         velDst.v[idx] = vel.v[idx];

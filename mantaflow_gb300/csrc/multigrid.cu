@@ -228,7 +228,8 @@ __global__ void k_mg_snapshot0(Dims d, const code_t* __restrict__ code, const fl
       c |= kMgActive;
       bool links = (c & (kLowX | kLowY | kLowZ | kHighX | kHighY | kHighZ)) != 0;
       if (Ai) {
-        const int i = (int)(v % d.nx), j = (int)((v / d.nx) % d.ny), k = d.is3d ? (int)(v / d.sz) : 0;
+        const unsigned u = (unsigned)v, q = u / (unsigned)d.nx, r = q / (unsigned)d.ny;  // < 2^31 cells
+        const int i = (int)(u - q * (unsigned)d.nx), j = (int)(q - r * (unsigned)d.ny), k = d.is3d ? (int)r : 0;
         links = Ai[v] != 0.f || Aj[v] != 0.f || (d.is3d && Ak[v] != 0.f) || (i > 0 && Ai[v - 1] != 0.f) ||
                 (j > 0 && Aj[v - d.sy] != 0.f) || (d.is3d && k > 0 && Ak[v - d.sz] != 0.f);
       }
@@ -527,8 +528,9 @@ __global__ void __launch_bounds__(256) k_dict_verify(Lev L, const uint16_t* sid,
   }
 }
 
-// stencil_sub with the coefficients from the dictionary tuple t
-template <bool IS3D, bool SKIP_CENTER>
+// stencil_sub with the coefficients from the dictionary tuple t (CG: x is
+// written by other CTAs of the same launch and read at L2)
+template <bool IS3D, bool SKIP_CENTER, bool CG = false>
 __device__ __forceinline__ float stencil_sub_dict(const Lev& L, const float* __restrict__ t, int vx, int vy, int vz,
                                                   float sum) {
   constexpr int ZL = IS3D ? -1 : 0, ZH = IS3D ? 1 : 0;
@@ -547,7 +549,7 @@ __device__ __forceinline__ float stencil_sub_dict(const Lev& L, const float* __r
         const int s = (dz - ZL) * 9 + q;
         in[q] = o.ix[dx + 1] && o.iy[dy + 1] && o.iz[dz + 1] && !(SKIP_CENTER && s == S - 1);
         a[q] = t[s];
-        xv[q] = in[q] ? L.x[vi + o.ox[dx + 1] + o.oy[dy + 1] + o.oz[dz + 1]] : 0.f;
+        xv[q] = in[q] ? ldv<CG>(&L.x[vi + o.ox[dx + 1] + o.oy[dy + 1] + o.oz[dz + 1]]) : 0.f;
       }
 #pragma unroll
     for (int q = 0; q < 9; q++)
@@ -595,6 +597,34 @@ __device__ __forceinline__ void residual_vertex_flat(const Lev& L, long long v) 
   coords(L, v, vx, vy, vz);
   const int8_t ty = L.type[v];
   const float r = stencil_sub_flat<IS3D, false>(L, vx, vy, vz, (int)v, __ldcg(&L.b[v]));
+  if (ty != kVtInactive) L.r[v] = r;
+}
+
+// the same two passes for the cluster tail on a level with a stencil
+// dictionary: the vertex's id, then its tuple and every x at once
+template <bool IS3D>
+__device__ __forceinline__ void smooth_vertex_dict_flat(const Lev& L, long long bi, int ox, int oy, int oz, int bx, int by) {
+  constexpr int S = IS3D ? 14 : 5;
+  int vx, vy, vz;
+  block_xyz(bi, bx, by, vx, vy, vz);
+  vx = 2 * vx + ox;
+  vy = 2 * vy + oy;
+  vz = 2 * vz + oz;
+  if (!inside(L, vx, vy, vz)) return;
+  const long long v = (long long)(ox | (oy << 1) | (oz << 2)) * L.nb + bi;
+  const int8_t ty = L.type[v];
+  const float* t = L.T + (int)L.sid[v] * kDictStride;
+  const float sum = stencil_sub_dict<IS3D, true, true>(L, t, vx, vy, vz, __ldcg(&L.b[v]));
+  if (ty != kVtInactive) L.x[v] = sum / t[S - 1];
+}
+template <bool IS3D>
+__device__ __forceinline__ void residual_vertex_dict_flat(const Lev& L, long long v) {
+  int vx, vy, vz;
+  coords(L, v, vx, vy, vz);
+  if (!inside(L, vx, vy, vz)) return;  // padding slot
+  const int8_t ty = L.type[v];
+  const float* t = L.T + (int)L.sid[v] * kDictStride;
+  const float r = stencil_sub_dict<IS3D, false, true>(L, t, vx, vy, vz, __ldcg(&L.b[v]));
   if (ty != kVtInactive) L.r[v] = r;
 }
 
@@ -1407,10 +1437,16 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(const Lev* __restri
     const int bx = (L.sx + 1) / 2, by = (L.sy + 1) / 2;
     const long long nb = (long long)bx * by * ((L.sz + 1) / 2);
     for (int c = 0; c < ncol; c++) {
-      for (long long bi = t0; bi < nb; bi += T) smooth_vertex_flat<IS3D>(L, bi, c & 1, (c >> 1) & 1, c >> 2, bx, by);
+      if (L.sid)
+        for (long long bi = t0; bi < nb; bi += T) smooth_vertex_dict_flat<IS3D>(L, bi, c & 1, (c >> 1) & 1, c >> 2, bx, by);
+      else
+        for (long long bi = t0; bi < nb; bi += T) smooth_vertex_flat<IS3D>(L, bi, c & 1, (c >> 1) & 1, c >> 2, bx, by);
       cl.sync();
     }
-    for (long long v = t0; v < L.n; v += T) residual_vertex_flat<IS3D>(L, v);
+    if (L.sid)
+      for (long long v = t0; v < L.n; v += T) residual_vertex_dict_flat<IS3D>(L, v);
+    else
+      for (long long v = t0; v < L.n; v += T) residual_vertex_flat<IS3D>(L, v);
     cl.sync();
     const Lev D = levs[l + 1];
     for (long long v = t0; v < D.n; v += T) restrict_vertex<false, true>(D, L, Lev0{}, v);
@@ -1425,7 +1461,10 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(const Lev* __restri
     const int bx = (D.sx + 1) / 2, by = (D.sy + 1) / 2;
     const long long nb = (long long)bx * by * ((D.sz + 1) / 2);
     for (int c = ncol - 1; c >= 0; c--) {
-      for (long long bi = t0; bi < nb; bi += T) smooth_vertex_flat<IS3D>(D, bi, c & 1, (c >> 1) & 1, c >> 2, bx, by);
+      if (D.sid)
+        for (long long bi = t0; bi < nb; bi += T) smooth_vertex_dict_flat<IS3D>(D, bi, c & 1, (c >> 1) & 1, c >> 2, bx, by);
+      else
+        for (long long bi = t0; bi < nb; bi += T) smooth_vertex_flat<IS3D>(D, bi, c & 1, (c >> 1) & 1, c >> 2, bx, by);
       cl.sync();
     }
   }
@@ -1758,10 +1797,12 @@ MgHierarchy* mg_hierarchy_create(const Dims& d) {
     h->dlev = h->alloc<Lev>(L);
     if (h->ok && cudaMemcpy(h->dlev, h->lev, sizeof(Lev) * (size_t)L, cudaMemcpyHostToDevice) != cudaSuccess) h->ok = false;
   }
-  // dictionary buffers for the colour-blocked levels outside the tail
+  // dictionary buffers for the colour-blocked levels (the cluster tail's too
+  // unless MANTAGPU_MG_NO_TAIL_DICT is set)
   if (h->ok && !std::getenv("MANTAGPU_MG_NO_DICT")) {
     bool any = false;
-    for (int l = 1; l < L - 1 && (!h->tailFirst || l < h->tailFirst); l++) {
+    const bool tailDict = !std::getenv("MANTAGPU_MG_NO_TAIL_DICT");
+    for (int l = 1; l < L - 1 && (tailDict || !h->tailFirst || l < h->tailFirst); l++) {
       h->dsid[l] = h->alloc<uint16_t>(h->lev[l].n);
       h->dT[l] = h->alloc<float>((long long)(kDictCap + 1) * kDictStride);
       any = true;
@@ -1928,6 +1969,9 @@ int mg_setup(MgHierarchy* h, const PcgBuffers& b, float coarseAccuracy, cudaStre
         h->ndict[l] = f[2];
       }
     }
+    // the cluster tail reads the levels from the device copy
+    if (h->dlev && cudaMemcpyAsync(h->dlev, h->lev, sizeof(Lev) * (size_t)h->nlev, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return 1;
   }
   h->isASet = true;
   return 0;
