@@ -581,6 +581,101 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(out), flush=True)
 
 
+def _events_ms(L, h, a, b):
+    import ctypes as C
+    from mantaflow_gb300 import _lib
+    ms = C.c_float()
+    _lib.check(L.mg_elapsed(h, a, b, C.byref(ms)))
+    return float(ms.value)
+
+
+def config_runs(m, seed, cpu_steps):
+    """Configs 1 and 3 at their own sizes and step counts on the plain path:
+    the 64^3 plume with PcMIC for 100 steps and the 128^3 dam break for 150
+    steps, device time per step from CUDA events on the solver's stream (the
+    plume's inflow noise uploaded before the timed steps), with the CG
+    iterations.  Beside them, the oracle on the host cores over the first
+    `cpu_steps` steps of the same scenes from rest, with the GPU's time for
+    the same first steps (a from-rest sample: fewer CG iterations than the
+    run's average)."""
+    from mantaflow_gb300 import _lib
+    from oracle import oracle as og
+    L = _lib.load()
+    threads = os.cpu_count() or 1
+    out = {}
+    # config 1: 64^3 plume, MacCormack, PcMIC, 100 steps
+    n, K = 64, 100
+    sim = Plume(m, n, m.PcMIC, seed, K)
+    noise = []
+    for _ in range(K):
+        g = sim.s.create(m.RealGrid)
+        m.copyArrayToGridReal(sim.noise(), g)
+        noise.append(g)
+    sim.s.sync()
+    _lib.check(L.mg_mark(sim.s._h, 0))
+    for t in range(K):
+        sim.step(noise[t])
+        if t + 1 == cpu_steps:
+            _lib.check(L.mg_mark(sim.s._h, 1))
+    _lib.check(L.mg_mark(sim.s._h, 2))
+    sim.s.sync()
+    tot = _events_ms(L, sim.s._h, 0, 2)
+    first = _events_ms(L, sim.s._h, 0, 1) if 0 < cpu_steps <= K else 0.0
+    c1 = {"workload": "config 1: 3D smoke plume 64^3, MacCormack advection, MIC(0)-PCG (PcMIC), cgAccuracy 1e-3, "
+                      "100 steps from rest", "cells_per_s": n ** 3 * K / (tot / 1e3), "ms_per_step": tot / K,
+          "cg_iterations_mean": float(np.mean(sim.iters)), "gpu_ms_first_steps": first / max(1, cpu_steps)}
+    del noise, sim
+    # config 3: 128^3 dam break, 150 steps
+    n3, K3 = 128, 150
+    g = _plain_dam(m, n3)
+    g["s"].sync()
+    its = []
+    _lib.check(L.mg_mark(g["s"]._h, 0))
+    for t in range(K3):
+        _plain_dam_step(m, g)
+        its.append(m.lastSolveStats()[0])
+        if t + 1 == cpu_steps:
+            _lib.check(L.mg_mark(g["s"]._h, 1))
+    _lib.check(L.mg_mark(g["s"]._h, 2))
+    g["s"].sync()
+    tot3 = _events_ms(L, g["s"]._h, 0, 2)
+    first3 = _events_ms(L, g["s"]._h, 0, 1) if 0 < cpu_steps <= K3 else 0.0
+    c3 = {"workload": "config 3: free-surface dam break 128^3, SL order 1, ghost-fluid MIC(0)-PCG, "
+                      "extrapolateMACSimple 4, 150 steps from rest", "cells_per_s": n3 ** 3 * K3 / (tot3 / 1e3),
+          "ms_per_step": tot3 / K3, "cg_iterations_mean": float(np.mean(its)),
+          "gpu_ms_first_steps": first3 / max(1, cpu_steps)}
+    del g
+    if cpu_steps > 0:
+        t1, it1 = cpu_plume_steps(64, cpu_steps, 0, threads, seed, pc=1)
+        c1["cpu_oracle"] = {"ms_per_step": 1e3 * float(np.mean(t1)), "cores": threads, "kind": "port",
+                            "sample": "steps 1..%d from rest, CG iterations %s" % (cpu_steps, it1)}
+        og.set_num_threads(threads)
+        f = np.zeros((n3, n3, n3), np.int32)
+        og.init_domain(f, 0)
+        phi = np.zeros((n3, n3, n3), np.float32)
+        og.box_sdf(phi, (0, 0, 0), (0.4 * n3, 0.6 * n3, n3))
+        og.update_from_levelset(f, phi)
+        vel = np.zeros((n3, n3, n3, 3), np.float32)
+        pres = np.zeros((n3, n3, n3), np.float32)
+        t3, it3 = [], []
+        for t in range(cpu_steps):
+            t0 = time.perf_counter()
+            og.extrapolate_mac_simple(f, vel, 4)
+            og.advect_semi_lagrange(f, vel, phi, og.KIND_REAL, order=1)
+            og.update_from_levelset(f, phi)
+            og.advect_semi_lagrange(f, vel, vel, og.KIND_MAC, order=1)
+            og.add_gravity(f, vel, (0, -1e-3, 0))
+            og.set_wall_bcs(f, vel)
+            it_o, _, _ = og.solve_pressure(f, vel, pres, phi=phi)
+            og.set_wall_bcs(f, vel)
+            t3.append(time.perf_counter() - t0)
+            it3.append(it_o)
+        og.set_num_threads(1)
+        c3["cpu_oracle"] = {"ms_per_step": 1e3 * float(np.mean(t3)), "cores": threads, "kind": "port",
+                            "sample": "steps 1..%d from rest, CG iterations %s" % (cpu_steps, it3)}
+    return {"config1_plume64_mic": c1, "config3_dam_break128": c3}
+
+
 def flip_form(m, n, ppc, reps, seed):
     """The FLIP transfers (plugin/flip.cpp:573-673) at n^3 with ppc particles
     per cell, seeded cell by cell with jitter as a fresh FLIP scene seeds
@@ -672,6 +767,9 @@ def main():
     ap.add_argument("--served-plain-sample", type=int, default=3,
                     help="timed steps per job measuring the plain sequential path")
     ap.add_argument("--flip-size", type=int, default=128, help="grid side of the FLIP transfer measurement (0: skip)")
+    ap.add_argument("--config-runs", type=int, default=1,
+                    help="run configs 1 (64^3 plume, PcMIC, 100 steps) and 3 (128^3 dam break, 150 steps) (0: skip)")
+    ap.add_argument("--config-cpu-steps", type=int, default=3, help="oracle steps beside each config run (0: skip)")
     ap.add_argument("--refined-steps", type=int, default=5,
                     help="timed 256^3 steps of the FP64-refined form reported beside the headline (0: skip)")
     args = ap.parse_args()
@@ -864,6 +962,9 @@ def main():
     flip = None
     if args.flip_size > 0 and rank == 0:
         flip = flip_form(m, args.flip_size, 8, 10, args.seed + 23)
+    configs = None
+    if args.config_runs > 0 and rank == 0:
+        configs = config_runs(m, args.seed + 29, args.config_cpu_steps)
     precision = None
     if args.precision_size > 0 and rank == 0 and world == 1:
         precision = precision_form(m, args.precision_size, args.precision_steps, args.seed + 5)
@@ -895,7 +996,7 @@ def main():
                "clocks": clk, "e2e": e2e, "roofline": roofline, "rooflines": rooflines, "cpu_baseline": cpu,
                "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])},
                "same_scene_pc_mic": alt, "precision_form": {"refined_256": refined, "errors_vs_fp64": precision},
-               "batched_form": batched, "served_form": served, "flip_transfers": flip}
+               "batched_form": batched, "served_form": served, "flip_transfers": flip, "config_runs": configs}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
