@@ -773,9 +773,12 @@ __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev S, const CgSca
 }
 
 // ---- fused level-0 passes, streamed along z.  A CTA of 512 threads owns
-// a 28 x 28 column of fine cells over zc planes (28 x 28 cells in 2D) and
-// walks the column's region -- the owned cells plus a 2-cell halo, 32 x 32
-// cells per plane -- plane by plane, keeping the last five planes of code,
+// a column of fine cells over zc planes (in 2D, one plane) and walks the
+// column's region -- 32 x 32 cells per plane starting at (28 tx, 28 ty) --
+// plane by plane.  It owns the region minus a 2-cell halo on each side
+// where the grid goes on (28 x 28 cells inside the grid, up to 30 where a
+// region edge is the grid's edge: at 256 cells, 9 tiles per row instead of
+// the 10 a fixed 28-cell tile takes), keeping the last five planes of code,
 // right-hand side, diagonal and x in shared memory.  In each step plane p
 // is staged (stage A, two cells per thread), plane p-1 gets its colour-1
 // pass (B, one colour-1 cell per thread) and plane p-2 its last pass (C), so
@@ -785,6 +788,12 @@ __global__ void __launch_bounds__(256) k_mg_interp_add(Lev D, Lev S, const CgSca
 // step writes a plane no thread still reads, so a step needs two barriers.
 constexpr int kTX = 28, kTY = 28, kZC = 32;  // kZC: default planes per CTA (even)
 constexpr int kRX = 32, kRY = 32, kRing = 5;
+// tiles of the level-0 passes along an axis of n cells (tile t's region
+// starts at 28 t; the last one reaches the grid's edge)
+__host__ __device__ constexpr int level0_tiles(int n) { return n <= kRX ? 1 : (n - 4 + kTX - 1) / kTX; }
+// the owned cells of a region along one axis: [lo, hi) in region coordinates
+__device__ __forceinline__ int owned_lo(int o) { return o == 0 ? 0 : 2; }
+__device__ __forceinline__ int owned_hi(int o, int n, int r) { return o + r >= n ? r : r - 2; }
 constexpr int kT0 = 512;  // threads of a level-0 CTA: rows w and w + 16 of warp w
 
 struct Ring0 {  // five planes of the region (dynamic shared memory)
@@ -888,16 +897,20 @@ __device__ __forceinline__ float add_links0(const Ring0& R, const Lev0& F, long 
   return sum;
 }
 
-// stage B: colour 1 on plane q, region minus its outer ring (reads
-// colour-0 values only).  A region row holds 16 colour-1 cells: thread t
-// takes cell t & 15 of row 1 + (t >> 4), so no lane idles on colour 0.
+// stage B: colour 1 on plane q (reads colour-0 values only).  A region row
+// holds 16 colour-1 cells: thread t takes cell t & 15 of row t >> 4, so no
+// lane idles on colour 0.  A cell on the region's outer ring is left out
+// where the grid goes on beyond the ring (its neighbour there is not in the
+// region); where the grid ends at the ring, the cell has no link across it
+// and is computed.
 template <bool IS3D, bool FRAC>
 __device__ __forceinline__ void stage0_b(Ring0& R, const Lev0& F, int ox, int oy, int q) {
   const int t = threadIdx.x;
-  if (t >= 16 * (kRY - 2)) return;
-  const int row = 1 + (t >> 4);
+  const int row = t >> 4;
   const int lx = ((1 + ox + oy + row + q) & 1) + 2 * (t & 15);
-  if (lx < 1 || lx > kRX - 2) return;
+  if ((lx == 0 && ox > 0) || (lx == kRX - 1 && ox + kRX < F.d.nx) || (row == 0 && oy > 0) ||
+      (row == kRY - 1 && oy + kRY < F.d.ny))
+    return;
   const int sl = ring0(q);
   const int c = R.code[sl][row][lx];
   if (!(c & kMgActive)) return;
@@ -916,7 +929,8 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_down(Lev0 F, const float* __rest
   Ring0& R = *reinterpret_cast<Ring0*>(t0_smem);
   const Dims& d = F.d;
   constexpr int ZH = IS3D ? 1 : 0;
-  const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2;
+  const int ox = blockIdx.x * kTX, oy = blockIdx.y * kTY;
+  const int xlo = owned_lo(ox), xhi = owned_hi(ox, d.nx, kRX), ylo = owned_lo(oy), yhi = owned_hi(oy, d.ny, kRY);
   const int zb = IS3D ? blockIdx.z * zc : 0, ze = IS3D ? min(zb + zc, d.nz) : 1;
   const int pbeg = zb - 2 * ZH, pend = ze - 1 + 2 * ZH;
   const bool hasA0f = F.a0f != nullptr;
@@ -939,7 +953,7 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_down(Lev0 F, const float* __rest
       for (int k = 0; k < 2; k++) {
         const int row = (threadIdx.x >> 5) + 16 * k;
         const int gy = oy + row;
-        if (lx < 2 || lx >= 2 + kTX || row < 2 || row >= 2 + kTY || gx >= d.nx || gy >= d.ny) continue;
+        if (lx < xlo || lx >= xhi || row < ylo || row >= yhi || gx >= d.nx || gy >= d.ny) continue;
         const long long g = ix(d, gx, gy, s);
         const int c = R.code[sl][row][lx];
         const float xv = R.x[sl][row][lx];
@@ -968,7 +982,8 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_up(Lev0 F, const float* __restri
   __shared__ float scx[2][CY][CX];  // level-1 parents of the region, two coarse planes
   const Dims& d = F.d;
   constexpr int ZH = IS3D ? 1 : 0;
-  const int ox = blockIdx.x * kTX - 2, oy = blockIdx.y * kTY - 2;
+  const int ox = blockIdx.x * kTX, oy = blockIdx.y * kTY;
+  const int xlo = owned_lo(ox), xhi = owned_hi(ox, d.nx, kRX), ylo = owned_lo(oy), yhi = owned_hi(oy, d.ny, kRY);
   const int zb = IS3D ? blockIdx.z * zc : 0, ze = IS3D ? min(zb + zc, d.nz) : 1;
   const int pbeg = zb - 2 * ZH, pend = ze - 1 + 2 * ZH;  // pbeg is even
   const bool hasA0f = F.a0f != nullptr;
@@ -1010,7 +1025,7 @@ __global__ void __launch_bounds__(kT0, 2) k_mg0_up(Lev0 F, const float* __restri
       for (int k = 0; k < 2; k++) {
         const int row = (threadIdx.x >> 5) + 16 * k;
         const int gy = oy + row;
-        if (lx < 2 || lx >= 2 + kTX || row < 2 || row >= 2 + kTY || gx >= d.nx || gy >= d.ny) continue;
+        if (lx < xlo || lx >= xhi || row < ylo || row >= yhi || gx >= d.nx || gy >= d.ny) continue;
         const long long g = ix(d, gx, gy, s);
         const int c = R.code[sl][row][lx];
         float v = R.x[sl][row][lx];
@@ -1740,8 +1755,7 @@ struct MgHierarchy {
 // planes per CTA of the level-0 passes: the even run length in [16, 64]
 // that minimises waves x planes a CTA walks (its run plus the 4-plane halo),
 // with two CTAs resident per SM; ties go to the longer run (less halo work).
-// At 256^3 that is 44 planes (600 CTAs, two full waves) rather than 32
-// (800 CTAs, 2.6 waves): 8.19 -> 8.10 ms per step.
+// At 256^3 (9 x 9 tiles per plane) that is 38 planes: 567 CTAs, 1.9 waves.
 static int level0_planes(const Dims& d) {
   if (!d.is3d) return kZC;
   int dev = 0, sms = 0;
@@ -1750,7 +1764,7 @@ static int level0_planes(const Dims& d) {
     cudaGetLastError();
     return kZC;
   }
-  const long long cols = (long long)((d.nx + kTX - 1) / kTX) * ((d.ny + kTY - 1) / kTY);
+  const long long cols = (long long)level0_tiles(d.nx) * level0_tiles(d.ny);
   const long long slots = 2LL * sms;
   int best = kZC;
   long long bestCost = -1;
@@ -2037,7 +2051,7 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
   const float* res = b.residual;
   const Lev none{};
   const int zc = h->zc;
-  const dim3 gt((d.nx + kTX - 1) / kTX, (d.ny + kTY - 1) / kTY, d.is3d ? (d.nz + zc - 1) / zc : 1);
+  const dim3 gt(level0_tiles(d.nx), level0_tiles(d.ny), d.is3d ? (d.nz + zc - 1) / zc : 1);
   if (gt.y > 65535u || gt.z > 65535u) return 1;  // beyond the launch limits (> 1.8 M cells along y or z)
   static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
   const int ncol = h->is3d ? 8 : 4;
