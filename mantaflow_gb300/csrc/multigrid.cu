@@ -757,12 +757,14 @@ __global__ void __launch_bounds__(256) k_mg_restrict(Lev D, Lev S, Lev0 F, const
   GRID_STRIDE(v, D.n) restrict_vertex<FROM0, false>(D, S, F, v);
 }
 
-// restriction from level 0 with threads in x-fastest coarse order (a warp's
-// 27 gathers then cover 64 neighbouring fine cells per row instead of 128)
+// restriction from level 0 with threads in x-fastest coarse order over a
+// coarse plane (a warp's 27 gathers then cover 64 neighbouring fine cells
+// per row instead of 128; no idle lanes at the end of a row)
 __global__ void __launch_bounds__(256) k_mg_restrict0(Lev D, Lev0 F, const CgScalars* sc) {
   if (sc->done) return;
-  const int vx = blockIdx.x * 32 + (threadIdx.x & 31), vy = blockIdx.y * 8 + (threadIdx.x >> 5), vz = blockIdx.z;
-  if (vx >= D.sx || vy >= D.sy) return;
+  const unsigned e = blockIdx.x * 256u + threadIdx.x;  // a coarse plane holds < 2^31 vertices
+  if (e >= (unsigned)D.sx * (unsigned)D.sy) return;
+  const int vy = (int)(e / (unsigned)D.sx), vx = (int)(e - (unsigned)vy * (unsigned)D.sx), vz = blockIdx.y;
   restrict_vertex_at<true, false>(D, D, F, lin(D, vx, vy, vz), vx, vy, vz);
 }
 
@@ -2094,8 +2096,8 @@ int mg_apply(MgHierarchy* h, const PcgBuffers& b, bool init, cudaStream_t s) {
       Fam f(h, "mg_restrict_l0");
       count_launch();
       const Lev& v1 = h->lev[1];
-      if (v1.sz <= 65535 && (v1.sy + 7) / 8 <= 65535)
-        k_mg_restrict0<<<dim3((v1.sx + 31) / 32, (v1.sy + 7) / 8, v1.sz), kThreads1, 0, s>>>(v1, l0, sc);
+      if (v1.sz <= 65535)
+        k_mg_restrict0<<<dim3((unsigned)(((long long)v1.sx * v1.sy + 255) / 256), v1.sz), kThreads1, 0, s>>>(v1, l0, sc);
       else  // grid dimensions beyond the y / z launch limits: slot order
         k_mg_restrict<true><<<blocks_for(v1.n), kThreads1, 0, s>>>(v1, none, l0, sc);
     }
