@@ -164,8 +164,10 @@ __global__ void k_compat_shift(long long n, float* rhs, const CgScalars* sc) {
 }
 
 // ------------------------------------------------------- stencil codes
-// MakeLaplaceMatrix (conjugategrad.h:154-187) as codes.  Pass 1: A0 count,
-// fluid bit and the upward links of interior fluid cells.
+// MakeLaplaceMatrix (conjugategrad.h:154-187) as codes.  The batched form
+// builds them in two passes (the single-scene path in one sweep,
+// make_codes_full_cell below).  Pass 1: A0 count, fluid bit and the upward
+// links of interior fluid cells.
 __device__ __forceinline__ void make_codes_cell(const Dims& d, const int* __restrict__ flags, code_t* code, int i, int j, int k) {
   const long long idx = ix(d, i, j, k);
   const int f = __ldg(flags + idx);
