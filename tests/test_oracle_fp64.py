@@ -91,3 +91,61 @@ def test_fp64_pressure_within_solver_tolerance(tag):
             diff = np.max(np.abs(got - want))
             assert diff <= 1e-3 * np.max(np.abs(want)) + 1e-6, "%s %s%s: max difference %g" % (tag, key, name, diff)
     cache.release()
+
+
+@pytest.mark.parametrize("case", ["plume_mic24", "plume_mgstat24"])
+def test_fp64_plume_steps_within_float_rounding(case):
+    """Whole plume steps (inflow, MacCormack advection, walls, buoyancy,
+    pressure) in double against the float executable's steps: the same CG
+    iteration counts and fields within float rounding of their magnitude."""
+    g = load(case)
+    flags, mask = g["flags"], g["mask"]
+    n = flags.shape[0]
+    rng = np.random.default_rng(int(g["seed"]))
+    dens = np.zeros((n, n, n))
+    vel = np.zeros((n, n, n, 3))
+    pres = np.zeros((n, n, n))
+    cache = og.MGCache()
+    for t in range(len(g["iters"])):
+        a = f64((rng.random((n, n, n), dtype=np.float32) * mask).astype(np.float32))
+        og.join_real(dens, a)
+        og.advect_semi_lagrange(flags, vel, dens, og.KIND_REAL, order=2, clampMode=2)
+        og.advect_semi_lagrange(flags, vel, vel, og.KIND_MAC, order=2, clampMode=2)
+        og.set_wall_bcs(flags, vel)
+        og.add_buoyancy(flags, dens, vel, (0, -4e-3, 0))
+        it, _, _ = og.solve_pressure(flags, vel, pres, cgAccuracy=1e-3, preconditioner=int(g["pc"]), mg_cache=cache)
+        assert it == int(g["iters"][t]), "%s step %d: iterations %d vs %d" % (case, t, it, g["iters"][t])
+        for name, got in (("density", dens), ("vel", vel), ("pressure", pres)):
+            want = f64(g[name][t])
+            diff = np.max(np.abs(got - want))
+            # float rounding accumulated over a few steps: 1e-5 of the magnitude
+            assert diff <= 1e-5 * max(np.max(np.abs(want)), 1.0), "%s step %d %s: %g" % (case, t, name, diff)
+    cache.release()
+
+
+def test_fp64_dam_steps_within_float_rounding():
+    """Dam-break steps (extrapolation, order-1 advection of phi and velocity,
+    flags from the levelset, gravity, walls, ghost-fluid pressure) in double
+    against the float executable's: the same flags and CG iteration counts,
+    fields within float rounding."""
+    g = load("dam_24")
+    flags = g["flags0"].copy()
+    phi = f64(g["phi0"])
+    n = flags.shape[0]
+    vel = np.zeros((n, n, n, 3))
+    pres = np.zeros((n, n, n))
+    for t in range(len(g["iters"])):
+        og.extrapolate_mac_simple(flags, vel, 4)
+        og.advect_semi_lagrange(flags, vel, phi, og.KIND_REAL, order=1)
+        og.update_from_levelset(flags, phi)
+        og.advect_semi_lagrange(flags, vel, vel, og.KIND_MAC, order=1)
+        og.add_gravity(flags, vel, (0, -1e-3, 0))
+        og.set_wall_bcs(flags, vel)
+        it, _, _ = og.solve_pressure(flags, vel, pres, phi=phi)
+        og.set_wall_bcs(flags, vel)
+        assert it == int(g["iters"][t]), "dam step %d: iterations %d vs %d" % (t, it, g["iters"][t])
+        assert np.array_equal(flags, g["flags"][t]), "dam step %d flags" % t
+        for name, got in (("phi", phi), ("vel", vel), ("pressure", pres)):
+            want = f64(g[name][t])
+            diff = np.max(np.abs(got - want))
+            assert diff <= 1e-5 * max(np.max(np.abs(want)), 1.0), "dam step %d %s: %g" % (t, name, diff)
